@@ -1,0 +1,776 @@
+// CPU oracle for the MDR refactor/retrieve path -- TEST INFRASTRUCTURE ONLY.
+//
+// This header restates, in plain single-threaded C++, the algorithms of ProDM's
+// MDR path (include/MDR/** of lxAltria/ProDM) so that the CUDA implementation
+// can be checked against it. Only the test suite, the smoke check and the CPU
+// baseline leg of the benchmark may use it; the product library never links it.
+//
+// Parity status:
+//  * level geometry, interleaver, both bitplane encoders/decoders, the error
+//    collectors, estimators and greedy interpreters are restated from the
+//    reference headers and pinned against the reference itself (compiled from
+//    its headers by oracle/ref_harness) through committed golden vectors.
+//  * the MGARD decomposition lives in the un-vendored MGARDx repository
+//    (github.com/lxAltria/MGARDx, no pinned commit). It is restated here from
+//    the published MGARD mathematics: multilinear nodal interpolation from the
+//    coarse grid (hierarchical basis) plus, for the orthogonal basis, the L2
+//    projection correction solved with tensor-product P1 mass matrices. At that
+//    boundary parity is UNPINNED; it is constrained only by the invariants the
+//    reference does pin (in-place level layout read by DirectInterleaver,
+//    linearity, recompose(decompose(x)) == x, the L-inf estimator constants).
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cstdlib>
+#include <cmath>
+#include <vector>
+#include <algorithm>
+#include <type_traits>
+
+namespace mdr_oracle {
+
+// ---------------------------------------------------------------------------
+// Level geometry -- RefactorUtils.hpp:21-34 (compute_level_dims) and :41-59
+// (compute_level_elements): every dim shrinks n -> (n >> 1) + 1 per level.
+// ---------------------------------------------------------------------------
+inline std::vector<std::vector<uint32_t>> level_dims(const std::vector<uint32_t>& dims, int L) {
+    std::vector<std::vector<uint32_t>> ld(L + 1, std::vector<uint32_t>(dims.size()));
+    for (size_t d = 0; d < dims.size(); d++) {
+        uint32_t n = dims[d];
+        for (int j = 0; j <= L; j++) { ld[L - j][d] = n; n = (n >> 1) + 1; }
+    }
+    return ld;
+}
+inline std::vector<uint32_t> level_elements(const std::vector<std::vector<uint32_t>>& ld) {
+    std::vector<uint32_t> out(ld.size());
+    uint64_t prev = 0;
+    for (size_t l = 0; l < ld.size(); l++) {
+        uint64_t v = 1;
+        for (auto x : ld[l]) v *= x;
+        out[l] = (uint32_t)(v - prev);
+        prev = v;
+    }
+    return out;
+}
+// ComposedRefactor.hpp:79 -- uint8_t max_level = log2(min dim) - 1.
+inline int max_level(const std::vector<uint32_t>& dims) {
+    uint32_t m = *std::min_element(dims.begin(), dims.end());
+    return (int)(uint8_t)(std::log2((double)m) - 1);
+}
+
+// Pads a 1-, 2- or 3-dim shape to 3 dims with leading 1s (dim 0 slowest).
+inline void pad3(const std::vector<uint32_t>& d, size_t out[3]) {
+    size_t k = 3 - d.size();
+    for (size_t i = 0; i < 3; i++) out[i] = (i < k) ? 1 : d[i - k];
+}
+
+// ---------------------------------------------------------------------------
+// DirectInterleaver -- DirectInterleaver.hpp:12-37 (interleave), :38-63
+// (reposition). Row-major walk of box(fine) skipping box(coarse); strides are
+// those of the full array. The reference supports 1-D and 3-D; the 2-D case
+// here is the same walk with a unit leading dim.
+// ---------------------------------------------------------------------------
+template <class T>
+void interleave(const T* data, const std::vector<uint32_t>& dims, const std::vector<uint32_t>& fine,
+                const std::vector<uint32_t>& coarse, T* buf) {
+    size_t D[3], F[3], C[3];
+    pad3(dims, D); pad3(fine, F);
+    {   // coarse box padded with 1s only where the dim is padded
+        size_t k = 3 - coarse.size();
+        for (size_t i = 0; i < 3; i++) C[i] = (i < k) ? 1 : coarse[i - k];
+        if (coarse.size() == dims.size()) {
+            bool allz = true; for (auto c : coarse) allz &= (c == 0);
+            if (allz) C[0] = C[1] = C[2] = 0;
+        }
+    }
+    size_t s0 = D[1] * D[2], s1 = D[2], cnt = 0;
+    for (size_t i = 0; i < F[0]; i++)
+        for (size_t j = 0; j < F[1]; j++)
+            for (size_t k = 0; k < F[2]; k++) {
+                if (i < C[0] && j < C[1] && k < C[2]) continue;
+                buf[cnt++] = data[i * s0 + j * s1 + k];
+            }
+}
+template <class T>
+void reposition(const T* buf, const std::vector<uint32_t>& dims, const std::vector<uint32_t>& fine,
+                const std::vector<uint32_t>& coarse, T* data) {
+    size_t D[3], F[3], C[3];
+    pad3(dims, D); pad3(fine, F);
+    {
+        size_t k = 3 - coarse.size();
+        for (size_t i = 0; i < 3; i++) C[i] = (i < k) ? 1 : coarse[i - k];
+        bool allz = true; for (auto c : coarse) allz &= (c == 0);
+        if (allz) C[0] = C[1] = C[2] = 0;
+    }
+    size_t s0 = D[1] * D[2], s1 = D[2], cnt = 0;
+    for (size_t i = 0; i < F[0]; i++)
+        for (size_t j = 0; j < F[1]; j++)
+            for (size_t k = 0; k < F[2]; k++) {
+                if (i < C[0] && j < C[1] && k < C[2]) continue;
+                data[i * s0 + j * s1 + k] = buf[cnt++];
+            }
+}
+
+template <class T>
+T max_abs(const T* d, size_t n) {  // RefactorUtils.hpp:68-76
+    T m = 0;
+    for (size_t i = 0; i < n; i++) { T v = std::fabs(d[i]); if (v > m) m = v; }
+    return m;
+}
+
+// ---------------------------------------------------------------------------
+// Bitplane encoders. Streams of one level are returned concatenated in plane
+// order, which is the byte layout of the reference's level file
+// (FileWriter.hpp:16-31) when the lossless stage is NullLevelCompressor.
+// A level with fewer elements than one block is encoded as one short block
+// (the reference's block loops wrap in unsigned arithmetic there).
+// ---------------------------------------------------------------------------
+template <class S> constexpr int block_bits() { return (int)(8 * sizeof(S)); }
+template <class T> using fps_t = typename std::conditional<std::is_same<T, double>::value, int64_t, int32_t>::type;
+template <class T> using fp_t = typename std::conditional<std::is_same<T, double>::value, uint64_t, uint32_t>::type;
+
+inline uint32_t nb_from_bin(int32_t x) { return (uint32_t)((uint32_t)x + 0xaaaaaaaau) ^ 0xaaaaaaaau; }   // NegaBinaryBPEncoder.hpp:222-224
+inline uint64_t nb_from_bin(int64_t x) { return ((uint64_t)x + 0xaaaaaaaaaaaaaaaaull) ^ 0xaaaaaaaaaaaaaaaaull; }  // :219-221
+inline int32_t nb_to_bin(uint32_t x) { return (int32_t)((x ^ 0xaaaaaaaau) - 0xaaaaaaaau); }  // :228-230
+inline int64_t nb_to_bin(uint64_t x) { return (int64_t)((x ^ 0xaaaaaaaaaaaaaaaaull) - 0xaaaaaaaaaaaaaaaaull); }  // :225-227
+
+// Word of plane p (MSB-first plane numbering) for n <= bits(S) integers.
+template <class S, class I>
+inline S gather_plane(const I* v, size_t n, int bit) {
+    S w = 0;
+    for (size_t i = 0; i < n; i++) w |= (S)((v[i] >> bit) & 1u) << i;
+    return w;
+}
+
+// NegaBinaryBPEncoder::encode -- NegaBinaryBPEncoder.hpp:18-62, with the
+// error-collecting overload :65-125 when errs != nullptr (B+1 doubles).
+// Returns total bytes written to blob; sizes[p] = bytes of plane p.
+template <class T, class S>
+size_t nb_encode(const T* data, size_t n, int exp, int B, uint8_t* blob, uint32_t* sizes, double* errs) {
+    using FPS = fps_t<T>; using FP = fp_t<T>;
+    const int bs = block_bits<S>();
+    exp += 2;                                    // :21 room for the negabinary range
+    size_t nblocks = (n + bs - 1) / bs;
+    std::vector<S> planes((size_t)B * nblocks, 0);
+    if (errs) for (int i = 0; i <= B; i++) errs[i] = 0;
+    std::vector<FP> buf(bs);
+    for (size_t b = 0; b < nblocks; b++) {
+        size_t m = std::min<size_t>(bs, n - b * bs);
+        for (size_t j = 0; j < m; j++) {
+            T cur = data[b * bs + j];
+            T shifted = std::ldexp(cur, B - exp);        // :42
+            FPS q = (FPS)shifted;                        // truncation toward zero
+            buf[j] = (FP)nb_from_bin(q);
+            if (errs) {
+                if (std::is_same<T, float>::value) {
+                    // NegaBinaryBPEncoder.hpp:231-239, float parameters as in the reference
+                    float fd = (float)shifted, fm = (float)(shifted - (T)q);
+                    uint32_t nbd = (uint32_t)buf[j];
+                    errs[B] += fm * fm;
+                    for (int k = 1; k < B; k++) {
+                        uint32_t mask = (uint32_t)((1u << k) - 1);
+                        double diff = (double)nb_to_bin((uint32_t)(nbd & mask)) + fm;
+                        errs[B - k] += diff * diff;
+                    }
+                    errs[0] += fd * fd;
+                } else {
+                    // fp64: the reference narrows to u32/float here (an
+                    // acknowledged defect); this restatement keeps 64-bit masks
+                    // and double arithmetic.
+                    double fd = (double)shifted, fm = (double)(shifted - (T)q);
+                    uint64_t nbd = (uint64_t)buf[j];
+                    errs[B] += fm * fm;
+                    for (int k = 1; k < B; k++) {
+                        uint64_t mask = (k >= 64) ? ~0ull : ((1ull << k) - 1);
+                        double diff = (double)nb_to_bin((uint64_t)(nbd & mask)) + fm;
+                        errs[B - k] += diff * diff;
+                    }
+                    errs[0] += fd * fd;
+                }
+            }
+        }
+        for (int k = B - 1; k >= 0; k--)                 // encode_block :240-250
+            planes[(size_t)(B - 1 - k) * nblocks + b] = gather_plane<S>(buf.data(), m, k);
+    }
+    size_t off = 0;
+    for (int p = 0; p < B; p++) {
+        sizes[p] = (uint32_t)(nblocks * sizeof(S));
+        std::memcpy(blob + off, planes.data() + (size_t)p * nblocks, nblocks * sizeof(S));
+        off += nblocks * sizeof(S);
+    }
+    if (errs) for (int i = 0; i <= B; i++) errs[i] = std::ldexp(errs[i], 2 * (-B + exp));  // :121-123
+    return off;
+}
+
+// NegaBinaryBPEncoder::progressive_decode -- :132-192. planes[i] points at the
+// stream of plane (s + i); returns the contribution of planes [s, s+num).
+template <class T, class S>
+void nb_decode(const uint8_t* const* planes, size_t n, int exp, int s, int num, T* out) {
+    using FP = fp_t<T>;
+    const int bs = block_bits<S>();
+    if (num == 0) { for (size_t i = 0; i < n; i++) out[i] = 0; return; }
+    exp += 2;
+    const int e = s + num;
+    size_t nblocks = (n + bs - 1) / bs;
+    for (size_t b = 0; b < nblocks; b++) {
+        size_t m = std::min<size_t>(bs, n - b * bs);
+        FP acc[64] = {0};
+        for (int k = num - 1; k >= 0; k--) {             // decode_block :251-260
+            S w;
+            std::memcpy(&w, planes[num - 1 - k] + b * sizeof(S), sizeof(S));
+            for (size_t i = 0; i < m; i++) acc[i] += (FP)((w >> i) & 1u) << k;
+        }
+        for (size_t i = 0; i < m; i++) {
+            T v = std::ldexp((T)nb_to_bin(acc[i]), -e + exp);
+            out[b * bs + i] = (e % 2 == 0) ? v : -v;     // :153 sign flips with odd ending plane
+        }
+    }
+}
+
+// GroupedBPEncoder::encode -- GroupedBPEncoder.hpp:18-73 (+ :76-145 errors).
+// Stream 0 is prefixed with [u32 nblocks][u8 rb per block] (merge_arrays :370-377).
+template <class T, class S>
+size_t gr_encode(const T* data, size_t n, int exp, int B, uint8_t* blob, uint32_t* sizes, double* errs) {
+    using FP = fp_t<T>;
+    const int bs = block_bits<S>();
+    size_t nblocks = (n + bs - 1) / bs;
+    std::vector<uint8_t> rbs(nblocks, 0);
+    std::vector<std::vector<S>> streams(B);
+    if (errs) for (int i = 0; i <= B; i++) errs[i] = 0;
+    std::vector<FP> buf(bs);
+    for (size_t b = 0; b < nblocks; b++) {
+        size_t m = std::min<size_t>(bs, n - b * bs);
+        S sign = 0;
+        for (size_t j = 0; j < m; j++) {
+            T cur = data[b * bs + j];
+            T shifted = std::ldexp(cur, B - exp);        // :41
+            if (errs) {
+                if (std::is_same<T, float>::value) {
+                    // collect_level_errors :324-335 with its float parameter
+                    float fdat = (float)std::fabs(shifted);
+                    uint32_t fpd = (uint32_t)fdat;
+                    double mant = fdat - (uint32_t)fdat;
+                    errs[B] += mant * mant;
+                    for (int k = 1; k < B; k++) {
+                        uint32_t mask = (uint32_t)((1u << k) - 1);
+                        double diff = (double)(fpd & mask) + mant;
+                        errs[B - k] += diff * diff;
+                    }
+                    errs[0] += fdat * fdat;
+                } else {
+                    double fdat = std::fabs((double)shifted);
+                    uint64_t fpd = (uint64_t)fdat;
+                    double mant = fdat - (double)fpd;
+                    errs[B] += mant * mant;
+                    for (int k = 1; k < B; k++) {
+                        uint64_t mask = (1ull << k) - 1;
+                        double diff = (double)(fpd & mask) + mant;
+                        errs[B - k] += diff * diff;
+                    }
+                    errs[0] += fdat * fdat;
+                }
+            }
+            int64_t fix = (int64_t)shifted;              // :42
+            S sg = cur < 0;
+            buf[j] = (FP)(sg ? -fix : +fix);
+            sign |= sg << j;
+        }
+        uint8_t rb = (uint8_t)B;                         // encode_block :337-357
+        bool rec = false;
+        for (int k = B - 1; k >= 0; k--) {
+            int p = B - 1 - k;
+            S w = gather_plane<S>(buf.data(), m, k);
+            if (w || rec) {
+                if (!rec) { rec = true; rb = (uint8_t)p; streams[p].push_back(sign); }
+                streams[p].push_back(w);
+            }
+        }
+        rbs[b] = rb;
+    }
+    size_t off = 0;
+    for (int p = 0; p < B; p++) {
+        size_t bytes = streams[p].size() * sizeof(S);
+        if (p == 0) {
+            uint32_t cnt = (uint32_t)nblocks;
+            std::memcpy(blob, &cnt, 4);
+            std::memcpy(blob + 4, rbs.data(), nblocks);
+            off = 4 + nblocks;
+            sizes[0] = (uint32_t)(4 + nblocks + bytes);
+        } else {
+            sizes[p] = (uint32_t)bytes;
+        }
+        if (bytes) std::memcpy(blob + off, streams[p].data(), bytes);
+        off += bytes;
+    }
+    if (errs) for (int i = 0; i <= B; i++) errs[i] = std::ldexp(errs[i], 2 * (-B + exp));  // :141-143
+    return off;
+}
+
+// Progressive grouped decoding state, kept per level and indexed by level
+// (GroupedBPEncoder.hpp:379-380 keeps it by push order).
+template <class S>
+struct GroupedState {
+    std::vector<std::vector<uint8_t>> rb;     // per level: recording bitplane per block
+    std::vector<std::vector<uint8_t>> sign;   // per level: sign per element
+    std::vector<uint8_t> have;
+    void ensure(int level) {
+        if ((int)rb.size() <= level) { rb.resize(level + 1); sign.resize(level + 1); have.resize(level + 1, 0); }
+    }
+};
+
+// GroupedBPEncoder::progressive_decode -- :210-297. planes[i] = stream of plane
+// s+i. The first call for a level must include plane 0 (it carries the rb header).
+template <class T, class S>
+int gr_decode(GroupedState<S>& st, const uint8_t* const* planes, size_t n, int exp, int s, int num, int level, T* out) {
+    using FP = fp_t<T>;
+    const int bs = block_bits<S>();
+    if (num == 0) { for (size_t i = 0; i < n; i++) out[i] = 0; return 0; }
+    st.ensure(level);
+    std::vector<const uint8_t*> pos(planes, planes + num);
+    size_t nblocks = (n + bs - 1) / bs;
+    if (!st.have[level]) {
+        if (s != 0) return -1;
+        uint32_t cnt; std::memcpy(&cnt, pos[0], 4);
+        if (cnt != nblocks) return -2;
+        st.rb[level].assign(pos[0] + 4, pos[0] + 4 + cnt);
+        st.sign[level].assign(n, 0);
+        st.have[level] = 1;
+        pos[0] += 4 + cnt;
+    }
+    const std::vector<uint8_t>& rb = st.rb[level];
+    std::vector<uint8_t>& sg = st.sign[level];
+    const int e = s + num;
+    for (size_t b = 0; b < nblocks; b++) {
+        size_t m = std::min<size_t>(bs, n - b * bs);
+        int r = rb[b];
+        if (r < e) {
+            FP acc[64] = {0};
+            int first = s;
+            if (r >= s) {
+                S w; std::memcpy(&w, pos[r - s], sizeof(S)); pos[r - s] += sizeof(S);
+                for (size_t j = 0; j < m; j++) sg[b * bs + j] = (w >> j) & 1u;
+                first = r;
+            }
+            // decode_block :359-368: planes first..e-1 -> bits e-1-p
+            for (int p = first; p < e; p++) {
+                S w; std::memcpy(&w, pos[p - s], sizeof(S)); pos[p - s] += sizeof(S);
+                int k = e - 1 - p;
+                for (size_t j = 0; j < m; j++) acc[j] += (FP)((w >> j) & 1u) << k;
+            }
+            for (size_t j = 0; j < m; j++) {
+                T v = std::ldexp((T)acc[j], -e + exp);
+                out[b * bs + j] = sg[b * bs + j] ? -v : v;
+            }
+        } else {
+            for (size_t j = 0; j < m; j++) out[b * bs + j] = 0;
+        }
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Error collectors.
+// ---------------------------------------------------------------------------
+// MaxErrorCollector::collect_level_error -- MaxErrorCollector.hpp:14-25.
+template <class T>
+void max_collect(T bound, int B, double* out) {
+    int e = 0; std::frexp(bound, &e);
+    out[0] = bound;
+    double err = std::ldexp(1.0, e - 1);
+    for (int i = 1; i <= B; i++) { out[i] = err; err /= 2; }
+}
+// SquaredErrorCollector::collect_level_error -- SquaredErrorCollector.hpp:54-96.
+// The fp64 variant uses 64-bit masks (the reference's 1u << b is undefined there).
+template <class T>
+void sq_collect(const T* data, size_t n, int B, T maxv, double* out) {
+    using UI = typename std::conditional<std::is_same<T, double>::value, uint64_t, uint32_t>::type;
+    int level_exp = 0; std::frexp(maxv, &level_exp);
+    const int prec = std::is_same<T, double>::value ? 52 : 23;
+    for (int i = 0; i <= B; i++) out[i] = 0;
+    for (size_t i = 0; i < n; i++) {
+        if (data[i] == 0) continue;
+        int de = 0; std::frexp(data[i], &de);
+        UI bits; T val = data[i]; std::memcpy(&bits, &val, sizeof(T));
+        int exp_diff = level_exp - de + prec - B;
+        int index = B;
+        if (exp_diff > 0) {
+            int lim = std::min(exp_diff, prec);
+            for (int b = 0; b < lim; b++) bits &= ~((UI)1 << b);
+        } else {
+            index += exp_diff; exp_diff = 0;
+        }
+        if (index > 0) {
+            for (int b = exp_diff; b < prec; b++) {
+                bits &= ~((UI)1 << b);
+                T f; std::memcpy(&f, &bits, sizeof(T));
+                T d = data[i] - f;
+                out[index] += d * d;
+                index--;
+            }
+            T dd = data[i] * data[i];
+            while (index >= 0) { out[index] += dd; index--; }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Error estimators -- MaxErrorEstimator.hpp:13-68, SquaredErrorEstimator.hpp:
+// 12-68. Arithmetic in T exactly as the reference templates do.
+// kind: 0 = MaxErrorEstimatorHB, 1 = MaxErrorEstimatorOB(ndims),
+//       2 = L2ErrorEstimator_HB(ndims, L), 3 = SNormErrorEstimator(ndims, L, s)
+// ---------------------------------------------------------------------------
+template <class T>
+struct Estimator {
+    int kind = 0; T c = 0; std::vector<T> table;
+    Estimator(int k, int ndims, int L, double s) : kind(k) {
+        if (k == 1) {
+            double cc = ndims == 1 ? 1.0 + std::sqrt(3.0) / 2 : ndims == 2 ? 1.0 + 9.0 / 4 : 1.0 + 21.0 * std::sqrt(3.0) / 8;
+            c = (T)cc; c *= 4;
+        } else if (k == 2) {
+            table.resize(L + 1);
+            for (int i = 0; i <= L; i++) table[i] = (T)std::pow(2, ndims * (L - i));
+        } else if (k == 3) {
+            T sT = (T)s;
+            table.resize(L + 1);
+            for (int i = 0; i <= L; i++) table[i] = (T)std::pow(2, 2 * sT * i + ndims * (L - i));
+        }
+    }
+    T est(T e, int l) const {
+        switch (kind) {
+            case 0: return e;
+            case 1: return c * e;
+            case 2: return table[l] * e * 2;
+            default: return table[l] * e;
+        }
+    }
+    T gain(T base, T cur, T next, int l) const {
+        (void)base;
+        switch (kind) {
+            case 0: return cur - next;
+            case 1: return c * (cur - next);
+            default: return table[l] * (cur - next);
+        }
+    }
+};
+
+// Binary max-heap with the sift order of the C++ standard library's
+// priority_queue (push_heap / pop_heap), so that ties break the same way.
+struct HeapItem { double u; int level; int num; };
+struct MaxHeap {
+    std::vector<HeapItem> h;
+    static bool less(const HeapItem& a, const HeapItem& b) { return a.u < b.u; }
+    void sift_up(size_t hole, size_t top, HeapItem v) {
+        size_t parent = (hole - 1) / 2;
+        while (hole > top && less(h[parent], v)) { h[hole] = h[parent]; hole = parent; parent = (hole - 1) / 2; }
+        h[hole] = v;
+    }
+    void push(HeapItem v) { h.push_back(v); sift_up(h.size() - 1, 0, v); }
+    HeapItem top() const { return h[0]; }
+    void pop() {
+        size_t len = h.size();
+        if (len > 1) {
+            HeapItem v = h[len - 1];
+            h[len - 1] = h[0];
+            size_t n = len - 1, hole = 0, child = 0;
+            while (child < (n - 1) / 2) {
+                child = 2 * (child + 1);
+                if (less(h[child], h[child - 1])) child--;
+                h[hole] = h[child]; hole = child;
+            }
+            if ((n & 1) == 0 && child == (n - 2) / 2) {
+                child = 2 * (child + 1);
+                h[hole] = h[child - 1]; hole = child - 1;
+            }
+            sift_up(hole, 0, v);
+        }
+        h.pop_back();
+    }
+    bool empty() const { return h.empty(); }
+};
+
+// Greedy interpreters -- GreedyBasedSizeInterpreter.hpp:28-64 (kind 0),
+// :78-140 sign-exclude (kind 1), :166-248 negabinary look-ahead (kind 2).
+// sizes: [nl][B] bytes; errs: [nl][B+1]; index in/out; returns retrieve sizes.
+template <class T>
+void interpret(int kind, const Estimator<T>& est, int nl, int B, const uint32_t* sizes, const double* errs,
+               double tol, uint8_t* index, uint32_t* rsz) {
+    auto E = [&](int l, int j) { return errs[(size_t)l * (B + 1) + j]; };
+    auto S = [&](int l, int j) { return sizes[(size_t)l * B + j]; };
+    for (int i = 0; i < nl; i++) rsz[i] = 0;
+    double acc = 0;
+    for (int i = 0; i < nl; i++) acc += est.est((T)E(i, index[i]), i);
+    MaxHeap heap;
+    if (kind == 0) {
+        for (int i = 0; i < nl; i++) {
+            double g = est.gain((T)acc, (T)E(i, index[i]), (T)E(i, index[i] + 1), i);
+            heap.push({g / S(i, index[i]), i, 1});
+        }
+        bool met = false;
+        while (!met && !heap.empty()) {
+            HeapItem t = heap.top(); heap.pop();
+            int i = t.level, j = index[i];
+            rsz[i] += S(i, j);
+            acc -= est.est((T)E(i, j), i);
+            acc += est.est((T)E(i, j + 1), i);
+            if (acc < tol) met = true;
+            index[i]++;
+            if (index[i] != B) {
+                double g = est.gain((T)acc, (T)E(i, index[i]), (T)E(i, index[i] + 1), i);
+                heap.push({g / S(i, index[i]), i, 1});
+            }
+        }
+        return;
+    }
+    if (kind == 1) {
+        if (acc < tol) return;
+        double minerr = acc;
+        int nlev = nl;
+        for (int i = 0; i < nlev; i++) {
+            minerr -= est.est((T)E(i, index[i]), i);
+            minerr += est.est((T)E(i, B), i);
+            if (index[i] == 0) {
+                rsz[i] += S(i, 0);
+                acc -= est.est((T)E(i, 0), i);
+                acc += est.est((T)E(i, 1), i);
+                index[i]++;
+            }
+            if (index[i] != B) {
+                double g = est.gain((T)acc, (T)E(i, index[i]), (T)E(i, index[i] + 1), i);
+                heap.push({g / S(i, index[i]), i, 1});
+            }
+            if (minerr < tol) { nlev = i + 1; break; }
+        }
+        bool met = acc < tol;
+        while (!met && !heap.empty()) {
+            HeapItem t = heap.top(); heap.pop();
+            int i = t.level, j = index[i];
+            rsz[i] += S(i, j);
+            acc -= est.est((T)E(i, j), i);
+            acc += est.est((T)E(i, j + 1), i);
+            if (acc < tol) met = true;
+            index[i]++;
+            if (index[i] != B) {
+                double g = est.gain((T)acc, (T)E(i, index[i]), (T)E(i, index[i] + 1), i);
+                heap.push({g / S(i, index[i]), i, 1});
+            }
+        }
+        return;
+    }
+    // kind 2: negabinary look-ahead (estimated_efficiency :228-248)
+    auto eff = [&](double a, int idx, int l) {
+        double cg = est.gain((T)a, (T)E(l, idx), (T)E(l, idx + 1), l);
+        uint32_t cs = S(l, idx);
+        double ce = cg / cs;
+        int cn = 1;
+        for (int i = 2; i < B - idx; i++) {
+            double ng = est.gain((T)a, (T)E(l, idx), (T)E(l, idx + i), l);
+            uint32_t ns = cs + S(l, idx + i - 1);
+            double ne = ng / ns;
+            if ((ce > 0) && (ce > ne)) break;
+            cg = ng; ce = ne; cs = ns; cn = i;
+        }
+        return HeapItem{ce, l, cn};
+    };
+    for (int i = 0; i < nl; i++)
+        if (index[i] != B) heap.push(eff(acc, index[i], i));
+    bool met = acc < tol;
+    if (met) return;
+    while (!met && !heap.empty()) {
+        HeapItem t = heap.top(); heap.pop();
+        int i = t.level, j = index[i], num = t.num;
+        for (int k = 0; k < num; k++) rsz[i] += S(i, j + k);
+        acc -= est.est((T)E(i, j), i);
+        acc += est.est((T)E(i, j + num), i);
+        if (acc < tol) met = true;
+        index[i] += num;
+        if (index[i] != B) heap.push(eff(acc, index[i], i));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// MGARD multilevel transform (restated from the MGARD mathematics; see header).
+// One level maps the nodal values of a fine box n[3] to
+//   * coefficients  c(x) = u(x) - (multilinear interpolant of the coarse nodal
+//     values)(x) at every node that is not a coarse node, and
+//   * coarse nodal values (orthogonal basis: plus the L2-projection correction z
+//     solving M_c z = P^T M_f c per dim).
+// Per dim, coarse nodes are the even indices below n-1 plus n-1 itself, giving
+// (n >> 1) + 1 of them; odd nodes interpolate from their +-1 neighbours. The
+// level is stored in place, reordered per dim so that coarse nodes occupy
+// [0, nc) and odd nodes follow in increasing order -- the layout that
+// DirectInterleaver.hpp:23-31 reads as box(fine) \ box(coarse).
+// ---------------------------------------------------------------------------
+struct DimMap {
+    size_t n, nc;
+    bool coarse(size_t x) const { return x == n - 1 || (x % 2 == 0); }
+    size_t reord(size_t x) const { return coarse(x) ? (x == n - 1 ? nc - 1 : x / 2) : nc + (x - 1) / 2; }
+    size_t fine_of_coarse(size_t m) const { return m == nc - 1 ? n - 1 : 2 * m; }
+    explicit DimMap(size_t n_) : n(n_), nc((n_ >> 1) + 1) {}
+};
+
+// Multilinear interpolation at fine node x from coarse corners of V (a natural
+// order fine box). Dims are averaged with dim 0 outermost.
+template <class T>
+T interp_at(const T* V, const size_t n[3], const size_t x[3], int mask) {
+    if (mask == 0) return V[(x[0] * n[1] + x[1]) * n[2] + x[2]];
+    int d = (mask & 1) ? 0 : (mask & 2) ? 1 : 2;
+    int rest = mask & ~(1 << d);
+    size_t a[3] = {x[0], x[1], x[2]}, b[3] = {x[0], x[1], x[2]};
+    a[d] -= 1; b[d] += 1;
+    return (T)0.5 * (interp_at(V, n, a, rest) + interp_at(V, n, b, rest));
+}
+
+// Apply the 1-D operator M_c^{-1} P^T M_f along dim d of the box src (dims n),
+// producing dst with dims n but n[d] replaced by nc. Index-space spacing 1.
+template <class T>
+void l2_project_dim(const std::vector<T>& src, const size_t n[3], int d, std::vector<T>& dst, size_t out_n[3]) {
+    DimMap dm(n[d]);
+    for (int i = 0; i < 3; i++) out_n[i] = n[i];
+    out_n[d] = dm.nc;
+    dst.assign(out_n[0] * out_n[1] * out_n[2], 0);
+    size_t nf = dm.n, nc = dm.nc;
+    std::vector<T> line(nf), mf(nf), b(nc), z(nc), cp(nc), dp(nc);
+    // coarse mass matrix with physical spacings h_m = c_{m+1} - c_m
+    std::vector<T> h(nc > 1 ? nc - 1 : 0);
+    for (size_t m = 0; m + 1 < nc; m++) h[m] = (T)(dm.fine_of_coarse(m + 1) - dm.fine_of_coarse(m));
+    size_t stride[3] = {n[1] * n[2], n[2], 1};
+    size_t ostride[3] = {out_n[1] * out_n[2], out_n[2], 1};
+    size_t o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    for (size_t p = 0; p < n[o1]; p++)
+        for (size_t q = 0; q < n[o2]; q++) {
+            size_t base = p * stride[o1] + q * stride[o2];
+            size_t obase = p * ostride[o1] + q * ostride[o2];
+            for (size_t x = 0; x < nf; x++) line[x] = src[base + x * stride[d]];
+            if (nf == nc) {  // no odd nodes along d: identity
+                for (size_t x = 0; x < nf; x++) dst[obase + x * ostride[d]] = line[x];
+                continue;
+            }
+            for (size_t x = 0; x < nf; x++) {
+                T l = x > 0 ? line[x - 1] : (T)0, r = x + 1 < nf ? line[x + 1] : (T)0;
+                T dg = (x == 0 || x == nf - 1) ? (T)1 / 3 : (T)2 / 3;
+                mf[x] = dg * line[x] + (l + r) / 6;
+            }
+            for (size_t m = 0; m < nc; m++) {
+                size_t c = dm.fine_of_coarse(m);
+                T acc = mf[c];
+                if (c > 0 && !dm.coarse(c - 1)) acc += (T)0.5 * mf[c - 1];
+                if (c + 1 < nf && !dm.coarse(c + 1)) acc += (T)0.5 * mf[c + 1];
+                b[m] = acc;
+            }
+            // Thomas solve: diag_m = (h_{m-1} + h_m)/3, off_m = h_m/6
+            for (size_t m = 0; m < nc; m++) {
+                T hl = m > 0 ? h[m - 1] : (T)0, hr = m + 1 < nc ? h[m] : (T)0;
+                T dg = (hl + hr) / 3, up = hr / 6, lo = hl / 6;
+                if (m == 0) { cp[0] = up / dg; dp[0] = b[0] / dg; }
+                else {
+                    T den = dg - lo * cp[m - 1];
+                    cp[m] = up / den;
+                    dp[m] = (b[m] - lo * dp[m - 1]) / den;
+                }
+            }
+            z[nc - 1] = dp[nc - 1];
+            for (size_t m = nc - 1; m-- > 0;) z[m] = dp[m] - cp[m] * z[m + 1];
+            for (size_t m = 0; m < nc; m++) dst[obase + m * ostride[d]] = z[m];
+        }
+}
+
+// Correction z (coarse box) from the coefficient field f (fine box, zeros at coarse nodes).
+template <class T>
+void l2_correction(const std::vector<T>& f, const size_t n[3], std::vector<T>& z) {
+    std::vector<T> a = f, b;
+    size_t cur[3] = {n[0], n[1], n[2]}, nxt[3];
+    for (int d = 2; d >= 0; d--) {
+        l2_project_dim(a, cur, d, b, nxt);
+        a.swap(b);
+        for (int i = 0; i < 3; i++) cur[i] = nxt[i];
+    }
+    z.swap(a);
+}
+
+// decompose one level in place on the sub-box n[3] of an array with strides s[3]
+template <class T>
+void decompose_level(T* data, const size_t n[3], const size_t s[3], bool hierarchical) {
+    DimMap dm[3] = {DimMap(n[0]), DimMap(n[1]), DimMap(n[2])};
+    size_t N = n[0] * n[1] * n[2];
+    std::vector<T> V(N), f;
+    for (size_t i = 0; i < n[0]; i++) for (size_t j = 0; j < n[1]; j++) for (size_t k = 0; k < n[2]; k++)
+        V[(i * n[1] + j) * n[2] + k] = data[i * s[0] + j * s[1] + k * s[2]];
+    if (!hierarchical) f.assign(N, 0);
+    size_t x[3];
+    for (x[0] = 0; x[0] < n[0]; x[0]++) for (x[1] = 0; x[1] < n[1]; x[1]++) for (x[2] = 0; x[2] < n[2]; x[2]++) {
+        int mask = (!dm[0].coarse(x[0]) ? 1 : 0) | (!dm[1].coarse(x[1]) ? 2 : 0) | (!dm[2].coarse(x[2]) ? 4 : 0);
+        size_t lin = (x[0] * n[1] + x[1]) * n[2] + x[2];
+        T v = V[lin];
+        if (mask) v = v - interp_at(V.data(), n, x, mask);
+        if (mask && !hierarchical) f[lin] = v;
+        data[dm[0].reord(x[0]) * s[0] + dm[1].reord(x[1]) * s[1] + dm[2].reord(x[2]) * s[2]] = v;
+    }
+    if (!hierarchical) {
+        std::vector<T> z;
+        l2_correction(f, n, z);
+        for (size_t i = 0; i < dm[0].nc; i++) for (size_t j = 0; j < dm[1].nc; j++) for (size_t k = 0; k < dm[2].nc; k++)
+            data[i * s[0] + j * s[1] + k * s[2]] += z[(i * dm[1].nc + j) * dm[2].nc + k];
+    }
+}
+
+template <class T>
+void recompose_level(T* data, const size_t n[3], const size_t s[3], bool hierarchical) {
+    DimMap dm[3] = {DimMap(n[0]), DimMap(n[1]), DimMap(n[2])};
+    size_t N = n[0] * n[1] * n[2];
+    std::vector<T> V(N, 0), f;
+    size_t x[3];
+    std::vector<T> C(dm[0].nc * dm[1].nc * dm[2].nc);
+    for (size_t i = 0; i < dm[0].nc; i++) for (size_t j = 0; j < dm[1].nc; j++) for (size_t k = 0; k < dm[2].nc; k++)
+        C[(i * dm[1].nc + j) * dm[2].nc + k] = data[i * s[0] + j * s[1] + k * s[2]];
+    if (!hierarchical) {
+        f.assign(N, 0);
+        for (x[0] = 0; x[0] < n[0]; x[0]++) for (x[1] = 0; x[1] < n[1]; x[1]++) for (x[2] = 0; x[2] < n[2]; x[2]++) {
+            int mask = (!dm[0].coarse(x[0]) ? 1 : 0) | (!dm[1].coarse(x[1]) ? 2 : 0) | (!dm[2].coarse(x[2]) ? 4 : 0);
+            if (mask) f[(x[0] * n[1] + x[1]) * n[2] + x[2]] = data[dm[0].reord(x[0]) * s[0] + dm[1].reord(x[1]) * s[1] + dm[2].reord(x[2]) * s[2]];
+        }
+        std::vector<T> z;
+        l2_correction(f, n, z);
+        for (size_t i = 0; i < C.size(); i++) C[i] -= z[i];
+    }
+    for (size_t i = 0; i < dm[0].nc; i++) for (size_t j = 0; j < dm[1].nc; j++) for (size_t k = 0; k < dm[2].nc; k++)
+        V[(dm[0].fine_of_coarse(i) * n[1] + dm[1].fine_of_coarse(j)) * n[2] + dm[2].fine_of_coarse(k)] = C[(i * dm[1].nc + j) * dm[2].nc + k];
+    for (x[0] = 0; x[0] < n[0]; x[0]++) for (x[1] = 0; x[1] < n[1]; x[1]++) for (x[2] = 0; x[2] < n[2]; x[2]++) {
+        int mask = (!dm[0].coarse(x[0]) ? 1 : 0) | (!dm[1].coarse(x[1]) ? 2 : 0) | (!dm[2].coarse(x[2]) ? 4 : 0);
+        if (!mask) continue;
+        T c = data[dm[0].reord(x[0]) * s[0] + dm[1].reord(x[1]) * s[1] + dm[2].reord(x[2]) * s[2]];
+        V[(x[0] * n[1] + x[1]) * n[2] + x[2]] = c + interp_at(V.data(), n, x, mask);
+    }
+    for (size_t i = 0; i < n[0]; i++) for (size_t j = 0; j < n[1]; j++) for (size_t k = 0; k < n[2]; k++)
+        data[i * s[0] + j * s[1] + k * s[2]] = V[(i * n[1] + j) * n[2] + k];
+}
+
+// Decomposer::decompose(data, dims, L, hierarchical, strides) as called at
+// MGARD.hpp:18/:22/:49/:53. Levels go fine -> coarse on the level boxes.
+template <class T>
+void decompose(T* data, const std::vector<uint32_t>& dims, int L, bool hierarchical, const std::vector<uint32_t>& strides) {
+    size_t D[3]; pad3(dims, D);
+    size_t s[3];
+    if (strides.empty()) { s[0] = D[1] * D[2]; s[1] = D[2]; s[2] = 1; }
+    else { std::vector<uint32_t> st = strides; size_t k = 3 - st.size(); for (size_t i = 0; i < 3; i++) s[i] = i < k ? 0 : st[i - k]; }
+    auto ld = level_dims(dims, L);
+    for (int l = L; l >= 1; l--) {
+        size_t n[3]; pad3(ld[l], n);
+        decompose_level(data, n, s, hierarchical);
+    }
+}
+// Recomposer::recompose(data, dims, L, hierarchical, strides), MGARD.hpp:29/:33/:60/:64:
+// dims is the finest box to produce, L the number of levels to undo.
+template <class T>
+void recompose(T* data, const std::vector<uint32_t>& dims, int L, bool hierarchical, const std::vector<uint32_t>& strides) {
+    size_t D[3]; pad3(dims, D);
+    size_t s[3];
+    if (strides.empty()) { s[0] = D[1] * D[2]; s[1] = D[2]; s[2] = 1; }
+    else { std::vector<uint32_t> st = strides; size_t k = 3 - st.size(); for (size_t i = 0; i < 3; i++) s[i] = i < k ? 0 : st[i - k]; }
+    auto ld = level_dims(dims, L);
+    for (int l = 1; l <= L; l++) {
+        size_t n[3]; pad3(ld[l], n);
+        recompose_level(data, n, s, hierarchical);
+    }
+}
+
+}  // namespace mdr_oracle

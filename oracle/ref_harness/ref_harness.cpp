@@ -1,0 +1,204 @@
+// Reference harness (test infrastructure only): compiles lxAltria/ProDM's own
+// MDR headers, unmodified, from the reference tree and exposes their
+// components through extern "C" entry points so that the oracle restatement
+// and the golden vectors can be checked against the reference itself.
+// The MGARDx decomposer the reference includes is absent; shim/ forwards it to
+// the oracle's restatement, so composed-refactor parity at that boundary stays
+// unpinned. Built into oracle/_ref/ by oracle/build_oracle.py.
+#include <iostream>
+#include <sstream>
+#include <vector>
+#include <string>
+#include <cstring>
+#include <cstdint>
+#include <cmath>
+#include <queue>
+#include <cassert>
+#include <type_traits>
+#include "MDR/RefactorUtils.hpp"
+#include "MDR/Interleaver/Interleaver.hpp"
+#include "MDR/BitplaneEncoder/BitplaneEncoder.hpp"
+#include "MDR/ErrorCollector/ErrorCollector.hpp"
+#include "MDR/ErrorEstimator/ErrorEstimator.hpp"
+#include "MDR/SizeInterpreter/SizeInterpreter.hpp"
+#include "MDR/Refactor/Refactor.hpp"
+#include "MDR/Reconstructor/Reconstructor.hpp"
+
+namespace {
+struct Quiet {  // the reference interpreters print to std::cout
+    std::streambuf* old;
+    std::ostringstream sink;
+    Quiet() { old = std::cout.rdbuf(sink.rdbuf()); }
+    ~Quiet() { std::cout.rdbuf(old); }
+};
+std::vector<uint32_t> vec(const uint32_t* p, int n) { return std::vector<uint32_t>(p, p + n); }
+
+template <class T, class S, class Enc>
+int64_t enc_call(const T* d, uint64_t n, int exp, int B, uint8_t* blob, uint32_t* sizes, double* errs) {
+    Enc enc;
+    std::vector<uint32_t> ss;
+    std::vector<uint8_t*> st;
+    if (errs) {
+        std::vector<double> e;
+        st = enc.encode(d, (int32_t)n, exp, (uint8_t)B, ss, e);
+        for (int i = 0; i <= B; i++) errs[i] = e[i];
+    } else {
+        st = enc.encode(d, (int32_t)n, exp, (uint8_t)B, ss);
+    }
+    size_t off = 0;
+    for (int p = 0; p < B; p++) {
+        sizes[p] = ss[p];
+        std::memcpy(blob + off, st[p], ss[p]);
+        off += ss[p];
+        free(st[p]);
+    }
+    return (int64_t)off;
+}
+
+template <class T, class Est>
+void interp_call(int kind, const Est& est, int nl, int B, const uint32_t* sizes, const double* errs, double tol,
+                 uint8_t* index, uint32_t* rsz) {
+    std::vector<std::vector<uint32_t>> ls(nl);
+    std::vector<std::vector<double>> le(nl);
+    for (int l = 0; l < nl; l++) {
+        ls[l].assign(sizes + (size_t)l * B, sizes + (size_t)(l + 1) * B);
+        le[l].assign(errs + (size_t)l * (B + 1), errs + (size_t)(l + 1) * (B + 1));
+    }
+    std::vector<uint8_t> idx(index, index + nl);
+    std::vector<uint32_t> r;
+    Quiet q;
+    if (kind == 0) r = MDR::GreedyBasedSizeInterpreter<Est>(est).interpret_retrieve_size(ls, le, tol, idx);
+    else if (kind == 1) r = MDR::SignExcludeGreedyBasedSizeInterpreter<Est>(est).interpret_retrieve_size(ls, le, tol, idx);
+    else r = MDR::NegaBinaryGreedyBasedSizeInterpreter<Est>(est).interpret_retrieve_size(ls, le, tol, idx);
+    for (int l = 0; l < nl; l++) { index[l] = idx[l]; rsz[l] = r[l]; }
+}
+
+template <class T>
+void interp_any(int kind, int est_kind, int ndims, int L, double s, int nl, int B, const uint32_t* sizes,
+                const double* errs, double tol, uint8_t* index, uint32_t* rsz) {
+    switch (est_kind) {
+        case 0: interp_call<T>(kind, MDR::MaxErrorEstimatorHB<T>(), nl, B, sizes, errs, tol, index, rsz); break;
+        case 1: interp_call<T>(kind, MDR::MaxErrorEstimatorOB<T>(ndims), nl, B, sizes, errs, tol, index, rsz); break;
+        case 2: interp_call<T>(kind, MDR::L2ErrorEstimator_HB<T>(ndims, L), nl, B, sizes, errs, tol, index, rsz); break;
+        default: interp_call<T>(kind, MDR::SNormErrorEstimator<T>(ndims, L, (T)s), nl, B, sizes, errs, tol, index, rsz); break;
+    }
+}
+
+// ComposedRefactor + ComposedReconstructor driven as test/test_mdr_refactor.cpp
+// and test/test_mdr_reconstructor.cpp do, on files under dir.
+template <class T, class S, class Dec, class Enc, class Est>
+int composed_roundtrip(const T* field, int ndims, const uint32_t* dims, int L, int B, bool negabinary,
+                       const char* dir, int ntol, const double* tols, T* outs, uint64_t* retrieved) {
+    std::string d(dir);
+    std::string meta = d + "/metadata.bin";
+    std::vector<std::string> files;
+    for (int i = 0; i <= L; i++) files.push_back(d + "/level_" + std::to_string(i) + ".bin");
+    size_t N = 1; for (int i = 0; i < ndims; i++) N *= dims[i];
+    Quiet q;
+    {
+        auto refactor = MDR::ComposedRefactor<T, Dec, MDR::DirectInterleaver<T>, Enc, MDR::NullLevelCompressor,
+                                              MDR::MaxErrorCollector<T>, MDR::ConcatLevelFileWriter>(
+            Dec(), MDR::DirectInterleaver<T>(), Enc(), MDR::NullLevelCompressor(), MDR::MaxErrorCollector<T>(),
+            MDR::ConcatLevelFileWriter(meta, files));
+        refactor.negabinary = negabinary;
+        refactor.refactor(field, vec(dims, ndims), (uint8_t)L, (uint8_t)B);
+    }
+    auto rec = MDR::ComposedReconstructor<T, Dec, MDR::DirectInterleaver<T>, Enc, MDR::NullLevelCompressor,
+                                          MDR::SignExcludeGreedyBasedSizeInterpreter<Est>, Est,
+                                          MDR::ConcatLevelFileRetriever>(
+        Dec(), MDR::DirectInterleaver<T>(), Enc(), MDR::NullLevelCompressor(),
+        MDR::SignExcludeGreedyBasedSizeInterpreter<Est>(Est()), MDR::ConcatLevelFileRetriever(meta, files));
+    rec.load_metadata();
+    for (int t = 0; t < ntol; t++) {
+        T* r = rec.progressive_reconstruct(tols[t], -1);
+        if (!r) return -1;
+        std::memcpy(outs + (size_t)t * N, r, N * sizeof(T));
+        retrieved[t] = rec.get_retrieved_size();
+    }
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+
+#define REF_T(SUF, T, S)                                                                                        \
+    int64_t ref_nb_encode_##SUF(const T* d, uint64_t n, int exp, int B, uint8_t* blob, uint32_t* sizes,        \
+                                double* errs) {                                                                 \
+        return enc_call<T, S, MDR::NegaBinaryBPEncoder<T, S>>(d, n, exp, B, blob, sizes, errs);                 \
+    }                                                                                                           \
+    int64_t ref_gr_encode_##SUF(const T* d, uint64_t n, int exp, int B, uint8_t* blob, uint32_t* sizes,        \
+                                double* errs) {                                                                 \
+        return enc_call<T, S, MDR::GroupedBPEncoder<T, S>>(d, n, exp, B, blob, sizes, errs);                    \
+    }                                                                                                           \
+    void* ref_nb_new_##SUF() { return new MDR::NegaBinaryBPEncoder<T, S>(); }                                   \
+    void ref_nb_free_##SUF(void* p) { delete (MDR::NegaBinaryBPEncoder<T, S>*)p; }                              \
+    void* ref_gr_new_##SUF() { return new MDR::GroupedBPEncoder<T, S>(); }                                      \
+    void ref_gr_free_##SUF(void* p) { delete (MDR::GroupedBPEncoder<T, S>*)p; }                                 \
+    int ref_decode_##SUF(void* h, int grouped, const uint8_t* blob, const uint32_t* sizes, uint64_t n, int exp, \
+                         int s, int num, int level, T* out) {                                                   \
+        std::vector<const uint8_t*> planes;                                                                     \
+        size_t o = 0;                                                                                           \
+        for (int i = 0; i < num; i++) { planes.push_back(blob + o); o += sizes[i]; }                            \
+        T* r = grouped ? ((MDR::GroupedBPEncoder<T, S>*)h)->progressive_decode(planes, (int32_t)n, exp,        \
+                                                                                (uint8_t)s, (uint8_t)num, level) \
+                       : ((MDR::NegaBinaryBPEncoder<T, S>*)h)->progressive_decode(planes, (int32_t)n, exp,     \
+                                                                                   (uint8_t)s, (uint8_t)num,    \
+                                                                                   level);                      \
+        std::memcpy(out, r, n * sizeof(T));                                                                     \
+        free(r);                                                                                                \
+        return 0;                                                                                               \
+    }                                                                                                           \
+    void ref_max_collect_##SUF(T bound, int B, double* out) {                                                   \
+        auto v = MDR::MaxErrorCollector<T>().collect_level_error(nullptr, 0, B, bound);                         \
+        for (int i = 0; i <= B; i++) out[i] = v[i];                                                             \
+    }                                                                                                           \
+    void ref_sq_collect_##SUF(const T* d, uint64_t n, int B, T mx, double* out) {                               \
+        auto v = MDR::SquaredErrorCollector<T>().collect_level_error(d, n, B, mx);                              \
+        for (int i = 0; i <= B; i++) out[i] = v[i];                                                             \
+    }                                                                                                           \
+    void ref_interleave_##SUF(const T* data, int ndims, const uint32_t* dims, const uint32_t* fine,             \
+                              const uint32_t* coarse, T* buf) {                                                 \
+        MDR::DirectInterleaver<T>().interleave(data, vec(dims, ndims), vec(fine, ndims), vec(coarse, ndims),   \
+                                                buf);                                                           \
+    }                                                                                                           \
+    void ref_reposition_##SUF(const T* buf, int ndims, const uint32_t* dims, const uint32_t* fine,             \
+                              const uint32_t* coarse, T* data) {                                                \
+        MDR::DirectInterleaver<T>().reposition(buf, vec(dims, ndims), vec(fine, ndims), vec(coarse, ndims),    \
+                                                data);                                                          \
+    }                                                                                                           \
+    void ref_interpret_##SUF(int kind, int est_kind, int ndims, int L, double s, int nl, int B,                 \
+                             const uint32_t* sizes, const double* errs, double tol, uint8_t* index,             \
+                             uint32_t* rsz) {                                                                   \
+        interp_any<T>(kind, est_kind, ndims, L, s, nl, B, sizes, errs, tol, index, rsz);                        \
+    }                                                                                                           \
+    void ref_level_dims_##SUF(int ndims, const uint32_t* dims, int L, uint32_t* out, uint32_t* elems) {         \
+        auto ld = MDR::compute_level_dims(vec(dims, ndims), L);                                                 \
+        auto le = MDR::compute_level_elements(ld, L);                                                           \
+        for (int l = 0; l <= L; l++) {                                                                          \
+            for (int d = 0; d < ndims; d++) out[l * ndims + d] = ld[l][d];                                      \
+            elems[l] = le[l];                                                                                   \
+        }                                                                                                       \
+    }                                                                                                           \
+    int ref_composed_##SUF(const T* field, int ndims, const uint32_t* dims, int L, int B, int enc, int hier,    \
+                           const char* dir, int ntol, const double* tols, T* outs, uint64_t* retrieved) {       \
+        if (hier) {                                                                                             \
+            if (enc == 0)                                                                                       \
+                return composed_roundtrip<T, S, MDR::MGARDHierarchicalDecomposer<T>,                            \
+                                          MDR::NegaBinaryBPEncoder<T, S>, MDR::MaxErrorEstimatorHB<T>>(         \
+                    field, ndims, dims, L, B, true, dir, ntol, tols, outs, retrieved);                          \
+            return composed_roundtrip<T, S, MDR::MGARDHierarchicalDecomposer<T>, MDR::GroupedBPEncoder<T, S>,   \
+                                      MDR::MaxErrorEstimatorHB<T>>(field, ndims, dims, L, B, false, dir, ntol,  \
+                                                                   tols, outs, retrieved);                      \
+        }                                                                                                       \
+        if (enc == 0)                                                                                           \
+            return composed_roundtrip<T, S, MDR::MGARDOrthoganalDecomposer<T>, MDR::NegaBinaryBPEncoder<T, S>,  \
+                                      MDR::MaxErrorEstimatorOB<T>>(field, ndims, dims, L, B, true, dir, ntol,   \
+                                                                   tols, outs, retrieved);                      \
+        return composed_roundtrip<T, S, MDR::MGARDOrthoganalDecomposer<T>, MDR::GroupedBPEncoder<T, S>,         \
+                                  MDR::MaxErrorEstimatorOB<T>>(field, ndims, dims, L, B, false, dir, ntol,      \
+                                                               tols, outs, retrieved);                          \
+    }
+
+REF_T(f32, float, uint32_t)
+REF_T(f64, double, uint64_t)
+}
