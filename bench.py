@@ -1,0 +1,447 @@
+"""Benchmark: MDR refactor + progressive retrieve throughput at 513^3 fp32.
+
+One step = refactor of a 513^3 fp32 Gaussian random field (power spectrum
+k^-5/3, seeded; 8 levels, 32 bitplanes, NegaBinary encoder, squared-error
+tables) followed by retrieval at relative L2 tolerances 1e-2 .. 1e-6
+(negabinary greedy interpreter, L2 hierarchical estimator), progressive from
+an empty retrieval state.
+
+Algorithmic bytes of a step (the metric's numerator):
+  refactor : field read once (N*4) + every stream byte written once
+  retrieve : the stream bytes of all retrieved planes + the field written (N*4),
+             per tolerance.
+value  = bytes of all ranks' steps / max-over-ranks device time (GB/s), inputs
+         resident in HBM; every input is larger than L2 (129 MB), no flush.
+e2e    = same bytes / time of the reference-facing flow with host buffers:
+         H2D field -> refactor -> D2H level files + metadata -> reconstructor
+         loads metadata, then per tolerance: interpret, H2D of the newly needed
+         level bytes, reconstruct, D2H of the field.
+
+--impl reference: the reference's CPU algorithm (oracle port; the reference's
+own headers cannot be built on the GPU host) on all host threads, each thread
+refactoring + retrieving its own 257^3 field with the same level count,
+bitplanes, encoder and tolerances (a bounded sample of this workload).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (513, 513, 513)
+LEVELS = 7              # target level 7 = 8 levels
+BITPLANES = 32
+REL_TOLS = (1e-2, 1e-3, 1e-4, 1e-5, 1e-6)
+CPU_SAMPLE = (257, 257, 257)
+METRIC = "refactor & retrieve GB/s at 513^3 fp32 (% HBM roofline), batched vs plain, at stated bound"
+WORKLOAD = ("513^3 fp32 Gaussian random field k^-5/3 (seeded), 8 levels, 32 bitplanes, NegaBinaryBPEncoder, "
+            "SquaredErrorCollector tables, MGARD hierarchical basis; retrieve at relative L2 1e-2..1e-6 "
+            "(progressive, NegaBinary greedy interpreter, L2 hierarchical estimator)")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        rows = []
+        for ts, line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((ts, float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        inside = [r for r in rows if t0 <= r[0] <= t1 + 0.15]
+        if not inside and rows:
+            inside = sorted(rows, key=lambda r: min(abs(r[0] - t0), abs(r[0] - t1)))[:3]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in inside for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": reasons, "samples": len(inside)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's algorithm (oracle port) on host threads
+# ---------------------------------------------------------------------------
+def cpu_sample_field(seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    # spectral field of the same slope, host generator (numpy FFT)
+    n = CPU_SAMPLE[0]
+    white = rng.standard_normal(CPU_SAMPLE).astype(np.float32)
+    spec = np.fft.rfftn(white)
+    k = [np.fft.fftfreq(n) * n, np.fft.fftfreq(n) * n, np.fft.rfftfreq(n) * n]
+    kk = k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2 + k[2][None, None, :] ** 2
+    kk[0, 0, 0] = 1.0
+    spec *= kk ** (-5.0 / 12.0)
+    spec[0, 0, 0] = 0
+    x = np.fft.irfftn(spec, s=CPU_SAMPLE).astype(np.float32)
+    x /= x.std()
+    return x
+
+
+def cpu_work(x):
+    """One bounded sample: refactor + progressive retrieval at the five tolerances."""
+    import numpy as np
+    import oracle
+    O = oracle.oracle()
+    L, B = LEVELS, BITPLANES
+    r = O.refactor(x, L, B, "negabinary", True, True)
+    nbytes = x.size * 4 + r["blob"].size
+    norm2 = float(np.sum(x.astype(np.float64) ** 2))
+    idx = np.zeros(L + 1, np.uint8)
+    for rel in REL_TOLS:
+        idx, _ = O.interpret("negabinary", "l2_hb", r["sizes"], r["errs"], (rel ** 2) * norm2, idx)
+        O.retrieve(x.shape, L, B, r["blob"], r["sizes"], r["bounds"], idx, "negabinary", True)
+        nbytes += int(sum(int(r["sizes"][l, :idx[l]].astype(np.int64).sum()) for l in range(L + 1))) + x.size * 4
+    return nbytes
+
+
+def cpu_baseline(steps, warmup, threads=None):
+    threads = threads or os.cpu_count() or 1
+    base = cpu_sample_field(100)
+    fields = [base] * threads            # read-only input; each refactor works on its own copy
+    results = [0] * threads
+
+    def run(t):
+        results[t] = cpu_work(fields[t])
+
+    total_bytes, total_time = 0, 0.0
+    for s in range(warmup + steps):
+        ths = [threading.Thread(target=run, args=(t,)) for t in range(threads)]
+        t0 = time.perf_counter()
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        dt = time.perf_counter() - t0
+        if s >= warmup:
+            total_bytes += sum(results)
+            total_time += dt
+    return total_bytes / total_time / 1e9, threads, total_time / max(steps, 1)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def stage_bytes(mdr, kind, level, step_bytes_info):
+    """algorithmic bytes of one launch of a stage."""
+    import numpy as np
+    ld = mdr.level_dims
+    box = lambda l: int(np.prod(ld[l].astype(np.int64)))
+    n = int(mdr.level_elements[level])
+    sizes = step_bytes_info["sizes"]
+    if kind == "decompose":
+        return 2 * 4 * box(level)
+    if kind == "encode":
+        return 4 * n + int(sizes[level].astype(np.int64).sum())
+    if kind == "decode":
+        return step_bytes_info["decode_bytes"][level] + 4 * n
+    if kind == "recompose":
+        return 4 * (box(level - 1) + n + box(level))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from prodm_gb300 import api, fields
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    x = fields.spectral_grf(SHAPE, slope=-5.0 / 3.0, seed=1234 + rank, dtype=torch.float32, device=dev)
+    N = x.numel()
+    norm2 = float((x.double() ** 2).sum().item())
+    tols = [(r ** 2) * norm2 for r in REL_TOLS]
+    mdr = api.MDRField(SHAPE, torch.float32, LEVELS, BITPLANES, "negabinary", "hierarchical", "squared")
+    out = torch.empty(SHAPE, dtype=torch.float32, device=dev)
+
+    def step():
+        mdr.refactor(x)
+        mdr.reset()
+        for t in tols:
+            mdr.retrieve(t, out=out, interpreter="negabinary", estimator="l2_hb")
+
+    # warm-up, and the per-tolerance retrieved bytes (deterministic)
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    sizes, bounds, _ = mdr.level_info()
+    mdr.refactor(x)
+    mdr.reset()
+    retrieved, achieved, idxs = [], [], []
+    for t in tols:
+        mdr.retrieve(t, out=out, interpreter="negabinary", estimator="l2_hb")
+        idx = mdr.index()
+        idxs.append(idx.tolist())
+        retrieved.append(mdr.retrieved_bytes(idx))
+        achieved.append(math.sqrt(float(((out.double() - x.double()) ** 2).sum().item()) / norm2))
+    refactor_bytes = N * 4 + int(sizes.astype(np.int64).sum())
+    retrieve_bytes = [r + N * 4 for r in retrieved]
+    step_bytes = refactor_bytes + sum(retrieve_bytes)
+    decode_bytes = [sum(int(sizes[l, :idxs[i][l]].astype(np.int64).sum()) for i in range(len(tols))) / len(tols)
+                    for l in range(LEVELS + 1)]
+
+    # timed region
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = api.kernel_launch_count()
+    timed_tail = min(args.steps, 20)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    t0 = time.time()
+    e0.record()
+    for i in range(args.steps):
+        if i == args.steps - timed_tail:
+            mdr.set_timing(True)
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    t1 = time.time()
+    if world > 1:
+        dist.barrier()
+    launches = api.kernel_launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    stages = mdr.stage_times()
+    mdr.set_timing(False)
+    sampler.stop()
+    clocks = sampler.summary(t0, t1)
+    if world > 1:
+        tt = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    total_bytes = step_bytes * args.steps * world
+    value = total_bytes / (ms / 1e3) / 1e9
+
+    # roofline of the dominant stage
+    peak, peak_src = measured_peak()
+    info = {"sizes": sizes, "decode_bytes": decode_bytes}
+    per_stage = {}
+    for (kind, level), (tms, cnt) in stages.items():
+        b = stage_bytes(mdr, kind, level, info)
+        per_stage["%s_l%d" % (kind, level)] = {"ms_avg": tms / cnt, "launches": cnt, "share": 0.0,
+                                               "gbs": (b / (tms / cnt / 1e3) / 1e9) if tms > 0 and b else None,
+                                               "bytes": b}
+    tot = sum(v["ms_avg"] * v["launches"] for v in per_stage.values()) or 1.0
+    for v in per_stage.values():
+        v["share"] = v["ms_avg"] * v["launches"] / tot
+    dom_name = max(per_stage, key=lambda k: per_stage[k]["ms_avg"] * per_stage[k]["launches"])
+    dom = per_stage[dom_name]
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_513.json")) as f:
+            traffic = json.load(f).get(dom_name)
+    except Exception:
+        pass
+    roofline = {"kernel": dom_name, "bound": "hbm", "achieved": dom["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": (dom["gbs"] / peak) if dom["gbs"] else None, "traffic": traffic,
+                "peak_source": peak_src + " (hbm_gbs, copy bandwidth)",
+                "algorithmic_bytes_per_launch": dom["bytes"]}
+
+    # end-to-end through the reference-facing flow with host buffers
+    e2e = run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev)
+
+    result = None
+    if rank == 0:
+        result = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian random field, k^-5/3)",
+            "config": {"workload": WORKLOAD, "shape": list(SHAPE), "levels": LEVELS + 1, "bitplanes": BITPLANES,
+                       "encoder": "negabinary", "basis": "hierarchical", "rel_l2_tolerances": list(REL_TOLS),
+                       "parallelism": "replicas (one independent field per GPU)",
+                       "l2_policy": "inputs (540 MB field, 540 MB streams) larger than L2; no flush",
+                       "bytes_per_step": step_bytes, "refactor_bytes": refactor_bytes,
+                       "retrieve_bytes": retrieve_bytes, "achieved_rel_l2": achieved,
+                       "planes_per_level": idxs},
+            "roofline": roofline,
+            "stages": per_stage,
+            "gpu_launches": launches,
+            "e2e": e2e,
+            "clocks": clocks,
+        }
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return result
+
+
+def run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev):
+    import numpy as np
+    import torch
+    from prodm_gb300 import api
+
+    L = LEVELS
+    host_field = torch.empty(SHAPE, dtype=torch.float32, pin_memory=True)
+    host_field.copy_(x.cpu())
+    host_out = torch.empty(SHAPE, dtype=torch.float32, pin_memory=True)
+    dfield = torch.empty_like(x)
+    out = torch.empty_like(x)
+    rec = api.MDRField(SHAPE, torch.float32, L, BITPLANES, "negabinary", "hierarchical", "squared")
+    sizes, _, _ = mdr.level_info()
+    level_bytes = [int(sizes[l].astype(np.int64).sum()) for l in range(L + 1)]
+    host_levels = [torch.empty(b, dtype=torch.uint8, pin_memory=True) for b in level_bytes]
+    h2d = d2h = 0
+
+    def one():
+        nonlocal h2d, d2h
+        h2d = d2h = 0
+        dfield.copy_(host_field, non_blocking=True)
+        h2d += x.numel() * 4
+        mdr.refactor(dfield)
+        for l in range(L + 1):                              # level files -> host
+            call_export(mdr, l, host_levels[l])
+            d2h += level_bytes[l]
+        meta = mdr.metadata()
+        d2h += len(meta)
+        rec.load_metadata(meta)
+        loaded = [0] * (L + 1)
+        for t in tols:
+            rec.interpret(t, interpreter="negabinary", estimator="l2_hb")
+            idx = rec.index()
+            for l in range(L + 1):
+                need = int(sizes[l, :idx[l]].astype(np.int64).sum())
+                if need > loaded[l]:
+                    rec.load_level(l, host_levels[l][loaded[l]:need], offset=loaded[l])
+                    h2d += need - loaded[l]
+                    loaded[l] = need
+            rec.reconstruct(out)
+            host_out.copy_(out, non_blocking=True)
+            d2h += x.numel() * 4
+        torch.cuda.current_stream().synchronize()
+
+    one()
+    torch.cuda.synchronize()
+    n = max(1, args.e2e_steps)
+    t0 = time.perf_counter()
+    for _ in range(n):
+        one()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / n
+    rec.close()
+    return {"value": step_bytes / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": dt * 1e3, "steps": n,
+            "flow": "H2D field, refactor, D2H level files + metadata, reconstructor: load metadata, per tolerance "
+                    "interpret -> H2D new level bytes -> reconstruct -> D2H field"}
+
+
+def call_export(mdr, level, host_tensor):
+    import ctypes as C
+    from prodm_gb300._lib import call
+    from prodm_gb300.api import _stream
+    n = C.c_uint64()
+    call("prodm_mdr_export_level", mdr.h, level, C.c_void_p(host_tensor.data_ptr()), host_tensor.numel(), 1,
+         C.byref(n), _stream())
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        value, cores, sec = cpu_baseline(args.steps, args.warmup)
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian random field)",
+            "config": {"workload": WORKLOAD, "sample": "257^3 per host thread (bounded sample)"},
+            "cpu_baseline": {"value": value, "unit": "GB/s", "cores": cores, "kind": "port",
+                             "sample": "each step: every host thread refactors its own 257^3 fp32 field (8 levels, "
+                                       "32 planes, NegaBinary, squared tables) and retrieves it at the five "
+                                       "tolerances; the reference's CPU algorithm as restated by the oracle"},
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return 0
+    res = run_ours(args)
+    if rank == 0:
+        if world == 1 and not args.no_cpu_baseline:
+            value, cores, sec = cpu_baseline(1, 0)
+            res["cpu_baseline"] = {"value": value, "unit": "GB/s", "cores": cores, "kind": "port",
+                                   "sample": "one step: each of %d host threads refactors + retrieves its own 257^3 "
+                                             "fp32 field with the same levels/planes/encoder/tolerances (oracle port "
+                                             "of the reference algorithm)" % cores}
+        print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

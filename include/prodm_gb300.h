@@ -1,0 +1,225 @@
+/*
+ * prodm_gb300 -- C ABI of the GB300 (sm_103a) implementation of ProDM's MDR
+ * refactor / retrieve path (lxAltria/ProDM, include/MDR/**).
+ *
+ * Plain C types only: device buffers are raw pointers, CUDA streams are passed
+ * as void* (cudaStream_t), sizes are 64-bit. Every function returns a status
+ * code; prodm_last_error_string() describes the last failure on the calling
+ * thread. Nothing here exits the process (the reference calls exit() on
+ * unsupported input, e.g. DirectInterleaver.hpp:33-36).
+ *
+ * Enumerations
+ *   dtype      PRODM_F32 (float data, u32 stream words, 32-value blocks)
+ *              PRODM_F64 (double data, u64 stream words, 64-value blocks)
+ *   encoder    PRODM_ENC_NEGABINARY  NegaBinaryBPEncoder<T, S>
+ *              PRODM_ENC_GROUPED     GroupedBPEncoder<T, S>
+ *   basis      PRODM_BASIS_HIERARCHICAL  MGARDHierarchicalDecomposer (MGARD.hpp:42-70)
+ *              PRODM_BASIS_ORTHOGONAL    MGARDOrthoganalDecomposer   (MGARD.hpp:11-39)
+ *   interpreter PRODM_INTERP_GREEDY / _SIGN_EXCLUDE / _NEGABINARY
+ *              (GreedyBasedSizeInterpreter.hpp:28-64 / :78-140 / :166-248)
+ *   estimator  PRODM_EST_MAX_HB / _MAX_OB / _L2_HB / _SNORM
+ *              (MaxErrorEstimator.hpp:53-68 / :13-49; SquaredErrorEstimator.hpp:12-38 / :42-68)
+ *   collector  PRODM_COLLECT_MAX / _SQUARED (MaxErrorCollector.hpp / SquaredErrorCollector.hpp)
+ */
+#ifndef PRODM_GB300_H
+#define PRODM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define PRODM_OK 0
+#define PRODM_EINVAL 1        /* invalid argument (sizes, levels, enums)      */
+#define PRODM_ENOMEM 2        /* device allocation failed                     */
+#define PRODM_ECUDA 3         /* CUDA runtime error                           */
+#define PRODM_ETIMEOUT 4      /* a bounded device wait gave up                */
+#define PRODM_ECORRUPT 5      /* malformed stream / metadata                  */
+#define PRODM_EUNSUPPORTED 6  /* valid but not supported combination          */
+
+#define PRODM_F32 0
+#define PRODM_F64 1
+#define PRODM_ENC_NEGABINARY 0
+#define PRODM_ENC_GROUPED 1
+#define PRODM_BASIS_HIERARCHICAL 0
+#define PRODM_BASIS_ORTHOGONAL 1
+#define PRODM_INTERP_GREEDY 0
+#define PRODM_INTERP_SIGN_EXCLUDE 1
+#define PRODM_INTERP_NEGABINARY 2
+#define PRODM_EST_MAX_HB 0
+#define PRODM_EST_MAX_OB 1
+#define PRODM_EST_L2_HB 2
+#define PRODM_EST_SNORM 3
+#define PRODM_COLLECT_MAX 0
+#define PRODM_COLLECT_SQUARED 1
+
+const char* prodm_last_error_string(void);
+int prodm_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Level geometry
+ * ------------------------------------------------------------------------- */
+/* ComposedRefactor.hpp:79 -- largest target level accepted for dims. */
+int prodm_max_level(int ndims, const uint32_t* dims, int* out_level);
+/* RefactorUtils.hpp:21-34 (compute_level_dims) and :41-59
+ * (compute_level_elements): out_dims[(L+1)*ndims], out_elems[L+1]. */
+int prodm_level_dims(int ndims, const uint32_t* dims, int target_level, uint32_t* out_dims, uint64_t* out_elems);
+
+/* ---------------------------------------------------------------------------
+ * Decomposer -- DecomposerInterface<T>::decompose / recompose
+ * (DecomposerInterface.hpp:14-16; MGARD.hpp:14-35, :45-66).
+ * In place on device data of shape dims (1-3 dims) with the reference's
+ * per-level reordered layout. strides: NULL for row-major, else ndims element
+ * strides with the last equal to 1. workspace: NULL to let the call allocate
+ * (stream ordered), else at least prodm_decompose_workspace() bytes.
+ * ------------------------------------------------------------------------- */
+int prodm_decompose_workspace(int dtype, int ndims, const uint32_t* dims, uint32_t target_level, int basis,
+                              size_t* bytes);
+int prodm_decompose(int dtype, void* d_data, int ndims, const uint32_t* dims, uint32_t target_level,
+                    const uint32_t* strides, int basis, void* d_workspace, size_t workspace_bytes, void* stream);
+int prodm_recompose(int dtype, void* d_data, int ndims, const uint32_t* dims, uint32_t target_level,
+                    const uint32_t* strides, int basis, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Interleaver -- DirectInterleaver<T>::interleave / reposition
+ * (InterleaverInterface.hpp:14-16; DirectInterleaver.hpp:12-37, :38-63).
+ * d_buf holds prod(fine) - prod(coarse) values in the reference's order.
+ * 1-D, 2-D and 3-D (the reference supports 1-D and 3-D).
+ * ------------------------------------------------------------------------- */
+int prodm_interleave(int dtype, const void* d_data, int ndims, const uint32_t* dims, const uint32_t* dims_fine,
+                     const uint32_t* dims_coarse, void* d_buf, const uint32_t* strides, void* stream);
+int prodm_reposition(int dtype, const void* d_buf, int ndims, const uint32_t* dims, const uint32_t* dims_fine,
+                     const uint32_t* dims_coarse, void* d_data, const uint32_t* strides, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Bitplane encoder -- BitplaneEncoderInterface<T>::encode
+ * (BitplaneEncoderInterface.hpp:16; NegaBinaryBPEncoder.hpp:18-125;
+ * GroupedBPEncoder.hpp:18-145).
+ * Writes the level's streams concatenated in plane order into d_blob (the
+ * byte layout of the reference level file with NullLevelCompressor) and the
+ * per-plane byte sizes into d_sizes[B]. d_errors (nullable): the
+ * error-collecting overload's B+1 squared-error table. n >= 1; a level with
+ * fewer values than one block is one short block (the reference's loops wrap
+ * there). workspace as for prodm_decompose.
+ * ------------------------------------------------------------------------- */
+int prodm_encode_bound(int encoder, int dtype, uint64_t n, int num_bitplanes, uint64_t* max_blob_bytes);
+int prodm_encode_workspace(int encoder, int dtype, uint64_t n, int num_bitplanes, size_t* bytes);
+int prodm_encode(int encoder, int dtype, const void* d_data, uint64_t n, int exp, int num_bitplanes, void* d_blob,
+                 uint64_t blob_capacity, uint32_t* d_sizes, double* d_errors, void* d_workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* Progressive decoder -- BitplaneEncoderInterface<T>::decode / progressive_decode
+ * (BitplaneEncoderInterface.hpp:18-20; NegaBinaryBPEncoder.hpp:127-192;
+ * GroupedBPEncoder.hpp:147-297). The handle keeps the per-level state of the
+ * grouped decoder (recording bitplanes and signs, GroupedBPEncoder.hpp:379-380),
+ * indexed by level. d_blob holds planes [start, start+num) concatenated as the
+ * reference retriever hands them over (FileRetriever.hpp:69-81); h_sizes are
+ * their byte sizes (host). The first call for a level must start at plane 0.
+ * Output: the contribution of these planes, n values, into d_out. */
+typedef struct prodm_decoder prodm_decoder;
+int prodm_decoder_create(prodm_decoder** out, int encoder, int dtype);
+int prodm_progressive_decode(prodm_decoder* h, const void* d_blob, const uint32_t* h_sizes, uint64_t n, int exp,
+                             int start_bitplane, int num_bitplanes, int level, int total_bitplanes, void* d_out,
+                             void* stream);
+int prodm_decoder_destroy(prodm_decoder* h);
+
+/* ---------------------------------------------------------------------------
+ * Error collectors -- ErrorCollectorInterface<T>::collect_level_error
+ * (ErrorCollectorInterface.hpp:14). Max: MaxErrorCollector.hpp:14-25 (needs
+ * no data; host output). Squared: SquaredErrorCollector.hpp:54-96 (device
+ * data, device output of B+1 doubles).
+ * ------------------------------------------------------------------------- */
+int prodm_collect_max(int dtype, double max_level_error, int num_bitplanes, double* h_out);
+int prodm_collect_squared_workspace(int dtype, int num_bitplanes, size_t* bytes);
+int prodm_collect_squared(int dtype, const void* d_data, uint64_t n, int num_bitplanes, double max_level_error,
+                          double* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Size interpreter -- SizeInterpreterInterface::interpret_retrieve_size
+ * (SizeInterpreterInterface.hpp:13). Runs on the device. d_sizes[nl*B] plane
+ * byte sizes, d_errors[nl*(B+1)] level error tables, d_index[nl] in/out
+ * bitplanes already retrieved, d_retrieve_sizes[nl] out. target_level and
+ * ndims parameterise the estimator tables; s is the S-norm exponent.
+ * ------------------------------------------------------------------------- */
+int prodm_interpret(int interpreter, int estimator, int dtype, int ndims, int target_level, double s, int nlevels,
+                    int num_bitplanes, const uint32_t* d_sizes, const double* d_errors, double tolerance,
+                    uint8_t* d_index, uint32_t* d_retrieve_sizes, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident composed refactor / reconstructor
+ * (ComposedRefactor.hpp:21-141; ComposedReconstructor.hpp:27-258).
+ * One handle per field configuration; all buffers are allocated at create.
+ * Refactor: decompose -> per level interleave + max -> encode (+ squared error
+ * tables when collector == PRODM_COLLECT_SQUARED), all on `stream`.
+ * Retrieve: error tables -> interpreter -> decode every retrieved plane ->
+ * recompose to full resolution into d_out; the per-level plane counts persist
+ * between calls (progressive retrieval), prodm_mdr_reset_retrieval() clears them.
+ * ------------------------------------------------------------------------- */
+typedef struct prodm_config {
+    int dtype;
+    int ndims;
+    uint32_t dims[3];
+    int target_level;
+    int num_bitplanes;
+    int encoder;
+    int basis;
+    int collector;
+} prodm_config;
+
+typedef struct prodm_mdr prodm_mdr;
+int prodm_mdr_create(prodm_mdr** out, const prodm_config* cfg);
+int prodm_mdr_refactor(prodm_mdr* h, const void* d_field, void* stream);
+/* host copies (synchronise the stream): sizes[(L+1)*B], bounds[L+1] as
+ * double, errors[(L+1)*(B+1)] (squared tables; zeros when not collected) */
+int prodm_mdr_level_info(prodm_mdr* h, uint32_t* h_sizes, double* h_bounds, double* h_errors, void* stream);
+/* reference metadata bytes (ComposedRefactor.hpp:48-67) followed by an
+ * extension carrying the squared-error tables; *len receives the size. */
+int prodm_mdr_metadata(prodm_mdr* h, uint8_t* h_buf, size_t capacity, size_t* len, void* stream);
+/* reference level-file bytes of one level into dst (device or host). */
+int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t capacity, int dst_is_host, uint64_t* len,
+                           void* stream);
+int prodm_mdr_retrieve(prodm_mdr* h, double tolerance, int interpreter, int estimator, double s, void* d_out,
+                       void* stream);
+/* the two halves of prodm_mdr_retrieve: the interpreter alone (updates the
+ * per-level plane counts on the device), then decode + recompose */
+int prodm_mdr_interpret(prodm_mdr* h, double tolerance, int interpreter, int estimator, double s, void* stream);
+int prodm_mdr_reconstruct(prodm_mdr* h, void* d_out, void* stream);
+/* Reconstructor fed from the reference's on-disk format instead of a device
+ * refactor (ComposedReconstructor::load_metadata, ComposedReconstructor.hpp:
+ * 133-154, and ConcatLevelFileRetriever::retrieve_level_components,
+ * FileRetriever.hpp:15-35): metadata bytes as written by
+ * ComposedRefactor::write_metadata (the squared-error extension is optional),
+ * then byte ranges [offset, offset+bytes) of level files as they are fetched.
+ * A level's planes must be loaded before a reconstruct uses them. */
+int prodm_mdr_load_metadata(prodm_mdr* h, const uint8_t* h_buf, size_t len, void* stream);
+int prodm_mdr_load_level(prodm_mdr* h, int level, const void* src, uint64_t offset, uint64_t bytes, int src_is_host,
+                         void* stream);
+/* retrieve with explicit per-level plane counts (h_index[L+1]) */
+int prodm_mdr_retrieve_planes(prodm_mdr* h, const uint8_t* h_index, void* d_out, void* stream);
+int prodm_mdr_get_index(prodm_mdr* h, uint8_t* h_index, void* stream);
+int prodm_mdr_reset_retrieval(prodm_mdr* h, void* stream);
+/* copies the packed level coefficients of the last refactor (level l at the
+ * offset given by the sum of the earlier level sizes) into d_dst */
+int prodm_mdr_coefficients(prodm_mdr* h, void* d_dst, void* stream);
+int prodm_mdr_destroy(prodm_mdr* h);
+
+/* ---------------------------------------------------------------------------
+ * Diagnostics (no counterpart in the reference, whose only instrument is a
+ * wall-clock Timer, RefactorUtils.hpp:145-170).
+ * Stage timing records CUDA events on the launching stream around each stage;
+ * prodm_mdr_stage_times returns accumulated milliseconds and counts for stage
+ * id = kind * 17 + level, kinds 0 decompose, 1 encode, 2 interpret,
+ * 3 decode, 4 recompose (arrays of 85 entries).
+ * prodm_kernel_launch_count: kernels launched by this library so far.
+ * ------------------------------------------------------------------------- */
+int prodm_mdr_set_timing(prodm_mdr* h, int enable);
+int prodm_mdr_stage_times(prodm_mdr* h, double* h_ms, uint32_t* h_counts);
+int prodm_kernel_launch_count(uint64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRODM_GB300_H */

@@ -29,7 +29,7 @@ def _stale(out, srcs):
 def build_oracle(force=False):
     srcs = [os.path.join(HERE, "mdr_oracle.cpp"), os.path.join(HERE, "mdr_oracle.hpp")]
     if force or _stale(ORACLE_SO, srcs):
-        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", ORACLE_SO, srcs[0]]
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", ORACLE_SO, srcs[0]]
         subprocess.check_call(cmd)
     return ORACLE_SO
 
@@ -43,7 +43,7 @@ def build_ref(force=False):
     src = os.path.join(HERE, "ref_harness", "ref_harness.cpp")
     deps = [src, os.path.join(HERE, "mdr_oracle.hpp")]
     if force or _stale(REF_SO, deps):
-        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-w",
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w",
                "-I", os.path.join(HERE, "ref_harness", "shim"), "-I", inc,
                "-o", REF_SO, src]
         if os.path.exists(ZSTD_LIB):

@@ -1,0 +1,304 @@
+"""Python host API over the C ABI (device memory and streams come from torch).
+
+Component functions mirror the reference's plugin concepts (decompose /
+recompose, interleave / reposition, encode / progressive_decode, error
+collectors, size interpreters); ``MDRField`` is the device-resident composed
+refactor / reconstructor. All arrays are torch CUDA tensors; nothing here
+computes on the CPU.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import BASIS, COLLECT, ENC, EST, INTERP, call, load
+
+_DT = {torch.float32: _lib.F32, torch.float64: _lib.F64}
+
+
+def _dtype(t):
+    try:
+        return _DT[t.dtype]
+    except KeyError:
+        raise TypeError("only float32 and float64 tensors are supported")
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _u32(seq):
+    a = (C.c_uint32 * len(seq))(*[int(x) for x in seq])
+    return a
+
+
+def _ptr(t):
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def max_level(dims):
+    out = C.c_int()
+    call("prodm_max_level", len(dims), _u32(dims), C.byref(out))
+    return out.value
+
+
+def level_dims(dims, L):
+    nd = len(dims)
+    out = (C.c_uint32 * ((L + 1) * nd))()
+    el = (C.c_uint64 * (L + 1))()
+    call("prodm_level_dims", nd, _u32(dims), L, out, el)
+    return np.array(out[:], np.uint32).reshape(L + 1, nd), np.array(el[:], np.uint64)
+
+
+# ---------------------------------------------------------------------------
+# components
+# ---------------------------------------------------------------------------
+def decompose(data, target_level, basis="hierarchical", dims=None, stream=None, workspace=None):
+    """In-place MGARD decomposition of a CUDA tensor (reference layout)."""
+    dims = list(dims or data.shape)
+    ws, wsb = (None, 0) if workspace is None else (_ptr(workspace), workspace.numel() * workspace.element_size())
+    call("prodm_decompose", _dtype(data), _ptr(data), len(dims), _u32(dims), target_level, None, BASIS[basis], ws, wsb,
+         _stream(stream))
+    return data
+
+
+def recompose(data, target_level, basis="hierarchical", dims=None, stream=None, workspace=None):
+    dims = list(dims or data.shape)
+    ws, wsb = (None, 0) if workspace is None else (_ptr(workspace), workspace.numel() * workspace.element_size())
+    call("prodm_recompose", _dtype(data), _ptr(data), len(dims), _u32(dims), target_level, None, BASIS[basis], ws, wsb,
+         _stream(stream))
+    return data
+
+
+def interleave(data, fine, coarse, stream=None):
+    n = int(np.prod(fine, dtype=np.int64)) - int(np.prod(coarse, dtype=np.int64))
+    buf = torch.empty(n, dtype=data.dtype, device=data.device)
+    dims = list(data.shape)
+    call("prodm_interleave", _dtype(data), _ptr(data), len(dims), _u32(dims), _u32(fine), _u32(coarse), _ptr(buf),
+         None, _stream(stream))
+    return buf
+
+
+def reposition(buf, data, fine, coarse, stream=None):
+    dims = list(data.shape)
+    call("prodm_reposition", _dtype(buf), _ptr(buf), len(dims), _u32(dims), _u32(fine), _u32(coarse), _ptr(data),
+         None, _stream(stream))
+    return data
+
+
+def encode(kind, data, exp, num_bitplanes, collect=False, stream=None):
+    """Returns (blob uint8 tensor cut to size, sizes numpy[B], errors numpy[B+1] or None)."""
+    n = data.numel()
+    bound = C.c_uint64()
+    call("prodm_encode_bound", ENC[kind], _dtype(data), n, num_bitplanes, C.byref(bound))
+    blob = torch.empty(bound.value + 16, dtype=torch.uint8, device=data.device)
+    sizes = torch.empty(num_bitplanes, dtype=torch.int32, device=data.device)
+    errs = torch.empty(num_bitplanes + 1, dtype=torch.float64, device=data.device) if collect else None
+    call("prodm_encode", ENC[kind], _dtype(data), _ptr(data), n, int(exp), num_bitplanes, _ptr(blob), bound.value,
+         _ptr(sizes), _ptr(errs) if collect else None, None, 0, _stream(stream))
+    sz = sizes.cpu().numpy().view(np.uint32).copy()
+    total = int(sz.astype(np.int64).sum())
+    return blob[:total], sz, (errs.cpu().numpy() if collect else None)
+
+
+class ProgressiveDecoder:
+    """Stateful decoder (grouped state per level), BitplaneEncoderInterface::progressive_decode."""
+
+    def __init__(self, kind, dtype):
+        self.kind, self.dtype = kind, dtype
+        self.h = C.c_void_p()
+        call("prodm_decoder_create", C.byref(self.h), ENC[kind], _DT[dtype])
+
+    def decode(self, blob, sizes, n, exp, start, num, level, total_bitplanes, stream=None):
+        out = torch.empty(n, dtype=self.dtype, device="cuda")
+        hs = (C.c_uint32 * max(1, num))(*[int(x) for x in sizes[:num]])
+        call("prodm_progressive_decode", self.h, _ptr(blob) if num else None, hs, n, int(exp), start, num, level,
+             total_bitplanes, _ptr(out), _stream(stream))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h:
+                load().prodm_decoder_destroy(self.h)
+        except Exception:
+            pass
+
+
+def collect_max(bound, num_bitplanes, dtype=torch.float32):
+    out = (C.c_double * (num_bitplanes + 1))()
+    call("prodm_collect_max", _DT[dtype], float(bound), num_bitplanes, out)
+    return np.array(out[:])
+
+
+def collect_squared(data, num_bitplanes, max_level_error, stream=None):
+    out = torch.empty(num_bitplanes + 1, dtype=torch.float64, device=data.device)
+    call("prodm_collect_squared", _dtype(data), _ptr(data), data.numel(), num_bitplanes, float(max_level_error),
+         _ptr(out), None, 0, _stream(stream))
+    return out.cpu().numpy()
+
+
+def interpret(kind, estimator, sizes, errors, tolerance, index, ndims=3, target_level=None, s=0.0,
+              dtype=torch.float32, stream=None):
+    """Device greedy interpreter. sizes [nl,B] (uint32), errors [nl,B+1]; returns (index, retrieve_sizes)."""
+    sizes = np.ascontiguousarray(sizes, np.uint32)
+    nl, B = sizes.shape
+    L = nl - 1 if target_level is None else target_level
+    dsz = torch.from_numpy(sizes.view(np.int32)).cuda()
+    derr = torch.from_numpy(np.ascontiguousarray(errors, np.float64)).cuda()
+    didx = torch.from_numpy(np.ascontiguousarray(index, np.uint8).copy()).cuda()
+    drsz = torch.zeros(nl, dtype=torch.int32, device="cuda")
+    call("prodm_interpret", INTERP[kind], EST[estimator], _DT[dtype], ndims, L, float(s), nl, B, _ptr(dsz), _ptr(derr),
+         float(tolerance), _ptr(didx), _ptr(drsz), _stream(stream))
+    return didx.cpu().numpy(), drsz.cpu().numpy().view(np.uint32)
+
+
+# ---------------------------------------------------------------------------
+# device-resident composed refactor / reconstructor
+# ---------------------------------------------------------------------------
+class MDRField:
+    """One field configuration: refactor on the device, retrieve progressively.
+
+    Mirrors ComposedRefactor::refactor (ComposedRefactor.hpp:21-141) and
+    ComposedReconstructor::progressive_reconstruct (ComposedReconstructor.hpp:
+    106-122) with all state resident in HBM.
+    """
+
+    def __init__(self, shape, dtype=torch.float32, target_level=None, num_bitplanes=32, encoder="negabinary",
+                 basis="hierarchical", collector="max"):
+        self.shape = tuple(int(x) for x in shape)
+        self.dtype = dtype
+        if target_level is None:
+            target_level = max_level(self.shape)
+        self.L, self.B = int(target_level), int(num_bitplanes)
+        self.encoder, self.basis, self.collector = encoder, basis, collector
+        cfg = _lib.prodm_config()
+        cfg.dtype = _DT[dtype]
+        cfg.ndims = len(self.shape)
+        for i, d in enumerate(self.shape):
+            cfg.dims[i] = d
+        cfg.target_level = self.L
+        cfg.num_bitplanes = self.B
+        cfg.encoder = ENC[encoder]
+        cfg.basis = BASIS[basis]
+        cfg.collector = COLLECT[collector]
+        self.h = C.c_void_p()
+        call("prodm_mdr_create", C.byref(self.h), C.byref(cfg))
+        self.level_dims, self.level_elements = level_dims(self.shape, self.L)
+
+    def refactor(self, field, stream=None):
+        if field.dtype != self.dtype or tuple(field.shape) != self.shape or not field.is_contiguous():
+            raise ValueError("field must be a contiguous %s tensor of shape %s" % (self.dtype, self.shape))
+        call("prodm_mdr_refactor", self.h, _ptr(field), _stream(stream))
+
+    def level_info(self, stream=None):
+        nl, B = self.L + 1, self.B
+        sizes = (C.c_uint32 * (nl * B))()
+        bounds = (C.c_double * nl)()
+        errs = (C.c_double * (nl * (B + 1)))()
+        call("prodm_mdr_level_info", self.h, sizes, bounds, errs, _stream(stream))
+        return (np.array(sizes[:], np.uint32).reshape(nl, B), np.array(bounds[:]),
+                np.array(errs[:]).reshape(nl, B + 1))
+
+    def metadata(self, stream=None):
+        n = C.c_size_t()
+        call("prodm_mdr_metadata", self.h, None, 0, C.byref(n), _stream(stream))
+        buf = (C.c_uint8 * n.value)()
+        call("prodm_mdr_metadata", self.h, buf, n.value, C.byref(n), _stream(stream))
+        return bytes(buf)
+
+    def export_level(self, level, stream=None):
+        n = C.c_uint64()
+        call("prodm_mdr_export_level", self.h, level, None, 0, 1, C.byref(n), _stream(stream))
+        buf = np.zeros(n.value, np.uint8)
+        call("prodm_mdr_export_level", self.h, level, C.c_void_p(buf.ctypes.data), n.value, 1, C.byref(n),
+             _stream(stream))
+        return buf
+
+    def retrieve(self, tolerance, out=None, interpreter="sign_exclude", estimator="max_hb", s=0.0, stream=None):
+        if out is None:
+            out = torch.empty(self.shape, dtype=self.dtype, device="cuda")
+        call("prodm_mdr_retrieve", self.h, float(tolerance), INTERP[interpreter], EST[estimator], float(s), _ptr(out),
+             _stream(stream))
+        return out
+
+    def interpret(self, tolerance, interpreter="sign_exclude", estimator="max_hb", s=0.0, stream=None):
+        call("prodm_mdr_interpret", self.h, float(tolerance), INTERP[interpreter], EST[estimator], float(s),
+             _stream(stream))
+
+    def reconstruct(self, out=None, stream=None):
+        if out is None:
+            out = torch.empty(self.shape, dtype=self.dtype, device="cuda")
+        call("prodm_mdr_reconstruct", self.h, _ptr(out), _stream(stream))
+        return out
+
+    def load_metadata(self, meta, stream=None):
+        buf = (C.c_uint8 * len(meta)).from_buffer_copy(meta)
+        call("prodm_mdr_load_metadata", self.h, buf, len(meta), _stream(stream))
+
+    def load_level(self, level, src, offset=0, stream=None):
+        """src: numpy uint8 array (host) or torch uint8 tensor (host pinned or device)."""
+        if isinstance(src, np.ndarray):
+            src = np.ascontiguousarray(src, np.uint8)
+            ptr, host, n = C.c_void_p(src.ctypes.data), 1, src.nbytes
+        else:
+            ptr, host, n = C.c_void_p(src.data_ptr()), 0 if src.is_cuda else 1, src.numel()
+        call("prodm_mdr_load_level", self.h, level, ptr, int(offset), int(n), host, _stream(stream))
+
+    def retrieve_planes(self, index, out=None, stream=None):
+        if out is None:
+            out = torch.empty(self.shape, dtype=self.dtype, device="cuda")
+        idx = (C.c_uint8 * (self.L + 1))(*[int(x) for x in index])
+        call("prodm_mdr_retrieve_planes", self.h, idx, _ptr(out), _stream(stream))
+        return out
+
+    def index(self, stream=None):
+        idx = (C.c_uint8 * (self.L + 1))()
+        call("prodm_mdr_get_index", self.h, idx, _stream(stream))
+        return np.array(idx[:], np.uint8)
+
+    def reset(self, stream=None):
+        call("prodm_mdr_reset_retrieval", self.h, _stream(stream))
+
+    def coefficients(self, stream=None):
+        """Packed level coefficients of the last refactor (a device copy)."""
+        n = int(self.level_elements.astype(np.int64).sum())
+        t = torch.empty(n, dtype=self.dtype, device="cuda")
+        call("prodm_mdr_coefficients", self.h, _ptr(t), _stream(stream))
+        return t
+
+    def retrieved_bytes(self, index=None):
+        sizes, _, _ = self.level_info()
+        idx = self.index() if index is None else index
+        return int(sum(int(sizes[l, :idx[l]].astype(np.int64).sum()) for l in range(self.L + 1)))
+
+    def set_timing(self, enable=True):
+        call("prodm_mdr_set_timing", self.h, int(enable))
+
+    def stage_times(self):
+        """{(kind, level): (total_ms, count)} for stages timed since set_timing(True)."""
+        ms = (C.c_double * 85)()
+        cnt = (C.c_uint32 * 85)()
+        call("prodm_mdr_stage_times", self.h, ms, cnt)
+        kinds = ("decompose", "encode", "interpret", "decode", "recompose")
+        return {(kinds[i // 17], i % 17): (ms[i], cnt[i]) for i in range(85) if cnt[i]}
+
+    def close(self):
+        if self.h:
+            load().prodm_mdr_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def kernel_launch_count():
+    out = C.c_uint64()
+    call("prodm_kernel_launch_count", C.byref(out))
+    return out.value

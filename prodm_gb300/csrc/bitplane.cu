@@ -1,0 +1,712 @@
+// Bitplane encoders / decoders and error collectors (sm_103a).
+//
+// Stream layout on the device ("aligned layout"): the words of plane p of a
+// level start at plane[p] (word aligned). NegaBinary planes all hold
+// ceil(n / block) words; grouped planes hold between 0 and 2 * nblocks words.
+// The grouped encoder's per-block recording bitplanes (the u8 header of
+// stream 0, GroupedBPEncoder.hpp:66-71) are kept in a separate rb array.
+// pack.cu turns this into the reference level-file byte layout.
+//
+// Warp mapping: one warp per block of 32 (fp32, u32 words) or 64 (fp64, u64
+// words: each lane holds elements lane and lane + 32) values; __ballot_sync
+// transposes one bitplane of the block into one stream word; lane p then
+// owns the word of plane p (and p + 32 for fp64).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace prodm {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <class T>
+__device__ __forceinline__ int level_exp(const typename KeyOf<T>::type* maxkey, int exp_arg) {
+    return maxkey ? frexp_exp(key_to_val(*maxkey, T())) : exp_arg;
+}
+
+// quantisation shared by the encoders
+__device__ __forceinline__ int32_t trunc_fps(float v) { return (int32_t)v; }
+__device__ __forceinline__ int64_t trunc_fps(double v) { return (int64_t)v; }
+
+// ---------------------------------------------------------------------------
+// per-thread error accumulators -> per-CTA partial tables (B+1 doubles each)
+// ---------------------------------------------------------------------------
+template <int NACC, class A>
+__device__ void flush_errors(A (&acc)[NACC], int B, double* partial) {
+    __shared__ double red[NACC];
+    for (int k = threadIdx.x; k < NACC; k += blockDim.x) red[k] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NACC; k++) {
+        A v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+        if ((threadIdx.x & 31) == 0 && k <= B) atomicAdd(&red[k], (double)v);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k <= B; k += blockDim.x) partial[(size_t)blockIdx.x * (B + 1) + k] = red[k];
+}
+
+// NegaBinaryBPEncoder::collect_level_errors (NegaBinaryBPEncoder.hpp:231-239)
+// in shifted units: acc[B] += m^2, acc[B-k] += (nb2bin(nb & (2^k-1)) + m)^2,
+// acc[0] += shifted^2.
+template <int NACC>
+__device__ __forceinline__ void nb_errors(float (&acc)[NACC], uint32_t nb, float shifted, float m, int B) {
+    acc[B < NACC ? B : NACC - 1] += m * m;
+#pragma unroll
+    for (int k = 1; k < NACC - 1; k++) {
+        if (k < B) {
+            float d = (float)nb_to_bin(nb & ((1u << k) - 1u)) + m;
+            acc[B - k] += d * d;
+        }
+    }
+    acc[0] += shifted * shifted;
+}
+template <int NACC>
+__device__ __forceinline__ void nb_errors(double (&acc)[NACC], uint64_t nb, double shifted, double m, int B) {
+    acc[B < NACC ? B : NACC - 1] += m * m;
+#pragma unroll
+    for (int k = 1; k < NACC - 1; k++) {
+        if (k < B) {
+            double d = (double)nb_to_bin((uint64_t)(nb & ((1ull << k) - 1ull))) + m;
+            acc[B - k] += d * d;
+        }
+    }
+    acc[0] += shifted * shifted;
+}
+// GroupedBPEncoder::collect_level_errors (GroupedBPEncoder.hpp:324-335), a = |shifted|
+template <int NACC>
+__device__ __forceinline__ void gr_errors(float (&acc)[NACC], float a, int B) {
+    uint32_t fp = (uint32_t)a;
+    float m = a - (float)fp;
+    acc[B < NACC ? B : NACC - 1] += m * m;
+#pragma unroll
+    for (int k = 1; k < NACC - 1; k++) {
+        if (k < B) {
+            float d = (float)(fp & ((1u << k) - 1u)) + m;
+            acc[B - k] += d * d;
+        }
+    }
+    acc[0] += a * a;
+}
+template <int NACC>
+__device__ __forceinline__ void gr_errors(double (&acc)[NACC], double a, int B) {
+    uint64_t fp = (uint64_t)a;
+    double m = a - (double)fp;
+    acc[B < NACC ? B : NACC - 1] += m * m;
+#pragma unroll
+    for (int k = 1; k < NACC - 1; k++) {
+        if (k < B) {
+            double d = (double)(fp & ((1ull << k) - 1ull)) + m;
+            acc[B - k] += d * d;
+        }
+    }
+    acc[0] += a * a;
+}
+
+template <class T> struct Acc { using type = float; static constexpr int N = 33; };
+template <> struct Acc<double> { using type = double; static constexpr int N = 65; };
+
+// ---------------------------------------------------------------------------
+// NegaBinary encoder -- NegaBinaryBPEncoder.hpp:18-62 (+ :65-125 errors)
+// ---------------------------------------------------------------------------
+template <class T, bool ERR>
+__global__ void __launch_bounds__(256) k_nb_encode(const T* __restrict__ x, uint64_t n,
+                                                   const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg,
+                                                   int B, typename Traits<T>::S* __restrict__ out, uint64_t stride,
+                                                   double* __restrict__ partial) {
+    using S = typename Traits<T>::S;
+    using FPS = typename Traits<T>::FPS;
+    using FP = typename Traits<T>::FP;
+    using A = typename Acc<T>::type;
+    constexpr int BS = Traits<T>::kBlock;
+    const int exp = level_exp<T>(maxkey, exp_arg) + 2;   // :21
+    const int lane = threadIdx.x & 31;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    A acc[Acc<T>::N];
+    if (ERR) {
+#pragma unroll
+        for (int k = 0; k < Acc<T>::N; k++) acc[k] = 0;
+    }
+    for (uint64_t b = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nblocks; b += warps) {
+        FP nb[BS / 32];
+#pragma unroll
+        for (int h = 0; h < BS / 32; h++) {
+            uint64_t i = b * BS + h * 32 + lane;
+            nb[h] = 0;
+            if (i < n) {
+                T shifted = ldexp_t(x[i], B - exp);          // :42
+                FPS q = trunc_fps(shifted);
+                nb[h] = nb_from_bin(q);
+                if (ERR) nb_errors(acc, nb[h], (A)shifted, (A)(shifted - (T)q), B);
+            }
+        }
+        S mine0 = 0, mine1 = 0;
+        for (int p = 0; p < B; p++) {                        // encode_block :240-250
+            const int k = B - 1 - p;
+            S w = (S)__ballot_sync(FULL, (nb[0] >> k) & 1u);
+            if (BS == 64) w |= (S)__ballot_sync(FULL, (nb[BS / 32 - 1] >> k) & 1u) << (BS == 64 ? 32 : 0);
+            if ((p & 31) == lane) {
+                if (p < 32) mine0 = w; else mine1 = w;
+            }
+        }
+        if (lane < B) out[(uint64_t)lane * stride + b] = mine0;
+        if (lane + 32 < B) out[(uint64_t)(lane + 32) * stride + b] = mine1;
+    }
+    if (ERR) flush_errors(acc, B, partial);
+}
+
+// NegaBinaryBPEncoder::progressive_decode -- :132-192. planes [s, s+num)
+// with plane (s+i) at base[i * stride]; a device count (dnum[0]) overrides num.
+template <class T>
+__global__ void __launch_bounds__(256) k_nb_decode(const typename Traits<T>::S* __restrict__ base, uint64_t stride,
+                                                   uint64_t n, const typename KeyOf<T>::type* __restrict__ maxkey,
+                                                   int exp_arg, int s, int num, const uint8_t* __restrict__ dnum,
+                                                   T* __restrict__ out) {
+    using S = typename Traits<T>::S;
+    using FP = typename Traits<T>::FP;
+    constexpr int BS = Traits<T>::kBlock;
+    if (dnum) num = dnum[0] - s;
+    const int exp = level_exp<T>(maxkey, exp_arg) + 2;
+    const int e = s + num;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t b = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); b < nblocks; b += warps) {
+        S w0 = 0, w1 = 0;
+        if (lane < num) w0 = __ldg(base + (uint64_t)lane * stride + b);
+        if (lane + 32 < num) w1 = __ldg(base + (uint64_t)(lane + 32) * stride + b);
+        FP acc[BS / 32];
+#pragma unroll
+        for (int h = 0; h < BS / 32; h++) acc[h] = 0;
+        for (int i = 0; i < num; i++) {                       // decode_block :251-260
+            S w = __shfl_sync(FULL, i < 32 ? w0 : w1, i & 31);
+            const int k = num - 1 - i;
+#pragma unroll
+            for (int h = 0; h < BS / 32; h++) acc[h] |= (FP)((w >> (h * 32 + lane)) & 1u) << k;
+        }
+#pragma unroll
+        for (int h = 0; h < BS / 32; h++) {
+            uint64_t i = b * BS + h * 32 + lane;
+            if (i < n) {
+                T v = num == 0 ? (T)0 : ldexp_t((T)nb_to_bin(acc[h]), -e + exp);
+                out[i] = (num != 0 && (e & 1)) ? -v : v;       // :153, :177
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Grouped encoder -- GroupedBPEncoder.hpp:18-73 (+ :76-145 errors)
+// Chunk = 8 warps x 32 blocks per CTA.
+// ---------------------------------------------------------------------------
+constexpr int GR_WARPS = 8;
+constexpr int GR_BPW = 32;                       // blocks per warp
+constexpr int GR_CHUNK = GR_WARPS * GR_BPW;      // blocks per CTA
+
+template <class T>
+__device__ __forceinline__ typename Traits<T>::FP gr_mag(T v, int B, int exp, bool& neg, T& shifted) {
+    shifted = ldexp_t(v, B - exp);                  // :41
+    int64_t fix = (int64_t)shifted;                 // :42
+    neg = v < 0;
+    return (typename Traits<T>::FP)(neg ? -fix : fix);
+}
+
+// word counts contributed by a block with recording plane r to plane p
+__device__ __forceinline__ uint32_t gr_words(int r, int p) { return (r < p ? 1u : 0u) + (r == p ? 2u : 0u); }
+
+template <class T, bool ERR>
+__global__ void __launch_bounds__(256) k_gr_rb(const T* __restrict__ x, uint64_t n,
+                                               const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg, int B,
+                                               uint8_t* __restrict__ rbs, uint32_t* __restrict__ chunk_words,
+                                               double* __restrict__ partial) {
+    using FP = typename Traits<T>::FP;
+    using A = typename Acc<T>::type;
+    constexpr int BS = Traits<T>::kBlock;
+    const int exp = level_exp<T>(maxkey, exp_arg);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    __shared__ uint32_t cnt[GR_WARPS][64];
+    uint32_t c0 = 0, c1 = 0;
+    A acc[Acc<T>::N];
+    if (ERR) {
+#pragma unroll
+        for (int k = 0; k < Acc<T>::N; k++) acc[k] = 0;
+    }
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    for (int j = 0; j < GR_BPW; j++) {
+        uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        FP orv = 0;
+#pragma unroll
+        for (int h = 0; h < BS / 32; h++) {
+            uint64_t i = b * BS + h * 32 + lane;
+            if (i < n) {
+                bool neg;
+                T sh;
+                FP q = gr_mag<T>(x[i], B, exp, neg, sh);
+                orv |= q;
+                if (ERR) gr_errors(acc, (A)fabs(sh), B);
+            }
+        }
+        int r;
+        if (BS == 32) {
+            uint32_t o = __reduce_or_sync(FULL, (uint32_t)orv);
+            r = o ? B - 1 - (31 - __clz(o)) : B;
+        } else {
+            uint32_t lo = __reduce_or_sync(FULL, (uint32_t)orv);
+            uint32_t hi = __reduce_or_sync(FULL, (uint32_t)((uint64_t)orv >> 32));
+            uint64_t o = ((uint64_t)hi << 32) | lo;
+            r = o ? B - 1 - (63 - __clzll((long long)o)) : B;
+        }
+        if (lane == 0) rbs[b] = (uint8_t)r;
+        c0 += gr_words(r, lane);
+        c1 += gr_words(r, lane + 32);
+    }
+    cnt[warp][lane] = c0;
+    cnt[warp][lane + 32] = c1;
+    __syncthreads();
+    if (threadIdx.x < 64 && (int)threadIdx.x < B) {
+        uint32_t s = 0;
+        for (int w = 0; w < GR_WARPS; w++) s += cnt[w][threadIdx.x];
+        chunk_words[(uint64_t)blockIdx.x * B + threadIdx.x] = s;
+    }
+    if (ERR) flush_errors(acc, B, partial);
+}
+
+// exclusive scan of chunk_words over chunks, per plane; stream byte sizes.
+__global__ void k_gr_scan(const uint32_t* __restrict__ chunk_words, uint64_t nchunks, int B, uint64_t nblocks,
+                          int word_bytes, uint32_t* __restrict__ chunk_off, uint32_t* __restrict__ sizes) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    for (int p = 0; p < B; p++) {
+        if (threadIdx.x == 0) carry = 0;
+        __syncthreads();
+        for (uint64_t base = 0; base < nchunks; base += blockDim.x) {
+            uint64_t c = base + threadIdx.x;
+            uint32_t v = c < nchunks ? chunk_words[c * B + p] : 0;
+            uint32_t incl = v;
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (lane == 31) wsum[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                uint32_t ws = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+                uint32_t wi = ws;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t t = __shfl_up_sync(FULL, wi, o);
+                    if (lane >= o) wi += t;
+                }
+                wsum[lane] = wi - ws;   // exclusive warp offsets
+            }
+            __syncthreads();
+            uint32_t excl = carry + wsum[warp] + incl - v;
+            if (c < nchunks) chunk_off[c * B + p] = excl;
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) sizes[p] = carry * word_bytes + (p == 0 ? (uint32_t)(4 + nblocks) : 0u);
+        __syncthreads();
+    }
+}
+
+// per-warp starting offsets (word index in each plane) for the warp's 32 blocks
+__device__ __forceinline__ void gr_warp_offsets(const uint8_t* __restrict__ rbs, uint64_t nblocks,
+                                                const uint32_t* __restrict__ chunk_off, int B, uint32_t& off0,
+                                                uint32_t& off1) {
+    __shared__ uint32_t cnt[GR_WARPS][64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    uint32_t c0 = 0, c1 = 0;
+    for (int j = 0; j < GR_BPW; j++) {
+        uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        int r = rbs[b];
+        c0 += gr_words(r, lane);
+        c1 += gr_words(r, lane + 32);
+    }
+    cnt[warp][lane] = c0;
+    cnt[warp][lane + 32] = c1;
+    __syncthreads();
+    off0 = lane < B ? chunk_off[(uint64_t)blockIdx.x * B + lane] : 0;
+    off1 = lane + 32 < B ? chunk_off[(uint64_t)blockIdx.x * B + lane + 32] : 0;
+    for (int w = 0; w < warp; w++) {
+        off0 += cnt[w][lane];
+        off1 += cnt[w][lane + 32];
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gr_write(const T* __restrict__ x, uint64_t n,
+                                                  const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg,
+                                                  int B, const uint8_t* __restrict__ rbs,
+                                                  const uint32_t* __restrict__ chunk_off,
+                                                  typename Traits<T>::S* __restrict__ out, uint64_t cap) {
+    using S = typename Traits<T>::S;
+    using FP = typename Traits<T>::FP;
+    constexpr int BS = Traits<T>::kBlock;
+    const int exp = level_exp<T>(maxkey, exp_arg);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    uint32_t off0, off1;
+    gr_warp_offsets(rbs, nblocks, chunk_off, B, off0, off1);
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    for (int j = 0; j < GR_BPW; j++) {
+        uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        FP q[BS / 32];
+        S sign = 0;
+#pragma unroll
+        for (int h = 0; h < BS / 32; h++) {
+            uint64_t i = b * BS + h * 32 + lane;
+            bool neg = false;
+            q[h] = 0;
+            if (i < n) {
+                T sh;
+                q[h] = gr_mag<T>(x[i], B, exp, neg, sh);
+            }
+            sign |= (S)__ballot_sync(FULL, neg) << (h * 32);
+        }
+        const int r = rbs[b];
+        S mine0 = 0, mine1 = 0;
+        for (int p = r; p < B; p++) {                          // encode_block :337-357
+            const int k = B - 1 - p;
+            S w = (S)__ballot_sync(FULL, (q[0] >> k) & 1u);
+            if (BS == 64) w |= (S)__ballot_sync(FULL, (q[BS / 32 - 1] >> k) & 1u) << (BS == 64 ? 32 : 0);
+            if ((p & 31) == lane) {
+                if (p < 32) mine0 = w; else mine1 = w;
+            }
+        }
+        if (lane < B && lane >= r) {
+            S* dst = out + (uint64_t)lane * cap + off0;
+            if (lane == r) { dst[0] = sign; dst[1] = mine0; }
+            else dst[0] = mine0;
+        }
+        if (lane + 32 < B && lane + 32 >= r) {
+            S* dst = out + (uint64_t)(lane + 32) * cap + off1;
+            if (lane + 32 == r) { dst[0] = sign; dst[1] = mine1; }
+            else dst[0] = mine1;
+        }
+        off0 += gr_words(r, lane);
+        off1 += gr_words(r, lane + 32);
+    }
+}
+
+// GroupedBPEncoder::progressive_decode -- :210-297 (planes [s, e)); plane p's
+// words at planes[p] (absolute plane index). signs: per-block sign words kept
+// between calls (nullable when s == 0). A device count (dnum[0]) overrides e.
+template <class T>
+__global__ void __launch_bounds__(256) k_gr_decode(const typename Traits<T>::S* const* __restrict__ planes,
+                                                   uint64_t n, const typename KeyOf<T>::type* __restrict__ maxkey,
+                                                   int exp_arg, int B, int s, int e,
+                                                   const uint8_t* __restrict__ dnum, const uint8_t* __restrict__ rbs,
+                                                   const uint32_t* __restrict__ chunk_off,
+                                                   typename Traits<T>::S* __restrict__ signs, T* __restrict__ out) {
+    using S = typename Traits<T>::S;
+    using FP = typename Traits<T>::FP;
+    constexpr int BS = Traits<T>::kBlock;
+    if (dnum) e = dnum[0];
+    const int exp = level_exp<T>(maxkey, exp_arg);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    uint32_t off0, off1;
+    gr_warp_offsets(rbs, nblocks, chunk_off, B, off0, off1);
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    for (int j = 0; j < GR_BPW; j++) {
+        uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        const int r = rbs[b];
+        if (r < e) {
+            S w0 = 0, w1 = 0, sg0 = 0, sg1 = 0;
+            int p0 = lane, p1 = lane + 32;
+            if (p0 < e && p0 >= s && p0 >= r) {
+                const S* src = planes[p0] + off0;
+                if (p0 == r) { sg0 = src[0]; w0 = src[1]; } else w0 = src[0];
+            }
+            if (p1 < e && p1 >= s && p1 >= r) {
+                const S* src = planes[p1] + off1;
+                if (p1 == r) { sg1 = src[0]; w1 = src[1]; } else w1 = src[0];
+            }
+            S sign;
+            if (r >= s) {
+                sign = __shfl_sync(FULL, r < 32 ? sg0 : sg1, r & 31);
+                if (signs && lane == 0) signs[b] = sign;
+            } else {
+                sign = signs[b];
+            }
+            FP acc[BS / 32];
+#pragma unroll
+            for (int h = 0; h < BS / 32; h++) acc[h] = 0;
+            const int first = r > s ? r : s;
+            for (int p = first; p < e; p++) {                 // decode_block :359-368
+                S w = __shfl_sync(FULL, p < 32 ? w0 : w1, p & 31);
+                const int k = e - 1 - p;
+#pragma unroll
+                for (int h = 0; h < BS / 32; h++) acc[h] |= (FP)((w >> (h * 32 + lane)) & 1u) << k;
+            }
+#pragma unroll
+            for (int h = 0; h < BS / 32; h++) {
+                uint64_t i = b * BS + h * 32 + lane;
+                if (i < n) {
+                    T v = ldexp_t((T)acc[h], -e + exp);
+                    out[i] = ((sign >> (h * 32 + lane)) & 1u) ? -v : v;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int h = 0; h < BS / 32; h++) {
+                uint64_t i = b * BS + h * 32 + lane;
+                if (i < n) out[i] = (T)0;
+            }
+        }
+        off0 += gr_words(r, lane);
+        off1 += gr_words(r, lane + 32);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Squared error collector -- SquaredErrorCollector.hpp:54-96. The bit-clearing
+// loop is evaluated in closed form: entry k receives (v - v with bits <= b
+// cleared)^2 for b = exp_diff + (idx0 - k) while b < prec, else v^2.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_sq_collect(const T* __restrict__ x, uint64_t n, int B, T maxv,
+                                                    double* __restrict__ partial) {
+    using A = typename Acc<T>::type;
+    using U = typename Traits<T>::Bits;
+    constexpr int prec = Traits<T>::kPrec;
+    A acc[Acc<T>::N];
+#pragma unroll
+    for (int k = 0; k < Acc<T>::N; k++) acc[k] = 0;
+    const int lexp = frexp_exp(maxv);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        T v = x[i];
+        if (v == (T)0) continue;
+        int de = frexp_exp(v);
+        U bits;
+        memcpy(&bits, &v, sizeof(T));
+        int exp_diff = lexp - de + prec - B;
+        int idx0 = B;
+        if (exp_diff <= 0) { idx0 += exp_diff; exp_diff = 0; }
+        if (idx0 <= 0) continue;
+        const T vv = v * v;
+#pragma unroll
+        for (int k = 0; k < Acc<T>::N; k++) {
+            if (k <= idx0 && k <= B) {
+                int bb = exp_diff + (idx0 - k);
+                if (bb < prec) {
+                    U cleared = bits & ~((((U)2) << bb) - (U)1);
+                    T f;
+                    memcpy(&f, &cleared, sizeof(T));
+                    T d = v - f;
+                    acc[k] += (A)(d * d);
+                } else {
+                    acc[k] += (A)vv;
+                }
+            }
+        }
+    }
+    flush_errors(acc, B, partial);
+}
+
+// sum partial tables in fixed order, then scale by 2^(2*(exp - B)) when exp
+// scaling applies (encoder tables, NegaBinaryBPEncoder.hpp:121-123).
+template <class T>
+__global__ void k_reduce_partials(const double* __restrict__ partial, int nparts, int B,
+                                  const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg, int exp_add,
+                                  int scale, double* __restrict__ out) {
+    for (int k = threadIdx.x; k <= B; k += blockDim.x) {
+        double s = 0;
+        for (int p = 0; p < nparts; p++) s += partial[(size_t)p * (B + 1) + k];
+        if (scale) {
+            int exp = level_exp<T>(maxkey, exp_arg) + exp_add;
+            s = ldexp(s, 2 * (-B + exp));
+        }
+        out[k] = s;
+    }
+}
+
+// MaxErrorCollector::collect_level_error -- MaxErrorCollector.hpp:14-25, for
+// all levels at once from the device bound array.
+template <class T>
+__global__ void k_max_collect(const T* __restrict__ bounds, int nl, int B, double* __restrict__ out) {
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
+        T bound = bounds[l];
+        int e = frexp_exp(bound);
+        double* o = out + (size_t)l * (B + 1);
+        o[0] = (double)bound;
+        double err = ldexp(1.0, e - 1);
+        for (int i = 1; i <= B; i++) { o[i] = err; err /= 2; }
+    }
+}
+
+// per-chunk word counts from an rb array (used when only the header is known)
+__global__ void k_chunk_words_from_rb(const uint8_t* __restrict__ rbs, uint64_t nblocks, int B,
+                                      uint32_t* __restrict__ chunk_words) {
+    __shared__ uint32_t cnt[GR_WARPS][64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    uint32_t c0 = 0, c1 = 0;
+    for (int j = 0; j < GR_BPW; j++) {
+        uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        int r = rbs[b];
+        c0 += gr_words(r, lane);
+        c1 += gr_words(r, lane + 32);
+    }
+    cnt[warp][lane] = c0;
+    cnt[warp][lane + 32] = c1;
+    __syncthreads();
+    if (threadIdx.x < 64 && (int)threadIdx.x < B) {
+        uint32_t s = 0;
+        for (int w = 0; w < GR_WARPS; w++) s += cnt[w][threadIdx.x];
+        chunk_words[(uint64_t)blockIdx.x * B + threadIdx.x] = s;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+int encode_partial_slots(uint64_t n, int elem_bytes) {
+    (void)n; (void)elem_bytes;
+    return kSMs * 4;
+}
+
+template <class T>
+int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, void* out, uint64_t stride,
+                     double* partial, double* errs_out, cudaStream_t st) {
+    using K = typename KeyOf<T>::type;
+    constexpr int BS = Traits<T>::kBlock;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    const int th = 256;
+    unsigned grid = errs_out ? (unsigned)kSMs * 4 : grid_for(nblocks * 32, th, 8);
+    if (errs_out) {
+        k_nb_encode<T, true><<<grid, th, 0, st>>>(x, n, (const K*)maxkey, exp, B, (typename Traits<T>::S*)out, stride,
+                                                  partial);
+        PRODM_CHECK_LAUNCH("k_nb_encode");
+        k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
+        PRODM_CHECK_LAUNCH("k_reduce_partials");
+    } else {
+        k_nb_encode<T, false><<<grid, th, 0, st>>>(x, n, (const K*)maxkey, exp, B, (typename Traits<T>::S*)out, stride,
+                                                   nullptr);
+        PRODM_CHECK_LAUNCH("k_nb_encode");
+    }
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_nb_decode(const void* base, uint64_t stride, uint64_t n, const void* maxkey, int exp, int s, int num,
+                     const uint8_t* dnum, T* out, cudaStream_t st) {
+    using K = typename KeyOf<T>::type;
+    constexpr int BS = Traits<T>::kBlock;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    const int th = 256;
+    k_nb_decode<T><<<grid_for(nblocks * 32, th, 8), th, 0, st>>>((const typename Traits<T>::S*)base, stride, n,
+                                                                 (const K*)maxkey, exp, s, num, dnum, out);
+    PRODM_CHECK_LAUNCH("k_nb_decode");
+    return PRODM_OK;
+}
+
+uint64_t gr_nchunks(uint64_t nblocks) { return (nblocks + GR_CHUNK - 1) / GR_CHUNK; }
+
+template <class T>
+int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, uint8_t* rbs, uint32_t* chunk_words,
+                     uint32_t* chunk_off, uint32_t* sizes, void* out, uint64_t cap, double* partial, double* errs_out,
+                     cudaStream_t st) {
+    using K = typename KeyOf<T>::type;
+    constexpr int BS = Traits<T>::kBlock;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    const uint64_t nch = gr_nchunks(nblocks);
+    if (errs_out) {
+        k_gr_rb<T, true><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(x, n, (const K*)maxkey, exp, B, rbs, chunk_words,
+                                                                  partial);
+    } else {
+        k_gr_rb<T, false><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(x, n, (const K*)maxkey, exp, B, rbs, chunk_words,
+                                                                   nullptr);
+    }
+    PRODM_CHECK_LAUNCH("k_gr_rb");
+    if (errs_out) {
+        k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
+        PRODM_CHECK_LAUNCH("k_reduce_partials");
+    }
+    k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, (int)sizeof(typename Traits<T>::S), chunk_off, sizes);
+    PRODM_CHECK_LAUNCH("k_gr_scan");
+    k_gr_write<T><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(x, n, (const K*)maxkey, exp, B, rbs, chunk_off,
+                                                           (typename Traits<T>::S*)out, cap);
+    PRODM_CHECK_LAUNCH("k_gr_write");
+    return PRODM_OK;
+}
+
+int launch_chunk_words_from_rb(const uint8_t* rbs, uint64_t nblocks, int B, uint32_t* chunk_words, cudaStream_t st) {
+    const uint64_t nch = gr_nchunks(nblocks);
+    k_chunk_words_from_rb<<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(rbs, nblocks, B, chunk_words);
+    PRODM_CHECK_LAUNCH("k_chunk_words_from_rb");
+    return PRODM_OK;
+}
+
+int launch_gr_scan_only(const uint32_t* chunk_words, uint64_t nchunks, int B, uint64_t nblocks, int word_bytes,
+                        uint32_t* chunk_off, uint32_t* sizes, cudaStream_t st) {
+    k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nchunks, B, nblocks, word_bytes, chunk_off, sizes);
+    PRODM_CHECK_LAUNCH("k_gr_scan");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_gr_decode(const void* const* planes, uint64_t n, const void* maxkey, int exp, int B, int s, int e,
+                     const uint8_t* dnum, const uint8_t* rbs, const uint32_t* chunk_off, void* signs, T* out,
+                     cudaStream_t st) {
+    using K = typename KeyOf<T>::type;
+    using S = typename Traits<T>::S;
+    constexpr int BS = Traits<T>::kBlock;
+    const uint64_t nblocks = (n + BS - 1) / BS;
+    const uint64_t nch = gr_nchunks(nblocks);
+    k_gr_decode<T><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const S* const*)planes, n, (const K*)maxkey, exp, B, s, e,
+                                                            dnum, rbs, chunk_off, (S*)signs, out);
+    PRODM_CHECK_LAUNCH("k_gr_decode");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_sq_collect(const T* x, uint64_t n, int B, T maxv, double* partial, double* out, cudaStream_t st) {
+    const int th = 256;
+    const unsigned grid = (unsigned)kSMs * 4;
+    k_sq_collect<T><<<grid, th, 0, st>>>(x, n, B, maxv, partial);
+    PRODM_CHECK_LAUNCH("k_sq_collect");
+    k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)grid, B, nullptr, 0, 0, 0, out);
+    PRODM_CHECK_LAUNCH("k_reduce_partials");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_max_collect(const T* bounds, int nl, int B, double* out, cudaStream_t st) {
+    k_max_collect<T><<<1, 32, 0, st>>>(bounds, nl, B, out);
+    PRODM_CHECK_LAUNCH("k_max_collect");
+    return PRODM_OK;
+}
+
+#define INST(T)                                                                                                       \
+    template int launch_nb_encode<T>(const T*, uint64_t, const void*, int, int, void*, uint64_t, double*, double*,    \
+                                     cudaStream_t);                                                                   \
+    template int launch_nb_decode<T>(const void*, uint64_t, uint64_t, const void*, int, int, int, const uint8_t*, T*, \
+                                     cudaStream_t);                                                                   \
+    template int launch_gr_encode<T>(const T*, uint64_t, const void*, int, int, uint8_t*, uint32_t*, uint32_t*,       \
+                                     uint32_t*, void*, uint64_t, double*, double*, cudaStream_t);                     \
+    template int launch_gr_decode<T>(const void* const*, uint64_t, const void*, int, int, int, int, const uint8_t*,   \
+                                     const uint8_t*, const uint32_t*, void*, T*, cudaStream_t);                       \
+    template int launch_sq_collect<T>(const T*, uint64_t, int, T, double*, double*, cudaStream_t);                   \
+    template int launch_max_collect<T>(const T*, int, int, double*, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace prodm

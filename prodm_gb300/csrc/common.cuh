@@ -1,0 +1,141 @@
+// Shared device/host helpers for the GB300 MDR kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "../../include/prodm_gb300.h"
+
+namespace prodm {
+
+// ---------------------------------------------------------------------------
+// error reporting (thread-local last error string for prodm_last_error_string)
+// ---------------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_status(cudaError_t e, const char* where);
+
+#define PRODM_CUDA(call)                                              \
+    do {                                                              \
+        cudaError_t _e = (call);                                      \
+        if (_e != cudaSuccess) return ::prodm::cuda_status(_e, #call); \
+    } while (0)
+void count_launch();
+#define PRODM_CHECK_LAUNCH(name)                                          \
+    do {                                                                  \
+        ::prodm::count_launch();                                          \
+        cudaError_t _e = cudaGetLastError();                              \
+        if (_e != cudaSuccess) return ::prodm::cuda_status(_e, name);     \
+    } while (0)
+
+constexpr int kSMs = 152;   // GB300: 2 dies x 76 SMs
+
+inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
+    size_t g = (work + threads - 1) / threads;
+    size_t cap = (size_t)kSMs * per_sm;
+    if (g > cap) g = cap;
+    if (g == 0) g = 1;
+    return (unsigned)g;
+}
+
+// ---------------------------------------------------------------------------
+// Level geometry (3-D with leading unit dims for 1-D and 2-D fields).
+// Every dim shrinks n -> (n >> 1) + 1 per level (RefactorUtils.hpp:21-34).
+// ---------------------------------------------------------------------------
+struct Box {
+    uint32_t n[3];
+    __host__ __device__ uint64_t size() const { return (uint64_t)n[0] * n[1] * n[2]; }
+};
+
+__host__ __device__ inline uint32_t coarse_len(uint32_t n) { return (n >> 1) + 1; }
+
+// coarse nodes: even indices below n-1, plus n-1 itself
+__host__ __device__ inline bool is_coarse(uint32_t x, uint32_t n) { return x == n - 1 || (x & 1u) == 0; }
+__host__ __device__ inline uint32_t reord(uint32_t x, uint32_t n, uint32_t nc) {
+    return is_coarse(x, n) ? (x == n - 1 ? nc - 1 : x >> 1) : nc + (x >> 1);
+}
+__host__ __device__ inline uint32_t fine_of_coarse(uint32_t m, uint32_t n, uint32_t nc) {
+    return m == nc - 1 ? n - 1 : 2 * m;
+}
+
+// Position of reordered coordinate r in the interleaved order of the level
+// box(F) \ box(C) (row-major walk that skips the coarse box,
+// DirectInterleaver.hpp:23-31).
+__host__ __device__ inline uint64_t level_rank(uint32_t r0, uint32_t r1, uint32_t r2, const Box& F, const Box& C) {
+    uint64_t lin = ((uint64_t)r0 * F.n[1] + r1) * F.n[2] + r2;
+    uint64_t pre = (uint64_t)min(r0, C.n[0]) * C.n[1] * C.n[2];
+    if (r0 < C.n[0]) {
+        pre += (uint64_t)min(r1, C.n[1]) * C.n[2];
+        if (r1 < C.n[1]) pre += min(r2, C.n[2]);
+    }
+    return lin - pre;
+}
+
+struct LevelGeom {
+    int ndims;
+    int L;
+    uint32_t dims[3];                  // as given (ndims entries)
+    Box box[17];                       // padded 3-D box of each level (0..L)
+    uint64_t elems[17];                // coefficients per level
+    uint64_t offset[17];               // offset of each level in a packed coefficient array
+    uint64_t total;
+};
+int make_geom(int ndims, const uint32_t* dims, int L, LevelGeom& g);
+int max_level(int ndims, const uint32_t* dims);
+
+// ---------------------------------------------------------------------------
+// numeric helpers (exact operations only)
+// ---------------------------------------------------------------------------
+template <class T> struct Traits;
+template <> struct Traits<float> {
+    using S = uint32_t;    // stream word
+    using FP = uint32_t;   // unsigned fixed point
+    using FPS = int32_t;   // signed fixed point (negabinary source)
+    using Bits = uint32_t;
+    static constexpr int kBlock = 32;
+    static constexpr int kPrec = 23;
+};
+template <> struct Traits<double> {
+    using S = uint64_t;
+    using FP = uint64_t;
+    using FPS = int64_t;
+    using Bits = uint64_t;
+    static constexpr int kBlock = 64;
+    static constexpr int kPrec = 52;
+};
+
+__device__ __forceinline__ uint32_t nb_from_bin(int32_t x) { return ((uint32_t)x + 0xaaaaaaaau) ^ 0xaaaaaaaau; }
+__device__ __forceinline__ uint64_t nb_from_bin(int64_t x) {
+    return ((uint64_t)x + 0xaaaaaaaaaaaaaaaaull) ^ 0xaaaaaaaaaaaaaaaaull;
+}
+__device__ __forceinline__ int32_t nb_to_bin(uint32_t x) { return (int32_t)((x ^ 0xaaaaaaaau) - 0xaaaaaaaau); }
+__device__ __forceinline__ int64_t nb_to_bin(uint64_t x) {
+    return (int64_t)((x ^ 0xaaaaaaaaaaaaaaaaull) - 0xaaaaaaaaaaaaaaaaull);
+}
+
+__device__ __forceinline__ int frexp_exp(float v) { int e; frexpf(v, &e); return e; }
+__device__ __forceinline__ int frexp_exp(double v) { int e; frexp(v, &e); return e; }
+__device__ __forceinline__ float ldexp_t(float v, int e) { return ldexpf(v, e); }
+__device__ __forceinline__ double ldexp_t(double v, int e) { return ldexp(v, e); }
+
+// uncontracted arithmetic (no FMA fusion), so that results match a host
+// evaluation of the same expression tree operation by operation
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+// |x| of a non-negative float/double as an order-preserving unsigned key
+__device__ __forceinline__ uint32_t abs_key(float v) { return __float_as_uint(v) & 0x7fffffffu; }
+__device__ __forceinline__ unsigned long long abs_key(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ float key_to_val(uint32_t k, float) { return __uint_as_float(k); }
+__device__ __forceinline__ double key_to_val(unsigned long long k, double) { return __longlong_as_double((long long)k); }
+template <class T> struct KeyOf { using type = uint32_t; };
+template <> struct KeyOf<double> { using type = unsigned long long; };
+
+}  // namespace prodm

@@ -1,0 +1,80 @@
+// Host-side launchers of the CUDA kernels (declarations).
+#pragma once
+#include "common.cuh"
+
+namespace prodm {
+
+// mgard.cu
+template <class T>
+int launch_decompose_level_packed(const T* in, uint64_t s0, uint64_t s1, const Box& F, const Box& C, T* coef, T* coarse,
+                                  T* fnat, void* maxkey_level, void* maxkey_coarse, cudaStream_t st);
+template <class T>
+int launch_decompose_level_inplace(const T* in, const Box& F, const Box& C, T* out, uint64_t o0, uint64_t o1, T* fnat,
+                                   cudaStream_t st);
+template <class T>
+int launch_recompose_level_packed(const T* coarse, const T* coef, const Box& F, const Box& C, T* out, uint64_t s0,
+                                  uint64_t s1, cudaStream_t st);
+template <class T>
+int launch_recompose_level_inplace(const T* rin, const Box& F, const Box& C, T* out, uint64_t s0, uint64_t s1,
+                                   cudaStream_t st);
+template <class T>
+int launch_copy_box(const T* src, uint64_t a0, uint64_t a1, const Box& B, T* dst, uint64_t b0, uint64_t b1,
+                    cudaStream_t st);
+template <class T>
+int launch_coef_to_natural(const T* coef, const Box& F, const Box& C, T* fnat, cudaStream_t st);
+template <class T>
+int launch_reordered_to_natural(const T* rin, const Box& F, const Box& C, T* fnat, cudaStream_t st);
+template <class W>
+void mass_factors(uint32_t n, W* tab);
+template <class T>
+int launch_l2_correction(const T* fnat, const Box& F, T* t1, T* t2, T* z, const T* const tabs[3], cudaStream_t st);
+template <class T>
+int launch_add_box(T* dst, uint64_t b0, uint64_t b1, const T* z, const Box& B, T sign, cudaStream_t st);
+template <class T>
+int launch_interleave(T* data, uint64_t s0, uint64_t s1, const Box& F, const Box& C, T* buf, bool gather,
+                      cudaStream_t st);
+
+// bitplane.cu
+template <class T>
+int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, void* out, uint64_t stride,
+                     double* partial, double* errs_out, cudaStream_t st);
+template <class T>
+int launch_nb_decode(const void* base, uint64_t stride, uint64_t n, const void* maxkey, int exp, int s, int num,
+                     const uint8_t* dnum, T* out, cudaStream_t st);
+uint64_t gr_nchunks(uint64_t nblocks);
+template <class T>
+int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, uint8_t* rbs, uint32_t* chunk_words,
+                     uint32_t* chunk_off, uint32_t* sizes, void* out, uint64_t cap, double* partial, double* errs_out,
+                     cudaStream_t st);
+template <class T>
+int launch_gr_decode(const void* const* planes, uint64_t n, const void* maxkey, int exp, int B, int s, int e,
+                     const uint8_t* dnum, const uint8_t* rbs, const uint32_t* chunk_off, void* signs, T* out,
+                     cudaStream_t st);
+template <class T>
+int launch_sq_collect(const T* x, uint64_t n, int B, T maxv, double* partial, double* out, cudaStream_t st);
+template <class T>
+int launch_max_collect(const T* bounds, int nl, int B, double* out, cudaStream_t st);
+constexpr int kPartialSlots = kSMs * 4;   // per-CTA partial error tables of the fused collectors
+
+// interpret.cu
+template <class T>
+int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, const int* d_levels, double s, int B,
+                     const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
+                     const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
+                     cudaStream_t st);
+
+// pack.cu
+int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,
+                   int word_bytes, uint8_t* dst, cudaStream_t st);
+int launch_unpack_planes(const uint8_t* src, const uint64_t* src_off, const uint64_t* nwords, int nplanes,
+                         int word_bytes, void* const* dst, uint64_t max_words, cudaStream_t st);
+int launch_chunk_words_from_rb(const uint8_t* rbs, uint64_t nblocks, int B, uint32_t* chunk_words, cudaStream_t st);
+int launch_gr_scan_only(const uint32_t* chunk_words, uint64_t nchunks, int B, uint64_t nblocks, int word_bytes,
+                        uint32_t* chunk_off, uint32_t* sizes, cudaStream_t st);
+template <class T>
+int launch_maxabs(const T* x, uint64_t n, void* maxkey, cudaStream_t st);
+template <class T>
+int launch_bounds_from_keys(const void* keys, int nl, int negabinary, T* bounds, cudaStream_t st);
+int launch_fill_u32(uint32_t* dst, uint64_t n, uint32_t v, cudaStream_t st);
+
+}  // namespace prodm

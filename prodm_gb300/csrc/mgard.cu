@@ -1,0 +1,449 @@
+// MGARD multilevel decomposition / recomposition kernels (sm_103a).
+//
+// One level maps the nodal values on a fine box F to
+//   * coefficients c(x) = u(x) - (multilinear interpolant of the coarse nodal
+//     values)(x) at every non-coarse node, and
+//   * the coarse nodal values (orthogonal basis: plus the L2-projection
+//     correction z = (M_c^-1 P^T M_f)^{(x)3} c, solved per dim with Thomas).
+// Per dim the coarse nodes are the even indices below n-1 plus n-1
+// ((n >> 1) + 1 of them, RefactorUtils.hpp:21-34). The reference obtains this
+// transform from MGARDx (MGARD.hpp:14-66); MGARDx is not part of the reference
+// tree, so the arithmetic here follows the published MGARD method.
+//
+// Two layouts are supported:
+//  * packed   -- level coefficients in interleaved order (the order
+//                DirectInterleaver.hpp:23-31 produces) plus a compact coarse
+//                box; used by the device-resident pipeline, which never
+//                materialises the in-place layout;
+//  * in place -- the reference layout: the level box of a strided array,
+//                reordered per dim so that coarse nodes come first
+//                (DecomposerInterface.hpp:14-16).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace prodm {
+
+namespace {
+
+// Multilinear interpolation at fine node (x0,x1,x2) from its corner values,
+// dims averaged with dim 0 outermost (the oracle uses the same order).
+template <class T, class Get>
+__device__ __forceinline__ T interp(int mask, Get at) {
+    const T h = (T)0.5;
+    auto avg = [&](T a, T b) { return mul_rn(h, add_rn(a, b)); };
+    switch (mask) {
+        case 1: return avg(at(-1, 0, 0), at(1, 0, 0));
+        case 2: return avg(at(0, -1, 0), at(0, 1, 0));
+        case 4: return avg(at(0, 0, -1), at(0, 0, 1));
+        case 3: return avg(avg(at(-1, -1, 0), at(-1, 1, 0)), avg(at(1, -1, 0), at(1, 1, 0)));
+        case 5: return avg(avg(at(-1, 0, -1), at(-1, 0, 1)), avg(at(1, 0, -1), at(1, 0, 1)));
+        case 6: return avg(avg(at(0, -1, -1), at(0, -1, 1)), avg(at(0, 1, -1), at(0, 1, 1)));
+        case 7: {
+            T a = avg(avg(at(-1, -1, -1), at(-1, -1, 1)), avg(at(-1, 1, -1), at(-1, 1, 1)));
+            T b = avg(avg(at(1, -1, -1), at(1, -1, 1)), avg(at(1, 1, -1), at(1, 1, 1)));
+            return avg(a, b);
+        }
+        default: return (T)0;
+    }
+}
+
+template <class K>
+__device__ __forceinline__ K warp_max(K v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        K w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// forward level: in = natural-order fine box (strides s0, s1, 1)
+// PACKED:  coef[rank] and coarse[compact C box]
+// INPLACE: out[reordered position] with strides o0, o1, 1 (coef and coarse)
+// fnat (optional): natural-order coefficient field, zero at coarse nodes
+// ---------------------------------------------------------------------------
+template <class T, bool PACKED>
+__global__ void k_decompose_level(const T* __restrict__ in, uint64_t s0, uint64_t s1, Box F, Box C,
+                                  T* __restrict__ coef, T* __restrict__ coarse, uint64_t o0, uint64_t o1,
+                                  T* __restrict__ fnat, typename KeyOf<T>::type* maxkey_level,
+                                  typename KeyOf<T>::type* maxkey_coarse) {
+    using K = typename KeyOf<T>::type;
+    K mk = 0, mc = 0;
+    const uint64_t total = F.size();
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % F.n[2]);
+        uint64_t t = idx / F.n[2];
+        uint32_t x1 = (uint32_t)(t % F.n[1]);
+        uint32_t x0 = (uint32_t)(t / F.n[1]);
+        const T* p = in + x0 * s0 + x1 * s1 + x2;
+        T v = *p;
+        int mask = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2) | (is_coarse(x2, F.n[2]) ? 0 : 4);
+        uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]), r2 = reord(x2, F.n[2], C.n[2]);
+        if (mask == 0) {
+            if (PACKED) coarse[((uint64_t)r0 * C.n[1] + r1) * C.n[2] + r2] = v;
+            else coef[r0 * o0 + r1 * o1 + r2] = v;
+            if (fnat) fnat[idx] = (T)0;
+            K k = abs_key(v);
+            mc = k > mc ? k : mc;
+        } else {
+            auto at = [&](int d0, int d1, int d2) -> T { return __ldg(p + (int64_t)d0 * (int64_t)s0 + (int64_t)d1 * (int64_t)s1 + d2); };
+            T c = sub_rn(v, interp<T>(mask, at));
+            if (PACKED) coef[level_rank(r0, r1, r2, F, C)] = c;
+            else coef[r0 * o0 + r1 * o1 + r2] = c;
+            if (fnat) fnat[idx] = c;
+            K k = abs_key(c);
+            mk = k > mk ? k : mk;
+        }
+    }
+    if (maxkey_level) {
+        mk = warp_max(mk);
+        if ((threadIdx.x & 31) == 0 && mk) atomicMax(maxkey_level, mk);
+    }
+    if (maxkey_coarse) {
+        mc = warp_max(mc);
+        if ((threadIdx.x & 31) == 0 && mc) atomicMax(maxkey_coarse, mc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// inverse level: coarse values (already corrected back to nodal values for
+// the orthogonal basis) + coefficients -> natural-order fine box.
+// PACKED:  coarse = compact C box, coef = packed level coefficients
+// INPLACE: both read from a compact reordered copy of the level box (rin)
+// ---------------------------------------------------------------------------
+template <class T, bool PACKED>
+__global__ void k_recompose_level(const T* __restrict__ coarse, const T* __restrict__ coef, Box F, Box C,
+                                  T* __restrict__ out, uint64_t s0, uint64_t s1) {
+    const uint64_t total = F.size();
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % F.n[2]);
+        uint64_t t = idx / F.n[2];
+        uint32_t x1 = (uint32_t)(t % F.n[1]);
+        uint32_t x0 = (uint32_t)(t / F.n[1]);
+        int mask = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2) | (is_coarse(x2, F.n[2]) ? 0 : 4);
+        // coarse-index coordinates of the "low" corner
+        uint32_t c0 = (mask & 1) ? (x0 >> 1) : reord(x0, F.n[0], C.n[0]);
+        uint32_t c1 = (mask & 2) ? (x1 >> 1) : reord(x1, F.n[1], C.n[1]);
+        uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, F.n[2], C.n[2]);
+        T v;
+        if (PACKED) {
+            const T* cb = coarse + ((uint64_t)c0 * C.n[1] + c1) * C.n[2] + c2;
+            const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
+            if (mask == 0) {
+                v = *cb;
+            } else {
+                // corner offsets: -1 -> low corner (0), +1 -> next coarse node (1)
+                auto at = [&](int d0, int d1, int d2) -> T {
+                    return __ldg(cb + (d0 > 0 ? cs0 : 0) + (d1 > 0 ? cs1 : 0) + (d2 > 0 ? 1 : 0));
+                };
+                uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]), r2 = reord(x2, F.n[2], C.n[2]);
+                v = add_rn(coef[level_rank(r0, r1, r2, F, C)], interp<T>(mask, at));
+            }
+        } else {
+            // rin: compact reordered fine box; coarse region = [0,C)
+            const uint64_t fs0 = (uint64_t)F.n[1] * F.n[2], fs1 = F.n[2];
+            const T* cb = coarse + c0 * fs0 + c1 * fs1 + c2;
+            if (mask == 0) {
+                v = *cb;
+            } else {
+                auto at = [&](int d0, int d1, int d2) -> T {
+                    return __ldg(cb + (d0 > 0 ? fs0 : 0) + (d1 > 0 ? fs1 : 0) + (d2 > 0 ? 1 : 0));
+                };
+                uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]), r2 = reord(x2, F.n[2], C.n[2]);
+                v = add_rn(coef[r0 * fs0 + r1 * fs1 + r2], interp<T>(mask, at));
+            }
+        }
+        out[x0 * s0 + x1 * s1 + x2] = v;
+    }
+}
+
+// copy a box between strided arrays
+template <class T>
+__global__ void k_copy_box(const T* __restrict__ src, uint64_t a0, uint64_t a1, Box B, T* __restrict__ dst, uint64_t b0,
+                           uint64_t b1) {
+    const uint64_t total = B.size();
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % B.n[2]);
+        uint64_t t = idx / B.n[2];
+        uint32_t x1 = (uint32_t)(t % B.n[1]);
+        uint32_t x0 = (uint32_t)(t / B.n[1]);
+        dst[x0 * b0 + x1 * b1 + x2] = src[x0 * a0 + x1 * a1 + x2];
+    }
+}
+
+// packed coefficients -> natural-order fine field, zeros at coarse nodes
+template <class T>
+__global__ void k_coef_to_natural(const T* __restrict__ coef, Box F, Box C, T* __restrict__ fnat) {
+    const uint64_t total = F.size();
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % F.n[2]);
+        uint64_t t = idx / F.n[2];
+        uint32_t x1 = (uint32_t)(t % F.n[1]);
+        uint32_t x0 = (uint32_t)(t / F.n[1]);
+        bool c = is_coarse(x0, F.n[0]) && is_coarse(x1, F.n[1]) && is_coarse(x2, F.n[2]);
+        T v = (T)0;
+        if (!c) {
+            uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]), r2 = reord(x2, F.n[2], C.n[2]);
+            v = coef[level_rank(r0, r1, r2, F, C)];
+        }
+        fnat[idx] = v;
+    }
+}
+
+// in-place reordered level box (compact copy) -> natural coefficient field
+template <class T>
+__global__ void k_reordered_to_natural(const T* __restrict__ rin, Box F, Box C, T* __restrict__ fnat) {
+    const uint64_t total = F.size();
+    const uint64_t fs0 = (uint64_t)F.n[1] * F.n[2], fs1 = F.n[2];
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % F.n[2]);
+        uint64_t t = idx / F.n[2];
+        uint32_t x1 = (uint32_t)(t % F.n[1]);
+        uint32_t x0 = (uint32_t)(t / F.n[1]);
+        bool c = is_coarse(x0, F.n[0]) && is_coarse(x1, F.n[1]) && is_coarse(x2, F.n[2]);
+        T v = (T)0;
+        if (!c) {
+            uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]), r2 = reord(x2, F.n[2], C.n[2]);
+            v = rin[r0 * fs0 + r1 * fs1 + r2];
+        }
+        fnat[idx] = v;
+    }
+}
+
+// One dim of the L2 projection: dst = M_c^-1 P^T M_f src along dim d.
+// Thread per line; forward sweep stores d'_m in dst, backward sweep in place.
+// cp / inv_den: Thomas factors of the coarse mass matrix (length nc, in W).
+template <class T, class W>
+__global__ void k_l2_line(const T* __restrict__ src, Box S, int d, T* __restrict__ dst, Box D, const W* __restrict__ cp,
+                          const W* __restrict__ lo_w, const W* __restrict__ inv_den) {
+    const uint32_t nf = S.n[d], nc = D.n[d];
+    const int o1 = d == 0 ? 1 : 0, o2 = d == 2 ? 1 : 2;
+    const uint64_t ss[3] = {(uint64_t)S.n[1] * S.n[2], S.n[2], 1};
+    const uint64_t ds[3] = {(uint64_t)D.n[1] * D.n[2], D.n[2], 1};
+    const uint64_t lines = (uint64_t)S.n[o1] * S.n[o2];
+    for (uint64_t li = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; li < lines;
+         li += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t q = (uint32_t)(li % S.n[o2]);
+        uint32_t p = (uint32_t)(li / S.n[o2]);
+        const T* sl = src + p * ss[o1] + q * ss[o2];
+        T* dl = dst + p * ds[o1] + q * ds[o2];
+        const uint64_t st = ss[d], dt = ds[d];
+        if (nf == nc) {
+            for (uint32_t x = 0; x < nf; x++) dl[x * dt] = sl[x * st];
+            continue;
+        }
+        auto mf = [&](uint32_t x) -> W {   // (M_f line)[x], spacing 1
+            W c = (W)sl[x * st];
+            W l = x > 0 ? (W)sl[(x - 1) * st] : (W)0;
+            W r = x + 1 < nf ? (W)sl[(x + 1) * st] : (W)0;
+            W dg = (x == 0 || x == nf - 1) ? (W)1 / 3 : (W)2 / 3;
+            return dg * c + (l + r) / 6;
+        };
+        W prev = 0;
+        for (uint32_t m = 0; m < nc; m++) {
+            uint32_t c = fine_of_coarse(m, nf, nc);
+            W b = mf(c);
+            if (c > 0 && !is_coarse(c - 1, nf)) b += (W)0.5 * mf(c - 1);
+            if (c + 1 < nf && !is_coarse(c + 1, nf)) b += (W)0.5 * mf(c + 1);
+            W dp = (m == 0) ? b * inv_den[0] : (b - lo_w[m] * prev) * inv_den[m];
+            dl[m * dt] = (T)dp;
+            prev = dp;
+        }
+        W z = (W)dl[(nc - 1) * dt];
+        for (uint32_t m = nc - 1; m-- > 0;) {
+            z = (W)dl[m * dt] - cp[m] * z;
+            dl[m * dt] = (T)z;
+        }
+    }
+}
+
+// dst[i] += sign * z[i] over a compact box written into a strided box
+template <class T>
+__global__ void k_add_box(T* __restrict__ dst, uint64_t b0, uint64_t b1, const T* __restrict__ z, Box B, T sign) {
+    const uint64_t total = B.size();
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % B.n[2]);
+        uint64_t t = idx / B.n[2];
+        uint32_t x1 = (uint32_t)(t % B.n[1]);
+        uint32_t x0 = (uint32_t)(t / B.n[1]);
+        dst[x0 * b0 + x1 * b1 + x2] += sign * z[idx];
+    }
+}
+
+// DirectInterleaver gather/scatter over box(fine) \ box(coarse).
+template <class T, bool GATHER>
+__global__ void k_interleave(T* __restrict__ data, uint64_t s0, uint64_t s1, Box F, Box C, T* __restrict__ buf) {
+    const uint64_t total = F.size();
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x2 = (uint32_t)(idx % F.n[2]);
+        uint64_t t = idx / F.n[2];
+        uint32_t x1 = (uint32_t)(t % F.n[1]);
+        uint32_t x0 = (uint32_t)(t / F.n[1]);
+        if (x0 < C.n[0] && x1 < C.n[1] && x2 < C.n[2]) continue;
+        uint64_t r = level_rank(x0, x1, x2, F, C);
+        if (GATHER) buf[r] = data[x0 * s0 + x1 * s1 + x2];
+        else data[x0 * s0 + x1 * s1 + x2] = buf[r];
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+template <class T>
+int launch_decompose_level_packed(const T* in, uint64_t s0, uint64_t s1, const Box& F, const Box& C, T* coef, T* coarse,
+                                  T* fnat, void* maxkey_level, void* maxkey_coarse, cudaStream_t st) {
+    using K = typename KeyOf<T>::type;
+    const int th = 256;
+    k_decompose_level<T, true><<<grid_for(F.size(), th), th, 0, st>>>(in, s0, s1, F, C, coef, coarse, 0, 0, fnat,
+                                                                      (K*)maxkey_level, (K*)maxkey_coarse);
+    PRODM_CHECK_LAUNCH("k_decompose_level");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_decompose_level_inplace(const T* in, const Box& F, const Box& C, T* out, uint64_t o0, uint64_t o1, T* fnat,
+                                   cudaStream_t st) {
+    const int th = 256;
+    k_decompose_level<T, false><<<grid_for(F.size(), th), th, 0, st>>>(
+        in, (uint64_t)F.n[1] * F.n[2], F.n[2], F, C, out, nullptr, o0, o1, fnat, nullptr, nullptr);
+    PRODM_CHECK_LAUNCH("k_decompose_level");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_recompose_level_packed(const T* coarse, const T* coef, const Box& F, const Box& C, T* out, uint64_t s0,
+                                  uint64_t s1, cudaStream_t st) {
+    const int th = 256;
+    k_recompose_level<T, true><<<grid_for(F.size(), th), th, 0, st>>>(coarse, coef, F, C, out, s0, s1);
+    PRODM_CHECK_LAUNCH("k_recompose_level");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_recompose_level_inplace(const T* rin, const Box& F, const Box& C, T* out, uint64_t s0, uint64_t s1,
+                                   cudaStream_t st) {
+    const int th = 256;
+    k_recompose_level<T, false><<<grid_for(F.size(), th), th, 0, st>>>(rin, rin, F, C, out, s0, s1);
+    PRODM_CHECK_LAUNCH("k_recompose_level");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_copy_box(const T* src, uint64_t a0, uint64_t a1, const Box& B, T* dst, uint64_t b0, uint64_t b1,
+                    cudaStream_t st) {
+    const int th = 256;
+    k_copy_box<T><<<grid_for(B.size(), th), th, 0, st>>>(src, a0, a1, B, dst, b0, b1);
+    PRODM_CHECK_LAUNCH("k_copy_box");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_coef_to_natural(const T* coef, const Box& F, const Box& C, T* fnat, cudaStream_t st) {
+    const int th = 256;
+    k_coef_to_natural<T><<<grid_for(F.size(), th), th, 0, st>>>(coef, F, C, fnat);
+    PRODM_CHECK_LAUNCH("k_coef_to_natural");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_reordered_to_natural(const T* rin, const Box& F, const Box& C, T* fnat, cudaStream_t st) {
+    const int th = 256;
+    k_reordered_to_natural<T><<<grid_for(F.size(), th), th, 0, st>>>(rin, F, C, fnat);
+    PRODM_CHECK_LAUNCH("k_reordered_to_natural");
+    return PRODM_OK;
+}
+
+// Thomas factors of the coarse mass matrix of a dim with n fine nodes.
+// layout in tab: [cp(nc) | lo(nc) | inv_den(nc)]
+template <class W>
+void mass_factors(uint32_t n, W* tab) {
+    uint32_t nc = coarse_len(n);
+    W* cp = tab;
+    W* lo = tab + nc;
+    W* inv = tab + 2 * nc;
+    double prev_cp = 0;
+    for (uint32_t m = 0; m < nc; m++) {
+        double hl = m > 0 ? (double)(fine_of_coarse(m, n, nc) - fine_of_coarse(m - 1, n, nc)) : 0.0;
+        double hr = m + 1 < nc ? (double)(fine_of_coarse(m + 1, n, nc) - fine_of_coarse(m, n, nc)) : 0.0;
+        double dg = (hl + hr) / 3, up = hr / 6, low = hl / 6;
+        double den = m == 0 ? dg : dg - low * prev_cp;
+        double c = up / den;
+        cp[m] = (W)c;
+        lo[m] = (W)low;
+        inv[m] = (W)(1.0 / den);
+        prev_cp = c;
+    }
+}
+template void mass_factors<float>(uint32_t, float*);
+template void mass_factors<double>(uint32_t, double*);
+
+// z (compact C box) = L2 projection of the natural coefficient field fnat (F box).
+// tabs[d] = device Thomas factors for dim d; t1/t2 scratch boxes.
+template <class T>
+int launch_l2_correction(const T* fnat, const Box& F, T* t1, T* t2, T* z, const T* const tabs[3], cudaStream_t st) {
+    const int th = 128;
+    Box a = F;
+    const T* src = fnat;
+    T* bufs[3] = {t1, t2, z};
+    for (int k = 0, d = 2; d >= 0; d--, k++) {
+        Box b = a;
+        b.n[d] = coarse_len(a.n[d]);
+        uint64_t lines = a.size() / a.n[d];
+        uint32_t nc = b.n[d];
+        const T* tab = tabs[d];
+        k_l2_line<T, T><<<grid_for(lines, th, 16), th, 0, st>>>(src, a, d, bufs[k], b, tab, tab + nc, tab + 2 * nc);
+        PRODM_CHECK_LAUNCH("k_l2_line");
+        src = bufs[k];
+        a = b;
+    }
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_add_box(T* dst, uint64_t b0, uint64_t b1, const T* z, const Box& B, T sign, cudaStream_t st) {
+    const int th = 256;
+    k_add_box<T><<<grid_for(B.size(), th), th, 0, st>>>(dst, b0, b1, z, B, sign);
+    PRODM_CHECK_LAUNCH("k_add_box");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_interleave(T* data, uint64_t s0, uint64_t s1, const Box& F, const Box& C, T* buf, bool gather,
+                      cudaStream_t st) {
+    const int th = 256;
+    if (gather) k_interleave<T, true><<<grid_for(F.size(), th), th, 0, st>>>(data, s0, s1, F, C, buf);
+    else k_interleave<T, false><<<grid_for(F.size(), th), th, 0, st>>>(data, s0, s1, F, C, buf);
+    PRODM_CHECK_LAUNCH("k_interleave");
+    return PRODM_OK;
+}
+
+#define INST(T)                                                                                                     \
+    template int launch_decompose_level_packed<T>(const T*, uint64_t, uint64_t, const Box&, const Box&, T*, T*, T*, \
+                                                  void*, void*, cudaStream_t);                                      \
+    template int launch_decompose_level_inplace<T>(const T*, const Box&, const Box&, T*, uint64_t, uint64_t, T*,    \
+                                                   cudaStream_t);                                                   \
+    template int launch_recompose_level_packed<T>(const T*, const T*, const Box&, const Box&, T*, uint64_t,         \
+                                                  uint64_t, cudaStream_t);                                          \
+    template int launch_recompose_level_inplace<T>(const T*, const Box&, const Box&, T*, uint64_t, uint64_t,        \
+                                                   cudaStream_t);                                                   \
+    template int launch_copy_box<T>(const T*, uint64_t, uint64_t, const Box&, T*, uint64_t, uint64_t, cudaStream_t); \
+    template int launch_coef_to_natural<T>(const T*, const Box&, const Box&, T*, cudaStream_t);                     \
+    template int launch_reordered_to_natural<T>(const T*, const Box&, const Box&, T*, cudaStream_t);                \
+    template int launch_l2_correction<T>(const T*, const Box&, T*, T*, T*, const T* const[3], cudaStream_t);        \
+    template int launch_add_box<T>(T*, uint64_t, uint64_t, const T*, const Box&, T, cudaStream_t);                  \
+    template int launch_interleave<T>(T*, uint64_t, uint64_t, const Box&, const Box&, T*, bool, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace prodm

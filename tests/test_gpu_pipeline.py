@@ -1,0 +1,177 @@
+"""Device-resident refactor / retrieve (MDRField) against the oracle.
+
+* coefficients: within 1e-6 (fp32) / 1e-13 (fp64) of max|x| against the FP64
+  oracle decomposition, in the interleaved level order;
+* streams: the exported level files are bit-exact with the oracle encoder fed
+  the GPU's own coefficients (the oracle encoder is pinned to the reference);
+* retrieval: the same plane counts as the oracle interpreter on the same
+  tables, reconstruction within float rounding of the oracle's, and the
+  achieved error within the requested bound.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+O = oracle.oracle()
+
+
+def api():
+    from prodm_gb300 import api as a
+    return a
+
+
+def fields():
+    from prodm_gb300 import fields as f
+    return f
+
+
+def oracle_levels(coef_nat, shape, L):
+    """level buffers from an in-place decomposed array (oracle interleaver)."""
+    ld = O.level_dims(shape, L)
+    out = []
+    for l in range(L + 1):
+        coarse = ld[l - 1] if l else np.zeros(len(shape), np.uint32)
+        out.append(O.interleave(coef_nat, shape, ld[l], coarse))
+    return out
+
+
+CASES = [
+    ((33, 33, 33), 3, "grouped", "hierarchical", np.float32),
+    ((65, 65, 65), 3, "negabinary", "hierarchical", np.float32),
+    ((65, 65, 65), 3, "grouped", "orthogonal", np.float32),
+    ((40, 33, 21), 2, "negabinary", "orthogonal", np.float32),
+    ((129, 65), 5, "grouped", "hierarchical", np.float32),
+    ((1000,), 6, "negabinary", "hierarchical", np.float32),
+    ((33, 33, 33), 3, "grouped", "orthogonal", np.float64),
+    ((17, 9, 33), 2, "negabinary", "hierarchical", np.float64),
+    ((9, 9, 9), 2, "negabinary", "hierarchical", np.float32),     # level 0 = 27 values < one block
+    ((16, 16, 16), 0, "grouped", "hierarchical", np.float32),     # no decomposition
+]
+
+
+@pytest.mark.parametrize("shape,L,enc,basis,dt", CASES)
+def test_refactor_matches_oracle(shape, L, enc, basis, dt):
+    B = 32 if dt == np.float32 else 60
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    x = fields().sinusoids(shape, seed=len(shape) + L, dtype=tdt).cpu().numpy()
+    mdr = api().MDRField(shape, tdt, L, B, enc, basis, "squared")
+    mdr.refactor(torch.from_numpy(x).cuda())
+    coef = mdr.coefficients().cpu().numpy()
+    ref_nat = O.decompose(x.astype(np.float64), shape, L, basis == "hierarchical")
+    ref_levels = oracle_levels(ref_nat, shape, L)
+    offs = np.concatenate([[0], np.cumsum(mdr.level_elements.astype(np.int64))])
+    tol = (1e-6 if dt == np.float32 else 1e-13) * float(np.abs(x).max())
+    sizes, bounds, errs = mdr.level_info()
+    for l in range(L + 1):
+        got = coef[offs[l]:offs[l + 1]]
+        assert np.max(np.abs(got.astype(np.float64) - ref_levels[l])) <= tol, l
+        # the streams of the GPU coefficients are what the oracle encoder makes of them
+        mx = O.max_abs(got)
+        assert bounds[l] == (float(mx) * 4 if enc == "negabinary" else float(mx))
+        e = math.frexp(float(mx))[1]
+        ob, osz, oerr = O.encode(enc, got, e, B, dt == np.float32)
+        assert np.array_equal(sizes[l], osz)
+        assert np.array_equal(mdr.export_level(l), ob), l
+        if dt == np.float32:
+            np.testing.assert_allclose(errs[l], oerr, rtol=1e-4, atol=1e-30)
+
+
+@pytest.mark.parametrize("enc", ["grouped", "negabinary"])
+@pytest.mark.parametrize("basis", ["hierarchical", "orthogonal"])
+def test_progressive_retrieve_linf(enc, basis):
+    shape, L, B = (65, 65, 65), 3, 32
+    x = fields().sinusoids(shape, seed=11).cpu().numpy()
+    mdr = api().MDRField(shape, torch.float32, L, B, enc, basis, "max")
+    mdr.refactor(torch.from_numpy(x).cuda())
+    sizes, bounds, _ = mdr.level_info()
+    blob = np.concatenate([mdr.export_level(l) for l in range(L + 1)])
+    vr = float(x.max() - x.min())
+    est = "max_hb" if basis == "hierarchical" else "max_ob"
+    idx_o = np.zeros(L + 1, np.uint8)
+    for rel in (1e-1, 1e-2, 1e-3, 1e-4, 1e-5):
+        tol = rel * vr
+        out = mdr.retrieve(tol, interpreter="sign_exclude", estimator=est).cpu().numpy()
+        idx = mdr.index()
+        errs = np.stack([O.max_collect(np.float32(b), B, np.float32) for b in bounds])
+        idx_o, _ = O.interpret("sign_exclude", est, sizes, errs, tol, idx_o, ndims=3)
+        assert np.array_equal(idx, idx_o)
+        rec_o = O.retrieve(shape, L, B, blob, sizes, bounds.astype(np.float32), idx, enc, basis == "hierarchical")
+        np.testing.assert_allclose(out, rec_o, rtol=0, atol=2e-6 * float(np.abs(x).max()))
+        assert float(np.abs(out - x).max()) <= tol
+
+
+def test_l2_retrieve_meets_bound_and_matches_interpreter():
+    shape, L, B = (65, 65, 65), 3, 32
+    x = fields().spectral_grf(shape, seed=5).cpu().numpy()
+    mdr = api().MDRField(shape, torch.float32, L, B, "negabinary", "hierarchical", "squared")
+    mdr.refactor(torch.from_numpy(x).cuda())
+    sizes, bounds, errs = mdr.level_info()
+    norm2 = float(np.sum(x.astype(np.float64) ** 2))
+    idx_o = np.zeros(L + 1, np.uint8)
+    for rel in (1e-2, 1e-3, 1e-4, 1e-5, 1e-6):
+        tol = (rel ** 2) * norm2
+        out = mdr.retrieve(tol, interpreter="negabinary", estimator="l2_hb").cpu().numpy()
+        idx = mdr.index()
+        idx_o, _ = O.interpret("negabinary", "l2_hb", sizes, errs, tol, idx_o, ndims=3)
+        assert np.array_equal(idx, idx_o)
+        achieved = float(np.sum((out.astype(np.float64) - x) ** 2))
+        assert achieved <= tol, (rel, achieved, tol)
+
+
+def test_all_planes_roundtrip_and_reset():
+    shape, L, B = (129, 129, 129), 5, 32
+    x = fields().spectral_grf(shape, seed=2)
+    mdr = api().MDRField(shape, torch.float32, L, B, "negabinary", "hierarchical", "max")
+    mdr.refactor(x)
+    out = mdr.retrieve_planes([B] * (L + 1))
+    sizes, bounds, _ = mdr.level_info()
+    # all planes: error = quantisation only, bounded by the sum of level quanta
+    quanta = sum(math.ldexp(1.0, math.frexp(b / 4)[1] + 2 - B) for b in bounds)
+    assert float((out - x).abs().max()) <= quanta
+    mdr.reset()
+    assert not mdr.index().any()
+    z = mdr.retrieve_planes([0] * (L + 1))
+    assert float(z.abs().max()) == 0.0
+
+
+def test_constant_and_zero_fields():
+    for val in (0.0, 3.5):
+        shape = (33, 33, 33)
+        x = torch.full(shape, val, dtype=torch.float32, device="cuda")
+        mdr = api().MDRField(shape, torch.float32, 3, 32, "grouped", "hierarchical", "max")
+        mdr.refactor(x)
+        out = mdr.retrieve(1e-6)
+        assert float((out - x).abs().max()) <= 1e-6
+
+
+def test_invalid_requests_raise():
+    from prodm_gb300._lib import ProdmError
+    with pytest.raises(ProdmError):
+        api().MDRField((65, 65, 65), torch.float32, 6, 32)      # above max level 5
+    with pytest.raises(ProdmError):
+        api().MDRField((65, 65, 65), torch.float32, 3, 33)      # > 32 planes for fp32
+    with pytest.raises(ProdmError):
+        api().MDRField((65, 65, 65), torch.float64, 3, 64, "grouped")
+
+
+def test_metadata_layout_matches_reference_format():
+    g = np.load(__import__("golden_io").GOLDEN + "/composed.npz")
+    field = g["field"]
+    for enc in ("grouped", "negabinary"):
+        mdr = api().MDRField(field.shape, torch.float32, 3, 32, enc, "hierarchical", "max")
+        mdr.refactor(torch.from_numpy(field).cuda())
+        meta = mdr.metadata()
+        ref = g[enc + "_metadata"].tobytes()
+        # the reference layout is a prefix; an extension carries the squared-error tables
+        assert len(meta) > len(ref)
+        hdr = 1 + 4 * 3 + 1
+        assert meta[:hdr] == ref[:hdr]
+        # sizes / stopping indices / level_num / negabinary flag sections
+        nl, B = 4, 32
+        tail = nl * (4 + 4 * B) + nl + 4 * nl + 1
+        assert meta[hdr + 4 * nl:hdr + 4 * nl + tail] == ref[hdr + 4 * nl:hdr + 4 * nl + tail]
