@@ -399,10 +399,13 @@ int progressive_decode_impl(prodm_decoder* h, const uint8_t* blob, const uint32_
         o += hs[i];
     }
     uint8_t* tmp;
-    size_t tbytes = (uint64_t)num * (maxw + 1) * sizeof(T) + 2 * num * 8 + B * sizeof(void*) + 256;
+    // staged planes first, then the (8-byte) offset / count / pointer arrays on a
+    // 256-byte boundary
+    const uint64_t plane_bytes = ((uint64_t)num * (maxw + 1) * sizeof(T) + 255) & ~(uint64_t)255;
+    size_t tbytes = plane_bytes + 2 * num * 8 + B * sizeof(void*) + 256;
     PRODM_CUDA(cudaMallocAsync((void**)&tmp, tbytes, st));
     uint8_t* planes = tmp;
-    uint64_t* doff = (uint64_t*)(tmp + (uint64_t)num * (maxw + 1) * sizeof(T));
+    uint64_t* doff = (uint64_t*)(tmp + plane_bytes);
     uint64_t* dnw = doff + num;
     void** dptr = (void**)(dnw + num);
     std::vector<void*> ptr(B, nullptr), uptr(num);
