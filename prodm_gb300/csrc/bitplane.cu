@@ -11,6 +11,9 @@
 // words: each lane holds elements lane and lane + 32) values; __ballot_sync
 // transposes one bitplane of the block into one stream word; lane p then
 // owns the word of plane p (and p + 32 for fp64).
+#include <algorithm>
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -107,6 +110,184 @@ __device__ __forceinline__ void gr_errors(double (&acc)[NACC], double a, int B) 
 
 template <class T> struct Acc { using type = float; static constexpr int N = 33; };
 template <> struct Acc<double> { using type = double; static constexpr int N = 65; };
+
+// ---------------------------------------------------------------------------
+// 32 x 32 bit transpose across a warp: lane e holds row e on entry; on exit
+// lane k holds the word whose bit e is bit k of row e (five butterfly stages).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
+                                                                                                       : 0x55555555u;
+        const uint32_t y = __shfl_xor_sync(FULL, x, j);
+        const bool hi = (lane & j) != 0;
+        const uint32_t u = hi ? y : x, v = hi ? x : y;
+        const uint32_t t = ((u >> j) ^ v) & m;
+        x ^= hi ? t : (t << j);
+    }
+    return x;
+}
+
+// (-2)^i as a float (exact)
+__device__ __forceinline__ constexpr float nbw(int i) { return (i & 1) ? -(float)(1u << i) : (float)(1u << i); }
+
+// per-lane squared-error accumulators of the negabinary table, indexed by
+// the number k of dropped low digits: acc[0] = m^2 (all planes kept),
+// acc[k] = (value of digits 0..k-1 + m)^2, accx = shifted^2 (no plane kept)
+struct NbErr32 {
+    float acc[32];
+    float accx;
+    __device__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 32; k++) acc[k] = 0.f;
+        accx = 0.f;
+    }
+    __device__ __forceinline__ void add(uint32_t nb, float shifted, float m, int B) {
+        float d = m;
+        acc[0] += m * m;
+#pragma unroll
+        for (int k = 1; k < 32; k++) {
+            if (k < B) {
+                if ((nb >> (k - 1)) & 1u) d += nbw(k - 1);
+                acc[k] += d * d;
+            }
+        }
+        accx += shifted * shifted;
+    }
+    // table entry B-k <- acc[k]; entry B <- acc[0]; entry 0 <- accx
+    __device__ void flush(int B, double* partial) {
+        __shared__ double red[33];
+        for (int k = threadIdx.x; k < 33; k += blockDim.x) red[k] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 33; k++) {
+            float v = k < 32 ? acc[k] : accx;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if ((threadIdx.x & 31) == 0) {
+                int idx = k == 32 ? 0 : B - k;
+                if (k == 32 || k < B) atomicAdd(&red[idx], (double)v);
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k <= B; k += blockDim.x) partial[(size_t)blockIdx.x * (B + 1) + k] = red[k];
+    }
+};
+
+// grouped table (GroupedBPEncoder.hpp:324-335) on a = |shifted|: fp = (u32)a,
+// m = a - fp; acc[0] = m^2, acc[k] = ((fp & (2^k-1)) + m)^2, accx = a^2
+struct GrErr32 {
+    float acc[32];
+    float accx;
+    __device__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 32; k++) acc[k] = 0.f;
+        accx = 0.f;
+    }
+    __device__ __forceinline__ void add(float a, int B) {
+        const uint32_t fp = (uint32_t)a;
+        const float m = a - (float)fp;
+        float d = m;
+        acc[0] += m * m;
+#pragma unroll
+        for (int k = 1; k < 32; k++) {
+            if (k < B) {
+                if ((fp >> (k - 1)) & 1u) d += (float)(1u << (k - 1));
+                acc[k] += d * d;
+            }
+        }
+        accx += a * a;
+    }
+    __device__ void flush(int B, double* partial) {
+        __shared__ double red[33];
+        for (int k = threadIdx.x; k < 33; k += blockDim.x) red[k] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 33; k++) {
+            float v = k < 32 ? acc[k] : accx;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if ((threadIdx.x & 31) == 0) {
+                int idx = k == 32 ? 0 : B - k;
+                if (k == 32 || k < B) atomicAdd(&red[idx], (double)v);
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k <= B; k += blockDim.x) partial[(size_t)blockIdx.x * (B + 1) + k] = red[k];
+    }
+};
+
+constexpr int NB_G = 8;   // blocks per warp iteration (one 32-byte sector per plane)
+
+// fp32 negabinary encoder: transpose-based, NB_G consecutive blocks per warp
+template <bool ERR>
+__global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x, uint64_t n,
+                                                    const uint32_t* __restrict__ maxkey, int exp_arg, int B,
+                                                    uint32_t* __restrict__ out, uint64_t stride,
+                                                    double* __restrict__ partial) {
+    const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;   // NegaBinaryBPEncoder.hpp:21
+    const int lane = threadIdx.x & 31;
+    const uint64_t nblocks = (n + 31) / 32;
+    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    NbErr32 er;
+    if (ERR) er.zero();
+    const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
+    for (uint64_t b0 = gw * NB_G; b0 < nblocks; b0 += nw * NB_G) {
+        float v[NB_G];
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) {
+            const uint64_t i = (b0 + g) * 32 + lane;
+            v[g] = i < n ? __ldcs(x + i) : 0.f;
+        }
+        uint32_t w[NB_G];
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) {
+            const float sh = ldexpf(v[g], B - exp);         // :42
+            const int32_t q = (int32_t)sh;
+            const uint32_t nb = nb_from_bin(q);
+            if (ERR && (b0 + g) * 32 + lane < n) er.add(nb, sh, sh - (float)q, B);
+            w[g] = transpose32(nb, lane);
+        }
+        if (lane < B) {
+            uint32_t* dst = out + (uint64_t)plane * stride + b0;
+#pragma unroll
+            for (int g = 0; g < NB_G; g++)
+                if (b0 + g < nblocks) dst[g] = w[g];
+        }
+    }
+    if (ERR) er.flush(B, partial);
+}
+
+// fp32 negabinary decoder: planes [s, s+num) at base[(i) * stride]; lane p
+// loads plane p's words, one transpose gives lane e the digits of value e
+__global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict__ base, uint64_t stride, uint64_t n,
+                                                    const uint32_t* __restrict__ maxkey, int exp_arg, int s, int num,
+                                                    const uint8_t* __restrict__ dnum, float* __restrict__ out) {
+    if (dnum) num = dnum[0] - s;
+    const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;
+    const int e = s + num;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nblocks = (n + 31) / 32;
+    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const bool neg = num != 0 && (e & 1);                   // :153, :177
+    for (uint64_t b0 = gw * NB_G; b0 < nblocks; b0 += nw * NB_G) {
+        uint32_t w[NB_G];
+        const uint32_t* src = base + (uint64_t)lane * stride + b0;
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) w[g] = (lane < num && b0 + g < nblocks) ? __ldcs(src + g) : 0u;
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) {
+            const uint32_t col = transpose32(w[g], lane);   // bit i = digit of plane s+i
+            const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
+            const float val = num ? ldexpf((float)nb_to_bin(acc), -e + exp) : 0.f;
+            const uint64_t i = (b0 + g) * 32 + lane;
+            if (i < n) out[i] = neg ? -val : val;
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------
 // NegaBinary encoder -- NegaBinaryBPEncoder.hpp:18-62 (+ :65-125 errors)
@@ -400,6 +581,125 @@ __global__ void __launch_bounds__(256) k_gr_write(const T* __restrict__ x, uint6
     }
 }
 
+// fp32 grouped writer: one transpose per block instead of B ballots
+__global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x, uint64_t n,
+                                                   const uint32_t* __restrict__ maxkey, int exp_arg, int B,
+                                                   const uint8_t* __restrict__ rbs,
+                                                   const uint32_t* __restrict__ chunk_off, uint32_t* __restrict__ out,
+                                                   uint64_t cap) {
+    const int exp = maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nblocks = (n + 31) / 32;
+    uint32_t off0, off1;
+    gr_warp_offsets(rbs, nblocks, chunk_off, B, off0, off1);
+    const int plane = B - 1 - lane;                    // lane k owns bit k
+    uint32_t off = __shfl_sync(FULL, off0, plane & 31);
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    for (int j = 0; j < GR_BPW; j++) {
+        const uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        const uint64_t i = b * 32 + lane;
+        float v = i < n ? __ldcs(x + i) : 0.f;
+        const float sh = ldexpf(v, B - exp);
+        const int64_t fix = (int64_t)sh;
+        const bool neg = v < 0.f;
+        const uint32_t q = (uint32_t)(neg ? -fix : fix);
+        const uint32_t sign = __ballot_sync(FULL, neg);
+        const uint32_t w = transpose32(q, lane);
+        const int r = rbs[b];
+        if (lane < B && plane >= r) {
+            uint32_t* dst = out + (uint64_t)plane * cap + off;
+            if (plane == r) { dst[0] = sign; dst[1] = w; }
+            else dst[0] = w;
+        }
+        off += gr_words(r, plane);
+    }
+}
+
+// fp32 grouped decoder, planes [s, e): lane p loads plane p's word of the block
+__global__ void __launch_bounds__(256) k_gr_decode32(const uint32_t* const* __restrict__ planes, uint64_t n,
+                                                    const uint32_t* __restrict__ maxkey, int exp_arg, int B, int s,
+                                                    int e, const uint8_t* __restrict__ dnum,
+                                                    const uint8_t* __restrict__ rbs,
+                                                    const uint32_t* __restrict__ chunk_off,
+                                                    uint32_t* __restrict__ signs, float* __restrict__ out) {
+    if (dnum) e = dnum[0];
+    const int exp = maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nblocks = (n + 31) / 32;
+    uint32_t off0, off1;
+    gr_warp_offsets(rbs, nblocks, chunk_off, B, off0, off1);
+    const uint32_t* src = (lane < B && lane >= s && lane < e) ? planes[lane] : nullptr;
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    for (int j = 0; j < GR_BPW; j++) {
+        const uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        const int r = rbs[b];
+        const uint64_t i = b * 32 + lane;
+        if (r < e) {
+            uint32_t w = 0, sg = 0;
+            if (src && lane >= r) {
+                if (lane == r) { sg = src[off0]; w = src[off0 + 1]; }
+                else w = src[off0];
+            }
+            uint32_t sign;
+            if (r >= s) {
+                sign = __shfl_sync(FULL, sg, r);
+                if (signs && lane == 0) signs[b] = sign;
+            } else {
+                sign = signs[b];
+            }
+            const uint32_t col = transpose32(w, lane);
+            const uint32_t acc = __brev(col) >> (32 - e);
+            const float v = ldexpf((float)acc, -e + exp);
+            if (i < n) out[i] = ((sign >> lane) & 1u) ? -v : v;
+        } else {
+            if (i < n) out[i] = 0.f;
+        }
+        off0 += gr_words(r, lane);
+    }
+}
+
+// fp32 grouped pass 1 with register error accumulators
+template <bool ERR>
+__global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, uint64_t n,
+                                                const uint32_t* __restrict__ maxkey, int exp_arg, int B,
+                                                uint8_t* __restrict__ rbs, uint32_t* __restrict__ chunk_words,
+                                                double* __restrict__ partial) {
+    const int exp = maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t nblocks = (n + 31) / 32;
+    __shared__ uint32_t cnt[GR_WARPS][32];
+    uint32_t c0 = 0;
+    GrErr32 er;
+    if (ERR) er.zero();
+    const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
+    for (int j = 0; j < GR_BPW; j++) {
+        const uint64_t b = b0 + j;
+        if (b >= nblocks) break;
+        const uint64_t i = b * 32 + lane;
+        uint32_t q = 0;
+        if (i < n) {
+            const float sh = ldexpf(__ldg(x + i), B - exp);
+            const int64_t fix = (int64_t)sh;
+            q = (uint32_t)(fix < 0 ? -fix : fix);
+            if (ERR) er.add(fabsf(sh), B);
+        }
+        const uint32_t o = __reduce_or_sync(FULL, q);
+        const int r = o ? B - 1 - (31 - __clz(o)) : B;
+        if (lane == 0) rbs[b] = (uint8_t)r;
+        c0 += gr_words(r, lane);
+    }
+    cnt[warp][lane] = c0;
+    __syncthreads();
+    if (threadIdx.x < 32 && (int)threadIdx.x < B) {
+        uint32_t t = 0;
+        for (int w = 0; w < GR_WARPS; w++) t += cnt[w][threadIdx.x];
+        chunk_words[(uint64_t)blockIdx.x * B + threadIdx.x] = t;
+    }
+    if (ERR) er.flush(B, partial);
+}
+
 // GroupedBPEncoder::progressive_decode -- :210-297 (planes [s, e)); plane p's
 // words at planes[p] (absolute plane index). signs: per-block sign words kept
 // between calls (nullable when s == 0). A device count (dnum[0]) overrides e.
@@ -589,6 +889,24 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     constexpr int BS = Traits<T>::kBlock;
     const uint64_t nblocks = (n + BS - 1) / BS;
     const int th = 256;
+    if (std::is_same<T, float>::value) {
+        const unsigned g32 = (unsigned)kSMs * 4;
+        const uint64_t groups = (nblocks + NB_G - 1) / NB_G;
+        unsigned grid = (unsigned)std::min<uint64_t>(g32, (groups + 7) / 8 ? (groups + 7) / 8 : 1);
+        if (errs_out) grid = (unsigned)kPartialSlots;
+        if (errs_out)
+            k_nb_encode32<true><<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
+                                                     (uint32_t*)out, stride, partial);
+        else
+            k_nb_encode32<false><<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
+                                                      (uint32_t*)out, stride, nullptr);
+        PRODM_CHECK_LAUNCH("k_nb_encode32");
+        if (errs_out) {
+            k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
+            PRODM_CHECK_LAUNCH("k_reduce_partials");
+        }
+        return PRODM_OK;
+    }
     unsigned grid = errs_out ? (unsigned)kSMs * 4 : grid_for(nblocks * 32, th, 8);
     if (errs_out) {
         k_nb_encode<T, true><<<grid, th, 0, st>>>(x, n, (const K*)maxkey, exp, B, (typename Traits<T>::S*)out, stride,
@@ -611,6 +929,14 @@ int launch_nb_decode(const void* base, uint64_t stride, uint64_t n, const void* 
     constexpr int BS = Traits<T>::kBlock;
     const uint64_t nblocks = (n + BS - 1) / BS;
     const int th = 256;
+    if (std::is_same<T, float>::value) {
+        const uint64_t groups = (nblocks + NB_G - 1) / NB_G;
+        const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)kSMs * 8, (groups + 7) / 8));
+        k_nb_decode32<<<grid, th, 0, st>>>((const uint32_t*)base, stride, n, (const uint32_t*)maxkey, exp, s, num, dnum,
+                                           (float*)out);
+        PRODM_CHECK_LAUNCH("k_nb_decode32");
+        return PRODM_OK;
+    }
     k_nb_decode<T><<<grid_for(nblocks * 32, th, 8), th, 0, st>>>((const typename Traits<T>::S*)base, stride, n,
                                                                  (const K*)maxkey, exp, s, num, dnum, out);
     PRODM_CHECK_LAUNCH("k_nb_decode");
@@ -627,6 +953,25 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     constexpr int BS = Traits<T>::kBlock;
     const uint64_t nblocks = (n + BS - 1) / BS;
     const uint64_t nch = gr_nchunks(nblocks);
+    if (std::is_same<T, float>::value) {
+        if (errs_out)
+            k_gr_rb32<true><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
+                                                                     rbs, chunk_words, partial);
+        else
+            k_gr_rb32<false><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp,
+                                                                      B, rbs, chunk_words, nullptr);
+        PRODM_CHECK_LAUNCH("k_gr_rb32");
+        if (errs_out) {
+            k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
+            PRODM_CHECK_LAUNCH("k_reduce_partials");
+        }
+        k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, 4, chunk_off, sizes);
+        PRODM_CHECK_LAUNCH("k_gr_scan");
+        k_gr_write32<<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B, rbs,
+                                                             chunk_off, (uint32_t*)out, cap);
+        PRODM_CHECK_LAUNCH("k_gr_write32");
+        return PRODM_OK;
+    }
     if (errs_out) {
         k_gr_rb<T, true><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(x, n, (const K*)maxkey, exp, B, rbs, chunk_words,
                                                                   partial);
@@ -670,6 +1015,13 @@ int launch_gr_decode(const void* const* planes, uint64_t n, const void* maxkey, 
     constexpr int BS = Traits<T>::kBlock;
     const uint64_t nblocks = (n + BS - 1) / BS;
     const uint64_t nch = gr_nchunks(nblocks);
+    if (std::is_same<T, float>::value) {
+        k_gr_decode32<<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const uint32_t* const*)planes, n,
+                                                              (const uint32_t*)maxkey, exp, B, s, e, dnum, rbs,
+                                                              chunk_off, (uint32_t*)signs, (float*)out);
+        PRODM_CHECK_LAUNCH("k_gr_decode32");
+        return PRODM_OK;
+    }
     k_gr_decode<T><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const S* const*)planes, n, (const K*)maxkey, exp, B, s, e,
                                                             dnum, rbs, chunk_off, (S*)signs, out);
     PRODM_CHECK_LAUNCH("k_gr_decode");

@@ -88,9 +88,8 @@ struct DevHeap {
 };
 
 template <class T>
-__device__ void interpret_one(int kind, const DevEstimator<T>& est, int nl, int B, const uint32_t* __restrict__ sizes,
-                              const double* __restrict__ errs, double tol, uint8_t* __restrict__ index,
-                              uint32_t* __restrict__ rsz) {
+__device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int B, const uint32_t* __restrict__ sizes,
+                               const double* __restrict__ errs, double tol, uint8_t* index, uint32_t* rsz) {
     auto E = [&](int l, int j) { return errs[(size_t)l * (B + 1) + j]; };
     auto S = [&](int l, int j) { return sizes[(size_t)l * B + j]; };
     for (int i = 0; i < nl; i++) rsz[i] = 0;
@@ -155,20 +154,51 @@ __device__ void interpret_one(int kind, const DevEstimator<T>& est, int nl, int 
         }
         return;
     }
+    // estimated_efficiency (GreedyBasedSizeInterpreter.hpp:228-248), warp-parallel:
+    // candidate i (run of i planes) has efficiency gain(E[idx], E[idx+i]) /
+    // (sizes[idx] + ... + sizes[idx+i-1]) with the reference's u32 size sums;
+    // the sequential loop stops at the first i >= 2 whose predecessor is
+    // positive and larger, which a ballot finds directly.
+    const int lane = threadIdx.x & 31;
     auto eff = [&](int idx, int l) {
-        double cg = est.gain((T)E(l, idx), (T)E(l, idx + 1), l);
-        uint32_t cs = S(l, idx);
-        double ce = cg / cs;
-        int cn = 1;
-        for (int i = 2; i < B - idx; i++) {
-            double ng = est.gain((T)E(l, idx), (T)E(l, idx + i), l);
-            uint32_t ns = cs + S(l, idx + i - 1);
-            double ne = ng / ns;
-            if ((ce > 0) && (ce > ne)) break;
-            cg = ng;
-            ce = ne;
-            cs = ns;
-            cn = i;
+        const int cnt = B - idx - 1;             // largest candidate run the loop visits
+        uint32_t carry = 0;
+        double prev_last = 0.0;
+        int cn = -1;
+        double ce = 0.0;
+        for (int base = 0; base <= (cnt > 1 ? cnt : 1); base += 32) {
+            const int i = base + lane;
+            uint32_t sz = (i >= 1 && idx + i - 1 < B) ? S(l, idx + i - 1) : 0u;
+            uint32_t incl = sz;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const uint32_t ns = carry + incl;
+            double ne = 0.0;
+            if (i >= 1 && idx + i <= B) ne = (double)est.gain((T)E(l, idx), (T)E(l, idx + i), l) / ns;
+            double prev = __shfl_up_sync(0xffffffffu, ne, 1);
+            if (lane == 0) prev = prev_last;
+            const bool stop = i >= 2 && i <= cnt && (prev > 0) && (prev > ne);
+            const unsigned m = __ballot_sync(0xffffffffu, stop);
+            if (m) {
+                const int bi = base + __ffs(m) - 1;      // first stopping candidate
+                cn = bi - 1;
+                const int src = cn - base;
+                const double a = __shfl_sync(0xffffffffu, ne, src < 0 ? 0 : src);
+                ce = src < 0 ? prev_last : a;
+                break;
+            }
+            prev_last = __shfl_sync(0xffffffffu, ne, 31);
+            carry = __shfl_sync(0xffffffffu, ns, 31);
+        }
+        if (cn < 0) {
+            cn = cnt >= 2 ? cnt : 1;
+            // efficiency of the accepted run cn (recomputed, same expression)
+            uint32_t tot = 0;
+            for (int j = 0; j < cn; j++) tot += S(l, idx + j);
+            ce = (double)est.gain((T)E(l, idx), (T)E(l, idx + cn), l) / tot;
         }
         return Item{ce, l, cn};
     };
@@ -189,6 +219,20 @@ __device__ void interpret_one(int kind, const DevEstimator<T>& est, int nl, int 
     }
 }
 
+// all lanes of the warp run the same sequence on private copies; lane 0 stores
+template <class T>
+__device__ void interpret_one(int kind, const DevEstimator<T>& est, int nl, int B, const uint32_t* __restrict__ sizes,
+                              const double* __restrict__ errs, double tol, uint8_t* __restrict__ index_io,
+                              uint32_t* __restrict__ rsz_io) {
+    uint8_t index[kMaxLevels];
+    uint32_t rsz[kMaxLevels];
+    for (int i = 0; i < nl; i++) index[i] = index_io[i];
+    interpret_core<T>(kind, est, nl, B, sizes, errs, tol, index, rsz);
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0)
+        for (int i = 0; i < nl; i++) { index_io[i] = index[i]; rsz_io[i] = rsz[i]; }
+}
+
 // one thread per field: field f uses sizes + f*sz_stride etc.
 template <class T>
 __global__ void k_interpret(int nfields, int kind, int est_kind, const int* __restrict__ ndims,
@@ -196,7 +240,7 @@ __global__ void k_interpret(int nfields, int kind, int est_kind, const int* __re
                             uint64_t sz_stride, const double* __restrict__ errs, uint64_t err_stride,
                             const double* __restrict__ tols, double tol0, uint8_t* __restrict__ index,
                             uint64_t idx_stride, uint32_t* __restrict__ rsz) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = blockIdx.x;              // one warp per field; all lanes run the same steps
     if (f >= nfields) return;
     int L = levels[f];
     DevEstimator<T> est;
@@ -212,8 +256,7 @@ int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, co
                      const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
                      cudaStream_t st) {
-    const int th = 32;
-    k_interpret<T><<<(nfields + th - 1) / th, th, 0, st>>>(nfields, kind, est_kind, d_ndims, d_levels, s, B, d_sizes,
+    k_interpret<T><<<nfields, 32, 0, st>>>(nfields, kind, est_kind, d_ndims, d_levels, s, B, d_sizes,
                                                            sz_stride, d_errs, err_stride, d_tols, tol0, d_index,
                                                            idx_stride, d_rsz);
     PRODM_CHECK_LAUNCH("k_interpret");

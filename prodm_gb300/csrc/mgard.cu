@@ -160,6 +160,103 @@ __global__ void k_recompose_level(const T* __restrict__ coarse, const T* __restr
     }
 }
 
+// ---------------------------------------------------------------------------
+// Row-parallel forms used by the device pipeline (packed layout). One CTA
+// walks fine rows (x0, x1); threads stride along x2, so loads and stores are
+// coalesced and there is no per-element 64-bit division. Same arithmetic
+// (and the same uncontracted operation order) as the generic kernels.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t row_rank_base(uint32_t r0, uint32_t r1, const Box& F, const Box& C, bool& cc) {
+    cc = r0 < C.n[0] && r1 < C.n[1];
+    // rank of (r0, r1, cc ? C2 : 0)
+    return level_rank(r0, r1, cc ? C.n[2] : 0u, F, C);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in, uint64_t s0, uint64_t s1, Box F, Box C,
+                                                        T* __restrict__ coef, T* __restrict__ coarse,
+                                                        T* __restrict__ fnat, typename KeyOf<T>::type* maxkey_level,
+                                                        typename KeyOf<T>::type* maxkey_coarse) {
+    using K = typename KeyOf<T>::type;
+    K mk = 0, mc = 0;
+    const uint32_t rows = F.n[0] * F.n[1];
+    const uint32_t n2 = F.n[2], c2n = C.n[2];
+    for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+        const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
+        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+        const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
+        bool cc;
+        const uint64_t rbase = row_rank_base(r0, r1, F, C, cc);
+        const T* p = in + x0 * s0 + x1 * s1;
+        T* frow = fnat ? fnat + (uint64_t)row * n2 : nullptr;
+        T* crow = coarse + ((uint64_t)r0 * C.n[1] + r1) * c2n;
+        for (uint32_t x2 = threadIdx.x; x2 < n2; x2 += blockDim.x) {
+            const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
+            const uint32_t r2 = reord(x2, n2, c2n);
+            const T* q = p + x2;
+            T v = *q;
+            if (mask == 0) {
+                crow[r2] = v;
+                if (frow) frow[x2] = (T)0;
+                K k = abs_key(v);
+                mc = k > mc ? k : mc;
+            } else {
+                auto at = [&](int d0, int d1, int d2) -> T {
+                    return __ldg(q + (int64_t)d0 * (int64_t)s0 + (int64_t)d1 * (int64_t)s1 + d2);
+                };
+                T c = sub_rn(v, interp<T>(mask, at));
+                coef[rbase + (cc ? r2 - c2n : r2)] = c;
+                if (frow) frow[x2] = c;
+                K k = abs_key(c);
+                mk = k > mk ? k : mk;
+            }
+        }
+    }
+    if (maxkey_level) {
+        mk = warp_max(mk);
+        if ((threadIdx.x & 31) == 0 && mk) atomicMax(maxkey_level, mk);
+    }
+    if (maxkey_coarse) {
+        mc = warp_max(mc);
+        if ((threadIdx.x & 31) == 0 && mc) atomicMax(maxkey_coarse, mc);
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ coarse, const T* __restrict__ coef, Box F,
+                                                        Box C, T* __restrict__ out, uint64_t s0, uint64_t s1) {
+    const uint32_t rows = F.n[0] * F.n[1];
+    const uint32_t n2 = F.n[2], c2n = C.n[2];
+    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
+    for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+        const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
+        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+        const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : reord(x0, F.n[0], C.n[0]);
+        const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : reord(x1, F.n[1], C.n[1]);
+        const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
+        bool cc;
+        const uint64_t rbase = row_rank_base(r0, r1, F, C, cc);
+        const T* cb0 = coarse + c0 * cs0 + c1 * cs1;
+        T* orow = out + x0 * s0 + x1 * s1;
+        for (uint32_t x2 = threadIdx.x; x2 < n2; x2 += blockDim.x) {
+            const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
+            const uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, n2, c2n);
+            const T* cb = cb0 + c2;
+            T v;
+            if (mask == 0) {
+                v = *cb;
+            } else {
+                auto at = [&](int d0, int d1, int d2) -> T {
+                    return __ldg(cb + (d0 > 0 ? cs0 : 0) + (d1 > 0 ? cs1 : 0) + (d2 > 0 ? 1 : 0));
+                };
+                const uint32_t r2 = reord(x2, n2, c2n);
+                v = add_rn(coef[rbase + (cc ? r2 - c2n : r2)], interp<T>(mask, at));
+            }
+            orow[x2] = v;
+        }
+    }
+}
+
 // copy a box between strided arrays
 template <class T>
 __global__ void k_copy_box(const T* __restrict__ src, uint64_t a0, uint64_t a1, Box B, T* __restrict__ dst, uint64_t b0,
@@ -299,14 +396,22 @@ __global__ void k_interleave(T* __restrict__ data, uint64_t s0, uint64_t s1, Box
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
+unsigned row_threads(uint32_t n2) { return n2 >= 256 ? 256 : n2 >= 128 ? 128 : n2 >= 64 ? 64 : 32; }
+unsigned row_grid(uint64_t rows, unsigned th) {
+    uint64_t per_sm = 2048 / th;
+    uint64_t cap = (uint64_t)kSMs * per_sm * 4;
+    uint64_t g = rows < cap ? rows : cap;
+    return (unsigned)(g ? g : 1);
+}
+
 template <class T>
 int launch_decompose_level_packed(const T* in, uint64_t s0, uint64_t s1, const Box& F, const Box& C, T* coef, T* coarse,
                                   T* fnat, void* maxkey_level, void* maxkey_coarse, cudaStream_t st) {
     using K = typename KeyOf<T>::type;
-    const int th = 256;
-    k_decompose_level<T, true><<<grid_for(F.size(), th), th, 0, st>>>(in, s0, s1, F, C, coef, coarse, 0, 0, fnat,
-                                                                      (K*)maxkey_level, (K*)maxkey_coarse);
-    PRODM_CHECK_LAUNCH("k_decompose_level");
+    const unsigned th = row_threads(F.n[2]);
+    k_decompose_rows<T><<<row_grid((uint64_t)F.n[0] * F.n[1], th), th, 0, st>>>(in, s0, s1, F, C, coef, coarse, fnat,
+                                                                                 (K*)maxkey_level, (K*)maxkey_coarse);
+    PRODM_CHECK_LAUNCH("k_decompose_rows");
     return PRODM_OK;
 }
 
@@ -323,9 +428,9 @@ int launch_decompose_level_inplace(const T* in, const Box& F, const Box& C, T* o
 template <class T>
 int launch_recompose_level_packed(const T* coarse, const T* coef, const Box& F, const Box& C, T* out, uint64_t s0,
                                   uint64_t s1, cudaStream_t st) {
-    const int th = 256;
-    k_recompose_level<T, true><<<grid_for(F.size(), th), th, 0, st>>>(coarse, coef, F, C, out, s0, s1);
-    PRODM_CHECK_LAUNCH("k_recompose_level");
+    const unsigned th = row_threads(F.n[2]);
+    k_recompose_rows<T><<<row_grid((uint64_t)F.n[0] * F.n[1], th), th, 0, st>>>(coarse, coef, F, C, out, s0, s1);
+    PRODM_CHECK_LAUNCH("k_recompose_rows");
     return PRODM_OK;
 }
 

@@ -130,9 +130,11 @@ def test_all_planes_roundtrip_and_reset():
     mdr.refactor(x)
     out = mdr.retrieve_planes([B] * (L + 1))
     sizes, bounds, _ = mdr.level_info()
-    # all planes: error = quantisation only, bounded by the sum of level quanta
+    # all planes: quantisation (sum of level quanta) plus fp32 rounding of the
+    # recomposition (a few ulp of the field magnitude per level)
     quanta = sum(math.ldexp(1.0, math.frexp(b / 4)[1] + 2 - B) for b in bounds)
-    assert float((out - x).abs().max()) <= quanta
+    rounding = 2 * (L + 1) * float(np.finfo(np.float32).eps) * float(x.abs().max())
+    assert float((out - x).abs().max()) <= quanta + rounding
     mdr.reset()
     assert not mdr.index().any()
     z = mdr.retrieve_planes([0] * (L + 1))
@@ -159,19 +161,47 @@ def test_invalid_requests_raise():
         api().MDRField((65, 65, 65), torch.float64, 3, 64, "grouped")
 
 
-def test_metadata_layout_matches_reference_format():
+def test_metadata_and_level_files_match_reference_composed_refactor():
+    """GPU refactor of the golden field reproduces the reference ComposedRefactor
+    byte for byte: level files and metadata (whose reference layout is a prefix
+    of ours; an extension carries the squared-error tables)."""
     g = np.load(__import__("golden_io").GOLDEN + "/composed.npz")
     field = g["field"]
     for enc in ("grouped", "negabinary"):
         mdr = api().MDRField(field.shape, torch.float32, 3, 32, enc, "hierarchical", "max")
         mdr.refactor(torch.from_numpy(field).cuda())
+        files = np.concatenate([mdr.export_level(l) for l in range(4)])
+        assert files.tobytes() == g[enc + "_levels"].tobytes()
         meta = mdr.metadata()
         ref = g[enc + "_metadata"].tobytes()
-        # the reference layout is a prefix; an extension carries the squared-error tables
-        assert len(meta) > len(ref)
-        hdr = 1 + 4 * 3 + 1
-        assert meta[:hdr] == ref[:hdr]
-        # sizes / stopping indices / level_num / negabinary flag sections
-        nl, B = 4, 32
-        tail = nl * (4 + 4 * B) + nl + 4 * nl + 1
-        assert meta[hdr + 4 * nl:hdr + 4 * nl + tail] == ref[hdr + 4 * nl:hdr + 4 * nl + tail]
+        assert meta[:len(ref)] == ref
+        assert meta[len(ref):len(ref) + 4] == b"SQER"
+
+
+@pytest.mark.parametrize("enc", ["grouped", "negabinary"])
+def test_reconstructor_fed_from_reference_files(enc):
+    """load_metadata + load_level from the reference's own level files, then the
+    progressive retrieval of the reference driver (sign-exclude greedy, max HB
+    estimator); results equal the reference's reconstruction up to float
+    rounding whenever every level received planes."""
+    g = np.load(__import__("golden_io").GOLDEN + "/composed.npz")
+    field = g["field"]
+    meta = g[enc + "_metadata"].tobytes()
+    lb = g[enc + "_level_bytes"]
+    levels = np.split(g[enc + "_levels"], np.cumsum(lb)[:-1])
+    rec = api().MDRField(field.shape, torch.float32, 3, 32, enc, "hierarchical", "max")
+    rec.load_metadata(meta)
+    sizes, _, _ = rec.level_info()
+    loaded = [0] * 4
+    for t, tol in enumerate(g["tols"]):
+        rec.interpret(float(tol), "sign_exclude", "max_hb")
+        idx = rec.index()
+        for l in range(4):
+            need = int(sizes[l, :idx[l]].astype(np.int64).sum())
+            if need > loaded[l]:
+                rec.load_level(l, levels[l][loaded[l]:need], offset=loaded[l])
+                loaded[l] = need
+        out = rec.reconstruct().cpu().numpy()
+        assert float(np.abs(out - field).max()) <= float(tol)
+        if (idx > 0).all():
+            np.testing.assert_allclose(out, g[enc + "_recon"][t], rtol=0, atol=1e-5 * float(np.abs(field).max()))
