@@ -129,6 +129,12 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
     return x;
 }
 
+// x * 2^e, equal to ldexpf(x, e): a single multiplication by an exact power of
+// two rounds once, as ldexpf does, whenever 2^e is a normal float
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+__device__ __forceinline__ bool pow2_normal(int e) { return e >= -126 && e <= 127; }
+__device__ __forceinline__ float scale2(float v, int e, bool fast, float sc) { return fast ? v * sc : ldexpf(v, e); }
+
 // (-2)^i as a float (exact)
 __device__ __forceinline__ constexpr float nbw(int i) { return (i & 1) ? -(float)(1u << i) : (float)(1u << i); }
 
@@ -231,8 +237,14 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
     const uint64_t nblocks = (n + 31) / 32;
     const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
-    NbErr32 er;
-    if (ERR) er.zero();
+    const int se = B - exp;
+    const bool fast = se >= -126 && se <= 127;
+    const float scale = fast ? pow2f(se) : 1.f;
+    float acc[32], accx = 0.f;
+    if (ERR) {
+#pragma unroll
+        for (int k = 0; k < 32; k++) acc[k] = 0.f;
+    }
     const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
     for (uint64_t b0 = gw * NB_G; b0 < nblocks; b0 += nw * NB_G) {
         float v[NB_G];
@@ -241,15 +253,36 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
             const uint64_t i = (b0 + g) * 32 + lane;
             v[g] = i < n ? __ldcs(x + i) : 0.f;
         }
-        uint32_t w[NB_G];
+        uint32_t nb[NB_G];
+        float sh[NB_G], d[NB_G];
 #pragma unroll
         for (int g = 0; g < NB_G; g++) {
-            const float sh = ldexpf(v[g], B - exp);         // :42
-            const int32_t q = (int32_t)sh;
-            const uint32_t nb = nb_from_bin(q);
-            if (ERR && (b0 + g) * 32 + lane < n) er.add(nb, sh, sh - (float)q, B);
-            w[g] = transpose32(nb, lane);
+            sh[g] = fast ? v[g] * scale : ldexpf(v[g], se);    // :42
+            const int32_t q = (int32_t)sh[g];
+            nb[g] = nb_from_bin(q);
+            d[g] = sh[g] - (float)q;                             // exact fraction
         }
+        if (ERR) {
+            // NegaBinaryBPEncoder.hpp:231-239; values past n contribute 0 (shifted = 0)
+#pragma unroll
+            for (int g = 0; g < NB_G; g++) {
+                acc[0] += d[g] * d[g];
+                accx += sh[g] * sh[g];
+            }
+#pragma unroll
+            for (int k = 1; k < 32; k++) {
+                if (k < B) {
+#pragma unroll
+                    for (int g = 0; g < NB_G; g++) {
+                        if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
+                        acc[k] += d[g] * d[g];
+                    }
+                }
+            }
+        }
+        uint32_t w[NB_G];
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) w[g] = transpose32(nb[g], lane);
         if (lane < B) {
             uint32_t* dst = out + (uint64_t)plane * stride + b0;
 #pragma unroll
@@ -257,7 +290,13 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
                 if (b0 + g < nblocks) dst[g] = w[g];
         }
     }
-    if (ERR) er.flush(B, partial);
+    if (ERR) {
+        NbErr32 er;
+#pragma unroll
+        for (int k = 0; k < 32; k++) er.acc[k] = acc[k];
+        er.accx = accx;
+        er.flush(B, partial);
+    }
 }
 
 // fp32 negabinary decoder: planes [s, s+num) at base[(i) * stride]; lane p
@@ -273,6 +312,8 @@ __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict_
     const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
     const bool neg = num != 0 && (e & 1);                   // :153, :177
+    const bool dfast = (exp - e) >= -126 && (exp - e) <= 127;
+    const float dscale = dfast ? pow2f(exp - e) : 1.f;
     for (uint64_t b0 = gw * NB_G; b0 < nblocks; b0 += nw * NB_G) {
         uint32_t w[NB_G];
         const uint32_t* src = base + (uint64_t)lane * stride + b0;
@@ -282,7 +323,7 @@ __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict_
         for (int g = 0; g < NB_G; g++) {
             const uint32_t col = transpose32(w[g], lane);   // bit i = digit of plane s+i
             const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
-            const float val = num ? ldexpf((float)nb_to_bin(acc), -e + exp) : 0.f;
+            const float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), -e + exp)) : 0.f;
             const uint64_t i = (b0 + g) * 32 + lane;
             if (i < n) out[i] = neg ? -val : val;
         }
@@ -594,13 +635,15 @@ __global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x,
     gr_warp_offsets(rbs, nblocks, chunk_off, B, off0, off1);
     const int plane = B - 1 - lane;                    // lane k owns bit k
     uint32_t off = __shfl_sync(FULL, off0, plane & 31);
+    const bool fast = pow2_normal(B - exp);
+    const float sc = fast ? pow2f(B - exp) : 1.f;
     const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
     for (int j = 0; j < GR_BPW; j++) {
         const uint64_t b = b0 + j;
         if (b >= nblocks) break;
         const uint64_t i = b * 32 + lane;
         float v = i < n ? __ldcs(x + i) : 0.f;
-        const float sh = ldexpf(v, B - exp);
+        const float sh = scale2(v, B - exp, fast, sc);
         const int64_t fix = (int64_t)sh;
         const bool neg = v < 0.f;
         const uint32_t q = (uint32_t)(neg ? -fix : fix);
@@ -630,6 +673,8 @@ __global__ void __launch_bounds__(256) k_gr_decode32(const uint32_t* const* __re
     uint32_t off0, off1;
     gr_warp_offsets(rbs, nblocks, chunk_off, B, off0, off1);
     const uint32_t* src = (lane < B && lane >= s && lane < e) ? planes[lane] : nullptr;
+    const bool fast = pow2_normal(exp - e);
+    const float sc = fast ? pow2f(exp - e) : 1.f;
     const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
     for (int j = 0; j < GR_BPW; j++) {
         const uint64_t b = b0 + j;
@@ -651,7 +696,7 @@ __global__ void __launch_bounds__(256) k_gr_decode32(const uint32_t* const* __re
             }
             const uint32_t col = transpose32(w, lane);
             const uint32_t acc = __brev(col) >> (32 - e);
-            const float v = ldexpf((float)acc, -e + exp);
+            const float v = scale2((float)acc, exp - e, fast, sc);
             if (i < n) out[i] = ((sign >> lane) & 1u) ? -v : v;
         } else {
             if (i < n) out[i] = 0.f;
@@ -671,6 +716,8 @@ __global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, ui
     const uint64_t nblocks = (n + 31) / 32;
     __shared__ uint32_t cnt[GR_WARPS][32];
     uint32_t c0 = 0;
+    const bool fast = pow2_normal(B - exp);
+    const float sc = fast ? pow2f(B - exp) : 1.f;
     GrErr32 er;
     if (ERR) er.zero();
     const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
@@ -680,7 +727,7 @@ __global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, ui
         const uint64_t i = b * 32 + lane;
         uint32_t q = 0;
         if (i < n) {
-            const float sh = ldexpf(__ldg(x + i), B - exp);
+            const float sh = scale2(__ldg(x + i), B - exp, fast, sc);
             const int64_t fix = (int64_t)sh;
             q = (uint32_t)(fix < 0 ? -fix : fix);
             if (ERR) er.add(fabsf(sh), B);
@@ -823,14 +870,21 @@ template <class T>
 __global__ void k_reduce_partials(const double* __restrict__ partial, int nparts, int B,
                                   const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg, int exp_add,
                                   int scale, double* __restrict__ out) {
-    for (int k = threadIdx.x; k <= B; k += blockDim.x) {
+    // one warp per table entry; lane-strided partial sums then a fixed-order
+    // shuffle tree, so the result does not depend on scheduling
+    const int lane = threadIdx.x & 31;
+    for (int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k <= B; k += gridDim.x * (blockDim.x >> 5)) {
         double s = 0;
-        for (int p = 0; p < nparts; p++) s += partial[(size_t)p * (B + 1) + k];
-        if (scale) {
-            int exp = level_exp<T>(maxkey, exp_arg) + exp_add;
-            s = ldexp(s, 2 * (-B + exp));
+        for (int p = lane; p < nparts; p += 32) s += partial[(size_t)p * (B + 1) + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+        if (lane == 0) {
+            if (scale) {
+                int exp = level_exp<T>(maxkey, exp_arg) + exp_add;
+                s = ldexp(s, 2 * (-B + exp));
+            }
+            out[k] = s;
         }
-        out[k] = s;
     }
 }
 
@@ -902,7 +956,7 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
                                                       (uint32_t*)out, stride, nullptr);
         PRODM_CHECK_LAUNCH("k_nb_encode32");
         if (errs_out) {
-            k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
+            k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
             PRODM_CHECK_LAUNCH("k_reduce_partials");
         }
         return PRODM_OK;
@@ -912,7 +966,7 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
         k_nb_encode<T, true><<<grid, th, 0, st>>>(x, n, (const K*)maxkey, exp, B, (typename Traits<T>::S*)out, stride,
                                                   partial);
         PRODM_CHECK_LAUNCH("k_nb_encode");
-        k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
+        k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
         PRODM_CHECK_LAUNCH("k_reduce_partials");
     } else {
         k_nb_encode<T, false><<<grid, th, 0, st>>>(x, n, (const K*)maxkey, exp, B, (typename Traits<T>::S*)out, stride,
@@ -962,7 +1016,7 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
                                                                       B, rbs, chunk_words, nullptr);
         PRODM_CHECK_LAUNCH("k_gr_rb32");
         if (errs_out) {
-            k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
+            k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
             PRODM_CHECK_LAUNCH("k_reduce_partials");
         }
         k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, 4, chunk_off, sizes);
@@ -981,7 +1035,7 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     }
     PRODM_CHECK_LAUNCH("k_gr_rb");
     if (errs_out) {
-        k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
+        k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
         PRODM_CHECK_LAUNCH("k_reduce_partials");
     }
     k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, (int)sizeof(typename Traits<T>::S), chunk_off, sizes);
@@ -1034,7 +1088,7 @@ int launch_sq_collect(const T* x, uint64_t n, int B, T maxv, double* partial, do
     const unsigned grid = (unsigned)kSMs * 4;
     k_sq_collect<T><<<grid, th, 0, st>>>(x, n, B, maxv, partial);
     PRODM_CHECK_LAUNCH("k_sq_collect");
-    k_reduce_partials<T><<<1, 128, 0, st>>>(partial, (int)grid, B, nullptr, 0, 0, 0, out);
+    k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)grid, B, nullptr, 0, 0, 0, out);
     PRODM_CHECK_LAUNCH("k_reduce_partials");
     return PRODM_OK;
 }

@@ -685,7 +685,10 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
     K* keys = (K*)h->keys;
     T* rcoef = (T*)h->rcoef;
     int rc;
+    // finest level: fused decode + recompose where the layout allows it
+    const bool fuse = h->nb && !h->orth && sizeof(T) == 4 && L >= 1 && decode_recompose_nb32_ok(g.box[L]);
     for (int l = 0; l <= L; l++) {
+        if (fuse && l == L) continue;
         const uint64_t n = g.elems[l];
         Stage sg(h, 3, l, st);
         if (h->nb) {
@@ -708,6 +711,13 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         T* cin = (l == 1) ? rcoef + g.offset[0] : (T*)h->rbuf[(l - 1) & 1];
         T* o = (l == L) ? out : (T*)h->rbuf[l & 1];
         Stage sg(h, 4, l, st);
+        if (fuse && l == L) {
+            if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->nblocks[l], keys + l,
+                                                   h->index + l, (const float*)cin, F, C, (float*)o,
+                                                   (uint64_t)F.n[1] * F.n[2], F.n[2], st)))
+                return rc;
+            continue;
+        }
         if (h->orth) {
             const T* tabs[3] = {level_tabs<T>(h, l, 0), level_tabs<T>(h, l, 1), level_tabs<T>(h, l, 2)};
             if ((rc = launch_coef_to_natural<T>(rcoef + g.offset[l], F, C, (T*)h->os.fnat, st))) return rc;

@@ -1,0 +1,152 @@
+// Fused finest-level retrieval (sm_103a): negabinary decode of the level's
+// retrieved planes + hierarchical recomposition, in one pass.
+//
+// The unfused path writes the decoded level coefficients (n_L values) and
+// reads them back in the recomposition; at the finest level that is most of
+// the field. Here one warp owns one fine row (x0, x1): the coefficients of a
+// row occupy one contiguous run of interleaved ranks, so the warp decodes the
+// 32-value blocks covering that run (one bit transpose per block) into shared
+// memory and then writes the recomposed row with coalesced stores. Decoding
+// and recomposition use exactly the arithmetic of the standalone kernels
+// (NegaBinaryBPEncoder.hpp:132-192; the multilinear interpolation of the
+// hierarchical basis), so the output is bit-identical to the unfused path.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace prodm {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t transpose32f(uint32_t x, int lane) {
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
+                                                                                                       : 0x55555555u;
+        const uint32_t y = __shfl_xor_sync(FULL, x, j);
+        const bool hi = (lane & j) != 0;
+        const uint32_t u = hi ? y : x, v = hi ? x : y;
+        const uint32_t t = ((u >> j) ^ v) & m;
+        x ^= hi ? t : (t << j);
+    }
+    return x;
+}
+
+__device__ __forceinline__ float pow2f_(int e) { return __int_as_float((e + 127) << 23); }
+
+template <class Get>
+__device__ __forceinline__ float interp_f(int mask, Get at) {
+    const float h = 0.5f;
+    auto avg = [&](float a, float b) { return __fmul_rn(h, __fadd_rn(a, b)); };
+    switch (mask) {
+        case 1: return avg(at(-1, 0, 0), at(1, 0, 0));
+        case 2: return avg(at(0, -1, 0), at(0, 1, 0));
+        case 4: return avg(at(0, 0, -1), at(0, 0, 1));
+        case 3: return avg(avg(at(-1, -1, 0), at(-1, 1, 0)), avg(at(1, -1, 0), at(1, 1, 0)));
+        case 5: return avg(avg(at(-1, 0, -1), at(-1, 0, 1)), avg(at(1, 0, -1), at(1, 0, 1)));
+        case 6: return avg(avg(at(0, -1, -1), at(0, -1, 1)), avg(at(0, 1, -1), at(0, 1, 1)));
+        case 7: {
+            float a = avg(avg(at(-1, -1, -1), at(-1, -1, 1)), avg(at(-1, 1, -1), at(-1, 1, 1)));
+            float b = avg(avg(at(1, -1, -1), at(1, -1, 1)), avg(at(1, 1, -1), at(1, 1, 1)));
+            return avg(a, b);
+        }
+        default: return 0.f;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* __restrict__ base, uint64_t stride,
+                                                              const uint32_t* __restrict__ maxkey,
+                                                              const uint8_t* __restrict__ dnum,
+                                                              const float* __restrict__ coarse, Box F, Box C,
+                                                              float* __restrict__ out, uint64_t s0, uint64_t s1,
+                                                              uint32_t row_blocks) {
+    extern __shared__ float sbuf[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* buf = sbuf + (size_t)warp * row_blocks * 32;
+    const int num = dnum[0];
+    const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
+    const int e = num;
+    const bool neg = num != 0 && (e & 1);
+    const bool dfast = (exp - e) >= -126 && (exp - e) <= 127;
+    const float dscale = dfast ? pow2f_(exp - e) : 1.f;
+    const uint32_t rows = F.n[0] * F.n[1];
+    const uint32_t n2 = F.n[2], c2n = C.n[2];
+    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
+    const uint32_t wpb = blockDim.x >> 5;
+    const uint32_t* pl = base + (uint64_t)lane * stride;   // lane p reads plane p
+    for (uint32_t row = blockIdx.x * wpb + warp; row < rows; row += gridDim.x * wpb) {
+        const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
+        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+        const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
+        const bool cc = r0 < C.n[0] && r1 < C.n[1];
+        const uint64_t rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
+        const uint32_t len = cc ? n2 - c2n : n2;
+        const uint64_t fb = rbase >> 5, lb = (rbase + len - 1) >> 5;
+        // decode the blocks covering ranks [rbase, rbase + len)
+        for (uint64_t blk = fb; blk <= lb; blk++) {
+            const uint32_t w = lane < num ? __ldcs(pl + blk) : 0u;
+            const uint32_t col = transpose32f(w, lane);
+            const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
+            float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
+            buf[(blk - fb) * 32 + lane] = neg ? -val : val;
+        }
+        __syncwarp();
+        const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
+        const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
+        const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
+        float* orow = out + x0 * s0 + x1 * s1;
+        const uint32_t boff = (uint32_t)(rbase - fb * 32);
+        for (uint32_t x2 = lane; x2 < n2; x2 += 32) {
+            const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
+            const uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, n2, c2n);
+            const float* cb = cb0 + c2;
+            float v;
+            if (mask == 0) {
+                v = *cb;
+            } else {
+                auto at = [&](int d0, int d1, int d2) -> float {
+                    return __ldg(cb + (d0 > 0 ? cs0 : 0) + (d1 > 0 ? cs1 : 0) + (d2 > 0 ? 1 : 0));
+                };
+                const uint32_t r2 = reord(x2, n2, c2n);
+                const float coef = buf[boff + (cc ? r2 - c2n : r2)];
+                v = __fadd_rn(coef, interp_f(mask, at));
+            }
+            orow[x2] = v;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+bool decode_recompose_nb32_ok(const Box& F) {
+    const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
+    const uint32_t row_blocks = (F.n[2] + 31) / 32 + 2;
+    return rows >= 1024 && (size_t)8 * row_blocks * 32 * sizeof(float) <= 200 * 1024;
+}
+
+// Returns PRODM_EUNSUPPORTED when the shape does not suit the row mapping
+// (the caller then runs the unfused kernels).
+int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* maxkey, const uint8_t* dnum,
+                                 const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
+                                 cudaStream_t st) {
+    const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
+    const uint32_t row_blocks = (F.n[2] + 31) / 32 + 2;
+    const size_t smem = (size_t)8 * row_blocks * 32 * sizeof(float);
+    if (rows < 1024 || smem > 200 * 1024) return PRODM_EUNSUPPORTED;
+    if (smem > 48 * 1024) {   // per device; cheap to repeat
+        cudaError_t e = cudaFuncSetAttribute(k_decode_recompose_nb32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             200 * 1024);
+        if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+    }
+    const uint64_t need = (rows + 7) / 8;
+    const uint64_t cap = (uint64_t)kSMs * 8;
+    const unsigned grid = (unsigned)(need < cap ? need : cap);
+    k_decode_recompose_nb32<<<grid, 256, smem, st>>>((const uint32_t*)base, stride, (const uint32_t*)maxkey, dnum,
+                                                     coarse, F, C, out, s0, s1, row_blocks);
+    PRODM_CHECK_LAUNCH("k_decode_recompose_nb32");
+    return PRODM_OK;
+}
+
+}  // namespace prodm

@@ -245,8 +245,15 @@ __global__ void k_interpret(int nfields, int kind, int est_kind, const int* __re
     int L = levels[f];
     DevEstimator<T> est;
     est.init(est_kind, ndims[f], L, s);
-    interpret_one<T>(kind, est, L + 1, B, sizes + f * sz_stride, errs + f * err_stride, tols ? tols[f] : tol0,
-                     index + f * idx_stride, rsz + f * idx_stride);
+    // stage this field's size and error tables in shared memory (latency)
+    __shared__ uint32_t s_sizes[kMaxLevels * 64];
+    __shared__ double s_errs[kMaxLevels * 65];
+    const int nl = L + 1;
+    for (int i = threadIdx.x; i < nl * B; i += blockDim.x) s_sizes[i] = sizes[f * sz_stride + i];
+    for (int i = threadIdx.x; i < nl * (B + 1); i += blockDim.x) s_errs[i] = errs[f * err_stride + i];
+    __syncwarp();
+    interpret_one<T>(kind, est, L + 1, B, s_sizes, s_errs, tols ? tols[f] : tol0, index + f * idx_stride,
+                     rsz + f * idx_stride);
 }
 
 }  // namespace

@@ -63,6 +63,12 @@ int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, co
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
                      cudaStream_t st);
 
+// fused.cu
+bool decode_recompose_nb32_ok(const Box& F);
+int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* maxkey, const uint8_t* dnum,
+                                 const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
+                                 cudaStream_t st);
+
 // pack.cu
 int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,
                    int word_bytes, uint8_t* dst, cudaStream_t st);

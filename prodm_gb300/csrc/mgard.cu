@@ -181,7 +181,8 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
     K mk = 0, mc = 0;
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t n2 = F.n[2], c2n = C.n[2];
-    for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
         const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
         const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
         const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
         const T* p = in + x0 * s0 + x1 * s1;
         T* frow = fnat ? fnat + (uint64_t)row * n2 : nullptr;
         T* crow = coarse + ((uint64_t)r0 * C.n[1] + r1) * c2n;
-        for (uint32_t x2 = threadIdx.x; x2 < n2; x2 += blockDim.x) {
+        for (uint32_t x2 = lane; x2 < n2; x2 += 32) {
             const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
             const uint32_t r2 = reord(x2, n2, c2n);
             const T* q = p + x2;
@@ -228,7 +229,8 @@ __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ co
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t n2 = F.n[2], c2n = C.n[2];
     const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
-    for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
         const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
         const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
         const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : reord(x0, F.n[0], C.n[0]);
@@ -238,7 +240,7 @@ __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ co
         const uint64_t rbase = row_rank_base(r0, r1, F, C, cc);
         const T* cb0 = coarse + c0 * cs0 + c1 * cs1;
         T* orow = out + x0 * s0 + x1 * s1;
-        for (uint32_t x2 = threadIdx.x; x2 < n2; x2 += blockDim.x) {
+        for (uint32_t x2 = lane; x2 < n2; x2 += 32) {
             const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
             const uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, n2, c2n);
             const T* cb = cb0 + c2;
@@ -396,11 +398,13 @@ __global__ void k_interleave(T* __restrict__ data, uint64_t s0, uint64_t s1, Box
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
-unsigned row_threads(uint32_t n2) { return n2 >= 256 ? 256 : n2 >= 128 ? 128 : n2 >= 64 ? 64 : 32; }
+// one warp per row, 8 warps per CTA; enough CTAs for full occupancy
+unsigned row_threads(uint32_t) { return 256; }
 unsigned row_grid(uint64_t rows, unsigned th) {
-    uint64_t per_sm = 2048 / th;
-    uint64_t cap = (uint64_t)kSMs * per_sm * 4;
-    uint64_t g = rows < cap ? rows : cap;
+    const uint64_t wpb = th / 32;
+    uint64_t need = (rows + wpb - 1) / wpb;
+    uint64_t cap = (uint64_t)kSMs * 8 * 4;
+    uint64_t g = need < cap ? need : cap;
     return (unsigned)(g ? g : 1);
 }
 
