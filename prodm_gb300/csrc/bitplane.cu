@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict_
         uint32_t w[NB_G];
         const uint32_t* src = base + (uint64_t)lane * stride + b0;
 #pragma unroll
-        for (int g = 0; g < NB_G; g++) w[g] = (lane < num && b0 + g < nblocks) ? __ldcs(src + g) : 0u;
+        for (int g = 0; g < NB_G; g++) w[g] = (lane < num && b0 + g < nblocks) ? __ldg(src + g) : 0u;
 #pragma unroll
         for (int g = 0; g < NB_G; g++) {
             const uint32_t col = transpose32(w[g], lane);   // bit i = digit of plane s+i

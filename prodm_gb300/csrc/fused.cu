@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
         const uint64_t fb = rbase >> 5, lb = (rbase + len - 1) >> 5;
         // decode the blocks covering ranks [rbase, rbase + len)
         for (uint64_t blk = fb; blk <= lb; blk++) {
-            const uint32_t w = lane < num ? __ldcs(pl + blk) : 0u;
+            const uint32_t w = lane < num ? __ldg(pl + blk) : 0u;
             const uint32_t col = transpose32f(w, lane);
             const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
             float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;

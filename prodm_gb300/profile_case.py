@@ -1,0 +1,48 @@
+"""Small, self-contained workload for kernel profiling (ncu) and quick timing.
+
+    python -m prodm_gb300.profile_case --shape 257 --levels 7 --reps 3
+
+Runs `reps` refactor + progressive-retrieve steps of a seeded Gaussian random
+field (k^-5/3) with the benchmark's component set (NegaBinary, 32 planes,
+hierarchical basis, squared-error tables, relative L2 tolerances 1e-2..1e-6)
+and prints per-stage CUDA-event times of the last step.
+"""
+import argparse
+import math
+
+import torch
+
+from . import api, fields
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--shape", type=int, default=257)
+    ap.add_argument("--levels", type=int, default=None)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--encoder", default="negabinary")
+    ap.add_argument("--basis", default="hierarchical")
+    a = ap.parse_args()
+    shape = (a.shape,) * 3
+    L = a.levels if a.levels is not None else min(7, api.max_level(shape))
+    x = fields.spectral_grf(shape, seed=3)
+    norm2 = float((x.double() ** 2).sum().item())
+    mdr = api.MDRField(shape, torch.float32, L, 32, a.encoder, a.basis, "squared")
+    out = torch.empty_like(x)
+    interp = "negabinary" if a.encoder == "negabinary" else "greedy"
+    for r in range(a.reps):
+        if r == a.reps - 1:
+            mdr.set_timing(True)
+        mdr.refactor(x)
+        mdr.reset()
+        for rel in (1e-2, 1e-3, 1e-4, 1e-5, 1e-6):
+            mdr.retrieve(rel * rel * norm2, out=out, interpreter=interp, estimator="l2_hb")
+    torch.cuda.synchronize()
+    err = math.sqrt(float(((out.double() - x.double()) ** 2).sum().item()) / norm2)
+    for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
+        print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
+    print("final relative L2 error %.3g" % err)
+
+
+if __name__ == "__main__":
+    main()
