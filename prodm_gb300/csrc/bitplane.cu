@@ -226,19 +226,25 @@ struct GrErr32 {
 
 constexpr int NB_G = 8;   // blocks per warp iteration (one 32-byte sector per plane)
 
-// fp32 negabinary encoder: transpose-based, NB_G consecutive blocks per warp
+// fp32 negabinary encoder. A CTA (8 warps) owns a chunk of NB_CHUNK
+// consecutive 32-value blocks: each warp transposes 32 blocks into a shared
+// [plane][block] tile, then the CTA writes every plane's NB_CHUNK words as one
+// contiguous run (coalesced 128-byte stores instead of 32 scattered sectors).
+constexpr int NB_CHUNK = 256;
+constexpr int NB_TILE_LD = NB_CHUNK + 1;     // padded row: conflict-free column writes
+
 template <bool ERR>
 __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x, uint64_t n,
                                                     const uint32_t* __restrict__ maxkey, int exp_arg, int B,
                                                     uint32_t* __restrict__ out, uint64_t stride,
                                                     double* __restrict__ partial) {
+    __shared__ uint32_t tile[32 * NB_TILE_LD];
     const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;   // NegaBinaryBPEncoder.hpp:21
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t nblocks = (n + 31) / 32;
-    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t nchunks = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
     const int se = B - exp;
-    const bool fast = se >= -126 && se <= 127;
+    const bool fast = pow2_normal(se);
     const float scale = fast ? pow2f(se) : 1.f;
     float acc[32], accx = 0.f;
     if (ERR) {
@@ -246,49 +252,59 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
         for (int k = 0; k < 32; k++) acc[k] = 0.f;
     }
     const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
-    for (uint64_t b0 = gw * NB_G; b0 < nblocks; b0 += nw * NB_G) {
-        float v[NB_G];
-#pragma unroll
-        for (int g = 0; g < NB_G; g++) {
-            const uint64_t i = (b0 + g) * 32 + lane;
-            v[g] = i < n ? __ldcs(x + i) : 0.f;
-        }
-        uint32_t nb[NB_G];
-        float sh[NB_G], d[NB_G];
-#pragma unroll
-        for (int g = 0; g < NB_G; g++) {
-            sh[g] = fast ? v[g] * scale : ldexpf(v[g], se);    // :42
-            const int32_t q = (int32_t)sh[g];
-            nb[g] = nb_from_bin(q);
-            d[g] = sh[g] - (float)q;                             // exact fraction
-        }
-        if (ERR) {
-            // NegaBinaryBPEncoder.hpp:231-239; values past n contribute 0 (shifted = 0)
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t cb0 = c * NB_CHUNK;
+        const uint64_t wb0 = cb0 + (uint64_t)warp * 32;
+#pragma unroll 1
+        for (int j0 = 0; j0 < 32; j0 += NB_G) {
+            float v[NB_G];
 #pragma unroll
             for (int g = 0; g < NB_G; g++) {
-                acc[0] += d[g] * d[g];
-                accx += sh[g] * sh[g];
+                const uint64_t i = (wb0 + j0 + g) * 32 + lane;
+                v[g] = i < n ? __ldcs(x + i) : 0.f;
             }
+            uint32_t nb[NB_G];
+            float sh[NB_G], d[NB_G];
 #pragma unroll
-            for (int k = 1; k < 32; k++) {
-                if (k < B) {
+            for (int g = 0; g < NB_G; g++) {
+                sh[g] = fast ? v[g] * scale : ldexpf(v[g], se);    // :42
+                const int32_t q = (int32_t)sh[g];
+                nb[g] = nb_from_bin(q);
+                d[g] = sh[g] - (float)q;                             // exact fraction
+            }
+            if (ERR) {
+                // NegaBinaryBPEncoder.hpp:231-239; values past n contribute 0
 #pragma unroll
-                    for (int g = 0; g < NB_G; g++) {
-                        if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
-                        acc[k] += d[g] * d[g];
+                for (int g = 0; g < NB_G; g++) {
+                    acc[0] += d[g] * d[g];
+                    accx += sh[g] * sh[g];
+                }
+#pragma unroll
+                for (int k = 1; k < 32; k++) {
+                    if (k < B) {
+#pragma unroll
+                        for (int g = 0; g < NB_G; g++) {
+                            if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
+                            acc[k] += d[g] * d[g];
+                        }
                     }
                 }
             }
-        }
-        uint32_t w[NB_G];
 #pragma unroll
-        for (int g = 0; g < NB_G; g++) w[g] = transpose32(nb[g], lane);
-        if (lane < B) {
-            uint32_t* dst = out + (uint64_t)plane * stride + b0;
-#pragma unroll
-            for (int g = 0; g < NB_G; g++)
-                if (b0 + g < nblocks) dst[g] = w[g];
+            for (int g = 0; g < NB_G; g++) {
+                const uint32_t w = transpose32(nb[g], lane);
+                if (lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
+            }
         }
+        __syncthreads();
+        // write plane rows: warp w handles planes w, w+8, ...
+        const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
+        for (int p = warp; p < B; p += 8) {
+            uint32_t* dst = out + (uint64_t)p * stride + cb0;
+            const uint32_t* row = tile + p * NB_TILE_LD;
+            for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
+        }
+        __syncthreads();
     }
     if (ERR) {
         NbErr32 er;
@@ -299,34 +315,42 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
     }
 }
 
-// fp32 negabinary decoder: planes [s, s+num) at base[(i) * stride]; lane p
-// loads plane p's words, one transpose gives lane e the digits of value e
+// fp32 negabinary decoder, planes [s, s+num) at base[i * stride]: the CTA
+// loads a [plane][block] tile with coalesced loads, then each warp transposes
+// its blocks (lane e receives the digits of value e) and stores coalesced.
 __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict__ base, uint64_t stride, uint64_t n,
                                                     const uint32_t* __restrict__ maxkey, int exp_arg, int s, int num,
                                                     const uint8_t* __restrict__ dnum, float* __restrict__ out) {
+    __shared__ uint32_t tile[32 * NB_TILE_LD];
     if (dnum) num = dnum[0] - s;
     const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;
     const int e = s + num;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t nblocks = (n + 31) / 32;
-    const uint64_t gw = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t nchunks = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
     const bool neg = num != 0 && (e & 1);                   // :153, :177
-    const bool dfast = (exp - e) >= -126 && (exp - e) <= 127;
+    const bool dfast = pow2_normal(exp - e);
     const float dscale = dfast ? pow2f(exp - e) : 1.f;
-    for (uint64_t b0 = gw * NB_G; b0 < nblocks; b0 += nw * NB_G) {
-        uint32_t w[NB_G];
-        const uint32_t* src = base + (uint64_t)lane * stride + b0;
-#pragma unroll
-        for (int g = 0; g < NB_G; g++) w[g] = (lane < num && b0 + g < nblocks) ? __ldg(src + g) : 0u;
-#pragma unroll
-        for (int g = 0; g < NB_G; g++) {
-            const uint32_t col = transpose32(w[g], lane);   // bit i = digit of plane s+i
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t cb0 = c * NB_CHUNK;
+        const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
+        for (int p = warp; p < num; p += 8) {
+            const uint32_t* src = base + (uint64_t)p * stride + cb0;
+            uint32_t* row = tile + p * NB_TILE_LD;
+            for (int j = lane; j < nvalid; j += 32) row[j] = __ldcs(src + j);
+        }
+        __syncthreads();
+        for (int j = 0; j < 32; j++) {
+            const int bl = warp * 32 + j;
+            if (bl >= nvalid) break;
+            const uint32_t w = lane < num ? tile[lane * NB_TILE_LD + bl] : 0u;
+            const uint32_t col = transpose32(w, lane);      // bit i = digit of plane s+i
             const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
-            const float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), -e + exp)) : 0.f;
-            const uint64_t i = (b0 + g) * 32 + lane;
+            const float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
+            const uint64_t i = (cb0 + bl) * 32 + lane;
             if (i < n) out[i] = neg ? -val : val;
         }
+        __syncthreads();
     }
 }
 
@@ -944,10 +968,9 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     const uint64_t nblocks = (n + BS - 1) / BS;
     const int th = 256;
     if (std::is_same<T, float>::value) {
-        const unsigned g32 = (unsigned)kSMs * 4;
-        const uint64_t groups = (nblocks + NB_G - 1) / NB_G;
-        unsigned grid = (unsigned)std::min<uint64_t>(g32, (groups + 7) / 8 ? (groups + 7) / 8 : 1);
-        if (errs_out) grid = (unsigned)kPartialSlots;
+        const uint64_t nch = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
+        unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)kSMs * 8, nch));
+        if (errs_out) grid = (unsigned)std::min<uint64_t>((uint64_t)kPartialSlots, std::max<uint64_t>(1, nch));
         if (errs_out)
             k_nb_encode32<true><<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
                                                      (uint32_t*)out, stride, partial);
@@ -984,8 +1007,8 @@ int launch_nb_decode(const void* base, uint64_t stride, uint64_t n, const void* 
     const uint64_t nblocks = (n + BS - 1) / BS;
     const int th = 256;
     if (std::is_same<T, float>::value) {
-        const uint64_t groups = (nblocks + NB_G - 1) / NB_G;
-        const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)kSMs * 8, (groups + 7) / 8));
+        const uint64_t nch = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
+        const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)kSMs * 8, nch));
         k_nb_decode32<<<grid, th, 0, st>>>((const uint32_t*)base, stride, n, (const uint32_t*)maxkey, exp, s, num, dnum,
                                            (float*)out);
         PRODM_CHECK_LAUNCH("k_nb_decode32");

@@ -55,15 +55,25 @@ __device__ __forceinline__ float interp_f(int mask, Get at) {
     }
 }
 
+__device__ __forceinline__ uint32_t natural_of(uint32_t r, uint32_t n, uint32_t nc) {
+    return r < nc ? fine_of_coarse(r, n, nc) : 2 * (r - nc) + 1;
+}
+
+// CTA = 8 warps = 8 consecutive rows in the reordered (interleaved-rank)
+// order, so the CTA's coefficients form one contiguous rank range: the CTA
+// stages the retrieved planes of that range in shared memory with coalesced
+// loads, decodes them (one transpose per 32-value block) into a shared
+// coefficient buffer, then each warp writes its natural-order output row.
 __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* __restrict__ base, uint64_t stride,
                                                               const uint32_t* __restrict__ maxkey,
                                                               const uint8_t* __restrict__ dnum,
                                                               const float* __restrict__ coarse, Box F, Box C,
                                                               float* __restrict__ out, uint64_t s0, uint64_t s1,
-                                                              uint32_t row_blocks) {
-    extern __shared__ float sbuf[];
+                                                              uint32_t max_blocks) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* tile = smem;                                   // [plane][max_blocks]
+    float* cbuf = (float*)(smem + 32 * max_blocks);          // [max_blocks * 32]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float* buf = sbuf + (size_t)warp * row_blocks * 32;
     const int num = dnum[0];
     const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
     const int e = num;
@@ -73,57 +83,80 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t n2 = F.n[2], c2n = C.n[2];
     const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
-    const uint32_t wpb = blockDim.x >> 5;
-    const uint32_t* pl = base + (uint64_t)lane * stride;   // lane p reads plane p
-    for (uint32_t row = blockIdx.x * wpb + warp; row < rows; row += gridDim.x * wpb) {
-        const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
-        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
-        const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
-        const bool cc = r0 < C.n[0] && r1 < C.n[1];
-        const uint64_t rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
-        const uint32_t len = cc ? n2 - c2n : n2;
-        const uint64_t fb = rbase >> 5, lb = (rbase + len - 1) >> 5;
-        // decode the blocks covering ranks [rbase, rbase + len)
-        for (uint64_t blk = fb; blk <= lb; blk++) {
-            const uint32_t w = lane < num ? __ldg(pl + blk) : 0u;
+    auto row_info = [&](uint32_t rho, uint32_t& r0, uint32_t& r1, bool& cc, uint64_t& rbase, uint32_t& len) {
+        r0 = rho / F.n[1];
+        r1 = rho - r0 * F.n[1];
+        cc = r0 < C.n[0] && r1 < C.n[1];
+        rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
+        len = cc ? n2 - c2n : n2;
+    };
+    for (uint32_t rho0 = blockIdx.x * 8; rho0 < rows; rho0 += gridDim.x * 8) {
+        const uint32_t rho_last = min(rho0 + 7, rows - 1);
+        uint32_t a0, a1, z0, z1, alen, zlen;
+        bool acc_, zcc;
+        uint64_t abase, zbase;
+        row_info(rho0, a0, a1, acc_, abase, alen);
+        row_info(rho_last, z0, z1, zcc, zbase, zlen);
+        const uint64_t fb = abase >> 5, lb = (zbase + zlen - 1) >> 5;
+        const uint32_t nbk = (uint32_t)(lb - fb + 1);
+        // stage the planes of blocks [fb, lb]
+        for (int p = warp; p < num; p += 8) {
+            const uint32_t* src = base + (uint64_t)p * stride + fb;
+            uint32_t* row = tile + p * max_blocks;
+            for (uint32_t j = lane; j < nbk; j += 32) row[j] = __ldcs(src + j);
+        }
+        __syncthreads();
+        for (uint32_t j = warp; j < nbk; j += 8) {
+            const uint32_t w = lane < num ? tile[lane * max_blocks + j] : 0u;
             const uint32_t col = transpose32f(w, lane);
             const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
             float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
-            buf[(blk - fb) * 32 + lane] = neg ? -val : val;
+            cbuf[j * 32 + lane] = neg ? -val : val;
         }
-        __syncwarp();
-        const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
-        const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
-        const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
-        float* orow = out + x0 * s0 + x1 * s1;
-        const uint32_t boff = (uint32_t)(rbase - fb * 32);
-        for (uint32_t x2 = lane; x2 < n2; x2 += 32) {
-            const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
-            const uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, n2, c2n);
-            const float* cb = cb0 + c2;
-            float v;
-            if (mask == 0) {
-                v = *cb;
-            } else {
-                auto at = [&](int d0, int d1, int d2) -> float {
-                    return __ldg(cb + (d0 > 0 ? cs0 : 0) + (d1 > 0 ? cs1 : 0) + (d2 > 0 ? 1 : 0));
-                };
-                const uint32_t r2 = reord(x2, n2, c2n);
-                const float coef = buf[boff + (cc ? r2 - c2n : r2)];
-                v = __fadd_rn(coef, interp_f(mask, at));
+        __syncthreads();
+        const uint32_t rho = rho0 + warp;
+        if (rho < rows) {
+            uint32_t r0, r1, len;
+            bool cc;
+            uint64_t rbase;
+            row_info(rho, r0, r1, cc, rbase, len);
+            const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
+            const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+            const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
+            const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
+            const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
+            float* orow = out + x0 * s0 + x1 * s1;
+            const uint32_t boff = (uint32_t)(rbase - fb * 32);
+            for (uint32_t x2 = lane; x2 < n2; x2 += 32) {
+                const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
+                const uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, n2, c2n);
+                const float* cb = cb0 + c2;
+                float v;
+                if (mask == 0) {
+                    v = *cb;
+                } else {
+                    auto at = [&](int d0, int d1, int d2) -> float {
+                        return __ldg(cb + (d0 > 0 ? cs0 : 0) + (d1 > 0 ? cs1 : 0) + (d2 > 0 ? 1 : 0));
+                    };
+                    const uint32_t r2 = reord(x2, n2, c2n);
+                    const float coef = cbuf[boff + (cc ? r2 - c2n : r2)];
+                    v = __fadd_rn(coef, interp_f(mask, at));
+                }
+                orow[x2] = v;
             }
-            orow[x2] = v;
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
 }  // namespace
 
+static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
+static size_t fused_smem(const Box& F) { return (size_t)fused_max_blocks(F) * 32 * 4 * 2; }
+
 bool decode_recompose_nb32_ok(const Box& F) {
     const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
-    const uint32_t row_blocks = (F.n[2] + 31) / 32 + 2;
-    return rows >= 1024 && (size_t)8 * row_blocks * 32 * sizeof(float) <= 200 * 1024;
+    return rows >= 1024 && fused_smem(F) <= 200 * 1024;
 }
 
 // Returns PRODM_EUNSUPPORTED when the shape does not suit the row mapping
@@ -131,20 +164,19 @@ bool decode_recompose_nb32_ok(const Box& F) {
 int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* maxkey, const uint8_t* dnum,
                                  const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
                                  cudaStream_t st) {
-    const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
-    const uint32_t row_blocks = (F.n[2] + 31) / 32 + 2;
-    const size_t smem = (size_t)8 * row_blocks * 32 * sizeof(float);
-    if (rows < 1024 || smem > 200 * 1024) return PRODM_EUNSUPPORTED;
+    if (!decode_recompose_nb32_ok(F)) return PRODM_EUNSUPPORTED;
+    const size_t smem = fused_smem(F);
     if (smem > 48 * 1024) {   // per device; cheap to repeat
         cudaError_t e = cudaFuncSetAttribute(k_decode_recompose_nb32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              200 * 1024);
         if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
     }
+    const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
     const uint64_t need = (rows + 7) / 8;
-    const uint64_t cap = (uint64_t)kSMs * 8;
+    const uint64_t cap = (uint64_t)kSMs * 6;
     const unsigned grid = (unsigned)(need < cap ? need : cap);
     k_decode_recompose_nb32<<<grid, 256, smem, st>>>((const uint32_t*)base, stride, (const uint32_t*)maxkey, dnum,
-                                                     coarse, F, C, out, s0, s1, row_blocks);
+                                                     coarse, F, C, out, s0, s1, fused_max_blocks(F));
     PRODM_CHECK_LAUNCH("k_decode_recompose_nb32");
     return PRODM_OK;
 }
