@@ -128,6 +128,32 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
+// ---------------------------------------------------------------------------
+// Column-pair form of the multilinear interpolation used by the row kernels.
+// For a fine row (x0, x1) with odd-dim mask m01 over dims 0/1, the corner rows
+// are: m01 = 0 -> 1 row; 1 -> (lo, hi) along dim 0; 2 -> (lo, hi) along dim 1;
+// 3 -> (lo,lo), (lo,hi), (hi,lo), (hi,hi). q holds the corner values at one
+// coarse column, qn those at the next coarse column. The even node of the
+// column interpolates as tree(q); the odd node between the two columns as
+// tree(avg(q, qn)): exactly the operation order of interp() (dim 0 outermost,
+// dim 2 innermost), without lane divergence.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T avg_rn(T a, T b) { return mul_rn((T)0.5, add_rn(a, b)); }
+template <class T>
+__device__ __forceinline__ T corner_tree(int m01, const T* q) {
+    if (m01 == 0) return q[0];
+    if (m01 != 3) return avg_rn(q[0], q[1]);
+    return avg_rn(avg_rn(q[0], q[1]), avg_rn(q[2], q[3]));
+}
+template <class T>
+__device__ __forceinline__ T corner_tree_mid(int m01, const T* q, const T* qn) {
+    if (m01 == 0) return avg_rn(q[0], qn[0]);
+    if (m01 != 3) return avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1]));
+    return avg_rn(avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])), avg_rn(avg_rn(q[2], qn[2]), avg_rn(q[3], qn[3])));
+}
+__host__ __device__ inline int corner_count(int m01) { return m01 == 0 ? 1 : (m01 == 3 ? 4 : 2); }
+
 // |x| of a non-negative float/double as an order-preserving unsigned key
 __device__ __forceinline__ uint32_t abs_key(float v) { return __float_as_uint(v) & 0x7fffffffu; }
 __device__ __forceinline__ unsigned long long abs_key(double v) {

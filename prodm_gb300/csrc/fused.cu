@@ -35,26 +35,6 @@ __device__ __forceinline__ uint32_t transpose32f(uint32_t x, int lane) {
 
 __device__ __forceinline__ float pow2f_(int e) { return __int_as_float((e + 127) << 23); }
 
-template <class Get>
-__device__ __forceinline__ float interp_f(int mask, Get at) {
-    const float h = 0.5f;
-    auto avg = [&](float a, float b) { return __fmul_rn(h, __fadd_rn(a, b)); };
-    switch (mask) {
-        case 1: return avg(at(-1, 0, 0), at(1, 0, 0));
-        case 2: return avg(at(0, -1, 0), at(0, 1, 0));
-        case 4: return avg(at(0, 0, -1), at(0, 0, 1));
-        case 3: return avg(avg(at(-1, -1, 0), at(-1, 1, 0)), avg(at(1, -1, 0), at(1, 1, 0)));
-        case 5: return avg(avg(at(-1, 0, -1), at(-1, 0, 1)), avg(at(1, 0, -1), at(1, 0, 1)));
-        case 6: return avg(avg(at(0, -1, -1), at(0, -1, 1)), avg(at(0, 1, -1), at(0, 1, 1)));
-        case 7: {
-            float a = avg(avg(at(-1, -1, -1), at(-1, -1, 1)), avg(at(-1, 1, -1), at(-1, 1, 1)));
-            float b = avg(avg(at(1, -1, -1), at(1, -1, 1)), avg(at(1, 1, -1), at(1, 1, 1)));
-            return avg(a, b);
-        }
-        default: return 0.f;
-    }
-}
-
 __device__ __forceinline__ uint32_t natural_of(uint32_t r, uint32_t n, uint32_t nc) {
     return r < nc ? fine_of_coarse(r, n, nc) : 2 * (r - nc) + 1;
 }
@@ -125,24 +105,32 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
             const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
             const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
             const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
+            int64_t co[4];
+            if (m01 == 0) { co[0] = 0; }
+            else if (m01 == 1) { co[0] = 0; co[1] = (int64_t)cs0; }
+            else if (m01 == 2) { co[0] = 0; co[1] = (int64_t)cs1; }
+            else { co[0] = 0; co[1] = (int64_t)cs1; co[2] = (int64_t)cs0; co[3] = (int64_t)(cs0 + cs1); }
+            const int nq = corner_count(m01);
             float* orow = out + x0 * s0 + x1 * s1;
-            const uint32_t boff = (uint32_t)(rbase - fb * 32);
-            for (uint32_t x2 = lane; x2 < n2; x2 += 32) {
-                const int mask = m01 | (is_coarse(x2, n2) ? 0 : 4);
-                const uint32_t c2 = (mask & 4) ? (x2 >> 1) : reord(x2, n2, c2n);
-                const float* cb = cb0 + c2;
-                float v;
-                if (mask == 0) {
-                    v = *cb;
-                } else {
-                    auto at = [&](int d0, int d1, int d2) -> float {
-                        return __ldg(cb + (d0 > 0 ? cs0 : 0) + (d1 > 0 ? cs1 : 0) + (d2 > 0 ? 1 : 0));
-                    };
-                    const uint32_t r2 = reord(x2, n2, c2n);
-                    const float coef = cbuf[boff + (cc ? r2 - c2n : r2)];
-                    v = __fadd_rn(coef, interp_f(mask, at));
+            const float* crow = cbuf + (rbase - fb * 32);
+            for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
+                const uint32_t c2 = cbase + lane;
+                const bool act = c2 < c2n;
+                const bool odd = act && c2 + 1 < c2n && fine_of_coarse(c2 + 1, n2, c2n) == 2 * c2 + 2;
+                float q[4] = {0.f, 0.f, 0.f, 0.f}, qn[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    if (i < nq && act) q[i] = __ldg(cb0 + c2 + co[i]);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    qn[i] = __shfl_down_sync(FULL, q[i], 1);
+                    if (i < nq && lane == 31 && odd) qn[i] = __ldg(cb0 + c2 + 1 + co[i]);
                 }
-                orow[x2] = v;
+                if (act) {
+                    const uint32_t xe = fine_of_coarse(c2, n2, c2n);
+                    orow[xe] = m01 == 0 ? q[0] : __fadd_rn(crow[cc ? c2 - c2n : c2], corner_tree(m01, q));
+                    if (odd) orow[2 * c2 + 1] = __fadd_rn(crow[cc ? c2 : c2n + c2], corner_tree_mid(m01, q, qn));
+                }
             }
         }
         __syncthreads();

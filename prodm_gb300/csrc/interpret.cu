@@ -87,21 +87,54 @@ struct DevHeap {
     }
 };
 
+// Efficiency of taking planes starting at index idx of level l. Every
+// estimator ignores its base argument, so this depends on (l, idx) only and is
+// tabulated once per call by the whole CTA.
+//   kinds 0 / 1: gain(E[idx], E[idx+1]) / sizes[idx]
+//   kind 2:      estimated_efficiency (GreedyBasedSizeInterpreter.hpp:228-248),
+//                the look-ahead over consecutive planes with u32 size sums
+template <class T>
+__device__ void eff_entry(int kind, const DevEstimator<T>& est, int B, const uint32_t* sizes, const double* errs, int l,
+                          int idx, double& u, int& num) {
+    auto E = [&](int lv, int j) { return errs[(size_t)lv * (B + 1) + j]; };
+    auto S = [&](int lv, int j) { return sizes[(size_t)lv * B + j]; };
+    double cg = est.gain((T)E(l, idx), (T)E(l, idx + 1), l);
+    uint32_t cs = S(l, idx);
+    double ce = cg / cs;
+    int cn = 1;
+    if (kind == 2) {
+        for (int i = 2; i < B - idx; i++) {
+            double ng = est.gain((T)E(l, idx), (T)E(l, idx + i), l);
+            uint32_t ns = cs + S(l, idx + i - 1);
+            double ne = ng / ns;
+            if ((ce > 0) && (ce > ne)) break;
+            cg = ng;
+            ce = ne;
+            cs = ns;
+            cn = i;
+        }
+    }
+    u = ce;
+    num = cn;
+}
+
 template <class T>
 __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int B, const uint32_t* __restrict__ sizes,
-                               const double* __restrict__ errs, double tol, uint8_t* index, uint32_t* rsz) {
+                               const double* __restrict__ errs, const double* __restrict__ eu,
+                               const int8_t* __restrict__ en, double tol, uint8_t* index, uint32_t* rsz) {
     auto E = [&](int l, int j) { return errs[(size_t)l * (B + 1) + j]; };
     auto S = [&](int l, int j) { return sizes[(size_t)l * B + j]; };
+    auto item = [&](int l, int j) { return Item{eu[l * 64 + j], l, (int)en[l * 64 + j]}; };
     for (int i = 0; i < nl; i++) rsz[i] = 0;
     double acc = 0;
     for (int i = 0; i < nl; i++) acc += est.est((T)E(i, index[i]), i);
     DevHeap heap;
     heap.len = 0;
     if (kind == 0) {
-        for (int i = 0; i < nl; i++) {
-            double g = est.gain((T)E(i, index[i]), (T)E(i, index[i] + 1), i);
-            heap.push({g / S(i, index[i]), i, 1});
-        }
+        // a fully retrieved level has no next plane (the reference would read
+        // past its error table here); it is not pushed
+        for (int i = 0; i < nl; i++)
+            if (index[i] != B) heap.push(item(i, index[i]));
         bool met = false;
         while (!met && heap.len > 0) {
             Item t = heap.h[0];
@@ -112,10 +145,7 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
             acc += est.est((T)E(i, j + 1), i);
             if (acc < tol) met = true;
             index[i]++;
-            if (index[i] != B) {
-                double g = est.gain((T)E(i, index[i]), (T)E(i, index[i] + 1), i);
-                heap.push({g / S(i, index[i]), i, 1});
-            }
+            if (index[i] != B) heap.push(item(i, index[i]));
         }
         return;
     }
@@ -131,10 +161,7 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
                 acc += est.est((T)E(i, 1), i);
                 index[i]++;
             }
-            if (index[i] != B) {
-                double g = est.gain((T)E(i, index[i]), (T)E(i, index[i] + 1), i);
-                heap.push({g / S(i, index[i]), i, 1});
-            }
+            if (index[i] != B) heap.push(item(i, index[i]));
             if (minerr < tol) break;
         }
         bool met = acc < tol;
@@ -147,63 +174,12 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
             acc += est.est((T)E(i, j + 1), i);
             if (acc < tol) met = true;
             index[i]++;
-            if (index[i] != B) {
-                double g = est.gain((T)E(i, index[i]), (T)E(i, index[i] + 1), i);
-                heap.push({g / S(i, index[i]), i, 1});
-            }
+            if (index[i] != B) heap.push(item(i, index[i]));
         }
         return;
     }
-    // estimated_efficiency (GreedyBasedSizeInterpreter.hpp:228-248), warp-parallel:
-    // candidate i (run of i planes) has efficiency gain(E[idx], E[idx+i]) /
-    // (sizes[idx] + ... + sizes[idx+i-1]) with the reference's u32 size sums;
-    // the sequential loop stops at the first i >= 2 whose predecessor is
-    // positive and larger, which a ballot finds directly.
-    const int lane = threadIdx.x & 31;
-    auto eff = [&](int idx, int l) {
-        const int cnt = B - idx - 1;             // largest candidate run the loop visits
-        uint32_t carry = 0;
-        double prev_last = 0.0;
-        int cn = -1;
-        double ce = 0.0;
-        for (int base = 0; base <= (cnt > 1 ? cnt : 1); base += 32) {
-            const int i = base + lane;
-            uint32_t sz = (i >= 1 && idx + i - 1 < B) ? S(l, idx + i - 1) : 0u;
-            uint32_t incl = sz;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            const uint32_t ns = carry + incl;
-            double ne = 0.0;
-            if (i >= 1 && idx + i <= B) ne = (double)est.gain((T)E(l, idx), (T)E(l, idx + i), l) / ns;
-            double prev = __shfl_up_sync(0xffffffffu, ne, 1);
-            if (lane == 0) prev = prev_last;
-            const bool stop = i >= 2 && i <= cnt && (prev > 0) && (prev > ne);
-            const unsigned m = __ballot_sync(0xffffffffu, stop);
-            if (m) {
-                const int bi = base + __ffs(m) - 1;      // first stopping candidate
-                cn = bi - 1;
-                const int src = cn - base;
-                const double a = __shfl_sync(0xffffffffu, ne, src < 0 ? 0 : src);
-                ce = src < 0 ? prev_last : a;
-                break;
-            }
-            prev_last = __shfl_sync(0xffffffffu, ne, 31);
-            carry = __shfl_sync(0xffffffffu, ns, 31);
-        }
-        if (cn < 0) {
-            cn = cnt >= 2 ? cnt : 1;
-            // efficiency of the accepted run cn (recomputed, same expression)
-            uint32_t tot = 0;
-            for (int j = 0; j < cn; j++) tot += S(l, idx + j);
-            ce = (double)est.gain((T)E(l, idx), (T)E(l, idx + cn), l) / tot;
-        }
-        return Item{ce, l, cn};
-    };
     for (int i = 0; i < nl; i++)
-        if (index[i] != B) heap.push(eff(index[i], i));
+        if (index[i] != B) heap.push(item(i, index[i]));
     bool met = acc < tol;
     if (met) return;
     while (!met && heap.len > 0) {
@@ -215,45 +191,51 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
         acc += est.est((T)E(i, j + num), i);
         if (acc < tol) met = true;
         index[i] += num;
-        if (index[i] != B) heap.push(eff(index[i], i));
+        if (index[i] != B) heap.push(item(i, index[i]));
     }
 }
 
-// all lanes of the warp run the same sequence on private copies; lane 0 stores
+// one CTA per field: all threads tabulate the efficiencies, thread 0 runs the
+// sequential heap walk on the staged tables
 template <class T>
-__device__ void interpret_one(int kind, const DevEstimator<T>& est, int nl, int B, const uint32_t* __restrict__ sizes,
-                              const double* __restrict__ errs, double tol, uint8_t* __restrict__ index_io,
-                              uint32_t* __restrict__ rsz_io) {
-    uint8_t index[kMaxLevels];
-    uint32_t rsz[kMaxLevels];
-    for (int i = 0; i < nl; i++) index[i] = index_io[i];
-    interpret_core<T>(kind, est, nl, B, sizes, errs, tol, index, rsz);
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0)
-        for (int i = 0; i < nl; i++) { index_io[i] = index[i]; rsz_io[i] = rsz[i]; }
-}
-
-// one thread per field: field f uses sizes + f*sz_stride etc.
-template <class T>
-__global__ void k_interpret(int nfields, int kind, int est_kind, const int* __restrict__ ndims,
-                            const int* __restrict__ levels, double s, int B, const uint32_t* __restrict__ sizes,
-                            uint64_t sz_stride, const double* __restrict__ errs, uint64_t err_stride,
-                            const double* __restrict__ tols, double tol0, uint8_t* __restrict__ index,
-                            uint64_t idx_stride, uint32_t* __restrict__ rsz) {
-    const int f = blockIdx.x;              // one warp per field; all lanes run the same steps
+__global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int est_kind, const int* __restrict__ ndims,
+                                                   const int* __restrict__ levels, double s, int B,
+                                                   const uint32_t* __restrict__ sizes, uint64_t sz_stride,
+                                                   const double* __restrict__ errs, uint64_t err_stride,
+                                                   const double* __restrict__ tols, double tol0,
+                                                   uint8_t* __restrict__ index, uint64_t idx_stride,
+                                                   uint32_t* __restrict__ rsz) {
+    const int f = blockIdx.x;
     if (f >= nfields) return;
-    int L = levels[f];
-    DevEstimator<T> est;
-    est.init(est_kind, ndims[f], L, s);
-    // stage this field's size and error tables in shared memory (latency)
+    const int L = levels[f];
+    const int nl = L + 1;
     __shared__ uint32_t s_sizes[kMaxLevels * 64];
     __shared__ double s_errs[kMaxLevels * 65];
-    const int nl = L + 1;
+    __shared__ double s_eu[kMaxLevels * 64];
+    __shared__ int8_t s_en[kMaxLevels * 64];
     for (int i = threadIdx.x; i < nl * B; i += blockDim.x) s_sizes[i] = sizes[f * sz_stride + i];
     for (int i = threadIdx.x; i < nl * (B + 1); i += blockDim.x) s_errs[i] = errs[f * err_stride + i];
-    __syncwarp();
-    interpret_one<T>(kind, est, L + 1, B, s_sizes, s_errs, tols ? tols[f] : tol0, index + f * idx_stride,
-                     rsz + f * idx_stride);
+    DevEstimator<T> est;
+    est.init(est_kind, ndims[f], L, s);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nl * B; t += blockDim.x) {
+        const int l = t / B, j = t - l * B;
+        double u;
+        int num;
+        eff_entry<T>(kind, est, B, s_sizes, s_errs, l, j, u, num);
+        s_eu[l * 64 + j] = u;
+        s_en[l * 64 + j] = (int8_t)num;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint8_t idx[kMaxLevels];
+        uint32_t rs[kMaxLevels];
+        uint8_t* gi = index + f * idx_stride;
+        for (int i = 0; i < nl; i++) idx[i] = gi[i];
+        interpret_core<T>(kind, est, nl, B, s_sizes, s_errs, s_eu, s_en, tols ? tols[f] : tol0, idx, rs);
+        uint32_t* gr = rsz + f * idx_stride;
+        for (int i = 0; i < nl; i++) { gi[i] = idx[i]; gr[i] = rs[i]; }
+    }
 }
 
 }  // namespace
@@ -263,7 +245,7 @@ int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, co
                      const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
                      cudaStream_t st) {
-    k_interpret<T><<<nfields, 32, 0, st>>>(nfields, kind, est_kind, d_ndims, d_levels, s, B, d_sizes,
+    k_interpret<T><<<nfields, 256, 0, st>>>(nfields, kind, est_kind, d_ndims, d_levels, s, B, d_sizes,
                                                            sz_stride, d_errs, err_stride, d_tols, tol0, d_index,
                                                            idx_stride, d_rsz);
     PRODM_CHECK_LAUNCH("k_interpret");
