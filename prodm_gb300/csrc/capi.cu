@@ -524,16 +524,26 @@ struct Stage {
     int id;
     cudaEvent_t a = nullptr, b = nullptr;
     cudaStream_t st;
+    bool capturing = false;
     Stage(prodm_mdr* h_, int kind, int level, cudaStream_t st_) : h(h_), id(kind * 17 + level), st(st_) {
         if (h->timing) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            cudaStreamIsCapturing(st, &cs);
+            capturing = cs == cudaStreamCaptureStatusActive;
             a = h->ev();
             b = h->ev();
-            cudaEventRecord(a, st);
+            record(a);
         }
+    }
+    // inside a stream capture the records become external event nodes, which
+    // every replay of the graph records and the host can time
+    void record(cudaEvent_t e) {
+        if (capturing) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+        else cudaEventRecord(e, st);
     }
     ~Stage() {
         if (a) {
-            cudaEventRecord(b, st);
+            record(b);
             h->pending.push_back({id, a, b});
         }
     }

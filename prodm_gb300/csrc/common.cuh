@@ -154,6 +154,24 @@ __device__ __forceinline__ T corner_tree_mid(int m01, const T* q, const T* qn) {
 }
 __host__ __device__ inline int corner_count(int m01) { return m01 == 0 ? 1 : (m01 == 3 ? 4 : 2); }
 
+// 32 x 32 bit transpose held in one thread's registers: on exit a[k] bit e =
+// bit k of the entry a[e] (five butterfly stages of 16 pair swaps)
+__device__ __forceinline__ void transpose32_regs(uint32_t (&a)[32]) {
+#pragma unroll
+    for (int s = 0; s < 5; s++) {
+        const int j = 16 >> s;
+        const uint32_t m = s == 0 ? 0x0000ffffu : s == 1 ? 0x00ff00ffu : s == 2 ? 0x0f0f0f0fu : s == 3 ? 0x33333333u
+                                                                                                     : 0x55555555u;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int k = (i / j) * 2 * j + (i % j);
+            const uint32_t t = ((a[k] >> j) ^ a[k + j]) & m;
+            a[k + j] ^= t;
+            a[k] ^= t << j;
+        }
+    }
+}
+
 // |x| of a non-negative float/double as an order-preserving unsigned key
 __device__ __forceinline__ uint32_t abs_key(float v) { return __float_as_uint(v) & 0x7fffffffu; }
 __device__ __forceinline__ unsigned long long abs_key(double v) {

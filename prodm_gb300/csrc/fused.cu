@@ -52,7 +52,8 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
                                                               uint32_t max_blocks) {
     extern __shared__ uint32_t smem[];
     uint32_t* tile = smem;                                   // [plane][max_blocks]
-    float* cbuf = (float*)(smem + 32 * max_blocks);          // [max_blocks * 32]
+    const uint32_t pad = max_blocks | 1u;                    // odd row length: conflict-free
+    float* cbuf = (float*)(smem + 32 * max_blocks);          // [32][pad]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int num = dnum[0];
     const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
@@ -86,12 +87,19 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
             for (uint32_t j = lane; j < nbk; j += 32) row[j] = __ldcs(src + j);
         }
         __syncthreads();
-        for (uint32_t j = warp; j < nbk; j += 8) {
-            const uint32_t w = lane < num ? tile[lane * max_blocks + j] : 0u;
-            const uint32_t col = transpose32f(w, lane);
-            const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
-            float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
-            cbuf[j * 32 + lane] = neg ? -val : val;
+        // one thread per 32-value block: register transpose of the block's
+        // plane words; value e of block t goes to cbuf[e * pad + t]
+        for (uint32_t t = threadIdx.x; t < nbk; t += blockDim.x) {
+            uint32_t a[32];
+#pragma unroll
+            for (int p = 0; p < 32; p++) a[p] = p < num ? tile[p * max_blocks + t] : 0u;
+            transpose32_regs(a);
+#pragma unroll
+            for (int v = 0; v < 32; v++) {
+                const uint32_t acc = num ? (__brev(a[v]) >> (32 - num)) : 0u;
+                float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
+                cbuf[v * pad + t] = neg ? -val : val;
+            }
         }
         __syncthreads();
         const uint32_t rho = rho0 + warp;
@@ -112,7 +120,8 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
             else { co[0] = 0; co[1] = (int64_t)cs1; co[2] = (int64_t)cs0; co[3] = (int64_t)(cs0 + cs1); }
             const int nq = corner_count(m01);
             float* orow = out + x0 * s0 + x1 * s1;
-            const float* crow = cbuf + (rbase - fb * 32);
+            const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
+            auto coefat = [&](uint32_t off) { const uint32_t r = rb0 + off; return cbuf[(r & 31) * pad + (r >> 5)]; };
             for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
                 const uint32_t c2 = cbase + lane;
                 const bool act = c2 < c2n;
@@ -128,8 +137,8 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
                 }
                 if (act) {
                     const uint32_t xe = fine_of_coarse(c2, n2, c2n);
-                    orow[xe] = m01 == 0 ? q[0] : __fadd_rn(crow[cc ? c2 - c2n : c2], corner_tree(m01, q));
-                    if (odd) orow[2 * c2 + 1] = __fadd_rn(crow[cc ? c2 : c2n + c2], corner_tree_mid(m01, q, qn));
+                    orow[xe] = m01 == 0 ? q[0] : __fadd_rn(coefat(cc ? c2 - c2n : c2), corner_tree(m01, q));
+                    if (odd) orow[2 * c2 + 1] = __fadd_rn(coefat(cc ? c2 : c2n + c2), corner_tree_mid(m01, q, qn));
                 }
             }
         }
@@ -140,7 +149,10 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
 }  // namespace
 
 static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
-static size_t fused_smem(const Box& F) { return (size_t)fused_max_blocks(F) * 32 * 4 * 2; }
+static size_t fused_smem(const Box& F) {
+    const uint32_t mb = fused_max_blocks(F);
+    return (size_t)mb * 32 * 4 + (size_t)(mb | 1u) * 32 * 4;
+}
 
 bool decode_recompose_nb32_ok(const Box& F) {
     const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
