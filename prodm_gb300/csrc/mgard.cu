@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
         const int nq = corner_count(m01);
         T* frow = fnat ? fnat + (uint64_t)row * n2 : nullptr;
         T* crow = coarse + ((uint64_t)r0 * C.n[1] + r1) * c2n;
+#pragma unroll 3
         for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
             const uint32_t c2 = cbase + lane;
             const bool act = c2 < c2n;
@@ -279,6 +280,7 @@ __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ co
         corner_offsets(m01, 0, (int64_t)cs0, 0, (int64_t)cs1, co);
         const int nq = corner_count(m01);
         T* orow = out + x0 * s0 + x1 * s1;
+#pragma unroll 3
         for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
             const uint32_t c2 = cbase + lane;
             const bool act = c2 < c2n;
