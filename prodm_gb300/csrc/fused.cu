@@ -19,28 +19,42 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+__device__ __forceinline__ uint32_t transpose32f(uint32_t x, int lane) {
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
+                                                                                                       : 0x55555555u;
+        const uint32_t y = __shfl_xor_sync(FULL, x, j);
+        const bool hi = (lane & j) != 0;
+        const uint32_t u = hi ? y : x, v = hi ? x : y;
+        const uint32_t t = ((u >> j) ^ v) & m;
+        x ^= hi ? t : (t << j);
+    }
+    return x;
+}
+
 __device__ __forceinline__ float pow2f_(int e) { return __int_as_float((e + 127) << 23); }
 
 __device__ __forceinline__ uint32_t natural_of(uint32_t r, uint32_t n, uint32_t nc) {
     return r < nc ? fine_of_coarse(r, n, nc) : 2 * (r - nc) + 1;
 }
 
-// One warp per fine row, rows taken in the reordered (interleaved-rank) order
-// so that neighbouring warps read neighbouring stream words. The row's
-// coefficients are one contiguous rank run [rbase, rbase + len): lane j owns
-// block fb + j of the run, loads that block's retrieved plane words (one
-// coalesced load per plane across the lanes), transposes them in registers
-// and leaves the 32 decoded values in the warp's shared buffer; the warp then
-// writes the recomposed natural-order row. No CTA-wide barrier is involved.
+// CTA = 8 warps = 8 consecutive rows in the reordered (interleaved-rank)
+// order, so the CTA's coefficients form one contiguous rank range: the CTA
+// stages the retrieved planes of that range in shared memory with coalesced
+// loads, decodes them (one transpose per 32-value block) into a shared
+// coefficient buffer, then each warp writes its natural-order output row.
 __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* __restrict__ base, uint64_t stride,
                                                               const uint32_t* __restrict__ maxkey,
                                                               const uint8_t* __restrict__ dnum,
                                                               const float* __restrict__ coarse, Box F, Box C,
                                                               float* __restrict__ out, uint64_t s0, uint64_t s1,
-                                                              uint32_t padw) {
-    extern __shared__ float sbuf[];
+                                                              uint32_t max_blocks) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* tile = smem;                                   // [plane][max_blocks]
+    const uint32_t pad = max_blocks | 1u;                    // odd row length: conflict-free
+    float* cbuf = (float*)(smem + 32 * max_blocks);          // [32][pad]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float* wbuf = sbuf + (size_t)warp * 32 * padw;          // [32][padw], padw odd
     const int num = dnum[0];
     const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
     const int e = num;
@@ -50,73 +64,95 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t n2 = F.n[2], c2n = C.n[2];
     const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
-    const uint32_t wpb = blockDim.x >> 5;
-    for (uint32_t rho = blockIdx.x * wpb + warp; rho < rows; rho += gridDim.x * wpb) {
-        const uint32_t r0 = rho / F.n[1], r1 = rho - r0 * F.n[1];
-        const bool cc = r0 < C.n[0] && r1 < C.n[1];
-        const uint64_t rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
-        const uint32_t len = cc ? n2 - c2n : n2;
-        const uint64_t fb = rbase >> 5, lb = (rbase + len - 1) >> 5;
+    auto row_info = [&](uint32_t rho, uint32_t& r0, uint32_t& r1, bool& cc, uint64_t& rbase, uint32_t& len) {
+        r0 = rho / F.n[1];
+        r1 = rho - r0 * F.n[1];
+        cc = r0 < C.n[0] && r1 < C.n[1];
+        rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
+        len = cc ? n2 - c2n : n2;
+    };
+    for (uint32_t rho0 = blockIdx.x * 8; rho0 < rows; rho0 += gridDim.x * 8) {
+        const uint32_t rho_last = min(rho0 + 7, rows - 1);
+        uint32_t a0, a1, z0, z1, alen, zlen;
+        bool acc_, zcc;
+        uint64_t abase, zbase;
+        row_info(rho0, a0, a1, acc_, abase, alen);
+        row_info(rho_last, z0, z1, zcc, zbase, zlen);
+        const uint64_t fb = abase >> 5, lb = (zbase + zlen - 1) >> 5;
         const uint32_t nbk = (uint32_t)(lb - fb + 1);
-        for (uint32_t bb = 0; bb < nbk; bb += 32) {
-            const uint32_t j = bb + lane;
-            const bool act = j < nbk;
+        // stage the planes of blocks [fb, lb]
+        for (int p = warp; p < num; p += 8) {
+            const uint32_t* src = base + (uint64_t)p * stride + fb;
+            uint32_t* row = tile + p * max_blocks;
+            for (uint32_t j = lane; j < nbk; j += 32) row[j] = __ldcs(src + j);
+        }
+        __syncthreads();
+        // one thread per 32-value block: register transpose of the block's
+        // plane words; value e of block t goes to cbuf[e * pad + t]
+        for (uint32_t t = threadIdx.x; t < nbk; t += blockDim.x) {
             uint32_t a[32];
-            const uint32_t* src = base + fb + j;
 #pragma unroll
-            for (int p = 0; p < 32; p++) a[p] = (p < num && act) ? __ldg(src + (uint64_t)p * stride) : 0u;
+            for (int p = 0; p < 32; p++) a[p] = p < num ? tile[p * max_blocks + t] : 0u;
             transpose32_regs(a);
-            if (act) {
 #pragma unroll
-                for (int v = 0; v < 32; v++) {
-                    const uint32_t acc = num ? (__brev(a[v]) >> (32 - num)) : 0u;
-                    float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
-                    wbuf[v * padw + j] = neg ? -val : val;
+            for (int v = 0; v < 32; v++) {
+                const uint32_t acc = num ? (__brev(a[v]) >> (32 - num)) : 0u;
+                float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
+                cbuf[v * pad + t] = neg ? -val : val;
+            }
+        }
+        __syncthreads();
+        const uint32_t rho = rho0 + warp;
+        if (rho < rows) {
+            uint32_t r0, r1, len;
+            bool cc;
+            uint64_t rbase;
+            row_info(rho, r0, r1, cc, rbase, len);
+            const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
+            const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+            const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
+            const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
+            const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
+            int64_t co[4];
+            if (m01 == 0) { co[0] = 0; }
+            else if (m01 == 1) { co[0] = 0; co[1] = (int64_t)cs0; }
+            else if (m01 == 2) { co[0] = 0; co[1] = (int64_t)cs1; }
+            else { co[0] = 0; co[1] = (int64_t)cs1; co[2] = (int64_t)cs0; co[3] = (int64_t)(cs0 + cs1); }
+            const int nq = corner_count(m01);
+            float* orow = out + x0 * s0 + x1 * s1;
+            const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
+            auto coefat = [&](uint32_t off) { const uint32_t r = rb0 + off; return cbuf[(r & 31) * pad + (r >> 5)]; };
+            for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
+                const uint32_t c2 = cbase + lane;
+                const bool act = c2 < c2n;
+                const bool odd = act && c2 + 1 < c2n && fine_of_coarse(c2 + 1, n2, c2n) == 2 * c2 + 2;
+                float q[4] = {0.f, 0.f, 0.f, 0.f}, qn[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    if (i < nq && act) q[i] = __ldg(cb0 + c2 + co[i]);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    qn[i] = __shfl_down_sync(FULL, q[i], 1);
+                    if (i < nq && lane == 31 && odd) qn[i] = __ldg(cb0 + c2 + 1 + co[i]);
+                }
+                if (act) {
+                    const uint32_t xe = fine_of_coarse(c2, n2, c2n);
+                    orow[xe] = m01 == 0 ? q[0] : __fadd_rn(coefat(cc ? c2 - c2n : c2), corner_tree(m01, q));
+                    if (odd) orow[2 * c2 + 1] = __fadd_rn(coefat(cc ? c2 : c2n + c2), corner_tree_mid(m01, q, qn));
                 }
             }
         }
-        __syncwarp();
-        const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
-        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
-        const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
-        const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
-        const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
-        int64_t co[4];
-        if (m01 == 0) { co[0] = 0; }
-        else if (m01 == 1) { co[0] = 0; co[1] = (int64_t)cs0; }
-        else if (m01 == 2) { co[0] = 0; co[1] = (int64_t)cs1; }
-        else { co[0] = 0; co[1] = (int64_t)cs1; co[2] = (int64_t)cs0; co[3] = (int64_t)(cs0 + cs1); }
-        const int nq = corner_count(m01);
-        float* orow = out + x0 * s0 + x1 * s1;
-        const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
-        auto coefat = [&](uint32_t off) { const uint32_t r = rb0 + off; return wbuf[(r & 31) * padw + (r >> 5)]; };
-        for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
-            const uint32_t c2 = cbase + lane;
-            const bool act = c2 < c2n;
-            const bool odd = act && c2 + 1 < c2n && fine_of_coarse(c2 + 1, n2, c2n) == 2 * c2 + 2;
-            float q[4] = {0.f, 0.f, 0.f, 0.f}, qn[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-                if (i < nq && act) q[i] = __ldg(cb0 + c2 + co[i]);
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                qn[i] = __shfl_down_sync(FULL, q[i], 1);
-                if (i < nq && lane == 31 && odd) qn[i] = __ldg(cb0 + c2 + 1 + co[i]);
-            }
-            if (act) {
-                const uint32_t xe = fine_of_coarse(c2, n2, c2n);
-                orow[xe] = m01 == 0 ? q[0] : __fadd_rn(coefat(cc ? c2 - c2n : c2), corner_tree(m01, q));
-                if (odd) orow[2 * c2 + 1] = __fadd_rn(coefat(cc ? c2 : c2n + c2), corner_tree_mid(m01, q, qn));
-            }
-        }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
 }  // namespace
 
-static uint32_t fused_padw(const Box& F) { return ((F.n[2] + 31) / 32 + 2) | 1u; }
-static size_t fused_smem(const Box& F) { return (size_t)8 * 32 * fused_padw(F) * 4; }
+static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
+static size_t fused_smem(const Box& F) {
+    const uint32_t mb = fused_max_blocks(F);
+    return (size_t)mb * 32 * 4 + (size_t)(mb | 1u) * 32 * 4;
+}
 
 bool decode_recompose_nb32_ok(const Box& F) {
     const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
@@ -137,10 +173,10 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* 
     }
     const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
     const uint64_t need = (rows + 7) / 8;
-    const uint64_t cap = (uint64_t)kSMs * 8;
+    const uint64_t cap = (uint64_t)kSMs * 6;
     const unsigned grid = (unsigned)(need < cap ? need : cap);
     k_decode_recompose_nb32<<<grid, 256, smem, st>>>((const uint32_t*)base, stride, (const uint32_t*)maxkey, dnum,
-                                                     coarse, F, C, out, s0, s1, fused_padw(F));
+                                                     coarse, F, C, out, s0, s1, fused_max_blocks(F));
     PRODM_CHECK_LAUNCH("k_decode_recompose_nb32");
     return PRODM_OK;
 }
