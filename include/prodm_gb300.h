@@ -207,6 +207,31 @@ int prodm_mdr_coefficients(prodm_mdr* h, void* d_dst, void* stream);
 int prodm_mdr_destroy(prodm_mdr* h);
 
 /* ---------------------------------------------------------------------------
+ * Batched refactor / retrieve of many fields (no counterpart in the
+ * reference, which refactors one field per ComposedRefactor call,
+ * ComposedRefactor.hpp:21-46). All fields share fp32, the negabinary encoder,
+ * the hierarchical basis and the bitplane count; shapes and target levels are
+ * per field. Each stage is one launch over all fields, so a whole batched
+ * refactor or retrieve is a short fixed launch sequence that can be captured
+ * in a CUDA graph (buffers are bound once with prodm_batch_bind).
+ * Retrieval uses the max-error estimators with per-field tolerances
+ * (prodm_batch_set_tolerances, L-inf absolute values).
+ * ------------------------------------------------------------------------- */
+typedef struct prodm_batch prodm_batch;
+int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs);
+int prodm_batch_bind(prodm_batch* h, const void* const* d_fields, void* const* d_outs);
+int prodm_batch_set_launch(prodm_batch* h, int threads_per_cta, int ctas_per_sm);
+int prodm_batch_refactor(prodm_batch* h, void* stream);
+int prodm_batch_set_tolerances(prodm_batch* h, const double* h_tolerances, void* stream);
+int prodm_batch_retrieve(prodm_batch* h, int interpreter, int estimator, double s, void* stream);
+int prodm_batch_reset(prodm_batch* h, void* stream);
+int prodm_batch_field_info(prodm_batch* h, int field, uint8_t* h_index, uint32_t* h_sizes, double* h_bounds,
+                           void* stream);
+int prodm_batch_export_level(prodm_batch* h, int field, int level, void* dst, uint64_t capacity, int dst_is_host,
+                             uint64_t* len, void* stream);
+int prodm_batch_destroy(prodm_batch* h);
+
+/* ---------------------------------------------------------------------------
  * Diagnostics (no counterpart in the reference, whose only instrument is a
  * wall-clock Timer, RefactorUtils.hpp:145-170).
  * Stage timing records CUDA events on the launching stream around each stage;

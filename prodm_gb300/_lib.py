@@ -72,6 +72,16 @@ _SIGS = {
     "prodm_mdr_reset_retrieval": (_i, [_P, _P]),
     "prodm_mdr_coefficients": (_i, [_P, _P, _P]),
     "prodm_mdr_destroy": (_i, [_P]),
+    "prodm_batch_create": (_i, [C.POINTER(_P), _i, C.POINTER(prodm_config)]),
+    "prodm_batch_bind": (_i, [_P, C.POINTER(_P), C.POINTER(_P)]),
+    "prodm_batch_set_launch": (_i, [_P, _i, _i]),
+    "prodm_batch_refactor": (_i, [_P, _P]),
+    "prodm_batch_set_tolerances": (_i, [_P, _dp, _P]),
+    "prodm_batch_retrieve": (_i, [_P, _i, _i, C.c_double, _P]),
+    "prodm_batch_reset": (_i, [_P, _P]),
+    "prodm_batch_field_info": (_i, [_P, _i, _u8p, _u32p, _dp, _P]),
+    "prodm_batch_export_level": (_i, [_P, _i, _i, _P, C.c_uint64, _i, _u64p, _P]),
+    "prodm_batch_destroy": (_i, [_P]),
     "prodm_mdr_set_timing": (_i, [_P, _i]),
     "prodm_mdr_stage_times": (_i, [_P, _dp, _u32p]),
     "prodm_kernel_launch_count": (_i, [_u64p]),

@@ -302,3 +302,83 @@ def kernel_launch_count():
     out = C.c_uint64()
     call("prodm_kernel_launch_count", C.byref(out))
     return out.value
+
+
+class MDRBatch:
+    """Many fp32 fields refactored / retrieved together (one launch per stage).
+
+    fields: list of contiguous fp32 CUDA tensors (kept referenced: their
+    device pointers are bound into the launch tables).
+    """
+
+    def __init__(self, fields, levels=None, num_bitplanes=32):
+        self.fields = list(fields)
+        self.outs = [torch.empty_like(f) for f in self.fields]
+        n = len(self.fields)
+        cfgs = (_lib.prodm_config * n)()
+        self.levels = []
+        for i, f in enumerate(self.fields):
+            if f.dtype != torch.float32 or not f.is_contiguous() or not f.is_cuda:
+                raise ValueError("batched fields must be contiguous fp32 CUDA tensors")
+            L = max_level(f.shape) if levels is None else int(levels[i])
+            self.levels.append(L)
+            c = cfgs[i]
+            c.dtype = _lib.F32
+            c.ndims = f.dim()
+            for d, v in enumerate(f.shape):
+                c.dims[d] = v
+            c.target_level = L
+            c.num_bitplanes = num_bitplanes
+            c.encoder = ENC["negabinary"]
+            c.basis = BASIS["hierarchical"]
+            c.collector = COLLECT["max"]
+        self.B = num_bitplanes
+        self.h = C.c_void_p()
+        call("prodm_batch_create", C.byref(self.h), n, cfgs)
+        fp = (C.c_void_p * n)(*[f.data_ptr() for f in self.fields])
+        op = (C.c_void_p * n)(*[o.data_ptr() for o in self.outs])
+        call("prodm_batch_bind", self.h, fp, op)
+
+    def set_launch(self, threads_per_cta, ctas_per_sm):
+        call("prodm_batch_set_launch", self.h, int(threads_per_cta), int(ctas_per_sm))
+
+    def refactor(self, stream=None):
+        call("prodm_batch_refactor", self.h, _stream(stream))
+
+    def set_tolerances(self, tols, stream=None):
+        arr = (C.c_double * len(self.fields))(*[float(t) for t in tols])
+        call("prodm_batch_set_tolerances", self.h, arr, _stream(stream))
+
+    def retrieve(self, interpreter="negabinary", estimator="max_hb", s=0.0, stream=None):
+        call("prodm_batch_retrieve", self.h, INTERP[interpreter], EST[estimator], float(s), _stream(stream))
+        return self.outs
+
+    def reset(self, stream=None):
+        call("prodm_batch_reset", self.h, _stream(stream))
+
+    def field_info(self, i, stream=None):
+        nl = self.levels[i] + 1
+        idx = (C.c_uint8 * nl)()
+        sz = (C.c_uint32 * (nl * self.B))()
+        bd = (C.c_double * nl)()
+        call("prodm_batch_field_info", self.h, i, idx, sz, bd, _stream(stream))
+        return np.array(idx[:], np.uint8), np.array(sz[:], np.uint32).reshape(nl, self.B), np.array(bd[:])
+
+    def export_level(self, i, level, stream=None):
+        n = C.c_uint64()
+        call("prodm_batch_export_level", self.h, i, level, None, 0, 1, C.byref(n), _stream(stream))
+        buf = np.zeros(n.value, np.uint8)
+        call("prodm_batch_export_level", self.h, i, level, C.c_void_p(buf.ctypes.data), n.value, 1, C.byref(n),
+             _stream(stream))
+        return buf
+
+    def close(self):
+        if self.h:
+            load().prodm_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

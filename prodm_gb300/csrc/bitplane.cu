@@ -16,6 +16,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "nbcodec.cuh"
 
 namespace prodm {
 
@@ -111,33 +112,6 @@ __device__ __forceinline__ void gr_errors(double (&acc)[NACC], double a, int B) 
 template <class T> struct Acc { using type = float; static constexpr int N = 33; };
 template <> struct Acc<double> { using type = double; static constexpr int N = 65; };
 
-// ---------------------------------------------------------------------------
-// 32 x 32 bit transpose across a warp: lane e holds row e on entry; on exit
-// lane k holds the word whose bit e is bit k of row e (five butterfly stages).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
-#pragma unroll
-    for (int j = 16; j > 0; j >>= 1) {
-        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
-                                                                                                       : 0x55555555u;
-        const uint32_t y = __shfl_xor_sync(FULL, x, j);
-        const bool hi = (lane & j) != 0;
-        const uint32_t u = hi ? y : x, v = hi ? x : y;
-        const uint32_t t = ((u >> j) ^ v) & m;
-        x ^= hi ? t : (t << j);
-    }
-    return x;
-}
-
-// x * 2^e, equal to ldexpf(x, e): a single multiplication by an exact power of
-// two rounds once, as ldexpf does, whenever 2^e is a normal float
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
-__device__ __forceinline__ bool pow2_normal(int e) { return e >= -126 && e <= 127; }
-__device__ __forceinline__ float scale2(float v, int e, bool fast, float sc) { return fast ? v * sc : ldexpf(v, e); }
-
-// (-2)^i as a float (exact)
-__device__ __forceinline__ constexpr float nbw(int i) { return (i & 1) ? -(float)(1u << i) : (float)(1u << i); }
-
 // per-lane squared-error accumulators of the negabinary table, indexed by
 // the number k of dropped low digits: acc[0] = m^2 (all planes kept),
 // acc[k] = (value of digits 0..k-1 + m)^2, accx = shifted^2 (no plane kept)
@@ -224,15 +198,8 @@ struct GrErr32 {
     }
 };
 
-constexpr int NB_G = 8;   // blocks per warp iteration (one 32-byte sector per plane)
 
-// fp32 negabinary encoder. A CTA (8 warps) owns a chunk of NB_CHUNK
-// consecutive 32-value blocks: each warp transposes 32 blocks into a shared
-// [plane][block] tile, then the CTA writes every plane's NB_CHUNK words as one
-// contiguous run (coalesced 128-byte stores instead of 32 scattered sectors).
-constexpr int NB_CHUNK = 256;
-constexpr int NB_TILE_LD = NB_CHUNK + 1;     // padded row: conflict-free column writes
-
+// fp32 negabinary encoder: grid-stride over NB_CHUNK-block chunks
 template <bool ERR>
 __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x, uint64_t n,
                                                     const uint32_t* __restrict__ maxkey, int exp_arg, int B,
@@ -240,72 +207,16 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
                                                     double* __restrict__ partial) {
     __shared__ uint32_t tile[32 * NB_TILE_LD];
     const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;   // NegaBinaryBPEncoder.hpp:21
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t nblocks = (n + 31) / 32;
     const uint64_t nchunks = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
     const int se = B - exp;
     const bool fast = pow2_normal(se);
     const float scale = fast ? pow2f(se) : 1.f;
     float acc[32], accx = 0.f;
-    if (ERR) {
 #pragma unroll
-        for (int k = 0; k < 32; k++) acc[k] = 0.f;
-    }
-    const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
-    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const uint64_t cb0 = c * NB_CHUNK;
-        const uint64_t wb0 = cb0 + (uint64_t)warp * 32;
-#pragma unroll 1
-        for (int j0 = 0; j0 < 32; j0 += NB_G) {
-            float v[NB_G];
-#pragma unroll
-            for (int g = 0; g < NB_G; g++) {
-                const uint64_t i = (wb0 + j0 + g) * 32 + lane;
-                v[g] = i < n ? __ldcs(x + i) : 0.f;
-            }
-            uint32_t nb[NB_G];
-            float sh[NB_G], d[NB_G];
-#pragma unroll
-            for (int g = 0; g < NB_G; g++) {
-                sh[g] = fast ? v[g] * scale : ldexpf(v[g], se);    // :42
-                const int32_t q = (int32_t)sh[g];
-                nb[g] = nb_from_bin(q);
-                d[g] = sh[g] - (float)q;                             // exact fraction
-            }
-            if (ERR) {
-                // NegaBinaryBPEncoder.hpp:231-239; values past n contribute 0
-#pragma unroll
-                for (int g = 0; g < NB_G; g++) {
-                    acc[0] += d[g] * d[g];
-                    accx += sh[g] * sh[g];
-                }
-#pragma unroll
-                for (int k = 1; k < 32; k++) {
-                    if (k < B) {
-#pragma unroll
-                        for (int g = 0; g < NB_G; g++) {
-                            if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
-                            acc[k] += d[g] * d[g];
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int g = 0; g < NB_G; g++) {
-                const uint32_t w = transpose32(nb[g], lane);
-                if (lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
-            }
-        }
-        __syncthreads();
-        // write plane rows: warp w handles planes w, w+8, ...
-        const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
-        for (int p = warp; p < B; p += 8) {
-            uint32_t* dst = out + (uint64_t)p * stride + cb0;
-            const uint32_t* row = tile + p * NB_TILE_LD;
-            for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
-        }
-        __syncthreads();
-    }
+    for (int k = 0; k < 32; k++) acc[k] = 0.f;
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x)
+        nb_encode32_chunk<ERR>(x, n, nblocks, B, se, fast, scale, out, stride, c, tile, acc, accx);
     if (ERR) {
         NbErr32 er;
 #pragma unroll
@@ -315,9 +226,7 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
     }
 }
 
-// fp32 negabinary decoder, planes [s, s+num) at base[i * stride]: the CTA
-// loads a [plane][block] tile with coalesced loads, then each warp transposes
-// its blocks (lane e receives the digits of value e) and stores coalesced.
+// fp32 negabinary decoder, planes [s, s+num) at base[i * stride]
 __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict__ base, uint64_t stride, uint64_t n,
                                                     const uint32_t* __restrict__ maxkey, int exp_arg, int s, int num,
                                                     const uint8_t* __restrict__ dnum, float* __restrict__ out) {
@@ -325,33 +234,12 @@ __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict_
     if (dnum) num = dnum[0] - s;
     const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;
     const int e = s + num;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t nblocks = (n + 31) / 32;
     const uint64_t nchunks = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
-    const bool neg = num != 0 && (e & 1);                   // :153, :177
     const bool dfast = pow2_normal(exp - e);
     const float dscale = dfast ? pow2f(exp - e) : 1.f;
-    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const uint64_t cb0 = c * NB_CHUNK;
-        const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
-        for (int p = warp; p < num; p += 8) {
-            const uint32_t* src = base + (uint64_t)p * stride + cb0;
-            uint32_t* row = tile + p * NB_TILE_LD;
-            for (int j = lane; j < nvalid; j += 32) row[j] = __ldcs(src + j);
-        }
-        __syncthreads();
-        for (int j = 0; j < 32; j++) {
-            const int bl = warp * 32 + j;
-            if (bl >= nvalid) break;
-            const uint32_t w = lane < num ? tile[lane * NB_TILE_LD + bl] : 0u;
-            const uint32_t col = transpose32(w, lane);      // bit i = digit of plane s+i
-            const uint32_t acc = num ? (__brev(col) >> (32 - num)) : 0u;
-            const float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - e)) : 0.f;
-            const uint64_t i = (cb0 + bl) * 32 + lane;
-            if (i < n) out[i] = neg ? -val : val;
-        }
-        __syncthreads();
-    }
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x)
+        nb_decode32_chunk(base, stride, n, nblocks, num, e, exp, dfast, dscale, c, tile, out);
 }
 
 // ---------------------------------------------------------------------------

@@ -20,6 +20,7 @@
 //                (DecomposerInterface.hpp:14-16).
 #include "common.cuh"
 #include "kernels.cuh"
+#include "rows.cuh"
 
 namespace prodm {
 
@@ -166,21 +167,6 @@ __global__ void k_recompose_level(const T* __restrict__ coarse, const T* __restr
 // coalesced and there is no per-element 64-bit division. Same arithmetic
 // (and the same uncontracted operation order) as the generic kernels.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint64_t row_rank_base(uint32_t r0, uint32_t r1, const Box& F, const Box& C, bool& cc) {
-    cc = r0 < C.n[0] && r1 < C.n[1];
-    // rank of (r0, r1, cc ? C2 : 0)
-    return level_rank(r0, r1, cc ? C.n[2] : 0u, F, C);
-}
-
-// corner row offsets (elements) of a row for mask m01, in corner_tree order
-__device__ __forceinline__ void corner_offsets(int m01, int64_t lo0, int64_t hi0, int64_t lo1, int64_t hi1,
-                                               int64_t* o) {
-    if (m01 == 0) { o[0] = 0; }
-    else if (m01 == 1) { o[0] = lo0; o[1] = hi0; }
-    else if (m01 == 2) { o[0] = lo1; o[1] = hi1; }
-    else { o[0] = lo0 + lo1; o[1] = lo0 + hi1; o[2] = hi0 + lo1; o[3] = hi0 + hi1; }
-}
-
 template <class T>
 __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in, uint64_t s0, uint64_t s1, Box F, Box C,
                                                         T* __restrict__ coef, T* __restrict__ coarse,
@@ -189,73 +175,15 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
     using K = typename KeyOf<T>::type;
     K mk = 0, mc = 0;
     const uint32_t rows = F.n[0] * F.n[1];
-    const uint32_t n2 = F.n[2], c2n = C.n[2];
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
-        const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
-        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
-        const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
-        bool cc;
-        const uint64_t rbase = row_rank_base(r0, r1, F, C, cc);
-        const T* p = in + x0 * s0 + x1 * s1;
-        int64_t co[4];
-        corner_offsets(m01, -(int64_t)s0, (int64_t)s0, -(int64_t)s1, (int64_t)s1, co);
-        const int nq = corner_count(m01);
-        T* frow = fnat ? fnat + (uint64_t)row * n2 : nullptr;
-        T* crow = coarse + ((uint64_t)r0 * C.n[1] + r1) * c2n;
-#pragma unroll 3
-        for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
-            const uint32_t c2 = cbase + lane;
-            const bool act = c2 < c2n;
-            const uint32_t xe = act ? fine_of_coarse(c2, n2, c2n) : 0;
-            const bool odd = act && c2 + 1 < c2n && fine_of_coarse(c2 + 1, n2, c2n) == 2 * c2 + 2;
-            T q[4] = {0, 0, 0, 0}, qn[4];
-            const T ve = act ? p[xe] : (T)0;
-            if (m01 == 0) q[0] = ve;
-            else {
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-                    if (i < nq && act) q[i] = __ldg(p + xe + co[i]);
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                qn[i] = __shfl_down_sync(0xffffffffu, q[i], 1);
-                if (i < nq && lane == 31 && odd) {
-                    const uint32_t xn = 2 * c2 + 2;
-                    qn[i] = m01 == 0 ? p[xn] : __ldg(p + xn + co[i]);
-                }
-            }
-            if (act) {
-                // even node of the column
-                if (m01 == 0) {
-                    crow[c2] = ve;
-                    if (frow) frow[xe] = (T)0;
-                    K k = abs_key(ve);
-                    mc = k > mc ? k : mc;
-                } else {
-                    T c = sub_rn(ve, corner_tree(m01, q));
-                    coef[rbase + (cc ? c2 - c2n : c2)] = c;
-                    if (frow) frow[xe] = c;
-                    K k = abs_key(c);
-                    mk = k > mk ? k : mk;
-                }
-                if (odd) {
-                    const uint32_t xo = 2 * c2 + 1;
-                    T c = sub_rn(p[xo], corner_tree_mid(m01, q, qn));
-                    coef[rbase + (cc ? c2 : c2n + c2)] = c;
-                    if (frow) frow[xo] = c;
-                    K k = abs_key(c);
-                    mk = k > mk ? k : mk;
-                }
-            }
-        }
-    }
+    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb)
+        decompose_row<T>(in, s0, s1, F, C, coef, coarse, fnat, row, lane, mk, mc);
     if (maxkey_level) {
-        mk = warp_max(mk);
+        mk = warp_max_key(mk);
         if ((threadIdx.x & 31) == 0 && mk) atomicMax(maxkey_level, mk);
     }
     if (maxkey_coarse) {
-        mc = warp_max(mc);
+        mc = warp_max_key(mc);
         if ((threadIdx.x & 31) == 0 && mc) atomicMax(maxkey_coarse, mc);
     }
 }
@@ -264,43 +192,9 @@ template <class T>
 __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ coarse, const T* __restrict__ coef, Box F,
                                                         Box C, T* __restrict__ out, uint64_t s0, uint64_t s1) {
     const uint32_t rows = F.n[0] * F.n[1];
-    const uint32_t n2 = F.n[2], c2n = C.n[2];
-    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
-        const uint32_t x0 = row / F.n[1], x1 = row - x0 * F.n[1];
-        const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
-        const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : reord(x0, F.n[0], C.n[0]);
-        const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : reord(x1, F.n[1], C.n[1]);
-        const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
-        bool cc;
-        const uint64_t rbase = row_rank_base(r0, r1, F, C, cc);
-        const T* cb0 = coarse + c0 * cs0 + c1 * cs1;
-        int64_t co[4];
-        corner_offsets(m01, 0, (int64_t)cs0, 0, (int64_t)cs1, co);
-        const int nq = corner_count(m01);
-        T* orow = out + x0 * s0 + x1 * s1;
-#pragma unroll 3
-        for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
-            const uint32_t c2 = cbase + lane;
-            const bool act = c2 < c2n;
-            const bool odd = act && c2 + 1 < c2n && fine_of_coarse(c2 + 1, n2, c2n) == 2 * c2 + 2;
-            T q[4] = {0, 0, 0, 0}, qn[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-                if (i < nq && act) q[i] = __ldg(cb0 + c2 + co[i]);
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                qn[i] = __shfl_down_sync(0xffffffffu, q[i], 1);
-                if (i < nq && lane == 31 && odd) qn[i] = __ldg(cb0 + c2 + 1 + co[i]);
-            }
-            if (act) {
-                const uint32_t xe = fine_of_coarse(c2, n2, c2n);
-                orow[xe] = m01 == 0 ? q[0] : add_rn(coef[rbase + (cc ? c2 - c2n : c2)], corner_tree(m01, q));
-                if (odd) orow[2 * c2 + 1] = add_rn(coef[rbase + (cc ? c2 : c2n + c2)], corner_tree_mid(m01, q, qn));
-            }
-        }
-    }
+    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb)
+        recompose_row<T>(coarse, coef, F, C, out, s0, s1, row, lane);
 }
 
 // copy a box between strided arrays

@@ -1,0 +1,132 @@
+// Negabinary fp32 codec bodies (bit transposes, chunk encode / decode),
+// shared by the single-level kernels and the multi-field batched kernels.
+#pragma once
+#include "common.cuh"
+
+namespace prodm {
+
+// ---------------------------------------------------------------------------
+// 32 x 32 bit transpose across a warp: lane e holds row e on entry; on exit
+// lane k holds the word whose bit e is bit k of row e (five butterfly stages).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
+                                                                                                       : 0x55555555u;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+        const bool hi = (lane & j) != 0;
+        const uint32_t u = hi ? y : x, v = hi ? x : y;
+        const uint32_t t = ((u >> j) ^ v) & m;
+        x ^= hi ? t : (t << j);
+    }
+    return x;
+}
+
+// x * 2^e, equal to ldexpf(x, e): a single multiplication by an exact power of
+// two rounds once, as ldexpf does, whenever 2^e is a normal float
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+__device__ __forceinline__ bool pow2_normal(int e) { return e >= -126 && e <= 127; }
+__device__ __forceinline__ float scale2(float v, int e, bool fast, float sc) { return fast ? v * sc : ldexpf(v, e); }
+
+// (-2)^i as a float (exact)
+__device__ __forceinline__ constexpr float nbw(int i) { return (i & 1) ? -(float)(1u << i) : (float)(1u << i); }
+
+
+constexpr int NB_G = 8;              // blocks per warp iteration
+constexpr int NB_CHUNK = 256;        // blocks per CTA chunk
+constexpr int NB_TILE_LD = NB_CHUNK + 1;   // padded tile row: conflict-free column writes
+
+// Encode chunk c (NB_CHUNK consecutive 32-value blocks) of a level: each warp
+// transposes 32 blocks into the shared [plane][block] tile, then the CTA
+// writes every plane's words of the chunk as one contiguous run.
+// Errors (ERR): negabinary truncation tables, NegaBinaryBPEncoder.hpp:231-239,
+// in per-lane accumulators indexed by dropped digits (acc[0] = m^2).
+template <bool ERR>
+__device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, uint64_t n, uint64_t nblocks, int B,
+                                                  int se, bool fast, float scale, uint32_t* __restrict__ out,
+                                                  uint64_t stride, uint64_t c, uint32_t* tile, float (&acc)[32],
+                                                  float& accx) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
+    const uint64_t cb0 = c * NB_CHUNK;
+    const uint64_t wb0 = cb0 + (uint64_t)warp * 32;
+#pragma unroll 1
+    for (int j0 = 0; j0 < 32; j0 += NB_G) {
+        float v[NB_G];
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) {
+            const uint64_t i = (wb0 + j0 + g) * 32 + lane;
+            v[g] = i < n ? __ldcs(x + i) : 0.f;
+        }
+        uint32_t nb[NB_G];
+        float sh[NB_G], d[NB_G];
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) {
+            sh[g] = fast ? v[g] * scale : ldexpf(v[g], se);    // NegaBinaryBPEncoder.hpp:42
+            const int32_t q = (int32_t)sh[g];
+            nb[g] = nb_from_bin(q);
+            d[g] = sh[g] - (float)q;                             // exact fraction
+        }
+        if (ERR) {
+#pragma unroll
+            for (int g = 0; g < NB_G; g++) {
+                acc[0] += d[g] * d[g];
+                accx += sh[g] * sh[g];
+            }
+#pragma unroll
+            for (int k = 1; k < 32; k++) {
+                if (k < B) {
+#pragma unroll
+                    for (int g = 0; g < NB_G; g++) {
+                        if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
+                        acc[k] += d[g] * d[g];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < NB_G; g++) {
+            const uint32_t w = transpose32(nb[g], lane);
+            if (lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
+        }
+    }
+    __syncthreads();
+    const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
+    for (int p = warp; p < B; p += 8) {
+        uint32_t* dst = out + (uint64_t)p * stride + cb0;
+        const uint32_t* row = tile + p * NB_TILE_LD;
+        for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
+    }
+    __syncthreads();
+}
+
+// Decode chunk c of planes [s, s+num) (plane s+i at base + i * stride):
+// coalesced tile load, one warp transpose per block, coalesced stores.
+__device__ __forceinline__ void nb_decode32_chunk(const uint32_t* __restrict__ base, uint64_t stride, uint64_t n,
+                                                  uint64_t nblocks, int num, int e, int exp, bool dfast, float dscale,
+                                                  uint64_t c, uint32_t* tile, float* __restrict__ out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool neg = num != 0 && (e & 1);                   // NegaBinaryBPEncoder.hpp:153, :177
+    const uint64_t cb0 = c * NB_CHUNK;
+    const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
+    for (int p = warp; p < num; p += 8) {
+        const uint32_t* src = base + (uint64_t)p * stride + cb0;
+        uint32_t* row = tile + p * NB_TILE_LD;
+        for (int j = lane; j < nvalid; j += 32) row[j] = __ldcs(src + j);
+    }
+    __syncthreads();
+    for (int j = 0; j < 32; j++) {
+        const int bl = warp * 32 + j;
+        if (bl >= nvalid) break;
+        const uint32_t w = lane < num ? tile[lane * NB_TILE_LD + bl] : 0u;
+        const uint32_t col = transpose32(w, lane);      // bit i = digit of plane s+i
+        const uint32_t a = num ? (__brev(col) >> (32 - num)) : 0u;
+        const float val = num ? (dfast ? (float)nb_to_bin(a) * dscale : ldexpf((float)nb_to_bin(a), exp - e)) : 0.f;
+        const uint64_t i = (cb0 + bl) * 32 + lane;
+        if (i < n) out[i] = neg ? -val : val;
+    }
+    __syncthreads();
+}
+
+}  // namespace prodm

@@ -109,3 +109,37 @@ def divergence_free_velocity(n, kmax=16, n_modes=64, seed=0, dtype=torch.float32
 def lognormal_density(n, sigma=0.5, seed=0, dtype=torch.float32, device=None):
     g = spectral_grf((n, n, n), slope=-3.0, seed=seed, dtype=torch.float32, device=device)
     return torch.exp(sigma * g.to(torch.float64)).to(dtype).contiguous()
+
+
+def batch_level(shape, max_level):
+    """Largest level count the reference accepts that keeps level 0 at >= 32
+    values (its block encoders need one full block, see the encoder loops)."""
+    L = max_level
+    while L > 0:
+        box = list(shape)
+        for _ in range(L):
+            box = [(n >> 1) + 1 for n in box]
+        if int(np.prod(box)) >= 32:
+            return L
+        L -= 1
+    return 0
+
+
+def batch_specs(seed=0):
+    """The 64-field batch: 24 cubes with sides from {33, 65, 129, 257}, 24 2-D
+    fields with sides from {513, 1025, 2049}, 16 anisotropic 129 x 257 x 65
+    fields; spectral slopes uniform in [-3, -1]; relative L-inf tolerances
+    log-uniform in [1e-5, 1e-2]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(24):
+        n = int(rng.choice([33, 65, 129, 257]))
+        specs.append((n, n, n))
+    for _ in range(24):
+        n = int(rng.choice([513, 1025, 2049]))
+        specs.append((n, n))
+    for _ in range(16):
+        specs.append((129, 257, 65))
+    slopes = rng.uniform(-3.0, -1.0, len(specs))
+    rel = 10.0 ** rng.uniform(-5.0, -2.0, len(specs))
+    return [(s, float(a), float(t)) for s, a, t in zip(specs, slopes, rel)]

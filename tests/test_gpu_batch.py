@@ -1,0 +1,71 @@
+"""Batched refactor / retrieve against the single-field device path: the same
+streams, the same plane counts and the same reconstructions (the batched
+launches run the same per-row / per-chunk code)."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_single_field_path():
+    from prodm_gb300 import api, fields
+    shapes = [(33, 33, 33), (65, 65, 65), (129, 65), (33, 65, 17), (1000,), (9, 9, 9), (257, 129)]
+    xs = [fields.spectral_grf(s, slope=-2.0, seed=i).contiguous() for i, s in enumerate(shapes)]
+    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+    batch = api.MDRBatch(xs, levels, 32)
+    batch.refactor()
+    tols = []
+    for i, x in enumerate(xs):
+        vr = float(x.max() - x.min())
+        tols.append(vr * 10.0 ** (-2 - i % 4))
+    batch.set_tolerances(tols)
+    batch.reset()
+    outs = batch.retrieve("negabinary", "max_hb")
+    torch.cuda.synchronize()
+    for i, (s, x) in enumerate(zip(shapes, xs)):
+        one = api.MDRField(s, torch.float32, levels[i], 32, "negabinary", "hierarchical", "max")
+        one.refactor(x)
+        sz1, b1, _ = one.level_info()
+        idxb, szb, bb = batch.field_info(i)
+        assert np.array_equal(szb, sz1)
+        np.testing.assert_array_equal(bb, b1)
+        for l in range(levels[i] + 1):
+            assert np.array_equal(batch.export_level(i, l), one.export_level(l)), (i, l)
+        out1 = one.retrieve(tols[i], interpreter="negabinary", estimator="max_hb")
+        assert np.array_equal(one.index(), idxb)
+        assert torch.equal(out1, outs[i]), i
+        assert float((outs[i] - x).abs().max()) <= tols[i]
+
+
+def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
+    from prodm_gb300 import api, autotune, fields
+    monkeypatch.setenv("PRODM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    shapes = [(65, 65, 65), (129, 129), (33, 65, 17)]
+    xs = [fields.spectral_grf(s, seed=10 + i) for i, s in enumerate(shapes)]
+    batch = api.MDRBatch(xs, None, 32)
+    t, c, timings = autotune.tune(batch, reps=1)
+    assert (t, c) in autotune.CANDIDATES and len(timings) == len(autotune.CANDIDATES)
+    assert autotune.tune(batch)[:2] == (t, c)          # served from the cache
+    batch.set_tolerances([1e-3] * 3)
+    ref = None
+    for capture in (False, True):
+        if capture:
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                batch.refactor(); batch.reset(); batch.retrieve()
+            torch.cuda.current_stream().wait_stream(s)
+            with torch.cuda.graph(g):
+                batch.refactor(); batch.reset(); batch.retrieve()
+            g.replay()
+            torch.cuda.synchronize()
+            for a, b in zip(ref, batch.outs):
+                assert torch.equal(a, b)
+        else:
+            batch.refactor(); batch.reset(); batch.retrieve()
+            torch.cuda.synchronize()
+            ref = [o.clone() for o in batch.outs]
