@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-graph", action="store_true", help="launch every kernel from the host instead of a CUDA graph")
+    ap.add_argument("--graph", action="store_true", help="replay the step as a captured CUDA graph (stage events "
+                    "are captured as external event nodes)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-field batched vs per-field-loop measurement")
     return ap.parse_args()
 
@@ -262,7 +263,7 @@ def run_ours(args):
     # stage events are captured too and time every kernel group of each replay
     graph = None
     launches_per_step = None
-    if not args.no_graph:
+    if args.graph:
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(side):
