@@ -209,6 +209,9 @@ def stage_bytes(mdr, kind, level, step_bytes_info):
     if kind == "decode":
         return step_bytes_info["decode_bytes"][level] + 4 * n
     if kind == "recompose":
+        if level == step_bytes_info["L"] and step_bytes_info.get("fused"):
+            # fused finest level: the retrieved planes are read instead of coefficients
+            return step_bytes_info["decode_bytes"][level] + 4 * (box(level - 1) + box(level))
         return 4 * (box(level - 1) + n + box(level))
     return 0
 
@@ -320,7 +323,8 @@ def run_ours(args):
 
     # roofline of the dominant stage
     peak, peak_src = measured_peak()
-    info = {"sizes": sizes, "decode_bytes": decode_bytes}
+    info = {"sizes": sizes, "decode_bytes": decode_bytes, "L": LEVELS,
+            "fused": ("decode", LEVELS) not in stages}
     per_stage = {}
     for (kind, level), (tms, cnt) in stages.items():
         b = stage_bytes(mdr, kind, level, info)
