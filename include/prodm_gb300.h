@@ -136,6 +136,17 @@ int prodm_collect_max(int dtype, double max_level_error, int num_bitplanes, doub
 int prodm_collect_squared_workspace(int dtype, int num_bitplanes, size_t* bytes);
 int prodm_collect_squared(int dtype, const void* d_data, uint64_t n, int num_bitplanes, double max_level_error,
                           double* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
+/* Same table as prodm_collect_squared, allocating nothing. No counterpart in
+ * the reference: it is for callers that cannot allocate device memory (hosts
+ * whose own pool owns the HBM, or that forbid the device-synchronising
+ * cudaMalloc/cudaFree inside their callbacks) and have no workspace to pass.
+ * Its scratch is a fixed 316,160-byte device array, enough for
+ * num_bitplanes <= 64 (fp64) / 32 (fp32); larger values return PRODM_EINVAL.
+ * The first call on a device looks up that array's address (make it before
+ * any stream capture). All calls on a device share the array: calls that
+ * overlap on the GPU race; calls on one stream are ordered. */
+int prodm_collect_squared_noalloc(int dtype, const void* d_data, uint64_t n, int num_bitplanes,
+                                  double max_level_error, double* d_out, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Size interpreter -- SizeInterpreterInterface::interpret_retrieve_size

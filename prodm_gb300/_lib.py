@@ -56,6 +56,7 @@ _SIGS = {
     "prodm_collect_max": (_i, [_i, C.c_double, _i, _dp]),
     "prodm_collect_squared_workspace": (_i, [_i, _i, C.POINTER(C.c_size_t)]),
     "prodm_collect_squared": (_i, [_i, _P, C.c_uint64, _i, C.c_double, _P, _P, C.c_size_t, _P]),
+    "prodm_collect_squared_noalloc": (_i, [_i, _P, C.c_uint64, _i, C.c_double, _P, _P]),
     "prodm_interpret": (_i, [_i, _i, _i, _i, _i, C.c_double, _i, _i, _P, _P, C.c_double, _P, _P, _P]),
     "prodm_mdr_create": (_i, [C.POINTER(_P), C.POINTER(prodm_config)]),
     "prodm_mdr_refactor": (_i, [_P, _P, _P]),
