@@ -207,7 +207,12 @@ def stage_bytes(mdr, kind, level, step_bytes_info):
     if kind == "encode":
         return 4 * n + int(sizes[level].astype(np.int64).sum())
     if kind == "decode":
-        return step_bytes_info["decode_bytes"][level] + 4 * n
+        levels = [level]
+        if level == 0 and step_bytes_info.get("decode_multi"):
+            # one launch decodes every level the fused kernel does not
+            top = step_bytes_info["L"] - (1 if step_bytes_info.get("fused") else 0)
+            levels = range(0, top + 1)
+        return sum(step_bytes_info["decode_bytes"][l] + 4 * int(mdr.level_elements[l]) for l in levels)
     if kind == "recompose":
         if level == step_bytes_info["L"] and step_bytes_info.get("fused"):
             # fused finest level: the retrieved planes are read instead of coefficients
@@ -324,7 +329,7 @@ def run_ours(args):
     # roofline of the dominant stage
     peak, peak_src = measured_peak()
     info = {"sizes": sizes, "decode_bytes": decode_bytes, "L": LEVELS,
-            "fused": ("decode", LEVELS) not in stages}
+            "fused": ("decode", LEVELS) not in stages, "decode_multi": ("decode", 1) not in stages}
     per_stage = {}
     for (kind, level), (tms, cnt) in stages.items():
         b = stage_bytes(mdr, kind, level, info)

@@ -35,25 +35,6 @@ struct RowSeg {
     uint32_t* key_c;        // decompose at level 1: level-0 |max| key
 };
 
-struct ChunkSeg {
-    const float* x;         // encode input / decode output
-    float* y;
-    uint32_t* words;        // plane 0 of the level's streams
-    uint64_t n, nblocks, stride;
-    const uint32_t* key;
-    const uint8_t* dnum;    // decode: retrieved plane count
-    uint64_t chunk_begin;
-};
-
-template <class Seg>
-__device__ __forceinline__ int find_seg(const Seg* segs, int nseg, uint64_t g, uint64_t Seg::*begin) {
-    int lo = 0, hi = nseg - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (segs[mid].*begin <= g) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
 __device__ __forceinline__ int find_row_seg(const RowSeg* segs, int nseg, uint32_t g) {
     int lo = 0, hi = nseg - 1;
     while (lo < hi) {
@@ -339,6 +320,14 @@ int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t s
 }
 
 }  // namespace
+
+int launch_nb_decode_multi(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st) {
+    const unsigned grid = persistent_grid_for((const void*)k_nb_decode_multi, 256, 0, total_chunks, total_chunks);
+    k_nb_decode_multi<<<grid, 256, 0, st>>>(segs, nseg, total_chunks);
+    PRODM_CHECK_LAUNCH("k_nb_decode_multi");
+    return PRODM_OK;
+}
+
 }  // namespace prodm
 
 extern "C" {

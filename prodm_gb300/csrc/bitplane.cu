@@ -226,6 +226,78 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
     }
 }
 
+// Every level of one fp32 field in one launch: segments are the levels in
+// chunk order, a CTA walks its chunks in increasing order and flushes its
+// error accumulators whenever the level changes. The per-level partial tables
+// sit at partial + level * gridDim.x * (B + 1); a CTA writes zero rows for the
+// levels it never visits, so every row the reduction reads is written.
+template <bool ERR>
+__global__ void __launch_bounds__(256) k_nb_encode32_levels(const ChunkSeg* __restrict__ segs, int nseg,
+                                                           uint64_t total, int B, double* __restrict__ partial) {
+    __shared__ uint32_t tile[32 * NB_TILE_LD];
+    float acc[32], accx = 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; k++) acc[k] = 0.f;
+    const size_t rows_per_level = (size_t)gridDim.x * (B + 1);
+    auto zero_rows = [&](int s0, int s1) {   // levels [s0, s1)
+        for (int s = s0; s < s1; s++)
+            for (int k = threadIdx.x; k <= B; k += blockDim.x)
+                partial[s * rows_per_level + (size_t)blockIdx.x * (B + 1) + k] = 0.0;
+    };
+    auto flush = [&](int s) {
+        NbErr32 er;
+#pragma unroll
+        for (int k = 0; k < 32; k++) { er.acc[k] = acc[k]; acc[k] = 0.f; }
+        er.accx = accx;
+        accx = 0.f;
+        er.flush(B, partial + s * rows_per_level);
+    };
+    int cur = -1, se = 0;
+    bool fast = true;
+    float scale = 1.f;
+    for (uint64_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const int s = find_seg(segs, nseg, c, &ChunkSeg::chunk_begin);
+        const ChunkSeg& q = segs[s];
+        if (s != cur) {
+            if (ERR) {
+                if (cur >= 0) flush(cur);
+                zero_rows(cur + 1, s);
+            }
+            cur = s;
+            se = B - (frexp_exp(__uint_as_float(*q.key)) + 2);     // NegaBinaryBPEncoder.hpp:21
+            fast = pow2_normal(se);
+            scale = fast ? pow2f(se) : 1.f;
+        }
+        nb_encode32_chunk<ERR>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin, tile,
+                               acc, accx);
+    }
+    if (ERR) {
+        if (cur >= 0) flush(cur);
+        zero_rows(cur + 1, nseg);
+    }
+}
+
+// per-level tables from the partial rows of k_nb_encode32_levels, scaled to
+// value units (NegaBinaryBPEncoder.hpp:121-123); one warp per table entry
+__global__ void k_reduce_partials_levels(const double* __restrict__ partial, int nparts, int B, int nl,
+                                         const uint32_t* __restrict__ keys, double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int entries = nl * (B + 1);
+    for (int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < entries;
+         e += gridDim.x * (blockDim.x >> 5)) {
+        const int l = e / (B + 1), k = e - l * (B + 1);
+        const double* rows = partial + (size_t)l * nparts * (B + 1);
+        double s = 0;
+        for (int p = lane; p < nparts; p += 32) s += rows[(size_t)p * (B + 1) + k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+        if (lane == 0) {
+            const int exp = frexp_exp(__uint_as_float(keys[l])) + 2;
+            out[e] = ldexp(s, 2 * (-B + exp));
+        }
+    }
+}
+
 // fp32 negabinary decoder, planes [s, s+num) at base[i * stride]
 __global__ void __launch_bounds__(256) k_nb_decode32(const uint32_t* __restrict__ base, uint64_t stride, uint64_t n,
                                                     const uint32_t* __restrict__ maxkey, int exp_arg, int s, int num,
@@ -857,8 +929,8 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     const int th = 256;
     if (std::is_same<T, float>::value) {
         const uint64_t nch = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
-        unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)kSMs * 8, nch));
-        if (errs_out) grid = (unsigned)std::min<uint64_t>((uint64_t)kPartialSlots, std::max<uint64_t>(1, nch));
+        const unsigned grid = errs_out ? persistent_grid_for((const void*)k_nb_encode32<true>, th, 0, nch, kPartialSlots)
+                                       : persistent_grid_for((const void*)k_nb_encode32<false>, th, 0, nch, nch);
         if (errs_out)
             k_nb_encode32<true><<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
                                                      (uint32_t*)out, stride, partial);
@@ -872,7 +944,8 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
         }
         return PRODM_OK;
     }
-    unsigned grid = errs_out ? (unsigned)kSMs * 4 : grid_for(nblocks * 32, th, 8);
+    const unsigned grid = errs_out ? persistent_grid_for((const void*)k_nb_encode<T, true>, th, 0, nblocks, kPartialSlots)
+                                   : grid_for(nblocks * 32, th, 8);
     if (errs_out) {
         k_nb_encode<T, true><<<grid, th, 0, st>>>(x, n, (const K*)maxkey, exp, B, (typename Traits<T>::S*)out, stride,
                                                   partial);
@@ -887,6 +960,27 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     return PRODM_OK;
 }
 
+int nb_encode_levels_grid(int with_errors) {
+    const void* k = with_errors ? (const void*)k_nb_encode32_levels<true> : (const void*)k_nb_encode32_levels<false>;
+    return (int)persistent_grid_for(k, 256, 0, (uint64_t)kPartialSlots, kPartialSlots);
+}
+
+int launch_nb_encode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, int B, double* partial,
+                            const uint32_t* keys, double* errs_out, cudaStream_t st) {
+    const unsigned grid = (unsigned)nb_encode_levels_grid(errs_out != nullptr);
+    if (errs_out) {
+        k_nb_encode32_levels<true><<<grid, 256, 0, st>>>(segs, nseg, total_chunks, B, partial);
+        PRODM_CHECK_LAUNCH("k_nb_encode32_levels");
+        const int warps = nseg * (B + 1);
+        k_reduce_partials_levels<<<(warps + 7) / 8, 256, 0, st>>>(partial, (int)grid, B, nseg, keys, errs_out);
+        PRODM_CHECK_LAUNCH("k_reduce_partials_levels");
+    } else {
+        k_nb_encode32_levels<false><<<grid, 256, 0, st>>>(segs, nseg, total_chunks, B, nullptr);
+        PRODM_CHECK_LAUNCH("k_nb_encode32_levels");
+    }
+    return PRODM_OK;
+}
+
 template <class T>
 int launch_nb_decode(const void* base, uint64_t stride, uint64_t n, const void* maxkey, int exp, int s, int num,
                      const uint8_t* dnum, T* out, cudaStream_t st) {
@@ -896,7 +990,7 @@ int launch_nb_decode(const void* base, uint64_t stride, uint64_t n, const void* 
     const int th = 256;
     if (std::is_same<T, float>::value) {
         const uint64_t nch = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
-        const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)kSMs * 8, nch));
+        const unsigned grid = persistent_grid_for((const void*)k_nb_decode32, th, 0, nch, nch);
         k_nb_decode32<<<grid, th, 0, st>>>((const uint32_t*)base, stride, n, (const uint32_t*)maxkey, exp, s, num, dnum,
                                            (float*)out);
         PRODM_CHECK_LAUNCH("k_nb_decode32");
@@ -996,7 +1090,7 @@ int launch_gr_decode(const void* const* planes, uint64_t n, const void* maxkey, 
 template <class T>
 int launch_sq_collect(const T* x, uint64_t n, int B, T maxv, double* partial, double* out, cudaStream_t st) {
     const int th = 256;
-    const unsigned grid = (unsigned)kSMs * 4;
+    const unsigned grid = persistent_grid_for((const void*)k_sq_collect<T>, th, 0, (n + th - 1) / th, kPartialSlots);
     k_sq_collect<T><<<grid, th, 0, st>>>(x, n, B, maxv, partial);
     PRODM_CHECK_LAUNCH("k_sq_collect");
     k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)grid, B, nullptr, 0, 0, 0, out);

@@ -3,6 +3,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -24,6 +25,34 @@ int fail(int status, const std::string& msg) {
 int cuda_status(cudaError_t e, const char* where) {
     g_err = std::string(where) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? PRODM_ENOMEM : PRODM_ECUDA;
+}
+
+unsigned resident_ctas(const void* kernel, int threads, size_t smem) {
+    struct Entry {
+        int dev;
+        const void* k;
+        int threads;
+        size_t smem;
+        unsigned ctas;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        for (const Entry& e : cache)
+            if (e.dev == dev && e.k == kernel && e.threads == threads && e.smem == smem) return e.ctas;
+    }
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = kSMs;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    (void)cudaGetLastError();
+    const unsigned ctas = (unsigned)(sms * per_sm);
+    std::lock_guard<std::mutex> lock(mu);
+    cache.push_back({dev, kernel, threads, smem, ctas});
+    return ctas;
 }
 
 int max_level(int ndims, const uint32_t* dims) {
@@ -466,6 +495,10 @@ struct prodm_mdr {
     int* levels_d = nullptr;
     void* rcoef = nullptr;
     void* rbuf[2] = {nullptr, nullptr};
+    // fp32 negabinary: the levels decoded by one multi-level launch
+    ChunkSeg* dseg = nullptr;
+    int dseg_n = 0;
+    uint64_t dseg_chunks = 0;
     uint8_t* pack_tmp = nullptr;
     // reconstructor fed from level files (reference on-disk format)
     bool from_files = false;
@@ -549,6 +582,13 @@ struct Stage {
     }
 };
 
+// fp32 negabinary hierarchical: the finest level is decoded inside the fused
+// decode + recompose kernel
+bool fuse_finest(const prodm_mdr* h) {
+    const int L = h->g.L;
+    return h->nb && !h->orth && h->cfg.dtype == PRODM_F32 && L >= 1 && decode_recompose_nb32_ok(h->g.box[L]);
+}
+
 int mdr_alloc_all(prodm_mdr* h) {
     const LevelGeom& g = h->g;
     const int L = g.L, B = h->B;
@@ -629,6 +669,30 @@ int mdr_alloc_all(prodm_mdr* h) {
                 ptrs[l * B + p] = h->streams + h->lvl_byte_off[l] + (uint64_t)p * h->plane_cap[l] * es;
         PRODM_CUDA(cudaMemcpy(h->plane_ptrs, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice));
     }
+    if (h->nb && dtype == PRODM_F32) {
+        // every level not decoded by the fused finest-level kernel, as one
+        // segment table (NB_CHUNK = 256 blocks per chunk)
+        const int top = fuse_finest(h) ? L - 1 : L;
+        std::vector<ChunkSeg> segs;
+        uint64_t chunks = 0;
+        for (int l = 0; l <= top; l++) {
+            ChunkSeg q{};
+            q.y = (float*)h->rcoef + g.offset[l];
+            q.words = (uint32_t*)(h->streams + h->lvl_byte_off[l]);
+            q.n = g.elems[l];
+            q.nblocks = h->nblocks[l];
+            q.stride = h->nblocks[l];
+            q.key = (const uint32_t*)h->keys + l;
+            q.dnum = h->index + l;
+            q.chunk_begin = chunks;
+            chunks += (q.nblocks + 255) / 256;
+            segs.push_back(q);
+        }
+        if ((rc = h->alloc((void**)&h->dseg, segs.size() * sizeof(ChunkSeg)))) return rc;
+        PRODM_CUDA(cudaMemcpy(h->dseg, segs.data(), segs.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
+        h->dseg_n = (int)segs.size();
+        h->dseg_chunks = chunks;
+    }
     return PRODM_OK;
 }
 
@@ -696,9 +760,14 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
     T* rcoef = (T*)h->rcoef;
     int rc;
     // finest level: fused decode + recompose where the layout allows it
-    const bool fuse = h->nb && !h->orth && sizeof(T) == 4 && L >= 1 && decode_recompose_nb32_ok(g.box[L]);
+    const bool fuse = fuse_finest(h);
+    if (h->dseg && sizeof(T) == 4) {
+        // fp32 negabinary: every other level in one launch (timed as level 0)
+        Stage sg(h, 3, 0, st);
+        if ((rc = launch_nb_decode_multi(h->dseg, h->dseg_n, h->dseg_chunks, st))) return rc;
+    }
     for (int l = 0; l <= L; l++) {
-        if (fuse && l == L) continue;
+        if ((fuse && l == L) || (h->dseg && sizeof(T) == 4)) continue;
         const uint64_t n = g.elems[l];
         Stage sg(h, 3, l, st);
         if (h->nb) {

@@ -31,6 +31,17 @@ void count_launch();
 
 constexpr int kSMs = 152;   // GB300: 2 dies x 76 SMs
 
+// CTAs of `kernel` (threads, dynamic smem) resident on the whole current
+// device at once: the grid of a persistent grid-stride kernel, so that no CTA
+// waits for a second wave (cached per device, kernel and launch shape)
+unsigned resident_ctas(const void* kernel, int threads, size_t smem);
+inline unsigned persistent_grid_for(const void* kernel, int threads, size_t smem, uint64_t need, uint64_t max_grid) {
+    uint64_t g = resident_ctas(kernel, threads, smem);
+    if (g > need) g = need;
+    if (g > max_grid) g = max_grid;
+    return (unsigned)(g ? g : 1);
+}
+
 inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
     size_t g = (work + threads - 1) / threads;
     size_t cap = (size_t)kSMs * per_sm;
@@ -170,6 +181,17 @@ __device__ __forceinline__ void transpose32_regs(uint32_t (&a)[32]) {
             a[k] ^= t << j;
         }
     }
+}
+
+// last segment whose first global item is <= g (segments sorted by `begin`)
+template <class Seg>
+__device__ __forceinline__ int find_seg(const Seg* segs, int nseg, uint64_t g, uint64_t Seg::*begin) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].*begin <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 // |x| of a non-negative float/double as an order-preserving unsigned key

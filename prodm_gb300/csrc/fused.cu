@@ -146,11 +146,174 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
     }
 }
 
+// ---------------------------------------------------------------------------
+// Odd row length (n = 2^k + 1 and every other odd n): fine node 2c of a row is
+// coarse node c and the odd node 2c+1 lies between coarse nodes c and c+1, so
+// the row walk needs no index remapping. The planes of the next 8 rows are
+// fetched with cp.async into a second tile while the current rows are decoded
+// and recomposed; the coefficient buffer is value-major ([block][33]).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+constexpr int CB_LD = 33;   // value-major coefficient rows: conflict-free both ways
+
+__device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[r + (r >> 5)]; }
+
+// one fine row of odd length; M01 = odd-dim mask over dims 0/1 (0: both
+// coarse -> only odd nodes carry coefficients, ranks c; otherwise even node
+// 2c has rank c and odd node 2c+1 rank c2n + c)
+template <int M01>
+__device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0, uint64_t cs0, uint64_t cs1,
+                                                  uint32_t c2n, const float* __restrict__ cb, uint32_t rb0,
+                                                  float* __restrict__ orow, int lane) {
+    constexpr int NQ = M01 == 0 ? 1 : (M01 == 3 ? 4 : 2);
+    const float* pc[4];
+    pc[0] = cb0;
+    pc[1] = cb0 + (M01 == 1 ? cs0 : cs1);
+    pc[2] = cb0 + cs0;
+    pc[3] = cb0 + cs0 + cs1;
+    for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
+        const uint32_t c2 = cbase + lane;
+        const bool act = c2 < c2n;
+        const bool odd = c2 + 1 < c2n;
+        float q[NQ], qn[NQ];
+#pragma unroll
+        for (int i = 0; i < NQ; i++) q[i] = act ? __ldg(pc[i] + c2) : 0.f;
+#pragma unroll
+        for (int i = 0; i < NQ; i++) {
+            qn[i] = __shfl_down_sync(FULL, q[i], 1);
+            if (lane == 31 && odd) qn[i] = __ldg(pc[i] + c2 + 1);
+        }
+        if (!act) continue;
+        float* o = orow + 2 * (uint64_t)c2;
+        if (M01 == 0) {
+            o[0] = q[0];
+            if (odd) o[1] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], qn[0]));
+        } else if (M01 == 3) {
+            o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(avg_rn(q[0], q[1]), avg_rn(q[2], q[3])));
+            if (odd)
+                o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2),
+                                 avg_rn(avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])),
+                                        avg_rn(avg_rn(q[2], qn[2]), avg_rn(q[3], qn[3]))));
+        } else {
+            o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], q[1]));
+            if (odd)
+                o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2), avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint32_t* __restrict__ base, uint64_t stride,
+                                                                  const uint32_t* __restrict__ maxkey,
+                                                                  const uint8_t* __restrict__ dnum,
+                                                                  const float* __restrict__ coarse, Box F, Box C,
+                                                                  float* __restrict__ out, uint64_t s0, uint64_t s1,
+                                                                  uint32_t tld) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* tiles = smem;                                  // 2 x [plane][tld]
+    float* cb = (float*)(smem + 2 * 32 * tld);               // [tld][CB_LD]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int num = dnum[0];
+    const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
+    const bool neg = num != 0 && (num & 1);
+    const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
+    const float dscale = dfast ? pow2f_(exp - num) : 1.f;
+    const uint32_t rows = F.n[0] * F.n[1];
+    const uint32_t n2 = F.n[2], c2n = C.n[2];
+    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
+    auto row_rank = [&](uint32_t rho, uint32_t& r0, uint32_t& r1, bool& cc, uint64_t& rbase, uint32_t& len) {
+        r0 = rho / F.n[1];
+        r1 = rho - r0 * F.n[1];
+        cc = r0 < C.n[0] && r1 < C.n[1];
+        rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
+        len = cc ? n2 - c2n : n2;
+    };
+    // block range [fb, fb + nbk) of the coefficients of rows [rho0, rho0 + 8)
+    auto block_range = [&](uint32_t rho0, uint64_t& fb, uint32_t& nbk) {
+        const uint32_t rho_last = min(rho0 + 7, rows - 1);
+        uint32_t a0, a1, z0, z1, alen, zlen;
+        bool acc_, zcc;
+        uint64_t abase, zbase;
+        row_rank(rho0, a0, a1, acc_, abase, alen);
+        row_rank(rho_last, z0, z1, zcc, zbase, zlen);
+        fb = abase >> 5;
+        nbk = (uint32_t)(((zbase + zlen - 1) >> 5) - fb + 1);
+    };
+    auto fetch = [&](uint64_t fb, uint32_t nbk, uint32_t* tile) {
+        for (int p = warp; p < num; p += 8) {
+            const uint32_t* src = base + (uint64_t)p * stride + fb;
+            uint32_t* row = tile + p * tld;
+            for (uint32_t j = lane; j < nbk; j += 32) cp_async4(row + j, src + j);
+        }
+        cp_async_commit();
+    };
+    uint32_t rho0 = blockIdx.x * 8;
+    if (rho0 >= rows) return;
+    uint64_t fb, fb_next = 0;
+    uint32_t nbk, nbk_next = 0;
+    block_range(rho0, fb, nbk);
+    fetch(fb, nbk, tiles);
+    for (int it = 0; rho0 < rows; it++, rho0 += gridDim.x * 8) {
+        uint32_t* tile = tiles + (it & 1) * 32 * tld;
+        cp_async_wait_all();
+        __syncthreads();
+        const uint32_t rho_next = rho0 + gridDim.x * 8;
+        if (rho_next < rows) {
+            block_range(rho_next, fb_next, nbk_next);
+            fetch(fb_next, nbk_next, tiles + ((it + 1) & 1) * 32 * tld);
+        }
+        // decode: one thread per 32-value block (register bit transpose)
+        for (uint32_t t = threadIdx.x; t < nbk; t += blockDim.x) {
+            uint32_t a[32];
+#pragma unroll
+            for (int p = 0; p < 32; p++) a[p] = p < num ? tile[p * tld + t] : 0u;
+            transpose32_regs(a);
+            float* dst = cb + t * CB_LD;
+#pragma unroll
+            for (int v = 0; v < 32; v++) {
+                const uint32_t acc = num ? (__brev(a[v]) >> (32 - num)) : 0u;
+                float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - num)) : 0.f;
+                dst[v] = neg ? -val : val;
+            }
+        }
+        __syncthreads();
+        const uint32_t rho = rho0 + warp;
+        if (rho < rows) {
+            uint32_t r0, r1, len;
+            bool cc;
+            uint64_t rbase;
+            row_rank(rho, r0, r1, cc, rbase, len);
+            const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
+            const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+            const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
+            const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
+            const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
+            float* orow = out + x0 * s0 + x1 * s1;
+            const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
+            switch (m01) {
+                case 0: recompose_row_odd<0>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+                case 1: recompose_row_odd<1>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+                case 2: recompose_row_odd<2>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+                default: recompose_row_odd<3>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+            }
+        }
+        fb = fb_next;
+        nbk = nbk_next;
+    }
+    cp_async_wait_all();
+}
+
 }  // namespace
 
 static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
 static size_t fused_smem(const Box& F) {
     const uint32_t mb = fused_max_blocks(F);
+    if (F.n[2] & 1u) return (size_t)mb * 32 * 4 * 2 + (size_t)mb * CB_LD * 4;
     return (size_t)mb * 32 * 4 + (size_t)(mb | 1u) * 32 * 4;
 }
 
@@ -166,15 +329,22 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* 
                                  cudaStream_t st) {
     if (!decode_recompose_nb32_ok(F)) return PRODM_EUNSUPPORTED;
     const size_t smem = fused_smem(F);
+    const bool odd = (F.n[2] & 1u) != 0;
+    const void* kern = odd ? (const void*)k_decode_recompose_nb32_odd : (const void*)k_decode_recompose_nb32;
     if (smem > 48 * 1024) {   // per device; cheap to repeat
-        cudaError_t e = cudaFuncSetAttribute(k_decode_recompose_nb32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             200 * 1024);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
     }
     const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
     const uint64_t need = (rows + 7) / 8;
-    const uint64_t cap = (uint64_t)kSMs * 6;
-    const unsigned grid = (unsigned)(need < cap ? need : cap);
+    if (odd) {
+        const unsigned grid = persistent_grid_for(kern, 256, smem, need, need);
+        k_decode_recompose_nb32_odd<<<grid, 256, smem, st>>>((const uint32_t*)base, stride, (const uint32_t*)maxkey,
+                                                             dnum, coarse, F, C, out, s0, s1, fused_max_blocks(F));
+        PRODM_CHECK_LAUNCH("k_decode_recompose_nb32_odd");
+        return PRODM_OK;
+    }
+    const unsigned grid = persistent_grid_for((const void*)k_decode_recompose_nb32, 256, smem, need, need);
     k_decode_recompose_nb32<<<grid, 256, smem, st>>>((const uint32_t*)base, stride, (const uint32_t*)maxkey, dnum,
                                                      coarse, F, C, out, s0, s1, fused_max_blocks(F));
     PRODM_CHECK_LAUNCH("k_decode_recompose_nb32");

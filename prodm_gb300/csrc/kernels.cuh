@@ -63,6 +63,26 @@ int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, co
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
                      cudaStream_t st);
 
+// batch.cu: one segment per (field, level) of the multi-level fp32
+// negabinary encode / decode launches; chunk_begin is the segment's first
+// global chunk (NB_CHUNK blocks each)
+struct ChunkSeg {
+    const float* x;         // encode input
+    float* y;               // decode output
+    uint32_t* words;        // plane 0 of the level's streams
+    uint64_t n, nblocks, stride;
+    const uint32_t* key;
+    const uint8_t* dnum;    // decode: retrieved plane count
+    uint64_t chunk_begin;
+};
+int launch_nb_decode_multi(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st);
+// bitplane.cu: every level of one fp32 field in one encode launch; with
+// errs_out, per-level squared-error tables (partial: nseg * nb_encode_levels_grid(1)
+// * (B + 1) doubles)
+int nb_encode_levels_grid(int with_errors);
+int launch_nb_encode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, int B, double* partial,
+                            const uint32_t* keys, double* errs_out, cudaStream_t st);
+
 // fused.cu
 bool decode_recompose_nb32_ok(const Box& F);
 int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* maxkey, const uint8_t* dnum,

@@ -205,3 +205,27 @@ def test_reconstructor_fed_from_reference_files(enc):
         assert float(np.abs(out - field).max()) <= float(tol)
         if (idx > 0).all():
             np.testing.assert_allclose(out, g[enc + "_recon"][t], rtol=0, atol=1e-5 * float(np.abs(field).max()))
+
+
+@pytest.mark.parametrize("shape,L", [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129, 129, 129), 4),
+                                     ((200, 131), 4)])
+def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
+    """fp32 negabinary hierarchical: the finest level is decoded inside the
+    recomposition kernel (odd and even row lengths take different kernels);
+    the other levels go through the multi-level decoder. The output equals the
+    oracle's decode -> reposition -> recompose in float bit for bit."""
+    B = 32
+    x = fields().spectral_grf(shape, seed=sum(shape)).cpu().numpy()
+    mdr = api().MDRField(shape, torch.float32, L, B, "negabinary", "hierarchical", "max")
+    mdr.refactor(torch.from_numpy(x).cuda())
+    sizes, bounds, _ = mdr.level_info()
+    blob = np.concatenate([mdr.export_level(l) for l in range(L + 1)])
+    rng = np.random.default_rng(len(shape) + L)
+    cases = [np.zeros(L + 1, np.uint8), np.full(L + 1, B, np.uint8)]
+    cases += [rng.integers(0, B + 1, L + 1).astype(np.uint8) for _ in range(4)]
+    cases += [np.full(L + 1, k, np.uint8) for k in (1, 2, 7, 16, 17, 31)]
+    for idx in cases:
+        mdr.reset()
+        out = mdr.retrieve_planes([int(v) for v in idx]).cpu().numpy()
+        ref = O.retrieve(shape, L, B, blob, sizes, bounds.astype(np.float32), idx, "negabinary", True)
+        assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), idx
