@@ -205,7 +205,10 @@ def stage_bytes(mdr, kind, level, step_bytes_info):
     if kind == "decompose":
         return 2 * 4 * box(level)
     if kind == "encode":
-        return 4 * n + int(sizes[level].astype(np.int64).sum())
+        levels = [level]
+        if level == step_bytes_info["L"] and step_bytes_info.get("encode_multi"):
+            levels = range(0, level + 1)     # one launch encodes every level
+        return sum(4 * int(mdr.level_elements[l]) + int(sizes[l].astype(np.int64).sum()) for l in levels)
     if kind == "decode":
         levels = [level]
         if level == 0 and step_bytes_info.get("decode_multi"):
@@ -329,7 +332,8 @@ def run_ours(args):
     # roofline of the dominant stage
     peak, peak_src = measured_peak()
     info = {"sizes": sizes, "decode_bytes": decode_bytes, "L": LEVELS,
-            "fused": ("decode", LEVELS) not in stages, "decode_multi": ("decode", 1) not in stages}
+            "fused": ("decode", LEVELS) not in stages, "decode_multi": ("decode", 1) not in stages,
+            "encode_multi": ("encode", 0) not in stages}
     per_stage = {}
     for (kind, level), (tms, cnt) in stages.items():
         b = stage_bytes(mdr, kind, level, info)

@@ -499,6 +499,11 @@ struct prodm_mdr {
     ChunkSeg* dseg = nullptr;
     int dseg_n = 0;
     uint64_t dseg_chunks = 0;
+    // fp32 negabinary: every level encoded by one launch (per-level partial
+    // error tables in lpartial)
+    ChunkSeg* eseg = nullptr;
+    uint64_t eseg_chunks = 0;
+    double* lpartial = nullptr;
     uint8_t* pack_tmp = nullptr;
     // reconstructor fed from level files (reference on-disk format)
     bool from_files = false;
@@ -692,6 +697,28 @@ int mdr_alloc_all(prodm_mdr* h) {
         PRODM_CUDA(cudaMemcpy(h->dseg, segs.data(), segs.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
         h->dseg_n = (int)segs.size();
         h->dseg_chunks = chunks;
+        // encode: every level, coefficients in, planes out
+        std::vector<ChunkSeg> esegs;
+        chunks = 0;
+        for (int l = 0; l <= L; l++) {
+            ChunkSeg q{};
+            q.x = (const float*)h->coef + g.offset[l];
+            q.words = (uint32_t*)(h->streams + h->lvl_byte_off[l]);
+            q.n = g.elems[l];
+            q.nblocks = h->nblocks[l];
+            q.stride = h->nblocks[l];
+            q.key = (const uint32_t*)h->keys + l;
+            q.chunk_begin = chunks;
+            chunks += (q.nblocks + 255) / 256;
+            esegs.push_back(q);
+        }
+        if ((rc = h->alloc((void**)&h->eseg, esegs.size() * sizeof(ChunkSeg)))) return rc;
+        PRODM_CUDA(cudaMemcpy(h->eseg, esegs.data(), esegs.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
+        h->eseg_chunks = chunks;
+        if (h->sq) {
+            const size_t rows = (size_t)(L + 1) * nb_encode_levels_grid(1);
+            if ((rc = h->alloc((void**)&h->lpartial, rows * (B + 1) * sizeof(double)))) return rc;
+        }
     }
     return PRODM_OK;
 }
@@ -734,6 +761,12 @@ int mdr_refactor(prodm_mdr* h, const T* field, cudaStream_t st) {
         if (h->orth && (rc = launch_maxabs<T>(coef, g.elems[0], keys, st))) return rc;
     }
     if ((rc = launch_bounds_from_keys<T>(keys, L + 1, h->nb ? 1 : 0, (T*)h->bounds, st))) return rc;
+    if (h->eseg && sizeof(T) == 4) {
+        // fp32 negabinary: every level in one launch (timed as the finest level)
+        Stage sg(h, 1, L, st);
+        return launch_nb_encode_levels(h->eseg, L + 1, h->eseg_chunks, B, h->lpartial, (const uint32_t*)keys,
+                                       h->sq ? h->sqerr : nullptr, st);
+    }
     for (int l = 0; l <= L; l++) {
         const uint64_t n = g.elems[l];
         uint8_t* out = h->streams + h->lvl_byte_off[l];

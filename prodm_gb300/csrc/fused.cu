@@ -166,47 +166,95 @@ __device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[
 
 // one fine row of odd length; M01 = odd-dim mask over dims 0/1 (0: both
 // coarse -> only odd nodes carry coefficients, ranks c; otherwise even node
-// 2c has rank c and odd node 2c+1 rank c2n + c)
+// 2c has rank c and odd node 2c+1 rank c2n + c). Lane l handles coarse
+// columns 32k + l; the corner values of D column groups are in flight at
+// once (a ring of D groups in registers, refilled as each group is used), so
+// a row waits for the L2 latency about once instead of once per group.
 template <int M01>
 __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0, uint64_t cs0, uint64_t cs1,
                                                   uint32_t c2n, const float* __restrict__ cb, uint32_t rb0,
                                                   float* __restrict__ orow, int lane) {
     constexpr int NQ = M01 == 0 ? 1 : (M01 == 3 ? 4 : 2);
+    constexpr int D = M01 == 3 ? 3 : 4;
     const float* pc[4];
     pc[0] = cb0;
     pc[1] = cb0 + (M01 == 1 ? cs0 : cs1);
     pc[2] = cb0 + cs0;
     pc[3] = cb0 + cs0 + cs1;
-    for (uint32_t cbase = 0; cbase < c2n; cbase += 32) {
-        const uint32_t c2 = cbase + lane;
-        const bool act = c2 < c2n;
-        const bool odd = c2 + 1 < c2n;
-        float q[NQ], qn[NQ];
+    auto load = [&](uint32_t k, float (&q)[NQ]) {
+        const uint32_t c = 32 * k + lane;
 #pragma unroll
-        for (int i = 0; i < NQ; i++) q[i] = act ? __ldg(pc[i] + c2) : 0.f;
+        for (int i = 0; i < NQ; i++) q[i] = c < c2n ? __ldg(pc[i] + c) : 0.f;
+    };
+    const uint32_t groups = (c2n + 31) / 32;
+    float ring[D][NQ];
 #pragma unroll
-        for (int i = 0; i < NQ; i++) {
-            qn[i] = __shfl_down_sync(FULL, q[i], 1);
-            if (lane == 31 && odd) qn[i] = __ldg(pc[i] + c2 + 1);
-        }
-        if (!act) continue;
-        float* o = orow + 2 * (uint64_t)c2;
-        if (M01 == 0) {
-            o[0] = q[0];
-            if (odd) o[1] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], qn[0]));
-        } else if (M01 == 3) {
-            o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(avg_rn(q[0], q[1]), avg_rn(q[2], q[3])));
-            if (odd)
-                o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2),
-                                 avg_rn(avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])),
-                                        avg_rn(avg_rn(q[2], qn[2]), avg_rn(q[3], qn[3]))));
-        } else {
-            o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], q[1]));
-            if (odd)
-                o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2), avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])));
+    for (int d = 0; d < D; d++) load(d, ring[d]);
+    for (uint32_t k0 = 0; k0 < groups; k0 += D) {
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const uint32_t k = k0 + d;
+            if (k >= groups) break;
+            const float(&q)[NQ] = ring[d];
+            const float(&qx)[NQ] = ring[(d + 1) % D];   // group k + 1
+            // lane l < 31 takes column c+1 from lane l+1; lane 31 from lane 0 of group k+1
+            float qn[NQ];
+#pragma unroll
+            for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], (lane + 1) & 31);
+            const uint32_t c2 = 32 * k + lane;
+            if (c2 < c2n) {
+                const bool odd = c2 + 1 < c2n;
+                float* o = orow + 2 * (uint64_t)c2;
+                if (M01 == 0) {
+                    o[0] = q[0];
+                    if (odd) o[1] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], qn[0]));
+                } else if (M01 == 3) {
+                    o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(avg_rn(q[0], q[1]), avg_rn(q[2], q[3])));
+                    if (odd)
+                        o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2),
+                                         avg_rn(avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])),
+                                                avg_rn(avg_rn(q[2], qn[2]), avg_rn(q[3], qn[3]))));
+                } else {
+                    o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], q[1]));
+                    if (odd)
+                        o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2),
+                                         avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])));
+                }
+            }
+            load(k + D, ring[d]);   // refill: group k + D
         }
     }
 }
+
+// Half of a 32 x 32 bit transpose: rows R[0..31] (R[r] bit e) -> the 16
+// words out[v] (v = 16 * half + 0..15) whose bit r is R[r] bit v. The two
+// byte-granular stages are byte permutes, the three sub-byte stages
+// mask-and-shift swaps.
+__device__ __forceinline__ void transpose32_half(const uint32_t (&R)[32], int half, uint32_t (&a)[16]) {
+    const uint32_t sel16 = half ? 0x7632u : 0x5410u;
+#pragma unroll
+    for (int k = 0; k < 16; k++) a[k] = __byte_perm(R[k], R[k + 16], sel16);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t x = a[k], y = a[k + 8];
+        a[k] = __byte_perm(x, y, 0x6240u);
+        a[k + 8] = __byte_perm(x, y, 0x7351u);
+    }
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        const int j = 4 >> s;
+        const uint32_t m = s == 0 ? 0x0f0f0f0fu : s == 1 ? 0x33333333u : 0x55555555u;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int k = (i / j) * 2 * j + (i % j);
+            const uint32_t t = ((a[k] >> j) ^ a[k + j]) & m;
+            a[k + j] ^= t;
+            a[k] ^= t << j;
+        }
+    }
+}
+
+constexpr int TB_LD = 36;   // block-major plane tile row: 32 planes + pad, 16-byte aligned rows
 
 __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint32_t* __restrict__ base, uint64_t stride,
                                                                   const uint32_t* __restrict__ maxkey,
@@ -214,15 +262,15 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
                                                                   const float* __restrict__ coarse, Box F, Box C,
                                                                   float* __restrict__ out, uint64_t s0, uint64_t s1,
                                                                   uint32_t tld) {
-    extern __shared__ uint32_t smem[];
-    uint32_t* tiles = smem;                                  // 2 x [plane][tld]
-    float* cb = (float*)(smem + 2 * 32 * tld);               // [tld][CB_LD]
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* tiles = smem;                                  // 2 x [block][TB_LD]
+    float* cb = (float*)(smem + 2 * TB_LD * tld);            // [block][CB_LD]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int num = dnum[0];
     const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
-    const bool neg = num != 0 && (num & 1);
+    const bool neg = num != 0 && (num & 1);                  // NegaBinaryBPEncoder.hpp:153, :177
     const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
-    const float dscale = dfast ? pow2f_(exp - num) : 1.f;
+    const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t n2 = F.n[2], c2n = C.n[2];
     const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
@@ -244,41 +292,63 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
         fb = abase >> 5;
         nbk = (uint32_t)(((zbase + zlen - 1) >> 5) - fb + 1);
     };
+    // plane p of block j -> tile[j * TB_LD + p]; warp w copies planes w, w+8, ..
     auto fetch = [&](uint64_t fb, uint32_t nbk, uint32_t* tile) {
         for (int p = warp; p < num; p += 8) {
             const uint32_t* src = base + (uint64_t)p * stride + fb;
-            uint32_t* row = tile + p * tld;
-            for (uint32_t j = lane; j < nbk; j += 32) cp_async4(row + j, src + j);
+            for (uint32_t j = lane; j < nbk; j += 32) cp_async4(tile + j * TB_LD + p, src + j);
         }
         cp_async_commit();
     };
     uint32_t rho0 = blockIdx.x * 8;
     if (rho0 >= rows) return;
+    // planes >= num stay zero in both tiles
+    for (uint32_t i = threadIdx.x; i < 2 * tld * (32 - num); i += blockDim.x) {
+        const uint32_t row = i / (32 - num), p = num + (i - row * (32 - num));
+        tiles[row * TB_LD + p] = 0u;
+    }
+    __syncthreads();
     uint64_t fb, fb_next = 0;
     uint32_t nbk, nbk_next = 0;
     block_range(rho0, fb, nbk);
     fetch(fb, nbk, tiles);
     for (int it = 0; rho0 < rows; it++, rho0 += gridDim.x * 8) {
-        uint32_t* tile = tiles + (it & 1) * 32 * tld;
+        const uint32_t* tile = tiles + (it & 1) * TB_LD * tld;
         cp_async_wait_all();
         __syncthreads();
         const uint32_t rho_next = rho0 + gridDim.x * 8;
         if (rho_next < rows) {
             block_range(rho_next, fb_next, nbk_next);
-            fetch(fb_next, nbk_next, tiles + ((it + 1) & 1) * 32 * tld);
+            fetch(fb_next, nbk_next, tiles + ((it + 1) & 1) * TB_LD * tld);
         }
-        // decode: one thread per 32-value block (register bit transpose)
-        for (uint32_t t = threadIdx.x; t < nbk; t += blockDim.x) {
-            uint32_t a[32];
+        // decode: two threads per 32-value block, each transposing one half;
+        // rows are taken in reverse plane order so that value v's digits come
+        // out most significant first (no bit reversal)
+        for (uint32_t i = threadIdx.x; i < 2 * nbk; i += blockDim.x) {
+            const uint32_t t = i >> 1;
+            const int half = i & 1;
+            float* dst = cb + t * CB_LD + 16 * half;
+            if (num == 0) {
 #pragma unroll
-            for (int p = 0; p < 32; p++) a[p] = p < num ? tile[p * tld + t] : 0u;
-            transpose32_regs(a);
-            float* dst = cb + t * CB_LD;
+                for (int v = 0; v < 16; v++) dst[v] = 0.f;
+                continue;
+            }
+            uint32_t R[32];
+            const uint4* src = reinterpret_cast<const uint4*>(tile + t * TB_LD);
 #pragma unroll
-            for (int v = 0; v < 32; v++) {
-                const uint32_t acc = num ? (__brev(a[v]) >> (32 - num)) : 0u;
-                float val = num ? (dfast ? (float)nb_to_bin(acc) * dscale : ldexpf((float)nb_to_bin(acc), exp - num)) : 0.f;
-                dst[v] = neg ? -val : val;
+            for (int q = 0; q < 8; q++) {
+                const uint4 w = src[q];
+                R[31 - 4 * q] = w.x;
+                R[30 - 4 * q] = w.y;
+                R[29 - 4 * q] = w.z;
+                R[28 - 4 * q] = w.w;
+            }
+            uint32_t a[16];
+            transpose32_half(R, half, a);
+#pragma unroll
+            for (int v = 0; v < 16; v++) {
+                const int32_t iv = nb_to_bin(a[v] >> (32 - num));
+                dst[v] = dfast ? (float)iv * dscale : (neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num));
             }
         }
         __syncthreads();
@@ -313,7 +383,7 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
 static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
 static size_t fused_smem(const Box& F) {
     const uint32_t mb = fused_max_blocks(F);
-    if (F.n[2] & 1u) return (size_t)mb * 32 * 4 * 2 + (size_t)mb * CB_LD * 4;
+    if (F.n[2] & 1u) return (size_t)mb * TB_LD * 4 * 2 + (size_t)mb * CB_LD * 4;
     return (size_t)mb * 32 * 4 + (size_t)(mb | 1u) * 32 * 4;
 }
 

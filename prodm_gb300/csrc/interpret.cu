@@ -53,12 +53,23 @@ struct DevEstimator {
     }
 };
 
-struct Item { double u; int level; int num; };
+// A heap entry carries its efficiency as an order-preserving integer key
+// (equal doubles -> equal keys, +0 and -0 included) and a NaN flag, so the
+// heap's `a.u < b.u` is evaluated with integer compares: every comparison
+// with a NaN is false, as for the doubles.
+struct Item { long long key; int nan; int level; int num; };
+
+__device__ __forceinline__ void eff_key(double u, long long& key, int& nan) {
+    const long long bits = __double_as_longlong(u);
+    const long long mag = bits & 0x7fffffffffffffffll;
+    nan = mag > 0x7ff0000000000000ll;
+    key = mag == 0 ? 0 : (bits >= 0 ? bits : (bits ^ 0x7fffffffffffffffll));
+}
 
 struct DevHeap {
     Item h[kMaxLevels + 1];
     int len;
-    __device__ static bool less(const Item& a, const Item& b) { return a.u < b.u; }
+    __device__ static bool less(const Item& a, const Item& b) { return !(a.nan | b.nan) && a.key < b.key; }
     __device__ void sift_up(int hole, int top, Item v) {
         int parent = (hole - 1) / 2;
         while (hole > top && less(h[parent], v)) { h[hole] = h[parent]; hole = parent; parent = (hole - 1) / 2; }
@@ -118,16 +129,18 @@ __device__ void eff_entry(int kind, const DevEstimator<T>& est, int B, const uin
     num = cn;
 }
 
-template <class T>
-__device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int B, const uint32_t* __restrict__ sizes,
-                               const double* __restrict__ errs, const double* __restrict__ eu,
-                               const int8_t* __restrict__ en, double tol, uint8_t* index, uint32_t* rsz) {
-    auto E = [&](int l, int j) { return errs[(size_t)l * (B + 1) + j]; };
+// ev[l * 65 + j] = (double) estimator(errors[l][j], l), tabulated by the CTA
+// (the reference converts the estimator's T result to double on every use)
+__device__ void interpret_core(int kind, int nl, int B, const uint32_t* __restrict__ sizes,
+                               const double* __restrict__ ev, const long long* __restrict__ ekey,
+                               const int8_t* __restrict__ enan, const int8_t* __restrict__ en, double tol,
+                               uint8_t* index, uint32_t* rsz) {
+    auto EST = [&](int l, int j) { return ev[l * 65 + j]; };
     auto S = [&](int l, int j) { return sizes[(size_t)l * B + j]; };
-    auto item = [&](int l, int j) { return Item{eu[l * 64 + j], l, (int)en[l * 64 + j]}; };
+    auto item = [&](int l, int j) { return Item{ekey[l * 64 + j], (int)enan[l * 64 + j], l, (int)en[l * 64 + j]}; };
     for (int i = 0; i < nl; i++) rsz[i] = 0;
     double acc = 0;
-    for (int i = 0; i < nl; i++) acc += est.est((T)E(i, index[i]), i);
+    for (int i = 0; i < nl; i++) acc += EST(i, index[i]);
     DevHeap heap;
     heap.len = 0;
     if (kind == 0) {
@@ -141,8 +154,8 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
             heap.pop();
             int i = t.level, j = index[i];
             rsz[i] += S(i, j);
-            acc -= est.est((T)E(i, j), i);
-            acc += est.est((T)E(i, j + 1), i);
+            acc -= EST(i, j);
+            acc += EST(i, j + 1);
             if (acc < tol) met = true;
             index[i]++;
             if (index[i] != B) heap.push(item(i, index[i]));
@@ -153,12 +166,12 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
         if (acc < tol) return;
         double minerr = acc;
         for (int i = 0; i < nl; i++) {
-            minerr -= est.est((T)E(i, index[i]), i);
-            minerr += est.est((T)E(i, B), i);
+            minerr -= EST(i, index[i]);
+            minerr += EST(i, B);
             if (index[i] == 0) {
                 rsz[i] += S(i, 0);
-                acc -= est.est((T)E(i, 0), i);
-                acc += est.est((T)E(i, 1), i);
+                acc -= EST(i, 0);
+                acc += EST(i, 1);
                 index[i]++;
             }
             if (index[i] != B) heap.push(item(i, index[i]));
@@ -170,8 +183,8 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
             heap.pop();
             int i = t.level, j = index[i];
             rsz[i] += S(i, j);
-            acc -= est.est((T)E(i, j), i);
-            acc += est.est((T)E(i, j + 1), i);
+            acc -= EST(i, j);
+            acc += EST(i, j + 1);
             if (acc < tol) met = true;
             index[i]++;
             if (index[i] != B) heap.push(item(i, index[i]));
@@ -187,8 +200,8 @@ __device__ void interpret_core(int kind, const DevEstimator<T>& est, int nl, int
         heap.pop();
         int i = t.level, j = index[i], num = t.num;
         for (int k = 0; k < num; k++) rsz[i] += S(i, j + k);
-        acc -= est.est((T)E(i, j), i);
-        acc += est.est((T)E(i, j + num), i);
+        acc -= EST(i, j);
+        acc += EST(i, j + num);
         if (acc < tol) met = true;
         index[i] += num;
         if (index[i] != B) heap.push(item(i, index[i]));
@@ -211,19 +224,29 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
     const int nl = L + 1;
     __shared__ uint32_t s_sizes[kMaxLevels * 64];
     __shared__ double s_errs[kMaxLevels * 65];
-    __shared__ double s_eu[kMaxLevels * 64];
+    __shared__ double s_ev[kMaxLevels * 65];
+    __shared__ long long s_key[kMaxLevels * 64];
+    __shared__ int8_t s_nan[kMaxLevels * 64];
     __shared__ int8_t s_en[kMaxLevels * 64];
     for (int i = threadIdx.x; i < nl * B; i += blockDim.x) s_sizes[i] = sizes[f * sz_stride + i];
     for (int i = threadIdx.x; i < nl * (B + 1); i += blockDim.x) s_errs[i] = errs[f * err_stride + i];
     DevEstimator<T> est;
     est.init(est_kind, ndims[f], L, s);
     __syncthreads();
+    for (int t = threadIdx.x; t < nl * (B + 1); t += blockDim.x) {
+        const int l = t / (B + 1), j = t - l * (B + 1);
+        s_ev[l * 65 + j] = (double)est.est((T)s_errs[t], l);
+    }
     for (int t = threadIdx.x; t < nl * B; t += blockDim.x) {
         const int l = t / B, j = t - l * B;
         double u;
         int num;
         eff_entry<T>(kind, est, B, s_sizes, s_errs, l, j, u, num);
-        s_eu[l * 64 + j] = u;
+        long long key;
+        int nan;
+        eff_key(u, key, nan);
+        s_key[l * 64 + j] = key;
+        s_nan[l * 64 + j] = (int8_t)nan;
         s_en[l * 64 + j] = (int8_t)num;
     }
     __syncthreads();
@@ -232,7 +255,7 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
         uint32_t rs[kMaxLevels];
         uint8_t* gi = index + f * idx_stride;
         for (int i = 0; i < nl; i++) idx[i] = gi[i];
-        interpret_core<T>(kind, est, nl, B, s_sizes, s_errs, s_eu, s_en, tols ? tols[f] : tol0, idx, rs);
+        interpret_core(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tols ? tols[f] : tol0, idx, rs);
         uint32_t* gr = rsz + f * idx_stride;
         for (int i = 0; i < nl; i++) { gi[i] = idx[i]; gr[i] = rs[i]; }
     }
