@@ -149,6 +149,28 @@ int prodm_collect_squared_noalloc(int dtype, const void* d_data, uint64_t n, int
                                   double max_level_error, double* d_out, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Packed level coefficients <-> natural field, hierarchical basis.
+ * prodm_recompose_packed: d_coef holds every level's coefficients packed as
+ * the retrieval decodes them (level 0 box, then box(l) minus box(l-1) per
+ * level in interleaved order, the layout of prodm_mdr_coefficients); output
+ * is the natural-order field -- the reconstructor's reposition + recompose
+ * (ComposedReconstructor.hpp:124-131; MGARD.hpp:25-35).
+ * prodm_recompose_adjoint: its transpose. d_grad is the gradient of a scalar
+ * quantity of interest with respect to the natural-order field; d_grad_coef
+ * receives the gradient with respect to the packed level coefficients. No
+ * counterpart in the reference (the reference has no derivatives); it gives
+ * the per-level sensitivities used for QoI-bounded retrieval.
+ * Workspace (both): prodm_recompose_packed_workspace bytes, or NULL to let
+ * the call allocate it stream-ordered.
+ * ------------------------------------------------------------------------- */
+int prodm_recompose_packed_workspace(int dtype, int ndims, const uint32_t* dims, uint32_t target_level,
+                                     size_t* bytes);
+int prodm_recompose_packed(int dtype, const void* d_coef, int ndims, const uint32_t* dims, uint32_t target_level,
+                           void* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
+int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint32_t* dims, uint32_t target_level,
+                            void* d_grad_coef, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Size interpreter -- SizeInterpreterInterface::interpret_retrieve_size
  * (SizeInterpreterInterface.hpp:13). Runs on the device. d_sizes[nl*B] plane
  * byte sizes, d_errors[nl*(B+1)] level error tables, d_index[nl] in/out

@@ -168,6 +168,22 @@ class Oracle(_Lib):
         f(out, len(dims), np.asarray(dims, np.uint32), L, int(hierarchical))
         return out
 
+    def recompose_packed(self, packed, dims, L, hierarchical=True):
+        """packed level coefficients -> natural field (the forward of the adjoint pair)."""
+        t = packed.dtype
+        f = self._fn("or_recompose_packed_" + _sfx(t), None, _tp(t), C.c_int, _u32p, C.c_int, C.c_int, _tp(t))
+        out = np.zeros(int(np.prod(dims)), t)
+        f(np.ascontiguousarray(packed), len(dims), np.asarray(dims, np.uint32), L, int(hierarchical), out)
+        return out.reshape(tuple(dims))
+
+    def recompose_adjoint(self, grad, dims, L):
+        """transpose of recompose_packed (hierarchical basis)."""
+        t = grad.dtype
+        f = self._fn("or_recompose_adjoint_" + _sfx(t), None, _tp(t), C.c_int, _u32p, C.c_int, _tp(t))
+        out = np.zeros(int(np.prod(dims)), t)
+        f(np.ascontiguousarray(grad).ravel(), len(dims), np.asarray(dims, np.uint32), L, out)
+        return out
+
     # composed -------------------------------------------------------------
     def refactor(self, field, L, B, encoder="negabinary", hierarchical=True, collect=False):
         """Composed refactor. Returns dict(blob, sizes[L+1,B], bounds[L+1], errs, coeffs)."""

@@ -42,6 +42,36 @@ int64_t refactor(const T* field, int ndims, const uint32_t* dims_, int L, int B,
     return (int64_t)off;
 }
 
+template <class T>
+void packed_recompose(const T* packed, const std::vector<uint32_t>& dims, int L, bool hier, T* out) {
+    auto ld = level_dims(dims, L);
+    auto le = level_elements(ld);
+    std::vector<uint32_t> zero(dims.size(), 0);
+    size_t N = 1; for (auto x : dims) N *= x;
+    std::fill(out, out + N, (T)0);
+    size_t off = 0;
+    for (int l = 0; l <= L; l++) {
+        reposition<T>(packed + off, dims, ld[l], l == 0 ? zero : ld[l - 1], out);
+        off += le[l];
+    }
+    recompose<T>(out, dims, L, hier, {});
+}
+
+template <class T>
+void packed_adjoint(const T* grad, const std::vector<uint32_t>& dims, int L, T* packed) {
+    auto ld = level_dims(dims, L);
+    auto le = level_elements(ld);
+    std::vector<uint32_t> zero(dims.size(), 0);
+    size_t N = 1; for (auto x : dims) N *= x;
+    std::vector<T> g(grad, grad + N);
+    recompose_adjoint<T>(g.data(), dims, L);
+    size_t off = 0;
+    for (int l = 0; l <= L; l++) {
+        interleave<T>(g.data(), dims, ld[l], l == 0 ? zero : ld[l - 1], packed + off);
+        off += le[l];
+    }
+}
+
 // Retrieval that decodes all planes [0, index[l]) of every level and
 // recomposes to full resolution (device-path semantics).
 template <class T>
@@ -132,6 +162,14 @@ void or_level_elements(int ndims, const uint32_t* dims, int L, uint32_t* out) {
     void or_recompose_strided_##SUF(T* d, int ndims, const uint32_t* dims, int L, int hier,                   \
                                     const uint32_t* strides) {                                                \
         recompose<T>(d, vec(dims, ndims), L, hier != 0, vec(strides, ndims));                                 \
+    }                                                                                                         \
+    /* packed levels (level 0 box, then box(l) minus box(l-1) per level, in     \
+       interleaved order) -> natural field, and its transpose (hierarchical) */ \
+    void or_recompose_packed_##SUF(const T* packed, int ndims, const uint32_t* dims, int L, int hier, T* out) { \
+        packed_recompose<T>(packed, vec(dims, ndims), L, hier != 0, out);                                     \
+    }                                                                                                         \
+    void or_recompose_adjoint_##SUF(const T* grad, int ndims, const uint32_t* dims, int L, T* packed) {      \
+        packed_adjoint<T>(grad, vec(dims, ndims), L, packed);                                                 \
     }                                                                                                         \
     int64_t or_refactor_##SUF(const T* f, int ndims, const uint32_t* dims, int L, int B, int enc, int hier,   \
                               int collect, uint8_t* blob, uint32_t* sizes, T* bounds, double* errs,           \

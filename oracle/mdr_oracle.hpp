@@ -744,6 +744,60 @@ void recompose_level(T* data, const size_t n[3], const size_t s[3], bool hierarc
         data[i * s[0] + j * s[1] + k * s[2]] = V[(i * n[1] + j) * n[2] + k];
 }
 
+// Adjoint (transpose) of recompose_level for the hierarchical basis, written
+// as reverse-mode differentiation of the loop above: g holds the gradient
+// with respect to the natural-order values of the sub-box on entry and the
+// gradient with respect to its in-place (reordered) coefficients on exit.
+// Every masked node passes its gradient to its own coefficient and, through
+// the interpolation weights (1/2 per odd dim), to its coarse corners.
+template <class T>
+void interp_adjoint(T* gV, const size_t n[3], const size_t x[3], int mask, T w) {
+    if (mask == 0) { gV[(x[0] * n[1] + x[1]) * n[2] + x[2]] += w; return; }
+    int d = (mask & 1) ? 0 : (mask & 2) ? 1 : 2;
+    int rest = mask & ~(1 << d);
+    size_t a[3] = {x[0], x[1], x[2]}, b[3] = {x[0], x[1], x[2]};
+    a[d] -= 1; b[d] += 1;
+    interp_adjoint(gV, n, a, rest, (T)0.5 * w);
+    interp_adjoint(gV, n, b, rest, (T)0.5 * w);
+}
+
+template <class T>
+void recompose_level_adjoint(T* g, const size_t n[3], const size_t s[3]) {
+    DimMap dm[3] = {DimMap(n[0]), DimMap(n[1]), DimMap(n[2])};
+    size_t N = n[0] * n[1] * n[2];
+    std::vector<T> gV(N), out(N, 0);
+    for (size_t i = 0; i < n[0]; i++) for (size_t j = 0; j < n[1]; j++) for (size_t k = 0; k < n[2]; k++)
+        gV[(i * n[1] + j) * n[2] + k] = g[i * s[0] + j * s[1] + k * s[2]];
+    // masked nodes: V(x) = c(x) + interp(x)  =>  g_c(x) = gV(x); corners += w gV(x)
+    size_t x[3];
+    for (x[0] = 0; x[0] < n[0]; x[0]++) for (x[1] = 0; x[1] < n[1]; x[1]++) for (x[2] = 0; x[2] < n[2]; x[2]++) {
+        int mask = (!dm[0].coarse(x[0]) ? 1 : 0) | (!dm[1].coarse(x[1]) ? 2 : 0) | (!dm[2].coarse(x[2]) ? 4 : 0);
+        if (!mask) continue;
+        T gx = gV[(x[0] * n[1] + x[1]) * n[2] + x[2]];
+        out[(dm[0].reord(x[0]) * n[1] + dm[1].reord(x[1])) * n[2] + dm[2].reord(x[2])] = gx;
+        interp_adjoint(gV.data(), n, x, mask, gx);
+    }
+    // coarse nodes: V(fine(c)) = C(c)  =>  g_C(c) = gV(fine(c)), stored at the reordered corner
+    for (size_t i = 0; i < dm[0].nc; i++) for (size_t j = 0; j < dm[1].nc; j++) for (size_t k = 0; k < dm[2].nc; k++)
+        out[(i * n[1] + j) * n[2] + k] =
+            gV[(dm[0].fine_of_coarse(i) * n[1] + dm[1].fine_of_coarse(j)) * n[2] + dm[2].fine_of_coarse(k)];
+    for (size_t i = 0; i < n[0]; i++) for (size_t j = 0; j < n[1]; j++) for (size_t k = 0; k < n[2]; k++)
+        g[i * s[0] + j * s[1] + k * s[2]] = out[(i * n[1] + j) * n[2] + k];
+}
+
+// Transpose of recompose(data, dims, L, hierarchical = true): natural-order
+// field gradient in, gradient with respect to the in-place coefficients out.
+template <class T>
+void recompose_adjoint(T* g, const std::vector<uint32_t>& dims, int L) {
+    size_t D[3]; pad3(dims, D);
+    size_t s[3] = {D[1] * D[2], D[2], 1};
+    auto ld = level_dims(dims, L);
+    for (int l = L; l >= 1; l--) {
+        size_t n[3]; pad3(ld[l], n);
+        recompose_level_adjoint(g, n, s);
+    }
+}
+
 // Decomposer::decompose(data, dims, L, hierarchical, strides) as called at
 // MGARD.hpp:18/:22/:49/:53. Levels go fine -> coarse on the level boxes.
 template <class T>

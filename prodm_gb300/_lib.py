@@ -57,6 +57,9 @@ _SIGS = {
     "prodm_collect_squared_workspace": (_i, [_i, _i, C.POINTER(C.c_size_t)]),
     "prodm_collect_squared": (_i, [_i, _P, C.c_uint64, _i, C.c_double, _P, _P, C.c_size_t, _P]),
     "prodm_collect_squared_noalloc": (_i, [_i, _P, C.c_uint64, _i, C.c_double, _P, _P]),
+    "prodm_recompose_packed_workspace": (_i, [_i, _i, _u32p, C.c_uint32, C.POINTER(C.c_size_t)]),
+    "prodm_recompose_packed": (_i, [_i, _P, _i, _u32p, C.c_uint32, _P, _P, C.c_size_t, _P]),
+    "prodm_recompose_adjoint": (_i, [_i, _P, _i, _u32p, C.c_uint32, _P, _P, C.c_size_t, _P]),
     "prodm_interpret": (_i, [_i, _i, _i, _i, _i, C.c_double, _i, _i, _P, _P, C.c_double, _P, _P, _P]),
     "prodm_mdr_create": (_i, [C.POINTER(_P), C.POINTER(prodm_config)]),
     "prodm_mdr_refactor": (_i, [_P, _P, _P]),

@@ -1024,6 +1024,50 @@ int mdr_load_level(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t 
 }  // namespace prodm
 
 // ===========================================================================
+// packed level coefficients <-> natural field (hierarchical basis), the pair
+// behind the QoI gradient: forward = reposition every level + recompose
+// (ComposedReconstructor.hpp:124-131 with MGARD.hpp:25-35), adjoint = its
+// transpose. Workspace: two boxes of level L-1.
+namespace prodm {
+template <class T>
+int packed_pair_impl(const T* in, int ndims, const uint32_t* dims, int L, T* out, bool adjoint, void* wsp, size_t wsb,
+                     cudaStream_t st) {
+    LevelGeom g;
+    int rc;
+    if ((rc = make_geom(ndims, dims, L, g))) return rc;
+    if (L > max_level(ndims, dims)) return fail(PRODM_EINVAL, "target level above the maximum for these dims");
+    if (L == 0) {
+        PRODM_CUDA(cudaMemcpyAsync(out, in, g.total * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        return PRODM_OK;
+    }
+    const size_t cb = g.box[L - 1].size() * sizeof(T);
+    Workspace ws(wsp, wsb, st);
+    ws.reserve(cb);
+    ws.reserve(cb);
+    if ((rc = ws.commit())) return rc;
+    T* buf[2] = {(T*)ws.take(cb), (T*)ws.take(cb)};
+    if (!adjoint) {
+        for (int l = 1; l <= L; l++) {
+            const Box& F = g.box[l];
+            const T* cin = (l == 1) ? in + g.offset[0] : buf[(l - 1) & 1];
+            T* o = (l == L) ? out : buf[l & 1];
+            if ((rc = launch_recompose_level_packed<T>(cin, in + g.offset[l], F, g.box[l - 1], o,
+                                                       (uint64_t)F.n[1] * F.n[2], F.n[2], st)))
+                return rc;
+        }
+        return PRODM_OK;
+    }
+    const T* gin = in;
+    for (int l = L; l >= 1; l--) {
+        T* gout = (l == 1) ? out + g.offset[0] : buf[l & 1];
+        if ((rc = launch_recompose_adjoint_level<T>(gin, g.box[l], g.box[l - 1], out + g.offset[l], gout, st)))
+            return rc;
+        gin = gout;
+    }
+    return PRODM_OK;
+}
+}  // namespace prodm
+
 // extern "C"
 // ===========================================================================
 #define DISPATCH(dtype, FN, ...) ((dtype) == PRODM_F64 ? FN<double>(__VA_ARGS__) : FN<float>(__VA_ARGS__))
@@ -1181,6 +1225,40 @@ int prodm_collect_max(int dtype, double bound, int B, double* out) {
     double err = std::ldexp(1.0, e - 1);
     for (int i = 1; i <= B; i++) { out[i] = err; err /= 2; }
     return PRODM_OK;
+}
+
+int prodm_recompose_packed_workspace(int dtype, int ndims, const uint32_t* dims, uint32_t L, size_t* bytes) {
+    int rc = check_dtype(dtype);
+    if (rc) return rc;
+    if (!dims || !bytes) return fail(PRODM_EINVAL, "NULL pointer");
+    LevelGeom g;
+    if ((rc = make_geom(ndims, dims, (int)L, g))) return rc;
+    *bytes = L == 0 ? 0 : 2 * Workspace::align(g.box[L - 1].size() * esize(dtype));
+    return PRODM_OK;
+}
+
+int prodm_recompose_packed(int dtype, const void* d_coef, int ndims, const uint32_t* dims, uint32_t L, void* d_out,
+                           void* ws, size_t wsb, void* stream) {
+    int rc = check_dtype(dtype);
+    if (rc) return rc;
+    if (!d_coef || !d_out || !dims) return fail(PRODM_EINVAL, "prodm_recompose_packed: NULL pointer");
+    if (dtype == PRODM_F64)
+        return packed_pair_impl<double>((const double*)d_coef, ndims, dims, (int)L, (double*)d_out, false, ws, wsb,
+                                        (cudaStream_t)stream);
+    return packed_pair_impl<float>((const float*)d_coef, ndims, dims, (int)L, (float*)d_out, false, ws, wsb,
+                                   (cudaStream_t)stream);
+}
+
+int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint32_t* dims, uint32_t L,
+                            void* d_grad_coef, void* ws, size_t wsb, void* stream) {
+    int rc = check_dtype(dtype);
+    if (rc) return rc;
+    if (!d_grad || !d_grad_coef || !dims) return fail(PRODM_EINVAL, "prodm_recompose_adjoint: NULL pointer");
+    if (dtype == PRODM_F64)
+        return packed_pair_impl<double>((const double*)d_grad, ndims, dims, (int)L, (double*)d_grad_coef, true, ws,
+                                        wsb, (cudaStream_t)stream);
+    return packed_pair_impl<float>((const float*)d_grad, ndims, dims, (int)L, (float*)d_grad_coef, true, ws, wsb,
+                                   (cudaStream_t)stream);
 }
 
 int prodm_collect_squared_workspace(int dtype, int B, size_t* bytes) {

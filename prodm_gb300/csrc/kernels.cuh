@@ -34,6 +34,12 @@ template <class T>
 int launch_interleave(T* data, uint64_t s0, uint64_t s1, const Box& F, const Box& C, T* buf, bool gather,
                       cudaStream_t st);
 
+// adjoint.cu: transpose of one hierarchical recomposition level (field
+// gradient of box F -> gradient of the level's packed coefficients and of the
+// coarse box C, natural order)
+template <class T>
+int launch_recompose_adjoint_level(const T* g, const Box& F, const Box& C, T* gcoef, T* gcoarse, cudaStream_t st);
+
 // bitplane.cu
 template <class T>
 int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, void* out, uint64_t stride,
