@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--graph", action="store_true", help="replay the step as a captured CUDA graph (stage events "
                     "are captured as external event nodes)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-field batched vs per-field-loop measurement")
+    ap.add_argument("--no-qoi", action="store_true", help="skip the QoI-guided vs uniform-halving retrieval comparison")
     return ap.parse_args()
 
 
@@ -357,6 +358,7 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": dom["bytes"]}
 
     batched = run_batched() if (not args.no_batched and world == 1) else None
+    qoi_res = run_qoi() if (not args.no_qoi and world == 1) else None
 
     # end-to-end through the reference-facing flow with host buffers
     e2e = run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev) if args.e2e_steps > 0 else None
@@ -380,6 +382,7 @@ def run_ours(args):
             "execution": "CUDA graph replay of one captured step" if graph is not None else "host launches",
             "e2e": e2e,
             "batched": batched,
+            "qoi": qoi_res,
             "clocks": clocks,
         }
     if world > 1:
@@ -525,6 +528,39 @@ def run_batched(steps=5):
             "workload": "24 cubes {33,65,129,257}^3, 24 2-D {513,1025,2049}^2, 16 x 129x257x65; spectral slopes "
                         "U[-3,-1]; levels = largest keeping level 0 >= 32 values; 32 planes; negabinary; "
                         "relative L-inf tolerances log-U[1e-5,1e-2]; refactor + retrieve per step"}
+
+
+def run_qoi(n=257, levels=6, rels=(1e-2, 1e-3, 1e-4)):
+    """QoI-bounded retrieval of Vx, Vy, Vz (+ rho): retrieved bytes of the
+    QoI-guided per-(field, level) budgets against the reference-style
+    uniform-halving loop, for |V| and 1/2 rho |V|^2 at pointwise bounds
+    tau = rel * range(QoI)."""
+    import torch
+    from prodm_gb300 import fields, qoi
+
+    V = [v.cuda() for v in fields.divergence_free_velocity(n, seed=11)]
+    rho = fields.lognormal_density(n, seed=12).cuda()
+    out = {"workload": "Vx, Vy, Vz %d^3 fp32 divergence-free random Fourier modes (|k| <= 16), rho lognormal "
+                       "(sigma 0.5); %d levels, 32 planes, grouped encoder, hierarchical basis, L-inf tables" %
+                       (n, levels + 1), "cases": []}
+    for kind in ("vmag", "ke"):
+        data = V + ([rho] if kind == "ke" else [])
+        q = qoi.qoi_value(kind, [v.double() for v in V], rho.double() if kind == "ke" else None)
+        for rel in rels:
+            tau = qoi.value_range(q) * rel
+            t0 = time.time()
+            base = qoi.halving_retrieve(kind, data, tau, rel, levels)
+            t1 = time.time()
+            ours = qoi.guided_retrieve(kind, data, tau, rel, levels)
+            t2 = time.time()
+            out["cases"].append({
+                "qoi": kind, "rel": rel, "tau": tau,
+                "halving": {k: base[k] for k in ("bytes", "bound", "achieved", "iterations", "met")},
+                "guided": {k: ours[k] for k in ("bytes", "bound", "achieved", "iterations", "met")},
+                "bytes_ratio_guided_over_halving": ours["bytes"] / max(base["bytes"], 1),
+                "seconds": {"halving": t1 - t0, "guided": t2 - t1}})
+            torch.cuda.empty_cache()
+    return out
 
 
 def call_export(mdr, level, host_tensor):
