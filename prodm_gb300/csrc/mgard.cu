@@ -176,8 +176,11 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
     K mk = 0, mc = 0;
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb)
-        decompose_row<T>(in, s0, s1, F, C, coef, coarse, fnat, row, lane, mk, mc);
+    const bool odd = (F.n[2] & 1u) != 0;
+    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
+        if (odd) decompose_row_odd_any<T>(in, s0, s1, F, C, coef, coarse, fnat, row, lane, mk, mc);
+        else decompose_row<T>(in, s0, s1, F, C, coef, coarse, fnat, row, lane, mk, mc);
+    }
     if (maxkey_level) {
         mk = warp_max_key(mk);
         if ((threadIdx.x & 31) == 0 && mk) atomicMax(maxkey_level, mk);
@@ -193,8 +196,11 @@ __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ co
                                                         Box C, T* __restrict__ out, uint64_t s0, uint64_t s1) {
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
-    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb)
-        recompose_row<T>(coarse, coef, F, C, out, s0, s1, row, lane);
+    const bool odd = (F.n[2] & 1u) != 0;
+    for (uint32_t row = blockIdx.x * wpb + (threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
+        if (odd) recompose_row_odd_any<T>(coarse, coef, F, C, out, s0, s1, row, lane);
+        else recompose_row<T>(coarse, coef, F, C, out, s0, s1, row, lane);
+    }
 }
 
 // copy a box between strided arrays
