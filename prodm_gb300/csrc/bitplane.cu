@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
 // sit at partial + level * gridDim.x * (B + 1); a CTA writes zero rows for the
 // levels it never visits, so every row the reduction reads is written.
 template <bool ERR>
-__global__ void __launch_bounds__(256) k_nb_encode32_levels(const ChunkSeg* __restrict__ segs, int nseg,
+__global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* __restrict__ segs, int nseg,
                                                            uint64_t total, int B, double* __restrict__ partial) {
     __shared__ uint32_t tile[32 * NB_TILE_LD];
     float acc[32], accx = 0.f;
@@ -275,6 +275,89 @@ __global__ void __launch_bounds__(256) k_nb_encode32_levels(const ChunkSeg* __re
         if (cur >= 0) flush(cur);
         zero_rows(cur + 1, nseg);
     }
+}
+
+// Every level of one fp32 field decoded in one launch (segments = levels in
+// chunk order, kDecodeChunkBlocks 32-value blocks per chunk). The planes of a
+// CTA's next chunk are fetched with cp.async into the second tile while the
+// current chunk is decoded; each 32-value block is decoded by two threads
+// (one half transpose each), and a thread writes its 16 values as four
+// 16-byte stores when the level's output is 16-byte aligned.
+// NegaBinaryBPEncoder.hpp:132-192 with start plane 0 and num = dnum planes.
+__global__ void __launch_bounds__(256) k_nb_decode_levels(const ChunkSeg* __restrict__ segs, int nseg,
+                                                         uint64_t total) {
+    constexpr int CB = kDecodeChunkBlocks;
+    __shared__ __align__(16) uint32_t tiles[2][CB * TB_LD];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    auto fetch = [&](uint64_t c, uint32_t* tile) {
+        const ChunkSeg& q = segs[find_seg(segs, nseg, c, &ChunkSeg::chunk_begin)];
+        const int num = q.dnum[0];
+        const uint64_t b0 = (c - q.chunk_begin) * CB;
+        const uint32_t nb = (uint32_t)min((uint64_t)CB, q.nblocks - b0);
+        for (int p = warp; p < num; p += 8) {
+            const uint32_t* src = q.words + (uint64_t)p * q.stride + b0;
+            for (uint32_t j = lane; j < nb; j += 32) cp_async4(tile + j * TB_LD + p, src + j);
+        }
+        cp_async_commit();
+    };
+    uint64_t c = blockIdx.x;
+    if (c >= total) return;
+    fetch(c, tiles[0]);
+    for (int it = 0; c < total; it++, c += gridDim.x) {
+        cp_async_wait_all();
+        __syncthreads();
+        if (c + gridDim.x < total) fetch(c + gridDim.x, tiles[(it + 1) & 1]);
+        const uint32_t* tile = tiles[it & 1];
+        const ChunkSeg& q = segs[find_seg(segs, nseg, c, &ChunkSeg::chunk_begin)];
+        const int num = q.dnum[0];
+        const uint64_t b0 = (c - q.chunk_begin) * CB;
+        const uint32_t nb = (uint32_t)min((uint64_t)CB, q.nblocks - b0);
+        const uint32_t t = threadIdx.x >> 1;
+        const int half = threadIdx.x & 1;
+        if (t < nb) {
+            float vals[16];
+            if (num == 0) {
+#pragma unroll
+                for (int v = 0; v < 16; v++) vals[v] = 0.f;
+            } else {
+                const int exp = frexp_exp(__uint_as_float(*q.key)) + 2;      // NegaBinaryBPEncoder.hpp:21
+                const bool neg = num & 1;                                     // :153, :177
+                const bool dfast = pow2_normal(exp - num);
+                const float dscale = dfast ? (neg ? -pow2f(exp - num) : pow2f(exp - num)) : 1.f;
+                // rows in reverse plane order: value v's digits come out most significant first
+                uint32_t R[32];
+                const uint4* src = reinterpret_cast<const uint4*>(tile + t * TB_LD);
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const uint4 w = src[k];
+                    R[31 - 4 * k] = 4 * k < num ? w.x : 0u;
+                    R[30 - 4 * k] = 4 * k + 1 < num ? w.y : 0u;
+                    R[29 - 4 * k] = 4 * k + 2 < num ? w.z : 0u;
+                    R[28 - 4 * k] = 4 * k + 3 < num ? w.w : 0u;
+                }
+                uint32_t a[16];
+                transpose32_half(R, half, a);
+#pragma unroll
+                for (int v = 0; v < 16; v++) {
+                    const int32_t iv = nb_to_bin(a[v] >> (32 - num));
+                    vals[v] = dfast ? (float)iv * dscale
+                                    : (neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num));
+                }
+            }
+            const uint64_t e0 = (b0 + t) * 32 + 16 * (uint64_t)half;
+            float* dst = q.y + e0;
+            if (e0 + 16 <= q.n && ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0)) {
+                float4* d4 = reinterpret_cast<float4*>(dst);
+#pragma unroll
+                for (int k = 0; k < 4; k++) d4[k] = make_float4(vals[4 * k], vals[4 * k + 1], vals[4 * k + 2], vals[4 * k + 3]);
+            } else {
+#pragma unroll
+                for (int v = 0; v < 16; v++)
+                    if (e0 + v < q.n) dst[v] = vals[v];
+            }
+        }
+    }
+    cp_async_wait_all();
 }
 
 // per-level tables from the partial rows of k_nb_encode32_levels, scaled to
@@ -957,6 +1040,13 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
                                                    nullptr);
         PRODM_CHECK_LAUNCH("k_nb_encode");
     }
+    return PRODM_OK;
+}
+
+int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st) {
+    const unsigned grid = persistent_grid_for((const void*)k_nb_decode_levels, 256, 0, total_chunks, total_chunks);
+    k_nb_decode_levels<<<grid, 256, 0, st>>>(segs, nseg, total_chunks);
+    PRODM_CHECK_LAUNCH("k_nb_decode_levels");
     return PRODM_OK;
 }
 

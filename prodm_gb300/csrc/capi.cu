@@ -676,7 +676,7 @@ int mdr_alloc_all(prodm_mdr* h) {
     }
     if (h->nb && dtype == PRODM_F32) {
         // every level not decoded by the fused finest-level kernel, as one
-        // segment table (NB_CHUNK = 256 blocks per chunk)
+        // segment table (kDecodeChunkBlocks blocks per chunk)
         const int top = fuse_finest(h) ? L - 1 : L;
         std::vector<ChunkSeg> segs;
         uint64_t chunks = 0;
@@ -690,7 +690,7 @@ int mdr_alloc_all(prodm_mdr* h) {
             q.key = (const uint32_t*)h->keys + l;
             q.dnum = h->index + l;
             q.chunk_begin = chunks;
-            chunks += (q.nblocks + 255) / 256;
+            chunks += (q.nblocks + kDecodeChunkBlocks - 1) / kDecodeChunkBlocks;
             segs.push_back(q);
         }
         if ((rc = h->alloc((void**)&h->dseg, segs.size() * sizeof(ChunkSeg)))) return rc;
@@ -797,7 +797,7 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
     if (h->dseg && sizeof(T) == 4) {
         // fp32 negabinary: every other level in one launch (timed as level 0)
         Stage sg(h, 3, 0, st);
-        if ((rc = launch_nb_decode_multi(h->dseg, h->dseg_n, h->dseg_chunks, st))) return rc;
+        if ((rc = launch_nb_decode_levels(h->dseg, h->dseg_n, h->dseg_chunks, st))) return rc;
     }
     for (int l = 0; l <= L; l++) {
         if ((fuse && l == L) || (h->dseg && sizeof(T) == 4)) continue;

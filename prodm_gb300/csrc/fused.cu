@@ -12,6 +12,7 @@
 // hierarchical basis), so the output is bit-identical to the unfused path.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "nbcodec.cuh"
 
 namespace prodm {
 
@@ -153,13 +154,6 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
 // fetched with cp.async into a second tile while the current rows are decoded
 // and recomposed; the coefficient buffer is value-major ([block][33]).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
 constexpr int CB_LD = 33;   // value-major coefficient rows: conflict-free both ways
 
 __device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[r + (r >> 5)]; }
@@ -226,35 +220,6 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
     }
 }
 
-// Half of a 32 x 32 bit transpose: rows R[0..31] (R[r] bit e) -> the 16
-// words out[v] (v = 16 * half + 0..15) whose bit r is R[r] bit v. The two
-// byte-granular stages are byte permutes, the three sub-byte stages
-// mask-and-shift swaps.
-__device__ __forceinline__ void transpose32_half(const uint32_t (&R)[32], int half, uint32_t (&a)[16]) {
-    const uint32_t sel16 = half ? 0x7632u : 0x5410u;
-#pragma unroll
-    for (int k = 0; k < 16; k++) a[k] = __byte_perm(R[k], R[k + 16], sel16);
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const uint32_t x = a[k], y = a[k + 8];
-        a[k] = __byte_perm(x, y, 0x6240u);
-        a[k + 8] = __byte_perm(x, y, 0x7351u);
-    }
-#pragma unroll
-    for (int s = 0; s < 3; s++) {
-        const int j = 4 >> s;
-        const uint32_t m = s == 0 ? 0x0f0f0f0fu : s == 1 ? 0x33333333u : 0x55555555u;
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int k = (i / j) * 2 * j + (i % j);
-            const uint32_t t = ((a[k] >> j) ^ a[k + j]) & m;
-            a[k + j] ^= t;
-            a[k] ^= t << j;
-        }
-    }
-}
-
-constexpr int TB_LD = 36;   // block-major plane tile row: 32 planes + pad, 16-byte aligned rows
 
 __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint32_t* __restrict__ base, uint64_t stride,
                                                                   const uint32_t* __restrict__ maxkey,

@@ -8,6 +8,8 @@
 // library's priority_queue, so ties resolve identically. One thread runs one
 // interpretation (one field); the kernel takes all inputs from device memory
 // so a whole retrieval can run without a host round trip.
+#include <climits>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -208,8 +210,90 @@ __device__ void interpret_core(int kind, int nl, int B, const uint32_t* __restri
     }
 }
 
-// one CTA per field: all threads tabulate the efficiencies, thread 0 runs the
-// sequential heap walk on the staged tables
+// The same walk with one lane per level. While every efficiency in the heap
+// is a number and the largest one is unique, a max-heap pops exactly the
+// largest entry, so the pop order is the arg-max order over the levels' next
+// entries and the heap's layout does not matter. The warp tracks that
+// condition at every pop; when it fails (a NaN efficiency -- zero-size
+// planes -- or a tie for the maximum) it returns false and the caller runs
+// the exact heap simulation from the original inputs. The estimate `acc` is
+// updated in the same order by every lane.
+__device__ bool interpret_warp(int kind, int nl, int B, const uint32_t* __restrict__ sizes,
+                               const double* __restrict__ ev, const long long* __restrict__ ekey,
+                               const int8_t* __restrict__ enan, const int8_t* __restrict__ en, double tol,
+                               uint8_t* index, uint32_t* rsz, int lane) {
+    const unsigned FULLM = 0xffffffffu;
+    const bool has = lane < nl;
+    int idx = has ? index[lane] : 0;
+    uint32_t rs = 0;
+    double acc = 0;
+    for (int i = 0; i < nl; i++) acc += ev[i * 65 + index[i]];
+    bool in_heap = has && idx != B;
+    bool met = false;
+    if (kind == 1) {
+        if (acc < tol) {
+            if (has) rsz[lane] = 0;
+            return true;
+        }
+        double minerr = acc;
+        in_heap = false;
+        for (int i = 0; i < nl; i++) {
+            const int ii = index[i];
+            minerr -= ev[i * 65 + ii];
+            minerr += ev[i * 65 + B];
+            int ni = ii;
+            if (ii == 0) {
+                acc -= ev[i * 65 + 0];
+                acc += ev[i * 65 + 1];
+                ni = 1;
+                if (lane == i) { rs += sizes[(size_t)i * B]; idx = 1; }
+            }
+            if (lane == i) in_heap = ni != B;
+            if (minerr < tol) break;
+        }
+        met = acc < tol;
+    } else if (kind == 2) {
+        met = acc < tol;
+    }
+    while (!met) {
+        long long k = LLONG_MIN;
+        int nan = 0, num = 1;
+        if (in_heap) {
+            k = ekey[lane * 64 + idx];
+            nan = enan[lane * 64 + idx];
+            num = en[lane * 64 + idx];
+        }
+        if (!__any_sync(FULLM, in_heap)) break;
+        if (__any_sync(FULLM, in_heap && nan)) return false;
+        long long best = k;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long other = __shfl_xor_sync(FULLM, best, o);
+            best = other > best ? other : best;
+        }
+        const unsigned at = __ballot_sync(FULLM, in_heap && k == best);
+        if (__popc(at) != 1) return false;
+        const int w = __ffs(at) - 1;
+        const int j = __shfl_sync(FULLM, idx, w);
+        const int take = __shfl_sync(FULLM, num, w);
+        if (lane == w) {
+            for (int t = 0; t < take; t++) rs += sizes[(size_t)lane * B + j + t];
+            idx += take;
+            in_heap = idx != B;
+        }
+        acc -= ev[w * 65 + j];
+        acc += ev[w * 65 + j + take];
+        if (acc < tol) met = true;
+    }
+    if (has) {
+        index[lane] = (uint8_t)idx;
+        rsz[lane] = rs;
+    }
+    return true;
+}
+
+// one CTA per field: all threads tabulate the efficiencies, warp 0 walks the
+// levels (the exact heap walk on thread 0 when the warp walk declines)
 template <class T>
 __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int est_kind, const int* __restrict__ ndims,
                                                    const int* __restrict__ levels, double s, int B,
@@ -250,13 +334,30 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
         s_en[l * 64 + j] = (int8_t)num;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    __shared__ uint8_t s_idx[kMaxLevels];
+    __shared__ uint32_t s_rs[kMaxLevels];
+    __shared__ int s_ok;
+    uint8_t* gi = index + f * idx_stride;
+    uint32_t* gr = rsz + f * idx_stride;
+    const double tol = tols ? tols[f] : tol0;
+    if (threadIdx.x < 32) {
+        if (threadIdx.x < nl) s_idx[threadIdx.x] = gi[threadIdx.x];
+        __syncwarp();
+        const bool ok = nl <= 32 && interpret_warp(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tol, s_idx, s_rs,
+                                                   threadIdx.x);
+        if (threadIdx.x == 0) s_ok = ok;
+        __syncwarp();
+        if (ok && threadIdx.x < nl) {
+            gi[threadIdx.x] = s_idx[threadIdx.x];
+            gr[threadIdx.x] = s_rs[threadIdx.x];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !s_ok) {
         uint8_t idx[kMaxLevels];
         uint32_t rs[kMaxLevels];
-        uint8_t* gi = index + f * idx_stride;
         for (int i = 0; i < nl; i++) idx[i] = gi[i];
-        interpret_core(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tols ? tols[f] : tol0, idx, rs);
-        uint32_t* gr = rsz + f * idx_stride;
+        interpret_core(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tol, idx, rs);
         for (int i = 0; i < nl; i++) { gi[i] = idx[i]; gr[i] = rs[i]; }
     }
 }

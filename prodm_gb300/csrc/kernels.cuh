@@ -82,6 +82,10 @@ struct ChunkSeg {
     uint64_t chunk_begin;
 };
 int launch_nb_decode_multi(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st);
+// bitplane.cu: every level of one fp32 field decoded in one launch; segments
+// chunked by kDecodeChunkBlocks blocks
+constexpr int kDecodeChunkBlocks = 128;
+int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st);
 // bitplane.cu: every level of one fp32 field in one encode launch; with
 // errs_out, per-level squared-error tables (partial: nseg * nb_encode_levels_grid(1)
 // * (B + 1) doubles)

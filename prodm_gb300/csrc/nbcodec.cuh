@@ -33,6 +33,44 @@ __device__ __forceinline__ float scale2(float v, int e, bool fast, float sc) { r
 __device__ __forceinline__ constexpr float nbw(int i) { return (i & 1) ? -(float)(1u << i) : (float)(1u << i); }
 
 
+// asynchronous 4-byte global -> shared copies (cp.async), one group per call
+__device__ __forceinline__ void cp_async4(uint32_t* dst, const uint32_t* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Half of a 32 x 32 bit transpose: rows R[0..31] (R[r] bit e) -> the 16
+// words out[v] (v = 16 * half + 0..15) whose bit r is R[r] bit v. The two
+// byte-granular stages are byte permutes, the three sub-byte stages
+// mask-and-shift swaps.
+__device__ __forceinline__ void transpose32_half(const uint32_t (&R)[32], int half, uint32_t (&a)[16]) {
+    const uint32_t sel16 = half ? 0x7632u : 0x5410u;
+#pragma unroll
+    for (int k = 0; k < 16; k++) a[k] = __byte_perm(R[k], R[k + 16], sel16);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t x = a[k], y = a[k + 8];
+        a[k] = __byte_perm(x, y, 0x6240u);
+        a[k + 8] = __byte_perm(x, y, 0x7351u);
+    }
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        const int j = 4 >> s;
+        const uint32_t m = s == 0 ? 0x0f0f0f0fu : s == 1 ? 0x33333333u : 0x55555555u;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int k = (i / j) * 2 * j + (i % j);
+            const uint32_t t = ((a[k] >> j) ^ a[k + j]) & m;
+            a[k + j] ^= t;
+            a[k] ^= t << j;
+        }
+    }
+}
+
+constexpr int TB_LD = 36;   // block-major plane tile row: 32 planes + pad, 16-byte aligned rows
+
 constexpr int NB_G = 8;              // blocks per warp iteration
 constexpr int NB_CHUNK = 256;        // blocks per CTA chunk
 constexpr int NB_TILE_LD = NB_CHUNK + 1;   // padded tile row: conflict-free column writes
