@@ -278,25 +278,35 @@ __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* _
 }
 
 // Every level of one fp32 field decoded in one launch (segments = levels in
-// chunk order, kDecodeChunkBlocks 32-value blocks per chunk). The planes of a
-// CTA's next chunk are fetched with cp.async into the second tile while the
-// current chunk is decoded; each 32-value block is decoded by two threads
-// (one half transpose each), and a thread writes its 16 values as four
-// 16-byte stores when the level's output is 16-byte aligned.
-// NegaBinaryBPEncoder.hpp:132-192 with start plane 0 and num = dnum planes.
+// chunk order, kDecodeChunkBlocks 32-value blocks per chunk). Plane rows start
+// on 16-byte boundaries, so a chunk's run of one plane (512 bytes) is one
+// warp-wide 16-byte cp.async; the next chunk's planes are fetched into the
+// second [plane][block] tile while the current chunk is decoded. Each
+// 32-value block is decoded by two threads (one half transpose each), and a
+// thread writes its 16 values as four 16-byte stores when the level's output
+// is 16-byte aligned. NegaBinaryBPEncoder.hpp:132-192 with start plane 0 and
+// num = dnum planes.
+constexpr int DEC_LD = kDecodeChunkBlocks + 4;   // tile row (words): 16-byte aligned, conflict-free columns
+
+__device__ __forceinline__ void cp_async16(uint32_t* dst, const uint32_t* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
 __global__ void __launch_bounds__(256) k_nb_decode_levels(const ChunkSeg* __restrict__ segs, int nseg,
                                                          uint64_t total) {
     constexpr int CB = kDecodeChunkBlocks;
-    __shared__ __align__(16) uint32_t tiles[2][CB * TB_LD];
+    __shared__ __align__(16) uint32_t tiles[2][32 * DEC_LD];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     auto fetch = [&](uint64_t c, uint32_t* tile) {
         const ChunkSeg& q = segs[find_seg(segs, nseg, c, &ChunkSeg::chunk_begin)];
         const int num = q.dnum[0];
         const uint64_t b0 = (c - q.chunk_begin) * CB;
         const uint32_t nb = (uint32_t)min((uint64_t)CB, q.nblocks - b0);
+        const uint32_t nq = (nb + 3) / 4;     // 16-byte pieces (inside the padded row)
         for (int p = warp; p < num; p += 8) {
             const uint32_t* src = q.words + (uint64_t)p * q.stride + b0;
-            for (uint32_t j = lane; j < nb; j += 32) cp_async4(tile + j * TB_LD + p, src + j);
+            for (uint32_t j = lane; j < nq; j += 32) cp_async16(tile + p * DEC_LD + 4 * j, src + 4 * j);
         }
         cp_async_commit();
     };
@@ -326,15 +336,8 @@ __global__ void __launch_bounds__(256) k_nb_decode_levels(const ChunkSeg* __rest
                 const float dscale = dfast ? (neg ? -pow2f(exp - num) : pow2f(exp - num)) : 1.f;
                 // rows in reverse plane order: value v's digits come out most significant first
                 uint32_t R[32];
-                const uint4* src = reinterpret_cast<const uint4*>(tile + t * TB_LD);
 #pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    const uint4 w = src[k];
-                    R[31 - 4 * k] = 4 * k < num ? w.x : 0u;
-                    R[30 - 4 * k] = 4 * k + 1 < num ? w.y : 0u;
-                    R[29 - 4 * k] = 4 * k + 2 < num ? w.z : 0u;
-                    R[28 - 4 * k] = 4 * k + 3 < num ? w.w : 0u;
-                }
+                for (int p = 0; p < 32; p++) R[31 - p] = p < num ? tile[p * DEC_LD + t] : 0u;
                 uint32_t a[16];
                 transpose32_half(R, half, a);
 #pragma unroll

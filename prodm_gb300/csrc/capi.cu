@@ -1,5 +1,6 @@
 // C ABI of the GB300 MDR path: component entry points (the reference's plugin
 // concepts) and the device-resident composed refactor / reconstructor.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -494,6 +495,7 @@ struct prodm_mdr {
     int* ndims_d = nullptr;
     int* levels_d = nullptr;
     void* rcoef = nullptr;
+    std::vector<uint64_t> roff;                    // level offsets in rcoef (elements, 16-byte aligned)
     void* rbuf[2] = {nullptr, nullptr};
     // fp32 negabinary: the levels decoded by one multi-level launch
     ChunkSeg* dseg = nullptr;
@@ -602,7 +604,10 @@ int mdr_alloc_all(prodm_mdr* h) {
     int rc;
     uint64_t N = g.total;
     if ((rc = h->alloc(&h->coef, N * es))) return rc;
-    if ((rc = h->alloc(&h->rcoef, N * es))) return rc;
+    // decoded levels: each level starts on a 16-byte boundary (vector stores)
+    h->roff.assign(L + 2, 0);
+    for (int l = 0; l <= L; l++) h->roff[l + 1] = (h->roff[l] + g.elems[l] + 16 / es - 1) / (16 / es) * (16 / es);
+    if ((rc = h->alloc(&h->rcoef, h->roff[L + 1] * es))) return rc;
     uint64_t cb = L >= 1 ? g.box[L - 1].size() : 1;
     for (int i = 0; i < 2; i++) {
         if ((rc = h->alloc(&h->cbuf[i], cb * es))) return rc;
@@ -635,7 +640,11 @@ int mdr_alloc_all(prodm_mdr* h) {
     for (int l = 0; l <= L; l++) {
         uint64_t nbk = nblocks_of(dtype, g.elems[l]);
         h->nblocks[l] = nbk;
-        h->plane_cap[l] = h->nb ? nbk : 2 * nbk;
+        // negabinary planes start on 16-byte boundaries (rows padded to a
+        // multiple of 16 bytes) so that whole plane runs move with 16-byte
+        // copies; the pad words are never part of a stream
+        const uint64_t pw = 16 / es;
+        h->plane_cap[l] = h->nb ? (nbk + pw - 1) / pw * pw : 2 * nbk;
         h->lvl_byte_off[l + 1] = h->lvl_byte_off[l] + (uint64_t)B * h->plane_cap[l] * es;
         h->rb_off[l + 1] = h->rb_off[l] + nbk;
         uint64_t nch = gr_nchunks(nbk);
@@ -682,11 +691,11 @@ int mdr_alloc_all(prodm_mdr* h) {
         uint64_t chunks = 0;
         for (int l = 0; l <= top; l++) {
             ChunkSeg q{};
-            q.y = (float*)h->rcoef + g.offset[l];
+            q.y = (float*)h->rcoef + h->roff[l];
             q.words = (uint32_t*)(h->streams + h->lvl_byte_off[l]);
             q.n = g.elems[l];
             q.nblocks = h->nblocks[l];
-            q.stride = h->nblocks[l];
+            q.stride = h->plane_cap[l];
             q.key = (const uint32_t*)h->keys + l;
             q.dnum = h->index + l;
             q.chunk_begin = chunks;
@@ -706,7 +715,7 @@ int mdr_alloc_all(prodm_mdr* h) {
             q.words = (uint32_t*)(h->streams + h->lvl_byte_off[l]);
             q.n = g.elems[l];
             q.nblocks = h->nblocks[l];
-            q.stride = h->nblocks[l];
+            q.stride = h->plane_cap[l];
             q.key = (const uint32_t*)h->keys + l;
             q.chunk_begin = chunks;
             chunks += (q.nblocks + 255) / 256;
@@ -773,7 +782,7 @@ int mdr_refactor(prodm_mdr* h, const T* field, cudaStream_t st) {
         double* errs = h->sq ? h->sqerr + (uint64_t)l * (B + 1) : nullptr;
         Stage sg(h, 1, l, st);
         if (h->nb) {
-            rc = launch_nb_encode<T>(coef + g.offset[l], n, keys + l, 0, B, out, h->nblocks[l], h->partial, errs, st);
+            rc = launch_nb_encode<T>(coef + g.offset[l], n, keys + l, 0, B, out, h->plane_cap[l], h->partial, errs, st);
         } else {
             rc = launch_gr_encode<T>(coef + g.offset[l], n, keys + l, 0, B, h->rbs + h->rb_off[l], h->chunk_words,
                                      h->chunk_off + h->co_off[l], h->sizes + (uint64_t)l * B, out, h->plane_cap[l],
@@ -804,12 +813,12 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         const uint64_t n = g.elems[l];
         Stage sg(h, 3, l, st);
         if (h->nb) {
-            rc = launch_nb_decode<T>(h->streams + h->lvl_byte_off[l], h->nblocks[l], n, keys + l, 0, 0, 0,
-                                     h->index + l, rcoef + g.offset[l], st);
+            rc = launch_nb_decode<T>(h->streams + h->lvl_byte_off[l], h->plane_cap[l], n, keys + l, 0, 0, 0,
+                                     h->index + l, rcoef + h->roff[l], st);
         } else {
             rc = launch_gr_decode<T>((const void* const*)(h->plane_ptrs + (uint64_t)l * B), n, keys + l, 0, B, 0, 0,
                                      h->index + l, h->rbs + h->rb_off[l], h->chunk_off + h->co_off[l], nullptr,
-                                     rcoef + g.offset[l], st);
+                                     rcoef + h->roff[l], st);
         }
         if (rc) return rc;
     }
@@ -820,11 +829,11 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
     for (int l = 1; l <= L; l++) {
         const Box& F = g.box[l];
         const Box& C = g.box[l - 1];
-        T* cin = (l == 1) ? rcoef + g.offset[0] : (T*)h->rbuf[(l - 1) & 1];
+        T* cin = (l == 1) ? rcoef + h->roff[0] : (T*)h->rbuf[(l - 1) & 1];
         T* o = (l == L) ? out : (T*)h->rbuf[l & 1];
         Stage sg(h, 4, l, st);
         if (fuse && l == L) {
-            if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->nblocks[l], keys + l,
+            if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->plane_cap[l], keys + l,
                                                    h->index + l, (const float*)cin, F, C, (float*)o,
                                                    (uint64_t)F.n[1] * F.n[2], F.n[2], st)))
                 return rc;
@@ -832,12 +841,12 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         }
         if (h->orth) {
             const T* tabs[3] = {level_tabs<T>(h, l, 0), level_tabs<T>(h, l, 1), level_tabs<T>(h, l, 2)};
-            if ((rc = launch_coef_to_natural<T>(rcoef + g.offset[l], F, C, (T*)h->os.fnat, st))) return rc;
+            if ((rc = launch_coef_to_natural<T>(rcoef + h->roff[l], F, C, (T*)h->os.fnat, st))) return rc;
             if ((rc = launch_l2_correction<T>((T*)h->os.fnat, F, (T*)h->os.t1, (T*)h->os.t2, (T*)h->os.z, tabs, st)))
                 return rc;
             if ((rc = launch_add_box<T>(cin, (uint64_t)C.n[1] * C.n[2], C.n[2], (T*)h->os.z, C, (T)-1, st))) return rc;
         }
-        if ((rc = launch_recompose_level_packed<T>(cin, rcoef + g.offset[l], F, C, o, (uint64_t)F.n[1] * F.n[2], F.n[2],
+        if ((rc = launch_recompose_level_packed<T>(cin, rcoef + h->roff[l], F, C, o, (uint64_t)F.n[1] * F.n[2], F.n[2],
                                                    st)))
             return rc;
     }
@@ -1007,8 +1016,17 @@ int mdr_load_level(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t 
     if (off + bytes > total) return fail(PRODM_EINVAL, "load_level: range beyond the level file");
     if (bytes == 0) return PRODM_OK;
     cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-    if (h->nb) {   // the aligned layout is the level-file layout
-        PRODM_CUDA(cudaMemcpyAsync(h->streams + h->lvl_byte_off[l] + off, src, bytes, kind, st));
+    if (h->nb) {   // level-file bytes [off, off + bytes) -> padded plane rows
+        const uint64_t row = h->nblocks[l] * h->es, pitch = h->plane_cap[l] * h->es;
+        uint64_t pos = off, done = 0;
+        while (done < bytes) {
+            const uint64_t p = pos / row, within = pos - p * row;
+            const uint64_t piece = std::min<uint64_t>(row - within, bytes - done);
+            PRODM_CUDA(cudaMemcpyAsync(h->streams + h->lvl_byte_off[l] + p * pitch + within,
+                                       (const uint8_t*)src + done, piece, kind, st));
+            pos += piece;
+            done += piece;
+        }
     } else {
         if (!h->lfile[l]) {
             int rc = h->alloc((void**)&h->lfile[l], total);
@@ -1407,8 +1425,10 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
     if (!dst) return PRODM_OK;
     if (cap < total) return fail(PRODM_EINVAL, "export buffer too small");
     const uint8_t* src = h->streams + h->lvl_byte_off[level];
-    if (h->nb) {
-        PRODM_CUDA(cudaMemcpyAsync(dst, src, total, dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    if (h->nb) {   // padded plane rows -> the contiguous level-file layout
+        const size_t row = (size_t)h->nblocks[level] * h->es;
+        PRODM_CUDA(cudaMemcpy2DAsync(dst, row, src, (size_t)h->plane_cap[level] * h->es, row, B,
+                                     dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
         PRODM_CUDA(cudaStreamSynchronize(st));
         return PRODM_OK;
     }
