@@ -288,11 +288,6 @@ __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* _
 // num = dnum planes.
 constexpr int DEC_LD = kDecodeChunkBlocks + 4;   // tile row (words): 16-byte aligned, conflict-free columns
 
-__device__ __forceinline__ void cp_async16(uint32_t* dst, const uint32_t* src) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-}
-
 __global__ void __launch_bounds__(256) k_nb_decode_levels(const ChunkSeg* __restrict__ segs, int nseg,
                                                          uint64_t total) {
     constexpr int CB = kDecodeChunkBlocks;
