@@ -348,9 +348,12 @@ def run_ours(args):
     dom = per_stage[dom_name]
     traffic = None
     try:
-        with open(os.path.join(ROOT, "profiles", "traffic_513.json")) as f:
-            traffic = json.load(f).get(dom_name)
-    except Exception:
+        with open(os.path.join(ROOT, "profiles", "traffic_513.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#") and parts[0] == dom_name:
+                    traffic = float(parts[1])
+    except OSError:
         pass
     roofline = {"kernel": dom_name, "bound": "hbm", "achieved": dom["gbs"], "peak": peak, "unit": "GB/s",
                 "frac": (dom["gbs"] / peak) if dom["gbs"] else None, "traffic": traffic,
