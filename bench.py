@@ -61,6 +61,20 @@ def parse():
     return ap.parse_args()
 
 
+def replica_throughput(ms_local, step_bytes, steps, world, device):
+    """Whole-job throughput of `world` replicas that each processed `steps`
+    steps of `step_bytes` in ms_local: the slowest rank's time (max over
+    ranks, one all-reduce) against all ranks' bytes. Returns (ms, GB/s)."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    return ms, step_bytes * steps * world / (ms / 1e3) / 1e9
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -323,12 +337,7 @@ def run_ours(args):
     mdr.set_timing(False)
     sampler.stop()
     clocks = sampler.summary(t0, t1)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    total_bytes = step_bytes * args.steps * world
-    value = total_bytes / (ms / 1e3) / 1e9
+    ms, value = replica_throughput(ms, step_bytes, args.steps, world, dev)
 
     # roofline of the dominant stage
     peak, peak_src = measured_peak()
