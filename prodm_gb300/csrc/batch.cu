@@ -61,7 +61,11 @@ __global__ void __launch_bounds__(256) k_decompose_multi(const RowSeg* __restric
         const int s = find_row_seg(segs, nseg, g);
         if (s != cur) { flush(); cur = s; }
         const RowSeg& q = segs[s];
-        decompose_row<float>(q.in, q.s0, q.s1, q.F, q.C, q.coef, q.out, nullptr, g - q.row_begin, lane, mk, mc);
+        if (q.F.n[2] & 1u)
+            decompose_row_odd_any<float>(q.in, q.s0, q.s1, q.F, q.C, q.coef, q.out, nullptr, g - q.row_begin, lane,
+                                         mk, mc);
+        else
+            decompose_row<float>(q.in, q.s0, q.s1, q.F, q.C, q.coef, q.out, nullptr, g - q.row_begin, lane, mk, mc);
     }
     flush();
 }
@@ -71,7 +75,10 @@ __global__ void __launch_bounds__(256) k_recompose_multi(const RowSeg* __restric
     for (uint32_t g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
         const int s = find_row_seg(segs, nseg, g);
         const RowSeg& q = segs[s];
-        recompose_row<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
+        if (q.F.n[2] & 1u)
+            recompose_row_odd_any<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
+        else
+            recompose_row<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
     }
 }
 
@@ -87,20 +94,6 @@ __global__ void __launch_bounds__(256) k_nb_encode_multi(const ChunkSeg* __restr
         const bool fast = pow2_normal(se);
         nb_encode32_chunk<false>(q.x, q.n, q.nblocks, B, se, fast, fast ? pow2f(se) : 1.f, q.words, q.stride,
                                  c - q.chunk_begin, tile, acc, accx);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_nb_decode_multi(const ChunkSeg* __restrict__ segs, int nseg,
-                                                        uint64_t total) {
-    __shared__ uint32_t tile[32 * NB_TILE_LD];
-    for (uint64_t c = blockIdx.x; c < total; c += gridDim.x) {
-        const int s = find_seg(segs, nseg, c, &ChunkSeg::chunk_begin);
-        const ChunkSeg& q = segs[s];
-        const int num = q.dnum[0];
-        const int exp = frexp_exp(__uint_as_float(*q.key)) + 2;
-        const bool dfast = pow2_normal(exp - num);
-        nb_decode32_chunk(q.words, q.stride, q.n, q.nblocks, num, num, exp, dfast, dfast ? pow2f(exp - num) : 1.f,
-                          c - q.chunk_begin, tile, q.y);
     }
 }
 
@@ -133,7 +126,8 @@ struct prodm_batch {
     std::vector<LevelGeom> g;
     std::vector<void*> allocs;
     // per field offsets into the arenas (elements / bytes)
-    std::vector<uint64_t> coef_off, cb_off, cb_len, stream_off;
+    std::vector<uint64_t> coef_off, rcoef_off, cb_off, cb_len, stream_off;
+    std::vector<std::vector<uint64_t>> roff;       // decoded level offsets within a field (16-byte aligned)
     std::vector<std::vector<uint64_t>> lvl_stream_off;
     float* coef = nullptr;
     float* rcoef = nullptr;
@@ -155,9 +149,9 @@ struct prodm_batch {
     std::vector<int> dn, rn;
     std::vector<uint32_t> drows, rrows;
     ChunkSeg* eseg = nullptr;
-    ChunkSeg* decseg = nullptr;
+    ChunkSeg* decseg = nullptr;                    // decode: kDecodeChunkBlocks blocks per chunk
     int en = 0;
-    uint64_t echunks = 0;
+    uint64_t echunks = 0, dchunks = 0;
     std::vector<const float*> fields;
     std::vector<float*> outs;
     bool bound = false;
@@ -197,7 +191,7 @@ int batch_build_segments(prodm_batch* h) {
             float* rb0 = h->rbuf + h->cb_off[f];
             float* rb1 = rb0 + h->cb_len[f];
             float* coef = h->coef + h->coef_off[f];
-            float* rcoef = h->rcoef + h->coef_off[f];
+            float* rcoef = h->rcoef + h->rcoef_off[f];
             const int l = L - d;                  // decompose level at this depth
             if (l >= 1) {
                 RowSeg s{};
@@ -219,8 +213,8 @@ int batch_build_segments(prodm_batch* h) {
                 RowSeg s{};
                 s.F = g.box[lr];
                 s.C = g.box[lr - 1];
-                s.in = (lr == 1) ? rcoef + g.offset[0] : ((lr - 1) & 1 ? rb1 : rb0);
-                s.coef = rcoef + g.offset[lr];
+                s.in = (lr == 1) ? rcoef + h->roff[f][0] : ((lr - 1) & 1 ? rb1 : rb0);
+                s.coef = rcoef + h->roff[f][lr];
                 s.out = (lr == L) ? h->outs[f] : (lr & 1 ? rb1 : rb0);
                 s.s0 = (uint64_t)s.F.n[1] * s.F.n[2];
                 s.s1 = s.F.n[2];
@@ -244,28 +238,35 @@ int batch_build_segments(prodm_batch* h) {
     }
     // encode / decode: every (field, level)
     std::vector<ChunkSeg> es, dc;
-    uint64_t ch = 0;
+    uint64_t ch = 0, dch = 0;
     for (int f = 0; f < nf; f++) {
         const LevelGeom& g = h->g[f];
         for (int l = 0; l <= g.L; l++) {
             ChunkSeg s{};
             s.n = g.elems[l];
             s.nblocks = (s.n + 31) / 32;
-            s.stride = s.nblocks;
+            s.stride = (s.nblocks + 3) / 4 * 4;   // plane rows on 16-byte boundaries
             s.words = (uint32_t*)(h->streams + h->lvl_stream_off[f][l]);
             s.key = h->keys + f * kMaxL + l;
             s.dnum = h->index + f * kMaxL + l;
             s.x = h->coef + h->coef_off[f] + g.offset[l];
-            s.y = h->rcoef + h->coef_off[f] + g.offset[l];
+            s.y = h->rcoef + h->rcoef_off[f] + h->roff[f][l];
+            ChunkSeg d = s;
             s.chunk_begin = ch;
             ch += (s.nblocks + NB_CHUNK - 1) / NB_CHUNK;
             es.push_back(s);
+            d.chunk_begin = dch;
+            dch += (d.nblocks + kDecodeChunkBlocks - 1) / kDecodeChunkBlocks;
+            dc.push_back(d);
         }
     }
     h->en = (int)es.size();
     h->echunks = ch;
+    h->dchunks = dch;
     if (!h->eseg && (rc = h->alloc((void**)&h->eseg, es.size() * sizeof(ChunkSeg)))) return rc;
     PRODM_CUDA(cudaMemcpy(h->eseg, es.data(), es.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
+    if (!h->decseg && (rc = h->alloc((void**)&h->decseg, dc.size() * sizeof(ChunkSeg)))) return rc;
+    PRODM_CUDA(cudaMemcpy(h->decseg, dc.data(), dc.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
     (void)B;
     return PRODM_OK;
 }
@@ -306,11 +307,10 @@ int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t s
                                       (uint64_t)kMaxL * h->B, h->maxerr, (uint64_t)kMaxL * (h->B + 1), h->tols, 0.0,
                                       h->index, kMaxL, h->rsz, st)))
         return rc;
-    k_nb_decode_multi<<<persistent_grid(h, h->echunks, 1), 256, 0, st>>>(h->eseg, h->en, h->echunks);
-    PRODM_CHECK_LAUNCH("k_nb_decode_multi");
+    if ((rc = launch_nb_decode_levels(h->decseg, h->en, h->dchunks, st))) return rc;
     for (int f = 0; f < h->nf; f++)
         if (h->g[f].L == 0)
-            PRODM_CUDA(cudaMemcpyAsync(h->outs[f], h->rcoef + h->coef_off[f], h->g[f].total * 4, cudaMemcpyDeviceToDevice, st));
+            PRODM_CUDA(cudaMemcpyAsync(h->outs[f], h->rcoef + h->rcoef_off[f], h->g[f].total * 4, cudaMemcpyDeviceToDevice, st));
     for (int d = 0; d < h->maxL; d++) {
         if (!h->rn[d]) continue;
         k_recompose_multi<<<persistent_grid(h, h->rrows[d], th / 32), th, 0, st>>>(h->rseg[d], h->rn[d], h->rrows[d]);
@@ -321,12 +321,6 @@ int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t s
 
 }  // namespace
 
-int launch_nb_decode_multi(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st) {
-    const unsigned grid = persistent_grid_for((const void*)k_nb_decode_multi, 256, 0, total_chunks, total_chunks);
-    k_nb_decode_multi<<<grid, 256, 0, st>>>(segs, nseg, total_chunks);
-    PRODM_CHECK_LAUNCH("k_nb_decode_multi");
-    return PRODM_OK;
-}
 
 }  // namespace prodm
 
@@ -350,8 +344,10 @@ int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs)
     h->B = B;
     h->cfg.assign(cfgs, cfgs + nfields);
     h->g.resize(nfields);
-    uint64_t coef = 0, cb = 0, sb = 0;
+    uint64_t coef = 0, rcoef = 0, cb = 0, sb = 0;
     h->coef_off.resize(nfields);
+    h->rcoef_off.resize(nfields);
+    h->roff.resize(nfields);
     h->cb_off.resize(nfields);
     h->cb_len.resize(nfields);
     h->lvl_stream_off.resize(nfields);
@@ -365,18 +361,22 @@ int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs)
         ndims[f] = g.ndims;
         h->coef_off[f] = coef;
         coef += (g.total + 63) & ~(uint64_t)63;
+        h->roff[f].assign(g.L + 2, 0);
+        for (int l = 0; l <= g.L; l++) h->roff[f][l + 1] = (h->roff[f][l] + g.elems[l] + 3) / 4 * 4;
+        h->rcoef_off[f] = rcoef;
+        rcoef += (h->roff[f][g.L + 1] + 63) & ~(uint64_t)63;
         h->cb_off[f] = cb;
         h->cb_len[f] = g.L >= 1 ? ((g.box[g.L - 1].size() + 63) & ~(uint64_t)63) : 64;
         cb += 2 * h->cb_len[f];
         h->lvl_stream_off[f].resize(g.L + 1);
         for (int l = 0; l <= g.L; l++) {
             h->lvl_stream_off[f][l] = sb;
-            sb += (uint64_t)B * ((g.elems[l] + 31) / 32) * 4;
+            sb += (uint64_t)B * (((g.elems[l] + 31) / 32 + 3) / 4 * 4) * 4;
             sb = (sb + 255) & ~(uint64_t)255;
         }
     }
     const size_t slots = (size_t)nfields * kMaxL;
-    if ((rc = h->alloc((void**)&h->coef, coef * 4)) || (rc = h->alloc((void**)&h->rcoef, coef * 4)) ||
+    if ((rc = h->alloc((void**)&h->coef, coef * 4)) || (rc = h->alloc((void**)&h->rcoef, rcoef * 4)) ||
         (rc = h->alloc((void**)&h->cbuf, cb * 4)) || (rc = h->alloc((void**)&h->rbuf, cb * 4)) ||
         (rc = h->alloc((void**)&h->streams, sb)) || (rc = h->alloc((void**)&h->keys, slots * 4)) ||
         (rc = h->alloc((void**)&h->bounds, slots * 4)) || (rc = h->alloc((void**)&h->sizes, slots * B * 4)) ||
@@ -466,8 +466,9 @@ int prodm_batch_export_level(prodm_batch* h, int field, int level, void* dst, ui
     if (!dst) return PRODM_OK;
     if (cap < bytes) return fail(PRODM_EINVAL, "export buffer too small");
     cudaStream_t st = (cudaStream_t)stream;
-    PRODM_CUDA(cudaMemcpyAsync(dst, h->streams + h->lvl_stream_off[field][level], bytes,
-                               dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+    const uint64_t nbk = (h->g[field].elems[level] + 31) / 32;
+    PRODM_CUDA(cudaMemcpy2DAsync(dst, nbk * 4, h->streams + h->lvl_stream_off[field][level], (nbk + 3) / 4 * 16, nbk * 4,
+                                 h->B, dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     PRODM_CUDA(cudaStreamSynchronize(st));
     return PRODM_OK;
 }

@@ -69,9 +69,8 @@ int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, co
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
                      cudaStream_t st);
 
-// batch.cu: one segment per (field, level) of the multi-level fp32
-// negabinary encode / decode launches; chunk_begin is the segment's first
-// global chunk (NB_CHUNK blocks each)
+// one segment per (field, level) of the multi-level fp32 negabinary encode /
+// decode launches; chunk_begin is the segment's first global chunk
 struct ChunkSeg {
     const float* x;         // encode input
     float* y;               // decode output
@@ -81,7 +80,6 @@ struct ChunkSeg {
     const uint8_t* dnum;    // decode: retrieved plane count
     uint64_t chunk_begin;
 };
-int launch_nb_decode_multi(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st);
 // bitplane.cu: every level of one fp32 field decoded in one launch; segments
 // chunked by kDecodeChunkBlocks blocks
 constexpr int kDecodeChunkBlocks = 128;
