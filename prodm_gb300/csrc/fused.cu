@@ -267,25 +267,30 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
     };
     uint32_t rho0 = blockIdx.x * 8;
     if (rho0 >= rows) return;
+    // block ranges of the CTA's iterations, computed by one thread two
+    // iterations ahead: slot k % 3 holds iteration k's range
+    __shared__ uint64_t s_fb[3];
+    __shared__ uint32_t s_nbk[3];
+    const uint32_t step = gridDim.x * 8;
+    if (threadIdx.x == 0) {
+        block_range(rho0, s_fb[0], s_nbk[0]);
+        if (rho0 + step < rows) block_range(rho0 + step, s_fb[1], s_nbk[1]);
+    }
     // planes >= num stay zero in both tiles
     for (uint32_t i = threadIdx.x; i < 2 * tld * (32 - num); i += blockDim.x) {
         const uint32_t row = i / (32 - num), p = num + (i - row * (32 - num));
         tiles[row * TB_LD + p] = 0u;
     }
     __syncthreads();
-    uint64_t fb, fb_next = 0;
-    uint32_t nbk, nbk_next = 0;
-    block_range(rho0, fb, nbk);
-    fetch(fb, nbk, tiles);
-    for (int it = 0; rho0 < rows; it++, rho0 += gridDim.x * 8) {
+    fetch(s_fb[0], s_nbk[0], tiles);
+    for (int it = 0; rho0 < rows; it++, rho0 += step) {
         const uint32_t* tile = tiles + (it & 1) * TB_LD * tld;
         cp_async_wait_all();
         __syncthreads();
-        const uint32_t rho_next = rho0 + gridDim.x * 8;
-        if (rho_next < rows) {
-            block_range(rho_next, fb_next, nbk_next);
-            fetch(fb_next, nbk_next, tiles + ((it + 1) & 1) * TB_LD * tld);
-        }
+        const uint64_t fb = s_fb[it % 3];
+        const uint32_t nbk = s_nbk[it % 3];
+        if (rho0 + step < rows) fetch(s_fb[(it + 1) % 3], s_nbk[(it + 1) % 3], tiles + ((it + 1) & 1) * TB_LD * tld);
+        if (threadIdx.x == 0 && rho0 + 2 * step < rows) block_range(rho0 + 2 * step, s_fb[(it + 2) % 3], s_nbk[(it + 2) % 3]);
         // decode: two threads per 32-value block, each transposing one half;
         // rows are taken in reverse plane order so that value v's digits come
         // out most significant first (no bit reversal)
@@ -337,8 +342,6 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
                 default: recompose_row_odd<3>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
             }
         }
-        fb = fb_next;
-        nbk = nbk_next;
     }
     cp_async_wait_all();
 }
