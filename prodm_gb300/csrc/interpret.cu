@@ -19,23 +19,28 @@ namespace {
 
 constexpr int kMaxLevels = 17;
 
+// level factor of the L2 / S-norm estimators (SquaredErrorEstimator.hpp:12-68):
+// 2^(ndims (L - i)), or 2^(2 s i + ndims (L - i)); the integer power is exact
+template <class T>
+__device__ T est_level_factor(int k, int ndims, int L, double s, int i) {
+    if (k == 2) return (T)ldexp(1.0, ndims * (L - i));
+    const T sT = (T)s;
+    return (T)exp2((double)(2 * sT * i + ndims * (L - i)));
+}
+
 template <class T>
 struct DevEstimator {
     int kind;
     T c;
-    T table[kMaxLevels];
-    __device__ void init(int k, int ndims, int L, double s) {
+    const T* table;    // per-level factors (shared memory), kinds 2 and 3
+    __device__ void init(int k, int ndims, const T* tab) {
         kind = k;
         c = 0;
+        table = tab;
         if (k == 1) {
             double cc = ndims == 1 ? 1.0 + sqrt(3.0) / 2 : ndims == 2 ? 1.0 + 9.0 / 4 : 1.0 + 21.0 * sqrt(3.0) / 8;
             c = (T)cc;
             c *= 4;
-        } else if (k == 2) {
-            for (int i = 0; i <= L && i < kMaxLevels; i++) table[i] = (T)exp2((double)(ndims * (L - i)));
-        } else if (k == 3) {
-            T sT = (T)s;
-            for (int i = 0; i <= L && i < kMaxLevels; i++) table[i] = (T)exp2((double)(2 * sT * i + ndims * (L - i)));
         }
     }
     __device__ T est(T e, int l) const {
@@ -314,15 +319,22 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
     __shared__ int8_t s_en[kMaxLevels * 64];
     for (int i = threadIdx.x; i < nl * B; i += blockDim.x) s_sizes[i] = sizes[f * sz_stride + i];
     for (int i = threadIdx.x; i < nl * (B + 1); i += blockDim.x) s_errs[i] = errs[f * err_stride + i];
-    DevEstimator<T> est;
-    est.init(est_kind, ndims[f], L, s);
+    __shared__ T s_tab[kMaxLevels];
+    __shared__ uint8_t s_idx[kMaxLevels];
+    uint8_t* gi = index + f * idx_stride;
+    if (threadIdx.x < nl) s_idx[threadIdx.x] = gi[threadIdx.x];
+    if ((est_kind == 2 || est_kind == 3) && threadIdx.x < nl && threadIdx.x < kMaxLevels)
+        s_tab[threadIdx.x] = est_level_factor<T>(est_kind, ndims[f], L, s, threadIdx.x);
     __syncthreads();
+    DevEstimator<T> est;
+    est.init(est_kind, ndims[f], s_tab);
     for (int t = threadIdx.x; t < nl * (B + 1); t += blockDim.x) {
         const int l = t / (B + 1), j = t - l * (B + 1);
         s_ev[l * 65 + j] = (double)est.est((T)s_errs[t], l);
     }
     for (int t = threadIdx.x; t < nl * B; t += blockDim.x) {
         const int l = t / B, j = t - l * B;
+        if (j < s_idx[l]) continue;    // planes already retrieved are never offered again
         double u;
         int num;
         eff_entry<T>(kind, est, B, s_sizes, s_errs, l, j, u, num);
@@ -334,15 +346,11 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
         s_en[l * 64 + j] = (int8_t)num;
     }
     __syncthreads();
-    __shared__ uint8_t s_idx[kMaxLevels];
     __shared__ uint32_t s_rs[kMaxLevels];
     __shared__ int s_ok;
-    uint8_t* gi = index + f * idx_stride;
     uint32_t* gr = rsz + f * idx_stride;
     const double tol = tols ? tols[f] : tol0;
     if (threadIdx.x < 32) {
-        if (threadIdx.x < nl) s_idx[threadIdx.x] = gi[threadIdx.x];
-        __syncwarp();
         const bool ok = nl <= 32 && interpret_warp(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tol, s_idx, s_rs,
                                                    threadIdx.x);
         if (threadIdx.x == 0) s_ok = ok;
