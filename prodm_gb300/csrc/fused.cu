@@ -221,15 +221,15 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
 }
 
 
-__global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint32_t* __restrict__ base, uint64_t stride,
+__global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint32_t* __restrict__ base, uint64_t stride,
                                                                   const uint32_t* __restrict__ maxkey,
                                                                   const uint8_t* __restrict__ dnum,
                                                                   const float* __restrict__ coarse, Box F, Box C,
                                                                   float* __restrict__ out, uint64_t s0, uint64_t s1,
                                                                   uint32_t tld) {
     extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t* tiles = smem;                                  // 2 x [block][TB_LD]
-    float* cb = (float*)(smem + 2 * TB_LD * tld);            // [block][CB_LD]
+    uint32_t* tiles = smem;                                  // [block][TB_LD]
+    float* cb = (float*)(smem + TB_LD * tld);                // [block][CB_LD]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int num = dnum[0];
     const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
@@ -276,20 +276,19 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
         block_range(rho0, s_fb[0], s_nbk[0]);
         if (rho0 + step < rows) block_range(rho0 + step, s_fb[1], s_nbk[1]);
     }
-    // planes >= num stay zero in both tiles
-    for (uint32_t i = threadIdx.x; i < 2 * tld * (32 - num); i += blockDim.x) {
+    // planes >= num stay zero in the tile
+    for (uint32_t i = threadIdx.x; i < tld * (32 - num); i += blockDim.x) {
         const uint32_t row = i / (32 - num), p = num + (i - row * (32 - num));
         tiles[row * TB_LD + p] = 0u;
     }
     __syncthreads();
     fetch(s_fb[0], s_nbk[0], tiles);
     for (int it = 0; rho0 < rows; it++, rho0 += step) {
-        const uint32_t* tile = tiles + (it & 1) * TB_LD * tld;
+        const uint32_t* tile = tiles;
         cp_async_wait_all();
         __syncthreads();
         const uint64_t fb = s_fb[it % 3];
         const uint32_t nbk = s_nbk[it % 3];
-        if (rho0 + step < rows) fetch(s_fb[(it + 1) % 3], s_nbk[(it + 1) % 3], tiles + ((it + 1) & 1) * TB_LD * tld);
         if (threadIdx.x == 0 && rho0 + 2 * step < rows) block_range(rho0 + 2 * step, s_fb[(it + 2) % 3], s_nbk[(it + 2) % 3]);
         // decode: two threads per 32-value block, each transposing one half;
         // rows are taken in reverse plane order so that value v's digits come
@@ -322,6 +321,8 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
             }
         }
         __syncthreads();
+        // the tile is free again: fetch the next rows' planes during the recomposition
+        if (rho0 + step < rows) fetch(s_fb[(it + 1) % 3], s_nbk[(it + 1) % 3], tiles);
         const uint32_t rho = rho0 + warp;
         if (rho < rows) {
             uint32_t r0, r1, len;
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_odd(const uint
 static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
 static size_t fused_smem(const Box& F) {
     const uint32_t mb = fused_max_blocks(F);
-    if (F.n[2] & 1u) return (size_t)mb * TB_LD * 4 * 2 + (size_t)mb * CB_LD * 4;
+    if (F.n[2] & 1u) return (size_t)mb * TB_LD * 4 + (size_t)mb * CB_LD * 4;
     return (size_t)mb * 32 * 4 + (size_t)(mb | 1u) * 32 * 4;
 }
 
