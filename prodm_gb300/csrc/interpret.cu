@@ -270,13 +270,13 @@ __device__ bool interpret_warp(int kind, int nl, int B, const uint32_t* __restri
         }
         if (!__any_sync(FULLM, in_heap)) break;
         if (__any_sync(FULLM, in_heap && nan)) return false;
-        long long best = k;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const long long other = __shfl_xor_sync(FULLM, best, o);
-            best = other > best ? other : best;
-        }
-        const unsigned at = __ballot_sync(FULLM, in_heap && k == best);
+        // arg-max of the 64-bit keys: unsigned order-preserving halves, two warp reductions
+        const unsigned long long uk = (unsigned long long)k ^ 0x8000000000000000ull;
+        const unsigned hi = (unsigned)(uk >> 32), lo = (unsigned)uk;
+        const unsigned best_hi = __reduce_max_sync(FULLM, in_heap ? hi : 0u);
+        const bool cand = in_heap && hi == best_hi;
+        const unsigned best_lo = __reduce_max_sync(FULLM, cand ? lo : 0u);
+        const unsigned at = __ballot_sync(FULLM, cand && lo == best_lo);
         if (__popc(at) != 1) return false;
         const int w = __ffs(at) - 1;
         const int j = __shfl_sync(FULLM, idx, w);
