@@ -268,8 +268,12 @@ __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* _
             fast = pow2_normal(se);
             scale = fast ? pow2f(se) : 1.f;
         }
-        nb_encode32_chunk<ERR>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin, tile,
-                               acc, accx);
+        if (B == 32)
+            nb_encode32_chunk<ERR, true>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin,
+                                         tile, acc, accx);
+        else
+            nb_encode32_chunk<ERR>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin, tile,
+                                   acc, accx);
     }
     if (ERR) {
         if (cur >= 0) flush(cur);

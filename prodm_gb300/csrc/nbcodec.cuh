@@ -85,7 +85,8 @@ constexpr int NB_TILE_LD = NB_CHUNK + 1;   // padded tile row: conflict-free col
 // writes every plane's words of the chunk as one contiguous run.
 // Errors (ERR): negabinary truncation tables, NegaBinaryBPEncoder.hpp:231-239,
 // in per-lane accumulators indexed by dropped digits (acc[0] = m^2).
-template <bool ERR>
+// FULLB: B == 32, so every digit has a plane and no per-digit guard is needed
+template <bool ERR, bool FULLB = false>
 __device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, uint64_t n, uint64_t nblocks, int B,
                                                   int se, bool fast, float scale, uint32_t* __restrict__ out,
                                                   uint64_t stride, uint64_t c, uint32_t* tile, float (&acc)[32],
@@ -119,7 +120,7 @@ __device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, u
             }
 #pragma unroll
             for (int k = 1; k < 32; k++) {
-                if (k < B) {
+                if (FULLB || k < B) {
 #pragma unroll
                     for (int g = 0; g < NB_G; g++) {
                         if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
@@ -131,7 +132,7 @@ __device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, u
 #pragma unroll
         for (int g = 0; g < NB_G; g++) {
             const uint32_t w = transpose32(nb[g], lane);
-            if (lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
+            if (FULLB || lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
         }
     }
     __syncthreads();
