@@ -171,6 +171,25 @@ int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint
                             void* d_grad_coef, void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * GE quantities of interest (fp64 fields), for QoI-bounded retrieval.
+ * prodm_qoi_ge_values -- QoI::compute_QoIs (qoi_utils.hpp:135-165): V_TOT, T,
+ * C, Mach, PT and mu of every point of (Vx, Vy, Vz, P, D), n values each.
+ * prodm_qoi_ge_bounds -- the pointwise error estimates the GE drivers form
+ * from the propagation rules (qoi_utils.hpp:18-98): V_TOT from the square
+ * and square-root rules given |error| <= eb_v* of each velocity component
+ * (halving_Vtot.cpp:38-45), T from the division rule given eb_p, eb_d (0 where
+ * the rule cannot bound it, as the reference). Pass NULL velocities or NULL
+ * P/D to skip one QoI; bound arrays may be NULL; max_bounds (nullable, device,
+ * 2 doubles) receives the maxima over the field.
+ * ------------------------------------------------------------------------- */
+int prodm_qoi_ge_values(int dtype, const void* d_vx, const void* d_vy, const void* d_vz, const void* d_p,
+                        const void* d_d, uint64_t n, void* d_vtot, void* d_temp, void* d_c, void* d_mach,
+                        void* d_pt, void* d_mu, void* stream);
+int prodm_qoi_ge_bounds(int dtype, const void* d_vx, const void* d_vy, const void* d_vz, const void* d_p,
+                        const void* d_d, uint64_t n, double eb_vx, double eb_vy, double eb_vz, double eb_p,
+                        double eb_d, double* d_bound_vtot, double* d_bound_t, double* d_max_bounds, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Size interpreter -- SizeInterpreterInterface::interpret_retrieve_size
  * (SizeInterpreterInterface.hpp:13). Runs on the device. d_sizes[nl*B] plane
  * byte sizes, d_errors[nl*(B+1)] level error tables, d_index[nl] in/out

@@ -184,6 +184,36 @@ class Oracle(_Lib):
         f(np.ascontiguousarray(grad).ravel(), len(dims), np.asarray(dims, np.uint32), L, out)
         return out
 
+    # GE quantities of interest (double) ----------------------------------
+    def qoi_values(self, vx, vy, vz, p, d):
+        """V_TOT, T, C, Mach, PT, mu (six arrays)."""
+        pre = self.prefix
+        a = [np.ascontiguousarray(x, np.float64) for x in (vx, vy, vz, p, d)]
+        n = a[0].size
+        outs = [np.zeros(n) for _ in range(6)]
+        dp = C.POINTER(C.c_double)
+        f = self._fn(pre + "_qoi_values_f64", None, *([_tp(np.float64)] * 5), C.c_uint64, *([_tp(np.float64)] * 6))
+        f(*a, n, *outs)
+        return outs
+
+    def qoi_vtot_bound(self, vx, vy, vz, ebs):
+        pre = self.prefix
+        a = [np.ascontiguousarray(x, np.float64) for x in (vx, vy, vz)]
+        out = np.zeros(a[0].size)
+        f = self._fn(pre + "_qoi_vtot_bound_f64", None, *([_tp(np.float64)] * 3), C.c_uint64, C.c_double,
+                     C.c_double, C.c_double, _tp(np.float64))
+        f(*a, a[0].size, float(ebs[0]), float(ebs[1]), float(ebs[2]), out)
+        return out
+
+    def qoi_t_bound(self, p, d, eb_p, eb_d):
+        pre = self.prefix
+        a = [np.ascontiguousarray(x, np.float64) for x in (p, d)]
+        out = np.zeros(a[0].size)
+        f = self._fn(pre + "_qoi_t_bound_f64", None, _tp(np.float64), _tp(np.float64), C.c_uint64, C.c_double,
+                     C.c_double, _tp(np.float64))
+        f(*a, a[0].size, float(eb_p), float(eb_d), out)
+        return out
+
     # composed -------------------------------------------------------------
     def refactor(self, field, L, B, encoder="negabinary", hierarchical=True, collect=False):
         """Composed refactor. Returns dict(blob, sizes[L+1,B], bounds[L+1], errs, coeffs)."""

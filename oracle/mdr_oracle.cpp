@@ -191,4 +191,16 @@ void or_level_elements(int ndims, const uint32_t* dims, int L, uint32_t* out) {
 OR_T(f32, float, uint32_t)
 OR_T(f64, double, uint64_t)
 
+void or_qoi_values_f64(const double* vx, const double* vy, const double* vz, const double* p, const double* d,
+                       uint64_t n, double* vtot, double* temp, double* c, double* mach, double* pt, double* mu) {
+    qoi_values(vx, vy, vz, p, d, (size_t)n, vtot, temp, c, mach, pt, mu);
+}
+void or_qoi_vtot_bound_f64(const double* vx, const double* vy, const double* vz, uint64_t n, double ebx, double eby,
+                           double ebz, double* out) {
+    vtot_bound(vx, vy, vz, (size_t)n, ebx, eby, ebz, out);
+}
+void or_qoi_t_bound_f64(const double* p, const double* d, uint64_t n, double ebp, double ebd, double* out) {
+    t_bound(p, d, (size_t)n, ebp, ebd, out);
+}
+
 }  // extern "C"

@@ -827,4 +827,55 @@ void recompose(T* data, const std::vector<uint32_t>& dims, int L, bool hierarchi
     }
 }
 
+// ---------------------------------------------------------------------------
+// GE quantities of interest (qoi_utils.hpp:135-165) and pointwise error
+// estimates from the propagation rules (qoi_utils.hpp:18-98): V_TOT with the
+// square and square-root rules, T = P / (D R) with the division rule.
+// ---------------------------------------------------------------------------
+struct GeConst {
+    static constexpr double R = 287.1, gamma = 1.4, mu_r = 1.716e-5, T_r = 273.15, S = 110.4;
+};
+
+inline void qoi_values(const double* vx, const double* vy, const double* vz, const double* p, const double* d,
+                       size_t n, double* vtot, double* temp, double* c, double* mach, double* pt, double* mu) {
+    using K = GeConst;
+    for (size_t i = 0; i < n; i++) {
+        double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        double v = std::sqrt(v2);
+        double t = p[i] / (d[i] * K::R);
+        double cc = std::sqrt(K::gamma * K::R * t);
+        double m = v / cc;
+        double mt = 1 + (K::gamma - 1) / 2 * m * m;
+        double ptv = p[i] * std::sqrt(std::pow(mt, 7));
+        double trs = (K::T_r + K::S) / (t + K::S);
+        double tt3 = std::sqrt(std::pow(t / K::T_r, 3));
+        vtot[i] = v; temp[i] = t; c[i] = cc; mach[i] = m; pt[i] = ptv; mu[i] = K::mu_r * tt3 * trs;
+    }
+}
+
+inline double bound_x_square(double x, double eb) { return 2 * std::fabs(x) * eb + eb * eb; }
+inline double bound_sqrt_x(double x, double eb) {
+    if (x == 0) return std::sqrt(eb);
+    if (x > eb) return eb / (std::sqrt(x - eb) + std::sqrt(x));
+    return eb / std::sqrt(x);
+}
+inline double bound_division(double x, double y, double ebx, double eby) {
+    if (eby < std::fabs(y)) {
+        double e = std::fabs(x) * eby + std::fabs(y) * ebx;
+        return y > 0 ? e / (y * (y - eby)) : e / (y * (y + eby));
+    }
+    return 0;   // the reference warns and gives no bound
+}
+inline void vtot_bound(const double* vx, const double* vy, const double* vz, size_t n, double ebx, double eby,
+                       double ebz, double* out) {
+    for (size_t i = 0; i < n; i++) {
+        double e2 = bound_x_square(vx[i], ebx) + bound_x_square(vy[i], eby) + bound_x_square(vz[i], ebz);
+        double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        out[i] = bound_sqrt_x(v2, e2);
+    }
+}
+inline void t_bound(const double* p, const double* d, size_t n, double ebp, double ebd, double* out) {
+    for (size_t i = 0; i < n; i++) out[i] = (1.0 / GeConst::R) * bound_division(p[i], d[i], ebp, ebd);
+}
+
 }  // namespace mdr_oracle

@@ -23,6 +23,7 @@
 #include "MDR/SizeInterpreter/SizeInterpreter.hpp"
 #include "MDR/Refactor/Refactor.hpp"
 #include "MDR/Reconstructor/Reconstructor.hpp"
+#include "qoi_utils.hpp"
 
 namespace {
 struct Quiet {  // the reference interpreters print to std::cout
@@ -201,4 +202,27 @@ extern "C" {
 
 REF_T(f32, float, uint32_t)
 REF_T(f64, double, uint64_t)
+
+// GE quantities of interest (qoi_utils.hpp:135-165) and the pointwise error
+// estimates the GE retrieval drivers form with the propagation rules of
+// qoi_utils.hpp:18-98: V_TOT as in halving_Vtot.cpp:38-45, T = P / (D R) as in
+// UniformTighteningT with c_1 = 1 / R
+void ref_qoi_values_f64(const double* vx, const double* vy, const double* vz, const double* p, const double* d,
+                        uint64_t n, double* vtot, double* temp, double* c, double* mach, double* pt, double* mu) {
+    QoI::compute_QoIs(vx, vy, vz, p, d, (size_t)n, vtot, temp, c, mach, pt, mu);
+}
+void ref_qoi_vtot_bound_f64(const double* vx, const double* vy, const double* vz, uint64_t n, double ebx, double eby,
+                            double ebz, double* out) {
+    for (uint64_t i = 0; i < n; i++) {
+        double e2 = QoI::compute_bound_x_square(vx[i], ebx) + QoI::compute_bound_x_square(vy[i], eby) +
+                    QoI::compute_bound_x_square(vz[i], ebz);
+        double v2 = vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i];
+        out[i] = QoI::compute_bound_square_root_x(v2, e2);
+    }
+}
+void ref_qoi_t_bound_f64(const double* p, const double* d, uint64_t n, double ebp, double ebd, double* out) {
+    Quiet q;   // the division rule prints a warning where it cannot bound the error
+    const double c1 = 1.0 / 287.1;
+    for (uint64_t i = 0; i < n; i++) out[i] = c1 * QoI::compute_bound_division(p[i], d[i], ebp, ebd);
+}
 }

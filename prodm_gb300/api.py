@@ -165,6 +165,45 @@ def recompose_adjoint(grad, target_level, out=None, stream=None):
     return out
 
 
+def _same_fields(ts):
+    """All given device fields contiguous, of one dtype and one element count
+    (the kernels index them with one flat index)."""
+    ts = [t for t in ts if t is not None]
+    if not ts:
+        raise ValueError("no fields given")
+    for t in ts:
+        if not t.is_contiguous():
+            raise ValueError("fields must be contiguous")
+        if t.dtype != ts[0].dtype or t.numel() != ts[0].numel():
+            raise ValueError("fields must share dtype and element count")
+    return ts[0]
+
+
+def qoi_ge_values(vx, vy, vz, p, d, stream=None):
+    """V_TOT, T, C, Mach, PT, mu of fp64 device fields (six new tensors)."""
+    _same_fields([vx, vy, vz, p, d])
+    outs = [torch.empty_like(vx) for _ in range(6)]
+    call("prodm_qoi_ge_values", _dtype(vx), _ptr(vx), _ptr(vy), _ptr(vz), _ptr(p), _ptr(d), vx.numel(),
+         *[_ptr(o) for o in outs], _stream(stream))
+    return outs
+
+
+def qoi_ge_bounds(V=None, ebs_v=(0.0, 0.0, 0.0), P=None, D=None, eb_p=0.0, eb_d=0.0, stream=None):
+    """Pointwise error estimates of V_TOT (from V = [vx, vy, vz]) and of T
+    (from P, D), fp64 device fields. Returns (bound_vtot, bound_t, maxima)."""
+    ref = _same_fields(list(V if V is not None else []) + [P, D])
+    n = ref.numel()
+    bv = torch.empty_like(ref) if V is not None else None
+    bt = torch.empty_like(ref) if P is not None else None
+    mx = torch.empty(2, dtype=torch.float64, device=ref.device)
+    nul = C.c_void_p(None)
+    vp = [_ptr(v) for v in V] if V is not None else [nul, nul, nul]
+    call("prodm_qoi_ge_bounds", _dtype(ref), *vp, _ptr(P) if P is not None else nul,
+         _ptr(D) if D is not None else nul, n, *[float(e) for e in ebs_v], float(eb_p), float(eb_d),
+         _ptr(bv) if bv is not None else nul, _ptr(bt) if bt is not None else nul, _ptr(mx), _stream(stream))
+    return bv, bt, mx
+
+
 def interpret(kind, estimator, sizes, errors, tolerance, index, ndims=3, target_level=None, s=0.0,
               dtype=torch.float32, stream=None):
     """Device greedy interpreter. sizes [nl,B] (uint32), errors [nl,B+1]; returns (index, retrieve_sizes)."""

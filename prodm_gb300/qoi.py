@@ -7,8 +7,9 @@ of interest holds: max_i |Q(V~(i)) - Q(V(i))| <= tau.
   (app/GE/sequential/halving_Vtot.cpp:31-84 and :153-189): every field is
   retrieved to its own L-inf bound eb_f (SignExclude greedy interpreter,
   MaxErrorEstimatorHB); the pointwise QoI bound is evaluated with the
-  reference's error propagation rules (include/qoi_utils.hpp:18-48, :95-98);
-  while its maximum exceeds tau, all eb_f shrink by 1.5 until the bound at
+  reference's error propagation rules (include/qoi_utils.hpp:18-48, :95-98;
+  for |V| by the device kernel behind ``prodm_qoi_ge_bounds``, bit for bit
+  the reference's V_TOT estimate); while its maximum exceeds tau, all eb_f shrink by 1.5 until the bound at
   the worst point holds, and the fields are retrieved again (at most 5 times).
 
 * ``guided_retrieve`` -- per-(field, level) bitplane budgets from the QoI's
@@ -143,8 +144,13 @@ def halving_retrieve(kind, data, tau, rel, L, B=32, encoder="grouped", max_iter=
         for f, eb in zip(fields, ebs):
             f.retrieve_tolerance(eb)
         V, rho = _unpack(kind, fields)
-        est = qoi_bound(kind, V, ebs[:3], rho, ebs[3] if kind == "ke" else None)
-        bound = float(est.max())
+        if kind == "vmag":
+            # the reference's V_TOT estimate, evaluated by prodm_qoi_ge_bounds
+            est, _, mx = api.qoi_ge_bounds([v.reshape(-1) for v in V], ebs[:3])
+            bound = float(mx[0])
+        else:
+            est = qoi_bound(kind, V, ebs[:3], rho, ebs[3] if kind == "ke" else None)
+            bound = float(est.max())
         if bound <= tau:
             met = True
             break
@@ -155,8 +161,11 @@ def halving_retrieve(kind, data, tau, rel, L, B=32, encoder="grouped", max_iter=
         e = bound
         while e > tau:
             ebs = [x / 1.5 for x in ebs]
-            e = float(qoi_bound(kind, Vi, [torch.tensor(x, dtype=torch.float64, device="cuda") for x in ebs[:3]], ri,
-                                torch.tensor(ebs[3], dtype=torch.float64, device="cuda") if kind == "ke" else None))
+            if kind == "vmag":
+                e = float(api.qoi_ge_bounds(Vi, ebs[:3])[2][0])
+            else:
+                e = float(qoi_bound(kind, Vi, [torch.tensor(x, dtype=torch.float64, device="cuda") for x in ebs[:3]],
+                                    ri, torch.tensor(ebs[3], dtype=torch.float64, device="cuda")))
     return {"bytes": sum(f.bytes() for f in fields), "bound": bound, "met": met, "iterations": it,
             "achieved": _achieved(kind, fields, data), "index": [f.index.tolist() for f in fields]}
 

@@ -183,14 +183,46 @@ def composed_fixtures(R, rng):
     return out
 
 
-def main():
+def qoi_fixtures(R, rng):
+    """GE quantities of interest and their error estimates from the reference's
+    qoi_utils.hpp (QoI::compute_QoIs and the propagation rules), fp64. Edge
+    points: zero velocity (sqrt rule at x == 0), velocities below the bound
+    (x <= eb branch), densities whose bound reaches |D| (no bound: 0) and
+    negative densities (the other branch of the division rule)."""
+    n = 4096
+    vx, vy, vz = (rng.normal(0.0, 50.0, n) for _ in range(3))
+    p = rng.uniform(0.5e5, 1.5e5, n)
+    d = rng.uniform(0.5, 1.5, n)
+    vx[:4] = vy[:4] = vz[:4] = 0.0
+    vx[4:8], vy[4:8], vz[4:8] = 1e-3, -2e-3, 5e-4
+    d[8:12] = [0.05, -0.05, 0.1, -0.5]
+    out = {"vx": vx, "vy": vy, "vz": vz, "p": p, "d": d}
+    for k, v in zip(("vtot", "temp", "c", "mach", "pt", "mu"), R.qoi_values(vx, vy, vz, p, d)):
+        out[k] = v
+    out["ebs_v"] = np.array([0.5, 0.25, 1.0])
+    out["bound_vtot"] = R.qoi_vtot_bound(vx, vy, vz, out["ebs_v"])
+    out["eb_pd"] = np.array([100.0, 0.1])
+    out["bound_t"] = R.qoi_t_bound(p, d, 100.0, 0.1)
+    return out
+
+
+FIXTURES = (("encoders", encoder_fixtures), ("collectors", collector_fixtures),
+            ("interpreters", interpreter_fixtures), ("geometry", geometry_fixtures),
+            ("composed", composed_fixtures), ("qoi", qoi_fixtures))
+
+
+def main(names=None):
+    """Regenerate the named fixture files (all by default)."""
     R = oracle.reference()
     if R is None:
         raise SystemExit("the reference harness is unavailable here; fixtures cannot be regenerated")
-    rng = np.random.default_rng(20240611)
-    for name, fn in (("encoders", encoder_fixtures), ("collectors", collector_fixtures),
-                     ("interpreters", interpreter_fixtures), ("geometry", geometry_fixtures),
-                     ("composed", composed_fixtures)):
+    shared = np.random.default_rng(20240611)    # the first five draw from one stream, in order
+    for name, fn in FIXTURES:
+        rng = np.random.default_rng(20241203) if name == "qoi" else shared
+        if names and name not in names:
+            if name != "qoi":
+                fn(R, rng)                         # keep the shared stream in step
+            continue
         d = fn(R, rng)
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **d)
@@ -198,4 +230,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -52,3 +52,31 @@ def test_guided_meets_bound_with_fewer_bytes(kind, rel):
         assert res["bound"] <= tau
         assert res["achieved"] <= res["bound"] * (1 + 1e-6) + 1e-12
     assert ours["bytes"] <= base["bytes"], (ours["bytes"], base["bytes"])
+
+
+def test_ge_qoi_device_kernels_match_reference_fixtures():
+    """prodm_qoi_ge_values / prodm_qoi_ge_bounds against the reference's
+    qoi_utils.hpp outputs (tests/golden/qoi.npz): products, quotients and
+    square roots bit for bit; PT and mu go through pow, within 1e-14."""
+    import os
+    from prodm_gb300 import api
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi.npz"))
+    t = {k: torch.from_numpy(g[k]).cuda() for k in ("vx", "vy", "vz", "p", "d")}
+    vals = api.qoi_ge_values(t["vx"], t["vy"], t["vz"], t["p"], t["d"])
+    for k, v in zip(("vtot", "temp", "c", "mach", "pt", "mu"), vals):
+        got = v.cpu().numpy()
+        if k in ("pt", "mu"):
+            np.testing.assert_allclose(got, g[k], rtol=1e-14, atol=0)
+        else:
+            assert np.array_equal(got, g[k], equal_nan=True), k
+    bv, bt, mx = api.qoi_ge_bounds([t["vx"], t["vy"], t["vz"]], g["ebs_v"], t["p"], t["d"], *g["eb_pd"])
+    assert np.array_equal(bv.cpu().numpy(), g["bound_vtot"])
+    assert np.array_equal(bt.cpu().numpy(), g["bound_t"])
+    m = mx.cpu().numpy()
+    assert m[0] == g["bound_vtot"].max() and m[1] == g["bound_t"].max()
+    # one QoI at a time; invalid requests raise
+    bv2, bt2, _ = api.qoi_ge_bounds([t["vx"], t["vy"], t["vz"]], g["ebs_v"])
+    assert bt2 is None and torch.equal(bv2, bv)
+    from prodm_gb300._lib import ProdmError
+    with pytest.raises(ProdmError):
+        api.qoi_ge_bounds([t["vx"], t["vy"], t["vz"]], (-1.0, 0.0, 0.0))

@@ -116,3 +116,19 @@ def test_composed_retrieve_meets_tolerance_like_reference(enc):
         # retrieved planes. Same planes => same result up to float rounding.
         if (idx > 0).all():
             np.testing.assert_allclose(rec, ref, atol=1e-5 * float(np.abs(field).max()), rtol=0)
+
+
+def test_ge_qoi_utilities_match_reference():
+    """oracle restatement of qoi_utils.hpp (values, V_TOT and T estimates)
+    against the reference's own functions on the same points, bit for bit"""
+    g = load("qoi")
+    O = oracle.oracle()
+    vals = O.qoi_values(g["vx"], g["vy"], g["vz"], g["p"], g["d"])
+    for k, v in zip(("vtot", "temp", "c", "mach", "pt", "mu"), vals):
+        assert np.array_equal(v, g[k], equal_nan=True), k
+    assert np.array_equal(O.qoi_vtot_bound(g["vx"], g["vy"], g["vz"], g["ebs_v"]), g["bound_vtot"])
+    assert np.array_equal(O.qoi_t_bound(g["p"], g["d"], *g["eb_pd"]), g["bound_t"])
+    # the edge points exercise every branch of the rules; a negative density
+    # gives a negative temperature, whose square root is NaN in the reference too
+    assert np.all(g["bound_vtot"][:4] > 0) and np.any(g["bound_t"][8:12] == 0)
+    assert np.isnan(g["c"][[9, 11]]).all() and not np.isnan(g["c"][[8, 10]]).any()
