@@ -17,7 +17,7 @@ _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 
-ENCODERS = {"negabinary": 0, "grouped": 1}
+ENCODERS = {"negabinary": 0, "grouped": 1, "perbit": 2}
 INTERPRETERS = {"greedy": 0, "sign_exclude": 1, "negabinary": 2}
 ESTIMATORS = {"max_hb": 0, "max_ob": 1, "l2_hb": 2, "snorm": 3}
 
@@ -114,6 +114,20 @@ class Oracle(_Lib):
         total = f(np.ascontiguousarray(data), len(data), int(exp), int(B), blob, sizes,
                   errs.ctypes.data if collect else None)
         return blob[:total].copy(), sizes, errs
+
+    def pb_encode(self, data, exp, B):
+        """PerBit streams of one level: (blob bytes, sizes[B])."""
+        f = self._fn("%s_pb_encode_%s" % (self.prefix, _sfx(data.dtype)), C.c_int64, _tp(data.dtype), C.c_uint64,
+                     C.c_int, C.c_int, _u8p, _u32p)
+        n = len(data)
+        blob = np.zeros(B * (2 * n // 8 + 8) + 64, np.uint8)
+        sizes = np.zeros(B, np.uint32)
+        total = f(np.ascontiguousarray(data), n, int(exp), int(B), blob, sizes)
+        return blob[:total].copy(), sizes
+
+    def perbit_state(self, dtype):
+        """Stateful PerBit progressive decoder (one per encoder object)."""
+        return _PerBitState(self, dtype)
 
     def nb_decode(self, blob, sizes, n, exp, s, num, dtype):
         f = self._fn("or_nb_decode_" + _sfx(dtype), C.c_int, _u8p, _u32p, C.c_uint64, C.c_int, C.c_int, C.c_int,
@@ -274,6 +288,31 @@ class _GroupedState:
             pass
 
 
+class _PerBitState:
+    def __init__(self, lib, dtype):
+        self.dtype, sfx, pre = np.dtype(dtype), _sfx(dtype), lib.prefix
+        if pre == "ref":
+            new, free, dec = "ref_pb_new_", "ref_pb_free_", "ref_pb_decode_"
+        else:
+            new, free, dec = "or_pb_state_new_", "or_pb_state_free_", "or_pb_decode_"
+        self._free = lib._fn(free + sfx, None, C.c_void_p)
+        self._dec = lib._fn(dec + sfx, C.c_int, C.c_void_p, _u8p, _u32p, C.c_uint64, C.c_int, C.c_int, C.c_int,
+                            C.c_int, _tp(dtype))
+        self.h = lib._fn(new + sfx, C.c_void_p)()
+
+    def decode(self, blob, sizes, n, exp, s, num, level):
+        out = np.zeros(n, self.dtype)
+        self._dec(self.h, np.ascontiguousarray(blob, np.uint8), np.ascontiguousarray(sizes, np.uint32), n, exp, s, num,
+                  level, out)
+        return out
+
+    def __del__(self):
+        try:
+            self._free(self.h)
+        except Exception:
+            pass
+
+
 class Reference(Oracle):
     """The reference's own components, compiled by oracle/build_oracle.build_ref."""
 
@@ -324,6 +363,16 @@ class Reference(Oracle):
         tols = np.asarray(tols, np.float64)
         outs = np.zeros((len(tols), field.size), dt)
         ret = np.zeros(len(tols), np.uint64)
+        if encoder == "perbit":
+            if not hierarchical:
+                raise ValueError("the reference's PerBit drivers use the hierarchical basis")
+            f = self._fn("ref_composed_pb_" + _sfx(dt), C.c_int, _tp(dt), C.c_int, _u32p, C.c_int, C.c_int,
+                         C.c_char_p, C.c_int, _f64p, _tp(dt), np.ctypeslib.ndpointer(np.uint64))
+            rc = f(np.ascontiguousarray(field).ravel(), len(dims), dims, L, B, workdir.encode(), len(tols), tols,
+                   outs, ret)
+            if rc != 0:
+                raise RuntimeError("reference composed round trip failed")
+            return outs.reshape((len(tols),) + field.shape), ret
         f = self._fn("ref_composed_" + _sfx(dt), C.c_int, _tp(dt), C.c_int, _u32p, C.c_int, C.c_int, C.c_int,
                      C.c_int, C.c_char_p, C.c_int, _f64p, _tp(dt), np.ctypeslib.ndpointer(np.uint64))
         rc = f(np.ascontiguousarray(field).ravel(), len(dims), dims, L, B, ENCODERS[encoder], int(hierarchical),

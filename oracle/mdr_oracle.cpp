@@ -10,6 +10,7 @@ std::vector<uint32_t> vec(const uint32_t* p, int n) { return std::vector<uint32_
 template <class T>
 size_t encode_any(int enc, const T* d, size_t n, int exp, int B, uint8_t* blob, uint32_t* sizes, double* errs) {
     using S = typename std::conditional<std::is_same<T, double>::value, uint64_t, uint32_t>::type;
+    if (enc == 2) return pb_encode<T>(d, n, exp, B, blob, sizes);
     return enc == 0 ? nb_encode<T, S>(d, n, exp, B, blob, sizes, errs) : gr_encode<T, S>(d, n, exp, B, blob, sizes, errs);
 }
 
@@ -86,6 +87,7 @@ int retrieve_full(int ndims, const uint32_t* dims_, int L, int B, int enc, int h
     std::fill(out, out + N, (T)0);
     size_t off = 0;
     GroupedState<S> st;
+    PerBitState pst;
     std::vector<T> buf;
     for (int i = 0; i <= L; i++) {
         std::vector<const uint8_t*> planes(B);
@@ -94,6 +96,7 @@ int retrieve_full(int ndims, const uint32_t* dims_, int L, int B, int enc, int h
         int e = 0; std::frexp(enc == 0 ? bounds[i] / 4 : bounds[i], &e);
         buf.assign(le[i], 0);
         if (enc == 0) nb_decode<T, S>(planes.data(), le[i], e, 0, index[i], buf.data());
+        else if (enc == 2) pb_decode<T>(pst, planes.data(), le[i], e, 0, index[i], i, buf.data());
         else if (gr_decode<T, S>(st, planes.data(), le[i], e, 0, index[i], i, buf.data()) != 0) return -2;
         reposition<T>(buf.data(), dims, ld[i], i == 0 ? zero : ld[i - 1], out);
         off = o;
@@ -139,6 +142,19 @@ void or_level_elements(int ndims, const uint32_t* dims, int L, uint32_t* out) {
         size_t o = 0;                                                                                         \
         for (int i = 0; i < num; i++) { planes[i] = blob + o; o += sizes[i]; }                                \
         nb_decode<T, S>(planes.data(), n, exp, s, num, out);                                                  \
+        return 0;                                                                                             \
+    }                                                                                                         \
+    int64_t or_pb_encode_##SUF(const T* d, uint64_t n, int exp, int B, uint8_t* blob, uint32_t* sizes) {      \
+        return (int64_t)pb_encode<T>(d, n, exp, B, blob, sizes);                                              \
+    }                                                                                                         \
+    void* or_pb_state_new_##SUF() { return new PerBitState(); }                                               \
+    void or_pb_state_free_##SUF(void* p) { delete (PerBitState*)p; }                                          \
+    int or_pb_decode_##SUF(void* st, const uint8_t* blob, const uint32_t* sizes, uint64_t n, int exp, int s,  \
+                           int num, int level, T* out) {                                                      \
+        std::vector<const uint8_t*> planes(num > 0 ? num : 1);                                                \
+        size_t o = 0;                                                                                         \
+        for (int i = 0; i < num; i++) { planes[i] = blob + o; o += sizes[i]; }                                \
+        pb_decode<T>(*(PerBitState*)st, planes.data(), n, exp, s, num, level, out);                           \
         return 0;                                                                                             \
     }                                                                                                         \
     void* or_gr_state_new_##SUF() { return new GroupedState<S>(); }                                           \

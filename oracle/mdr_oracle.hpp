@@ -368,6 +368,100 @@ int gr_decode(GroupedState<S>& st, const uint8_t* const* planes, size_t n, int e
     return 0;
 }
 
+// PerBitBPEncoder::encode -- PerBitBPEncoder.hpp:81-146 (the stream word type
+// of the template does not enter the format). One bit stream per plane, bits
+// packed from the least significant end of 64-bit words (BitEncoder :7-39).
+// Element i writes, in plane p, bit (B-1-p) of its fixed-point magnitude and,
+// right after its first 1 bit, its sign (1 = negative); a stream's size is its
+// 64-bit word count times 8.
+template <class T>
+size_t pb_encode(const T* data, size_t n, int exp, int B, uint8_t* blob, uint32_t* sizes) {
+    using FP = fp_t<T>;
+    std::vector<std::vector<uint64_t>> words(B);
+    std::vector<uint64_t> buf(B, 0);
+    std::vector<int> fill(B, 0);
+    auto put = [&](int p, uint64_t b) {
+        buf[p] += b << fill[p];
+        if (++fill[p] == 64) { words[p].push_back(buf[p]); buf[p] = 0; fill[p] = 0; }
+    };
+    for (size_t i = 0; i < n; i++) {
+        const T v = data[i];
+        const T shifted = std::ldexp(v, B - exp);
+        const bool neg = v < 0;
+        const int64_t fx = (int64_t)shifted;
+        const FP mag = neg ? (FP)(-fx) : (FP)fx;
+        bool first = true;
+        for (int k = B - 1; k >= 0; k--) {
+            const int p = B - 1 - k;
+            const uint64_t bit = (mag >> k) & 1u;
+            put(p, bit);
+            if (bit && first) { put(p, neg); first = false; }
+        }
+    }
+    size_t off = 0;
+    for (int p = 0; p < B; p++) {
+        if (fill[p]) words[p].push_back(buf[p]);
+        sizes[p] = (uint32_t)(words[p].size() * 8);
+        if (sizes[p]) std::memcpy(blob + off, words[p].data(), sizes[p]);
+        off += sizes[p];
+    }
+    return off;
+}
+
+// Progressive per-bit decoding state per level (PerBitBPEncoder.hpp:399-400
+// keeps it by push order): whether an element's sign has been read, and the sign.
+struct PerBitState {
+    std::vector<std::vector<uint8_t>> sign, flag;
+    void ensure(int level, size_t n) {
+        if ((int)sign.size() <= level) { sign.resize(level + 1); flag.resize(level + 1); }
+        if (sign[level].size() != n) { sign[level].assign(n, 0); flag[level].assign(n, 0); }
+    }
+};
+
+// PerBitBPEncoder::progressive_decode -- :290-383. planes[i] = stream of plane
+// s+i; returns the contribution of planes [s, s+num), scaled by 2^(exp-(s+num)).
+template <class T>
+void pb_decode(PerBitState& st, const uint8_t* const* planes, size_t n, int exp, int s, int num, int level, T* out) {
+    using FP = fp_t<T>;
+    if (num == 0) { for (size_t i = 0; i < n; i++) out[i] = 0; return; }
+    st.ensure(level, n);
+    std::vector<uint8_t>& sg = st.sign[level];
+    std::vector<uint8_t>& fl = st.flag[level];
+    std::vector<uint64_t> word(num, 0);
+    std::vector<int> left(num, 0);
+    std::vector<size_t> next(num, 0);
+    auto get = [&](int i) -> uint64_t {   // BitDecoder::decode :49-58
+        if (left[i] == 0) {
+            std::memcpy(&word[i], planes[i] + 8 * next[i]++, 8);
+            left[i] = 64;
+        }
+        const uint64_t b = word[i] & 1u;
+        word[i] >>= 1;
+        left[i]--;
+        return b;
+    };
+    const int e = s + num;
+    for (size_t j = 0; j < n; j++) {
+        FP acc = 0;
+        bool neg = false;
+        if (fl[j]) {
+            neg = sg[j];
+            for (int k = num - 1; k >= 0; k--) acc += (FP)get(num - 1 - k) << k;
+        } else {
+            bool first = true;
+            for (int k = num - 1; k >= 0; k--) {
+                const int i = num - 1 - k;
+                const FP bit = (FP)get(i);
+                acc += bit << k;
+                if (bit && first) { neg = get(i) != 0; first = false; fl[j] = 1; }
+            }
+            sg[j] = neg;
+        }
+        const T v = std::ldexp((T)acc, exp - e);
+        out[j] = neg ? -v : v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Error collectors.
 // ---------------------------------------------------------------------------

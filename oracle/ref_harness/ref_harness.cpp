@@ -203,6 +203,35 @@ extern "C" {
 REF_T(f32, float, uint32_t)
 REF_T(f64, double, uint64_t)
 
+// PerBitBPEncoder with the stream word type the GE applications instantiate it
+// with (refactorGE.cpp:72: PerBitBPEncoder<Type, uint32_t>)
+#define REF_PB(SUF, T)                                                                                          \
+    int64_t ref_pb_encode_##SUF(const T* d, uint64_t n, int exp, int B, uint8_t* blob, uint32_t* sizes) {      \
+        return enc_call<T, uint32_t, MDR::PerBitBPEncoder<T, uint32_t>>(d, n, exp, B, blob, sizes, nullptr);    \
+    }                                                                                                           \
+    void* ref_pb_new_##SUF() { return new MDR::PerBitBPEncoder<T, uint32_t>(); }                                \
+    void ref_pb_free_##SUF(void* p) { delete (MDR::PerBitBPEncoder<T, uint32_t>*)p; }                           \
+    int ref_pb_decode_##SUF(void* h, const uint8_t* blob, const uint32_t* sizes, uint64_t n, int exp, int s,    \
+                            int num, int level, T* out) {                                                       \
+        std::vector<const uint8_t*> planes;                                                                     \
+        size_t o = 0;                                                                                           \
+        for (int i = 0; i < num; i++) { planes.push_back(blob + o); o += sizes[i]; }                            \
+        T* r = ((MDR::PerBitBPEncoder<T, uint32_t>*)h)->progressive_decode(planes, (int32_t)n, exp, (uint8_t)s, \
+                                                                          (uint8_t)num, level);                 \
+        std::memcpy(out, r, n * sizeof(T));                                                                     \
+        free(r);                                                                                                \
+        return 0;                                                                                               \
+    }                                                                                                           \
+    int ref_composed_pb_##SUF(const T* field, int ndims, const uint32_t* dims, int L, int B, const char* dir,   \
+                              int ntol, const double* tols, T* outs, uint64_t* retrieved) {                     \
+        return composed_roundtrip<T, uint32_t, MDR::MGARDHierarchicalDecomposer<T>,                             \
+                                  MDR::PerBitBPEncoder<T, uint32_t>, MDR::MaxErrorEstimatorHB<T>>(              \
+            field, ndims, dims, L, B, false, dir, ntol, tols, outs, retrieved);                                 \
+    }
+
+REF_PB(f32, float)
+REF_PB(f64, double)
+
 // GE quantities of interest (qoi_utils.hpp:135-165) and the pointwise error
 // estimates the GE retrieval drivers form with the propagation rules of
 // qoi_utils.hpp:18-98: V_TOT as in halving_Vtot.cpp:38-45, T = P / (D R) as in

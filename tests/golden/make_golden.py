@@ -3,7 +3,7 @@
 Runs only where the reference tree is present: the reference's MDR headers are
 compiled by oracle/build_oracle.build_ref (oracle/_ref/libprodm_ref.so) and
 every fixture below is produced by calling the reference's own classes
-(NegaBinaryBPEncoder, GroupedBPEncoder, MaxErrorCollector,
+(NegaBinaryBPEncoder, GroupedBPEncoder, PerBitBPEncoder, MaxErrorCollector,
 SquaredErrorCollector, the greedy size interpreters, DirectInterleaver,
 compute_level_dims/elements and the ComposedRefactor -> ComposedReconstructor
 pair). Inputs are seeded and stored beside the outputs so that the fixtures
@@ -206,9 +206,69 @@ def qoi_fixtures(R, rng):
     return out
 
 
+PB_N = (1, 2, 31, 32, 33, 63, 64, 65, 95, 127, 729, 4184)
+
+
+def perbit_fixtures(R, rng):
+    """PerBitBPEncoder<T, uint32_t> (the GE applications' encoder): streams and
+    sizes, and the progressive decode in three steps ([0, s1), [s1, s2),
+    [s2, B)) through one decoder object; then a ComposedRefactor ->
+    ComposedReconstructor round trip with it (fp64, 60 planes, hierarchical
+    basis, SignExclude greedy interpreter, MaxErrorEstimatorHB). fp64 stops at
+    63 planes: at 64 the level-max element scales to >= 2^63, whose int64
+    conversion in the reference is undefined (it differs between x86 and Arm)."""
+    out = {}
+    cases = []
+    for dt, Bs in ((np.float32, (2, 8, 32)), (np.float64, (2, 33, 60, 63))):
+        for n in PB_N:
+            for B in Bs:
+                scale = float(rng.choice([1e-3, 1.0, 1e3]))
+                x = coeff_like(rng, n, dt, scale)
+                if n >= 8:
+                    x[5] = -np.abs(x).max()                # the level-max element, negative
+                    x[6] = np.ldexp(dt(1.0), -40)          # below the last plane
+                mx = float(np.max(np.abs(x)))
+                e = math.frexp(mx)[1] if mx > 0 else 0
+                blob, sizes = R.pb_encode(x, e, B)
+                dec = R.perbit_state(dt)
+                s1, s2 = max(1, B // 3), max(1, B // 3) + max(1, B // 4)
+                s2 = min(s2, B)
+                offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+                key = "%s_n%d_B%d" % (np.dtype(dt).name, n, B)
+                steps = [(0, s1), (s1, s2), (s2, B)]
+                for i, (a, b) in enumerate(steps):
+                    out["%s_dec%d" % (key, i)] = dec.decode(blob[offs[a]:offs[b]], sizes[a:b], n, e, a, b - a, 0)
+                out[key + "_x"] = x
+                out[key + "_exp"] = np.int32(e)
+                out[key + "_blob"] = blob
+                out[key + "_sizes"] = sizes
+                out[key + "_steps"] = np.array(steps, np.int32)
+                cases.append(key)
+    out["cases"] = np.array(cases)
+    shape, L, B = (17, 17, 17), 3, 60
+    g = sinusoid_field(rng, 17).astype(np.float64) * 1e3
+    vr = float(g.max() - g.min())
+    tols = np.array([vr * t for t in (1e-2, 1e-5, 1e-9)])
+    with tempfile.TemporaryDirectory() as d:
+        outs, ret = R.composed(g, L, B, "perbit", True, tols, d)
+        levels = [np.frombuffer(open(os.path.join(d, "level_%d.bin" % i), "rb").read(), np.uint8)
+                  for i in range(L + 1)]
+        meta = np.frombuffer(open(os.path.join(d, "metadata.bin"), "rb").read(), np.uint8)
+    out["composed_field"] = g
+    out["composed_tols"] = tols
+    out["composed_levels"] = np.concatenate(levels)
+    out["composed_level_bytes"] = np.array([len(x) for x in levels], np.int64)
+    out["composed_metadata"] = meta
+    out["composed_recon"] = outs
+    out["composed_retrieved"] = ret
+    return out
+
+
 FIXTURES = (("encoders", encoder_fixtures), ("collectors", collector_fixtures),
             ("interpreters", interpreter_fixtures), ("geometry", geometry_fixtures),
-            ("composed", composed_fixtures), ("qoi", qoi_fixtures))
+            ("composed", composed_fixtures), ("qoi", qoi_fixtures), ("perbit", perbit_fixtures))
+
+OWN_SEED = {"qoi": 20241203, "perbit": 20241204}   # fixtures with their own random stream
 
 
 def main(names=None):
@@ -218,9 +278,9 @@ def main(names=None):
         raise SystemExit("the reference harness is unavailable here; fixtures cannot be regenerated")
     shared = np.random.default_rng(20240611)    # the first five draw from one stream, in order
     for name, fn in FIXTURES:
-        rng = np.random.default_rng(20241203) if name == "qoi" else shared
+        rng = np.random.default_rng(OWN_SEED[name]) if name in OWN_SEED else shared
         if names and name not in names:
-            if name != "qoi":
+            if name not in OWN_SEED:
                 fn(R, rng)                         # keep the shared stream in step
             continue
         d = fn(R, rng)

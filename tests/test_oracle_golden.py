@@ -132,3 +132,49 @@ def test_ge_qoi_utilities_match_reference():
     # gives a negative temperature, whose square root is NaN in the reference too
     assert np.all(g["bound_vtot"][:4] > 0) and np.any(g["bound_t"][8:12] == 0)
     assert np.isnan(g["c"][[9, 11]]).all() and not np.isnan(g["c"][[8, 10]]).any()
+
+
+def _perbit_cases():
+    return [str(c) for c in load("perbit")["cases"]]
+
+
+@pytest.mark.parametrize("case", _perbit_cases())
+def test_perbit_streams_and_progressive_decode_bit_exact(case):
+    """oracle PerBit encode / progressive decode (three steps through one
+    decoder state) against PerBitBPEncoder<T, uint32_t> itself"""
+    g = load("perbit")
+    dt, n, B = case.split("_")
+    n, B, dtype = int(n[1:]), int(B[1:]), np.dtype(dt)
+    x, e = g[case + "_x"], int(g[case + "_exp"])
+    blob, sizes = O.pb_encode(x, e, B)
+    assert np.array_equal(sizes, g[case + "_sizes"])
+    assert np.array_equal(blob, g[case + "_blob"])
+    offs = split_streams(blob, sizes)
+    dec = O.perbit_state(dtype)
+    total = np.zeros(n, dtype)
+    for i, (a, b) in enumerate(g[case + "_steps"]):
+        d = dec.decode(blob[offs[a]:offs[b]], sizes[a:b], n, e, int(a), int(b - a), 0)
+        assert np.array_equal(d.view(np.uint8), g["%s_dec%d" % (case, i)].view(np.uint8)), i
+        total = total + d
+    # all planes: every element within one unit of the last plane
+    assert np.all(np.abs(total.astype(np.float64) - x.astype(np.float64)) <= np.ldexp(1.0, e - B) * (1 + 1e-6))
+
+
+def test_perbit_composed_level_files_and_retrieval_match_reference():
+    g = load("perbit")
+    field = g["composed_field"]
+    L, B = 3, 60
+    res = O.refactor(field, L, B, "perbit", True)
+    assert res["blob"].tobytes() == g["composed_levels"].tobytes()
+    idx = np.zeros(L + 1, np.uint8)
+    for t, tol in enumerate(g["composed_tols"]):
+        errs = np.stack([O.max_collect(b, B, np.float64) for b in res["bounds"]])
+        idx, _ = O.interpret("sign_exclude", "max_hb", res["sizes"], errs, float(tol), idx, dtype=np.float64)
+        rec = O.retrieve(field.shape, L, B, res["blob"], res["sizes"], res["bounds"], idx, "perbit", True,
+                         np.float64)
+        assert np.max(np.abs(rec - field)) <= tol
+        # same planes as the reference: the bytes it read are the planes' sizes
+        sz = res["sizes"].reshape(L + 1, B).astype(np.int64)
+        planes = sum(int(sz[l, :idx[l]].sum()) for l in range(L + 1))
+        assert planes == int(g["composed_retrieved"][t]), t
+        np.testing.assert_allclose(rec, g["composed_recon"][t], atol=1e-12 * float(np.abs(field).max()), rtol=0)
