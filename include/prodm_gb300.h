@@ -13,6 +13,8 @@
  *              PRODM_F64 (double data, u64 stream words, 64-value blocks)
  *   encoder    PRODM_ENC_NEGABINARY  NegaBinaryBPEncoder<T, S>
  *              PRODM_ENC_GROUPED     GroupedBPEncoder<T, S>
+ *              PRODM_ENC_PERBIT      PerBitBPEncoder<T, S> (the stream word type
+ *                                    does not enter its format; fp64 up to 63 planes)
  *   basis      PRODM_BASIS_HIERARCHICAL  MGARDHierarchicalDecomposer (MGARD.hpp:42-70)
  *              PRODM_BASIS_ORTHOGONAL    MGARDOrthoganalDecomposer   (MGARD.hpp:11-39)
  *   interpreter PRODM_INTERP_GREEDY / _SIGN_EXCLUDE / _NEGABINARY
@@ -44,6 +46,7 @@ extern "C" {
 #define PRODM_F64 1
 #define PRODM_ENC_NEGABINARY 0
 #define PRODM_ENC_GROUPED 1
+#define PRODM_ENC_PERBIT 2
 #define PRODM_BASIS_HIERARCHICAL 0
 #define PRODM_BASIS_ORTHOGONAL 1
 #define PRODM_INTERP_GREEDY 0
@@ -97,7 +100,9 @@ int prodm_reposition(int dtype, const void* d_buf, int ndims, const uint32_t* di
 /* ---------------------------------------------------------------------------
  * Bitplane encoder -- BitplaneEncoderInterface<T>::encode
  * (BitplaneEncoderInterface.hpp:16; NegaBinaryBPEncoder.hpp:18-125;
- * GroupedBPEncoder.hpp:18-145).
+ * GroupedBPEncoder.hpp:18-145; PerBitBPEncoder.hpp:81-146, whose d_errors is
+ * not computed: the reference pipeline calls its plain overload,
+ * ComposedRefactor.hpp:124). PRODM_ENC_PERBIT needs d_blob 8-byte aligned.
  * Writes the level's streams concatenated in plane order into d_blob (the
  * byte layout of the reference level file with NullLevelCompressor) and the
  * per-plane byte sizes into d_sizes[B]. d_errors (nullable): the
@@ -113,9 +118,13 @@ int prodm_encode(int encoder, int dtype, const void* d_data, uint64_t n, int exp
 
 /* Progressive decoder -- BitplaneEncoderInterface<T>::decode / progressive_decode
  * (BitplaneEncoderInterface.hpp:18-20; NegaBinaryBPEncoder.hpp:127-192;
- * GroupedBPEncoder.hpp:147-297). The handle keeps the per-level state of the
- * grouped decoder (recording bitplanes and signs, GroupedBPEncoder.hpp:379-380),
- * indexed by level. d_blob holds planes [start, start+num) concatenated as the
+ * GroupedBPEncoder.hpp:147-297; PerBitBPEncoder.hpp:290-383). The handle keeps
+ * the per-level state of the grouped decoder (recording bitplanes and signs,
+ * GroupedBPEncoder.hpp:379-380) and of the per-bit decoder (which elements'
+ * signs are known, and the signs, PerBitBPEncoder.hpp:399-400), indexed by
+ * level. A per-bit level is decoded plane after plane (each call starts where
+ * the previous one stopped): a plane's bit positions depend on the planes
+ * before it. d_blob holds planes [start, start+num) concatenated as the
  * reference retriever hands them over (FileRetriever.hpp:69-81); h_sizes are
  * their byte sizes (host). The first call for a level must start at plane 0.
  * Output: the contribution of these planes, n values, into d_out. */

@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libprodm_gb300.so")
 
 F32, F64 = 0, 1
-ENC = {"negabinary": 0, "grouped": 1}
+ENC = {"negabinary": 0, "grouped": 1, "perbit": 2}
 BASIS = {"hierarchical": 0, "orthogonal": 1}
 INTERP = {"greedy": 0, "sign_exclude": 1, "negabinary": 2}
 EST = {"max_hb": 0, "max_ob": 1, "l2_hb": 2, "snorm": 3}

@@ -131,7 +131,7 @@ int check_dtype(int dtype) {
     return PRODM_OK;
 }
 int check_bitplanes(int dtype, int enc, int B) {
-    int maxB = dtype == PRODM_F64 ? (enc == PRODM_ENC_GROUPED ? 63 : 64) : 32;
+    int maxB = dtype == PRODM_F64 ? (enc == PRODM_ENC_NEGABINARY ? 64 : 63) : 32;
     if (B < 1 || B > maxB) return fail(PRODM_EINVAL, "num_bitplanes must be in [1, " + std::to_string(maxB) + "]");
     return PRODM_OK;
 }
@@ -280,6 +280,7 @@ uint64_t encode_bound(int enc, int dtype, uint64_t n, int B) {
     uint64_t nb = nblocks_of(dtype, n);
     uint64_t wb = esize(dtype);
     if (enc == PRODM_ENC_NEGABINARY) return (uint64_t)B * nb * wb;
+    if (enc == PRODM_ENC_PERBIT) return (uint64_t)B * ((2 * n + 63) / 64 * 8);   // <= 2 bits per value and plane
     return (uint64_t)B * nb * wb + nb * wb + 4 + nb;   // each block: rb header + (B - rb) words + one sign word
 }
 
@@ -288,6 +289,11 @@ void encode_reserve(Workspace& ws, int enc, int dtype, uint64_t n, int B) {
     uint64_t nch = gr_nchunks(nb);
     uint64_t parts = nch > (uint64_t)kPartialSlots ? nch : (uint64_t)kPartialSlots;
     ws.reserve(parts * (B + 1) * sizeof(double));
+    if (enc == PRODM_ENC_PERBIT) {
+        ws.reserve((uint64_t)(B + 1) * pb_row_words(n) * 4);   // magnitude + sign rows
+        ws.reserve(64 * 4);                                    // first-one counts
+        ws.reserve(pb_pack_scratch_bytes(n, B));
+    }
     if (enc == PRODM_ENC_GROUPED) {
         ws.reserve((uint64_t)B * 2 * nb * esize(dtype));  // aligned staging
         ws.reserve(nb);                                   // rb
@@ -312,6 +318,15 @@ int encode_impl(int enc, const T* x, uint64_t n, int exp, int B, uint8_t* blob, 
     encode_reserve(ws, enc, dtype, n, B);
     if ((rc = ws.commit())) return rc;
     double* partial = (double*)ws.take(parts * (B + 1) * sizeof(double));
+    if (enc == PRODM_ENC_PERBIT) {
+        if ((uintptr_t)blob % 8) return fail(PRODM_EINVAL, "encode: the per-bit blob must be 8-byte aligned");
+        const uint64_t rw = pb_row_words(n);
+        uint32_t* rows = (uint32_t*)ws.take((uint64_t)(B + 1) * rw * 4);
+        uint32_t* counts = (uint32_t*)ws.take(64 * 4);
+        void* scratch = ws.take(pb_pack_scratch_bytes(n, B));
+        if ((rc = launch_pb_encode<T>(x, n, nullptr, exp, B, rows, rw, counts, sizes, st))) return rc;
+        return launch_pb_pack(rows, rw, n, B, sizes, encode_bound(enc, dtype, n, B), blob, scratch, st);
+    }
     if (enc == PRODM_ENC_NEGABINARY) {
         if ((uintptr_t)blob % sizeof(T)) return fail(PRODM_EINVAL, "encode: blob must be aligned to the stream word");
         if ((rc = launch_fill_u32(sizes, (uint64_t)B, (uint32_t)(nb * sizeof(T)), st))) return rc;
@@ -348,10 +363,13 @@ struct prodm_decoder {
         uint8_t* rbs = nullptr;
         uint32_t* chunk_off = nullptr;
         void* signs = nullptr;
+        uint32_t* pbrows = nullptr;   // per-bit: rows 0..B-1, sign row, unseen row, status word
+        int parsed = 0;               // per-bit: planes decoded so far
     };
     std::vector<Level> levels;
     ~prodm_decoder() {
         for (auto& l : levels) {
+            if (l.pbrows) cudaFree(l.pbrows);
             if (l.rbs) cudaFree(l.rbs);
             if (l.chunk_off) cudaFree(l.chunk_off);
             if (l.signs) cudaFree(l.signs);
@@ -361,6 +379,80 @@ struct prodm_decoder {
 
 namespace prodm {
 namespace {
+// per-bit levels: parse planes [s, s+num) of the reference streams into the
+// level's rows (the unseen / sign rows carry the state of the planes before),
+// then decode their contribution
+template <class T>
+int pb_progressive_decode(prodm_decoder* h, const uint8_t* blob, const uint32_t* hs, uint64_t n, int exp, int s,
+                          int num, int level, int B, T* out, cudaStream_t st) {
+    if (B > (sizeof(T) == 8 ? 63 : 32)) return fail(PRODM_EINVAL, "decode: per-bit fp64 streams hold at most 63 planes");
+    if ((int)h->levels.size() <= level) h->levels.resize(level + 1);
+    auto& L = h->levels[level];
+    const uint64_t rw = pb_row_words(n);
+    if (!L.have) {
+        if (s != 0) return fail(PRODM_EINVAL, "decode: the first call for a level must start at plane 0");
+        if (L.pbrows && (L.n != n || L.B != B)) { cudaFree(L.pbrows); L.pbrows = nullptr; }
+        if (!L.pbrows) PRODM_CUDA(cudaMalloc((void**)&L.pbrows, (uint64_t)(B + 2) * rw * 4 + 16));
+        int rc = launch_pb_init_unseen(L.pbrows + (uint64_t)(B + 1) * rw, L.pbrows + (uint64_t)B * rw, n, st);
+        if (rc) return rc;
+        L.have = true;
+        L.n = n;
+        L.B = B;
+        L.parsed = 0;
+    } else if (L.n != n || L.B != B) {
+        return fail(PRODM_EINVAL, "decode: level shape changed between calls");
+    }
+    if (s != L.parsed)
+        return fail(PRODM_EINVAL, "decode: per-bit planes are decoded in order; this level continues at plane " +
+                                      std::to_string(L.parsed));
+    uint64_t total = 0;
+    for (int i = 0; i < num; i++) {
+        if (hs[i] % 8 || hs[i] == 0) return fail(PRODM_ECORRUPT, "decode: per-bit stream size not a positive multiple of 8");
+        total += hs[i];
+    }
+    uint32_t* rows = L.pbrows;
+    int* status = (int*)(rows + (uint64_t)(B + 2) * rw);
+    uint8_t* tmp = nullptr;
+    const uint8_t* base = blob;
+    if ((uintptr_t)blob % 8) {   // streams are read as 64-bit words
+        PRODM_CUDA(cudaMallocAsync((void**)&tmp, total, st));
+        PRODM_CUDA(cudaMemcpyAsync(tmp, blob, total, cudaMemcpyDeviceToDevice, st));
+        base = tmp;
+    }
+    std::vector<uint64_t> hv(2 * num);
+    uint64_t o = 0;
+    for (int i = 0; i < num; i++) {
+        hv[i] = (uint64_t)(uintptr_t)(base + o);
+        hv[num + i] = hs[i] / 8;
+        o += hs[i];
+    }
+    uint64_t* dv;
+    PRODM_CUDA(cudaMallocAsync((void**)&dv, hv.size() * 8, st));
+    PRODM_CUDA(cudaMemcpyAsync(dv, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st));
+    PRODM_CUDA(cudaMemsetAsync(status, 0, 4, st));
+    int rc = launch_pb_parse((const uint64_t* const*)dv, dv + num, s, num, n, rows, rw, rows + (uint64_t)(B + 1) * rw,
+                             rows + (uint64_t)B * rw, status, st);
+    if (!rc)
+        rc = launch_pb_decode<T>(rows, rw, n, nullptr, exp, B, s, s + num, nullptr, rows + (uint64_t)B * rw,
+                                 rows + (uint64_t)(B + 1) * rw, out, st);
+    int hstat = 0;
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(&hstat, status, 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_status(e, "per-bit decode");
+    }
+    cudaFreeAsync(dv, st);
+    if (tmp) cudaFreeAsync(tmp, st);
+    // a failed parse leaves the level's state behind the data: the next call
+    // for this level starts again at plane 0
+    if (rc || hstat) L.have = false;
+    if (rc) return rc;
+    if (hstat == PRODM_ETIMEOUT) return fail(PRODM_ETIMEOUT, "decode: the per-bit parse pipeline stalled");
+    if (hstat) return fail(PRODM_ECORRUPT, "decode: a per-bit stream does not end where its size says");
+    L.parsed = s + num;
+    return PRODM_OK;
+}
+
 template <class T>
 int progressive_decode_impl(prodm_decoder* h, const uint8_t* blob, const uint32_t* hs, uint64_t n, int exp, int s,
                             int num, int level, int B, T* out, cudaStream_t st) {
@@ -372,6 +464,7 @@ int progressive_decode_impl(prodm_decoder* h, const uint8_t* blob, const uint32_
     }
     if (n == 0) return fail(PRODM_EINVAL, "decode: n must be >= 1");
     if (s < 0 || num < 0 || s + num > B) return fail(PRODM_EINVAL, "decode: planes outside [0, total_bitplanes)");
+    if (h->enc == PRODM_ENC_PERBIT) return pb_progressive_decode<T>(h, blob, hs, n, exp, s, num, level, B, out, st);
     const uint64_t nb = nblocks_of(dtype, n);
     int rc;
     if (h->enc == PRODM_ENC_NEGABINARY) {
@@ -471,6 +564,9 @@ struct prodm_mdr {
     int B = 0;
     size_t es = 4;
     bool nb = true, orth = false, sq = false;
+    bool pb = false;                               // per-bit encoder
+    uint32_t* pbcounts = nullptr;                  // per-bit: first-one counts, 64 per level
+    int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
     std::vector<void*> allocs;
     void* coef = nullptr;
     void* cbuf[2] = {nullptr, nullptr};
@@ -644,8 +740,10 @@ int mdr_alloc_all(prodm_mdr* h) {
         // multiple of 16 bytes) so that whole plane runs move with 16-byte
         // copies; the pad words are never part of a stream
         const uint64_t pw = 16 / es;
-        h->plane_cap[l] = h->nb ? (nbk + pw - 1) / pw * pw : 2 * nbk;
-        h->lvl_byte_off[l + 1] = h->lvl_byte_off[l] + (uint64_t)B * h->plane_cap[l] * es;
+        // per-bit: B magnitude rows + sign row + unseen row of u32 group words
+        h->plane_cap[l] = h->pb ? pb_row_words(g.elems[l]) : h->nb ? (nbk + pw - 1) / pw * pw : 2 * nbk;
+        h->lvl_byte_off[l + 1] = h->lvl_byte_off[l] + (h->pb ? (uint64_t)(B + 2) * h->plane_cap[l] * 4
+                                                             : (uint64_t)B * h->plane_cap[l] * es);
         h->rb_off[l + 1] = h->rb_off[l] + nbk;
         uint64_t nch = gr_nchunks(nbk);
         maxch = nch > maxch ? nch : maxch;
@@ -672,6 +770,9 @@ int mdr_alloc_all(prodm_mdr* h) {
         for (int l = 0; l <= L; l++)
             for (int p = 0; p < B; p++) sz[l * B + p] = (uint32_t)(h->nblocks[l] * es);
         PRODM_CUDA(cudaMemcpy(h->sizes, sz.data(), sz.size() * 4, cudaMemcpyHostToDevice));
+    } else if (h->pb) {
+        if ((rc = h->alloc((void**)&h->pbcounts, (L + 1) * 64 * 4))) return rc;
+        if ((rc = h->alloc((void**)&h->pbstatus, 16))) return rc;
     } else {
         if ((rc = h->alloc((void**)&h->rbs, h->rb_off[L + 1]))) return rc;
         if ((rc = h->alloc((void**)&h->chunk_words, maxch * B * 4))) return rc;
@@ -781,7 +882,10 @@ int mdr_refactor(prodm_mdr* h, const T* field, cudaStream_t st) {
         uint8_t* out = h->streams + h->lvl_byte_off[l];
         double* errs = h->sq ? h->sqerr + (uint64_t)l * (B + 1) : nullptr;
         Stage sg(h, 1, l, st);
-        if (h->nb) {
+        if (h->pb) {
+            rc = launch_pb_encode<T>(coef + g.offset[l], n, keys + l, 0, B, (uint32_t*)out, h->plane_cap[l],
+                                     h->pbcounts + l * 64, h->sizes + (uint64_t)l * B, st);
+        } else if (h->nb) {
             rc = launch_nb_encode<T>(coef + g.offset[l], n, keys + l, 0, B, out, h->plane_cap[l], h->partial, errs, st);
         } else {
             rc = launch_gr_encode<T>(coef + g.offset[l], n, keys + l, 0, B, h->rbs + h->rb_off[l], h->chunk_words,
@@ -812,7 +916,11 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         if ((fuse && l == L) || (h->dseg && sizeof(T) == 4)) continue;
         const uint64_t n = g.elems[l];
         Stage sg(h, 3, l, st);
-        if (h->nb) {
+        if (h->pb) {
+            const uint32_t* rows = (const uint32_t*)(h->streams + h->lvl_byte_off[l]);
+            rc = launch_pb_decode<T>(rows, h->plane_cap[l], n, keys + l, 0, B, 0, 0, h->index + l,
+                                     rows + (uint64_t)B * h->plane_cap[l], nullptr, rcoef + h->roff[l], st);
+        } else if (h->nb) {
             rc = launch_nb_decode<T>(h->streams + h->lvl_byte_off[l], h->plane_cap[l], n, keys + l, 0, 0, 0,
                                      h->index + l, rcoef + h->roff[l], st);
         } else {
@@ -872,12 +980,67 @@ int mdr_interpret(prodm_mdr* h, double tol, int interp, int est, double s, cudaS
 
 // grouped levels loaded from files: header -> rb + chunk offsets, then the
 // planes completely inside the loaded prefix -> aligned layout
+// per-bit levels loaded from files: parse the planes that lie completely
+// inside the loaded prefix and are not parsed yet into the level's rows
+int pb_parse_loaded(prodm_mdr* h, int l, cudaStream_t st) {
+    const int B = h->B;
+    const uint64_t n = h->g.elems[l], rw = h->plane_cap[l];
+    uint32_t* rows = (uint32_t*)(h->streams + h->lvl_byte_off[l]);
+    int rc;
+    if (!h->header_done[l]) {
+        if ((rc = launch_pb_init_unseen(rows + (uint64_t)(B + 1) * rw, rows + (uint64_t)B * rw, n, st))) return rc;
+        h->header_done[l] = 1;
+    }
+    uint64_t off = 0;
+    int complete = 0;
+    for (int p = 0; p < B; p++) {
+        off += h->hsizes[l * B + p];
+        if (off <= h->loaded[l]) complete = p + 1;
+        else break;
+    }
+    const int first = (int)h->unpacked[l];
+    if (complete <= first) return PRODM_OK;
+    const int num = complete - first;
+    std::vector<uint64_t> hv(2 * num);
+    uint64_t o = 0;
+    for (int p = 0; p < first; p++) o += h->hsizes[l * B + p];
+    for (int i = 0; i < num; i++) {
+        const uint64_t sz = h->hsizes[l * B + first + i];
+        if (sz == 0 || sz % 8) return fail(PRODM_ECORRUPT, "load: per-bit stream size not a positive multiple of 8");
+        hv[i] = (uint64_t)(uintptr_t)(h->lfile[l] + o);
+        hv[num + i] = sz / 8;
+        o += sz;
+    }
+    uint64_t* dv;
+    PRODM_CUDA(cudaMallocAsync((void**)&dv, hv.size() * 8, st));
+    PRODM_CUDA(cudaMemcpyAsync(dv, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st));
+    PRODM_CUDA(cudaMemsetAsync(h->pbstatus, 0, 4, st));
+    rc = launch_pb_parse((const uint64_t* const*)dv, dv + num, first, num, n, rows, rw, rows + (uint64_t)(B + 1) * rw,
+                         rows + (uint64_t)B * rw, h->pbstatus, st);
+    int hstat = 0;
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(&hstat, h->pbstatus, 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_status(e, "per-bit load");
+    }
+    cudaFreeAsync(dv, st);
+    if (rc) return rc;
+    if (hstat == PRODM_ETIMEOUT) return fail(PRODM_ETIMEOUT, "load: the per-bit parse pipeline stalled");
+    if (hstat) return fail(PRODM_ECORRUPT, "load: a per-bit stream does not end where its size says");
+    h->unpacked[l] = complete;
+    return PRODM_OK;
+}
+
 int mdr_unpack_loaded(prodm_mdr* h, cudaStream_t st) {
     const int L = h->g.L, B = h->B;
     const int wb = (int)h->es;
     int rc;
     for (int l = 0; l <= L; l++) {
         if (!h->lfile[l]) continue;
+        if (h->pb) {
+            if ((rc = pb_parse_loaded(h, l, st))) return rc;
+            continue;
+        }
         const uint64_t nbk = h->nblocks[l];
         const uint64_t hdr = 4 + nbk;
         if (!h->header_done[l]) {
@@ -1195,7 +1358,8 @@ int prodm_encode(int enc, int dtype, const void* d, uint64_t n, int exp, int B, 
                  uint32_t* sizes, double* errs, void* ws, size_t wsb, void* stream) {
     int rc = check_dtype(dtype);
     if (rc) return rc;
-    if (enc != PRODM_ENC_NEGABINARY && enc != PRODM_ENC_GROUPED) return fail(PRODM_EINVAL, "unknown encoder");
+    if (enc != PRODM_ENC_NEGABINARY && enc != PRODM_ENC_GROUPED && enc != PRODM_ENC_PERBIT)
+        return fail(PRODM_EINVAL, "unknown encoder");
     if (!d || !blob || !sizes) return fail(PRODM_EINVAL, "prodm_encode: NULL pointer");
     if (dtype == PRODM_F64)
         return encode_impl<double>(enc, (const double*)d, n, exp, B, (uint8_t*)blob, cap, sizes, errs, ws, wsb,
@@ -1208,7 +1372,8 @@ int prodm_decoder_create(prodm_decoder** out, int enc, int dtype) {
     int rc = check_dtype(dtype);
     if (rc) return rc;
     if (!out) return fail(PRODM_EINVAL, "NULL output");
-    if (enc != PRODM_ENC_NEGABINARY && enc != PRODM_ENC_GROUPED) return fail(PRODM_EINVAL, "unknown encoder");
+    if (enc != PRODM_ENC_NEGABINARY && enc != PRODM_ENC_GROUPED && enc != PRODM_ENC_PERBIT)
+        return fail(PRODM_EINVAL, "unknown encoder");
     prodm_decoder* h = new prodm_decoder();
     h->enc = enc;
     h->dtype = dtype;
@@ -1332,7 +1497,12 @@ int prodm_mdr_create(prodm_mdr** out, const prodm_config* cfg) {
     if (!out || !cfg) return fail(PRODM_EINVAL, "prodm_mdr_create: NULL pointer");
     int rc = check_dtype(cfg->dtype);
     if (rc) return rc;
-    if (cfg->encoder != PRODM_ENC_NEGABINARY && cfg->encoder != PRODM_ENC_GROUPED) return fail(PRODM_EINVAL, "unknown encoder");
+    if (cfg->encoder != PRODM_ENC_NEGABINARY && cfg->encoder != PRODM_ENC_GROUPED && cfg->encoder != PRODM_ENC_PERBIT)
+        return fail(PRODM_EINVAL, "unknown encoder");
+    // the per-bit encoder's error-collecting overload shifts 32-bit integers by
+    // up to B-1 bits (PerBitBPEncoder.hpp:388-397); its drivers use the max collector
+    if (cfg->encoder == PRODM_ENC_PERBIT && cfg->collector == PRODM_COLLECT_SQUARED)
+        return fail(PRODM_EUNSUPPORTED, "the per-bit encoder is used with PRODM_COLLECT_MAX");
     if (cfg->basis != PRODM_BASIS_HIERARCHICAL && cfg->basis != PRODM_BASIS_ORTHOGONAL) return fail(PRODM_EINVAL, "unknown basis");
     if ((rc = check_bitplanes(cfg->dtype, cfg->encoder, cfg->num_bitplanes))) return rc;
     if (cfg->ndims < 1 || cfg->ndims > 3) return fail(PRODM_EINVAL, "ndims must be 1, 2 or 3");
@@ -1345,6 +1515,7 @@ int prodm_mdr_create(prodm_mdr** out, const prodm_config* cfg) {
     h->B = cfg->num_bitplanes;
     h->es = esize(cfg->dtype);
     h->nb = cfg->encoder == PRODM_ENC_NEGABINARY;
+    h->pb = cfg->encoder == PRODM_ENC_PERBIT;
     h->orth = cfg->basis == PRODM_BASIS_ORTHOGONAL;
     h->sq = cfg->collector == PRODM_COLLECT_SQUARED;
     if ((rc = mdr_alloc_all(h))) { delete h; return rc; }
@@ -1429,6 +1600,26 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
         const size_t row = (size_t)h->nblocks[level] * h->es;
         PRODM_CUDA(cudaMemcpy2DAsync(dst, row, src, (size_t)h->plane_cap[level] * h->es, row, B,
                                      dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+        PRODM_CUDA(cudaStreamSynchronize(st));
+        return PRODM_OK;
+    }
+    if (h->pb) {   // rows -> reference streams (8-byte aligned staging where dst is not)
+        const bool direct = !dst_is_host && (uintptr_t)dst % 8 == 0;
+        const uint64_t n = h->g.elems[level];
+        const size_t scr = pb_pack_scratch_bytes(n, B);
+        uint8_t* tmp;
+        PRODM_CUDA(cudaMallocAsync((void**)&tmp, scr + (direct ? 0 : (total + 255) / 256 * 256), st));
+        uint8_t* out = direct ? (uint8_t*)dst : tmp + scr;
+        const uint32_t* rows = (const uint32_t*)src;
+        int rc = launch_pb_pack(rows, h->plane_cap[level], n, B, h->sizes + (uint64_t)level * B, total,
+                                out, tmp, st);
+        if (!rc && !direct) {
+            const cudaError_t e = cudaMemcpyAsync(dst, out, total,
+                                                  dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) rc = cuda_status(e, "export copy");
+        }
+        cudaFreeAsync(tmp, st);
+        if (rc) return rc;
         PRODM_CUDA(cudaStreamSynchronize(st));
         return PRODM_OK;
     }

@@ -97,6 +97,23 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* 
                                  const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
                                  cudaStream_t st);
 
+// perbit.cu: per-bit format; rows of 32-element group words (magnitude
+// planes 0..B-1, sign row B, unseen row B+1), each row `stride` words
+uint64_t pb_groups(uint64_t n);
+uint64_t pb_row_words(uint64_t n);
+template <class T>
+int launch_pb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, uint32_t* rows, uint64_t stride,
+                     uint32_t* counts, uint32_t* sizes, cudaStream_t st);
+template <class T>
+int launch_pb_decode(const uint32_t* rows, uint64_t stride, uint64_t n, const void* maxkey, int exp, int B, int s, int e,
+                     const uint8_t* dnum, const uint32_t* srow, const uint32_t* unseen, T* out, cudaStream_t st);
+size_t pb_pack_scratch_bytes(uint64_t n, int B);
+int launch_pb_pack(const uint32_t* rows, uint64_t stride, uint64_t n, int B, const uint32_t* sizes, uint64_t total,
+                   uint8_t* dst, void* scratch, cudaStream_t st);
+int launch_pb_init_unseen(uint32_t* unseen, uint32_t* signs, uint64_t n, cudaStream_t st);
+int launch_pb_parse(const uint64_t* const* planes, const uint64_t* nwords, int a, int np, uint64_t n, uint32_t* rows,
+                    uint64_t stride, uint32_t* unseen, uint32_t* signs, int* status, cudaStream_t st);
+
 // pack.cu
 int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,
                    int word_bytes, uint8_t* dst, cudaStream_t st);

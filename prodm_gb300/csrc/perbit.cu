@@ -1,0 +1,519 @@
+// Per-bit bitplane format on the device (sm_103a): PerBitBPEncoder
+// (PerBitBPEncoder.hpp:7-146 encode, :290-383 progressive_decode).
+//
+// Reference stream format: one bit stream per plane, bits packed from the
+// least significant end of 64-bit words. Element i writes, in plane p, bit
+// (B-1-p) of its fixed-point magnitude and, right after its first 1 bit, its
+// sign. Where a bit of plane p sits therefore depends on how many earlier
+// elements had their first 1 bit in plane p: a stream can only be parsed with
+// the planes before it.
+//
+// Device layout ("rows"): the level's elements in groups of 32; row p (p < B)
+// holds one 32-bit word per group whose bit j is bit (B-1-p) of element
+// 32g+j's magnitude; row B holds the sign words (bit j set: element negative
+// and nonzero); row B+1 (parsed streams only) the elements that have no 1 bit
+// in the planes parsed so far. Every row starts on a 16-byte boundary. In this
+// layout decoding is a transpose per group and needs no parse; the reference
+// stream sizes (ceil((n + first-ones in p) / 64) * 8 bytes) are computed at
+// encode time, and pb_pack writes the reference streams on export.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "nbcodec.cuh"
+
+namespace prodm {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int PB_WARPS = 8;
+constexpr int PB_GPW = 16;                        // groups per warp per chunk
+constexpr int PB_CHUNK = PB_WARPS * PB_GPW;       // groups per CTA chunk
+constexpr int PB_LD = PB_CHUNK + 1;               // padded tile row
+
+template <class T>
+__device__ __forceinline__ int pb_exp(const typename KeyOf<T>::type* maxkey, int exp_arg) {
+    return maxkey ? frexp_exp(key_to_val(*maxkey, T())) : exp_arg;
+}
+
+// fixed-point magnitude of one value (PerBitBPEncoder.hpp:100-104)
+template <class T>
+__device__ __forceinline__ typename Traits<T>::FP pb_mag(T v, int B, int exp) {
+    const T shifted = ldexp_t(v, B - exp);
+    const int64_t fx = (int64_t)shifted;
+    return (typename Traits<T>::FP)(v < 0 ? -fx : fx);
+}
+
+__device__ __forceinline__ uint32_t valid_mask(int nvalid) { return nvalid >= 32 ? FULL : ((1u << nvalid) - 1u); }
+
+// ---------------------------------------------------------------------------
+// encode: values -> rows 0..B (magnitude planes + signs) and, per plane, the
+// number of elements whose first 1 bit is in that plane
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_pb_encode(const T* __restrict__ x, uint64_t n,
+                                                   const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg,
+                                                   int B, uint32_t* __restrict__ rows, uint64_t stride,
+                                                   uint32_t* __restrict__ counts) {
+    using FP = typename Traits<T>::FP;
+    extern __shared__ uint32_t tile[];   // (B + 1) rows x PB_LD
+    __shared__ uint32_t cnt[64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int exp = pb_exp<T>(maxkey, exp_arg);
+    const uint64_t ng = (n + 31) / 32;
+    const uint64_t nch = (ng + PB_CHUNK - 1) / PB_CHUNK;
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    uint32_t c_lo = 0, c_hi = 0;   // first-one counts of bit `lane` and bit 32 + lane
+    for (uint64_t c = blockIdx.x; c < nch; c += gridDim.x) {
+        const uint64_t g0 = c * PB_CHUNK;
+#pragma unroll 2
+        for (int j = 0; j < PB_GPW; j++) {
+            const int gl = warp * PB_GPW + j;
+            const uint64_t i = (g0 + gl) * 32 + lane;
+            const T v = i < n ? __ldcs(x + i) : (T)0;
+            const FP m = pb_mag(v, B, exp);
+            const uint32_t sgn = __ballot_sync(FULL, v < 0 && m != 0);
+            const uint32_t lo = transpose32((uint32_t)m, lane);          // lane k: bit k of the 32 magnitudes
+            const uint32_t hi = sizeof(T) == 8 ? transpose32((uint32_t)((uint64_t)m >> 32), lane) : 0u;
+            // OR of the words of all higher bits: first 1 bits = word & ~that
+            uint32_t s_lo = lo, s_hi = hi;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t t1 = __shfl_down_sync(FULL, s_lo, d);
+                const uint32_t t2 = __shfl_down_sync(FULL, s_hi, d);
+                if (lane + d < 32) { s_lo |= t1; s_hi |= t2; }
+            }
+            uint32_t ex_lo = __shfl_down_sync(FULL, s_lo, 1), ex_hi = __shfl_down_sync(FULL, s_hi, 1);
+            if (lane == 31) { ex_lo = 0; ex_hi = 0; }
+            ex_lo |= __shfl_sync(FULL, s_hi, 0);
+            c_lo += __popc(lo & ~ex_lo);
+            c_hi += __popc(hi & ~ex_hi);
+            if (lane < B) tile[(B - 1 - lane) * PB_LD + gl] = lo;
+            if (sizeof(T) == 8 && lane + 32 < B) tile[(B - 33 - lane) * PB_LD + gl] = hi;
+            if (lane == 0) tile[B * PB_LD + gl] = sgn;
+        }
+        __syncthreads();
+        const int nvalid = (int)((ng - g0) < (uint64_t)PB_CHUNK ? (ng - g0) : PB_CHUNK);
+        for (int p = warp; p <= B; p += PB_WARPS) {
+            uint32_t* dst = rows + (uint64_t)p * stride + g0;
+            const uint32_t* src = tile + p * PB_LD;
+            for (int j = lane; j < nvalid; j += 32) dst[j] = src[j];
+        }
+        __syncthreads();
+    }
+    if (lane < B && c_lo) atomicAdd(&cnt[B - 1 - lane], c_lo);
+    if (sizeof(T) == 8 && lane + 32 < B && c_hi) atomicAdd(&cnt[B - 33 - lane], c_hi);
+    __syncthreads();
+    for (int p = threadIdx.x; p < B; p += blockDim.x)
+        if (cnt[p]) atomicAdd(&counts[p], cnt[p]);
+}
+
+// reference stream sizes: BitEncoder words (n + first-one count bits) * 8
+__global__ void k_pb_sizes(const uint32_t* __restrict__ counts, int B, uint64_t n, uint32_t* __restrict__ sizes) {
+    const int p = threadIdx.x;
+    if (p < B) sizes[p] = (uint32_t)((n + counts[p] + 63) / 64 * 8);
+}
+
+// ---------------------------------------------------------------------------
+// decode planes [s, e): value = 2^(exp-e) * (magnitude bits of planes s..e-1),
+// negative where the element's sign is known by plane e (progressive_decode
+// :315-344: a sign is read with the first 1 bit) and its sign bit is set.
+// `unseen` (row of elements without a 1 bit in planes < e) may be NULL when
+// s == 0: then "known" is "nonzero". dnum (device plane count) overrides e.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_pb_decode(const uint32_t* __restrict__ rows, uint64_t stride, uint64_t n,
+                                                   const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg,
+                                                   int s, int e, const uint8_t* __restrict__ dnum,
+                                                   const uint32_t* __restrict__ srow,
+                                                   const uint32_t* __restrict__ unseen, T* __restrict__ out) {
+    using FP = typename Traits<T>::FP;
+    extern __shared__ uint32_t tile[];   // num + 2 rows x PB_LD
+    if (dnum) e = dnum[0];
+    const int num = e - s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int exp = pb_exp<T>(maxkey, exp_arg);
+    const uint64_t ng = (n + 31) / 32;
+    const uint64_t nch = (ng + PB_CHUNK - 1) / PB_CHUNK;
+    const int extra = unseen ? 2 : 1;
+    for (uint64_t c = blockIdx.x; c < nch; c += gridDim.x) {
+        const uint64_t g0 = c * PB_CHUNK;
+        const int nvalid = (int)((ng - g0) < (uint64_t)PB_CHUNK ? (ng - g0) : PB_CHUNK);
+        for (int r = warp; r < num + extra; r += PB_WARPS) {
+            const uint32_t* src = r < num ? rows + (uint64_t)(s + r) * stride + g0
+                                          : (r == num ? srow + g0 : unseen + g0);
+            uint32_t* dst = tile + r * PB_LD;
+            for (int j = lane; j < nvalid; j += 32) dst[j] = __ldcs(src + j);
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int j = 0; j < PB_GPW; j++) {
+            const int gl = warp * PB_GPW + j;
+            if (gl >= nvalid) break;
+            const uint32_t wl = lane < num ? tile[(num - 1 - lane) * PB_LD + gl] : 0u;
+            FP acc = transpose32(wl, lane);
+            if (sizeof(T) == 8 && num > 32) {
+                const uint32_t wh = lane + 32 < num ? tile[(num - 33 - lane) * PB_LD + gl] : 0u;
+                acc |= (FP)((uint64_t)transpose32(wh, lane) << 32);
+            }
+            const uint32_t sg = tile[num * PB_LD + gl];
+            const bool known = unseen ? !((tile[(num + 1) * PB_LD + gl] >> lane) & 1u) : acc != 0;
+            const T v = ldexp_t((T)acc, exp - e);
+            const uint64_t i = (g0 + gl) * 32 + lane;
+            if (i < n) out[i] = (known && ((sg >> lane) & 1u)) ? -v : v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// export: rows -> reference streams (BitEncoder layout), three passes
+//   count: bits of every (plane, 256-group chunk)
+//   scan:  chunk bit offsets within each plane
+//   write: each group's segment of each plane (<= 64 bits) OR-ed into the
+//          zeroed destination
+// ---------------------------------------------------------------------------
+constexpr int PK_T = 256;   // groups (threads) per chunk
+
+__device__ __forceinline__ int pk_nvalid(uint64_t g, uint64_t ng, uint64_t n) {
+    if (g >= ng) return 0;
+    const uint64_t r = n - g * 32;
+    return r < 32 ? (int)r : 32;
+}
+
+__global__ void __launch_bounds__(PK_T) k_pb_pack_count(const uint32_t* __restrict__ rows, uint64_t stride, uint64_t n,
+                                                        int B, uint32_t* __restrict__ chunk_bits, uint64_t nch) {
+    __shared__ uint32_t red[64];
+    const int lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < 64; k += blockDim.x) red[k] = 0;
+    __syncthreads();
+    const uint64_t ng = (n + 31) / 32;
+    const uint64_t g = (uint64_t)blockIdx.x * PK_T + threadIdx.x;
+    const int nvalid = pk_nvalid(g, ng, n);
+    const uint32_t vm = valid_mask(nvalid);
+    uint32_t seen = 0;
+    for (int p = 0; p < B; p++) {
+        const uint32_t M = nvalid ? rows[(uint64_t)p * stride + g] & vm : 0u;
+        const uint32_t F = M & ~seen;
+        seen |= M;
+        uint32_t bits = nvalid + __popc(F);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) bits += __shfl_xor_sync(FULL, bits, o);
+        if (lane == 0 && bits) atomicAdd(&red[p], bits);
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < B; p += blockDim.x) chunk_bits[(uint64_t)p * nch + blockIdx.x] = red[p];
+}
+
+__global__ void k_pb_pack_scan(const uint32_t* __restrict__ chunk_bits, uint64_t nch, uint64_t* __restrict__ chunk_off) {
+    const int lane = threadIdx.x;
+    const uint64_t base = (uint64_t)blockIdx.x * nch;
+    uint64_t run = 0;
+    for (uint64_t c0 = 0; c0 < nch; c0 += 32) {
+        const uint64_t c = c0 + lane;
+        const uint64_t v = c < nch ? chunk_bits[base + c] : 0;
+        uint64_t inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t t = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (c < nch) chunk_off[base + c] = run + inc - v;
+        run += __shfl_sync(FULL, inc, 31);
+    }
+}
+
+// segment of one group in one plane: magnitude bit of each element, with the
+// sign bit inserted after each element whose first 1 bit is in the plane
+__device__ __forceinline__ uint64_t pb_segment(uint32_t M, uint32_t F, uint32_t S) {
+    uint64_t seg = M;
+    uint32_t f = F;
+    while (f) {   // highest first: the positions below stay in place
+        const int j = 31 - __clz(f);
+        f &= ~(1u << j);
+        const uint64_t low = seg & ((2ull << j) - 1ull);
+        const uint64_t high = seg >> (j + 1);
+        seg = low | ((uint64_t)((S >> j) & 1u) << (j + 1)) | (high << (j + 2));
+    }
+    return seg;
+}
+
+__global__ void __launch_bounds__(PK_T) k_pb_pack_write(const uint32_t* __restrict__ rows, uint64_t stride, uint64_t n,
+                                                        int B, const uint32_t* __restrict__ srow,
+                                                        const uint64_t* __restrict__ chunk_off, uint64_t nch,
+                                                        const uint32_t* __restrict__ sizes,
+                                                        unsigned long long* __restrict__ dst) {
+    __shared__ uint64_t base[64];
+    __shared__ uint32_t wsum[PK_T / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        uint64_t a = 0;
+        for (int p = 0; p < B; p++) { base[p] = a * 8; a += sizes[p]; }
+    }
+    __syncthreads();
+    const uint64_t ng = (n + 31) / 32;
+    const uint64_t g = (uint64_t)blockIdx.x * PK_T + threadIdx.x;
+    const int nvalid = pk_nvalid(g, ng, n);
+    const uint32_t vm = valid_mask(nvalid);
+    const uint32_t S = nvalid ? srow[g] : 0u;
+    uint32_t seen = 0;
+    for (int p = 0; p < B; p++) {
+        const uint32_t M = nvalid ? rows[(uint64_t)p * stride + g] & vm : 0u;
+        const uint32_t F = M & ~seen;
+        seen |= M;
+        const uint32_t len = nvalid + __popc(F);
+        uint32_t inc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t woff = 0;
+        for (int w = 0; w < warp; w++) woff += wsum[w];
+        __syncthreads();
+        if (len) {
+            const uint64_t seg = pb_segment(M, F, S);
+            const uint64_t off = base[p] + chunk_off[(uint64_t)p * nch + blockIdx.x] + woff + inc - len;
+            const uint64_t w = off >> 6;
+            const int sh = (int)(off & 63);
+            atomicOr(dst + w, (unsigned long long)(seg << sh));
+            if (sh && sh + (int)len > 64) atomicOr(dst + w + 1, (unsigned long long)(seg >> (64 - sh)));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// parse: reference streams of planes [a, a+np) -> rows a..a+np-1, with the
+// unseen / sign rows carried from the planes before a and updated.
+//
+// One CTA per level. Warp w parses planes a+2w and a+2w+1; the chain over
+// planes is a software pipeline over chunks of PZ_G groups: warp w receives
+// each chunk's unseen / sign masks from warp w-1 through a shared-memory ring
+// and hands them on after its two planes. Within a plane, each group's bit
+// positions follow from the fixed point of
+//     q_j = j + #{k < j : k unseen and its bit (read at q_k) is 1},
+// iterated from q_j = j; every round settles at least one more element with a
+// sign bit, so at most 33 rounds are needed. Every wait is bounded: past the
+// limit the warp records PRODM_ETIMEOUT in *status and returns.
+// ---------------------------------------------------------------------------
+constexpr int PZ_G = 16;            // groups per chunk
+constexpr int PZ_R = 4;             // ring depth (chunks)
+constexpr long long kPzSpin = 1ll << 26;
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+    const uint32_t lo = __shfl_sync(FULL, (uint32_t)v, src);
+    const uint32_t hi = __shfl_sync(FULL, (uint32_t)(v >> 32), src);
+    return ((uint64_t)hi << 32) | lo;
+}
+
+struct PlaneReader {
+    const uint64_t* w;
+    uint64_t nw;
+    uint64_t pos;    // bit position in the stream
+    uint64_t pb;     // word index held by lane 0 of buf
+    uint64_t buf;    // lane i: word pb + i
+    uint64_t nxt;    // prefetch: lane i: word npb + i
+    uint64_t npb;
+    __device__ __forceinline__ uint64_t load(uint64_t k) const { return k < nw ? __ldcs(w + k) : 0ull; }
+};
+
+// one chunk of one plane; lane j (< PZ_G) holds group j's unseen / sign masks
+__device__ __forceinline__ void pz_chunk(PlaneReader& r, bool first, uint64_t g0, uint64_t ng, uint64_t n,
+                                         uint32_t& U, uint32_t& S, uint32_t* __restrict__ row, int lane) {
+    // the chunk reads words [pos/64, pos/64 + 16]; keep them in buf and
+    // prefetch the next chunk's (which starts 8..16 words further on)
+    const uint64_t wb = r.pos >> 6;
+    if (first) {
+        r.pb = wb;
+        r.buf = r.load(wb + lane);
+    } else {
+        r.pb = r.npb;
+        r.buf = r.nxt;
+    }
+    r.npb = wb + 8;
+    r.nxt = r.load(r.npb + lane);
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t Mkeep = 0;
+    for (int j = 0; j < PZ_G; j++) {
+        const uint64_t g = g0 + j;
+        if (g >= ng) break;
+        const int nvalid = pk_nvalid(g, ng, n);
+        const uint32_t Uj = __shfl_sync(FULL, U, j), Sj = __shfl_sync(FULL, S, j);
+        const int wi = (int)((r.pos >> 6) - r.pb);
+        const uint64_t w0 = shfl64(r.buf, wi), w1 = shfl64(r.buf, wi + 1);
+        const int sh = (int)(r.pos & 63);
+        const uint64_t W = sh ? (w0 >> sh) | (w1 << (64 - sh)) : w0;
+        const bool u = lane < nvalid && ((Uj >> lane) & 1u);
+        int q = lane;
+        uint32_t f = 0, b = 0;
+        for (int it = 0; it < 34; it++) {
+            b = (uint32_t)(W >> q) & 1u;
+            f = __ballot_sync(FULL, u && b);
+            const int qn = lane + __popc(f & lt);
+            if (__all_sync(FULL, qn == q)) break;
+            q = qn;
+        }
+        const uint32_t M = __ballot_sync(FULL, lane < nvalid && b);
+        const uint32_t SG = __ballot_sync(FULL, ((f >> lane) & 1u) && ((W >> (q + 1)) & 1ull));
+        r.pos += (uint64_t)(nvalid + __popc(f));
+        if (lane == j) {
+            U = Uj & ~M;
+            S = Sj | SG;
+            Mkeep = M;
+        }
+    }
+    if (lane < PZ_G && g0 + lane < ng) row[g0 + lane] = Mkeep;
+}
+
+__global__ void __launch_bounds__(1024, 1) k_pb_parse(const uint64_t* const* __restrict__ planes,
+                                                      const uint64_t* __restrict__ nwords, int a, int np, uint64_t n,
+                                                      uint32_t* __restrict__ rows, uint64_t stride,
+                                                      uint32_t* __restrict__ unseen, uint32_t* __restrict__ signs,
+                                                      int* __restrict__ status) {
+    __shared__ uint32_t ring[32][PZ_R][2][PZ_G];
+    __shared__ int produced[32], consumed[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 32) { produced[threadIdx.x] = 0; consumed[threadIdx.x] = 0; }
+    __syncthreads();
+    const int active = (np + 1) / 2;
+    if (warp >= active) return;
+    volatile int* vprod = produced;
+    volatile int* vcons = consumed;
+    const int i0 = 2 * warp, i1 = 2 * warp + 1;
+    const bool two = i1 < np, last = warp == active - 1;
+    const uint64_t ng = (n + 31) / 32, nch = (ng + PZ_G - 1) / PZ_G;
+    PlaneReader r0{planes[i0], nwords[i0], 0, 0, 0, 0, 0};
+    PlaneReader r1{two ? planes[i1] : nullptr, two ? nwords[i1] : 0, 0, 0, 0, 0, 0};
+    uint32_t* row0 = rows + (uint64_t)(a + i0) * stride;
+    uint32_t* row1 = rows + (uint64_t)(a + (two ? i1 : i0)) * stride;
+    for (uint64_t c = 0; c < nch; c++) {
+        const uint64_t g0 = c * PZ_G;
+        const int slot = (int)(c % PZ_R);
+        uint32_t U = 0, S = 0;
+        if (warp == 0) {
+            if (lane < PZ_G && g0 + lane < ng) { U = unseen[g0 + lane]; S = signs[g0 + lane]; }
+        } else {
+            long long spins = 0;
+            while (vprod[warp - 1] <= (int)c) {
+                if (++spins > kPzSpin) { if (lane == 0) atomicExch(status, PRODM_ETIMEOUT); return; }
+                __nanosleep(64);
+            }
+            __threadfence_block();
+            if (lane < PZ_G) { U = ring[warp - 1][slot][0][lane]; S = ring[warp - 1][slot][1][lane]; }
+            __syncwarp();
+            if (lane == 0) { __threadfence_block(); vcons[warp - 1] = (int)c + 1; }
+        }
+        pz_chunk(r0, c == 0, g0, ng, n, U, S, row0, lane);
+        if (two) pz_chunk(r1, c == 0, g0, ng, n, U, S, row1, lane);
+        if (last) {
+            if (lane < PZ_G && g0 + lane < ng) { unseen[g0 + lane] = U; signs[g0 + lane] = S; }
+        } else {
+            long long spins = 0;
+            while ((int)c - vcons[warp] >= PZ_R) {
+                if (++spins > kPzSpin) { if (lane == 0) atomicExch(status, PRODM_ETIMEOUT); return; }
+                __nanosleep(64);
+            }
+            if (lane < PZ_G) { ring[warp][slot][0][lane] = U; ring[warp][slot][1][lane] = S; }
+            __threadfence_block();
+            __syncwarp();
+            if (lane == 0) vprod[warp] = (int)c + 1;
+        }
+    }
+    // a well-formed stream ends in its last word
+    if (lane == 0) {
+        if ((r0.pos + 63) / 64 != r0.nw) atomicCAS(status, 0, PRODM_ECORRUPT);
+        if (two && (r1.pos + 63) / 64 != r1.nw) atomicCAS(status, 0, PRODM_ECORRUPT);
+    }
+}
+
+// unseen row of a fresh level: every element present
+__global__ void k_pb_init_unseen(uint32_t* __restrict__ unseen, uint32_t* __restrict__ signs, uint64_t n) {
+    const uint64_t ng = (n + 31) / 32;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += (uint64_t)gridDim.x * blockDim.x) {
+        unseen[g] = valid_mask(pk_nvalid(g, ng, n));
+        signs[g] = 0;
+    }
+}
+
+}  // namespace
+
+uint64_t pb_groups(uint64_t n) { return (n + 31) / 32; }
+uint64_t pb_row_words(uint64_t n) { return (pb_groups(n) + 3) / 4 * 4; }
+
+template <class T>
+int launch_pb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B, uint32_t* rows, uint64_t stride,
+                     uint32_t* counts, uint32_t* sizes, cudaStream_t st) {
+    if (B < 1 || B > (sizeof(T) == 8 ? 63 : 32)) return fail(PRODM_EINVAL, "perbit: num_bitplanes out of range");
+    PRODM_CUDA(cudaMemsetAsync(counts, 0, B * sizeof(uint32_t), st));
+    const uint64_t nch = (pb_groups(n) + PB_CHUNK - 1) / PB_CHUNK;
+    const size_t smem = (size_t)(B + 1) * PB_LD * 4;
+    const unsigned grid = persistent_grid_for((const void*)k_pb_encode<T>, 256, smem, nch, 1u << 20);
+    k_pb_encode<T><<<grid, 256, smem, st>>>(x, n, (const typename KeyOf<T>::type*)maxkey, exp, B, rows, stride, counts);
+    PRODM_CHECK_LAUNCH("k_pb_encode");
+    k_pb_sizes<<<1, 64, 0, st>>>(counts, B, n, sizes);
+    PRODM_CHECK_LAUNCH("k_pb_sizes");
+    return PRODM_OK;
+}
+
+template <class T>
+int launch_pb_decode(const uint32_t* rows, uint64_t stride, uint64_t n, const void* maxkey, int exp, int B, int s, int e,
+                     const uint8_t* dnum, const uint32_t* srow, const uint32_t* unseen, T* out, cudaStream_t st) {
+    const int maxnum = dnum ? B : e - s;
+    const size_t smem = (size_t)(maxnum + 2) * PB_LD * 4;
+    const uint64_t nch = (pb_groups(n) + PB_CHUNK - 1) / PB_CHUNK;
+    const unsigned grid = persistent_grid_for((const void*)k_pb_decode<T>, 256, smem, nch, 1u << 20);
+    k_pb_decode<T><<<grid, 256, smem, st>>>(rows, stride, n, (const typename KeyOf<T>::type*)maxkey, exp, s, e, dnum,
+                                            srow, unseen, out);
+    PRODM_CHECK_LAUNCH("k_pb_decode");
+    return PRODM_OK;
+}
+
+size_t pb_pack_scratch_bytes(uint64_t n, int B) {
+    const uint64_t nch = (pb_groups(n) + PK_T - 1) / PK_T;
+    return ((size_t)B * nch * (4 + 8) + 511) / 256 * 256;   // a multiple of 256 bytes
+}
+
+int launch_pb_pack(const uint32_t* rows, uint64_t stride, uint64_t n, int B, const uint32_t* sizes, uint64_t total,
+                   uint8_t* dst, void* scratch, cudaStream_t st) {
+    if ((uintptr_t)dst % 8) return fail(PRODM_EINVAL, "perbit pack: destination must be 8-byte aligned");
+    const uint64_t nch = (pb_groups(n) + PK_T - 1) / PK_T;
+    uint64_t* chunk_off = (uint64_t*)scratch;
+    uint32_t* chunk_bits = (uint32_t*)(chunk_off + (uint64_t)B * nch);
+    PRODM_CUDA(cudaMemsetAsync(dst, 0, total, st));
+    if (nch == 0) return PRODM_OK;
+    k_pb_pack_count<<<(unsigned)nch, PK_T, 0, st>>>(rows, stride, n, B, chunk_bits, nch);
+    PRODM_CHECK_LAUNCH("k_pb_pack_count");
+    k_pb_pack_scan<<<B, 32, 0, st>>>(chunk_bits, nch, chunk_off);
+    PRODM_CHECK_LAUNCH("k_pb_pack_scan");
+    k_pb_pack_write<<<(unsigned)nch, PK_T, 0, st>>>(rows, stride, n, B, rows + (uint64_t)B * stride, chunk_off, nch,
+                                                    sizes, (unsigned long long*)dst);
+    PRODM_CHECK_LAUNCH("k_pb_pack_write");
+    return PRODM_OK;
+}
+
+int launch_pb_init_unseen(uint32_t* unseen, uint32_t* signs, uint64_t n, cudaStream_t st) {
+    k_pb_init_unseen<<<grid_for(pb_groups(n), 256), 256, 0, st>>>(unseen, signs, n);
+    PRODM_CHECK_LAUNCH("k_pb_init_unseen");
+    return PRODM_OK;
+}
+
+int launch_pb_parse(const uint64_t* const* planes, const uint64_t* nwords, int a, int np, uint64_t n, uint32_t* rows,
+                    uint64_t stride, uint32_t* unseen, uint32_t* signs, int* status, cudaStream_t st) {
+    if (np < 1 || np > 64) return fail(PRODM_EINVAL, "perbit parse: 1..64 planes per call");
+    k_pb_parse<<<1, 1024, 0, st>>>(planes, nwords, a, np, n, rows, stride, unseen, signs, status);
+    PRODM_CHECK_LAUNCH("k_pb_parse");
+    return PRODM_OK;
+}
+
+template int launch_pb_encode<float>(const float*, uint64_t, const void*, int, int, uint32_t*, uint64_t, uint32_t*,
+                                     uint32_t*, cudaStream_t);
+template int launch_pb_encode<double>(const double*, uint64_t, const void*, int, int, uint32_t*, uint64_t, uint32_t*,
+                                      uint32_t*, cudaStream_t);
+template int launch_pb_decode<float>(const uint32_t*, uint64_t, uint64_t, const void*, int, int, int, int,
+                                     const uint8_t*, const uint32_t*, const uint32_t*, float*, cudaStream_t);
+template int launch_pb_decode<double>(const uint32_t*, uint64_t, uint64_t, const void*, int, int, int, int,
+                                      const uint8_t*, const uint32_t*, const uint32_t*, double*, cudaStream_t);
+
+}  // namespace prodm
