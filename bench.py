@@ -58,6 +58,7 @@ def parse():
                     "are captured as external event nodes)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-field batched vs per-field-loop measurement")
     ap.add_argument("--no-qoi", action="store_true", help="skip the QoI-guided vs uniform-halving retrieval comparison")
+    ap.add_argument("--no-perbit", action="store_true", help="skip the fp64 per-bit encoder measurement")
     return ap.parse_args()
 
 
@@ -371,6 +372,7 @@ def run_ours(args):
 
     batched = run_batched() if (not args.no_batched and world == 1) else None
     qoi_res = run_qoi() if (not args.no_qoi and world == 1) else None
+    perbit = run_perbit() if (not args.no_perbit and world == 1) else None
 
     # end-to-end through the reference-facing flow with host buffers
     e2e = run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev) if args.e2e_steps > 0 else None
@@ -395,6 +397,7 @@ def run_ours(args):
             "e2e": e2e,
             "batched": batched,
             "qoi": qoi_res,
+            "perbit": perbit,
             "clocks": clocks,
         }
     if world > 1:
@@ -586,6 +589,129 @@ def run_qoi(n=257, levels=6, rels=(1e-2, 1e-3, 1e-4)):
                 "seconds": {"halving": t1 - t0, "guided": t2 - t1}})
             torch.cuda.empty_cache()
     return out
+
+
+def run_perbit(shape=(513, 513, 513), levels=7, planes=60, rels=(1e-3, 1e-5, 1e-7, 1e-9), steps=3):
+    """The GE applications' encoder (PerBitBPEncoder, fp64, 60 planes, max
+    collector, SignExclude interpreter with MaxErrorEstimatorHB) on a 513^3
+    fp64 shear layer: the refactor + retrieve step (bytes counted as for the
+    headline metric), the per-bit encode / decode kernels against the HBM
+    roofline (stage events), export of the reference streams, import of them
+    (the plane-by-plane parse), and the oracle's single-thread decode of one
+    level beside the device's parse + decode of the same level."""
+    import numpy as np
+    import torch
+    import oracle
+    from prodm_gb300 import api, fields
+
+    x = fields.shear_layer(shape, delta=0.05, noise_rel=1e-6, seed=21, dtype=torch.float64, device="cuda")
+    N = x.numel()
+    vr = float(x.max() - x.min())
+    m = api.MDRField(shape, torch.float64, levels, planes, "perbit", "hierarchical", "max")
+    out = torch.empty_like(x)
+
+    def step(record=None):
+        m.refactor(x)
+        m.reset()
+        for r in rels:
+            m.retrieve(r * vr, out=out, interpreter="sign_exclude", estimator="max_hb")
+            if record is not None:
+                record.append(m.index().astype(np.int64))
+
+    idxs = []
+    step(idxs)
+    torch.cuda.synchronize()
+    sizes, _, _ = m.level_info()
+    sizes = sizes.astype(np.int64)
+    stream_bytes = int(sizes.sum())
+    retrieved = [int(sum(sizes[l, :ix[l]].sum() for l in range(levels + 1))) for ix in idxs]
+    step_bytes = (N * 8 + stream_bytes) + sum(r + N * 8 for r in retrieved)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    err = float((out - x).abs().max())
+
+    # kernel stages (finest level): algorithmic bytes / event time
+    m.set_timing(True)
+    step()
+    torch.cuda.synchronize()
+    st = m.stage_times()
+    m.set_timing(False)
+    lel = api.level_dims(shape, levels)[1]
+    n_f = int(lel[levels])
+    peak, peak_src = measured_peak()
+    enc_ms = st[("encode", levels)][0]
+    enc_bytes = n_f * 8 + n_f * (planes + 1) // 8
+    dec_ms, dec_bytes = st[("decode", levels)][0], sum(n_f * (int(ix[levels]) + 1) // 8 + n_f * 8 for ix in idxs)
+
+    # export: rows -> reference streams on the host
+    t0 = time.time()
+    files = [m.export_level(l) for l in range(levels + 1)]
+    t_exp = time.time() - t0
+    meta = m.metadata()
+    # import: the reference streams loaded into a fresh handle, parsed plane by plane
+    m2 = api.MDRField(shape, torch.float64, levels, planes, "perbit", "hierarchical", "max")
+    m2.load_metadata(meta)
+    for l in range(levels + 1):
+        m2.load_level(l, files[l], 0)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    full = m2.retrieve_planes([planes] * (levels + 1))
+    torch.cuda.synchronize()
+    t_imp = time.time() - t0
+    same = bool(torch.equal(full, m.retrieve_planes([planes] * (levels + 1))))
+    m2.close()
+
+    # oracle (single thread) decode of level levels-1 against the device's
+    # parse + decode of the same streams through the progressive decoder
+    lv = levels - 1
+    n_l = int(lel[lv])
+    blob = files[lv]
+    _, b, _ = m.level_info()
+    e = math.frexp(float(b[lv]))[1]                 # the level exponent (ComposedRefactor.hpp:118-123)
+    dev = api.ProgressiveDecoder("perbit", torch.float64)
+    dblob = torch.from_numpy(blob).cuda()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    dout = dev.decode(dblob, sizes[lv].astype(np.uint32), n_l, e, 0, planes, lv, planes)
+    torch.cuda.synchronize()
+    t_dev = time.time() - t0
+    O = oracle.oracle()
+    stt = O.perbit_state(np.float64)
+    t0 = time.time()
+    cout = stt.decode(blob, sizes[lv].astype(np.uint32), n_l, e, 0, planes, lv)
+    t_cpu = time.time() - t0
+    dec_same = bool(np.array_equal(dout.cpu().numpy(), cout))
+    m.close()
+    del x, out, full
+    torch.cuda.empty_cache()
+    return {
+        "workload": "%s fp64 tanh shear layer + 1e-6 relative noise (seeded), %d levels, %d planes, PerBit encoder, "
+                    "max collector, SignExclude greedy interpreter + MaxErrorEstimatorHB, relative L-inf %s" %
+                    ("x".join(map(str, shape)), levels + 1, planes, list(rels)),
+        "step": {"ms": ms, "bytes": step_bytes, "gbs": step_bytes / ms / 1e6, "max_error_at_tightest": err,
+                 "tightest_bound": rels[-1] * vr, "planes_per_level": [ix.tolist() for ix in idxs]},
+        "encode_finest": {"ms": enc_ms, "bytes": enc_bytes, "gbs": enc_bytes / enc_ms / 1e6,
+                          "frac": enc_bytes / enc_ms / 1e6 / peak,
+                          "bytes_model": "n*8 read + n*(B+1)/8 rows written"},
+        "decode_finest": {"ms": dec_ms, "bytes": dec_bytes, "gbs": dec_bytes / dec_ms / 1e6,
+                          "frac": dec_bytes / dec_ms / 1e6 / peak,
+                          "bytes_model": "per retrieval n*(planes+1)/8 rows read + n*8 written"},
+        "peak": {"gbs": peak, "source": peak_src},
+        "export": {"stream_bytes": stream_bytes, "seconds": t_exp, "gbs": stream_bytes / t_exp / 1e9,
+                   "flow": "pack kernels + D2H into pageable host memory"},
+        "import": {"stream_bytes": stream_bytes, "seconds": t_imp, "gbs": stream_bytes / t_imp / 1e9,
+                   "identical_to_device_refactor": same,
+                   "flow": "all levels' reference streams resident; parse (one CTA per level, plane pipeline) + "
+                           "decode + recompose of all planes"},
+        "level_decode_vs_cpu": {"level": lv, "elements": n_l, "stream_bytes": int(sizes[lv].sum()),
+                                "device_seconds": t_dev, "cpu_oracle_seconds": t_cpu, "cores": 1,
+                                "identical": dec_same, "speedup": t_cpu / t_dev},
+    }
 
 
 def call_export(mdr, level, host_tensor):

@@ -29,10 +29,12 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstddef>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -295,6 +297,137 @@ class GpuBPEncoder PRODM_BASE(MDR::concepts::BitplaneEncoderInterface<T>) {
 template <class T, class S> using GpuNegaBinaryBPEncoder = GpuBPEncoder<T, S, PRODM_ENC_NEGABINARY>;
 template <class T, class S> using GpuGroupedBPEncoder = GpuBPEncoder<T, S, PRODM_ENC_GROUPED>;
 
+// Stream sizes of every level and plane ([level][plane] bytes), shared between
+// adapter objects and their copies. The reference's progressive_decode
+// receives stream pointers but no sizes; a per-bit stream's length depends on
+// its contents, so GpuPerBitBPEncoder takes the sizes from this table, which a
+// GpuGreedySizeInterpreter constructed with the same table fills with the
+// metadata sizes it is given on every retrieval.
+struct StreamSizeTable {
+    std::vector<std::vector<uint32_t>> level;
+};
+
+// ---------------------------------------------------------------------------
+// Bitplane encoder: PerBitBPEncoder (PerBitBPEncoder.hpp:71-401). S, the
+// reference's stream word template argument, does not enter the format.
+// progressive_decode takes each stream's size from the next stream's start
+// (the retriever hands over one contiguous buffer per level,
+// FileRetriever.hpp:69-81); the last stream's size from the shared table when
+// it holds the level, else by walking the streams on the host with the
+// elements whose sign is known so far.
+// ---------------------------------------------------------------------------
+template <class T, class S>
+class GpuPerBitBPEncoder PRODM_BASE(MDR::concepts::BitplaneEncoderInterface<T>) {
+  public:
+    explicit GpuPerBitBPEncoder(std::shared_ptr<StreamSizeTable> sizes = nullptr) : table_(std::move(sizes)) {
+        check(prodm_decoder_create(&dec_, PRODM_ENC_PERBIT, dtype_of<T>()), "prodm_decoder_create");
+    }
+    GpuPerBitBPEncoder(const GpuPerBitBPEncoder& o) : GpuPerBitBPEncoder(o.table_) {}   // decoding state is per object
+    GpuPerBitBPEncoder& operator=(const GpuPerBitBPEncoder& o) {
+        table_ = o.table_;
+        return *this;
+    }
+    ~GpuPerBitBPEncoder() { prodm_decoder_destroy(dec_); }
+
+    std::vector<uint8_t*> encode(T const* data, int32_t n, int32_t exp, uint8_t B,
+                                 std::vector<uint32_t>& stream_sizes) const {
+        uint64_t cap = 0;
+        check(prodm_encode_bound(PRODM_ENC_PERBIT, dtype_of<T>(), (uint64_t)n, B, &cap), "prodm_encode_bound");
+        DeviceBuffer d((size_t)n * sizeof(T)), blob(cap + 16), dsz(B * 4);
+        cuda_check(cudaMemcpy(d.get(), data, (size_t)n * sizeof(T), cudaMemcpyHostToDevice), "H2D");
+        check(prodm_encode(PRODM_ENC_PERBIT, dtype_of<T>(), d.get(), (uint64_t)n, exp, B, blob.get(), cap,
+                           dsz.as<uint32_t>(), nullptr, nullptr, 0, nullptr),
+              "prodm_encode");
+        stream_sizes.assign(B, 0);
+        cuda_check(cudaMemcpy(stream_sizes.data(), dsz.get(), B * 4, cudaMemcpyDeviceToHost), "D2H");
+        size_t total = 0;
+        for (auto x : stream_sizes) total += x;
+        std::vector<uint8_t> host(total);
+        cuda_check(cudaMemcpy(host.data(), blob.get(), total, cudaMemcpyDeviceToHost), "D2H");
+        std::vector<uint8_t*> streams(B);
+        size_t off = 0;
+        for (int p = 0; p < B; p++) {
+            streams[p] = (uint8_t*)std::malloc(stream_sizes[p] ? stream_sizes[p] : 1);
+            std::memcpy(streams[p], host.data() + off, stream_sizes[p]);
+            off += stream_sizes[p];
+        }
+        return streams;
+    }
+    T* decode(const std::vector<uint8_t const*>& streams, int32_t n, int exp, uint8_t num_bitplanes) {
+        GpuPerBitBPEncoder fresh(table_);   // no progressive state leaks into a one-shot decode
+        return fresh.decode_impl(streams, n, exp, 0, num_bitplanes, 0);
+    }
+    T* progressive_decode(const std::vector<uint8_t const*>& streams, int32_t n, int exp, uint8_t starting_bitplane,
+                          uint8_t num_bitplanes, int level) {
+        return decode_impl(streams, n, exp, starting_bitplane, num_bitplanes, level);
+    }
+    void set_total_bitplanes(int) {}   // per-bit streams carry no level-wide header
+    void print() const { std::printf("GPU per-bit bitplane encoder\n"); }
+
+  private:
+    // BitDecoder walk (PerBitBPEncoder.hpp:41-67) of planes [s, s+num) for
+    // their sizes: one bit per element, plus the sign after a first 1 bit
+    std::vector<uint32_t> walk_sizes(const std::vector<uint8_t const*>& streams, int32_t n, int level, int s,
+                                     int num) {
+        std::vector<uint8_t> known(known_[level]);
+        std::vector<uint32_t> sz(num);
+        for (int i = 0; i < num; i++) {
+            const uint8_t* w = streams[i];
+            uint64_t pos = 0;
+            for (int32_t j = 0; j < n; j++) {
+                const uint64_t b = (w[pos >> 3] >> (pos & 7)) & 1u;
+                pos++;
+                if (b && !known[j]) { known[j] = 1; pos++; }
+            }
+            sz[i] = (uint32_t)((pos + 63) / 64 * 8);
+        }
+        (void)s;
+        return sz;
+    }
+    T* decode_impl(const std::vector<uint8_t const*>& streams, int32_t n, int exp, int s, int num, int level) {
+        T* out = (T*)std::malloc((size_t)n * sizeof(T));
+        if (num == 0) {
+            std::memset(out, 0, (size_t)n * sizeof(T));
+            return out;
+        }
+        if ((int)known_.size() <= level) known_.resize(level + 1);
+        if (s == 0 || known_[level].size() != (size_t)n) known_[level].assign(n, 0);
+        std::vector<uint32_t> sizes(num, 0);
+        bool have = true;
+        for (int i = 0; i + 1 < num; i++) {
+            const ptrdiff_t d = streams[i + 1] - streams[i];
+            if (d <= 0 || d % 8) { have = false; break; }
+            sizes[i] = (uint32_t)d;
+        }
+        const int last = s + num - 1;
+        if (have && table_ && level < (int)table_->level.size() && last < (int)table_->level[level].size())
+            sizes[num - 1] = table_->level[level][last];
+        else
+            have = false;
+        if (!have) sizes = walk_sizes(streams, n, level, s, num);
+        size_t total = 0;
+        for (auto x : sizes) total += x;
+        DeviceBuffer blob(total + 16), dout((size_t)n * sizeof(T));
+        std::vector<uint8_t> host(total);
+        size_t off = 0;
+        for (int i = 0; i < num; i++) { std::memcpy(host.data() + off, streams[i], sizes[i]); off += sizes[i]; }
+        cuda_check(cudaMemcpy(blob.get(), host.data(), total, cudaMemcpyHostToDevice), "H2D");
+        // the level's plane count is not part of the signature: room for the most
+        check(prodm_progressive_decode(dec_, blob.get(), sizes.data(), (uint64_t)n, exp, s, num, level,
+                                       sizeof(T) == 8 ? 63 : 32, dout.get(), nullptr),
+              "prodm_progressive_decode");
+        cuda_check(cudaMemcpy(out, dout.get(), (size_t)n * sizeof(T), cudaMemcpyDeviceToHost), "D2H");
+        // a sign becomes known with an element's first 1 bit: a nonzero contribution
+        std::vector<uint8_t>& k = known_[level];
+        for (int32_t j = 0; j < n; j++) k[j] |= out[j] != (T)0;
+        return out;
+    }
+
+    prodm_decoder* dec_ = nullptr;
+    std::shared_ptr<StreamSizeTable> table_;
+    std::vector<std::vector<uint8_t>> known_;
+};
+
 // ---------------------------------------------------------------------------
 // Error collectors (MaxErrorCollector.hpp:14-25, SquaredErrorCollector.hpp:54-96)
 // ---------------------------------------------------------------------------
@@ -336,9 +469,14 @@ class GpuGreedySizeInterpreter PRODM_BASE(MDR::concepts::SizeInterpreterInterfac
     explicit GpuGreedySizeInterpreter(int ndims = 3, double s = 0.0) : ndims_(ndims), s_(s) {}
     template <class E>
     explicit GpuGreedySizeInterpreter(const E&, int ndims = 3, double s = 0.0) : ndims_(ndims), s_(s) {}
+    // publishes the stream sizes it is given into `sizes` (for GpuPerBitBPEncoder)
+    template <class E>
+    GpuGreedySizeInterpreter(const E&, std::shared_ptr<StreamSizeTable> sizes, int ndims = 3, double s = 0.0)
+        : ndims_(ndims), s_(s), table_(std::move(sizes)) {}
     std::vector<uint32_t> interpret_retrieve_size(const std::vector<std::vector<uint32_t>>& level_sizes,
                                                   const std::vector<std::vector<double>>& level_errors,
                                                   double tolerance, std::vector<uint8_t>& index) const {
+        if (table_) table_->level = level_sizes;
         const int nl = (int)level_sizes.size();
         const int B = (int)level_sizes[0].size();
         std::vector<uint32_t> sz(nl * B);
@@ -364,6 +502,7 @@ class GpuGreedySizeInterpreter PRODM_BASE(MDR::concepts::SizeInterpreterInterfac
   private:
     int ndims_;
     double s_;
+    std::shared_ptr<StreamSizeTable> table_;
 };
 
 // ---------------------------------------------------------------------------
@@ -455,7 +594,9 @@ class GpuComposedReconstructor {
         c.num_bitplanes = (int)B;
         c.encoder = enc_;
         c.basis = basis_;
-        c.collector = PRODM_COLLECT_SQUARED;
+        // the squared-error table of the metadata feeds the L2 estimators; the
+        // per-bit encoder is used with the max collector only
+        c.collector = enc_ == PRODM_ENC_PERBIT ? PRODM_COLLECT_MAX : PRODM_COLLECT_SQUARED;
         if (h_) prodm_mdr_destroy(h_);
         check(prodm_mdr_create(&h_, &c), "prodm_mdr_create");
         check(prodm_mdr_load_metadata(h_, m.data(), m.size(), nullptr), "prodm_mdr_load_metadata");

@@ -10,14 +10,24 @@
 //     to float rounding.
 #include <cmath>
 #include <cstdint>
+#include <memory>
+#include <type_traits>
 #include <cstdio>
 #include <string>
 #include <vector>
 
 #include "prodm_gb300_mdr.hpp"
 
+struct MDR_EST_TAG {};   // stands for the estimator object the reference interpreters take
+
+// decoders: the per-bit adapter takes the shared size table, the others not
+template <class E>
+static E make_decoder(std::shared_ptr<prodm_gb300::StreamSizeTable> t) {
+    if constexpr (std::is_same<E, prodm_gb300::GpuPerBitBPEncoder<double, uint32_t>>::value) return E(t);
+    else return E();
+}
+
 using namespace prodm_gb300;
-using T = float;
 
 static std::vector<uint8_t> read_all(const std::string& f) {
     FILE* fp = std::fopen(f.c_str(), "rb");
@@ -30,10 +40,12 @@ static std::vector<uint8_t> read_all(const std::string& f) {
     return b;
 }
 
-template <int Enc>
-static int run(const char* dir, const char* tag) {
+// Enc: encoder id; EncT: its adapter class. The per-bit run decodes twice:
+// stream sizes from the table the interpreter fills, and found by the host walk
+template <class T, int Enc, class EncT>
+static int run(const char* dir, const char* tag, int B) {
     const std::vector<uint32_t> dims = {65, 65, 65};
-    const int L = 3, B = 32;
+    const int L = 3;
     const size_t N = 65 * 65 * 65;
     std::vector<T> field(N);
     for (size_t i = 0; i < 65; i++)
@@ -48,7 +60,7 @@ static int run(const char* dir, const char* tag) {
     // 1. adapters through the ComposedRefactor steps
     GpuMGARDHierarchicalDecomposer<T> dec;
     GpuDirectInterleaver<T> il;
-    GpuBPEncoder<T, uint32_t, Enc> enc;
+    EncT enc;
     std::vector<T> data(field);
     dec.decompose(data.data(), dims, L);
     std::vector<std::vector<uint32_t>> ld(L + 1, std::vector<uint32_t>(3));
@@ -93,9 +105,12 @@ static int run(const char* dir, const char* tag) {
     const int interp = PRODM_INTERP_SIGN_EXCLUDE;
     GpuComposedReconstructor<T> rec(Enc, PRODM_BASIS_HIERARCHICAL, interp, PRODM_EST_MAX_HB, meta, files);
     rec.load_metadata();
-    GpuGreedySizeInterpreter<T, PRODM_INTERP_SIGN_EXCLUDE, PRODM_EST_MAX_HB> gi;
-    GpuBPEncoder<T, uint32_t, Enc> pdec;
+    auto table = std::make_shared<StreamSizeTable>();
+    GpuGreedySizeInterpreter<T, PRODM_INTERP_SIGN_EXCLUDE, PRODM_EST_MAX_HB> gi(MDR_EST_TAG(), table);
+    EncT pdec = make_decoder<EncT>(table);
+    EncT wdec = make_decoder<EncT>(nullptr);   // per-bit: sizes by the host walk
     pdec.set_total_bitplanes(B);
+    wdec.set_total_bitplanes(B);
     GpuMaxErrorCollector<T> mc;
     std::vector<std::vector<double>> lerr(L + 1);
     for (int l = 0; l <= L; l++) lerr[l] = mc.collect_level_error(nullptr, 0, B, bounds[l]);
@@ -123,6 +138,12 @@ static int run(const char* dir, const char* tag) {
             const size_t box = (size_t)ld[l][0] * ld[l][1] * ld[l][2];
             const size_t pbox = l ? (size_t)ld[l - 1][0] * ld[l - 1][1] * ld[l - 1][2] : 0;
             T* lv = pdec.progressive_decode(st, (int32_t)(box - pbox), e, prev_index[l], num, l);
+            if (Enc == PRODM_ENC_PERBIT) {
+                T* lw = wdec.progressive_decode(st, (int32_t)(box - pbox), e, prev_index[l], num, l);
+                const bool same = std::memcmp(lv, lw, (box - pbox) * sizeof(T)) == 0;
+                std::free(lw);
+                if (!same) { std::printf("%s: table and walked stream sizes decode differently\n", tag); return 1; }
+            }
             std::vector<uint32_t> coarse = l ? ld[l - 1] : std::vector<uint32_t>(3, 0);
             std::vector<T> cur(N, 0);
             il.reposition(lv, dims, ld[l], coarse, cur.data());
@@ -141,8 +162,9 @@ static int run(const char* dir, const char* tag) {
 
 int main(int argc, char** argv) {
     const char* dir = argc > 1 ? argv[1] : ".";
-    int rc = run<PRODM_ENC_NEGABINARY>(dir, "negabinary");
-    rc |= run<PRODM_ENC_GROUPED>(dir, "grouped");
+    int rc = run<float, PRODM_ENC_NEGABINARY, GpuNegaBinaryBPEncoder<float, uint32_t>>(dir, "negabinary", 32);
+    rc |= run<float, PRODM_ENC_GROUPED, GpuGroupedBPEncoder<float, uint32_t>>(dir, "grouped", 32);
+    rc |= run<double, PRODM_ENC_PERBIT, GpuPerBitBPEncoder<double, uint32_t>>(dir, "perbit", 60);
     if (rc == 0) std::printf("PLUGIN PARITY OK\n");
     return rc;
 }

@@ -2,6 +2,7 @@
 // ComposedReconstructor templates instantiated with the GPU plugin adapters
 // (only built where the reference headers are available; never run).
 #include <cstdint>
+#include <memory>
 #include <iostream>
 #include <vector>
 #include <string>
@@ -32,5 +33,27 @@ int main() {
         MDR::NullLevelCompressor(), Interp(MDR::MaxErrorEstimatorHB<T>()), MDR::ConcatLevelFileRetriever("meta.bin", files));
     rec.load_metadata();
     T* out = rec.progressive_reconstruct(1e-3, -1);
-    return out ? 0 : 1;
+
+    // the GE applications' configuration: per-bit encoder, fp64, max collector;
+    // the interpreter hands the metadata stream sizes to the per-bit decoder
+    using D = double;
+    std::vector<std::string> gfiles = {"g0.bin", "g1.bin"};
+    auto grefactor = MDR::ComposedRefactor<D, GpuMGARDHierarchicalDecomposer<D>, GpuDirectInterleaver<D>,
+                                           GpuPerBitBPEncoder<D, uint32_t>, MDR::NullLevelCompressor,
+                                           GpuMaxErrorCollector<D>, MDR::ConcatLevelFileWriter>(
+        GpuMGARDHierarchicalDecomposer<D>(), GpuDirectInterleaver<D>(), GpuPerBitBPEncoder<D, uint32_t>(),
+        MDR::NullLevelCompressor(), GpuMaxErrorCollector<D>(), MDR::ConcatLevelFileWriter("gmeta.bin", gfiles));
+    std::vector<D> gdata(33 * 33 * 33, 1.0);
+    grefactor.refactor(gdata.data(), {33, 33, 33}, 1, 60);
+    auto table = std::make_shared<StreamSizeTable>();
+    using GInterp = GpuGreedySizeInterpreter<D, PRODM_INTERP_SIGN_EXCLUDE, PRODM_EST_MAX_HB>;
+    auto grec = MDR::ComposedReconstructor<D, GpuMGARDHierarchicalDecomposer<D>, GpuDirectInterleaver<D>,
+                                           GpuPerBitBPEncoder<D, uint32_t>, MDR::NullLevelCompressor, GInterp,
+                                           MDR::MaxErrorEstimatorHB<D>, MDR::ConcatLevelFileRetriever>(
+        GpuMGARDHierarchicalDecomposer<D>(), GpuDirectInterleaver<D>(), GpuPerBitBPEncoder<D, uint32_t>(table),
+        MDR::NullLevelCompressor(), GInterp(MDR::MaxErrorEstimatorHB<D>(), table),
+        MDR::ConcatLevelFileRetriever("gmeta.bin", gfiles));
+    grec.load_metadata();
+    D* gout = grec.progressive_reconstruct(1e-6, -1);
+    return out && gout ? 0 : 1;
 }
