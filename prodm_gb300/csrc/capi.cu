@@ -426,12 +426,13 @@ int pb_progressive_decode(prodm_decoder* h, const uint8_t* blob, const uint32_t*
         hv[num + i] = hs[i] / 8;
         o += hs[i];
     }
-    uint64_t* dv;
-    PRODM_CUDA(cudaMallocAsync((void**)&dv, hv.size() * 8, st));
+    uint64_t* dv;   // plane pointers, word counts, then the parse pipeline's scratch
+    const size_t head = (hv.size() * 8 + 255) / 256 * 256;
+    PRODM_CUDA(cudaMallocAsync((void**)&dv, head + pb_parse_scratch_bytes(num), st));
     PRODM_CUDA(cudaMemcpyAsync(dv, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st));
     PRODM_CUDA(cudaMemsetAsync(status, 0, 4, st));
     int rc = launch_pb_parse((const uint64_t* const*)dv, dv + num, s, num, n, rows, rw, rows + (uint64_t)(B + 1) * rw,
-                             rows + (uint64_t)B * rw, status, st);
+                             rows + (uint64_t)B * rw, (uint8_t*)dv + head, status, st);
     if (!rc)
         rc = launch_pb_decode<T>(rows, rw, n, nullptr, exp, B, s, s + num, nullptr, rows + (uint64_t)B * rw,
                                  rows + (uint64_t)(B + 1) * rw, out, st);
@@ -1011,12 +1012,13 @@ int pb_parse_loaded(prodm_mdr* h, int l, cudaStream_t st) {
         hv[num + i] = sz / 8;
         o += sz;
     }
-    uint64_t* dv;
-    PRODM_CUDA(cudaMallocAsync((void**)&dv, hv.size() * 8, st));
+    uint64_t* dv;   // plane pointers, word counts, then the parse pipeline's scratch
+    const size_t head = (hv.size() * 8 + 255) / 256 * 256;
+    PRODM_CUDA(cudaMallocAsync((void**)&dv, head + pb_parse_scratch_bytes(num), st));
     PRODM_CUDA(cudaMemcpyAsync(dv, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st));
     PRODM_CUDA(cudaMemsetAsync(h->pbstatus, 0, 4, st));
     rc = launch_pb_parse((const uint64_t* const*)dv, dv + num, first, num, n, rows, rw, rows + (uint64_t)(B + 1) * rw,
-                         rows + (uint64_t)B * rw, h->pbstatus, st);
+                         rows + (uint64_t)B * rw, (uint8_t*)dv + head, h->pbstatus, st);
     int hstat = 0;
     if (!rc) {
         cudaError_t e = cudaMemcpyAsync(&hstat, h->pbstatus, 4, cudaMemcpyDeviceToHost, st);

@@ -111,8 +111,9 @@ size_t pb_pack_scratch_bytes(uint64_t n, int B);
 int launch_pb_pack(const uint32_t* rows, uint64_t stride, uint64_t n, int B, const uint32_t* sizes, uint64_t total,
                    uint8_t* dst, void* scratch, cudaStream_t st);
 int launch_pb_init_unseen(uint32_t* unseen, uint32_t* signs, uint64_t n, cudaStream_t st);
+size_t pb_parse_scratch_bytes(int np);
 int launch_pb_parse(const uint64_t* const* planes, const uint64_t* nwords, int a, int np, uint64_t n, uint32_t* rows,
-                    uint64_t stride, uint32_t* unseen, uint32_t* signs, int* status, cudaStream_t st);
+                    uint64_t stride, uint32_t* unseen, uint32_t* signs, void* scratch, int* status, cudaStream_t st);
 
 // pack.cu
 int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,

@@ -288,144 +288,224 @@ __global__ void __launch_bounds__(PK_T) k_pb_pack_write(const uint32_t* __restri
 // parse: reference streams of planes [a, a+np) -> rows a..a+np-1, with the
 // unseen / sign rows carried from the planes before a and updated.
 //
-// One CTA per level. Warp w parses planes a+2w and a+2w+1; the chain over
-// planes is a software pipeline over chunks of PZ_G groups: warp w receives
-// each chunk's unseen / sign masks from warp w-1 through a shared-memory ring
-// and hands them on after its two planes. Within a plane, each group's bit
-// positions follow from the fixed point of
-//     q_j = j + #{k < j : k unseen and its bit (read at q_k) is 1},
-// iterated from q_j = j; every round settles at least one more element with a
-// sign bit, so at most 33 rounds are needed. Every wait is bounded: past the
-// limit the warp records PRODM_ETIMEOUT in *status and returns.
+// One single-warp CTA per plane, all co-resident (cooperative launch). The
+// chain over planes is a software pipeline over chunks of 32 groups: CTA k
+// receives each chunk's unseen / sign masks from CTA k-1 through a ring in
+// global memory (release / acquire flags) and hands them on after its plane.
+// Within a chunk, only groups with unseen elements can hold sign bits: they
+// are parsed in order, one step per sign bit (pz_group); the other groups
+// hold exactly one bit per element, so once the sign bits before them are
+// counted, every lane reads its group's word directly. Every wait is bounded: past the limit the CTA
+// records PRODM_ETIMEOUT in *status and returns.
 // ---------------------------------------------------------------------------
-constexpr int PZ_G = 16;            // groups per chunk
-constexpr int PZ_R = 4;             // ring depth (chunks)
-constexpr long long kPzSpin = 1ll << 26;
+constexpr int PZ_R = 8;                      // ring depth (chunks)
+constexpr long long kPzSpin = 1ll << 24;     // x >= 256 ns per wait
 
-__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
-    const uint32_t lo = __shfl_sync(FULL, (uint32_t)v, src);
-    const uint32_t hi = __shfl_sync(FULL, (uint32_t)(v >> 32), src);
-    return ((uint64_t)hi << 32) | lo;
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// a plane's stream: the chunk's 64 64-bit words are staged in shared memory;
+// the next chunk's are prefetched into registers n0 / n1 (lane i: words
+// npb + i and npb + 32 + i)
 struct PlaneReader {
     const uint64_t* w;
-    uint64_t nw;
-    uint64_t pos;    // bit position in the stream
-    uint64_t pb;     // word index held by lane 0 of buf
-    uint64_t buf;    // lane i: word pb + i
-    uint64_t nxt;    // prefetch: lane i: word npb + i
-    uint64_t npb;
+    uint64_t nw, pos, pb, npb;
+    uint64_t n0, n1;
     __device__ __forceinline__ uint64_t load(uint64_t k) const { return k < nw ? __ldcs(w + k) : 0ull; }
 };
 
-// one chunk of one plane; lane j (< PZ_G) holds group j's unseen / sign masks
-__device__ __forceinline__ void pz_chunk(PlaneReader& r, bool first, uint64_t g0, uint64_t ng, uint64_t n,
-                                         uint32_t& U, uint32_t& S, uint32_t* __restrict__ row, int lane) {
-    // the chunk reads words [pos/64, pos/64 + 16]; keep them in buf and
-    // prefetch the next chunk's (which starts 8..16 words further on)
-    const uint64_t wb = r.pos >> 6;
-    if (first) {
-        r.pb = wb;
-        r.buf = r.load(wb + lane);
-    } else {
-        r.pb = r.npb;
-        r.buf = r.nxt;
+__device__ __forceinline__ uint32_t bits_below(int k) { return k >= 32 ? FULL : ((1u << k) - 1u); }
+
+// One group of one plane from the 64 stream bits W at its start. With d sign
+// bits before them, the remaining elements' bits are the frame W >> d (bit i
+// = element i); the next element to carry a sign is the lowest unseen one
+// whose bit is set there, and its sign is bit i of the next frame W >> (d+1).
+// One step per sign.
+__device__ __forceinline__ void pz_group(uint64_t W, uint32_t U, int nv, uint32_t& M, uint32_t& SG, uint32_t& cnt) {
+    const uint32_t lo32 = (uint32_t)W, hi32 = (uint32_t)(W >> 32);
+    const uint32_t vm = bits_below(nv);
+    uint32_t rest = U & vm, m = 0, sg = 0, below = 0, d = 0;
+    uint32_t Wd = lo32;
+    for (int it = 0; it < 33; it++) {
+        const uint32_t T = rest & Wd;
+        if (!T) break;
+        const uint32_t bit = T & (0u - T);          // element i
+        const uint32_t upto = (bit << 1) - 1u;      // elements 0..i
+        m |= Wd & upto & ~below;
+        below = upto;
+        rest &= ~upto;
+        d++;
+        Wd = __funnelshift_rc(lo32, hi32, d);
+        sg |= Wd & bit;
     }
-    r.npb = wb + 8;
-    r.nxt = r.load(r.npb + lane);
-    const uint32_t lt = (1u << lane) - 1u;
-    uint32_t Mkeep = 0;
-    for (int j = 0; j < PZ_G; j++) {
-        const uint64_t g = g0 + j;
-        if (g >= ng) break;
-        const int nvalid = pk_nvalid(g, ng, n);
-        const uint32_t Uj = __shfl_sync(FULL, U, j), Sj = __shfl_sync(FULL, S, j);
-        const int wi = (int)((r.pos >> 6) - r.pb);
-        const uint64_t w0 = shfl64(r.buf, wi), w1 = shfl64(r.buf, wi + 1);
-        const int sh = (int)(r.pos & 63);
-        const uint64_t W = sh ? (w0 >> sh) | (w1 << (64 - sh)) : w0;
-        const bool u = lane < nvalid && ((Uj >> lane) & 1u);
-        int q = lane;
-        uint32_t f = 0, b = 0;
-        for (int it = 0; it < 34; it++) {
-            b = (uint32_t)(W >> q) & 1u;
-            f = __ballot_sync(FULL, u && b);
-            const int qn = lane + __popc(f & lt);
-            if (__all_sync(FULL, qn == q)) break;
-            q = qn;
-        }
-        const uint32_t M = __ballot_sync(FULL, lane < nvalid && b);
-        const uint32_t SG = __ballot_sync(FULL, ((f >> lane) & 1u) && ((W >> (q + 1)) & 1ull));
-        r.pos += (uint64_t)(nvalid + __popc(f));
-        if (lane == j) {
-            U = Uj & ~M;
-            S = Sj | SG;
-            Mkeep = M;
-        }
-    }
-    if (lane < PZ_G && g0 + lane < ng) row[g0 + lane] = Mkeep;
+    M = m | (Wd & vm & ~below);
+    SG = sg;
+    cnt = d;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_pb_parse(const uint64_t* const* __restrict__ planes,
-                                                      const uint64_t* __restrict__ nwords, int a, int np, uint64_t n,
-                                                      uint32_t* __restrict__ rows, uint64_t stride,
-                                                      uint32_t* __restrict__ unseen, uint32_t* __restrict__ signs,
-                                                      int* __restrict__ status) {
-    __shared__ uint32_t ring[32][PZ_R][2][PZ_G];
-    __shared__ int produced[32], consumed[32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 32) { produced[threadIdx.x] = 0; consumed[threadIdx.x] = 0; }
-    __syncthreads();
-    const int active = (np + 1) / 2;
-    if (warp >= active) return;
-    volatile int* vprod = produced;
-    volatile int* vcons = consumed;
-    const int i0 = 2 * warp, i1 = 2 * warp + 1;
-    const bool two = i1 < np, last = warp == active - 1;
-    const uint64_t ng = (n + 31) / 32, nch = (ng + PZ_G - 1) / PZ_G;
-    PlaneReader r0{planes[i0], nwords[i0], 0, 0, 0, 0, 0};
-    PlaneReader r1{two ? planes[i1] : nullptr, two ? nwords[i1] : 0, 0, 0, 0, 0, 0};
-    uint32_t* row0 = rows + (uint64_t)(a + i0) * stride;
-    uint32_t* row1 = rows + (uint64_t)(a + (two ? i1 : i0)) * stride;
+// one chunk (32 groups, lane g = group g0 + g) of one plane; U / S: the
+// lane's group's unseen and sign masks, updated; returns the group's word.
+// ws: the chunk's stream as 128 32-bit words (word 2*pb + i at ws[i])
+__device__ __forceinline__ uint32_t pz_chunk(PlaneReader& r, bool first, uint64_t g0, uint64_t ng, uint64_t n,
+                                             uint32_t& U, uint32_t& S, int lane, uint32_t* ws, uint32_t* us,
+                                             int* nvs) {
+    // the chunk reads words [pos/64, pos/64 + 33); its successor starts 16..32
+    // 64-bit words on (a full group takes 32..64 bits)
+    const uint64_t wb = r.pos >> 6;
+    __syncwarp();
+    uint64_t a, b;
+    if (first) {
+        r.pb = wb;
+        a = r.load(wb + lane);
+        b = r.load(wb + 32 + lane);
+    } else {
+        r.pb = r.npb;
+        a = r.n0;
+        b = r.n1;
+    }
+    ws[2 * lane] = (uint32_t)a;
+    ws[2 * lane + 1] = (uint32_t)(a >> 32);
+    ws[64 + 2 * lane] = (uint32_t)b;
+    ws[64 + 2 * lane + 1] = (uint32_t)(b >> 32);
+    r.npb = wb + 16;
+    r.n0 = r.load(r.npb + lane);
+    r.n1 = r.load(r.npb + 32 + lane);
+    const uint64_t g = g0 + lane;
+    const int nv = pk_nvalid(g, ng, n);
+    us[lane] = U;
+    nvs[lane] = nv;
+    __syncwarp();
+    const uint32_t p0 = (uint32_t)(r.pos - 64 * r.pb);   // chunk start within the staged words (< 1088)
+    uint32_t M = 0, extra = 0;
+    // groups with unseen elements, in order (every lane computes the same):
+    // the sign bits before group j are those of the earlier groups of this kind
+    const uint32_t seq = __ballot_sync(FULL, nv > 0 && U != 0);
+    uint32_t todo = seq, run = 0;
+    while (todo) {
+        const int j = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t Uj = us[j];
+        const int nvj = nvs[j];
+        const uint32_t at = p0 + 32u * j + run;
+        const uint32_t k = at >> 5, sh = at & 31;
+        const uint32_t x0 = ws[k], x1 = ws[k + 1], x2 = ws[k + 2];
+        const uint64_t W = ((uint64_t)__funnelshift_r(x1, x2, sh) << 32) | __funnelshift_r(x0, x1, sh);
+        uint32_t Mj, SG, cnt;
+        pz_group(W, Uj, nvj, Mj, SG, cnt);
+        const bool mine = lane == j;
+        M = mine ? Mj : M;
+        extra = mine ? cnt : extra;
+        U = mine ? (Uj & ~Mj) : U;
+        S = mine ? (S | SG) : S;
+        run += cnt;
+    }
+    // groups without unseen elements: one bit per element at known offsets
+    uint32_t inc = extra;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (nv > 0 && !((seq >> lane) & 1u)) {
+        const uint32_t at = p0 + 32u * lane + (inc - extra);
+        M = __funnelshift_r(ws[at >> 5], ws[(at >> 5) + 1], at & 31) & valid_mask(nv);
+    }
+    uint32_t used = (uint32_t)nv;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) used += __shfl_xor_sync(FULL, used, o);
+    r.pos += used + run;
+    return M;
+}
+
+constexpr int PZ_SUB = 4;                    // 32-group sub-chunks per hand-off
+constexpr int PZ_E = 64 * PZ_SUB;            // ring entry: unseen + sign words of 32 * PZ_SUB groups
+// dynamic shared memory reserved (unused) so that no two planes' CTAs share an SM
+constexpr int PZ_SPREAD_SMEM = 116 * 1024;
+
+__global__ void __launch_bounds__(32) k_pb_parse(const uint64_t* const* __restrict__ planes,
+                                                 const uint64_t* __restrict__ nwords, int a, int np, uint64_t n,
+                                                 uint32_t* __restrict__ rows, uint64_t stride,
+                                                 uint32_t* __restrict__ unseen, uint32_t* __restrict__ signs,
+                                                 uint32_t* __restrict__ ring, int* __restrict__ flags,
+                                                 int* __restrict__ status) {
+    __shared__ uint32_t ws[130];
+    __shared__ uint32_t us[32];
+    __shared__ int nvs[32];
+    const int k = blockIdx.x, lane = threadIdx.x;
+    int* produced = flags;
+    int* consumed = flags + np;
+    const uint64_t ng = (n + 31) / 32, nch = (ng + 32 * PZ_SUB - 1) / (32 * PZ_SUB);
+    PlaneReader r{planes[k], nwords[k], 0, 0, 0, 0, 0};
+    uint32_t* row = rows + (uint64_t)(a + k) * stride;
+    const bool last = k == np - 1;
+    int seen_consumed = 0;   // the consumer's progress as last read
     for (uint64_t c = 0; c < nch; c++) {
-        const uint64_t g0 = c * PZ_G;
         const int slot = (int)(c % PZ_R);
-        uint32_t U = 0, S = 0;
-        if (warp == 0) {
-            if (lane < PZ_G && g0 + lane < ng) { U = unseen[g0 + lane]; S = signs[g0 + lane]; }
+        uint32_t U[PZ_SUB], S[PZ_SUB];
+        if (k == 0) {
+#pragma unroll
+            for (int t = 0; t < PZ_SUB; t++) {
+                const uint64_t g = c * 32 * PZ_SUB + t * 32 + lane;
+                U[t] = g < ng ? unseen[g] : 0u;
+                S[t] = g < ng ? signs[g] : 0u;
+            }
         } else {
             long long spins = 0;
-            while (vprod[warp - 1] <= (int)c) {
+            while (ld_acquire(produced + k - 1) <= (int)c) {
                 if (++spins > kPzSpin) { if (lane == 0) atomicExch(status, PRODM_ETIMEOUT); return; }
-                __nanosleep(64);
+                __nanosleep(128);
             }
-            __threadfence_block();
-            if (lane < PZ_G) { U = ring[warp - 1][slot][0][lane]; S = ring[warp - 1][slot][1][lane]; }
+            const uint32_t* src = ring + ((uint64_t)(k - 1) * PZ_R + slot) * PZ_E;
+#pragma unroll
+            for (int t = 0; t < PZ_SUB; t++) {
+                U[t] = __ldcg(src + t * 64 + lane);
+                S[t] = __ldcg(src + t * 64 + 32 + lane);
+            }
             __syncwarp();
-            if (lane == 0) { __threadfence_block(); vcons[warp - 1] = (int)c + 1; }
+            if (lane == 0) st_release(consumed + k - 1, (int)c + 1);
         }
-        pz_chunk(r0, c == 0, g0, ng, n, U, S, row0, lane);
-        if (two) pz_chunk(r1, c == 0, g0, ng, n, U, S, row1, lane);
+#pragma unroll
+        for (int t = 0; t < PZ_SUB; t++) {
+            const uint64_t g0 = c * 32 * PZ_SUB + t * 32;
+            if (g0 >= ng) break;
+            const uint32_t M = pz_chunk(r, c == 0 && t == 0, g0, ng, n, U[t], S[t], lane, ws, us, nvs);
+            if (g0 + lane < ng) row[g0 + lane] = M;
+        }
         if (last) {
-            if (lane < PZ_G && g0 + lane < ng) { unseen[g0 + lane] = U; signs[g0 + lane] = S; }
-        } else {
-            long long spins = 0;
-            while ((int)c - vcons[warp] >= PZ_R) {
-                if (++spins > kPzSpin) { if (lane == 0) atomicExch(status, PRODM_ETIMEOUT); return; }
-                __nanosleep(64);
+#pragma unroll
+            for (int t = 0; t < PZ_SUB; t++) {
+                const uint64_t g = c * 32 * PZ_SUB + t * 32 + lane;
+                if (g < ng) { unseen[g] = U[t]; signs[g] = S[t]; }
             }
-            if (lane < PZ_G) { ring[warp][slot][0][lane] = U; ring[warp][slot][1][lane] = S; }
-            __threadfence_block();
+        } else {
+            if ((int)c - seen_consumed >= PZ_R) {
+                long long spins = 0;
+                while ((int)c - (seen_consumed = ld_acquire(consumed + k)) >= PZ_R) {
+                    if (++spins > kPzSpin) { if (lane == 0) atomicExch(status, PRODM_ETIMEOUT); return; }
+                    __nanosleep(128);
+                }
+            }
+            uint32_t* dst = ring + ((uint64_t)k * PZ_R + slot) * PZ_E;
+#pragma unroll
+            for (int t = 0; t < PZ_SUB; t++) {
+                __stcg(dst + t * 64 + lane, U[t]);
+                __stcg(dst + t * 64 + 32 + lane, S[t]);
+            }
             __syncwarp();
-            if (lane == 0) vprod[warp] = (int)c + 1;
+            if (lane == 0) {
+                __threadfence();
+                st_release(produced + k, (int)c + 1);
+            }
         }
     }
     // a well-formed stream ends in its last word
-    if (lane == 0) {
-        if ((r0.pos + 63) / 64 != r0.nw) atomicCAS(status, 0, PRODM_ECORRUPT);
-        if (two && (r1.pos + 63) / 64 != r1.nw) atomicCAS(status, 0, PRODM_ECORRUPT);
-    }
+    if (lane == 0 && (r.pos + 63) / 64 != r.nw) atomicCAS(status, 0, PRODM_ECORRUPT);
 }
 
 // unseen row of a fresh level: every element present
@@ -499,10 +579,27 @@ int launch_pb_init_unseen(uint32_t* unseen, uint32_t* signs, uint64_t n, cudaStr
     return PRODM_OK;
 }
 
+size_t pb_parse_scratch_bytes(int np) { return (size_t)np * PZ_R * PZ_E * 4 + (size_t)2 * np * 4 + 256; }
+
 int launch_pb_parse(const uint64_t* const* planes, const uint64_t* nwords, int a, int np, uint64_t n, uint32_t* rows,
-                    uint64_t stride, uint32_t* unseen, uint32_t* signs, int* status, cudaStream_t st) {
+                    uint64_t stride, uint32_t* unseen, uint32_t* signs, void* scratch, int* status, cudaStream_t st) {
     if (np < 1 || np > 64) return fail(PRODM_EINVAL, "perbit parse: 1..64 planes per call");
-    k_pb_parse<<<1, 1024, 0, st>>>(planes, nwords, a, np, n, rows, stride, unseen, signs, status);
+    uint32_t* ring = (uint32_t*)scratch;
+    int* flags = (int*)(ring + (size_t)np * PZ_R * PZ_E);
+    PRODM_CUDA(cudaMemsetAsync(flags, 0, (size_t)2 * np * 4, st));
+    static thread_local int attr_dev = -1;
+    int dev = 0;
+    PRODM_CUDA(cudaGetDevice(&dev));
+    if (attr_dev != dev) {
+        PRODM_CUDA(cudaFuncSetAttribute((const void*)k_pb_parse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        PZ_SPREAD_SMEM));
+        attr_dev = dev;
+    }
+    // the planes' CTAs wait on one another: launched cooperatively, so that
+    // all of them are resident together
+    void* args[] = {(void*)&planes, (void*)&nwords, &a, &np, &n, &rows, &stride, &unseen, &signs, &ring, &flags,
+                    &status};
+    PRODM_CUDA(cudaLaunchCooperativeKernel((const void*)k_pb_parse, dim3(np), dim3(32), args, PZ_SPREAD_SMEM, st));
     PRODM_CHECK_LAUNCH("k_pb_parse");
     return PRODM_OK;
 }
