@@ -35,13 +35,66 @@ __device__ __forceinline__ int pb_exp(const typename KeyOf<T>::type* maxkey, int
     return maxkey ? frexp_exp(key_to_val(*maxkey, T())) : exp_arg;
 }
 
-// fixed-point magnitude of one value (PerBitBPEncoder.hpp:100-104)
-template <class T>
-__device__ __forceinline__ typename Traits<T>::FP pb_mag(T v, int B, int exp) {
-    const T shifted = ldexp_t(v, B - exp);
-    const int64_t fx = (int64_t)shifted;
-    return (typename Traits<T>::FP)(v < 0 ? -fx : fx);
+// Fixed-point magnitude of one value, |trunc(ldexp(v, k))| with k = B - exp
+// (PerBitBPEncoder.hpp:100-104). The scaling is exact (the result stays
+// below 2^B), so the truncated magnitude is floor(|v| * 2^k): for doubles it
+// is taken from the exponent and mantissa bits with integer operations
+// (GB300's FP64 pipe is slow); for floats by one multiplication with an exact
+// power of two where that is a normal float, else ldexpf.
+__device__ __forceinline__ uint64_t pb_mag(double v, int k, bool, float) {
+    const uint64_t bits = (uint64_t)__double_as_longlong(v);
+    const int ev = (int)((bits >> 52) & 0x7ff);
+    uint64_t m = bits & 0xfffffffffffffull;
+    int e = -1074;
+    if (ev) {
+        m |= 1ull << 52;
+        e = ev - 1075;
+    }
+    const int sh = e + k;   // |v| * 2^k = m * 2^sh
+    if (sh >= 0) return m << sh;
+    return sh <= -64 ? 0ull : m >> (-sh);
 }
+__device__ __forceinline__ uint32_t pb_mag(float v, int k, bool fast, float sc) {
+    return (uint32_t)fabsf(fast ? v * sc : ldexpf(v, k));
+}
+__device__ __forceinline__ bool pb_neg(double v) { return __double_as_longlong(v) < 0; }
+__device__ __forceinline__ bool pb_neg(float v) { return v < 0.f; }
+
+// ldexp((T)acc, s) (PerBitBPEncoder.hpp:343). For doubles with every result
+// normal (fast: -1022 <= s <= 960), acc is rounded once to 53 bits (nearest,
+// ties to even, as the conversion does) and the exponent field written
+// directly; otherwise, and for floats, the conversion and an exact scaling.
+__device__ __forceinline__ double pb_value(uint64_t acc, int s, bool fast, float) {
+    if (!fast) return ldexp((double)acc, s);
+    if (acc == 0) return 0.0;
+    const int msb = 63 - __clzll((long long)acc);
+    int e2 = msb;
+    uint64_t mant;
+    if (msb <= 52) {
+        mant = acc << (52 - msb);
+    } else {
+        const int sh = msb - 52;
+        mant = acc >> sh;
+        const uint64_t rem = acc & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1))) {
+            mant++;
+            if (mant >> 53) {
+                mant >>= 1;
+                e2++;
+            }
+        }
+    }
+    return __longlong_as_double((long long)(((uint64_t)(e2 + s + 1023) << 52) | (mant & 0xfffffffffffffull)));
+}
+__device__ __forceinline__ float pb_value(uint32_t acc, int s, bool fast, float sc) {
+    return fast ? (float)acc * sc : ldexpf((float)acc, s);
+}
+__device__ __forceinline__ double pb_negate(double v) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ float pb_negate(float v) { return -v; }
+__device__ __forceinline__ bool pb_value_fast(double*, int s) { return s >= -1022 && s <= 960; }
+__device__ __forceinline__ bool pb_value_fast(float*, int s) { return pow2_normal(s); }
 
 __device__ __forceinline__ uint32_t valid_mask(int nvalid) { return nvalid >= 32 ? FULL : ((1u << nvalid) - 1u); }
 
@@ -59,6 +112,9 @@ __global__ void __launch_bounds__(256) k_pb_encode(const T* __restrict__ x, uint
     __shared__ uint32_t cnt[64];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int exp = pb_exp<T>(maxkey, exp_arg);
+    const int ks = B - exp;
+    const bool fast = pow2_normal(ks);
+    const float sc = fast ? pow2f(ks) : 1.f;
     const uint64_t ng = (n + 31) / 32;
     const uint64_t nch = (ng + PB_CHUNK - 1) / PB_CHUNK;
     for (int k = threadIdx.x; k < 64; k += blockDim.x) cnt[k] = 0;
@@ -71,8 +127,8 @@ __global__ void __launch_bounds__(256) k_pb_encode(const T* __restrict__ x, uint
             const int gl = warp * PB_GPW + j;
             const uint64_t i = (g0 + gl) * 32 + lane;
             const T v = i < n ? __ldcs(x + i) : (T)0;
-            const FP m = pb_mag(v, B, exp);
-            const uint32_t sgn = __ballot_sync(FULL, v < 0 && m != 0);
+            const FP m = pb_mag(v, ks, fast, sc);
+            const uint32_t sgn = __ballot_sync(FULL, pb_neg(v) && m != 0);
             const uint32_t lo = transpose32((uint32_t)m, lane);          // lane k: bit k of the 32 magnitudes
             const uint32_t hi = sizeof(T) == 8 ? transpose32((uint32_t)((uint64_t)m >> 32), lane) : 0u;
             // OR of the words of all higher bits: first 1 bits = word & ~that
@@ -133,6 +189,9 @@ __global__ void __launch_bounds__(256) k_pb_decode(const uint32_t* __restrict__ 
     const int num = e - s;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int exp = pb_exp<T>(maxkey, exp_arg);
+    const int vs = exp - e;
+    const bool fast = pb_value_fast((T*)nullptr, vs);
+    const float sc = (sizeof(T) == 4 && fast) ? pow2f(vs) : 1.f;
     const uint64_t ng = (n + 31) / 32;
     const uint64_t nch = (ng + PB_CHUNK - 1) / PB_CHUNK;
     const int extra = unseen ? 2 : 1;
@@ -158,9 +217,9 @@ __global__ void __launch_bounds__(256) k_pb_decode(const uint32_t* __restrict__ 
             }
             const uint32_t sg = tile[num * PB_LD + gl];
             const bool known = unseen ? !((tile[(num + 1) * PB_LD + gl] >> lane) & 1u) : acc != 0;
-            const T v = ldexp_t((T)acc, exp - e);
+            const T v = pb_value(acc, vs, fast, sc);
             const uint64_t i = (g0 + gl) * 32 + lane;
-            if (i < n) out[i] = (known && ((sg >> lane) & 1u)) ? -v : v;
+            if (i < n) out[i] = (known && ((sg >> lane) & 1u)) ? pb_negate(v) : v;
         }
         __syncthreads();
     }

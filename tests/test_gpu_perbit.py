@@ -145,6 +145,32 @@ def test_pipeline_shapes_match_oracle(shape, L, dt, B):
         assert err <= rel * vr * (1 + 1e-6) or np.all(idx == B), (rel, err, idx)
 
 
+@pytest.mark.parametrize("dt,scale", [(np.float64, 1e-300), (np.float64, 1e300), (np.float64, 1e-310),
+                                      (np.float32, 1e-36), (np.float32, 1e36), (np.float32, 1e-42)])
+def test_extreme_exponents_match_oracle(dt, scale):
+    """level exponents far from 0 (subnormal values, scalings outside the
+    normal range): the device encode / decode paths against the oracle"""
+    rng = np.random.default_rng(int(abs(math.log10(scale))))
+    n = 4099
+    B = 60 if dt == np.float64 else 32
+    x = (rng.standard_normal(n) * scale).astype(dt)
+    x[rng.random(n) < 0.1] = 0
+    mx = float(np.abs(x).max())
+    e = math.frexp(mx)[1]
+    blob, sizes = O.pb_encode(x, e, B)
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    gblob, gsizes, _ = api().encode("perbit", torch.from_numpy(x).cuda(), e, B)
+    assert np.array_equal(gsizes, sizes) and np.array_equal(gblob.cpu().numpy(), blob)
+    offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+    dev = api().ProgressiveDecoder("perbit", tdt)
+    st = O.perbit_state(dt)
+    d = torch.from_numpy(blob).cuda()
+    for a, b in [(0, 5), (5, B)]:
+        got = dev.decode(d[offs[a]:offs[b]], sizes[a:b], n, e, a, b - a, 0, B).cpu().numpy()
+        ref = st.decode(blob[offs[a]:offs[b]], sizes[a:b], n, e, a, b - a, 0)
+        assert np.array_equal(got.view(np.uint8), ref.view(np.uint8)), (a, b)
+
+
 @pytest.mark.parametrize("dt,B,n", [(np.float64, 60, 300001), (np.float32, 32, 1 << 20)])
 def test_parse_many_chunks(dt, B, n):
     """one level large enough that the plane pipeline wraps its ring many
