@@ -644,6 +644,9 @@ def run_perbit(shape=(513, 513, 513), levels=7, planes=60, rels=(1e-3, 1e-5, 1e-
     lel = api.level_dims(shape, levels)[1]
     n_f = int(lel[levels])
     peak, peak_src = measured_peak()
+    stage_ms = {}
+    for (kind, _), (t, _) in st.items():
+        stage_ms[kind] = stage_ms.get(kind, 0.0) + t
     enc_ms = st[("encode", levels)][0]
     enc_bytes = n_f * 8 + n_f * (planes + 1) // 8
     dec_ms, dec_bytes = st[("decode", levels)][0], sum(n_f * (int(ix[levels]) + 1) // 8 + n_f * 8 for ix in idxs)
@@ -695,6 +698,7 @@ def run_perbit(shape=(513, 513, 513), levels=7, planes=60, rels=(1e-3, 1e-5, 1e-
                     ("x".join(map(str, shape)), levels + 1, planes, list(rels)),
         "step": {"ms": ms, "bytes": step_bytes, "gbs": step_bytes / ms / 1e6, "max_error_at_tightest": err,
                  "tightest_bound": rels[-1] * vr, "planes_per_level": [ix.tolist() for ix in idxs]},
+        "stage_ms": stage_ms,
         "encode_finest": {"ms": enc_ms, "bytes": enc_bytes, "gbs": enc_bytes / enc_ms / 1e6,
                           "frac": enc_bytes / enc_ms / 1e6 / peak,
                           "bytes_model": "n*8 read + n*(B+1)/8 rows written"},

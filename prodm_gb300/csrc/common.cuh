@@ -151,6 +151,25 @@ __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(
 // ---------------------------------------------------------------------------
 template <class T>
 __device__ __forceinline__ T avg_rn(T a, T b) { return mul_rn((T)0.5, add_rn(a, b)); }
+// x * 0.5 for doubles with integer operations (GB300's FP64 pipe is slow, its
+// integer pipes idle in these kernels): while the result is normal the
+// halving is exact and only the exponent field drops by one; zeros and
+// subnormal results take the significand halved with ties to even (what the
+// multiplication rounds to), Inf and NaN stay as they are
+static __device__ __noinline__ double half_rare(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if (((b >> 52) & 0x7ffu) == 0x7ffu) return x;
+    const unsigned long long sig = b & 0x1fffffffffffffull;   // hidden bit included when the field is 1
+    const unsigned long long q = sig >> 1;
+    return __longlong_as_double((long long)((b & 0x8000000000000000ull) | (q + (sig & q & 1ull))));
+}
+__device__ __forceinline__ double half_rn(double x) {
+    const int hi = __double2hiint(x);
+    const unsigned f = ((unsigned)hi >> 20) & 0x7ffu;
+    if (f - 2u < 0x7fdu) return __hiloint2double(hi - 0x100000, __double2loint(x));
+    return half_rare(x);
+}
+__device__ __forceinline__ double avg_rn(double a, double b) { return half_rn(__dadd_rn(a, b)); }
 template <class T>
 __device__ __forceinline__ T corner_tree(int m01, const T* q) {
     if (m01 == 0) return q[0];

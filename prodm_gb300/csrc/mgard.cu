@@ -30,8 +30,7 @@ namespace {
 // dims averaged with dim 0 outermost (the oracle uses the same order).
 template <class T, class Get>
 __device__ __forceinline__ T interp(int mask, Get at) {
-    const T h = (T)0.5;
-    auto avg = [&](T a, T b) { return mul_rn(h, add_rn(a, b)); };
+    auto avg = [&](T a, T b) { return avg_rn(a, b); };
     switch (mask) {
         case 1: return avg(at(-1, 0, 0), at(1, 0, 0));
         case 2: return avg(at(0, -1, 0), at(0, 1, 0));

@@ -119,7 +119,6 @@ __global__ void __launch_bounds__(256) k_pb_encode(const T* __restrict__ x, uint
     const uint64_t nch = (ng + PB_CHUNK - 1) / PB_CHUNK;
     for (int k = threadIdx.x; k < 64; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
-    uint32_t c_lo = 0, c_hi = 0;   // first-one counts of bit `lane` and bit 32 + lane
     for (uint64_t c = blockIdx.x; c < nch; c += gridDim.x) {
         const uint64_t g0 = c * PB_CHUNK;
 #pragma unroll 2
@@ -129,21 +128,14 @@ __global__ void __launch_bounds__(256) k_pb_encode(const T* __restrict__ x, uint
             const T v = i < n ? __ldcs(x + i) : (T)0;
             const FP m = pb_mag(v, ks, fast, sc);
             const uint32_t sgn = __ballot_sync(FULL, pb_neg(v) && m != 0);
+            // a value's first 1 bit is its most significant one: count the
+            // group's values per msb (one shared atomic per distinct msb)
+            const int msb = m ? (int)(8 * sizeof(FP)) - 1 - (sizeof(T) == 8 ? __clzll((long long)m) : __clz((int)m))
+                              : -1;
+            const unsigned same = __match_any_sync(FULL, msb);
+            if (msb >= 0 && lane == __ffs(same) - 1) atomicAdd(&cnt[B - 1 - msb], (uint32_t)__popc(same));
             const uint32_t lo = transpose32((uint32_t)m, lane);          // lane k: bit k of the 32 magnitudes
             const uint32_t hi = sizeof(T) == 8 ? transpose32((uint32_t)((uint64_t)m >> 32), lane) : 0u;
-            // OR of the words of all higher bits: first 1 bits = word & ~that
-            uint32_t s_lo = lo, s_hi = hi;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t t1 = __shfl_down_sync(FULL, s_lo, d);
-                const uint32_t t2 = __shfl_down_sync(FULL, s_hi, d);
-                if (lane + d < 32) { s_lo |= t1; s_hi |= t2; }
-            }
-            uint32_t ex_lo = __shfl_down_sync(FULL, s_lo, 1), ex_hi = __shfl_down_sync(FULL, s_hi, 1);
-            if (lane == 31) { ex_lo = 0; ex_hi = 0; }
-            ex_lo |= __shfl_sync(FULL, s_hi, 0);
-            c_lo += __popc(lo & ~ex_lo);
-            c_hi += __popc(hi & ~ex_hi);
             if (lane < B) tile[(B - 1 - lane) * PB_LD + gl] = lo;
             if (sizeof(T) == 8 && lane + 32 < B) tile[(B - 33 - lane) * PB_LD + gl] = hi;
             if (lane == 0) tile[B * PB_LD + gl] = sgn;
@@ -157,8 +149,6 @@ __global__ void __launch_bounds__(256) k_pb_encode(const T* __restrict__ x, uint
         }
         __syncthreads();
     }
-    if (lane < B && c_lo) atomicAdd(&cnt[B - 1 - lane], c_lo);
-    if (sizeof(T) == 8 && lane + 32 < B && c_hi) atomicAdd(&cnt[B - 33 - lane], c_hi);
     __syncthreads();
     for (int p = threadIdx.x; p < B; p += blockDim.x)
         if (cnt[p]) atomicAdd(&counts[p], cnt[p]);
@@ -177,13 +167,37 @@ __global__ void k_pb_sizes(const uint32_t* __restrict__ counts, int B, uint64_t 
 // `unseen` (row of elements without a 1 bit in planes < e) may be NULL when
 // s == 0: then "known" is "nonzero". dnum (device plane count) overrides e.
 // ---------------------------------------------------------------------------
+// the groups of one staged chunk; FAST: every value is normal (no FP64 path
+// in the loop)
+template <class T, bool FAST>
+__device__ __forceinline__ void pb_decode_groups(const uint32_t* tile, int num, int nvalid, uint64_t g0, uint64_t n,
+                                                 int vs, float sc, bool with_unseen, T* __restrict__ out) {
+    using FP = typename Traits<T>::FP;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 2
+    for (int j = 0; j < PB_GPW; j++) {
+        const int gl = warp * PB_GPW + j;
+        if (gl >= nvalid) break;
+        const uint32_t wl = lane < num ? tile[(num - 1 - lane) * PB_LD + gl] : 0u;
+        FP acc = transpose32(wl, lane);
+        if (sizeof(T) == 8 && num > 32) {
+            const uint32_t wh = lane + 32 < num ? tile[(num - 33 - lane) * PB_LD + gl] : 0u;
+            acc |= (FP)((uint64_t)transpose32(wh, lane) << 32);
+        }
+        const uint32_t sg = tile[num * PB_LD + gl];
+        const bool known = with_unseen ? !((tile[(num + 1) * PB_LD + gl] >> lane) & 1u) : acc != 0;
+        const T v = pb_value(acc, vs, FAST, sc);
+        const uint64_t i = (g0 + gl) * 32 + lane;
+        if (i < n) out[i] = (known && ((sg >> lane) & 1u)) ? pb_negate(v) : v;
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_pb_decode(const uint32_t* __restrict__ rows, uint64_t stride, uint64_t n,
                                                    const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg,
                                                    int s, int e, const uint8_t* __restrict__ dnum,
                                                    const uint32_t* __restrict__ srow,
                                                    const uint32_t* __restrict__ unseen, T* __restrict__ out) {
-    using FP = typename Traits<T>::FP;
     extern __shared__ uint32_t tile[];   // num + 2 rows x PB_LD
     if (dnum) e = dnum[0];
     const int num = e - s;
@@ -205,22 +219,8 @@ __global__ void __launch_bounds__(256) k_pb_decode(const uint32_t* __restrict__ 
             for (int j = lane; j < nvalid; j += 32) dst[j] = __ldcs(src + j);
         }
         __syncthreads();
-#pragma unroll 2
-        for (int j = 0; j < PB_GPW; j++) {
-            const int gl = warp * PB_GPW + j;
-            if (gl >= nvalid) break;
-            const uint32_t wl = lane < num ? tile[(num - 1 - lane) * PB_LD + gl] : 0u;
-            FP acc = transpose32(wl, lane);
-            if (sizeof(T) == 8 && num > 32) {
-                const uint32_t wh = lane + 32 < num ? tile[(num - 33 - lane) * PB_LD + gl] : 0u;
-                acc |= (FP)((uint64_t)transpose32(wh, lane) << 32);
-            }
-            const uint32_t sg = tile[num * PB_LD + gl];
-            const bool known = unseen ? !((tile[(num + 1) * PB_LD + gl] >> lane) & 1u) : acc != 0;
-            const T v = pb_value(acc, vs, fast, sc);
-            const uint64_t i = (g0 + gl) * 32 + lane;
-            if (i < n) out[i] = (known && ((sg >> lane) & 1u)) ? pb_negate(v) : v;
-        }
+        if (fast) pb_decode_groups<T, true>(tile, num, nvalid, g0, n, vs, sc, unseen != nullptr, out);
+        else pb_decode_groups<T, false>(tile, num, nvalid, g0, n, vs, sc, unseen != nullptr, out);
         __syncthreads();
     }
 }

@@ -5,7 +5,10 @@
 Runs `reps` refactor + progressive-retrieve steps of a seeded Gaussian random
 field (k^-5/3) with the benchmark's component set (NegaBinary, 32 planes,
 hierarchical basis, squared-error tables, relative L2 tolerances 1e-2..1e-6)
-and prints per-stage CUDA-event times of the last step.
+and prints per-stage CUDA-event times of the last step. With --encoder perbit
+the step is the GE applications' configuration instead: a seeded fp64 tanh
+shear layer (+1e-6 relative noise), 60 planes, max collector, SignExclude
+interpreter with MaxErrorEstimatorHB, relative L-inf tolerances 1e-3..1e-9.
 """
 import argparse
 import math
@@ -25,6 +28,8 @@ def main():
     a = ap.parse_args()
     shape = (a.shape,) * 3
     L = a.levels if a.levels is not None else min(7, api.max_level(shape))
+    if a.encoder == "perbit":
+        return perbit(shape, L, a.reps)
     x = fields.spectral_grf(shape, seed=3)
     norm2 = float((x.double() ** 2).sum().item())
     mdr = api.MDRField(shape, torch.float32, L, 32, a.encoder, a.basis, "squared")
@@ -42,6 +47,24 @@ def main():
     for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
         print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
     print("final relative L2 error %.3g" % err)
+
+
+def perbit(shape, L, reps):
+    x = fields.shear_layer(shape, delta=0.05, noise_rel=1e-6, seed=21, dtype=torch.float64, device="cuda")
+    vr = float((x.max() - x.min()).item())
+    mdr = api.MDRField(shape, torch.float64, L, 60, "perbit", "hierarchical", "max")
+    out = torch.empty_like(x)
+    for r in range(reps):
+        if r == reps - 1:
+            mdr.set_timing(True)
+        mdr.refactor(x)
+        mdr.reset()
+        for rel in (1e-3, 1e-5, 1e-7, 1e-9):
+            mdr.retrieve(rel * vr, out=out, interpreter="sign_exclude", estimator="max_hb")
+    torch.cuda.synchronize()
+    for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
+        print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
+    print("final max error %.3g of range %.3g" % (float((out - x).abs().max().item()), vr))
 
 
 if __name__ == "__main__":
