@@ -136,6 +136,29 @@ int prodm_progressive_decode(prodm_decoder* h, const void* d_blob, const uint32_
 int prodm_decoder_destroy(prodm_decoder* h);
 
 /* ---------------------------------------------------------------------------
+ * Lossless stage -- LevelCompressorInterface::compress_level / decompress_level
+ * (LevelCompressorInterface.hpp:14-18) with AdaptiveLevelCompressor's rule
+ * (AdaptiveLevelCompressor.hpp:13-53: planes 0..stopping and those from
+ * max(latter, stopping + 1) on are compressed; the run stops at the first
+ * plane after plane 0 whose ratio raw/compressed is below 1.05). The codec is
+ * this library's GPU codec "ZCB" (zero-compacted bytes: u64 raw length, u32
+ * chunk count, chunk end offsets, then per 4096-byte chunk 32 word masks, a
+ * nibble of nonzero bytes per nonzero word and the nonzero bytes), not zstd:
+ * files compressed by the reference's zstd stage are not readable with it.
+ * d_blob: the level's streams concatenated (raw for compress, stored for
+ * decompress); h_sizes: their byte sizes (host; for decompress the sizes of
+ * planes [starting_bitplane, +num)). Outputs are concatenated into d_out;
+ * h_out_sizes / h_raw_sizes receive the per-stream sizes (host).
+ * ------------------------------------------------------------------------- */
+int prodm_lossless_compress_bound(const uint32_t* h_sizes, int num_bitplanes, uint64_t* max_bytes);
+int prodm_lossless_compress_level(const void* d_blob, const uint32_t* h_sizes, int num_bitplanes, int latter_index,
+                                  void* d_out, uint64_t capacity, uint32_t* h_out_sizes, int* h_stopping_index,
+                                  void* stream);
+int prodm_lossless_decompress_level(const void* d_blob, const uint32_t* h_sizes, int starting_bitplane,
+                                    int num_bitplanes, int stopping_index, int latter_index, void* d_out,
+                                    uint64_t capacity, uint32_t* h_raw_sizes, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Error collectors -- ErrorCollectorInterface<T>::collect_level_error
  * (ErrorCollectorInterface.hpp:14). Max: MaxErrorCollector.hpp:14-25 (needs
  * no data; host output). Squared: SquaredErrorCollector.hpp:54-96 (device

@@ -125,6 +125,31 @@ class Oracle(_Lib):
         total = f(np.ascontiguousarray(data), n, int(exp), int(B), blob, sizes)
         return blob[:total].copy(), sizes
 
+    # lossless stage ------------------------------------------------------
+    def adaptive_stopping(self, raw_sizes, comp_sizes, latter=26):
+        """(stopping index, compressed flags) of AdaptiveLevelCompressor's rule."""
+        raw = np.ascontiguousarray(raw_sizes, np.uint32)
+        comp = np.ascontiguousarray(comp_sizes, np.uint32)
+        flags = np.zeros(len(raw), np.uint8)
+        f = self._fn("or_adaptive_stopping", C.c_int, _u32p, _u32p, C.c_int, C.c_int, _u8p)
+        return f(raw, comp, len(raw), int(latter), flags), flags
+
+    def zcb_compress(self, raw):
+        raw = np.ascontiguousarray(raw, np.uint8)
+        size = self._fn("or_zcb_size", C.c_uint64, _u8p, C.c_uint64)(raw, raw.size)
+        out = np.zeros(max(int(size), 1), np.uint8)
+        n = self._fn("or_zcb_compress", C.c_uint64, _u8p, C.c_uint64, _u8p)(raw, raw.size, out)
+        assert n == size
+        return out[:n]
+
+    def zcb_decompress(self, comp, cap):
+        comp = np.ascontiguousarray(comp, np.uint8)
+        out = np.zeros(max(int(cap), 1), np.uint8)
+        n = self._fn("or_zcb_decompress", C.c_int64, _u8p, C.c_uint64, _u8p, C.c_uint64)(comp, comp.size, out, cap)
+        if n < 0:
+            raise ValueError("malformed ZCB stream")
+        return out[:n]
+
     def perbit_state(self, dtype):
         """Stateful PerBit progressive decoder (one per encoder object)."""
         return _PerBitState(self, dtype)
@@ -356,6 +381,16 @@ class Reference(Oracle):
         out = np.zeros(B + 1, np.float64)
         f(np.ascontiguousarray(data), len(data), B, maxv, out)
         return out
+
+    def adaptive_compress(self, blob, sizes, latter=26):
+        """The reference's AdaptiveLevelCompressor (zstd level 3) on one level's
+        streams: (stopping index, sizes it leaves, zstd size of every stream)."""
+        B = len(sizes)
+        out = np.zeros(B, np.uint32)
+        zs = np.zeros(B, np.uint32)
+        f = self._fn("ref_adaptive_compress", C.c_int, _u8p, _u32p, C.c_int, C.c_int, _u32p, _u32p)
+        stop = f(np.ascontiguousarray(blob, np.uint8), np.ascontiguousarray(sizes, np.uint32), B, int(latter), out, zs)
+        return stop, out, zs
 
     def composed(self, field, L, B, encoder, hierarchical, tols, workdir):
         dims = np.asarray(field.shape, np.uint32)

@@ -110,6 +110,15 @@ extern "C" {
 
 int or_max_level(int ndims, const uint32_t* dims) { return max_level(vec(dims, ndims)); }
 
+int or_adaptive_stopping(const uint32_t* raw, const uint32_t* comp, int B, int latter, uint8_t* compressed) {
+    return adaptive_stopping(raw, comp, B, latter, compressed);
+}
+uint64_t or_zcb_size(const uint8_t* raw, uint64_t n) { return zcb_size(raw, n); }
+uint64_t or_zcb_compress(const uint8_t* raw, uint64_t n, uint8_t* out) { return zcb_compress(raw, n, out); }
+int64_t or_zcb_decompress(const uint8_t* in, uint64_t len, uint8_t* raw, uint64_t cap) {
+    return zcb_decompress(in, len, raw, cap);
+}
+
 void or_level_dims(int ndims, const uint32_t* dims, int L, uint32_t* out) {
     auto ld = level_dims(vec(dims, ndims), L);
     for (int l = 0; l <= L; l++) for (int d = 0; d < ndims; d++) out[l * ndims + d] = ld[l][d];

@@ -463,6 +463,132 @@ void pb_decode(PerBitState& st, const uint8_t* const* planes, size_t n, int exp,
 }
 
 // ---------------------------------------------------------------------------
+// Lossless stage.
+// AdaptiveLevelCompressor::compress_level (AdaptiveLevelCompressor.hpp:13-40)
+// with the compressed sizes given: planes 0..stopping are compressed (the
+// first plane after plane 0 whose ratio raw/compressed, taken as a float, is
+// below 1.05 stops the run and stays compressed), the next ones stay raw,
+// and planes from max(latter, stopping + 1) on are compressed again.
+// Returns the stopping index (B if no plane stops the run); compressed[p] = 1
+// where plane p is stored compressed.
+inline int adaptive_stopping(const uint32_t* raw, const uint32_t* comp, int B, int latter, uint8_t* compressed) {
+    int stopping = B;
+    for (int p = 0; p < B; p++) compressed[p] = 0;
+    for (int i = 0; i < B; i++) {
+        const float ratio = (float)(raw[i] * 1.0 / comp[i]);
+        compressed[i] = 1;
+        if (i && ratio < 1.05) { stopping = i; break; }
+    }
+    const int start = stopping < latter ? latter : stopping + 1;
+    for (int i = start; i < B; i++) compressed[i] = 1;
+    return stopping;
+}
+
+// The device codec of the lossless stage (format "ZCB", zero-compacted
+// bytes; this project's own, not zstd): the raw stream as 4096-byte chunks of
+// 32-bit words (the last word zero-padded)
+//   u64 raw length | u32 chunk count C | u32 end offset of each chunk's data
+//   (relative to the end of this table) | chunk data
+// chunk data: 32 u32 word masks (bit k of mask m: word 32m+k nonzero), then a
+// 4-bit byte mask per nonzero word (bit b: byte b nonzero; 8 per u32, in word
+// order, padded to a u32), then the nonzero bytes in order, padded to 4 bytes.
+inline size_t zcb_size(const uint8_t* raw, size_t n) {
+    const size_t nch = (n + 4095) / 4096;
+    size_t total = 12 + 4 * nch;
+    for (size_t c = 0; c < nch; c++) {
+        size_t nzw = 0, nzb = 0;
+        for (size_t b = 4096 * c; b < n && b < 4096 * (c + 1); b += 4) {
+            bool any = false;
+            for (size_t k = b; k < b + 4 && k < n; k++)
+                if (raw[k]) { any = true; nzb++; }
+            nzw += any;
+        }
+        total += 128 + 4 * ((nzw + 7) / 8) + 4 * ((nzb + 3) / 4);
+    }
+    return total;
+}
+inline size_t zcb_compress(const uint8_t* raw, size_t n, uint8_t* out) {
+    const size_t nch = (n + 4095) / 4096;
+    const uint64_t n64 = n;
+    std::memcpy(out, &n64, 8);
+    const uint32_t c32 = (uint32_t)nch;
+    std::memcpy(out + 8, &c32, 4);
+    uint8_t* data = out + 12 + 4 * nch;
+    size_t pos = 0;
+    for (size_t c = 0; c < nch; c++) {
+        uint32_t masks[32] = {0};
+        std::vector<uint32_t> nib;
+        std::vector<uint8_t> bytes;
+        size_t nzw = 0;
+        for (size_t w = 0; w < 1024; w++) {
+            const size_t b = 4096 * c + 4 * w;
+            uint32_t bm = 0;
+            for (size_t k = 0; k < 4; k++)
+                if (b + k < n && raw[b + k]) { bm |= 1u << k; bytes.push_back(raw[b + k]); }
+            if (bm) {
+                masks[w / 32] |= 1u << (w % 32);
+                if (nzw % 8 == 0) nib.push_back(0);
+                nib.back() |= bm << (4 * (nzw % 8));
+                nzw++;
+            }
+        }
+        while (bytes.size() % 4) bytes.push_back(0);
+        std::memcpy(data + pos, masks, 128);
+        pos += 128;
+        if (!nib.empty()) std::memcpy(data + pos, nib.data(), 4 * nib.size());
+        pos += 4 * nib.size();
+        if (!bytes.empty()) std::memcpy(data + pos, bytes.data(), bytes.size());
+        pos += bytes.size();
+        const uint32_t end = (uint32_t)pos;
+        std::memcpy(out + 12 + 4 * c, &end, 4);
+    }
+    return 12 + 4 * nch + pos;
+}
+// returns the raw length, or -1 for a malformed stream of `len` bytes
+inline int64_t zcb_decompress(const uint8_t* in, size_t len, uint8_t* raw, size_t cap) {
+    if (len < 12) return -1;
+    uint64_t n;
+    uint32_t nch;
+    std::memcpy(&n, in, 8);
+    std::memcpy(&nch, in + 8, 4);
+    if (nch != (n + 4095) / 4096 || n > cap || len < 12 + 4 * (size_t)nch) return -1;
+    const uint8_t* data = in + 12 + 4 * (size_t)nch;
+    const size_t dlen = len - 12 - 4 * (size_t)nch;
+    uint32_t start = 0;
+    for (uint32_t c = 0; c < nch; c++) {
+        uint32_t end;
+        std::memcpy(&end, in + 12 + 4 * c, 4);
+        if (end < start + 128 || end > dlen) return -1;
+        const uint8_t* d = data + start;
+        uint32_t masks[32];
+        std::memcpy(masks, d, 128);
+        size_t nzw = 0;
+        for (int m = 0; m < 32; m++) nzw += __builtin_popcount(masks[m]);
+        const uint8_t* nibp = d + 128;
+        const uint8_t* bp = nibp + 4 * ((nzw + 7) / 8);
+        size_t ord = 0, bi = 0;
+        for (size_t w = 0; w < 1024; w++) {
+            uint32_t word = 0;
+            if ((masks[w / 32] >> (w % 32)) & 1u) {
+                uint32_t nw;
+                std::memcpy(&nw, nibp + 4 * (ord / 8), 4);
+                const uint32_t bm = (nw >> (4 * (ord % 8))) & 15u;
+                for (int k = 0; k < 4; k++)
+                    if ((bm >> k) & 1u) {
+                        if ((size_t)(bp - data) + bi >= end) return -1;
+                        word |= (uint32_t)bp[bi++] << (8 * k);
+                    }
+                ord++;
+            }
+            const size_t b = 4096 * (size_t)c + 4 * w;
+            for (size_t k = 0; k < 4 && b + k < n; k++) raw[b + k] = (uint8_t)(word >> (8 * k));
+        }
+        start = end;
+    }
+    return (int64_t)n;
+}
+
+// ---------------------------------------------------------------------------
 // Error collectors.
 // ---------------------------------------------------------------------------
 // MaxErrorCollector::collect_level_error -- MaxErrorCollector.hpp:14-25.

@@ -22,6 +22,7 @@
 #include "MDR/ErrorEstimator/ErrorEstimator.hpp"
 #include "MDR/SizeInterpreter/SizeInterpreter.hpp"
 #include "MDR/Refactor/Refactor.hpp"
+#include "MDR/LosslessCompressor/AdaptiveLevelCompressor.hpp"
 #include "MDR/Reconstructor/Reconstructor.hpp"
 #include "qoi_utils.hpp"
 
@@ -231,6 +232,28 @@ REF_T(f64, double, uint64_t)
 
 REF_PB(f32, float)
 REF_PB(f64, double)
+
+// AdaptiveLevelCompressor (zstd, level 3) on B streams concatenated in blob:
+// returns the stopping index; out_sizes = the sizes it leaves (compressed or
+// raw); zstd_sizes = ZSTD::compress's size of every stream on its own
+int ref_adaptive_compress(const uint8_t* blob, const uint32_t* sizes, int B, int latter, uint32_t* out_sizes,
+                          uint32_t* zstd_sizes) {
+    std::vector<uint8_t*> st(B);
+    std::vector<uint32_t> sz(sizes, sizes + B);
+    size_t o = 0;
+    for (int p = 0; p < B; p++) {
+        st[p] = (uint8_t*)malloc(sizes[p] ? sizes[p] : 1);
+        std::memcpy(st[p], blob + o, sizes[p]);
+        uint8_t* c = nullptr;
+        zstd_sizes[p] = MDR::ZSTD::compress(blob + o, sizes[p], &c);
+        free(c);
+        o += sizes[p];
+    }
+    MDR::AdaptiveLevelCompressor comp(latter);
+    const int stop = comp.compress_level(st, sz);
+    for (int p = 0; p < B; p++) { out_sizes[p] = sz[p]; free(st[p]); }
+    return stop;
+}
 
 // GE quantities of interest (qoi_utils.hpp:135-165) and the pointwise error
 // estimates the GE retrieval drivers form with the propagation rules of

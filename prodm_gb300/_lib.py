@@ -63,6 +63,9 @@ _SIGS = {
     "prodm_qoi_ge_values": (_i, [_i, _P, _P, _P, _P, _P, C.c_uint64, _P, _P, _P, _P, _P, _P, _P]),
     "prodm_qoi_ge_bounds": (_i, [_i, _P, _P, _P, _P, _P, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, _P, _P, _P, _P]),
+    "prodm_lossless_compress_bound": (_i, [_u32p, _i, _u64p]),
+    "prodm_lossless_compress_level": (_i, [_P, _u32p, _i, _i, _P, C.c_uint64, _u32p, C.POINTER(_i), _P]),
+    "prodm_lossless_decompress_level": (_i, [_P, _u32p, _i, _i, _i, _i, _P, C.c_uint64, _u32p, _P]),
     "prodm_interpret": (_i, [_i, _i, _i, _i, _i, C.c_double, _i, _i, _P, _P, C.c_double, _P, _P, _P]),
     "prodm_mdr_create": (_i, [C.POINTER(_P), C.POINTER(prodm_config)]),
     "prodm_mdr_refactor": (_i, [_P, _P, _P]),

@@ -105,6 +105,34 @@ def encode(kind, data, exp, num_bitplanes, collect=False, stream=None):
     return blob[:total], sz, (errs.cpu().numpy() if collect else None)
 
 
+def compress_level(blob, sizes, latter_index=26, stream=None):
+    """The lossless stage on one level's streams (device uint8 tensor, sizes):
+    returns (stored streams as a device uint8 tensor, their sizes, stopping index)."""
+    B = len(sizes)
+    hs = (C.c_uint32 * B)(*[int(x) for x in sizes])
+    bound = C.c_uint64()
+    call("prodm_lossless_compress_bound", hs, B, C.byref(bound))
+    out = torch.empty(max(bound.value, 1), dtype=torch.uint8, device=blob.device)
+    osz = (C.c_uint32 * B)()
+    stop = C.c_int()
+    call("prodm_lossless_compress_level", _ptr(blob), hs, B, int(latter_index), _ptr(out), bound.value, osz,
+         C.byref(stop), _stream(stream))
+    sz = np.array(osz[:], np.uint32)
+    return out[:int(sz.astype(np.int64).sum())], sz, stop.value
+
+
+def decompress_level(blob, sizes, start, num, stopping_index, latter_index=26, raw_capacity=None, stream=None):
+    """Stored streams of planes [start, start+num) -> (raw streams concatenated, raw sizes)."""
+    hs = (C.c_uint32 * max(num, 1))(*[int(x) for x in sizes[:num]])
+    cap = int(raw_capacity) if raw_capacity is not None else 64 * max(int(blob.numel()), 1)
+    out = torch.empty(max(cap, 1), dtype=torch.uint8, device=blob.device)
+    rsz = (C.c_uint32 * max(num, 1))()
+    call("prodm_lossless_decompress_level", _ptr(blob), hs, int(start), int(num), int(stopping_index),
+         int(latter_index), _ptr(out), cap, rsz, _stream(stream))
+    r = np.array(rsz[:num], np.uint32)
+    return out[:int(r.astype(np.int64).sum())], r
+
+
 class ProgressiveDecoder:
     """Stateful decoder (grouped state per level), BitplaneEncoderInterface::progressive_decode."""
 

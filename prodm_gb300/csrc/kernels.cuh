@@ -115,6 +115,33 @@ size_t pb_parse_scratch_bytes(int np);
 int launch_pb_parse(const uint64_t* const* planes, const uint64_t* nwords, int a, int np, uint64_t n, uint32_t* rows,
                     uint64_t stride, uint32_t* unseen, uint32_t* signs, void* scratch, int* status, cudaStream_t st);
 
+// lossless.cu: ZCB codec, one descriptor per stream; chunk0 = the stream's
+// first chunk in the flattened chunk index (sorted), clen = compressed length
+struct ZStream {
+    const uint8_t* src;
+    uint8_t* dst;
+    uint64_t len;
+    uint64_t clen;
+    uint64_t chunk0;
+};
+uint64_t zcb_bound(uint64_t len);
+int launch_zcb_count(const ZStream* d_ss, int ns, uint64_t total_chunks, uint32_t* csize, uint32_t* coff,
+                     uint32_t* out_sizes, cudaStream_t st);
+int launch_zcb_write(const ZStream* d_ss, int ns, uint64_t total_chunks, const uint32_t* csize, const uint32_t* coff,
+                     cudaStream_t st);
+int launch_zcb_read(const ZStream* d_ss, int ns, uint64_t total_chunks, int* status, cudaStream_t st);
+int adaptive_stopping(const uint32_t* raw, const uint32_t* comp, int B, int latter, uint8_t* compressed);
+// one level's streams (device, concatenated, raw sizes h_sizes) -> stored
+// streams (compressed where flags say, else raw) concatenated into d_out
+int ll_compress_level(const uint8_t* d_raw, const uint32_t* h_sizes, int B, int latter, uint8_t* d_out,
+                      uint64_t cap, uint32_t* h_out_sizes, int* h_stop, const uint8_t* h_flags, cudaStream_t st);
+// compressed sizes of every stream (the ZCB size; no output written)
+int ll_stream_sizes(const uint8_t* d_raw, const uint32_t* h_sizes, int B, uint32_t* h_comp, cudaStream_t st);
+// stored streams of `num` planes (sizes h_sizes, flags) -> raw streams
+// concatenated into d_out (capacity cap); h_raw_sizes: their raw sizes
+int ll_decompress_planes(const uint8_t* d_in, const uint32_t* h_sizes, const uint8_t* h_flags, int num, uint8_t* d_out,
+                         uint64_t cap, uint32_t* h_raw_sizes, cudaStream_t st);
+
 // pack.cu
 int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,
                    int word_bytes, uint8_t* dst, cudaStream_t st);

@@ -3,7 +3,7 @@
 Runs only where the reference tree is present: the reference's MDR headers are
 compiled by oracle/build_oracle.build_ref (oracle/_ref/libprodm_ref.so) and
 every fixture below is produced by calling the reference's own classes
-(NegaBinaryBPEncoder, GroupedBPEncoder, PerBitBPEncoder, MaxErrorCollector,
+(NegaBinaryBPEncoder, GroupedBPEncoder, PerBitBPEncoder, AdaptiveLevelCompressor, MaxErrorCollector,
 SquaredErrorCollector, the greedy size interpreters, DirectInterleaver,
 compute_level_dims/elements and the ComposedRefactor -> ComposedReconstructor
 pair). Inputs are seeded and stored beside the outputs so that the fixtures
@@ -206,6 +206,31 @@ def qoi_fixtures(R, rng):
     return out
 
 
+def lossless_fixtures(R, rng):
+    """AdaptiveLevelCompressor (zstd level 3) on the encoder and per-bit fixture
+    levels (read from encoders.npz / perbit.npz): its stopping index, the sizes
+    it leaves and every stream's zstd size, for latter indices 26 (default),
+    3 and 40."""
+    out = {}
+    cases = []
+    for name in ("encoders", "perbit"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        for c in g["cases"]:
+            c = str(c)
+            blob, sizes = g[c + "_blob"], g[c + "_sizes"]
+            for latter in (26, 3, 40):
+                stop, left, zs = R.adaptive_compress(blob, sizes, latter)
+                key = "%s_%s_L%d" % (name, c, latter)
+                out[key + "_raw"] = sizes
+                out[key + "_zstd"] = zs
+                out[key + "_left"] = left
+                out[key + "_stop"] = np.int32(stop)
+                out[key + "_latter"] = np.int32(latter)
+                cases.append(key)
+    out["cases"] = np.array(cases)
+    return out
+
+
 PB_N = (1, 2, 31, 32, 33, 63, 64, 65, 95, 127, 729, 4184)
 
 
@@ -266,9 +291,10 @@ def perbit_fixtures(R, rng):
 
 FIXTURES = (("encoders", encoder_fixtures), ("collectors", collector_fixtures),
             ("interpreters", interpreter_fixtures), ("geometry", geometry_fixtures),
-            ("composed", composed_fixtures), ("qoi", qoi_fixtures), ("perbit", perbit_fixtures))
+            ("composed", composed_fixtures), ("qoi", qoi_fixtures), ("perbit", perbit_fixtures),
+            ("lossless", lossless_fixtures))
 
-OWN_SEED = {"qoi": 20241203, "perbit": 20241204}   # fixtures with their own random stream
+OWN_SEED = {"qoi": 20241203, "perbit": 20241204, "lossless": 0}   # fixtures with their own random stream
 
 
 def main(names=None):

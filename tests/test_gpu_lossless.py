@@ -1,0 +1,105 @@
+"""Lossless stage on the device (prodm_lossless_*): the ZCB codec and
+AdaptiveLevelCompressor's stopping rule against the oracle.
+
+* every encoder / per-bit fixture level: the device's stopping index equals
+  the oracle rule on the oracle codec's sizes, the stored bytes equal the
+  oracle's (compressed planes bit for bit, the others raw), and decoding the
+  stored planes in two calls gives the raw streams back;
+* larger sparse and dense planes, input at an odd byte offset;
+* malformed stored streams are rejected.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+O = oracle.oracle()
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def api():
+    from prodm_gb300 import api as a
+    return a
+
+
+def levels():
+    out = []
+    for name in ("encoders", "perbit"):
+        g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+        for c in list(g["cases"])[::3]:
+            out.append((name, str(c)))
+    return out
+
+
+def expected(blob, sizes, latter):
+    offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+    comp = [O.zcb_compress(blob[offs[p]:offs[p + 1]]) for p in range(len(sizes))]
+    stop, flags = O.adaptive_stopping(sizes, [c.size for c in comp], latter)
+    parts = [comp[p] if flags[p] else blob[offs[p]:offs[p + 1]] for p in range(len(sizes))]
+    return stop, flags, np.concatenate(parts) if parts else np.zeros(0, np.uint8), \
+        np.array([p.size for p in parts], np.uint32)
+
+
+@pytest.mark.parametrize("name,case", levels())
+@pytest.mark.parametrize("latter", [26, 3])
+def test_level_matches_oracle_and_round_trips(name, case, latter):
+    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    blob, sizes = g[case + "_blob"], g[case + "_sizes"]
+    stop, flags, stored, ssz = expected(blob, sizes, latter)
+    out, osz, dstop = api().compress_level(torch.from_numpy(blob).cuda(), sizes, latter)
+    assert dstop == stop
+    assert np.array_equal(osz, ssz)
+    assert np.array_equal(out.cpu().numpy(), stored)
+    B = len(sizes)
+    s1 = max(1, B // 2)
+    offs = np.concatenate([[0], np.cumsum(osz.astype(np.int64))])
+    raw_offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+    for a, b in ((0, s1), (s1, B)):
+        raw, rsz = api().decompress_level(out[offs[a]:offs[b]], osz[a:b], a, b - a, dstop, latter,
+                                          raw_capacity=int(raw_offs[b] - raw_offs[a]) + 16)
+        assert np.array_equal(rsz, sizes[a:b])
+        assert np.array_equal(raw.cpu().numpy(), blob[raw_offs[a]:raw_offs[b]])
+
+
+@pytest.mark.parametrize("n", [1, 4095, 4096, 4097, 3 * 1024 * 1024 + 5])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_large_planes_and_odd_offsets(n, offset):
+    rng = np.random.default_rng(n + offset)
+    planes = []
+    for dens in (0.0, 0.0005, 0.02, 0.3, 1.0):
+        planes.append(((rng.random(n) < dens) * rng.integers(1, 256, n)).astype(np.uint8))
+    sizes = np.array([p.size for p in planes], np.uint32)
+    blob = np.concatenate(planes)
+    stop, flags, stored, ssz = expected(blob, sizes, 26)
+    buf = torch.zeros(blob.size + offset, dtype=torch.uint8, device="cuda")
+    buf[offset:] = torch.from_numpy(blob).cuda()
+    out, osz, dstop = api().compress_level(buf[offset:], sizes, 26)
+    assert dstop == stop and np.array_equal(osz, ssz)
+    assert np.array_equal(out.cpu().numpy(), stored)
+    raw, rsz = api().decompress_level(out, osz, 0, len(sizes), dstop, 26, raw_capacity=blob.size + 16)
+    assert np.array_equal(raw.cpu().numpy(), blob)
+
+
+def test_malformed_streams_rejected():
+    from prodm_gb300._lib import ProdmError
+    raw = (np.arange(20000) % 7 == 0).astype(np.uint8)
+    comp = O.zcb_compress(raw)
+    d = torch.from_numpy(comp).cuda()
+    with pytest.raises(ProdmError):                       # shorter than its header
+        api().decompress_level(d[:8], [8], 0, 1, 5, 26, raw_capacity=30000)
+    bad = comp.copy()
+    bad[8] = 99                                           # chunk count does not match the length
+    with pytest.raises(ProdmError):
+        api().decompress_level(torch.from_numpy(bad).cuda(), [bad.size], 0, 1, 5, 26, raw_capacity=30000)
+    bad = comp.copy()
+    bad[12:16] = 0                                        # first chunk ends before its masks
+    with pytest.raises(ProdmError):
+        api().decompress_level(torch.from_numpy(bad).cuda(), [bad.size], 0, 1, 5, 26, raw_capacity=30000)
+    with pytest.raises(ProdmError):                       # truncated data area
+        api().decompress_level(d[:comp.size - 200], [comp.size - 200], 0, 1, 5, 26, raw_capacity=30000)
+    raw2, _ = api().decompress_level(d, [comp.size], 0, 1, 5, 26, raw_capacity=30000)
+    assert np.array_equal(raw2.cpu().numpy(), raw)

@@ -178,3 +178,32 @@ def test_perbit_composed_level_files_and_retrieval_match_reference():
         planes = sum(int(sz[l, :idx[l]].sum()) for l in range(L + 1))
         assert planes == int(g["composed_retrieved"][t]), t
         np.testing.assert_allclose(rec, g["composed_recon"][t], atol=1e-12 * float(np.abs(field).max()), rtol=0)
+
+
+def test_adaptive_stopping_rule_matches_reference():
+    """AdaptiveLevelCompressor's rule restated (oracle) on the reference's own
+    zstd sizes: same stopping index, same sizes left, on every fixture level
+    and latter index"""
+    g = load("lossless")
+    for key in g["cases"]:
+        key = str(key)
+        raw, zs = g[key + "_raw"], g[key + "_zstd"]
+        stop, flags = O.adaptive_stopping(raw, zs, int(g[key + "_latter"]))
+        assert stop == int(g[key + "_stop"]), key
+        assert np.array_equal(np.where(flags == 1, zs, raw), g[key + "_left"]), key
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 4, 5, 4095, 4096, 4097, 12289])
+def test_zcb_codec_round_trip(n):
+    """the lossless stage's codec (oracle restatement): every density round
+    trips; all-zero data keeps only the header and each chunk's word masks"""
+    rng = np.random.default_rng(n)
+    for dens in (0.0, 0.001, 0.05, 0.5, 1.0):
+        raw = ((rng.random(n) < dens) * rng.integers(1, 256, n)).astype(np.uint8)
+        comp = O.zcb_compress(raw)
+        assert np.array_equal(O.zcb_decompress(comp, n), raw)
+        if dens == 0.0:
+            nch = (n + 4095) // 4096
+            assert comp.size == 12 + 4 * nch + 128 * nch
+    with pytest.raises(ValueError):
+        O.zcb_decompress(np.zeros(11, np.uint8), 100)
