@@ -265,6 +265,20 @@ int prodm_mdr_metadata(prodm_mdr* h, uint8_t* h_buf, size_t capacity, size_t* le
 /* reference level-file bytes of one level into dst (device or host). */
 int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t capacity, int dst_is_host, uint64_t* len,
                            void* stream);
+
+/* Lossless stage of the handle (AdaptiveLevelCompressor's rule with the ZCB
+ * codec, see prodm_lossless_compress_level): latter_index >= 0 switches it on
+ * (the reference's default is 26), < 0 off. While on, the plane sizes the
+ * interpreter uses, prodm_mdr_level_info reports and the metadata carries are
+ * the stored (compressed where the rule says) sizes, exactly as the
+ * reference's ComposedRefactor records them after compress_level
+ * (ComposedRefactor.hpp:131-135); the planes stay uncompressed in HBM;
+ * prodm_mdr_export_level writes the stored streams and the metadata the
+ * stopping indices plus a "ZCB1" marker with the latter index. A handle fed by
+ * prodm_mdr_load_metadata takes the stage from the metadata; levels whose
+ * metadata has stopping indices but no marker (the reference's zstd stage)
+ * return PRODM_EUNSUPPORTED. */
+int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream);
 int prodm_mdr_retrieve(prodm_mdr* h, double tolerance, int interpreter, int estimator, double s, void* d_out,
                        void* stream);
 /* the two halves of prodm_mdr_retrieve: the interpreter alone (updates the

@@ -429,6 +429,99 @@ class GpuPerBitBPEncoder PRODM_BASE(MDR::concepts::BitplaneEncoderInterface<T>) 
 };
 
 // ---------------------------------------------------------------------------
+// Lossless stage: AdaptiveLevelCompressor's rule (AdaptiveLevelCompressor.hpp:
+// 13-60) with this library's GPU codec ZCB instead of zstd (files of the
+// reference's zstd stage are not readable with it)
+// ---------------------------------------------------------------------------
+class GpuAdaptiveLevelCompressor PRODM_BASE(MDR::concepts::LevelCompressorInterface) {
+  public:
+    explicit GpuAdaptiveLevelCompressor(int latter = 26) : latter_(latter) {}
+    GpuAdaptiveLevelCompressor(const GpuAdaptiveLevelCompressor& o) : latter_(o.latter_) {}
+    GpuAdaptiveLevelCompressor& operator=(const GpuAdaptiveLevelCompressor& o) {
+        latter_ = o.latter_;
+        return *this;
+    }
+    ~GpuAdaptiveLevelCompressor() { decompress_release(); }
+
+    uint8_t compress_level(std::vector<uint8_t*>& streams, std::vector<uint32_t>& stream_sizes) const {
+        const int B = (int)stream_sizes.size();
+        size_t total = 0;
+        for (auto x : stream_sizes) total += x;
+        std::vector<uint8_t> host(total);
+        size_t o = 0;
+        for (int p = 0; p < B; p++) { std::memcpy(host.data() + o, streams[p], stream_sizes[p]); o += stream_sizes[p]; }
+        uint64_t cap = 0;
+        check(prodm_lossless_compress_bound(stream_sizes.data(), B, &cap), "prodm_lossless_compress_bound");
+        DeviceBuffer in(total + 16), out(cap + 16);
+        cuda_check(cudaMemcpy(in.get(), host.data(), total, cudaMemcpyHostToDevice), "H2D");
+        std::vector<uint32_t> osz(B);
+        int stop = 0;
+        check(prodm_lossless_compress_level(in.get(), stream_sizes.data(), B, latter_, out.get(), cap, osz.data(), &stop,
+                                            nullptr),
+              "prodm_lossless_compress_level");
+        size_t ot = 0;
+        for (auto x : osz) ot += x;
+        std::vector<uint8_t> res(ot);
+        cuda_check(cudaMemcpy(res.data(), out.get(), ot, cudaMemcpyDeviceToHost), "D2H");
+        o = 0;
+        for (int p = 0; p < B; p++) {   // overwrite and free the original streams (LevelCompressorInterface.hpp:13)
+            std::free(streams[p]);
+            streams[p] = (uint8_t*)std::malloc(osz[p] ? osz[p] : 1);
+            std::memcpy(streams[p], res.data() + o, osz[p]);
+            stream_sizes[p] = osz[p];
+            o += osz[p];
+        }
+        return (uint8_t)stop;
+    }
+    void decompress_level(std::vector<const uint8_t*>& streams, const std::vector<uint32_t>& stream_sizes,
+                          uint8_t starting_bitplane, uint8_t num_bitplanes, uint8_t stopping_index) {
+        if (!num_bitplanes) return;
+        std::vector<uint32_t> sz(num_bitplanes);
+        size_t total = 0, raw = 0;
+        for (int i = 0; i < num_bitplanes; i++) {
+            const int p = starting_bitplane + i;
+            sz[i] = stream_sizes.at(p);
+            total += sz[i];
+            if (p <= stopping_index || p >= latter_) {   // the raw length leads a compressed stream
+                uint64_t n = 0;
+                if (sz[i] >= 8) std::memcpy(&n, streams[i], 8);
+                raw += n;
+            } else {
+                raw += sz[i];
+            }
+        }
+        std::vector<uint8_t> host(total);
+        size_t o = 0;
+        for (int i = 0; i < num_bitplanes; i++) { std::memcpy(host.data() + o, streams[i], sz[i]); o += sz[i]; }
+        DeviceBuffer in(total + 16), out(raw + 16);
+        cuda_check(cudaMemcpy(in.get(), host.data(), total, cudaMemcpyHostToDevice), "H2D");
+        std::vector<uint32_t> rsz(num_bitplanes);
+        check(prodm_lossless_decompress_level(in.get(), sz.data(), starting_bitplane, num_bitplanes, stopping_index,
+                                              latter_, out.get(), raw, rsz.data(), nullptr),
+              "prodm_lossless_decompress_level");
+        std::vector<uint8_t> res(raw);
+        cuda_check(cudaMemcpy(res.data(), out.get(), raw, cudaMemcpyDeviceToHost), "D2H");
+        o = 0;
+        for (int i = 0; i < num_bitplanes; i++) {
+            uint8_t* b = (uint8_t*)std::malloc(rsz[i] ? rsz[i] : 1);
+            std::memcpy(b, res.data() + o, rsz[i]);
+            o += rsz[i];
+            buffer_.push_back(b);
+            streams[i] = b;
+        }
+    }
+    void decompress_release() {
+        for (auto* b : buffer_) std::free(b);
+        buffer_.clear();
+    }
+    void print() const { std::printf("GPU adaptive level compressor (ZCB codec)\n"); }
+
+  private:
+    int latter_;
+    std::vector<uint8_t*> buffer_;
+};
+
+// ---------------------------------------------------------------------------
 // Error collectors (MaxErrorCollector.hpp:14-25, SquaredErrorCollector.hpp:54-96)
 // ---------------------------------------------------------------------------
 template <class T>
@@ -519,6 +612,8 @@ class GpuComposedRefactor {
     GpuComposedRefactor(int encoder, int basis, int collector, std::string metadata_file,
                         std::vector<std::string> level_files)
         : enc_(encoder), basis_(basis), col_(collector), meta_(std::move(metadata_file)), files_(std::move(level_files)) {}
+    // the lossless stage (AdaptiveLevelCompressor's rule, ZCB codec); < 0: none
+    void set_lossless(int latter_index) { latter_ = latter_index; }
     ~GpuComposedRefactor() { if (h_) prodm_mdr_destroy(h_); }
 
     void refactor(T const* data, const std::vector<uint32_t>& dims, uint8_t target_level, uint8_t num_bitplanes) {
@@ -536,6 +631,7 @@ class GpuComposedRefactor {
         const size_t n = product(dims);
         DeviceBuffer d(n * sizeof(T));
         cuda_check(cudaMemcpy(d.get(), data, n * sizeof(T), cudaMemcpyHostToDevice), "H2D");
+        check(prodm_mdr_set_lossless(h_, latter_, nullptr), "prodm_mdr_set_lossless");
         check(prodm_mdr_refactor(h_, d.get(), nullptr), "prodm_mdr_refactor");
         for (int l = 0; l <= target_level; l++) {
             uint64_t len = 0;
@@ -563,6 +659,7 @@ class GpuComposedRefactor {
         std::fclose(fp);
     }
     int enc_, basis_, col_;
+    int latter_ = -1;
     std::string meta_;
     std::vector<std::string> files_;
     prodm_mdr* h_ = nullptr;

@@ -72,6 +72,7 @@ _SIGS = {
     "prodm_mdr_level_info": (_i, [_P, _u32p, _dp, _dp, _P]),
     "prodm_mdr_metadata": (_i, [_P, _u8p, C.c_size_t, C.POINTER(C.c_size_t), _P]),
     "prodm_mdr_export_level": (_i, [_P, _i, _P, C.c_uint64, _i, _u64p, _P]),
+    "prodm_mdr_set_lossless": (_i, [_P, _i, _P]),
     "prodm_mdr_retrieve": (_i, [_P, C.c_double, _i, _i, C.c_double, _P, _P]),
     "prodm_mdr_retrieve_planes": (_i, [_P, _u8p, _P, _P]),
     "prodm_mdr_interpret": (_i, [_P, C.c_double, _i, _i, C.c_double, _P]),

@@ -309,6 +309,10 @@ class MDRField:
              _stream(stream))
         return buf
 
+    def set_lossless(self, latter_index=26, stream=None):
+        """Lossless stage on (latter_index >= 0, the reference's default 26) or off (None / < 0)."""
+        call("prodm_mdr_set_lossless", self.h, -1 if latter_index is None else int(latter_index), _stream(stream))
+
     def retrieve(self, tolerance, out=None, interpreter="sign_exclude", estimator="max_hb", s=0.0, stream=None):
         if out is None:
             out = torch.empty(self.shape, dtype=self.dtype, device="cuda")

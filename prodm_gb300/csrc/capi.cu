@@ -566,6 +566,16 @@ struct prodm_mdr {
     size_t es = 4;
     bool nb = true, orth = false, sq = false;
     bool pb = false;                               // per-bit encoder
+    // lossless stage (off while ll_latter < 0): stored sizes go to `sizes`
+    // (the interpreter's cost model), the encoders' raw sizes to `rsizes`
+    int ll_latter = -1;
+    bool refactored = false;
+    uint32_t* rsizes = nullptr;
+    std::vector<uint8_t> ll_stop, ll_flags;        // per level; per level and plane
+    std::vector<uint8_t*> ll_cbuf;                 // loading: stored level bytes as they arrive
+    std::vector<uint64_t> ll_cloaded, ll_rawoff;   // stored bytes loaded, raw bytes expanded, per level
+    std::vector<int> ll_expanded;                  // planes expanded per level
+    std::vector<uint32_t> ll_stored;               // loading: stored sizes from the metadata
     uint32_t* pbcounts = nullptr;                  // per-bit: first-one counts, 64 per level
     int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
     std::vector<void*> allocs;
@@ -754,6 +764,7 @@ int mdr_alloc_all(prodm_mdr* h) {
     if ((rc = h->alloc(&h->keys, (L + 1) * 8))) return rc;
     if ((rc = h->alloc(&h->bounds, (L + 1) * es))) return rc;
     if ((rc = h->alloc((void**)&h->sizes, (L + 1) * B * 4))) return rc;
+    if ((rc = h->alloc((void**)&h->rsizes, (L + 1) * B * 4))) return rc;
     if ((rc = h->alloc((void**)&h->sqerr, (L + 1) * (B + 1) * 8))) return rc;
     if ((rc = h->alloc((void**)&h->maxerr, (L + 1) * (B + 1) * 8))) return rc;
     uint64_t parts = maxch > (uint64_t)kPartialSlots ? maxch : (uint64_t)kPartialSlots;
@@ -1092,9 +1103,68 @@ int mdr_unpack_loaded(prodm_mdr* h, cudaStream_t st) {
     return PRODM_OK;
 }
 
+int mdr_load_level(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t bytes, int host, cudaStream_t st);
+
+// lossless stage: stored level bytes as they arrive
+int mdr_ll_load(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t bytes, int host, cudaStream_t st) {
+    const int B = h->B;
+    uint64_t total = 0;
+    for (int p = 0; p < B; p++) total += h->ll_stored[l * B + p];
+    if (off + bytes > total) return fail(PRODM_EINVAL, "load_level: range beyond the level file");
+    if (bytes == 0) return PRODM_OK;
+    if (!h->ll_cbuf[l]) {
+        int rc = h->alloc((void**)&h->ll_cbuf[l], total);
+        if (rc) return rc;
+    }
+    PRODM_CUDA(cudaMemcpyAsync(h->ll_cbuf[l] + off, src, bytes, host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                               st));
+    if (off + bytes > h->ll_cloaded[l]) h->ll_cloaded[l] = off + bytes;
+    return PRODM_OK;
+}
+
+// stored planes completely loaded and not expanded yet -> raw plane bytes
+// (decompressed where the stage compressed them) -> the raw loading path
+int mdr_ll_expand(prodm_mdr* h, cudaStream_t st) {
+    const int L = h->g.L, B = h->B;
+    for (int l = 0; l <= L; l++) {
+        if (!h->ll_cbuf[l]) continue;
+        uint64_t off = 0, soff = 0;
+        int complete = 0;
+        for (int p = 0; p < B; p++) {
+            off += h->ll_stored[l * B + p];
+            if (off <= h->ll_cloaded[l]) complete = p + 1;
+            else break;
+        }
+        const int first = h->ll_expanded[l];
+        if (complete <= first) continue;
+        const int num = complete - first;
+        for (int p = 0; p < first; p++) soff += h->ll_stored[l * B + p];
+        const uint64_t cap = encode_bound(h->cfg.encoder, h->cfg.dtype, h->g.elems[l], B);
+        uint8_t* raw;
+        PRODM_CUDA(cudaMallocAsync((void**)&raw, cap + 256, st));
+        std::vector<uint32_t> rsz(num);
+        int rc = ll_decompress_planes(h->ll_cbuf[l] + soff, h->ll_stored.data() + l * B + first,
+                                      h->ll_flags.data() + (size_t)l * B + first, num, raw, cap, rsz.data(), st);
+        uint64_t rbytes = 0;
+        if (!rc) {
+            for (int i = 0; i < num; i++) {
+                h->hsizes[l * B + first + i] = rsz[i];
+                rbytes += rsz[i];
+            }
+            rc = mdr_load_level(h, l, raw, h->ll_rawoff[l], rbytes, 0, st);
+        }
+        cudaFreeAsync(raw, st);
+        if (rc) return rc;
+        h->ll_rawoff[l] += rbytes;
+        h->ll_expanded[l] = complete;
+    }
+    return PRODM_OK;
+}
+
 template <class T>
 int mdr_reconstruct(prodm_mdr* h, T* out, cudaStream_t st) {
     int rc;
+    if (h->from_files && h->ll_latter >= 0 && (rc = mdr_ll_expand(h, st))) return rc;
     if (h->from_files && !h->nb && (rc = mdr_unpack_loaded(h, st))) return rc;
     return mdr_decode_recompose<T>(h, out, st);
 }
@@ -1137,8 +1207,9 @@ int mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, cudaStream_t
         p += 4 * B;
     }
     if (!need(nl + 4 * nl + 1)) return fail(PRODM_ECORRUPT, "metadata truncated");
-    for (int l = 0; l < nl; l++)
-        if (p[l] != 0) return fail(PRODM_EUNSUPPORTED, "metadata: levels compressed by a lossless stage");
+    std::vector<uint8_t> stops(p, p + nl);
+    bool any_stop = false;
+    for (int l = 0; l < nl; l++) any_stop |= stops[l] != 0;
     p += nl + 4 * nl;
     uint8_t negab = *p++;
     if ((negab != 0) != h->nb) return fail(PRODM_ECORRUPT, "metadata: encoder kind mismatch");
@@ -1149,6 +1220,16 @@ int mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, cudaStream_t
         p += 8;
         if ((int)c != B + 1 || !need(nl * (B + 1) * 8)) return fail(PRODM_ECORRUPT, "metadata: bad error-table extension");
         memcpy(sq.data(), p, nl * (B + 1) * 8);
+        p += nl * (B + 1) * 8;
+    }
+    int latter = -1;
+    if (need(8) && memcmp(p, "ZCB1", 4) == 0) {
+        uint32_t lt;
+        memcpy(&lt, p + 4, 4);
+        if (lt > 255) return fail(PRODM_ECORRUPT, "metadata: bad lossless-stage extension");
+        latter = (int)lt;
+    } else if (any_stop) {
+        return fail(PRODM_EUNSUPPORTED, "metadata: levels compressed by the reference's zstd stage");
     }
     // device state: sizes, bounds, level max keys (exponents) and error tables
     using K = typename KeyOf<T>::type;
@@ -1169,6 +1250,25 @@ int mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, cudaStream_t
     h->loaded.assign(nl, 0);
     h->unpacked.assign(nl, 0);
     h->header_done.assign(nl, 0);
+    h->ll_latter = latter;
+    if (latter >= 0) {
+        // stored sizes stay the cost model; the raw sizes of compressed planes
+        // become known as the planes are expanded (until then a placeholder
+        // larger than any plane, so that no raw path counts them as loaded)
+        h->ll_stop = stops;
+        h->ll_stored = h->hsizes;
+        h->ll_flags.assign((size_t)nl * B, 0);
+        for (int l = 0; l < nl; l++)
+            for (int q = 0; q < B; q++) {
+                const bool c = q <= stops[l] || q >= latter;   // AdaptiveLevelCompressor.hpp:43-52
+                h->ll_flags[(size_t)l * B + q] = c;
+                if (c) h->hsizes[l * B + q] = h->nb ? (uint32_t)(h->nblocks[l] * h->es) : 0x3fffffffu;
+            }
+        h->ll_cloaded.assign(nl, 0);
+        h->ll_rawoff.assign(nl, 0);
+        h->ll_expanded.assign(nl, 0);
+        if (h->ll_cbuf.empty()) h->ll_cbuf.assign(nl, nullptr);
+    }
     if (h->lfile.empty()) h->lfile.assign(nl, nullptr);
     return PRODM_OK;
 }
@@ -1178,6 +1278,9 @@ int mdr_load_level(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t 
     if (!h->from_files) return fail(PRODM_EINVAL, "load_level: load the metadata first");
     uint64_t total = 0;
     for (int p = 0; p < B; p++) total += h->hsizes[l * B + p];
+    // with the lossless stage the raw sizes of planes not yet expanded are
+    // unknown: the raw level file is bounded by the encoder's bound
+    if (h->ll_latter >= 0) total = encode_bound(h->cfg.encoder, h->cfg.dtype, h->g.elems[l], B);
     if (off + bytes > total) return fail(PRODM_EINVAL, "load_level: range beyond the level file");
     if (bytes == 0) return PRODM_OK;
     cudaMemcpyKind kind = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
@@ -1525,12 +1628,18 @@ int prodm_mdr_create(prodm_mdr** out, const prodm_config* cfg) {
     return PRODM_OK;
 }
 
+static int mdr_lossless_sizes(prodm_mdr* h, cudaStream_t st);
+
 int prodm_mdr_refactor(prodm_mdr* h, const void* field, void* stream) {
     if (!h || !field) return fail(PRODM_EINVAL, "prodm_mdr_refactor: NULL pointer");
     cudaStream_t st = (cudaStream_t)stream;
+    if (h->from_files) h->ll_latter = -1;   // a loaded stage does not carry over to a new refactor
     h->from_files = false;
-    if (h->cfg.dtype == PRODM_F64) return mdr_refactor<double>(h, (const double*)field, st);
-    return mdr_refactor<float>(h, (const float*)field, st);
+    const int rc = h->cfg.dtype == PRODM_F64 ? mdr_refactor<double>(h, (const double*)field, st)
+                                             : mdr_refactor<float>(h, (const float*)field, st);
+    if (rc) return rc;
+    h->refactored = true;
+    return h->ll_latter >= 0 ? mdr_lossless_sizes(h, st) : PRODM_OK;
 }
 
 int prodm_mdr_level_info(prodm_mdr* h, uint32_t* hs, double* hb, double* he, void* stream) {
@@ -1552,7 +1661,8 @@ int prodm_mdr_metadata(prodm_mdr* h, uint8_t* buf, size_t cap, size_t* len, void
     if (!h || !len) return fail(PRODM_EINVAL, "NULL pointer");
     const int L = h->g.L, B = h->B, nl = L + 1, nd = h->g.ndims;
     // ComposedRefactor.hpp:48-67 + extension: "SQER" u32 (B+1) doubles per level
-    size_t need = 1 + 4 * nd + 1 + nl * h->es + nl * (4 + 4 * B) + nl + 4 * nl + 1 + 4 + 4 + nl * (B + 1) * 8;
+    size_t need = 1 + 4 * nd + 1 + nl * h->es + nl * (4 + 4 * B) + nl + 4 * nl + 1 + 4 + 4 + nl * (B + 1) * 8 +
+                  (h->ll_latter >= 0 ? 8 : 0);
     *len = need;
     if (!buf) return PRODM_OK;
     if (cap < need) return fail(PRODM_EINVAL, "metadata buffer too small");
@@ -1574,23 +1684,28 @@ int prodm_mdr_metadata(prodm_mdr* h, uint8_t* buf, size_t cap, size_t* len, void
         memcpy(p, &c, 4); p += 4;
         memcpy(p, sz.data() + l * B, 4 * B); p += 4 * B;
     }
-    for (int l = 0; l < nl; l++) *p++ = 0;                     // stopping indices (no lossless stage)
+    for (int l = 0; l < nl; l++) *p++ = h->ll_latter >= 0 ? h->ll_stop[l] : 0;   // stopping indices
     for (int l = 0; l < nl; l++) { uint32_t one = 1; memcpy(p, &one, 4); p += 4; }   // level_num
     *p++ = (uint8_t)(h->nb ? 1 : 0);
     memcpy(p, "SQER", 4); p += 4;
     uint32_t cnt = (uint32_t)(B + 1);
     memcpy(p, &cnt, 4); p += 4;
     memcpy(p, er.data(), er.size() * 8); p += er.size() * 8;
+    if (h->ll_latter >= 0) {   // the lossless stage's codec and latter index
+        memcpy(p, "ZCB1", 4); p += 4;
+        uint32_t lt = (uint32_t)h->ll_latter;
+        memcpy(p, &lt, 4); p += 4;
+    }
     return PRODM_OK;
 }
 
-int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int dst_is_host, uint64_t* len, void* stream) {
-    if (!h) return fail(PRODM_EINVAL, "NULL handle");
-    const int L = h->g.L, B = h->B;
-    if (level < 0 || level > L) return fail(PRODM_EINVAL, "level out of range");
-    cudaStream_t st = (cudaStream_t)stream;
+// the level file with raw (uncompressed) streams; dsizes: the level's raw
+// plane sizes on the device
+static int export_raw_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int dst_is_host, uint64_t* len,
+                            const uint32_t* dsizes, cudaStream_t st) {
+    const int B = h->B;
     std::vector<uint32_t> sz(B);
-    PRODM_CUDA(cudaMemcpyAsync(sz.data(), h->sizes + (uint64_t)level * B, B * 4, cudaMemcpyDeviceToHost, st));
+    PRODM_CUDA(cudaMemcpyAsync(sz.data(), dsizes, B * 4, cudaMemcpyDeviceToHost, st));
     PRODM_CUDA(cudaStreamSynchronize(st));
     uint64_t total = 0;
     for (int p = 0; p < B; p++) total += sz[p];
@@ -1613,7 +1728,7 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
         PRODM_CUDA(cudaMallocAsync((void**)&tmp, scr + (direct ? 0 : (total + 255) / 256 * 256), st));
         uint8_t* out = direct ? (uint8_t*)dst : tmp + scr;
         const uint32_t* rows = (const uint32_t*)src;
-        int rc = launch_pb_pack(rows, h->plane_cap[level], n, B, h->sizes + (uint64_t)level * B, total,
+        int rc = launch_pb_pack(rows, h->plane_cap[level], n, B, dsizes, total,
                                 out, tmp, st);
         if (!rc && !direct) {
             const cudaError_t e = cudaMemcpyAsync(dst, out, total,
@@ -1627,7 +1742,7 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
     }
     uint8_t* tmp = (uint8_t*)dst;
     if (dst_is_host) PRODM_CUDA(cudaMallocAsync((void**)&tmp, total, st));
-    int rc = launch_gr_pack((const void* const*)(h->plane_ptrs + (uint64_t)level * B), h->sizes + (uint64_t)level * B, B,
+    int rc = launch_gr_pack((const void* const*)(h->plane_ptrs + (uint64_t)level * B), dsizes, B,
                             h->nblocks[level], h->rbs + h->rb_off[level], (int)h->es, tmp, st);
     if (rc) return rc;
     if (dst_is_host) {
@@ -1636,6 +1751,99 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
     }
     PRODM_CUDA(cudaStreamSynchronize(st));
     return PRODM_OK;
+}
+
+// lossless stage on: the encoders' (raw) sizes -> rsizes; per level the raw
+// level file is built in scratch, each stream's ZCB size counted and the
+// adaptive rule applied; the stored sizes -> sizes (the interpreter's cost
+// model, as the reference's metadata carries them)
+static int mdr_lossless_sizes(prodm_mdr* h, cudaStream_t st) {
+    const int nl = h->g.L + 1, B = h->B;
+    std::vector<uint32_t> raw(nl * B), stored(nl * B);
+    if (h->nb) {   // fixed raw sizes (the refactor does not rewrite them)
+        for (int l = 0; l < nl; l++)
+            for (int p = 0; p < B; p++) raw[l * B + p] = (uint32_t)(h->nblocks[l] * h->es);
+        PRODM_CUDA(cudaMemcpyAsync(h->rsizes, raw.data(), nl * B * 4, cudaMemcpyHostToDevice, st));
+    } else {
+        PRODM_CUDA(cudaMemcpyAsync(h->rsizes, h->sizes, nl * B * 4, cudaMemcpyDeviceToDevice, st));
+        PRODM_CUDA(cudaMemcpyAsync(raw.data(), h->sizes, nl * B * 4, cudaMemcpyDeviceToHost, st));
+    }
+    PRODM_CUDA(cudaStreamSynchronize(st));
+    h->ll_stop.assign(nl, 0);
+    h->ll_flags.assign((size_t)nl * B, 0);
+    uint64_t maxraw = 0;
+    for (int l = 0; l < nl; l++) {
+        uint64_t t = 0;
+        for (int p = 0; p < B; p++) t += raw[l * B + p];
+        maxraw = t > maxraw ? t : maxraw;
+    }
+    uint8_t* tmp;
+    PRODM_CUDA(cudaMallocAsync((void**)&tmp, maxraw + 256, st));
+    int rc = PRODM_OK;
+    std::vector<uint32_t> comp(B);
+    for (int l = 0; l < nl && !rc; l++) {
+        rc = export_raw_level(h, l, tmp, maxraw, 0, nullptr, h->rsizes + (uint64_t)l * B, st);
+        if (!rc) rc = ll_stream_sizes(tmp, raw.data() + l * B, B, comp.data(), st);
+        if (rc) break;
+        h->ll_stop[l] = (uint8_t)adaptive_stopping(raw.data() + l * B, comp.data(), B, h->ll_latter,
+                                                    h->ll_flags.data() + (size_t)l * B);
+        for (int p = 0; p < B; p++) stored[l * B + p] = h->ll_flags[(size_t)l * B + p] ? comp[p] : raw[l * B + p];
+    }
+    cudaFreeAsync(tmp, st);
+    if (rc) return rc;
+    PRODM_CUDA(cudaMemcpyAsync(h->sizes, stored.data(), nl * B * 4, cudaMemcpyHostToDevice, st));
+    PRODM_CUDA(cudaStreamSynchronize(st));
+    return PRODM_OK;
+}
+
+int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int dst_is_host, uint64_t* len, void* stream) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    const int L = h->g.L, B = h->B;
+    if (level < 0 || level > L) return fail(PRODM_EINVAL, "level out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (h->ll_latter < 0) return export_raw_level(h, level, dst, cap, dst_is_host, len, h->sizes + (uint64_t)level * B, st);
+    // lossless stage: the raw level into scratch, then its stored streams
+    std::vector<uint32_t> raw(B), stored(B);
+    PRODM_CUDA(cudaMemcpyAsync(raw.data(), h->rsizes + (uint64_t)level * B, B * 4, cudaMemcpyDeviceToHost, st));
+    PRODM_CUDA(cudaMemcpyAsync(stored.data(), h->sizes + (uint64_t)level * B, B * 4, cudaMemcpyDeviceToHost, st));
+    PRODM_CUDA(cudaStreamSynchronize(st));
+    uint64_t rtotal = 0, total = 0;
+    for (int p = 0; p < B; p++) { rtotal += raw[p]; total += stored[p]; }
+    if (len) *len = total;
+    if (!dst) return PRODM_OK;
+    if (cap < total) return fail(PRODM_EINVAL, "export buffer too small");
+    uint8_t* tmp;
+    const uint64_t rpad = (rtotal + 255) / 256 * 256;
+    PRODM_CUDA(cudaMallocAsync((void**)&tmp, rpad + (dst_is_host ? total + 256 : 256), st));
+    int rc = export_raw_level(h, level, tmp, rtotal, 0, nullptr, h->rsizes + (uint64_t)level * B, st);
+    uint8_t* out = dst_is_host ? tmp + rpad : (uint8_t*)dst;
+    std::vector<uint32_t> osz(B);
+    int stop = 0;
+    if (!rc)
+        rc = ll_compress_level(tmp, raw.data(), B, h->ll_latter, out, total, osz.data(), &stop,
+                               h->ll_flags.data() + (size_t)level * B, st);
+    if (!rc && dst_is_host) {
+        cudaError_t e = cudaMemcpyAsync(dst, out, total, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_status(e, "export copy");
+    }
+    cudaFreeAsync(tmp, st);
+    return rc;
+}
+
+int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    if (h->from_files) return fail(PRODM_EINVAL, "set_lossless: a handle fed from files takes the stage from its metadata");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nl = h->g.L + 1, B = h->B;
+    if (latter_index < 0) {   // off: the raw sizes back to the cost model
+        if (h->ll_latter >= 0) PRODM_CUDA(cudaMemcpyAsync(h->sizes, h->rsizes, nl * B * 4, cudaMemcpyDeviceToDevice, st));
+        h->ll_latter = -1;
+        return PRODM_OK;
+    }
+    if (h->ll_latter >= 0) PRODM_CUDA(cudaMemcpyAsync(h->sizes, h->rsizes, nl * B * 4, cudaMemcpyDeviceToDevice, st));
+    h->ll_latter = latter_index;
+    return h->refactored ? mdr_lossless_sizes(h, st) : PRODM_OK;
 }
 
 int prodm_mdr_retrieve(prodm_mdr* h, double tol, int interp, int est, double s, void* out, void* stream) {
@@ -1671,6 +1879,7 @@ int prodm_mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, void* 
 int prodm_mdr_load_level(prodm_mdr* h, int level, const void* src, uint64_t off, uint64_t bytes, int host, void* stream) {
     if (!h || (!src && bytes)) return fail(PRODM_EINVAL, "NULL pointer");
     if (level < 0 || level > h->g.L) return fail(PRODM_EINVAL, "level out of range");
+    if (h->from_files && h->ll_latter >= 0) return mdr_ll_load(h, level, src, off, bytes, host, (cudaStream_t)stream);
     return mdr_load_level(h, level, src, off, bytes, host, (cudaStream_t)stream);
 }
 

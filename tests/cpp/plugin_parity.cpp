@@ -160,11 +160,91 @@ static int run(const char* dir, const char* tag, int B) {
     return 0;
 }
 
+// the lossless stage: GpuComposedRefactor with it on writes the level files
+// the adapters produce with GpuAdaptiveLevelCompressor::compress_level, and
+// GpuComposedReconstructor reading them meets every tolerance
+static int run_lossless(const char* dir) {
+    using T = float;
+    const std::vector<uint32_t> dims = {65, 65, 65};
+    const int L = 3, B = 32;
+    const size_t N = 65 * 65 * 65;
+    std::vector<T> field(N);
+    for (size_t i = 0; i < N; i++) field[i] = (T)(std::sin(0.001 * i) + 0.01 * std::cos(0.37 * i));
+    std::string d(dir);
+    std::vector<std::string> files;
+    for (int l = 0; l <= L; l++) files.push_back(d + "/lossless_level_" + std::to_string(l) + ".bin");
+    const std::string meta = d + "/lossless_metadata.bin";
+    GpuComposedRefactor<T> ref(PRODM_ENC_GROUPED, PRODM_BASIS_HIERARCHICAL, PRODM_COLLECT_MAX, meta, files);
+    ref.set_lossless(26);
+    ref.refactor(field.data(), dims, L, B);
+    GpuMGARDHierarchicalDecomposer<T> dec;
+    GpuDirectInterleaver<T> il;
+    GpuGroupedBPEncoder<T, uint32_t> enc;
+    GpuAdaptiveLevelCompressor comp;
+    std::vector<T> data(field);
+    dec.decompose(data.data(), dims, L);
+    std::vector<std::vector<uint32_t>> ld(L + 1, std::vector<uint32_t>(3));
+    for (int dd = 0; dd < 3; dd++) {
+        uint32_t n = dims[dd];
+        for (int j = 0; j <= L; j++) { ld[L - j][dd] = n; n = (n >> 1) + 1; }
+    }
+    size_t prev = 0;
+    for (int l = 0; l <= L; l++) {
+        const size_t box = (size_t)ld[l][0] * ld[l][1] * ld[l][2];
+        const size_t n = box - prev;
+        prev = box;
+        std::vector<uint32_t> coarse = l ? ld[l - 1] : std::vector<uint32_t>(3, 0);
+        std::vector<T> buf(n);
+        il.interleave(data.data(), dims, ld[l], coarse, buf.data());
+        T mx = 0;
+        for (T v : buf) mx = std::fabs(v) > mx ? std::fabs(v) : mx;
+        int e = 0;
+        std::frexp(mx, &e);
+        std::vector<uint32_t> sizes;
+        auto streams = enc.encode(buf.data(), (int32_t)n, e, B, sizes);
+        std::vector<uint32_t> raw(sizes);
+        std::vector<uint8_t*> keep(B);
+        for (int p = 0; p < B; p++) {   // copies for the round trip below
+            keep[p] = (uint8_t*)std::malloc(sizes[p] ? sizes[p] : 1);
+            std::memcpy(keep[p], streams[p], sizes[p]);
+        }
+        const uint8_t stop = comp.compress_level(streams, sizes);
+        std::vector<uint8_t> bytes;
+        for (int p = 0; p < B; p++) {
+            bytes.insert(bytes.end(), streams[p], streams[p] + sizes[p]);
+        }
+        if (read_all(files[l]) != bytes) { std::printf("lossless: level %d file differs from the adapters'\n", l); return 1; }
+        std::vector<const uint8_t*> cst(streams.begin(), streams.end());
+        comp.decompress_level(cst, sizes, 0, (uint8_t)B, stop);
+        for (int p = 0; p < B; p++) {
+            if (std::memcmp(cst[p], keep[p], raw[p]) != 0) { std::printf("lossless: level %d plane %d round trip\n", l, p); return 1; }
+            std::free(keep[p]);
+            std::free(streams[p]);
+        }
+        comp.decompress_release();
+    }
+    GpuComposedReconstructor<T> rec(PRODM_ENC_GROUPED, PRODM_BASIS_HIERARCHICAL, PRODM_INTERP_SIGN_EXCLUDE,
+                                    PRODM_EST_MAX_HB, meta, files);
+    rec.load_metadata();
+    T vmin = field[0], vmax = field[0];
+    for (T v : field) { vmin = v < vmin ? v : vmin; vmax = v > vmax ? v : vmax; }
+    for (double rel : {1e-1, 1e-3, 1e-5}) {
+        const double tol = rel * (vmax - vmin);
+        T* out = rec.progressive_reconstruct(tol);
+        double err = 0;
+        for (size_t i = 0; i < N; i++) err = std::fmax(err, std::fabs((double)out[i] - field[i]));
+        if (err > tol) { std::printf("lossless: tolerance %g missed (%g)\n", tol, err); return 1; }
+    }
+    std::printf("lossless ok\n");
+    return 0;
+}
+
 int main(int argc, char** argv) {
     const char* dir = argc > 1 ? argv[1] : ".";
     int rc = run<float, PRODM_ENC_NEGABINARY, GpuNegaBinaryBPEncoder<float, uint32_t>>(dir, "negabinary", 32);
     rc |= run<float, PRODM_ENC_GROUPED, GpuGroupedBPEncoder<float, uint32_t>>(dir, "grouped", 32);
     rc |= run<double, PRODM_ENC_PERBIT, GpuPerBitBPEncoder<double, uint32_t>>(dir, "perbit", 60);
+    rc |= run_lossless(dir);
     if (rc == 0) std::printf("PLUGIN PARITY OK\n");
     return rc;
 }

@@ -55,5 +55,21 @@ int main() {
         MDR::ConcatLevelFileRetriever("gmeta.bin", gfiles));
     grec.load_metadata();
     D* gout = grec.progressive_reconstruct(1e-6, -1);
-    return out && gout ? 0 : 1;
+
+    // the lossless stage as the composed classes' compressor
+    auto lrefactor = MDR::ComposedRefactor<T, GpuMGARDHierarchicalDecomposer<T>, GpuDirectInterleaver<T>,
+                                           GpuGroupedBPEncoder<T, uint32_t>, GpuAdaptiveLevelCompressor,
+                                           GpuMaxErrorCollector<T>, MDR::ConcatLevelFileWriter>(
+        GpuMGARDHierarchicalDecomposer<T>(), GpuDirectInterleaver<T>(), GpuGroupedBPEncoder<T, uint32_t>(),
+        GpuAdaptiveLevelCompressor(), GpuMaxErrorCollector<T>(), MDR::ConcatLevelFileWriter("lmeta.bin", files));
+    lrefactor.refactor(data.data(), {33, 33, 33}, 1, 32);
+    auto lrec = MDR::ComposedReconstructor<T, GpuMGARDHierarchicalDecomposer<T>, GpuDirectInterleaver<T>,
+                                           GpuGroupedBPEncoder<T, uint32_t>, GpuAdaptiveLevelCompressor, Interp,
+                                           MDR::MaxErrorEstimatorHB<T>, MDR::ConcatLevelFileRetriever>(
+        GpuMGARDHierarchicalDecomposer<T>(), GpuDirectInterleaver<T>(), GpuGroupedBPEncoder<T, uint32_t>(),
+        GpuAdaptiveLevelCompressor(), Interp(MDR::MaxErrorEstimatorHB<T>()),
+        MDR::ConcatLevelFileRetriever("lmeta.bin", files));
+    lrec.load_metadata();
+    T* lout = lrec.progressive_reconstruct(1e-3, -1);
+    return out && gout && lout ? 0 : 1;
 }

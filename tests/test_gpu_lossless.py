@@ -103,3 +103,88 @@ def test_malformed_streams_rejected():
         api().decompress_level(d[:comp.size - 200], [comp.size - 200], 0, 1, 5, 26, raw_capacity=30000)
     raw2, _ = api().decompress_level(d, [comp.size], 0, 1, 5, 26, raw_capacity=30000)
     assert np.array_equal(raw2.cpu().numpy(), raw)
+
+
+def oracle_stored(res, L, B, latter):
+    """per level: raw streams -> (stored bytes, stored sizes, stopping index, flags)"""
+    sizes = res["sizes"].reshape(L + 1, B)
+    offs = np.concatenate([[0], np.cumsum(sizes.sum(axis=1).astype(np.int64))])
+    out = []
+    for l in range(L + 1):
+        blob = res["blob"][offs[l]:offs[l + 1]]
+        out.append(expected(blob, sizes[l], latter))
+    return out
+
+
+CASES = [((65, 65, 65), 3, np.float32, 32, "negabinary", "squared", "negabinary", "l2_hb"),
+         ((33, 40, 21), 2, np.float32, 32, "grouped", "max", "sign_exclude", "max_hb"),
+         ((17, 17, 17), 3, np.float64, 60, "perbit", "max", "sign_exclude", "max_hb")]
+
+
+@pytest.mark.parametrize("shape,L,dt,B,enc,col,interp,est", CASES)
+def test_handle_with_lossless_stage(shape, L, dt, B, enc, col, interp, est, tmp_path):
+    rng = np.random.default_rng(B + L)
+    field = (np.cumsum(rng.standard_normal(shape), axis=-1) + 0.05 * rng.standard_normal(shape)).astype(dt)
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    m = api().MDRField(shape, tdt, L, B, enc, "hierarchical", col)
+    m.refactor(torch.from_numpy(field).cuda())
+    raw_sizes, _, _ = m.level_info()
+    m.set_lossless(26)
+    res = O.refactor(field, L, B, enc, True)
+    exp = oracle_stored(res, L, B, 26)
+    sizes, _, _ = m.level_info()
+    for l in range(L + 1):
+        stop, flags, stored, ssz = exp[l]
+        assert np.array_equal(sizes[l], ssz), l
+        assert np.array_equal(m.export_level(l), stored), l
+    meta = m.metadata()
+    vr = float(field.max() - field.min())
+    norm2 = float((field.astype(np.float64) ** 2).sum())
+    tols = [r * r * norm2 for r in (1e-2, 1e-4)] if est == "l2_hb" else [r * vr for r in (1e-2, 1e-4)]
+    outs, idxs = [], []
+    for tol in tols:
+        out = m.retrieve(tol, interpreter=interp, estimator=est)
+        idx = m.index()
+        ref = O.retrieve(shape, L, B, res["blob"], res["sizes"], res["bounds"], idx, enc, True, dt)
+        assert np.array_equal(out.cpu().numpy(), ref)
+        outs.append(out.clone())
+        idxs.append(idx)
+    # the stored files, loaded in two pieces per level, retrieve the same
+    files = [m.export_level(l) for l in range(L + 1)]
+    r = api().MDRField(shape, tdt, L, B, enc, "hierarchical", col)
+    r.load_metadata(meta)
+    s2, _, _ = r.level_info()
+    assert np.array_equal(s2, sizes)
+    for half in (0, 1):
+        for l in range(L + 1):
+            cut = len(files[l]) // 2
+            if half == 0:
+                r.load_level(l, files[l][:cut], 0)
+            else:
+                r.load_level(l, files[l][cut:], cut)
+        if half == 0:   # expands the planes complete in the first pieces
+            r.retrieve_planes([0] * (L + 1))
+    for tol, o, idx in zip(tols, outs, idxs):
+        got = r.retrieve(tol, interpreter=interp, estimator=est)
+        assert np.array_equal(r.index(), idx)
+        assert torch.equal(got, o)
+    # off again: the raw sizes are the cost model
+    m.set_lossless(None)
+    s3, _, _ = m.level_info()
+    assert np.array_equal(s3, raw_sizes)
+
+
+def test_reference_zstd_levels_rejected():
+    """metadata with stopping indices but no ZCB1 marker: levels the
+    reference's zstd stage compressed"""
+    from prodm_gb300._lib import ProdmError
+    g = np.load(os.path.join(HERE, "golden", "composed.npz"))
+    meta = bytearray(g["grouped_metadata"].tobytes())
+    nd = meta[0]
+    nl = meta[1 + 4 * nd]
+    B = 32
+    stops_at = 2 + 4 * nd + nl * 4 + nl * (4 + 4 * B)
+    meta[stops_at] = 3
+    r = api().MDRField((33, 33, 33), torch.float32, 3, 32, "grouped", "hierarchical", "max")
+    with pytest.raises(ProdmError):
+        r.load_metadata(bytes(meta))
