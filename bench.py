@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-field batched vs per-field-loop measurement")
     ap.add_argument("--no-qoi", action="store_true", help="skip the QoI-guided vs uniform-halving retrieval comparison")
     ap.add_argument("--no-perbit", action="store_true", help="skip the fp64 per-bit encoder measurement")
+    ap.add_argument("--no-lossless", action="store_true", help="skip the lossless-stage measurement")
     return ap.parse_args()
 
 
@@ -373,6 +374,7 @@ def run_ours(args):
     batched = run_batched() if (not args.no_batched and world == 1) else None
     qoi_res = run_qoi() if (not args.no_qoi and world == 1) else None
     perbit = run_perbit() if (not args.no_perbit and world == 1) else None
+    lossless = run_lossless() if (not args.no_lossless and world == 1) else None
 
     # end-to-end through the reference-facing flow with host buffers
     e2e = run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev) if args.e2e_steps > 0 else None
@@ -398,6 +400,7 @@ def run_ours(args):
             "batched": batched,
             "qoi": qoi_res,
             "perbit": perbit,
+            "lossless": lossless,
             "clocks": clocks,
         }
     if world > 1:
@@ -716,6 +719,67 @@ def run_perbit(shape=(513, 513, 513), levels=7, planes=60, rels=(1e-3, 1e-5, 1e-
                                 "device_seconds": t_dev, "cpu_oracle_seconds": t_cpu, "cores": 1,
                                 "identical": dec_same, "speedup": t_cpu / t_dev},
     }
+
+
+def run_lossless(reps=3):
+    """The lossless stage (AdaptiveLevelCompressor's rule, ZCB codec) on the
+    headline workload's streams: stored / raw sizes and stopping indices per
+    level, the retrieved bytes at each tolerance with and without the stage,
+    and the codec's throughput on the finest level's streams (raw bytes per
+    second through prodm_lossless_compress_level / _decompress_level, each
+    call including its host synchronisation)."""
+    import numpy as np
+    import torch
+    from prodm_gb300 import api, fields
+
+    x = fields.spectral_grf(SHAPE, slope=-5.0 / 3.0, seed=1234, device="cuda")
+    norm2 = float((x.double() ** 2).sum())
+    m = api.MDRField(SHAPE, torch.float32, LEVELS, BITPLANES, "negabinary", "hierarchical", "squared")
+    m.refactor(x)
+    raw, _, _ = m.level_info()
+    out = torch.empty_like(x)
+
+    def retrieved(sizes):
+        m.reset()
+        res = []
+        for rel in REL_TOLS:
+            m.retrieve(rel * rel * norm2, out=out, interpreter="negabinary", estimator="l2_hb")
+            idx = m.index()
+            res.append(int(sum(int(sizes[l, :idx[l]].astype(np.int64).sum()) for l in range(LEVELS + 1))))
+        return res
+
+    raw_ret = retrieved(raw)
+    m.set_lossless(26)
+    stored, _, _ = m.level_info()
+    stored_ret = retrieved(stored)
+    m.set_lossless(None)
+    blob = m.export_level_device(LEVELS)
+    sizes = raw[LEVELS]
+    nbytes = int(sizes.astype(np.int64).sum())
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for _ in range(reps):
+        comp, csz, stop = api.compress_level(blob, sizes, 26)
+    torch.cuda.synchronize()
+    t_c = (time.time() - t0) / reps
+    t0 = time.time()
+    for _ in range(reps):
+        back, _ = api.decompress_level(comp, csz, 0, BITPLANES, stop, 26, raw_capacity=nbytes + 16)
+    torch.cuda.synchronize()
+    t_d = (time.time() - t0) / reps
+    same = bool(torch.equal(back, blob))
+    m.close()
+    del x, out, blob, comp, back
+    torch.cuda.empty_cache()
+    rs, ss = raw.astype(np.int64).sum(axis=1), stored.astype(np.int64).sum(axis=1)
+    return {"workload": WORKLOAD + "; lossless stage AdaptiveLevelCompressor rule (latter index 26), ZCB codec",
+            "raw_bytes_per_level": rs.tolist(), "stored_bytes_per_level": ss.tolist(),
+            "ratio": float(rs.sum() / ss.sum()),
+            "retrieved_bytes_raw": raw_ret, "retrieved_bytes_stored": stored_ret,
+            "finest_level": {"raw_bytes": nbytes, "stopping_index": stop, "stored_bytes": int(csz.astype(np.int64).sum()),
+                             "compress_seconds": t_c, "compress_gbs": nbytes / t_c / 1e9,
+                             "decompress_seconds": t_d, "decompress_gbs": nbytes / t_d / 1e9,
+                             "round_trip_identical": same}}
 
 
 def call_export(mdr, level, host_tensor):

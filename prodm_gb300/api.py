@@ -309,6 +309,14 @@ class MDRField:
              _stream(stream))
         return buf
 
+    def export_level_device(self, level, stream=None):
+        """The level file's bytes as a device uint8 tensor."""
+        n = C.c_uint64()
+        call("prodm_mdr_export_level", self.h, level, None, 0, 0, C.byref(n), _stream(stream))
+        buf = torch.empty(max(n.value, 1), dtype=torch.uint8, device="cuda")
+        call("prodm_mdr_export_level", self.h, level, _ptr(buf), n.value, 0, C.byref(n), _stream(stream))
+        return buf[:n.value]
+
     def set_lossless(self, latter_index=26, stream=None):
         """Lossless stage on (latter_index >= 0, the reference's default 26) or off (None / < 0)."""
         call("prodm_mdr_set_lossless", self.h, -1 if latter_index is None else int(latter_index), _stream(stream))
