@@ -25,11 +25,15 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--encoder", default="negabinary")
     ap.add_argument("--basis", default="hierarchical")
+    ap.add_argument("--lossless", action="store_true",
+                    help="after the steps, the lossless stage on the finest level's streams: compress + decompress")
+    ap.add_argument("--import-streams", action="store_true",
+                    help="per-bit only: export the level files and load them into a second handle (the parse)")
     a = ap.parse_args()
     shape = (a.shape,) * 3
     L = a.levels if a.levels is not None else min(7, api.max_level(shape))
     if a.encoder == "perbit":
-        return perbit(shape, L, a.reps)
+        return perbit(shape, L, a.reps, a.import_streams)
     x = fields.spectral_grf(shape, seed=3)
     norm2 = float((x.double() ** 2).sum().item())
     mdr = api.MDRField(shape, torch.float32, L, 32, a.encoder, a.basis, "squared")
@@ -47,9 +51,17 @@ def main():
     for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
         print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
     print("final relative L2 error %.3g" % err)
+    if a.lossless:
+        sizes, _, _ = mdr.level_info()
+        blob = mdr.export_level_device(L)
+        comp, csz, stop = api.compress_level(blob, sizes[L], 26)
+        back, _ = api.decompress_level(comp, csz, 0, len(csz), stop, 26, raw_capacity=blob.numel() + 16)
+        torch.cuda.synchronize()
+        print("lossless: level %d %d -> %d bytes, stopping index %d, round trip %s"
+              % (L, blob.numel(), comp.numel(), stop, bool(torch.equal(back, blob))))
 
 
-def perbit(shape, L, reps):
+def perbit(shape, L, reps, import_streams=False):
     x = fields.shear_layer(shape, delta=0.05, noise_rel=1e-6, seed=21, dtype=torch.float64, device="cuda")
     vr = float((x.max() - x.min()).item())
     mdr = api.MDRField(shape, torch.float64, L, 60, "perbit", "hierarchical", "max")
@@ -65,6 +77,16 @@ def perbit(shape, L, reps):
     for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
         print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
     print("final max error %.3g of range %.3g" % (float((out - x).abs().max().item()), vr))
+    if import_streams:
+        files = [mdr.export_level(l) for l in range(L + 1)]
+        r = api.MDRField(shape, torch.float64, L, 60, "perbit", "hierarchical", "max")
+        r.load_metadata(mdr.metadata())
+        for l in range(L + 1):
+            r.load_level(l, files[l], 0)
+        full = r.retrieve_planes([60] * (L + 1))
+        ref = mdr.retrieve_planes([60] * (L + 1))
+        torch.cuda.synchronize()
+        print("imported streams reconstruct identically: %s" % bool(torch.equal(full, ref)))
 
 
 if __name__ == "__main__":
