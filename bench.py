@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-qoi", action="store_true", help="skip the QoI-guided vs uniform-halving retrieval comparison")
     ap.add_argument("--no-perbit", action="store_true", help="skip the fp64 per-bit encoder measurement")
     ap.add_argument("--no-lossless", action="store_true", help="skip the lossless-stage measurement")
+    ap.add_argument("--no-files", action="store_true", help="skip the level-file read / write measurement")
     return ap.parse_args()
 
 
@@ -375,6 +376,7 @@ def run_ours(args):
     qoi_res = run_qoi() if (not args.no_qoi and world == 1) else None
     perbit = run_perbit() if (not args.no_perbit and world == 1) else None
     lossless = run_lossless() if (not args.no_lossless and world == 1) else None
+    files = run_files() if (not args.no_files and world == 1) else None
 
     # end-to-end through the reference-facing flow with host buffers
     e2e = run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev) if args.e2e_steps > 0 else None
@@ -401,6 +403,7 @@ def run_ours(args):
             "qoi": qoi_res,
             "perbit": perbit,
             "lossless": lossless,
+            "files": files,
             "clocks": clocks,
         }
     if world > 1:
@@ -780,6 +783,57 @@ def run_lossless(reps=3):
                              "compress_seconds": t_c, "compress_gbs": nbytes / t_c / 1e9,
                              "decompress_seconds": t_d, "decompress_gbs": nbytes / t_d / 1e9,
                              "round_trip_identical": same}}
+
+
+def run_files():
+    """Level files of the headline workload written and read back: every level
+    file written by prodm_mdr_write_level_file, then loaded into a second
+    handle by prodm_mdr_load_level_file (cuFile where it registers the file,
+    else pinned staging) into a RAM-backed directory, so that the numbers are
+    the path's, not a disk's; the loaded handle's retrieval equals the
+    device-resident one."""
+    import shutil
+    import tempfile
+    import torch
+    from prodm_gb300 import api, fields
+
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    d = tempfile.mkdtemp(prefix="prodm_files_", dir=base)
+    try:
+        x = fields.spectral_grf(SHAPE, slope=-5.0 / 3.0, seed=1234, device="cuda")
+        m = api.MDRField(SHAPE, torch.float32, LEVELS, BITPLANES, "negabinary", "hierarchical", "squared")
+        m.refactor(x)
+        paths = [os.path.join(d, "level_%d.bin" % l) for l in range(LEVELS + 1)]
+        t0 = time.time()
+        for l, pth in enumerate(paths):
+            m.write_level_file(l, pth)
+        t_w = time.time() - t0
+        nbytes = sum(os.path.getsize(pth) for pth in paths)
+        r = api.MDRField(SHAPE, torch.float32, LEVELS, BITPLANES, "negabinary", "hierarchical", "squared")
+        r.load_metadata(m.metadata())
+        torch.cuda.synchronize()
+        t0 = time.time()
+        for l, pth in enumerate(paths):
+            r.load_level_file(l, pth)
+        torch.cuda.synchronize()
+        t_r = time.time() - t0
+        norm2 = float((x.double() ** 2).sum())
+        tol = REL_TOLS[-1] ** 2 * norm2
+        same = bool(torch.equal(m.retrieve(tol, interpreter="negabinary", estimator="l2_hb"),
+                                r.retrieve(tol, interpreter="negabinary", estimator="l2_hb")))
+        mode = r.file_read_mode()
+        m.close()
+        r.close()
+        del x
+        torch.cuda.empty_cache()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"workload": WORKLOAD + "; all level files written, then read into a second handle",
+            "directory": "RAM-backed (/dev/shm)" if base else "temporary directory", "bytes": nbytes,
+            "write_seconds": t_w, "write_gbs": nbytes / t_w / 1e9,
+            "read_seconds": t_r, "read_gbs": nbytes / t_r / 1e9,
+            "read_path": {1: "cuFile (GPUDirect Storage)", 0: "pread into pinned staging + async copies"}.get(mode, "none"),
+            "retrieval_identical": same}
 
 
 def call_export(mdr, level, host_tensor):

@@ -279,6 +279,18 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t capacity
  * metadata has stopping indices but no marker (the reference's zstd stage)
  * return PRODM_EUNSUPPORTED. */
 int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream);
+/* Level files (ConcatLevelFileWriter / ConcatLevelFileRetriever,
+ * FileWriter.hpp:13-39, FileRetriever.hpp:15-35). load_level_file reads bytes
+ * [file_offset, file_offset + bytes) of a level file straight into device
+ * memory as the level's data at level_offset, like prodm_mdr_load_level: via
+ * cuFile (GPUDirect Storage) where its driver opens and the file registers,
+ * else via pread into pinned buffers whose asynchronous copies overlap the
+ * next read. read_mode: 1 cuFile, 0 pinned, -1 no read yet. write_level_file
+ * writes the level file (the bytes of prodm_mdr_export_level). */
+int prodm_mdr_load_level_file(prodm_mdr* h, int level, const char* path, uint64_t file_offset, uint64_t level_offset,
+                              uint64_t bytes, void* stream);
+int prodm_mdr_write_level_file(prodm_mdr* h, int level, const char* path, void* stream);
+int prodm_mdr_file_read_mode(prodm_mdr* h, int* read_mode);
 int prodm_mdr_retrieve(prodm_mdr* h, double tolerance, int interpreter, int estimator, double s, void* d_out,
                        void* stream);
 /* the two halves of prodm_mdr_retrieve: the interpreter alone (updates the

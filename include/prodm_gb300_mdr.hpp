@@ -633,13 +633,8 @@ class GpuComposedRefactor {
         cuda_check(cudaMemcpy(d.get(), data, n * sizeof(T), cudaMemcpyHostToDevice), "H2D");
         check(prodm_mdr_set_lossless(h_, latter_, nullptr), "prodm_mdr_set_lossless");
         check(prodm_mdr_refactor(h_, d.get(), nullptr), "prodm_mdr_refactor");
-        for (int l = 0; l <= target_level; l++) {
-            uint64_t len = 0;
-            check(prodm_mdr_export_level(h_, l, nullptr, 0, 1, &len, nullptr), "prodm_mdr_export_level");
-            std::vector<uint8_t> buf(len);
-            check(prodm_mdr_export_level(h_, l, buf.data(), len, 1, &len, nullptr), "prodm_mdr_export_level");
-            write_file(files_.at(l), buf);
-        }
+        for (int l = 0; l <= target_level; l++)
+            check(prodm_mdr_write_level_file(h_, l, files_.at(l).c_str(), nullptr), "prodm_mdr_write_level_file");
         write_metadata();
     }
     void write_metadata() const {
@@ -702,7 +697,6 @@ class GpuComposedReconstructor {
         sizes_.assign(nl * B, 0);
         check(prodm_mdr_level_info(h_, sizes_.data(), nullptr, nullptr, nullptr), "prodm_mdr_level_info");
         loaded_.assign(nl, 0);
-        files_data_.assign(nl, std::vector<uint8_t>());
         out_.resize(product(dims_) * sizeof(T));
         host_.assign(product(dims_), (T)0);
     }
@@ -716,10 +710,9 @@ class GpuComposedReconstructor {
             uint64_t need = 0;
             for (int p = 0; p < idx[l]; p++) need += sizes_[l * B_ + p];
             if (need > loaded_[l]) {   // ConcatLevelFileRetriever: read the next bytes of the level file
-                if (files_data_[l].empty()) files_data_[l] = read_file(files_.at(l));
-                check(prodm_mdr_load_level(h_, l, files_data_[l].data() + loaded_[l], loaded_[l], need - loaded_[l], 1,
-                                           nullptr),
-                      "prodm_mdr_load_level");
+                check(prodm_mdr_load_level_file(h_, l, files_.at(l).c_str(), loaded_[l], loaded_[l], need - loaded_[l],
+                                                nullptr),
+                      "prodm_mdr_load_level_file");
                 loaded_[l] = need;
             }
             retrieved_ += loaded_[l];
@@ -752,7 +745,6 @@ class GpuComposedReconstructor {
     std::vector<uint32_t> dims_, sizes_;
     int nl_ = 0, B_ = 0;
     std::vector<uint64_t> loaded_;
-    std::vector<std::vector<uint8_t>> files_data_;
     DeviceBuffer out_;
     std::vector<T> host_;
     size_t retrieved_ = 0;

@@ -351,6 +351,23 @@ class MDRField:
             ptr, host, n = C.c_void_p(src.data_ptr()), 0 if src.is_cuda else 1, src.numel()
         call("prodm_mdr_load_level", self.h, level, ptr, int(offset), int(n), host, _stream(stream))
 
+    def load_level_file(self, level, path, file_offset=0, level_offset=0, nbytes=None, stream=None):
+        """Bytes of a level file straight into device memory (cuFile or pinned staging)."""
+        import os
+        if nbytes is None:
+            nbytes = os.path.getsize(path) - int(file_offset)
+        call("prodm_mdr_load_level_file", self.h, level, str(path).encode(), int(file_offset), int(level_offset),
+             int(nbytes), _stream(stream))
+
+    def write_level_file(self, level, path, stream=None):
+        call("prodm_mdr_write_level_file", self.h, level, str(path).encode(), _stream(stream))
+
+    def file_read_mode(self):
+        """1: cuFile (GPUDirect Storage), 0: pinned staging, -1: no file read yet."""
+        m = C.c_int()
+        call("prodm_mdr_file_read_mode", self.h, C.byref(m))
+        return m.value
+
     def retrieve_planes(self, index, out=None, stream=None):
         if out is None:
             out = torch.empty(self.shape, dtype=self.dtype, device="cuda")

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -576,6 +577,7 @@ struct prodm_mdr {
     std::vector<uint64_t> ll_cloaded, ll_rawoff;   // stored bytes loaded, raw bytes expanded, per level
     std::vector<int> ll_expanded;                  // planes expanded per level
     std::vector<uint32_t> ll_stored;               // loading: stored sizes from the metadata
+    FileStaging* fstage = nullptr;                 // level-file reads: staging buffers
     uint32_t* pbcounts = nullptr;                  // per-bit: first-one counts, 64 per level
     int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
     std::vector<void*> allocs;
@@ -648,6 +650,7 @@ struct prodm_mdr {
         return PRODM_OK;
     }
     ~prodm_mdr() {
+        if (fstage) file_staging_free(fstage);
         for (auto& p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (auto e : pool) cudaEventDestroy(e);
         for (void* p : allocs) cudaFree(p);
@@ -1881,6 +1884,40 @@ int prodm_mdr_load_level(prodm_mdr* h, int level, const void* src, uint64_t off,
     if (level < 0 || level > h->g.L) return fail(PRODM_EINVAL, "level out of range");
     if (h->from_files && h->ll_latter >= 0) return mdr_ll_load(h, level, src, off, bytes, host, (cudaStream_t)stream);
     return mdr_load_level(h, level, src, off, bytes, host, (cudaStream_t)stream);
+}
+
+int prodm_mdr_load_level_file(prodm_mdr* h, int level, const char* path, uint64_t file_offset, uint64_t level_offset,
+                              uint64_t bytes, void* stream) {
+    if (!h || !path) return fail(PRODM_EINVAL, "NULL pointer");
+    if (level < 0 || level > h->g.L) return fail(PRODM_EINVAL, "level out of range");
+    if (!h->from_files) return fail(PRODM_EINVAL, "load_level_file: load the metadata first");
+    cudaStream_t st = (cudaStream_t)stream;
+    auto sink = [&](const void* src, uint64_t at, uint64_t n, int host) -> int {
+        return h->ll_latter >= 0 ? mdr_ll_load(h, level, src, level_offset + at, n, host, st)
+                                 : mdr_load_level(h, level, src, level_offset + at, n, host, st);
+    };
+    return read_file_range(h->fstage, path, file_offset, bytes, sink, st, nullptr);
+}
+
+int prodm_mdr_write_level_file(prodm_mdr* h, int level, const char* path, void* stream) {
+    if (!h || !path) return fail(PRODM_EINVAL, "NULL pointer");
+    uint64_t len = 0;
+    int rc = prodm_mdr_export_level(h, level, nullptr, 0, 1, &len, stream);
+    if (rc) return rc;
+    std::vector<uint8_t> buf(len);
+    if ((rc = prodm_mdr_export_level(h, level, buf.data(), len, 1, &len, stream))) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(PRODM_EINVAL, std::string("cannot write ") + path);
+    const size_t w = len ? std::fwrite(buf.data(), 1, len, f) : 0;
+    const int c = std::fclose(f);
+    if (w != len || c != 0) return fail(PRODM_EINVAL, std::string("short write to ") + path);
+    return PRODM_OK;
+}
+
+int prodm_mdr_file_read_mode(prodm_mdr* h, int* mode) {
+    if (!h || !mode) return fail(PRODM_EINVAL, "NULL pointer");
+    *mode = h->fstage ? file_staging_mode(h->fstage) : -1;
+    return PRODM_OK;
 }
 
 int prodm_mdr_retrieve_planes(prodm_mdr* h, const uint8_t* hidx, void* out, void* stream) {

@@ -1,5 +1,7 @@
 // Host-side launchers of the CUDA kernels (declarations).
 #pragma once
+#include <functional>
+
 #include "common.cuh"
 
 namespace prodm {
@@ -141,6 +143,15 @@ int ll_stream_sizes(const uint8_t* d_raw, const uint32_t* h_sizes, int B, uint32
 // concatenated into d_out (capacity cap); h_raw_sizes: their raw sizes
 int ll_decompress_planes(const uint8_t* d_in, const uint32_t* h_sizes, const uint8_t* h_flags, int num, uint8_t* d_out,
                          uint64_t cap, uint32_t* h_raw_sizes, cudaStream_t st);
+
+// fileio.cu: byte ranges of a file into the handle's loader (sink(src,
+// offset within the range, bytes, src_is_host)); *mode: 1 cuFile, 0 pinned
+struct FileStaging;
+void file_staging_free(FileStaging* s);
+int file_staging_mode(const FileStaging* s);
+int read_file_range(FileStaging*& fs, const char* path, uint64_t file_off, uint64_t bytes,
+                    const std::function<int(const void*, uint64_t, uint64_t, int)>& sink, cudaStream_t st,
+                    int* mode);
 
 // pack.cu
 int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,
