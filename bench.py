@@ -574,9 +574,10 @@ def run_qoi(n=257, levels=6, rels=(1e-2, 1e-3, 1e-4)):
 
     V = [v.cuda() for v in fields.divergence_free_velocity(n, seed=11)]
     rho = fields.lognormal_density(n, seed=12).cuda()
+    ge = ge_utilities([v.double() for v in V], rho.double())
     out = {"workload": "Vx, Vy, Vz %d^3 fp32 divergence-free random Fourier modes (|k| <= 16), rho lognormal "
                        "(sigma 0.5); %d levels, 32 planes, grouped encoder, hierarchical basis, L-inf tables" %
-                       (n, levels + 1), "cases": []}
+                       (n, levels + 1), "cases": [], "ge_utilities": ge}
     for kind in ("vmag", "ke"):
         data = V + ([rho] if kind == "ke" else [])
         q = qoi.qoi_value(kind, [v.double() for v in V], rho.double() if kind == "ke" else None)
@@ -771,6 +772,16 @@ def run_lossless(reps=3):
     torch.cuda.synchronize()
     t_d = (time.time() - t0) / reps
     same = bool(torch.equal(back, blob))
+    # CPU beside it: the oracle's single-thread ZCB compression of planes 0-3
+    import oracle
+    O = oracle.oracle()
+    host = blob.cpu().numpy()
+    offs = np.concatenate([[0], np.cumsum(sizes.astype(np.int64))])
+    t0 = time.time()
+    for p in range(4):
+        O.zcb_compress(host[offs[p]:offs[p + 1]])
+    t_cpu = time.time() - t0
+    cpu_bytes = int(offs[4])
     m.close()
     del x, out, blob, comp, back
     torch.cuda.empty_cache()
@@ -782,7 +793,9 @@ def run_lossless(reps=3):
             "finest_level": {"raw_bytes": nbytes, "stopping_index": stop, "stored_bytes": int(csz.astype(np.int64).sum()),
                              "compress_seconds": t_c, "compress_gbs": nbytes / t_c / 1e9,
                              "decompress_seconds": t_d, "decompress_gbs": nbytes / t_d / 1e9,
-                             "round_trip_identical": same}}
+                             "round_trip_identical": same},
+            "cpu_baseline": {"kind": "port", "cores": 1, "sample": "oracle ZCB compression of planes 0-3 of the "
+                             "finest level (%d bytes)" % cpu_bytes, "value": cpu_bytes / t_cpu / 1e9, "unit": "GB/s"}}
 
 
 def run_files():
@@ -809,6 +822,12 @@ def run_files():
             m.write_level_file(l, pth)
         t_w = time.time() - t0
         nbytes = sum(os.path.getsize(pth) for pth in paths)
+        # the file path's one-time set-up (cuFile's driver, staging buffers) on a
+        # throw-away handle first
+        w = api.MDRField(SHAPE, torch.float32, LEVELS, BITPLANES, "negabinary", "hierarchical", "squared")
+        w.load_metadata(m.metadata())
+        w.load_level_file(0, paths[0])
+        w.close()
         r = api.MDRField(SHAPE, torch.float32, LEVELS, BITPLANES, "negabinary", "hierarchical", "squared")
         r.load_metadata(m.metadata())
         torch.cuda.synchronize()
@@ -822,6 +841,12 @@ def run_files():
         same = bool(torch.equal(m.retrieve(tol, interpreter="negabinary", estimator="l2_hb"),
                                 r.retrieve(tol, interpreter="negabinary", estimator="l2_hb")))
         mode = r.file_read_mode()
+        t0 = time.time()   # CPU beside it: the files read into host memory (ConcatLevelFileRetriever's fread)
+        host_bytes = 0
+        for pth in paths:
+            with open(pth, "rb") as f:
+                host_bytes += len(f.read())
+        t_h = time.time() - t0
         m.close()
         r.close()
         del x
@@ -833,7 +858,52 @@ def run_files():
             "write_seconds": t_w, "write_gbs": nbytes / t_w / 1e9,
             "read_seconds": t_r, "read_gbs": nbytes / t_r / 1e9,
             "read_path": {1: "cuFile (GPUDirect Storage)", 0: "pread into pinned staging + async copies"}.get(mode, "none"),
-            "retrieval_identical": same}
+            "retrieval_identical": same,
+            "cpu_baseline": {"kind": "reference-style", "cores": 1, "sample": "every level file read into host "
+                             "memory", "value": host_bytes / t_h / 1e9, "unit": "GB/s"}}
+
+
+def ge_utilities(V, rho, reps=5):
+    """GE quantities of interest on the device (prodm_qoi_ge_values /
+    prodm_qoi_ge_bounds) on fp64 fields: V_TOT, T, C, Mach, PT, mu and the V_TOT
+    / T error estimates; algorithmic bytes (fields read + results written) per
+    CUDA-event time, beside the oracle's single-thread evaluation of a sample."""
+    import numpy as np
+    import torch
+    import oracle
+    from prodm_gb300 import api
+
+    N = V[0].numel()
+    vx, vy, vz = (v.reshape(-1) for v in V)
+    p = (1e5 * (1.0 + 0.1 * rho)).reshape(-1)      # pressure-like field around 1 bar
+    d = rho.reshape(-1)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    api.qoi_ge_values(vx, vy, vz, p, d)
+    api.qoi_ge_bounds([vx, vy, vz], (0.01, 0.01, 0.01), p, d, 10.0, 1e-4)
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        api.qoi_ge_values(vx, vy, vz, p, d)
+    ev[1].record()
+    for _ in range(reps):
+        api.qoi_ge_bounds([vx, vy, vz], (0.01, 0.01, 0.01), p, d, 10.0, 1e-4)
+    ev[2].record()
+    torch.cuda.synchronize()
+    t_v = ev[0].elapsed_time(ev[1]) / reps / 1e3
+    t_b = ev[1].elapsed_time(ev[2]) / reps / 1e3
+    k = min(N, 1 << 21)
+    h = [t[:k].cpu().numpy() for t in (vx, vy, vz, p, d)]
+    O = oracle.oracle()
+    t0 = time.time()
+    O.qoi_values(*h)
+    t_c = time.time() - t0
+    peak, src = measured_peak()
+    bv, bb = 11 * 8 * N, 7 * 8 * N
+    return {"points": N, "values_ms": t_v * 1e3, "values_gbs": bv / t_v / 1e9, "values_frac": bv / t_v / 1e9 / peak,
+            "bounds_ms": t_b * 1e3, "bounds_gbs": bb / t_b / 1e9, "bounds_frac": bb / t_b / 1e9 / peak,
+            "bytes_model": "values: 5 fields read + 6 written; bounds: 5 read + 2 written (8 bytes each)",
+            "cpu_baseline": {"kind": "port", "cores": 1, "sample": "oracle qoi_values on %d points" % k,
+                             "points_per_s": k / t_c, "device_points_per_s": N / t_v}}
 
 
 def call_export(mdr, level, host_tensor):

@@ -10,12 +10,14 @@
 // ordinary loading path (the lossless stage's stored bytes included).
 #include <dlfcn.h>
 #include <fcntl.h>
+#include <sys/stat.h>
 #include <unistd.h>
 
 #include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -57,6 +59,10 @@ CuFileApi& cufile() {
 
 constexpr uint64_t kChunk = 16ull << 20;
 
+// file systems on which cuFile refused to register a file: not tried again
+std::mutex g_noreg_mu;
+std::set<dev_t> g_noreg;
+
 }  // namespace
 
 // per-handle staging (two device and two pinned buffers of kChunk bytes, and
@@ -95,12 +101,23 @@ int read_file_range(FileStaging*& fs, const char* path, uint64_t file_off, uint6
     CuFileApi& cf = cufile();
     CUfileHandle_t fh{};
     bool direct = false;
-    if (cf.ok) {
+    struct stat sb;
+    const bool have_dev = fstat(fd, &sb) == 0;
+    bool refused = false;
+    if (have_dev) {
+        std::lock_guard<std::mutex> g(g_noreg_mu);
+        refused = g_noreg.count(sb.st_dev) != 0;
+    }
+    if (cf.ok && !refused) {
         CUfileDescr_t d;
         std::memset(&d, 0, sizeof(d));
         d.handle.fd = fd;
         d.type = CU_FILE_HANDLE_TYPE_OPAQUE_FD;
         direct = cf.reg(&fh, &d).err == CU_FILE_SUCCESS;
+        if (!direct && have_dev) {
+            std::lock_guard<std::mutex> g(g_noreg_mu);
+            g_noreg.insert(sb.st_dev);
+        }
     }
     fs->mode = direct ? 1 : 0;
     if (mode_out) *mode_out = fs->mode;

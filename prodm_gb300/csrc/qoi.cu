@@ -3,7 +3,8 @@
 //
 // Values: V_TOT = |V|, T = P / (D R), C = sqrt(gamma R T), Mach = V_TOT / C,
 // PT = P (1 + (gamma - 1) / 2 Mach^2)^(7/2), mu = mu_r (T / T_r)^(3/2)
-// (T_r + S) / (T + S), in double as qoi_utils.hpp:135-165 computes them.
+// (T_r + S) / (T + S), in double as qoi_utils.hpp:135-165 computes them;
+// the reference's pow(x, 7) and pow(x, 3) are multiplication chains here.
 // Estimates (qoi_utils.hpp:18-98): |V_TOT~ - V_TOT| <= sqrt-rule(V^2,
 // sum_f square-rule(V_f, eb_f)) as halving_Vtot.cpp:38-45 forms it, and
 // |T~ - T| <= division-rule(P, D, eb_P, eb_D) / R (0 where the rule gives no
@@ -49,9 +50,13 @@ __global__ void k_qoi_values(const double* __restrict__ vx, const double* __rest
         const double c = sqrt(__dmul_rn(__dmul_rn(Ge::gamma, Ge::R), t));
         const double m = v / c;
         const double mt = __dadd_rn(1.0, __dmul_rn(__dmul_rn((Ge::gamma - 1) / 2, m), m));
-        const double ptv = __dmul_rn(p[i], sqrt(pow(mt, 7.0)));
+        // x^7 and x^3 by multiplication chains instead of pow (GB300's FP64
+        // pipe is slow; the chains stay within a few units in the last place)
+        const double mt2 = __dmul_rn(mt, mt), mt4 = __dmul_rn(mt2, mt2);
+        const double ptv = __dmul_rn(p[i], sqrt(__dmul_rn(__dmul_rn(mt4, mt2), mt)));
         const double trs = (Ge::T_r + Ge::S) / __dadd_rn(t, Ge::S);
-        const double tt3 = sqrt(pow(t / Ge::T_r, 3.0));
+        const double tr = t / Ge::T_r;
+        const double tt3 = sqrt(__dmul_rn(__dmul_rn(tr, tr), tr));
         vtot[i] = v;
         temp[i] = t;
         cs[i] = c;
