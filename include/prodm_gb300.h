@@ -205,7 +205,9 @@ int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint
 /* ---------------------------------------------------------------------------
  * GE quantities of interest (fp64 fields), for QoI-bounded retrieval.
  * prodm_qoi_ge_values -- QoI::compute_QoIs (qoi_utils.hpp:135-165): V_TOT, T,
- * C, Mach, PT and mu of every point of (Vx, Vy, Vz, P, D), n values each.
+ * C, Mach, PT and mu of every point of (Vx, Vy, Vz, P, D), n values each
+ * (products, quotients and square roots as the reference rounds them; its
+ * pow(x, 7) and pow(x, 3) as multiplication chains, within a few ulp).
  * prodm_qoi_ge_bounds -- the pointwise error estimates the GE drivers form
  * from the propagation rules (qoi_utils.hpp:18-98): V_TOT from the square
  * and square-root rules given |error| <= eb_v* of each velocity component

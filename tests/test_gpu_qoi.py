@@ -57,7 +57,8 @@ def test_guided_meets_bound_with_fewer_bytes(kind, rel):
 def test_ge_qoi_device_kernels_match_reference_fixtures():
     """prodm_qoi_ge_values / prodm_qoi_ge_bounds against the reference's
     qoi_utils.hpp outputs (tests/golden/qoi.npz): products, quotients and
-    square roots bit for bit; PT and mu go through pow, within 1e-14."""
+    square roots bit for bit; PT and mu (the reference takes pow(x, 7) and
+    pow(x, 3), the kernel multiplication chains) within 1e-14."""
     import os
     from prodm_gb300 import api
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", "qoi.npz"))
