@@ -408,6 +408,34 @@ __device__ __forceinline__ void pz_group(uint64_t W, uint32_t U, int nv, uint32_
     cnt = d;
 }
 
+// A group whose values are all unseen is a stream of the tokens "0" and
+// "1 s": a 1 at a token start escapes the next bit. Runs of 1s start at token
+// starts; inside a run the odd offsets are escaped, and the bit after a run
+// of odd length is escaped too (the run-start parities split by adding the
+// run starts: the carry clears a run and marks its end).
+__device__ __forceinline__ uint64_t pz_escaped(uint64_t W) {
+    constexpr uint64_t EVEN = 0x5555555555555555ull, ODD = 0xaaaaaaaaaaaaaaaaull;
+    const uint64_t starts = W & ~(W << 1);
+    const uint64_t es = W + (starts & EVEN), os = W + (starts & ODD);
+    const uint64_t inside = ((W & ~es) & ODD) | ((W & ~os) & EVEN);
+    const uint64_t after = ((es & ~W) & ODD) | ((os & ~W) & EVEN);
+    return inside | after;
+}
+// position of zero number e (from 0) of E: binary search on popcounts
+__device__ __forceinline__ int pz_select_zero(uint64_t E, int e) {
+    const uint64_t Z = ~E;
+    int pos = 0, rem = e;
+#pragma unroll
+    for (int step = 32; step > 0; step >>= 1) {
+        const int c = __popcll((Z >> pos) & ((1ull << step) - 1ull));
+        if (c <= rem) {
+            rem -= c;
+            pos += step;
+        }
+    }
+    return pos;
+}
+
 // one chunk (32 groups, lane g = group g0 + g) of one plane; U / S: the
 // lane's group's unseen and sign masks, updated; returns the group's word.
 // ws: the chunk's stream as 128 32-bit words (word 2*pb + i at ws[i])
@@ -456,7 +484,15 @@ __device__ __forceinline__ uint32_t pz_chunk(PlaneReader& r, bool first, uint64_
         const uint32_t x0 = ws[k], x1 = ws[k + 1], x2 = ws[k + 2];
         const uint64_t W = ((uint64_t)__funnelshift_r(x1, x2, sh) << 32) | __funnelshift_r(x0, x1, sh);
         uint32_t Mj, SG, cnt;
-        pz_group(W, Uj, nvj, Mj, SG, cnt);
+        if (Uj == bits_below(nvj)) {   // all unseen: bit-parallel, one value per lane
+            const int q = pz_select_zero(pz_escaped(W), lane);
+            const bool b = lane < nvj && ((W >> q) & 1ull);
+            Mj = __ballot_sync(FULL, b);
+            SG = __ballot_sync(FULL, b && ((W >> (q + 1)) & 1ull));
+            cnt = __popc(Mj);
+        } else {
+            pz_group(W, Uj, nvj, Mj, SG, cnt);
+        }
         const bool mine = lane == j;
         M = mine ? Mj : M;
         extra = mine ? cnt : extra;
