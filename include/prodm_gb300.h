@@ -264,7 +264,10 @@ int prodm_mdr_level_info(prodm_mdr* h, uint32_t* h_sizes, double* h_bounds, doub
 /* reference metadata bytes (ComposedRefactor.hpp:48-67) followed by an
  * extension carrying the squared-error tables; *len receives the size. */
 int prodm_mdr_metadata(prodm_mdr* h, uint8_t* h_buf, size_t capacity, size_t* len, void* stream);
-/* reference level-file bytes of one level into dst (device or host). */
+/* reference level-file bytes of one level into dst: dst_is_host 0 device
+ * memory, 1 host memory (returns when the bytes are there), 2 pinned host
+ * memory filled asynchronously in stream order (synchronise the stream, or
+ * wait on an event recorded after the call, before reading it). */
 int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t capacity, int dst_is_host, uint64_t* len,
                            void* stream);
 

@@ -317,6 +317,19 @@ class MDRField:
         call("prodm_mdr_export_level", self.h, level, _ptr(buf), n.value, 0, C.byref(n), _stream(stream))
         return buf[:n.value]
 
+    def export_level_into(self, level, out, stream=None):
+        """The level file's bytes into `out` (a uint8 tensor: CUDA, or pinned
+        host memory filled asynchronously in the stream's order); returns the
+        byte count."""
+        if out.dtype != torch.uint8 or not out.is_contiguous():
+            raise ValueError("expected a contiguous uint8 tensor")
+        if not out.is_cuda and not out.is_pinned():
+            raise ValueError("host output must be pinned memory")
+        n = C.c_uint64()
+        call("prodm_mdr_export_level", self.h, level, C.c_void_p(out.data_ptr()), out.numel(),
+             0 if out.is_cuda else 2, C.byref(n), _stream(stream))
+        return n.value
+
     def set_lossless(self, latter_index=26, stream=None):
         """Lossless stage on (latter_index >= 0, the reference's default 26) or off (None / < 0)."""
         call("prodm_mdr_set_lossless", self.h, -1 if latter_index is None else int(latter_index), _stream(stream))

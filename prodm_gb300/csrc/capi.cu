@@ -578,6 +578,8 @@ struct prodm_mdr {
     std::vector<int> ll_expanded;                  // planes expanded per level
     std::vector<uint32_t> ll_stored;               // loading: stored sizes from the metadata
     FileStaging* fstage = nullptr;                 // level-file reads: staging buffers
+    std::vector<uint32_t> hsz;                     // host copy of `sizes` (export), valid while hsz_valid
+    bool hsz_valid = false;
     uint32_t* pbcounts = nullptr;                  // per-bit: first-one counts, 64 per level
     int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
     std::vector<void*> allocs;
@@ -1250,6 +1252,7 @@ int mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, cudaStream_t
     PRODM_CUDA(cudaMemsetAsync(h->index, 0, nl, st));
     PRODM_CUDA(cudaStreamSynchronize(st));
     h->from_files = true;
+    h->hsz_valid = false;
     h->loaded.assign(nl, 0);
     h->unpacked.assign(nl, 0);
     h->header_done.assign(nl, 0);
@@ -1638,6 +1641,7 @@ int prodm_mdr_refactor(prodm_mdr* h, const void* field, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (h->from_files) h->ll_latter = -1;   // a loaded stage does not carry over to a new refactor
     h->from_files = false;
+    h->hsz_valid = false;
     const int rc = h->cfg.dtype == PRODM_F64 ? mdr_refactor<double>(h, (const double*)field, st)
                                              : mdr_refactor<float>(h, (const float*)field, st);
     if (rc) return rc;
@@ -1704,12 +1708,19 @@ int prodm_mdr_metadata(prodm_mdr* h, uint8_t* buf, size_t cap, size_t* len, void
 
 // the level file with raw (uncompressed) streams; dsizes: the level's raw
 // plane sizes on the device
+// (hsizes: the same on the host when the caller has them, else NULL);
+// dst_is_host == 2: pinned host memory, left to complete in stream order
 static int export_raw_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int dst_is_host, uint64_t* len,
-                            const uint32_t* dsizes, cudaStream_t st) {
+                            const uint32_t* dsizes, cudaStream_t st, const uint32_t* hsizes = nullptr) {
     const int B = h->B;
+    const bool async = dst_is_host == 2;
     std::vector<uint32_t> sz(B);
-    PRODM_CUDA(cudaMemcpyAsync(sz.data(), dsizes, B * 4, cudaMemcpyDeviceToHost, st));
-    PRODM_CUDA(cudaStreamSynchronize(st));
+    if (hsizes) {
+        std::memcpy(sz.data(), hsizes, B * 4);
+    } else {
+        PRODM_CUDA(cudaMemcpyAsync(sz.data(), dsizes, B * 4, cudaMemcpyDeviceToHost, st));
+        PRODM_CUDA(cudaStreamSynchronize(st));
+    }
     uint64_t total = 0;
     for (int p = 0; p < B; p++) total += sz[p];
     if (len) *len = total;
@@ -1720,7 +1731,7 @@ static int export_raw_level(prodm_mdr* h, int level, void* dst, uint64_t cap, in
         const size_t row = (size_t)h->nblocks[level] * h->es;
         PRODM_CUDA(cudaMemcpy2DAsync(dst, row, src, (size_t)h->plane_cap[level] * h->es, row, B,
                                      dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
-        PRODM_CUDA(cudaStreamSynchronize(st));
+        if (!async) PRODM_CUDA(cudaStreamSynchronize(st));
         return PRODM_OK;
     }
     if (h->pb) {   // rows -> reference streams (8-byte aligned staging where dst is not)
@@ -1740,7 +1751,7 @@ static int export_raw_level(prodm_mdr* h, int level, void* dst, uint64_t cap, in
         }
         cudaFreeAsync(tmp, st);
         if (rc) return rc;
-        PRODM_CUDA(cudaStreamSynchronize(st));
+        if (!async) PRODM_CUDA(cudaStreamSynchronize(st));
         return PRODM_OK;
     }
     uint8_t* tmp = (uint8_t*)dst;
@@ -1752,7 +1763,7 @@ static int export_raw_level(prodm_mdr* h, int level, void* dst, uint64_t cap, in
         PRODM_CUDA(cudaMemcpyAsync(dst, tmp, total, cudaMemcpyDeviceToHost, st));
         cudaFreeAsync(tmp, st);
     }
-    PRODM_CUDA(cudaStreamSynchronize(st));
+    if (!async) PRODM_CUDA(cudaStreamSynchronize(st));
     return PRODM_OK;
 }
 
@@ -1804,7 +1815,19 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
     const int L = h->g.L, B = h->B;
     if (level < 0 || level > L) return fail(PRODM_EINVAL, "level out of range");
     cudaStream_t st = (cudaStream_t)stream;
-    if (h->ll_latter < 0) return export_raw_level(h, level, dst, cap, dst_is_host, len, h->sizes + (uint64_t)level * B, st);
+    if (dst_is_host < 0 || dst_is_host > 2) return fail(PRODM_EINVAL, "dst_is_host must be 0, 1 or 2");
+    if (h->ll_latter < 0) {
+        // the plane sizes, on the host once per refactor: later exports need no
+        // synchronisation before their copies
+        if (!h->hsz_valid) {
+            h->hsz.resize((size_t)(L + 1) * B);
+            PRODM_CUDA(cudaMemcpyAsync(h->hsz.data(), h->sizes, (L + 1) * B * 4, cudaMemcpyDeviceToHost, st));
+            PRODM_CUDA(cudaStreamSynchronize(st));
+            h->hsz_valid = true;
+        }
+        return export_raw_level(h, level, dst, cap, dst_is_host, len, h->sizes + (uint64_t)level * B, st,
+                                h->hsz.data() + (size_t)level * B);
+    }
     // lossless stage: the raw level into scratch, then its stored streams
     std::vector<uint32_t> raw(B), stored(B);
     PRODM_CUDA(cudaMemcpyAsync(raw.data(), h->rsizes + (uint64_t)level * B, B * 4, cudaMemcpyDeviceToHost, st));
@@ -1837,6 +1860,7 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
 int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
     if (h->from_files) return fail(PRODM_EINVAL, "set_lossless: a handle fed from files takes the stage from its metadata");
+    h->hsz_valid = false;
     cudaStream_t st = (cudaStream_t)stream;
     const int nl = h->g.L + 1, B = h->B;
     if (latter_index < 0) {   // off: the raw sizes back to the cost model

@@ -57,6 +57,41 @@ def test_level_files_round_trip(shape, L, dt, B, enc, col, interp, est, latter, 
         assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("enc,dt,B,latter", [("negabinary", torch.float32, 32, None),
+                                              ("grouped", torch.float32, 32, None),
+                                              ("perbit", torch.float64, 60, None),
+                                              ("grouped", torch.float32, 32, 26)])
+def test_export_into_pinned_on_a_side_stream(enc, dt, B, latter):
+    """exports into pinned memory are stream-ordered: issued finest level
+    first on a second stream, each is the level file once its event is done;
+    device exports and a refactor with other data invalidate nothing stale"""
+    from prodm_gb300 import fields
+    shape, L = (45, 38, 29), 3
+    m = api().MDRField(shape, dt, L, B, enc, "hierarchical", "max")
+    for seed in (1, 2):
+        x = fields.spectral_grf(shape, seed=seed, dtype=dt, device="cuda")
+        m.refactor(x)
+        if latter is not None:
+            m.set_lossless(latter)
+        want = [m.export_level(l) for l in range(L + 1)]
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        outs, evs = [None] * (L + 1), [None] * (L + 1)
+        for l in reversed(range(L + 1)):
+            outs[l] = torch.empty(len(want[l]) + 3, dtype=torch.uint8, pin_memory=True)
+            assert m.export_level_into(l, outs[l], side) == len(want[l])
+            evs[l] = torch.cuda.Event()
+            evs[l].record(side)
+        for l in range(L + 1):
+            evs[l].synchronize()
+            assert outs[l][:len(want[l])].numpy().tobytes() == want[l].tobytes(), (seed, l)
+            d = torch.empty(len(want[l]), dtype=torch.uint8, device="cuda")
+            assert m.export_level_into(l, d) == len(want[l])
+            assert d.cpu().numpy().tobytes() == want[l].tobytes(), (seed, l)
+    with pytest.raises(ValueError):
+        m.export_level_into(0, torch.empty(16, dtype=torch.uint8))      # pageable
+
+
 def test_file_errors(tmp_path):
     from prodm_gb300._lib import ProdmError
     shape = (33, 33, 33)
