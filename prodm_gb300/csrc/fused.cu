@@ -20,20 +20,6 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-__device__ __forceinline__ uint32_t transpose32f(uint32_t x, int lane) {
-#pragma unroll
-    for (int j = 16; j > 0; j >>= 1) {
-        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
-                                                                                                       : 0x55555555u;
-        const uint32_t y = __shfl_xor_sync(FULL, x, j);
-        const bool hi = (lane & j) != 0;
-        const uint32_t u = hi ? y : x, v = hi ? x : y;
-        const uint32_t t = ((u >> j) ^ v) & m;
-        x ^= hi ? t : (t << j);
-    }
-    return x;
-}
-
 __device__ __forceinline__ float pow2f_(int e) { return __int_as_float((e + 127) << 23); }
 
 __device__ __forceinline__ uint32_t natural_of(uint32_t r, uint32_t n, uint32_t nc) {
@@ -158,64 +144,136 @@ constexpr int CB_LD = 33;   // value-major coefficient rows: conflict-free both 
 
 __device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[r + (r >> 5)]; }
 
-// one fine row of odd length; M01 = odd-dim mask over dims 0/1 (0: both
-// coarse -> only odd nodes carry coefficients, ranks c; otherwise even node
-// 2c has rank c and odd node 2c+1 rank c2n + c). Lane l handles coarse
-// columns 32k + l; the corner values of D column groups are in flight at
-// once (a ring of D groups in registers, refilled as each group is used), so
-// a row waits for the L2 latency about once instead of once per group.
+// one fine row of odd length n = 2 c2n - 1; M01 = odd-dim mask over dims
+// 0/1 (0: both coarse -> only odd nodes carry coefficients, ranks c;
+// otherwise even node 2c has rank c and odd node 2c+1 rank c2n + c). The row
+// is c2n - 1 column pairs (nodes 2c, 2c+1) and a last node 2(c2n - 1). Lane l
+// handles the pairs 32k + l; the corner values of D column groups are in
+// flight at once (a ring of D groups in registers, refilled as each group is
+// used), so a row waits for the L2 latency about once instead of once per
+// group. Groups in which every lane has a pair run without bounds checks, on
+// pointers advanced once per D groups; the last node is written by lane 0.
 template <int M01>
 __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0, uint64_t cs0, uint64_t cs1,
                                                   uint32_t c2n, const float* __restrict__ cb, uint32_t rb0,
                                                   float* __restrict__ orow, int lane) {
     constexpr int NQ = M01 == 0 ? 1 : (M01 == 3 ? 4 : 2);
     constexpr int D = M01 == 3 ? 3 : 4;
-    const float* pc[4];
-    pc[0] = cb0;
-    pc[1] = cb0 + (M01 == 1 ? cs0 : cs1);
-    pc[2] = cb0 + cs0;
-    pc[3] = cb0 + cs0 + cs1;
-    auto load = [&](uint32_t k, float (&q)[NQ]) {
-        const uint32_t c = 32 * k + lane;
+    int64_t co[NQ];   // corner row offsets, in corner_tree order
+    co[0] = 0;
+    if constexpr (NQ == 2) co[1] = (int64_t)(M01 == 1 ? cs0 : cs1);
+    if constexpr (NQ == 4) {
+        co[1] = (int64_t)cs1;
+        co[2] = (int64_t)cs0;
+        co[3] = (int64_t)(cs0 + cs1);
+    }
+    const uint32_t P = c2n - 1;
+    if (lane == 0) {   // the last node: coarse column P
+        float q[NQ];
 #pragma unroll
-        for (int i = 0; i < NQ; i++) q[i] = c < c2n ? __ldg(pc[i] + c) : 0.f;
-    };
-    const uint32_t groups = (c2n + 31) / 32;
+        for (int i = 0; i < NQ; i++) q[i] = __ldg(cb0 + P + co[i]);
+        if constexpr (M01 == 0) orow[2 * (uint64_t)P] = q[0];
+        else orow[2 * (uint64_t)P] = __fadd_rn(cb_at(cb, rb0 + P), corner_tree(M01, q));
+    }
+    if (P == 0) return;
+    const float* pc[NQ];
+#pragma unroll
+    for (int i = 0; i < NQ; i++) pc[i] = cb0 + co[i] + lane;
+    // coefficient of rank r at cb[r + (r >> 5)]: 33 floats further per 32 ranks
+    const uint32_t re = rb0 + lane, ro = rb0 + (M01 == 0 ? 0u : c2n) + lane;
+    const float* pe = cb + re + (re >> 5);
+    const float* po = cb + ro + (ro >> 5);
+    float* o = orow + 2 * lane;
+    const int lim = (int)c2n - lane;   // column 32k + lane exists <=> 32k < lim
+    const uint32_t groups = (P + 31) >> 5, full = P >> 5;
     float ring[D][NQ];
 #pragma unroll
-    for (int d = 0; d < D; d++) load(d, ring[d]);
-    for (uint32_t k0 = 0; k0 < groups; k0 += D) {
+    for (int d = 0; d < D; d++)
+#pragma unroll
+        for (int i = 0; i < NQ; i++) ring[d][i] = 32 * d < lim ? __ldg(pc[i] + 32 * d) : 0.f;
+    const int src = (lane + 1) & 31;
+    auto pair = [&](const float (&q)[NQ], const float (&qn)[NQ], const float* e, const float* od, float* out) {
+        if constexpr (M01 == 0) {
+            out[0] = q[0];
+            out[1] = __fadd_rn(*od, avg_rn(q[0], qn[0]));
+        } else if constexpr (M01 == 3) {
+            out[0] = __fadd_rn(*e, avg_rn(avg_rn(q[0], q[1]), avg_rn(q[2], q[3])));
+            out[1] = __fadd_rn(*od, avg_rn(avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])),
+                                           avg_rn(avg_rn(q[2], qn[2]), avg_rn(q[3], qn[3]))));
+        } else {
+            out[0] = __fadd_rn(*e, avg_rn(q[0], q[1]));
+            out[1] = __fadd_rn(*od, avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])));
+        }
+    };
+    uint32_t k0 = 0;
+    for (; k0 + D <= full; k0 += D) {
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            const uint32_t k = k0 + d;
-            if (k >= groups) break;
             const float(&q)[NQ] = ring[d];
             const float(&qx)[NQ] = ring[(d + 1) % D];   // group k + 1
             // lane l < 31 takes column c+1 from lane l+1; lane 31 from lane 0 of group k+1
             float qn[NQ];
 #pragma unroll
-            for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], (lane + 1) & 31);
-            const uint32_t c2 = 32 * k + lane;
-            if (c2 < c2n) {
-                const bool odd = c2 + 1 < c2n;
-                float* o = orow + 2 * (uint64_t)c2;
-                if (M01 == 0) {
-                    o[0] = q[0];
-                    if (odd) o[1] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], qn[0]));
-                } else if (M01 == 3) {
-                    o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(avg_rn(q[0], q[1]), avg_rn(q[2], q[3])));
-                    if (odd)
-                        o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2),
-                                         avg_rn(avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])),
-                                                avg_rn(avg_rn(q[2], qn[2]), avg_rn(q[3], qn[3]))));
-                } else {
-                    o[0] = __fadd_rn(cb_at(cb, rb0 + c2), avg_rn(q[0], q[1]));
-                    if (odd)
-                        o[1] = __fadd_rn(cb_at(cb, rb0 + c2n + c2),
-                                         avg_rn(avg_rn(q[0], qn[0]), avg_rn(q[1], qn[1])));
-                }
-            }
-            load(k + D, ring[d]);   // refill: group k + D
+            for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], src);
+            pair(q, qn, pe + 33 * d, po + 33 * d, o + 64 * d);
+            const bool more = (int)(32 * (k0 + d + D)) < lim;   // refill: group k + D
+#pragma unroll
+            for (int i = 0; i < NQ; i++) ring[d][i] = more ? __ldg(pc[i] + 32 * (d + D)) : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < NQ; i++) pc[i] += 32 * D;
+        pe += 33 * D;
+        po += 33 * D;
+        o += 64 * D;
+    }
+    // the remaining groups: fewer than D complete ones and at most one partial
+    const int plim = (int)P - lane;   // pair 32k + lane exists <=> 32k < plim
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        const uint32_t k = k0 + d;
+        if (k >= groups) break;
+        const float(&q)[NQ] = ring[d];
+        const float(&qx)[NQ] = ring[(d + 1) % D];
+        float qn[NQ];
+#pragma unroll
+        for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], src);
+        if ((int)(32 * k) < plim) pair(q, qn, pe + 33 * d, po + 33 * d, o + 64 * d);
+        const bool more = (int)(32 * (k + D)) < lim;
+#pragma unroll
+        for (int i = 0; i < NQ; i++) ring[d][i] = more ? __ldg(pc[i] + 32 * (d + D)) : 0.f;
+    }
+}
+
+
+// decode of a staged tile: two threads per 32-value block, each transposing
+// one half; rows are taken in reverse tile order, so that value v's word has
+// plane p at bit num - 1 - p, its negabinary digits in place
+// (NegaBinaryBPEncoder.hpp:132-192); value v of block t -> cb[t * CB_LD + v].
+// FAST: 2^(exp - num) is a normal float (one exact multiplication).
+template <bool FAST>
+__device__ __forceinline__ void decode_tile(const uint32_t* __restrict__ tile, float* __restrict__ cb, uint32_t nbk,
+                                            int num, int exp, bool neg, float dscale) {
+    for (uint32_t i = threadIdx.x; i < 2 * nbk; i += blockDim.x) {
+        const uint32_t t = i >> 1;
+        const int half = i & 1;
+        float* dst = cb + t * CB_LD + 16 * half;
+        uint32_t R[32];
+        const uint4* src = reinterpret_cast<const uint4*>(tile + t * TB_LD);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const uint4 w = src[q];
+            R[31 - 4 * q] = w.x;
+            R[30 - 4 * q] = w.y;
+            R[29 - 4 * q] = w.z;
+            R[28 - 4 * q] = w.w;
+        }
+        uint32_t a[16];
+        transpose32_half(R, half, a);
+#pragma unroll
+        for (int v = 0; v < 16; v++) {
+            const int32_t iv = nb_to_bin(a[v]);
+            if constexpr (FAST) dst[v] = (float)iv * dscale;
+            else dst[v] = neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num);
         }
     }
 }
@@ -257,11 +315,14 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
         fb = abase >> 5;
         nbk = (uint32_t)(((zbase + zlen - 1) >> 5) - fb + 1);
     };
-    // plane p of block j -> tile[j * TB_LD + p]; warp w copies planes w, w+8, ..
+    // plane p of block j -> tile[j * TB_LD + 32 - num + p] (so that the
+    // transposed words hold plane p at bit num - 1 - p); warp w copies planes
+    // w, w+8, ..
+    const int poff = 32 - num;
     auto fetch = [&](uint64_t fb, uint32_t nbk, uint32_t* tile) {
         for (int p = warp; p < num; p += 8) {
             const uint32_t* src = base + (uint64_t)p * stride + fb;
-            for (uint32_t j = lane; j < nbk; j += 32) cp_async4(tile + j * TB_LD + p, src + j);
+            for (uint32_t j = lane; j < nbk; j += 32) cp_async4(tile + j * TB_LD + poff + p, src + j);
         }
         cp_async_commit();
     };
@@ -276,9 +337,9 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
         block_range(rho0, s_fb[0], s_nbk[0]);
         if (rho0 + step < rows) block_range(rho0 + step, s_fb[1], s_nbk[1]);
     }
-    // planes >= num stay zero in the tile
-    for (uint32_t i = threadIdx.x; i < tld * (32 - num); i += blockDim.x) {
-        const uint32_t row = i / (32 - num), p = num + (i - row * (32 - num));
+    // the tile words of the planes not retrieved stay zero
+    for (uint32_t i = threadIdx.x; i < tld * poff; i += blockDim.x) {
+        const uint32_t row = i / poff, p = i - row * poff;
         tiles[row * TB_LD + p] = 0u;
     }
     __syncthreads();
@@ -290,36 +351,8 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
         const uint64_t fb = s_fb[it % 3];
         const uint32_t nbk = s_nbk[it % 3];
         if (threadIdx.x == 0 && rho0 + 2 * step < rows) block_range(rho0 + 2 * step, s_fb[(it + 2) % 3], s_nbk[(it + 2) % 3]);
-        // decode: two threads per 32-value block, each transposing one half;
-        // rows are taken in reverse plane order so that value v's digits come
-        // out most significant first (no bit reversal)
-        for (uint32_t i = threadIdx.x; i < 2 * nbk; i += blockDim.x) {
-            const uint32_t t = i >> 1;
-            const int half = i & 1;
-            float* dst = cb + t * CB_LD + 16 * half;
-            if (num == 0) {
-#pragma unroll
-                for (int v = 0; v < 16; v++) dst[v] = 0.f;
-                continue;
-            }
-            uint32_t R[32];
-            const uint4* src = reinterpret_cast<const uint4*>(tile + t * TB_LD);
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const uint4 w = src[q];
-                R[31 - 4 * q] = w.x;
-                R[30 - 4 * q] = w.y;
-                R[29 - 4 * q] = w.z;
-                R[28 - 4 * q] = w.w;
-            }
-            uint32_t a[16];
-            transpose32_half(R, half, a);
-#pragma unroll
-            for (int v = 0; v < 16; v++) {
-                const int32_t iv = nb_to_bin(a[v] >> (32 - num));
-                dst[v] = dfast ? (float)iv * dscale : (neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num));
-            }
-        }
+        if (dfast) decode_tile<true>(tile, cb, nbk, num, exp, neg, dscale);
+        else decode_tile<false>(tile, cb, nbk, num, exp, neg, dscale);
         __syncthreads();
         // the tile is free again: fetch the next rows' planes during the recomposition
         if (rho0 + step < rows) fetch(s_fb[(it + 1) % 3], s_nbk[(it + 1) % 3], tiles);

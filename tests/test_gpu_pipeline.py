@@ -208,7 +208,7 @@ def test_reconstructor_fed_from_reference_files(enc):
 
 
 @pytest.mark.parametrize("shape,L", [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129, 129, 129), 4),
-                                     ((200, 131), 4)])
+                                     ((200, 131), 4), ((33, 33, 1025), 2), ((40, 33, 301), 3)])
 def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
     """fp32 negabinary hierarchical: the finest level is decoded inside the
     recomposition kernel (odd and even row lengths take different kernels);
