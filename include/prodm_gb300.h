@@ -314,7 +314,19 @@ int prodm_mdr_load_level(prodm_mdr* h, int level, const void* src, uint64_t offs
                          void* stream);
 /* retrieve with explicit per-level plane counts (h_index[L+1]) */
 int prodm_mdr_retrieve_planes(prodm_mdr* h, const uint8_t* h_index, void* d_out, void* stream);
+/* h_index[L+1] <- the per-level plane counts; also reports (and clears) a
+ * bounded wait of an earlier retrieval kernel that gave up (PRODM_ETIMEOUT) */
 int prodm_mdr_get_index(prodm_mdr* h, uint8_t* h_index, void* stream);
+/* synchronises the stream and reports (and clears) the status of the handle's
+ * retrieval kernels: PRODM_OK, or PRODM_ETIMEOUT when a bounded wait for the
+ * plane tiles of the fused finest-level kernel gave up (the output of that
+ * retrieval is then incomplete) */
+int prodm_mdr_status(prodm_mdr* h, void* stream);
+/* test hook for the timeout path: later fused finest-level launches expect
+ * extra_tx_bytes more bytes per plane tile than their copies deliver, so each
+ * wait runs out after wait_cycles SM clock cycles (0, 0 restores the
+ * defaults: exact byte counts, about two seconds) */
+int prodm_debug_tile_wait(int extra_tx_bytes, long long wait_cycles);
 int prodm_mdr_reset_retrieval(prodm_mdr* h, void* stream);
 /* copies the packed level coefficients of the last refactor (level l at the
  * offset given by the sum of the earlier level sizes) into d_dst */

@@ -84,6 +84,8 @@ _SIGS = {
     "prodm_mdr_load_level": (_i, [_P, _i, _P, C.c_uint64, C.c_uint64, _i, _P]),
     "prodm_mdr_get_index": (_i, [_P, _u8p, _P]),
     "prodm_mdr_reset_retrieval": (_i, [_P, _P]),
+    "prodm_mdr_status": (_i, [_P, _P]),
+    "prodm_debug_tile_wait": (_i, [_i, C.c_longlong]),
     "prodm_mdr_coefficients": (_i, [_P, _P, _P]),
     "prodm_mdr_destroy": (_i, [_P]),
     "prodm_batch_create": (_i, [C.POINTER(_P), _i, C.POINTER(prodm_config)]),

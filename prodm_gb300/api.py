@@ -396,6 +396,11 @@ class MDRField:
     def reset(self, stream=None):
         call("prodm_mdr_reset_retrieval", self.h, _stream(stream))
 
+    def status(self, stream=None):
+        """Raises ProdmError (PRODM_ETIMEOUT) when a bounded wait of an earlier
+        retrieval kernel gave up; the status is cleared once reported."""
+        call("prodm_mdr_status", self.h, _stream(stream))
+
     def coefficients(self, stream=None):
         """Packed level coefficients of the last refactor (a device copy)."""
         n = int(self.level_elements.astype(np.int64).sum())
@@ -435,6 +440,12 @@ def kernel_launch_count():
     out = C.c_uint64()
     call("prodm_kernel_launch_count", C.byref(out))
     return out.value
+
+
+def debug_tile_wait(extra_tx_bytes=0, wait_cycles=0):
+    """Test hook for the fused kernel's timeout path (prodm_debug_tile_wait);
+    (0, 0) restores normal operation."""
+    call("prodm_debug_tile_wait", int(extra_tx_bytes), int(wait_cycles))
 
 
 class MDRBatch:

@@ -582,6 +582,7 @@ struct prodm_mdr {
     bool hsz_valid = false;
     uint32_t* pbcounts = nullptr;                  // per-bit: first-one counts, 64 per level
     int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
+    int* kstatus = nullptr;                        // bounded device waits of retrievals (0 or a PRODM_E* code)
     std::vector<void*> allocs;
     void* coef = nullptr;
     void* cbuf[2] = {nullptr, nullptr};
@@ -776,6 +777,8 @@ int mdr_alloc_all(prodm_mdr* h) {
     if ((rc = h->alloc((void**)&h->partial, parts * (B + 1) * 8))) return rc;
     if ((rc = h->alloc((void**)&h->index, L + 1 + 15))) return rc;
     if ((rc = h->alloc((void**)&h->rsz, (L + 1) * 4))) return rc;
+    if ((rc = h->alloc((void**)&h->kstatus, 16))) return rc;
+    PRODM_CUDA(cudaMemset(h->kstatus, 0, 16));
     if ((rc = h->alloc((void**)&h->ndims_d, 4))) return rc;
     if ((rc = h->alloc((void**)&h->levels_d, 4))) return rc;
     PRODM_CUDA(cudaMemset(h->sqerr, 0, (L + 1) * (B + 1) * 8));
@@ -958,9 +961,9 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         T* o = (l == L) ? out : (T*)h->rbuf[l & 1];
         Stage sg(h, 4, l, st);
         if (fuse && l == L) {
-            if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->plane_cap[l], keys + l,
-                                                   h->index + l, (const float*)cin, F, C, (float*)o,
-                                                   (uint64_t)F.n[1] * F.n[2], F.n[2], st)))
+            if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->plane_cap[l], B,
+                                                   h->nblocks[l], keys + l, h->index + l, (const float*)cin, F, C,
+                                                   (float*)o, (uint64_t)F.n[1] * F.n[2], F.n[2], h->kstatus, st)))
                 return rc;
             continue;
         }
@@ -1956,11 +1959,33 @@ int prodm_mdr_retrieve_planes(prodm_mdr* h, const uint8_t* hidx, void* out, void
     return mdr_reconstruct<float>(h, (float*)out, st);
 }
 
+// the retrieval kernels' bounded waits: a nonzero code is reported once and cleared
+static int take_kstatus(prodm_mdr* h, cudaStream_t st) {
+    int code = 0;
+    PRODM_CUDA(cudaMemcpyAsync(&code, h->kstatus, 4, cudaMemcpyDeviceToHost, st));
+    PRODM_CUDA(cudaStreamSynchronize(st));
+    if (!code) return PRODM_OK;
+    PRODM_CUDA(cudaMemsetAsync(h->kstatus, 0, 4, st));
+    PRODM_CUDA(cudaStreamSynchronize(st));
+    if (code == PRODM_ETIMEOUT) return fail(PRODM_ETIMEOUT, "a retrieval kernel's bounded wait for its plane tiles gave up");
+    return fail(code, "a retrieval kernel found its shared memory misaligned for TMA");
+}
+
 int prodm_mdr_get_index(prodm_mdr* h, uint8_t* hidx, void* stream) {
     if (!h || !hidx) return fail(PRODM_EINVAL, "NULL pointer");
     cudaStream_t st = (cudaStream_t)stream;
     PRODM_CUDA(cudaMemcpyAsync(hidx, h->index, h->g.L + 1, cudaMemcpyDeviceToHost, st));
-    PRODM_CUDA(cudaStreamSynchronize(st));
+    return take_kstatus(h, st);
+}
+
+int prodm_mdr_status(prodm_mdr* h, void* stream) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    return take_kstatus(h, (cudaStream_t)stream);
+}
+
+int prodm_debug_tile_wait(int extra_tx_bytes, long long wait_cycles) {
+    if (extra_tx_bytes < 0 || extra_tx_bytes > (1 << 16)) return fail(PRODM_EINVAL, "extra_tx_bytes out of range");
+    prodm::fused_tma_test_hook(extra_tx_bytes, wait_cycles);
     return PRODM_OK;
 }
 

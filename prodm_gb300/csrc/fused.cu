@@ -10,6 +10,11 @@
 // and recomposition use exactly the arithmetic of the standalone kernels
 // (NegaBinaryBPEncoder.hpp:132-192; the multilinear interpolation of the
 // hierarchical basis), so the output is bit-identical to the unfused path.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "nbcodec.cuh"
@@ -19,6 +24,44 @@ namespace prodm {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// TMA (cp.async.bulk.tensor) + mbarrier helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// this thread's arrival plus `bytes` more expected from asynchronous copies
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// waits for the phase with this parity at most `limit` SM clock cycles
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > limit) return false;
+    return true;
+}
+// generic-proxy accesses of shared memory before async-proxy (TMA) ones
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// box {x .. x + box_w - 1} of row y of a 2-D tensor map into shared memory
+__device__ __forceinline__ void tma_load_2d(uint32_t* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
 
 __device__ __forceinline__ float pow2f_(int e) { return __int_as_float((e + 127) << 23); }
 
@@ -140,9 +183,9 @@ __global__ void __launch_bounds__(256) k_decode_recompose_nb32(const uint32_t* _
 // fetched with cp.async into a second tile while the current rows are decoded
 // and recomposed; the coefficient buffer is value-major ([block][33]).
 // ---------------------------------------------------------------------------
-constexpr int CB_LD = 33;   // value-major coefficient rows: conflict-free both ways
+constexpr int CB_LD = 36;   // value-major coefficient rows: conflict-free both ways
 
-__device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[r + (r >> 5)]; }
+__device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[(r >> 5) * CB_LD + (r & 31)]; }
 
 // one fine row of odd length n = 2 c2n - 1; M01 = odd-dim mask over dims
 // 0/1 (0: both coarse -> only odd nodes carry coefficients, ranks c;
@@ -181,8 +224,8 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
     for (int i = 0; i < NQ; i++) pc[i] = cb0 + co[i] + lane;
     // coefficient of rank r at cb[r + (r >> 5)]: 33 floats further per 32 ranks
     const uint32_t re = rb0 + lane, ro = rb0 + (M01 == 0 ? 0u : c2n) + lane;
-    const float* pe = cb + re + (re >> 5);
-    const float* po = cb + ro + (ro >> 5);
+    const float* pe = cb + (re >> 5) * CB_LD + (re & 31);
+    const float* po = cb + (ro >> 5) * CB_LD + (ro & 31);
     float* o = orow + 2 * lane;
     const int lim = (int)c2n - lane;   // column 32k + lane exists <=> 32k < lim
     const uint32_t groups = (P + 31) >> 5, full = P >> 5;
@@ -215,15 +258,15 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
             float qn[NQ];
 #pragma unroll
             for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], src);
-            pair(q, qn, pe + 33 * d, po + 33 * d, o + 64 * d);
+            pair(q, qn, pe + CB_LD * d, po + CB_LD * d, o + 64 * d);
             const bool more = (int)(32 * (k0 + d + D)) < lim;   // refill: group k + D
 #pragma unroll
             for (int i = 0; i < NQ; i++) ring[d][i] = more ? __ldg(pc[i] + 32 * (d + D)) : 0.f;
         }
 #pragma unroll
         for (int i = 0; i < NQ; i++) pc[i] += 32 * D;
-        pe += 33 * D;
-        po += 33 * D;
+        pe += CB_LD * D;
+        po += CB_LD * D;
         o += 64 * D;
     }
     // the remaining groups: fewer than D complete ones and at most one partial
@@ -237,13 +280,65 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
         float qn[NQ];
 #pragma unroll
         for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], src);
-        if ((int)(32 * k) < plim) pair(q, qn, pe + 33 * d, po + 33 * d, o + 64 * d);
+        if ((int)(32 * k) < plim) pair(q, qn, pe + CB_LD * d, po + CB_LD * d, o + 64 * d);
         const bool more = (int)(32 * (k + D)) < lim;
 #pragma unroll
         for (int i = 0; i < NQ; i++) ring[d][i] = more ? __ldg(pc[i] + 32 * (d + D)) : 0.f;
     }
 }
 
+
+// reordered row rho of the fine box: its reordered coordinates (r0, r1),
+// whether both are coarse (the row then holds only odd nodes), the rank of
+// its first coefficient in the level's interleaved order, and its length
+__device__ __forceinline__ void fused_row_rank(uint32_t rho, const Box& F, const Box& C, uint32_t& r0, uint32_t& r1,
+                                               bool& cc, uint64_t& rbase, uint32_t& len) {
+    r0 = rho / F.n[1];
+    r1 = rho - r0 * F.n[1];
+    cc = r0 < C.n[0] && r1 < C.n[1];
+    rbase = level_rank(r0, r1, cc ? C.n[2] : 0u, F, C);
+    len = cc ? F.n[2] - C.n[2] : F.n[2];
+}
+
+// block range [fb, fb + nbk) of the coefficients of rows [rho0, rho0 + 8)
+__device__ __forceinline__ void fused_block_range(uint32_t rho0, uint32_t rows, const Box& F, const Box& C,
+                                                  uint64_t& fb, uint32_t& nbk) {
+    const uint32_t rho_last = min(rho0 + 7, rows - 1);
+    uint32_t a0, a1, z0, z1, alen, zlen;
+    bool acc_, zcc;
+    uint64_t abase, zbase;
+    fused_row_rank(rho0, F, C, a0, a1, acc_, abase, alen);
+    fused_row_rank(rho_last, F, C, z0, z1, zcc, zbase, zlen);
+    fb = abase >> 5;
+    nbk = (uint32_t)(((zbase + zlen - 1) >> 5) - fb + 1);
+}
+
+// one warp: fine row rho (odd length) from the coarse box and the decoded
+// coefficients in cb (value v of block t at cb[t * CB_LD + v], block fb first)
+__device__ __forceinline__ void recompose_fine_row(uint32_t rho, const Box& F, const Box& C,
+                                                   const float* __restrict__ coarse, float* __restrict__ out,
+                                                   uint64_t s0, uint64_t s1, const float* __restrict__ cb, uint64_t fb,
+                                                   int lane) {
+    const uint32_t c2n = C.n[2];
+    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
+    uint32_t r0, r1, len;
+    bool cc;
+    uint64_t rbase;
+    fused_row_rank(rho, F, C, r0, r1, cc, rbase, len);
+    const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
+    const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+    const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
+    const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
+    const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
+    float* orow = out + x0 * s0 + x1 * s1;
+    const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
+    switch (m01) {
+        case 0: recompose_row_odd<0>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        case 1: recompose_row_odd<1>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        case 2: recompose_row_odd<2>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        default: recompose_row_odd<3>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+    }
+}
 
 // decode of a staged tile: two threads per 32-value block, each transposing
 // one half; rows are taken in reverse tile order, so that value v's word has
@@ -257,24 +352,31 @@ __device__ __forceinline__ void decode_tile(const uint32_t* __restrict__ tile, f
         const uint32_t t = i >> 1;
         const int half = i & 1;
         float* dst = cb + t * CB_LD + 16 * half;
-        uint32_t R[32];
+        // row r of the transpose is tile word 31 - r: words 4q.. (rows
+        // 31-4q..28-4q) meet words 16+4q.. (rows 15-4q..12-4q) in the first
+        // stage, so each pair of 16-byte reads is consumed at once
         const uint4* src = reinterpret_cast<const uint4*>(tile + t * TB_LD);
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const uint4 w = src[q];
-            R[31 - 4 * q] = w.x;
-            R[30 - 4 * q] = w.y;
-            R[29 - 4 * q] = w.z;
-            R[28 - 4 * q] = w.w;
-        }
+        const uint32_t sel16 = half ? 0x7632u : 0x5410u;
         uint32_t a[16];
-        transpose32_half(R, half, a);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint4 hi = src[q], lo = src[q + 4];
+            a[15 - 4 * q] = __byte_perm(lo.x, hi.x, sel16);
+            a[14 - 4 * q] = __byte_perm(lo.y, hi.y, sel16);
+            a[13 - 4 * q] = __byte_perm(lo.z, hi.z, sel16);
+            a[12 - 4 * q] = __byte_perm(lo.w, hi.w, sel16);
+        }
+        transpose32_half_tail(a);
+        float f[16];
 #pragma unroll
         for (int v = 0; v < 16; v++) {
             const int32_t iv = nb_to_bin(a[v]);
-            if constexpr (FAST) dst[v] = (float)iv * dscale;
-            else dst[v] = neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num);
+            if constexpr (FAST) f[v] = (float)iv * dscale;
+            else f[v] = neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num);
         }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            reinterpret_cast<float4*>(dst)[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
     }
 }
 
@@ -295,26 +397,7 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
     const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
     const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
     const uint32_t rows = F.n[0] * F.n[1];
-    const uint32_t n2 = F.n[2], c2n = C.n[2];
-    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
-    auto row_rank = [&](uint32_t rho, uint32_t& r0, uint32_t& r1, bool& cc, uint64_t& rbase, uint32_t& len) {
-        r0 = rho / F.n[1];
-        r1 = rho - r0 * F.n[1];
-        cc = r0 < C.n[0] && r1 < C.n[1];
-        rbase = level_rank(r0, r1, cc ? c2n : 0u, F, C);
-        len = cc ? n2 - c2n : n2;
-    };
-    // block range [fb, fb + nbk) of the coefficients of rows [rho0, rho0 + 8)
-    auto block_range = [&](uint32_t rho0, uint64_t& fb, uint32_t& nbk) {
-        const uint32_t rho_last = min(rho0 + 7, rows - 1);
-        uint32_t a0, a1, z0, z1, alen, zlen;
-        bool acc_, zcc;
-        uint64_t abase, zbase;
-        row_rank(rho0, a0, a1, acc_, abase, alen);
-        row_rank(rho_last, z0, z1, zcc, zbase, zlen);
-        fb = abase >> 5;
-        nbk = (uint32_t)(((zbase + zlen - 1) >> 5) - fb + 1);
-    };
+    auto block_range = [&](uint32_t r, uint64_t& fb, uint32_t& nbk) { fused_block_range(r, rows, F, C, fb, nbk); };
     // plane p of block j -> tile[j * TB_LD + 32 - num + p] (so that the
     // transposed words hold plane p at bit num - 1 - p); warp w copies planes
     // w, w+8, ..
@@ -357,27 +440,116 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
         // the tile is free again: fetch the next rows' planes during the recomposition
         if (rho0 + step < rows) fetch(s_fb[(it + 1) % 3], s_nbk[(it + 1) % 3], tiles);
         const uint32_t rho = rho0 + warp;
-        if (rho < rows) {
-            uint32_t r0, r1, len;
-            bool cc;
-            uint64_t rbase;
-            row_rank(rho, r0, r1, cc, rbase, len);
-            const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
-            const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
-            const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
-            const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
-            const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
-            float* orow = out + x0 * s0 + x1 * s1;
-            const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
-            switch (m01) {
-                case 0: recompose_row_odd<0>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-                case 1: recompose_row_odd<1>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-                case 2: recompose_row_odd<2>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-                default: recompose_row_odd<3>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-            }
-        }
+        if (rho < rows) recompose_fine_row(rho, F, C, coarse, out, s0, s1, cb, fb, lane);
     }
     cp_async_wait_all();
+}
+
+// decode of a plane-major tile (row 32 - num + p = plane p, rows below zero;
+// block t of the range at column t): the same half transposes, each thread
+// reading its block's 32 rows and combining rows 31-k and 15-k at once
+template <bool FAST, int RS>
+__device__ __forceinline__ void decode_tile_pm(const uint32_t* __restrict__ tile, float* __restrict__ cb,
+                                               uint32_t nbk, int num, int exp, bool neg, float dscale) {
+    for (uint32_t i = threadIdx.x; i < 2 * nbk; i += blockDim.x) {
+        const uint32_t t = i >> 1;
+        const int half = i & 1;
+        float* dst = cb + t * CB_LD + 16 * half;
+        const uint32_t* col = tile + t;
+        const uint32_t sel16 = half ? 0x7632u : 0x5410u;
+        uint32_t a[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) a[k] = __byte_perm(col[(31 - k) * RS], col[(15 - k) * RS], sel16);
+        transpose32_half_tail(a);
+        float f[16];
+#pragma unroll
+        for (int v = 0; v < 16; v++) {
+            const int32_t iv = nb_to_bin(a[v]);
+            if constexpr (FAST) f[v] = (float)iv * dscale;
+            else f[v] = neg ? -ldexpf((float)iv, exp - num) : ldexpf((float)iv, exp - num);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            reinterpret_cast<float4*>(dst)[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+    }
+}
+
+// Odd row length, planes staged by TMA: per CTA iteration (8 rows) one
+// elected warp issues one 2-D tensor copy per retrieved plane (box: `bw`
+// words of that plane's row, from the 16-byte aligned block fb & ~3) into the
+// plane-major tile, completing on an mbarrier; the copy for the next
+// iteration is issued once the tile is decoded and overlaps the
+// recomposition. Every wait on the mbarrier is bounded by `wait_limit` SM
+// cycles: a CTA whose wait gives up writes PRODM_ETIMEOUT to *status, waits
+// (bounded again) for its copies in flight and returns. `tx_extra` raises the
+// expected byte count (0 in normal use; a positive value makes every wait run
+// out, which is how the timeout path is tested).
+template <int RS>
+__global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
+    const __grid_constant__ CUtensorMap tmap, uint32_t bw, const uint32_t* __restrict__ maxkey,
+    const uint8_t* __restrict__ dnum, const float* __restrict__ coarse, Box F, Box C, float* __restrict__ out,
+    uint64_t s0, uint64_t s1, int* __restrict__ status, long long wait_limit, uint32_t tx_extra) {
+    extern __shared__ __align__(128) uint32_t tma_smem[];
+    uint32_t* tile = tma_smem;                               // [32][RS] plane-major
+    float* cb = (float*)(tma_smem + 32 * RS);                // [block][CB_LD]
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint64_t s_fb[3];
+    __shared__ uint32_t s_nbk[3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int num = dnum[0];
+    const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
+    const bool neg = num != 0 && (num & 1);                  // NegaBinaryBPEncoder.hpp:153, :177
+    const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
+    const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
+    const uint32_t rows = F.n[0] * F.n[1];
+    const int poff = 32 - num;
+    uint32_t rho0 = blockIdx.x * 8;
+    if (rho0 >= rows) return;
+    if ((smem_addr(tile) & 127u) != 0) {   // TMA destinations need 128-byte alignment
+        if (threadIdx.x == 0) atomicExch(status, PRODM_ECUDA);
+        return;
+    }
+    const uint32_t step = gridDim.x * 8;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fused_block_range(rho0, rows, F, C, s_fb[0], s_nbk[0]);
+        if (rho0 + step < rows) fused_block_range(rho0 + step, rows, F, C, s_fb[1], s_nbk[1]);
+    }
+    for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) tile[i] = 0u;   // planes not retrieved
+    __syncthreads();
+    const uint32_t bytes = (uint32_t)num * bw * 4u + tx_extra;
+    auto issue = [&](uint64_t fb) {   // warp 0
+        if (lane == 0) mbar_arrive_expect_tx(&bar, bytes);
+        __syncwarp();
+        const int x = (int)(fb & ~3ull);
+        for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar);
+    };
+    if (warp == 0) issue(s_fb[0]);
+    uint32_t parity = 0;
+    for (int it = 0; rho0 < rows; it++, rho0 += step) {
+        const bool ok = mbar_wait_bounded(&bar, parity, wait_limit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicExch(status, PRODM_ETIMEOUT);
+            mbar_wait_bounded(&bar, parity, wait_limit);
+            return;
+        }
+        parity ^= 1u;
+        const uint64_t fb = s_fb[it % 3];
+        const uint32_t nbk = s_nbk[it % 3];
+        if (threadIdx.x == 0 && rho0 + 2 * step < rows)
+            fused_block_range(rho0 + 2 * step, rows, F, C, s_fb[(it + 2) % 3], s_nbk[(it + 2) % 3]);
+        const uint32_t* t0 = tile + (fb & 3u);
+        if (dfast) decode_tile_pm<true, RS>(t0, cb, nbk, num, exp, neg, dscale);
+        else decode_tile_pm<false, RS>(t0, cb, nbk, num, exp, neg, dscale);
+        __syncthreads();
+        // the tile is free again: the next rows' planes arrive during the recomposition
+        if (warp == 0 && rho0 + step < rows) {
+            fence_proxy_async_smem();
+            issue(s_fb[(it + 1) % 3]);
+        }
+        const uint32_t rho = rho0 + warp;
+        if (rho < rows) recompose_fine_row(rho, F, C, coarse, out, s0, s1, cb, fb, lane);
+    }
 }
 
 }  // namespace
@@ -394,14 +566,78 @@ bool decode_recompose_nb32_ok(const Box& F) {
     return rows >= 1024 && fused_smem(F) <= 200 * 1024;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); NULL when the driver does not provide it
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+static int g_tma_tx_extra = 0;                 // test hook: extra expected bytes per tile
+static long long g_tma_wait_cycles = 4000000000ll;   // about two seconds at 2 GHz
+
+void fused_tma_test_hook(int tx_extra, long long wait_cycles) {
+    g_tma_tx_extra = tx_extra > 0 ? tx_extra : 0;
+    g_tma_wait_cycles = wait_cycles > 0 ? wait_cycles : 4000000000ll;
+}
+
+// The TMA kernel for odd rows whose 8-row block range fits one box (at most
+// 256 words): box width and tile row stride (a multiple of 32 words, so that
+// every tile row starts on a 128-byte boundary).
+template <int RS>
+static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
+                            const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
+                            int* status, cudaStream_t st) {
+    const size_t smem = (size_t)32 * RS * 4 + (size_t)fused_max_blocks(F) * CB_LD * 4;
+    const void* kern = (const void*)k_decode_recompose_nb32_tma<RS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+    const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
+    const uint64_t need = (rows + 7) / 8;
+    const unsigned grid = persistent_grid_for(kern, 256, smem, need, need);
+    k_decode_recompose_nb32_tma<RS><<<grid, 256, smem, st>>>(map, bw, (const uint32_t*)maxkey, dnum, coarse, F, C, out,
+                                                             s0, s1, status, g_tma_wait_cycles,
+                                                             (uint32_t)g_tma_tx_extra);
+    PRODM_CHECK_LAUNCH("k_decode_recompose_nb32_tma");
+    return PRODM_OK;
+}
+
 // Returns PRODM_EUNSUPPORTED when the shape does not suit the row mapping
-// (the caller then runs the unfused kernels).
-int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* maxkey, const uint8_t* dnum,
-                                 const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
-                                 cudaStream_t st) {
+// (the caller then runs the unfused kernels). Odd rows take the TMA kernel
+// when the planes' tensor map can be built (base and row stride 16-byte
+// aligned, box of at most 256 words), else the cp.async kernel.
+int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, uint64_t nblocks, const void* maxkey,
+                                 const uint8_t* dnum, const float* coarse, const Box& F, const Box& C, float* out,
+                                 uint64_t s0, uint64_t s1, int* status, cudaStream_t st) {
     if (!decode_recompose_nb32_ok(F)) return PRODM_EUNSUPPORTED;
     const size_t smem = fused_smem(F);
     const bool odd = (F.n[2] & 1u) != 0;
+    if (odd && status && (uintptr_t)base % 16 == 0 && stride % 4 == 0) {
+        const uint32_t bw = (fused_max_blocks(F) + 3 + 3) & ~3u;   // block range + up to 3 words of alignment
+        PFN_cuTensorMapEncodeTiled_v12000 enc = bw <= 256 ? tensor_map_encoder() : nullptr;
+        if (enc) {
+            CUtensorMap map;
+            const cuuint64_t dims[2] = {nblocks, (cuuint64_t)planes};
+            const cuuint64_t strides[1] = {stride * 4};
+            const cuuint32_t box[2] = {bw, 1};
+            const cuuint32_t estr[2] = {1, 1};
+            if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+                if (bw <= 96) return launch_fused_tma<96>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st);
+                if (bw <= 160) return launch_fused_tma<160>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st);
+                return launch_fused_tma<256>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st);
+            }
+        }
+    }
     const void* kern = odd ? (const void*)k_decode_recompose_nb32_odd : (const void*)k_decode_recompose_nb32;
     if (smem > 48 * 1024) {   // per device; cheap to repeat
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);

@@ -95,9 +95,10 @@ int launch_nb_encode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunk
 
 // fused.cu
 bool decode_recompose_nb32_ok(const Box& F);
-int launch_decode_recompose_nb32(const void* base, uint64_t stride, const void* maxkey, const uint8_t* dnum,
-                                 const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
-                                 cudaStream_t st);
+int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, uint64_t nblocks, const void* maxkey,
+                                 const uint8_t* dnum, const float* coarse, const Box& F, const Box& C, float* out,
+                                 uint64_t s0, uint64_t s1, int* status, cudaStream_t st);
+void fused_tma_test_hook(int tx_extra, long long wait_cycles);
 
 // perbit.cu: per-bit format; rows of 32-element group words (magnitude
 // planes 0..B-1, sign row B, unseen row B+1), each row `stride` words

@@ -46,14 +46,9 @@ __device__ __forceinline__ void cp_async16(uint32_t* dst, const uint32_t* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Half of a 32 x 32 bit transpose: rows R[0..31] (R[r] bit e) -> the 16
-// words out[v] (v = 16 * half + 0..15) whose bit r is R[r] bit v. The two
-// byte-granular stages are byte permutes, the three sub-byte stages
-// mask-and-shift swaps.
-__device__ __forceinline__ void transpose32_half(const uint32_t (&R)[32], int half, uint32_t (&a)[16]) {
-    const uint32_t sel16 = half ? 0x7632u : 0x5410u;
-#pragma unroll
-    for (int k = 0; k < 16; k++) a[k] = __byte_perm(R[k], R[k + 16], sel16);
+// The byte-granular second stage and the three sub-byte stages of a half
+// transpose (below), on the 16 words the first stage selected.
+__device__ __forceinline__ void transpose32_half_tail(uint32_t (&a)[16]) {
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         const uint32_t x = a[k], y = a[k + 8];
@@ -72,6 +67,17 @@ __device__ __forceinline__ void transpose32_half(const uint32_t (&R)[32], int ha
             a[k] ^= t << j;
         }
     }
+}
+
+// Half of a 32 x 32 bit transpose: rows R[0..31] (R[r] bit e) -> the 16
+// words out[v] (v = 16 * half + 0..15) whose bit r is R[r] bit v. The two
+// byte-granular stages are byte permutes, the three sub-byte stages
+// mask-and-shift swaps.
+__device__ __forceinline__ void transpose32_half(const uint32_t (&R)[32], int half, uint32_t (&a)[16]) {
+    const uint32_t sel16 = half ? 0x7632u : 0x5410u;
+#pragma unroll
+    for (int k = 0; k < 16; k++) a[k] = __byte_perm(R[k], R[k + 16], sel16);
+    transpose32_half_tail(a);
 }
 
 constexpr int TB_LD = 36;   // block-major plane tile row: 32 planes + pad, 16-byte aligned rows

@@ -229,3 +229,31 @@ def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
         out = mdr.retrieve_planes([int(v) for v in idx]).cpu().numpy()
         ref = O.retrieve(shape, L, B, blob, sizes, bounds.astype(np.float32), idx, "negabinary", True)
         assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), idx
+
+
+def test_fused_tile_wait_timeout_is_reported_and_recoverable():
+    """The fused finest-level kernel waits for its TMA plane tiles on an
+    mbarrier, each wait bounded. With the expected byte count raised (the test
+    hook) no tile ever completes: every CTA gives up after a short limit,
+    reports PRODM_ETIMEOUT and returns; the status is cleared once read and
+    the next retrieval is exact again."""
+    from prodm_gb300._lib import ProdmError
+    shape, L = (65, 65, 65), 3
+    x = fields().spectral_grf(shape, seed=11, device="cuda")
+    m = api().MDRField(shape, torch.float32, L, 32, "negabinary", "hierarchical", "max")
+    m.refactor(x)
+    idx = [16] * (L + 1)
+    good = m.retrieve_planes(idx).clone()
+    m.status()
+    api().debug_tile_wait(64, 20000)
+    try:
+        m.reset()
+        m.retrieve_planes(idx)
+        with pytest.raises(ProdmError) as e:
+            m.status()
+        assert e.value.status == 4          # PRODM_ETIMEOUT
+    finally:
+        api().debug_tile_wait(0, 0)
+    m.status()                              # reported once
+    m.reset()
+    assert torch.equal(m.retrieve_planes(idx), good)
