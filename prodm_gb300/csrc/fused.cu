@@ -259,9 +259,11 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
 #pragma unroll
             for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], src);
             pair(q, qn, pe + CB_LD * d, po + CB_LD * d, o + 64 * d);
-            const bool more = (int)(32 * (k0 + d + D)) < lim;   // refill: group k + D
+            // refill: group k + D (a slot past the row keeps stale values, never used)
+            if ((int)(32 * (k0 + d + D)) < lim) {
 #pragma unroll
-            for (int i = 0; i < NQ; i++) ring[d][i] = more ? __ldg(pc[i] + 32 * (d + D)) : 0.f;
+                for (int i = 0; i < NQ; i++) ring[d][i] = __ldg(pc[i] + 32 * (d + D));
+            }
         }
 #pragma unroll
         for (int i = 0; i < NQ; i++) pc[i] += 32 * D;
@@ -281,9 +283,10 @@ __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0,
 #pragma unroll
         for (int i = 0; i < NQ; i++) qn[i] = __shfl_sync(FULL, lane == 0 ? qx[i] : q[i], src);
         if ((int)(32 * k) < plim) pair(q, qn, pe + CB_LD * d, po + CB_LD * d, o + 64 * d);
-        const bool more = (int)(32 * (k + D)) < lim;
+        if ((int)(32 * (k + D)) < lim) {
 #pragma unroll
-        for (int i = 0; i < NQ; i++) ring[d][i] = more ? __ldg(pc[i] + 32 * (d + D)) : 0.f;
+            for (int i = 0; i < NQ; i++) ring[d][i] = __ldg(pc[i] + 32 * (d + D));
+        }
     }
 }
 
@@ -313,26 +316,42 @@ __device__ __forceinline__ void fused_block_range(uint32_t rho0, uint32_t rows, 
     nbk = (uint32_t)(((zbase + zlen - 1) >> 5) - fb + 1);
 }
 
-// one warp: fine row rho (odd length) from the coarse box and the decoded
-// coefficients in cb (value v of block t at cb[t * CB_LD + v], block fb first)
-__device__ __forceinline__ void recompose_fine_row(uint32_t rho, const Box& F, const Box& C,
-                                                   const float* __restrict__ coarse, float* __restrict__ out,
-                                                   uint64_t s0, uint64_t s1, const float* __restrict__ cb, uint64_t fb,
-                                                   int lane) {
-    const uint32_t c2n = C.n[2];
+// where fine row rho's inputs and output lie: the first coarse corner row
+// (element offset in the coarse box), the output row (element offset), the
+// rank of its first coefficient relative to block fb, and its odd-dim mask
+struct FusedRow {
+    uint64_t coarse_off, out_off;
+    uint32_t rb;
+    int m01;
+};
+__device__ __forceinline__ FusedRow fused_row(uint32_t rho, const Box& F, const Box& C, uint64_t s0, uint64_t s1,
+                                              uint64_t fb) {
     const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
     uint32_t r0, r1, len;
     bool cc;
     uint64_t rbase;
     fused_row_rank(rho, F, C, r0, r1, cc, rbase, len);
     const uint32_t x0 = natural_of(r0, F.n[0], C.n[0]), x1 = natural_of(r1, F.n[1], C.n[1]);
-    const int m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
-    const uint32_t c0 = (m01 & 1) ? (x0 >> 1) : r0;
-    const uint32_t c1 = (m01 & 2) ? (x1 >> 1) : r1;
-    const float* cb0 = coarse + c0 * cs0 + c1 * cs1;
-    float* orow = out + x0 * s0 + x1 * s1;
-    const uint32_t rb0 = (uint32_t)(rbase - fb * 32);
-    switch (m01) {
+    FusedRow r;
+    r.m01 = (is_coarse(x0, F.n[0]) ? 0 : 1) | (is_coarse(x1, F.n[1]) ? 0 : 2);
+    const uint32_t c0 = (r.m01 & 1) ? (x0 >> 1) : r0;
+    const uint32_t c1 = (r.m01 & 2) ? (x1 >> 1) : r1;
+    r.coarse_off = c0 * cs0 + c1 * cs1;
+    r.out_off = x0 * s0 + x1 * s1;
+    r.rb = (uint32_t)(rbase - fb * 32);
+    return r;
+}
+
+// one warp: a fine row (odd length) from the coarse box and the decoded
+// coefficients in cb (value v of block t at cb[t * CB_LD + v], block fb first)
+__device__ __forceinline__ void recompose_fine_row(const FusedRow& r, const Box& C, const float* __restrict__ coarse,
+                                                   float* __restrict__ out, const float* __restrict__ cb, int lane) {
+    const uint32_t c2n = C.n[2];
+    const uint64_t cs0 = (uint64_t)C.n[1] * C.n[2], cs1 = C.n[2];
+    const float* cb0 = coarse + r.coarse_off;
+    float* orow = out + r.out_off;
+    const uint32_t rb0 = r.rb;
+    switch (r.m01) {
         case 0: recompose_row_odd<0>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
         case 1: recompose_row_odd<1>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
         case 2: recompose_row_odd<2>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
@@ -440,7 +459,7 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
         // the tile is free again: fetch the next rows' planes during the recomposition
         if (rho0 + step < rows) fetch(s_fb[(it + 1) % 3], s_nbk[(it + 1) % 3], tiles);
         const uint32_t rho = rho0 + warp;
-        if (rho < rows) recompose_fine_row(rho, F, C, coarse, out, s0, s1, cb, fb, lane);
+        if (rho < rows) recompose_fine_row(fused_row(rho, F, C, s0, s1, fb), C, coarse, out, cb, lane);
     }
     cp_async_wait_all();
 }
@@ -495,6 +514,7 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint64_t s_fb[3];
     __shared__ uint32_t s_nbk[3];
+    __shared__ FusedRow s_row[2][8];   // the rows of iterations it (slot it & 1) and it + 1
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int num = dnum[0];
     const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
@@ -503,6 +523,10 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
     const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
     const uint32_t rows = F.n[0] * F.n[1];
     const int poff = 32 - num;
+    // lanes 0..7 of warp 0: the rows of the iteration starting at r, block range fb
+    auto rows_of = [&](uint32_t r, uint64_t fb, FusedRow* slot) {
+        if (lane < 8 && r + lane < rows) slot[lane] = fused_row(r + lane, F, C, s0, s1, fb);
+    };
     uint32_t rho0 = blockIdx.x * 8;
     if (rho0 >= rows) return;
     if ((smem_addr(tile) & 127u) != 0) {   // TMA destinations need 128-byte alignment
@@ -517,6 +541,7 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
     }
     for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) tile[i] = 0u;   // planes not retrieved
     __syncthreads();
+    if (warp == 0) rows_of(rho0, s_fb[0], s_row[0]);
     const uint32_t bytes = (uint32_t)num * bw * 4u + tx_extra;
     auto issue = [&](uint64_t fb) {   // warp 0
         if (lane == 0) mbar_arrive_expect_tx(&bar, bytes);
@@ -546,9 +571,9 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
         if (warp == 0 && rho0 + step < rows) {
             fence_proxy_async_smem();
             issue(s_fb[(it + 1) % 3]);
+            rows_of(rho0 + step, s_fb[(it + 1) % 3], s_row[(it + 1) & 1]);
         }
-        const uint32_t rho = rho0 + warp;
-        if (rho < rows) recompose_fine_row(rho, F, C, coarse, out, s0, s1, cb, fb, lane);
+        if (rho0 + warp < rows) recompose_fine_row(s_row[it & 1][warp], C, coarse, out, cb, lane);
     }
 }
 
