@@ -583,6 +583,8 @@ struct prodm_mdr {
     uint32_t* pbcounts = nullptr;                  // per-bit: first-one counts, 64 per level
     int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
     int* kstatus = nullptr;                        // bounded device waits of retrievals (0 or a PRODM_E* code)
+    uint8_t* hmap = nullptr;                       // mapped pinned host memory: plane counts [0, 64), status [64, 68)
+    uint8_t* dmap = nullptr;                       // its device address
     std::vector<void*> allocs;
     void* coef = nullptr;
     void* cbuf[2] = {nullptr, nullptr};
@@ -657,6 +659,7 @@ struct prodm_mdr {
         for (auto& p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
         for (auto e : pool) cudaEventDestroy(e);
         for (void* p : allocs) cudaFree(p);
+        if (hmap) cudaFreeHost(hmap);
     }
     int alloc(void** p, size_t bytes) {
         if (bytes == 0) bytes = 256;
@@ -779,6 +782,8 @@ int mdr_alloc_all(prodm_mdr* h) {
     if ((rc = h->alloc((void**)&h->rsz, (L + 1) * 4))) return rc;
     if ((rc = h->alloc((void**)&h->kstatus, 16))) return rc;
     PRODM_CUDA(cudaMemset(h->kstatus, 0, 16));
+    PRODM_CUDA(cudaHostAlloc((void**)&h->hmap, 128, cudaHostAllocMapped));
+    PRODM_CUDA(cudaHostGetDevicePointer((void**)&h->dmap, h->hmap, 0));
     if ((rc = h->alloc((void**)&h->ndims_d, 4))) return rc;
     if ((rc = h->alloc((void**)&h->levels_d, 4))) return rc;
     PRODM_CUDA(cudaMemset(h->sqerr, 0, (L + 1) * (B + 1) * 8));
@@ -1959,11 +1964,30 @@ int prodm_mdr_retrieve_planes(prodm_mdr* h, const uint8_t* hidx, void* out, void
     return mdr_reconstruct<float>(h, (float*)out, st);
 }
 
-// the retrieval kernels' bounded waits: a nonzero code is reported once and cleared
-static int take_kstatus(prodm_mdr* h, cudaStream_t st) {
-    int code = 0;
-    PRODM_CUDA(cudaMemcpyAsync(&code, h->kstatus, 4, cudaMemcpyDeviceToHost, st));
+// The plane counts and the retrieval status are read back through mapped
+// host memory written by a one-block kernel: a small copy on a copy engine
+// would wait behind any large device-to-host copy already queued there (the
+// previous reconstruction on its way to the host, for instance).
+static __global__ void k_read_index(const uint8_t* __restrict__ idx, int n, const int* __restrict__ status,
+                                    uint8_t* __restrict__ map) {
+    const int t = threadIdx.x;
+    if (t < n) map[t] = idx[t];
+    if (t == 0) *reinterpret_cast<volatile int*>(map + 64) = *status;
+    __threadfence_system();
+}
+
+static int read_index(prodm_mdr* h, uint8_t* hidx, cudaStream_t st, int* code) {
+    const int n = hidx ? h->g.L + 1 : 0;
+    k_read_index<<<1, 64, 0, st>>>(h->index, n, h->kstatus, h->dmap);
+    PRODM_CHECK_LAUNCH("k_read_index");
     PRODM_CUDA(cudaStreamSynchronize(st));
+    if (n) std::memcpy(hidx, h->hmap, n);
+    *code = *reinterpret_cast<volatile int*>(h->hmap + 64);
+    return PRODM_OK;
+}
+
+// the retrieval kernels' bounded waits: a nonzero code is reported once and cleared
+static int report_kstatus(prodm_mdr* h, int code, cudaStream_t st) {
     if (!code) return PRODM_OK;
     PRODM_CUDA(cudaMemsetAsync(h->kstatus, 0, 4, st));
     PRODM_CUDA(cudaStreamSynchronize(st));
@@ -1974,13 +1998,17 @@ static int take_kstatus(prodm_mdr* h, cudaStream_t st) {
 int prodm_mdr_get_index(prodm_mdr* h, uint8_t* hidx, void* stream) {
     if (!h || !hidx) return fail(PRODM_EINVAL, "NULL pointer");
     cudaStream_t st = (cudaStream_t)stream;
-    PRODM_CUDA(cudaMemcpyAsync(hidx, h->index, h->g.L + 1, cudaMemcpyDeviceToHost, st));
-    return take_kstatus(h, st);
+    int code = 0, rc;
+    if ((rc = read_index(h, hidx, st, &code))) return rc;
+    return report_kstatus(h, code, st);
 }
 
 int prodm_mdr_status(prodm_mdr* h, void* stream) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
-    return take_kstatus(h, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    int code = 0, rc;
+    if ((rc = read_index(h, nullptr, st, &code))) return rc;
+    return report_kstatus(h, code, st);
 }
 
 int prodm_debug_tile_wait(int extra_tx_bytes, long long wait_cycles) {
