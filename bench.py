@@ -431,12 +431,18 @@ def run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev):
     sizes, _, _ = mdr.level_info()
     level_bytes = [int(sizes[l].astype(np.int64).sum()) for l in range(L + 1)]
     host_levels = [torch.empty(b, dtype=torch.uint8, pin_memory=True) for b in level_bytes]
-    # the level files go to the host on their own stream, finest level first,
-    # while the reconstructor loads what it needs of each level as soon as that
-    # level has arrived (the host link carries both directions at once)
+    # the level files go to the host on their own stream while the
+    # reconstructor loads what it needs of each level as soon as those bytes
+    # have arrived (the host link carries both directions at once): the coarse
+    # levels first, then the part of the finest level the first tolerance
+    # needs, then the rest of it
     exp_stream = torch.cuda.Stream()
     exported = [torch.cuda.Event() for _ in range(L + 1)]
+    head = torch.cuda.Event()
     h2d = d2h = 0
+
+    def needed(idx, l):
+        return int(sizes[l, :idx[l]].astype(np.int64).sum())
 
     def one():
         nonlocal h2d, d2h
@@ -448,19 +454,32 @@ def run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev):
         meta = mdr.metadata()
         d2h += len(meta)
         exp_stream.wait_stream(main)
-        for l in reversed(range(L + 1)):                    # level files -> host
+        for l in range(L):                                  # coarse level files -> host
             mdr.export_level_into(l, host_levels[l], exp_stream)
             exported[l].record(exp_stream)
             d2h += level_bytes[l]
         rec.load_metadata(meta)
+        rec.interpret(tols[0], interpreter="negabinary", estimator="l2_hb")
+        idx = rec.index()
+        first = needed(idx, L)                              # finest level file, in two parts
+        if 0 < first < level_bytes[L]:
+            mdr.export_level_range_into(L, 0, host_levels[L][:first], exp_stream)
+            head.record(exp_stream)
+            mdr.export_level_range_into(L, first, host_levels[L][first:], exp_stream)
+        else:
+            mdr.export_level_into(L, host_levels[L], exp_stream)
+            head.record(exp_stream)
+        exported[L].record(exp_stream)
+        d2h += level_bytes[L]
         loaded = [0] * (L + 1)
         for i, t in enumerate(tols):
-            rec.interpret(t, interpreter="negabinary", estimator="l2_hb")
-            idx = rec.index()
+            if i:
+                rec.interpret(t, interpreter="negabinary", estimator="l2_hb")
+                idx = rec.index()
             for l in range(L + 1):
-                need = int(sizes[l, :idx[l]].astype(np.int64).sum())
+                need = needed(idx, l)
                 if need > loaded[l]:
-                    main.wait_event(exported[l])
+                    main.wait_event(head if l == L and need <= first else exported[l])
                     rec.load_level(l, host_levels[l][loaded[l]:need], offset=loaded[l])
                     h2d += need - loaded[l]
                     loaded[l] = need
@@ -488,10 +507,11 @@ def run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev):
     rec.close()
     return {"value": step_bytes / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "ms_per_step": dt * 1e3, "steps": n,
-            "flow": "H2D field, refactor, D2H metadata; D2H level files (own stream, finest first, pinned, "
-                    "asynchronous); reconstructor: load metadata, per tolerance interpret -> H2D of the new level "
-                    "bytes (each level once its file is on the host) -> reconstruct -> D2H field (side stream, "
-                    "overlapping the next tolerance)"}
+            "flow": "H2D field, refactor, D2H metadata; D2H level files (own stream, pinned, asynchronous: "
+                    "coarse levels, then the finest level's bytes the first tolerance needs, then the rest); "
+                    "reconstructor: load metadata, per tolerance interpret -> H2D of the new level bytes (each "
+                    "part once it is on the host) -> reconstruct -> D2H field (side stream, overlapping the next "
+                    "tolerance)"}
 
 
 def run_batched(steps=5):

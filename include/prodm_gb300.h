@@ -270,6 +270,12 @@ int prodm_mdr_metadata(prodm_mdr* h, uint8_t* h_buf, size_t capacity, size_t* le
  * wait on an event recorded after the call, before reading it). */
 int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t capacity, int dst_is_host, uint64_t* len,
                            void* stream);
+/* bytes [offset, offset + bytes) of the same level file into dst (dst_is_host
+ * as above): a reader can start on the first planes of a level before the
+ * rest of the file is out (ConcatLevelFileRetriever reads level files in
+ * such consecutive pieces, FileRetriever.hpp:15-35) */
+int prodm_mdr_export_level_range(prodm_mdr* h, int level, uint64_t offset, uint64_t bytes, void* dst,
+                                 int dst_is_host, void* stream);
 
 /* Lossless stage of the handle (AdaptiveLevelCompressor's rule with the ZCB
  * codec, see prodm_lossless_compress_level): latter_index >= 0 switches it on

@@ -330,6 +330,17 @@ class MDRField:
              0 if out.is_cuda else 2, C.byref(n), _stream(stream))
         return n.value
 
+    def export_level_range_into(self, level, offset, out, stream=None):
+        """Bytes [offset, offset + out.numel()) of the level file into `out` (a
+        uint8 tensor: CUDA, or pinned host memory filled asynchronously in the
+        stream's order)."""
+        if out.dtype != torch.uint8 or not out.is_contiguous():
+            raise ValueError("expected a contiguous uint8 tensor")
+        if not out.is_cuda and out.numel() and not out.is_pinned():
+            raise ValueError("host output must be pinned memory")
+        call("prodm_mdr_export_level_range", self.h, level, int(offset), out.numel(),
+             C.c_void_p(out.data_ptr()) if out.numel() else None, 0 if out.is_cuda else 2, _stream(stream))
+
     def set_lossless(self, latter_index=26, stream=None):
         """Lossless stage on (latter_index >= 0, the reference's default 26) or off (None / < 0)."""
         call("prodm_mdr_set_lossless", self.h, -1 if latter_index is None else int(latter_index), _stream(stream))

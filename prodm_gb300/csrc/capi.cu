@@ -1865,6 +1865,54 @@ int prodm_mdr_export_level(prodm_mdr* h, int level, void* dst, uint64_t cap, int
     return rc;
 }
 
+int prodm_mdr_export_level_range(prodm_mdr* h, int level, uint64_t offset, uint64_t bytes, void* dst,
+                                 int dst_is_host, void* stream) {
+    if (!h || (!dst && bytes)) return fail(PRODM_EINVAL, "NULL pointer");
+    if (level < 0 || level > h->g.L) return fail(PRODM_EINVAL, "level out of range");
+    if (dst_is_host < 0 || dst_is_host > 2) return fail(PRODM_EINVAL, "dst_is_host must be 0, 1 or 2");
+    cudaStream_t st = (cudaStream_t)stream;
+    uint64_t total = 0;
+    int rc = prodm_mdr_export_level(h, level, nullptr, 0, 0, &total, stream);
+    if (rc) return rc;
+    if (offset > total || bytes > total - offset) return fail(PRODM_EINVAL, "byte range past the end of the level file");
+    if (!bytes) return PRODM_OK;
+    const cudaMemcpyKind kind = dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    uint8_t* out = (uint8_t*)dst;
+    if (h->nb && h->ll_latter < 0) {
+        // fixed-size plane rows: the range is a tail of one row, whole rows, a head of one row
+        const uint64_t row = h->nblocks[level] * h->es, pitch = (uint64_t)h->plane_cap[level] * h->es;
+        const uint8_t* src = h->streams + h->lvl_byte_off[level];
+        uint64_t a = offset;
+        const uint64_t b = offset + bytes;
+        if (a % row) {
+            const uint64_t n = std::min(b, (a / row + 1) * row) - a;
+            PRODM_CUDA(cudaMemcpyAsync(out, src + (a / row) * pitch + a % row, n, kind, st));
+            out += n;
+            a += n;
+        }
+        if (b - a >= row) {
+            const uint64_t rows = (b - a) / row;
+            PRODM_CUDA(cudaMemcpy2DAsync(out, row, src + (a / row) * pitch, pitch, row, rows, kind, st));
+            out += rows * row;
+            a += rows * row;
+        }
+        if (a < b) PRODM_CUDA(cudaMemcpyAsync(out, src + (a / row) * pitch, b - a, kind, st));
+    } else {   // the whole file into device scratch, then the range
+        uint8_t* tmp;
+        PRODM_CUDA(cudaMallocAsync((void**)&tmp, total, st));
+        uint64_t len = 0;
+        rc = prodm_mdr_export_level(h, level, tmp, total, 0, &len, stream);
+        if (!rc) {
+            const cudaError_t e = cudaMemcpyAsync(out, tmp + offset, bytes, kind, st);
+            if (e != cudaSuccess) rc = cuda_status(e, "export copy");
+        }
+        cudaFreeAsync(tmp, st);
+        if (rc) return rc;
+    }
+    if (dst_is_host == 1) PRODM_CUDA(cudaStreamSynchronize(st));
+    return PRODM_OK;
+}
+
 int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
     if (h->from_files) return fail(PRODM_EINVAL, "set_lossless: a handle fed from files takes the stage from its metadata");

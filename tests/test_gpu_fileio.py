@@ -92,6 +92,49 @@ def test_export_into_pinned_on_a_side_stream(enc, dt, B, latter):
         m.export_level_into(0, torch.empty(16, dtype=torch.uint8))      # pageable
 
 
+@pytest.mark.parametrize("enc,dt,B,latter", [("negabinary", torch.float32, 32, None),
+                                              ("grouped", torch.float32, 32, None),
+                                              ("perbit", torch.float64, 60, None),
+                                              ("negabinary", torch.float32, 32, 26)])
+def test_export_level_ranges(enc, dt, B, latter):
+    """byte ranges of a level file (prodm_mdr_export_level_range) equal the
+    same bytes of the whole export: ranges inside one plane row, across rows,
+    on row boundaries, empty and whole, into device and pinned host memory;
+    ranges past the end are errors"""
+    from prodm_gb300 import fields
+    from prodm_gb300._lib import ProdmError
+    shape, L = (45, 38, 29), 3
+    m = api().MDRField(shape, dt, L, B, enc, "hierarchical", "max")
+    m.refactor(fields.spectral_grf(shape, seed=5, dtype=dt, device="cuda"))
+    if latter is not None:
+        m.set_lossless(latter)
+    rng = np.random.default_rng(B)
+    for l in range(L + 1):
+        want = m.export_level(l)
+        n = len(want)
+        row = n // B
+        cuts = [(0, n), (0, 0), (n, 0), (0, 1), (n - 1, 1), (1, n - 2)]      # (offset, length)
+        if row:
+            cuts += [(row, row), (row - 1, 2), (row // 2, 3 * row), (2 * row + 3, row - 3)]
+        for _ in range(6):
+            a, b = sorted(int(v) for v in rng.integers(0, n + 1, 2))
+            cuts.append((a, b - a))
+        for a, nb in cuts:
+            a = min(max(a, 0), n)
+            nb = min(max(nb, 0), n - a)
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            h = torch.empty(nb, dtype=torch.uint8, pin_memory=True)
+            m.export_level_range_into(l, a, h, side)
+            side.synchronize()
+            assert h.numpy().tobytes() == want[a:a + nb].tobytes(), (l, a, nb)
+            d = torch.empty(nb, dtype=torch.uint8, device="cuda")
+            m.export_level_range_into(l, a, d)
+            assert d.cpu().numpy().tobytes() == want[a:a + nb].tobytes(), (l, a, nb)
+        with pytest.raises(ProdmError):
+            m.export_level_range_into(l, n - 2, torch.empty(3, dtype=torch.uint8, device="cuda"))
+
+
 def test_file_errors(tmp_path):
     from prodm_gb300._lib import ProdmError
     shape = (33, 33, 33)
