@@ -297,6 +297,8 @@ __global__ void __launch_bounds__(256) k_nb_decode_levels(const ChunkSeg* __rest
     constexpr int CB = kDecodeChunkBlocks;
     __shared__ __align__(16) uint32_t tiles[2][32 * DEC_LD];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pdl_wait();   // plane counts from the interpreter
+    pdl_release();
     auto fetch = [&](uint64_t c, uint32_t* tile) {
         const ChunkSeg& q = segs[find_seg(segs, nseg, c, &ChunkSeg::chunk_begin)];
         const int num = q.dnum[0];
@@ -1045,10 +1047,11 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     return PRODM_OK;
 }
 
-int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st) {
+int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st, bool pdl) {
     const unsigned grid = persistent_grid_for((const void*)k_nb_decode_levels, 256, 0, total_chunks, total_chunks);
-    k_nb_decode_levels<<<grid, 256, 0, st>>>(segs, nseg, total_chunks);
-    PRODM_CHECK_LAUNCH("k_nb_decode_levels");
+    count_launch();
+    const cudaError_t e = launch_chain(pdl, k_nb_decode_levels, dim3(grid), dim3(256), 0, st, segs, nseg, total_chunks);
+    if (e != cudaSuccess) return cuda_status(e, "k_nb_decode_levels");
     return PRODM_OK;
 }
 

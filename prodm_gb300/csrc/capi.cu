@@ -19,6 +19,13 @@ thread_local std::string g_err;
 std::atomic<uint64_t> g_launches{0};
 }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* v = getenv("PRODM_NO_PDL");
+        return !(v && v[0] == '1');
+    }();
+    return on;
+}
 void set_error(const std::string& msg) { g_err = msg; }
 int fail(int status, const std::string& msg) {
     g_err = msg;
@@ -935,7 +942,7 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
     if (h->dseg && sizeof(T) == 4) {
         // fp32 negabinary: every other level in one launch (timed as level 0)
         Stage sg(h, 3, 0, st);
-        if ((rc = launch_nb_decode_levels(h->dseg, h->dseg_n, h->dseg_chunks, st))) return rc;
+        if ((rc = launch_nb_decode_levels(h->dseg, h->dseg_n, h->dseg_chunks, st, true))) return rc;
     }
     for (int l = 0; l <= L; l++) {
         if ((fuse && l == L) || (h->dseg && sizeof(T) == 4)) continue;
@@ -968,7 +975,8 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         if (fuse && l == L) {
             if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->plane_cap[l], B,
                                                    h->nblocks[l], keys + l, h->index + l, (const float*)cin, F, C,
-                                                   (float*)o, (uint64_t)F.n[1] * F.n[2], F.n[2], h->kstatus, st)))
+                                                   (float*)o, (uint64_t)F.n[1] * F.n[2], F.n[2], h->kstatus, st,
+                                                   true)))
                 return rc;
             continue;
         }
@@ -980,7 +988,7 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
             if ((rc = launch_add_box<T>(cin, (uint64_t)C.n[1] * C.n[2], C.n[2], (T*)h->os.z, C, (T)-1, st))) return rc;
         }
         if ((rc = launch_recompose_level_packed<T>(cin, rcoef + h->roff[l], F, C, o, (uint64_t)F.n[1] * F.n[2], F.n[2],
-                                                   st)))
+                                                   st, true)))
             return rc;
     }
     return PRODM_OK;
@@ -1000,7 +1008,7 @@ int mdr_interpret(prodm_mdr* h, double tol, int interp, int est, double s, cudaS
     }
     Stage sg(h, 2, 0, st);
     return launch_interpret<T>(1, interp, est, h->ndims_d, h->levels_d, s, B, h->sizes, 0, errs, 0, nullptr, tol,
-                               h->index, 0, h->rsz, st);
+                               h->index, 0, h->rsz, st, true);
 }
 
 // grouped levels loaded from files: header -> rb + chunk offsets, then the

@@ -31,6 +31,39 @@ void count_launch();
 
 constexpr int kSMs = 152;   // GB300: 2 dies x 76 SMs
 
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch along a chain of dependent kernels (one
+// retrieval: interpreter -> multi-level decode -> level recompositions ->
+// fused finest level). A kernel launched with launch_chain may start while
+// its predecessor in the stream is still running; it calls pdl_wait() before
+// touching anything the predecessor writes or reads, and pdl_release() only
+// after that wait, so a kernel that starts early knows every kernel two or
+// more launches back has completed. Both are no-ops for a normal launch.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+bool pdl_enabled();   // false when the environment sets PRODM_NO_PDL=1
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chain(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                         Args... args) {
+    if (!pdl || !pdl_enabled()) {
+        kernel<<<grid, block, smem, st>>>(args...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // CTAs of `kernel` (threads, dynamic smem) resident on the whole current
 // device at once: the grid of a persistent grid-stride kernel, so that no CTA
 // waits for a second wave (cached per device, kernel and launch shape)

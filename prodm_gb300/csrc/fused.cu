@@ -550,6 +550,10 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
         for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar);
     };
     if (warp == 0) issue(s_fb[0]);
+    // the first tile is on its way; the coarse box and the output belong to
+    // the previous launches (the plane counts and the planes are older)
+    pdl_wait();
+    pdl_release();
     uint32_t parity = 0;
     for (int it = 0; rho0 < rows; it++, rho0 += step) {
         const bool ok = mbar_wait_bounded(&bar, parity, wait_limit);
@@ -620,7 +624,7 @@ void fused_tma_test_hook(int tx_extra, long long wait_cycles) {
 template <int RS>
 static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
                             const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
-                            int* status, cudaStream_t st) {
+                            int* status, cudaStream_t st, bool pdl) {
     const size_t smem = (size_t)32 * RS * 4 + (size_t)fused_max_blocks(F) * CB_LD * 4;
     const void* kern = (const void*)k_decode_recompose_nb32_tma<RS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -628,10 +632,11 @@ static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* max
     const uint64_t rows = (uint64_t)F.n[0] * F.n[1];
     const uint64_t need = (rows + 7) / 8;
     const unsigned grid = persistent_grid_for(kern, 256, smem, need, need);
-    k_decode_recompose_nb32_tma<RS><<<grid, 256, smem, st>>>(map, bw, (const uint32_t*)maxkey, dnum, coarse, F, C, out,
-                                                             s0, s1, status, g_tma_wait_cycles,
-                                                             (uint32_t)g_tma_tx_extra);
-    PRODM_CHECK_LAUNCH("k_decode_recompose_nb32_tma");
+    count_launch();
+    e = launch_chain(pdl, k_decode_recompose_nb32_tma<RS>, dim3(grid), dim3(256), smem, st, map, bw,
+                     (const uint32_t*)maxkey, dnum, coarse, F, C, out, s0, s1, status, g_tma_wait_cycles,
+                     (uint32_t)g_tma_tx_extra);
+    if (e != cudaSuccess) return cuda_status(e, "k_decode_recompose_nb32_tma");
     return PRODM_OK;
 }
 
@@ -641,7 +646,7 @@ static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* max
 // aligned, box of at most 256 words), else the cp.async kernel.
 int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, uint64_t nblocks, const void* maxkey,
                                  const uint8_t* dnum, const float* coarse, const Box& F, const Box& C, float* out,
-                                 uint64_t s0, uint64_t s1, int* status, cudaStream_t st) {
+                                 uint64_t s0, uint64_t s1, int* status, cudaStream_t st, bool pdl) {
     if (!decode_recompose_nb32_ok(F)) return PRODM_EUNSUPPORTED;
     const size_t smem = fused_smem(F);
     const bool odd = (F.n[2] & 1u) != 0;
@@ -657,9 +662,9 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
             if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
-                if (bw <= 96) return launch_fused_tma<96>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st);
-                if (bw <= 160) return launch_fused_tma<160>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st);
-                return launch_fused_tma<256>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st);
+                if (bw <= 96) return launch_fused_tma<96>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
+                if (bw <= 160) return launch_fused_tma<160>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
+                return launch_fused_tma<256>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
             }
         }
     }

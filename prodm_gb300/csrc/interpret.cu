@@ -307,6 +307,8 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
                                                    const double* __restrict__ tols, double tol0,
                                                    uint8_t* __restrict__ index, uint64_t idx_stride,
                                                    uint32_t* __restrict__ rsz) {
+    pdl_wait();   // writes the plane counts the previous retrieval's kernels read
+    pdl_release();
     const int f = blockIdx.x;
     if (f >= nfields) return;
     const int L = levels[f];
@@ -376,19 +378,20 @@ template <class T>
 int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, const int* d_levels, double s, int B,
                      const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
-                     cudaStream_t st) {
-    k_interpret<T><<<nfields, 256, 0, st>>>(nfields, kind, est_kind, d_ndims, d_levels, s, B, d_sizes,
-                                                           sz_stride, d_errs, err_stride, d_tols, tol0, d_index,
-                                                           idx_stride, d_rsz);
-    PRODM_CHECK_LAUNCH("k_interpret");
+                     cudaStream_t st, bool pdl) {
+    count_launch();
+    const cudaError_t e = launch_chain(pdl, k_interpret<T>, dim3(nfields), dim3(256), 0, st, nfields, kind, est_kind,
+                                       d_ndims, d_levels, s, B, d_sizes, sz_stride, d_errs, err_stride, d_tols, tol0,
+                                       d_index, idx_stride, d_rsz);
+    if (e != cudaSuccess) return cuda_status(e, "k_interpret");
     return PRODM_OK;
 }
 
 template int launch_interpret<float>(int, int, int, const int*, const int*, double, int, const uint32_t*, uint64_t,
                                      const double*, uint64_t, const double*, double, uint8_t*, uint64_t,
-                                     uint32_t*, cudaStream_t);
+                                     uint32_t*, cudaStream_t, bool);
 template int launch_interpret<double>(int, int, int, const int*, const int*, double, int, const uint32_t*, uint64_t,
                                       const double*, uint64_t, const double*, double, uint8_t*, uint64_t,
-                                      uint32_t*, cudaStream_t);
+                                      uint32_t*, cudaStream_t, bool);
 
 }  // namespace prodm

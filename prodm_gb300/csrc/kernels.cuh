@@ -15,7 +15,7 @@ int launch_decompose_level_inplace(const T* in, const Box& F, const Box& C, T* o
                                    cudaStream_t st);
 template <class T>
 int launch_recompose_level_packed(const T* coarse, const T* coef, const Box& F, const Box& C, T* out, uint64_t s0,
-                                  uint64_t s1, cudaStream_t st);
+                                  uint64_t s1, cudaStream_t st, bool pdl = false);
 template <class T>
 int launch_recompose_level_inplace(const T* rin, const Box& F, const Box& C, T* out, uint64_t s0, uint64_t s1,
                                    cudaStream_t st);
@@ -69,7 +69,7 @@ template <class T>
 int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, const int* d_levels, double s, int B,
                      const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
-                     cudaStream_t st);
+                     cudaStream_t st, bool pdl = false);
 
 // one segment per (field, level) of the multi-level fp32 negabinary encode /
 // decode launches; chunk_begin is the segment's first global chunk
@@ -85,7 +85,7 @@ struct ChunkSeg {
 // bitplane.cu: every level of one fp32 field decoded in one launch; segments
 // chunked by kDecodeChunkBlocks blocks
 constexpr int kDecodeChunkBlocks = 128;
-int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st);
+int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st, bool pdl = false);
 // bitplane.cu: every level of one fp32 field in one encode launch; with
 // errs_out, per-level squared-error tables (partial: nseg * nb_encode_levels_grid(1)
 // * (B + 1) doubles)
@@ -97,7 +97,7 @@ int launch_nb_encode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunk
 bool decode_recompose_nb32_ok(const Box& F);
 int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, uint64_t nblocks, const void* maxkey,
                                  const uint8_t* dnum, const float* coarse, const Box& F, const Box& C, float* out,
-                                 uint64_t s0, uint64_t s1, int* status, cudaStream_t st);
+                                 uint64_t s0, uint64_t s1, int* status, cudaStream_t st, bool pdl = false);
 void fused_tma_test_hook(int tx_extra, long long wait_cycles);
 
 // perbit.cu: per-bit format; rows of 32-element group words (magnitude

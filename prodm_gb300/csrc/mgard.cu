@@ -193,6 +193,8 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
 template <class T>
 __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ coarse, const T* __restrict__ coef, Box F,
                                                         Box C, T* __restrict__ out, uint64_t s0, uint64_t s1) {
+    pdl_wait();   // the coarse box and the coefficients come from the previous launches
+    pdl_release();
     const uint32_t rows = F.n[0] * F.n[1];
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     const bool odd = (F.n[2] & 1u) != 0;
@@ -374,10 +376,12 @@ int launch_decompose_level_inplace(const T* in, const Box& F, const Box& C, T* o
 
 template <class T>
 int launch_recompose_level_packed(const T* coarse, const T* coef, const Box& F, const Box& C, T* out, uint64_t s0,
-                                  uint64_t s1, cudaStream_t st) {
+                                  uint64_t s1, cudaStream_t st, bool pdl) {
     const unsigned th = row_threads(F.n[2]);
-    k_recompose_rows<T><<<row_grid((uint64_t)F.n[0] * F.n[1], th), th, 0, st>>>(coarse, coef, F, C, out, s0, s1);
-    PRODM_CHECK_LAUNCH("k_recompose_rows");
+    count_launch();
+    const cudaError_t e = launch_chain(pdl, k_recompose_rows<T>, dim3(row_grid((uint64_t)F.n[0] * F.n[1], th)), dim3(th),
+                                       0, st, coarse, coef, F, C, out, s0, s1);
+    if (e != cudaSuccess) return cuda_status(e, "k_recompose_rows");
     return PRODM_OK;
 }
 
@@ -485,7 +489,7 @@ int launch_interleave(T* data, uint64_t s0, uint64_t s1, const Box& F, const Box
     template int launch_decompose_level_inplace<T>(const T*, const Box&, const Box&, T*, uint64_t, uint64_t, T*,    \
                                                    cudaStream_t);                                                   \
     template int launch_recompose_level_packed<T>(const T*, const T*, const Box&, const Box&, T*, uint64_t,         \
-                                                  uint64_t, cudaStream_t);                                          \
+                                                  uint64_t, cudaStream_t, bool);                                    \
     template int launch_recompose_level_inplace<T>(const T*, const Box&, const Box&, T*, uint64_t, uint64_t,        \
                                                    cudaStream_t);                                                   \
     template int launch_copy_box<T>(const T*, uint64_t, uint64_t, const Box&, T*, uint64_t, uint64_t, cudaStream_t); \
