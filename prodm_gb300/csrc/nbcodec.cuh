@@ -7,18 +7,23 @@ namespace prodm {
 
 // ---------------------------------------------------------------------------
 // 32 x 32 bit transpose across a warp: lane e holds row e on entry; on exit
-// lane k holds the word whose bit e is bit k of row e (five butterfly stages).
+// lane k holds the word whose bit e is bit k of row e. Five exchange stages
+// with the lane l ^ j: the two byte-granular stages (j = 16, 8) are one byte
+// permute each with a per-lane selector, the three sub-byte stages one
+// rotate (a funnel shift by a per-lane amount) and one masked merge each, so a
+// stage is a shuffle plus one or two instructions.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+    x = __byte_perm(x, __shfl_xor_sync(0xffffffffu, x, 16), (lane & 16) ? 0x3276u : 0x5410u);
+    x = __byte_perm(x, __shfl_xor_sync(0xffffffffu, x, 8), (lane & 8) ? 0x3715u : 0x6240u);
 #pragma unroll
-    for (int j = 16; j > 0; j >>= 1) {
-        const uint32_t m = j == 16 ? 0x0000ffffu : j == 8 ? 0x00ff00ffu : j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u
-                                                                                                       : 0x55555555u;
-        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    for (int j = 4; j > 0; j >>= 1) {
+        const uint32_t m = j == 4 ? 0x0f0f0f0fu : j == 2 ? 0x33333333u : 0x55555555u;
         const bool hi = (lane & j) != 0;
-        const uint32_t u = hi ? y : x, v = hi ? x : y;
-        const uint32_t t = ((u >> j) ^ v) & m;
-        x ^= hi ? t : (t << j);
+        const uint32_t keep = hi ? ~m : m;                       // bits of x that stay
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+        const uint32_t ys = __funnelshift_l(y, y, hi ? 32 - j : j);   // partner's bits moved into place
+        x = (x & keep) | (ys & ~keep);
     }
     return x;
 }
