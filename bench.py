@@ -213,6 +213,23 @@ def cpu_baseline(steps, warmup, threads=None):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+FUSED_LEVELS = 2   # the library's kFusedLevels
+
+
+def fused_from(level_dims, L):
+    """Lowest level decoded inside its recomposition (the library's rule for
+    fp32 negabinary hierarchical handles: the finest level, and the levels
+    below it down to FUSED_LEVELS in all while a level's plane has at least
+    4096 rows)."""
+    rows = [int(d[0]) * int(d[1]) for d in level_dims]
+    if rows[L] < 1024:
+        return L + 1
+    f = L
+    while f - 1 >= 1 and L - (f - 1) < FUSED_LEVELS and rows[f - 1] >= 4096:
+        f -= 1
+    return f
+
+
 def stage_bytes(mdr, kind, level, step_bytes_info):
     """algorithmic bytes of one launch of a stage."""
     import numpy as np
@@ -227,16 +244,16 @@ def stage_bytes(mdr, kind, level, step_bytes_info):
         if level == step_bytes_info["L"] and step_bytes_info.get("encode_multi"):
             levels = range(0, level + 1)     # one launch encodes every level
         return sum(4 * int(mdr.level_elements[l]) + int(sizes[l].astype(np.int64).sum()) for l in levels)
+    ffrom = step_bytes_info.get("fused_from", step_bytes_info["L"] + 1)
     if kind == "decode":
         levels = [level]
         if level == 0 and step_bytes_info.get("decode_multi"):
             # one launch decodes every level the fused kernel does not
-            top = step_bytes_info["L"] - (1 if step_bytes_info.get("fused") else 0)
-            levels = range(0, top + 1)
+            levels = range(0, ffrom)
         return sum(step_bytes_info["decode_bytes"][l] + 4 * int(mdr.level_elements[l]) for l in levels)
     if kind == "recompose":
-        if level == step_bytes_info["L"] and step_bytes_info.get("fused"):
-            # fused finest level: the retrieved planes are read instead of coefficients
+        if level >= ffrom:
+            # fused level: its retrieved planes are read instead of coefficients
             return step_bytes_info["decode_bytes"][level] + 4 * (box(level - 1) + box(level))
         return 4 * (box(level - 1) + n + box(level))
     return 0
@@ -345,8 +362,8 @@ def run_ours(args):
     # roofline of the dominant stage
     peak, peak_src = measured_peak()
     info = {"sizes": sizes, "decode_bytes": decode_bytes, "L": LEVELS,
-            "fused": ("decode", LEVELS) not in stages, "decode_multi": ("decode", 1) not in stages,
-            "encode_multi": ("encode", 0) not in stages}
+            "fused_from": fused_from(mdr.level_dims, LEVELS) if ("decode", LEVELS) not in stages else LEVELS + 1,
+            "decode_multi": ("decode", 1) not in stages, "encode_multi": ("encode", 0) not in stages}
     per_stage = {}
     for (kind, level), (tms, cnt) in stages.items():
         b = stage_bytes(mdr, kind, level, info)

@@ -712,11 +712,20 @@ struct Stage {
     }
 };
 
-// fp32 negabinary hierarchical: the finest level is decoded inside the fused
-// decode + recompose kernel
-bool fuse_finest(const prodm_mdr* h) {
+// Levels decoded inside their recomposition (fp32 negabinary, hierarchical):
+// the finest level and the next one down when its rows are plenty
+// (kFusedLevels in all; a third level, 129^3 at 513^3, measured slower);
+// returns the lowest such level, or L + 1 for none.
+constexpr int kFusedLevels = 2;
+int fused_from(const prodm_mdr* h) {
     const int L = h->g.L;
-    return h->nb && !h->orth && h->cfg.dtype == PRODM_F32 && L >= 1 && decode_recompose_nb32_ok(h->g.box[L]);
+    if (!(h->nb && !h->orth && h->cfg.dtype == PRODM_F32 && L >= 1 && decode_recompose_nb32_ok(h->g.box[L])))
+        return L + 1;
+    int from = L;
+    while (from - 1 >= 1 && L - (from - 1) < kFusedLevels && decode_recompose_nb32_ok(h->g.box[from - 1]) &&
+           (uint64_t)h->g.box[from - 1].n[0] * h->g.box[from - 1].n[1] >= 4096)
+        from--;
+    return from;
 }
 
 int mdr_alloc_all(prodm_mdr* h) {
@@ -817,9 +826,9 @@ int mdr_alloc_all(prodm_mdr* h) {
         PRODM_CUDA(cudaMemcpy(h->plane_ptrs, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice));
     }
     if (h->nb && dtype == PRODM_F32) {
-        // every level not decoded by the fused finest-level kernel, as one
-        // segment table (kDecodeChunkBlocks blocks per chunk)
-        const int top = fuse_finest(h) ? L - 1 : L;
+        // every level not decoded inside its recomposition, as one segment
+        // table (kDecodeChunkBlocks blocks per chunk)
+        const int top = fused_from(h) - 1;
         std::vector<ChunkSeg> segs;
         uint64_t chunks = 0;
         for (int l = 0; l <= top; l++) {
@@ -938,14 +947,14 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
     T* rcoef = (T*)h->rcoef;
     int rc;
     // finest level: fused decode + recompose where the layout allows it
-    const bool fuse = fuse_finest(h);
+    const int ffrom = fused_from(h);
     if (h->dseg && sizeof(T) == 4) {
         // fp32 negabinary: every other level in one launch (timed as level 0)
         Stage sg(h, 3, 0, st);
         if ((rc = launch_nb_decode_levels(h->dseg, h->dseg_n, h->dseg_chunks, st, true))) return rc;
     }
     for (int l = 0; l <= L; l++) {
-        if ((fuse && l == L) || (h->dseg && sizeof(T) == 4)) continue;
+        if (l >= ffrom || (h->dseg && sizeof(T) == 4)) continue;
         const uint64_t n = g.elems[l];
         Stage sg(h, 3, l, st);
         if (h->pb) {
@@ -972,7 +981,7 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         T* cin = (l == 1) ? rcoef + h->roff[0] : (T*)h->rbuf[(l - 1) & 1];
         T* o = (l == L) ? out : (T*)h->rbuf[l & 1];
         Stage sg(h, 4, l, st);
-        if (fuse && l == L) {
+        if (l >= ffrom) {
             if ((rc = launch_decode_recompose_nb32(h->streams + h->lvl_byte_off[l], h->plane_cap[l], B,
                                                    h->nblocks[l], keys + l, h->index + l, (const float*)cin, F, C,
                                                    (float*)o, (uint64_t)F.n[1] * F.n[2], F.n[2], h->kstatus, st,
