@@ -116,9 +116,17 @@ __device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, u
         }
         uint32_t nb[NB_G];
         float sh[NB_G], d[NB_G];
+        // NegaBinaryBPEncoder.hpp:42; the scaling is chosen once per chunk
+        // (an exact multiplication whenever 2^se is a normal float)
+        if (fast) {
+#pragma unroll
+            for (int g = 0; g < NB_G; g++) sh[g] = v[g] * scale;
+        } else {
+#pragma unroll
+            for (int g = 0; g < NB_G; g++) sh[g] = ldexpf(v[g], se);
+        }
 #pragma unroll
         for (int g = 0; g < NB_G; g++) {
-            sh[g] = fast ? v[g] * scale : ldexpf(v[g], se);    // NegaBinaryBPEncoder.hpp:42
             const int32_t q = (int32_t)sh[g];
             nb[g] = nb_from_bin(q);
             d[g] = sh[g] - (float)q;                             // exact fraction
