@@ -13,6 +13,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
 #include <mutex>
 
 #include "common.cuh"
@@ -53,6 +54,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
         if (clock64() - t0 > limit) return false;
     return true;
 }
+// this thread's arrival (release of its earlier shared-memory writes)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+// named barrier 1 over the first `n` threads of the block, OR of a flag
+__device__ __forceinline__ bool group_any(bool v, int n) {
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r)
+                 : "r"((uint32_t)v), "r"(n)
+                 : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void group_sync(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
 // generic-proxy accesses of shared memory before async-proxy (TMA) ones
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 // box {x .. x + box_w - 1} of row y of a 2-D tensor map into shared memory
@@ -196,12 +211,12 @@ __device__ __forceinline__ float cb_at(const float* cb, uint32_t r) { return cb[
 // used), so a row waits for the L2 latency about once instead of once per
 // group. Groups in which every lane has a pair run without bounds checks, on
 // pointers advanced once per D groups; the last node is written by lane 0.
-template <int M01>
+template <int M01, bool DEEP = false>
 __device__ __forceinline__ void recompose_row_odd(const float* __restrict__ cb0, uint64_t cs0, uint64_t cs1,
                                                   uint32_t c2n, const float* __restrict__ cb, uint32_t rb0,
                                                   float* __restrict__ orow, int lane) {
     constexpr int NQ = M01 == 0 ? 1 : (M01 == 3 ? 4 : 2);
-    constexpr int D = M01 == 3 ? 3 : 4;
+    constexpr int D = DEEP ? (M01 == 3 ? 4 : 6) : (M01 == 3 ? 3 : 4);   // column groups in flight
     int64_t co[NQ];   // corner row offsets, in corner_tree order
     co[0] = 0;
     if constexpr (NQ == 2) co[1] = (int64_t)(M01 == 1 ? cs0 : cs1);
@@ -344,6 +359,7 @@ __device__ __forceinline__ FusedRow fused_row(uint32_t rho, const Box& F, const 
 
 // one warp: a fine row (odd length) from the coarse box and the decoded
 // coefficients in cb (value v of block t at cb[t * CB_LD + v], block fb first)
+template <bool DEEP = false>
 __device__ __forceinline__ void recompose_fine_row(const FusedRow& r, const Box& C, const float* __restrict__ coarse,
                                                    float* __restrict__ out, const float* __restrict__ cb, int lane) {
     const uint32_t c2n = C.n[2];
@@ -352,10 +368,10 @@ __device__ __forceinline__ void recompose_fine_row(const FusedRow& r, const Box&
     float* orow = out + r.out_off;
     const uint32_t rb0 = r.rb;
     switch (r.m01) {
-        case 0: recompose_row_odd<0>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-        case 1: recompose_row_odd<1>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-        case 2: recompose_row_odd<2>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
-        default: recompose_row_odd<3>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        case 0: recompose_row_odd<0, DEEP>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        case 1: recompose_row_odd<1, DEEP>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        case 2: recompose_row_odd<2, DEEP>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
+        default: recompose_row_odd<3, DEEP>(cb0, cs0, cs1, c2n, cb, rb0, orow, lane); break;
     }
 }
 
@@ -469,8 +485,9 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
 // reading its block's 32 rows and combining rows 31-k and 15-k at once
 template <bool FAST, int RS>
 __device__ __forceinline__ void decode_tile_pm(const uint32_t* __restrict__ tile, float* __restrict__ cb,
-                                               uint32_t nbk, int num, int exp, bool neg, float dscale) {
-    for (uint32_t i = threadIdx.x; i < 2 * nbk; i += blockDim.x) {
+                                               uint32_t nbk, int num, int exp, bool neg, float dscale,
+                                               uint32_t tid = threadIdx.x, uint32_t nthreads = blockDim.x) {
+    for (uint32_t i = tid; i < 2 * nbk; i += nthreads) {
         const uint32_t t = i >> 1;
         const int half = i & 1;
         float* dst = cb + t * CB_LD + 16 * half;
@@ -581,6 +598,128 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
     }
 }
 
+// Warp-specialised form of the TMA kernel: 16 warps, warps 0..7 decode and
+// warps 8..15 recompose, with both the plane tile and the coefficient tile
+// double buffered, so the decode of unit it + 1 runs while unit it is
+// recomposed. The groups meet only on mbarriers: tile_full (the TMA bytes of
+// a unit's planes), coef_full (all decode threads arrived after writing a
+// unit's coefficients and row geometry) and coef_empty (all recomposition
+// threads arrived after their rows). The decode warps stay in step with a
+// named barrier; with 64 registers the recomposition keeps six column groups
+// in flight (four for four-corner rows). Every wait is bounded by
+// `wait_limit` SM cycles; a group that gives up writes PRODM_ETIMEOUT to
+// *status, lets its copies in flight land (bounded again) and returns, and
+// the other group's waits then run out too.
+template <int RS>
+__global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
+    const __grid_constant__ CUtensorMap tmap, uint32_t bw, const uint32_t* __restrict__ maxkey,
+    const uint8_t* __restrict__ dnum, const float* __restrict__ coarse, Box F, Box C, float* __restrict__ out,
+    uint64_t s0, uint64_t s1, uint32_t tld, int* __restrict__ status, long long wait_limit, uint32_t tx_extra) {
+    extern __shared__ __align__(128) uint32_t ws_smem[];
+    uint32_t* tiles = ws_smem;                               // [2][32][RS] plane-major
+    float* cbs = (float*)(ws_smem + 2 * 32 * RS);            // [2][tld][CB_LD]
+    __shared__ __align__(8) uint64_t bar_tile[2], bar_full[2], bar_empty[2];
+    __shared__ uint64_t s_fb[2];
+    __shared__ uint32_t s_nbk[2];
+    __shared__ FusedRow s_row[2][8];
+    constexpr int GROUP = 256;                               // threads per group
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool dec = threadIdx.x < GROUP;
+    const int num = dnum[0];
+    const int exp = frexp_exp(__uint_as_float(*maxkey)) + 2;
+    const bool neg = num != 0 && (num & 1);                  // NegaBinaryBPEncoder.hpp:153, :177
+    const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
+    const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
+    const uint32_t rows = F.n[0] * F.n[1];
+    const uint32_t nunits = (rows + 7) / 8;
+    const int poff = 32 - num;
+    const uint32_t u0 = blockIdx.x, step = gridDim.x;
+    if (u0 >= nunits) return;
+    const int myunits = (int)((nunits - u0 + step - 1) / step);
+    if ((smem_addr(tiles) & 127u) != 0) {   // TMA destinations need 128-byte alignment
+        if (threadIdx.x == 0) atomicExch(status, PRODM_ECUDA);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar_tile[0], 1);
+        mbar_init(&bar_tile[1], 1);
+        mbar_init(&bar_full[0], GROUP);
+        mbar_init(&bar_full[1], GROUP);
+        mbar_init(&bar_empty[0], GROUP);
+        mbar_init(&bar_empty[1], GROUP);
+    }
+    for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) {   // planes not retrieved
+        tiles[i] = 0u;
+        tiles[32 * RS + i] = 0u;
+    }
+    __syncthreads();
+    const uint32_t bytes = (uint32_t)num * bw * 4u + tx_extra;
+    // warp 0: block range of unit k of this CTA into slot b, then its planes into tile b
+    auto issue = [&](int k, int b) {
+        if (lane == 0) {
+            const uint32_t r0 = (u0 + (uint32_t)k * step) * 8;
+            fused_block_range(r0, rows, F, C, s_fb[b], s_nbk[b]);
+            mbar_arrive_expect_tx(&bar_tile[b], bytes);
+        }
+        __syncwarp();
+        const int x = (int)(s_fb[b] & ~3ull);
+        uint32_t* tile = tiles + b * 32 * RS;
+        for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar_tile[b]);
+    };
+    if (warp == 0) {
+        issue(0, 0);
+        if (myunits > 1) issue(1, 1);
+    }
+    // the first tiles are on their way; the coarse box and the output belong
+    // to the previous launches (the plane counts and the planes are older)
+    pdl_wait();
+    pdl_release();
+    if (dec) {
+        for (int it = 0; it < myunits; it++) {
+            const int b = it & 1;
+            const uint32_t ph = (uint32_t)(it >> 1) & 1u;
+            bool ok = mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
+            ok = ok && mbar_wait_bounded(&bar_empty[b], ph ^ 1u, wait_limit);   // first use: the phase before is done
+            if (group_any(!ok, GROUP)) {
+                if (threadIdx.x == 0) atomicExch(status, PRODM_ETIMEOUT);
+                mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
+                if (it + 1 < myunits) mbar_wait_bounded(&bar_tile[b ^ 1], ((uint32_t)(it + 1) >> 1) & 1u, wait_limit);
+                return;
+            }
+            const uint64_t fb = s_fb[b];
+            const uint32_t nbk = s_nbk[b];
+            if (warp == 0 && lane < 8) {
+                const uint32_t r = (u0 + (uint32_t)it * step) * 8 + lane;
+                if (r < rows) s_row[b][lane] = fused_row(r, F, C, s0, s1, fb);
+                else s_row[b][lane].m01 = -1;
+            }
+            const uint32_t* t0 = tiles + b * 32 * RS + (fb & 3u);
+            float* cb = cbs + (size_t)b * tld * CB_LD;
+            if (dfast) decode_tile_pm<true, RS>(t0, cb, nbk, num, exp, neg, dscale, threadIdx.x, GROUP);
+            else decode_tile_pm<false, RS>(t0, cb, nbk, num, exp, neg, dscale, threadIdx.x, GROUP);
+            mbar_arrive(&bar_full[b]);
+            group_sync(GROUP);   // tile b is decoded: it may take unit it + 2
+            if (warp == 0 && it + 2 < myunits) {
+                fence_proxy_async_smem();
+                issue(it + 2, b);
+            }
+        }
+    } else {
+        const int rw = warp - GROUP / 32;
+        for (int it = 0; it < myunits; it++) {
+            const int b = it & 1;
+            const uint32_t ph = (uint32_t)(it >> 1) & 1u;
+            if (!mbar_wait_bounded(&bar_full[b], ph, wait_limit)) {
+                if (lane == 0) atomicExch(status, PRODM_ETIMEOUT);
+                return;
+            }
+            const FusedRow r = s_row[b][rw];
+            if (r.m01 >= 0) recompose_fine_row<true>(r, C, coarse, out, cbs + (size_t)b * tld * CB_LD, lane);
+            mbar_arrive(&bar_empty[b]);
+        }
+    }
+}
+
 }  // namespace
 
 static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
@@ -621,10 +760,44 @@ void fused_tma_test_hook(int tx_extra, long long wait_cycles) {
 // The TMA kernel for odd rows whose 8-row block range fits one box (at most
 // 256 words): box width and tile row stride (a multiple of 32 words, so that
 // every tile row starts on a 128-byte boundary).
+// Which TMA kernel a fused level takes: the warp-specialised form where the
+// tile rows are 160 words or more (rows of about 360 values and up), the
+// 8-warp form below that (measured at 513^3, step 3.047 ms with the 8-warp
+// form everywhere, 3.008 ms warp-specialised everywhere, 2.966 ms mixed).
+// PRODM_FUSED_WS overrides: 0 never, 1 always, 2 the default rule.
+static int fused_ws() {
+    static const int mode = [] {
+        const char* v = getenv("PRODM_FUSED_WS");
+        return v ? atoi(v) : 2;
+    }();
+    return mode;
+}
+
+template <int RS>
+static int launch_fused_ws(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
+                           const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
+                           int* status, cudaStream_t st, bool pdl) {
+    const uint32_t tld = fused_max_blocks(F);
+    const size_t smem = (size_t)2 * 32 * RS * 4 + (size_t)2 * tld * CB_LD * 4;
+    const void* kern = (const void*)k_decode_recompose_nb32_ws<RS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+    const uint64_t need = ((uint64_t)F.n[0] * F.n[1] + 7) / 8;
+    const unsigned grid = persistent_grid_for(kern, 512, smem, need, need);
+    count_launch();
+    e = launch_chain(pdl, k_decode_recompose_nb32_ws<RS>, dim3(grid), dim3(512), smem, st, map, bw,
+                     (const uint32_t*)maxkey, dnum, coarse, F, C, out, s0, s1, tld, status, g_tma_wait_cycles,
+                     (uint32_t)g_tma_tx_extra);
+    if (e != cudaSuccess) return cuda_status(e, "k_decode_recompose_nb32_ws");
+    return PRODM_OK;
+}
+
 template <int RS>
 static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
                             const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
                             int* status, cudaStream_t st, bool pdl) {
+    if (fused_ws() == 1 || (fused_ws() == 2 && RS >= 160))
+        return launch_fused_ws<RS>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
     const size_t smem = (size_t)32 * RS * 4 + (size_t)fused_max_blocks(F) * CB_LD * 4;
     const void* kern = (const void*)k_decode_recompose_nb32_tma<RS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -208,7 +208,8 @@ def test_reconstructor_fed_from_reference_files(enc):
 
 
 @pytest.mark.parametrize("shape,L", [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129, 129, 129), 4),
-                                     ((200, 131), 4), ((33, 33, 1025), 2), ((40, 33, 301), 3)])
+                                     ((200, 131), 4), ((33, 33, 1025), 2), ((40, 33, 301), 3), ((33, 33, 513), 3),
+                                     ((40, 36, 411), 2)])
 def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
     """fp32 negabinary hierarchical: the finest level is decoded inside the
     recomposition kernel (odd and even row lengths take different kernels);
@@ -231,14 +232,16 @@ def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
         assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), idx
 
 
-def test_fused_tile_wait_timeout_is_reported_and_recoverable():
-    """The fused finest-level kernel waits for its TMA plane tiles on an
-    mbarrier, each wait bounded. With the expected byte count raised (the test
+@pytest.mark.parametrize("shape", [(65, 65, 65), (33, 33, 513)])
+def test_fused_tile_wait_timeout_is_reported_and_recoverable(shape):
+    """The fused finest-level kernels (the 8-warp form at 65^3, the
+    warp-specialised form at 33 x 33 x 513) wait for their TMA plane tiles on
+    mbarriers, each wait bounded. With the expected byte count raised (the test
     hook) no tile ever completes: every CTA gives up after a short limit,
     reports PRODM_ETIMEOUT and returns; the status is cleared once read and
     the next retrieval is exact again."""
     from prodm_gb300._lib import ProdmError
-    shape, L = (65, 65, 65), 3
+    L = 3
     x = fields().spectral_grf(shape, seed=11, device="cuda")
     m = api().MDRField(shape, torch.float32, L, 32, "negabinary", "hierarchical", "max")
     m.refactor(x)
