@@ -58,15 +58,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
-// named barrier 1 over the first `n` threads of the block, OR of a flag
-__device__ __forceinline__ bool group_any(bool v, int n) {
-    uint32_t r;
-    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
-                 : "=r"(r)
-                 : "r"((uint32_t)v), "r"(n)
-                 : "memory");
-    return r != 0;
-}
+// named barrier 1 over the first `n` threads of the block
 __device__ __forceinline__ void group_sync(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
 // generic-proxy accesses of shared memory before async-proxy (TMA) ones
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -607,9 +599,12 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
 // threads arrived after their rows). The decode warps stay in step with a
 // named barrier; with 64 registers the recomposition keeps six column groups
 // in flight (four for four-corner rows). Every wait is bounded by
-// `wait_limit` SM cycles; a group that gives up writes PRODM_ETIMEOUT to
-// *status, lets its copies in flight land (bounded again) and returns, and
-// the other group's waits then run out too.
+// `wait_limit` SM cycles. A decode thread whose wait gives up raises a
+// shared flag that the whole decode group reads after its barrier (so the
+// group leaves together: it writes PRODM_ETIMEOUT to *status, lets its copies
+// in flight land, bounded again, and returns); a recomposition warp that
+// gives up writes the status and returns, and the other group's waits then
+// run out too.
 template <int RS>
 __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     const __grid_constant__ CUtensorMap tmap, uint32_t bw, const uint32_t* __restrict__ maxkey,
@@ -622,6 +617,7 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     __shared__ uint64_t s_fb[2];
     __shared__ uint32_t s_nbk[2];
     __shared__ FusedRow s_row[2][8];
+    __shared__ volatile int s_abort;
     constexpr int GROUP = 256;                               // threads per group
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool dec = threadIdx.x < GROUP;
@@ -641,6 +637,7 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
         return;
     }
     if (threadIdx.x == 0) {
+        s_abort = 0;
         mbar_init(&bar_tile[0], 1);
         mbar_init(&bar_tile[1], 1);
         mbar_init(&bar_full[0], GROUP);
@@ -680,12 +677,7 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
             const uint32_t ph = (uint32_t)(it >> 1) & 1u;
             bool ok = mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
             ok = ok && mbar_wait_bounded(&bar_empty[b], ph ^ 1u, wait_limit);   // first use: the phase before is done
-            if (group_any(!ok, GROUP)) {
-                if (threadIdx.x == 0) atomicExch(status, PRODM_ETIMEOUT);
-                mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
-                if (it + 1 < myunits) mbar_wait_bounded(&bar_tile[b ^ 1], ((uint32_t)(it + 1) >> 1) & 1u, wait_limit);
-                return;
-            }
+            if (!ok) s_abort = 1;   // read by the whole group after its next barrier
             const uint64_t fb = s_fb[b];
             const uint32_t nbk = s_nbk[b];
             if (warp == 0 && lane < 8) {
@@ -699,6 +691,12 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
             else decode_tile_pm<false, RS>(t0, cb, nbk, num, exp, neg, dscale, threadIdx.x, GROUP);
             mbar_arrive(&bar_full[b]);
             group_sync(GROUP);   // tile b is decoded: it may take unit it + 2
+            if (s_abort) {   // a wait gave up: report, let the copies in flight land, leave
+                if (threadIdx.x == 0) atomicExch(status, PRODM_ETIMEOUT);
+                mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
+                if (it + 1 < myunits) mbar_wait_bounded(&bar_tile[b ^ 1], ((uint32_t)(it + 1) >> 1) & 1u, wait_limit);
+                return;
+            }
             if (warp == 0 && it + 2 < myunits) {
                 fence_proxy_async_smem();
                 issue(it + 2, b);
