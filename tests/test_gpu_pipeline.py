@@ -209,10 +209,13 @@ def test_reconstructor_fed_from_reference_files(enc):
 
 @pytest.mark.parametrize("shape,L", [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129, 129, 129), 4),
                                      ((200, 131), 4), ((33, 33, 1025), 2), ((40, 33, 301), 3), ((33, 33, 513), 3),
-                                     ((40, 36, 411), 2)])
+                                     ((40, 36, 411), 2), ((33, 32, 801), 2)])
 def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
     """fp32 negabinary hierarchical: the finest level is decoded inside the
-    recomposition kernel (odd and even row lengths take different kernels);
+    recomposition kernel (odd and even row lengths take different kernels;
+    odd rows of up to ~360 values the 8-warp TMA kernel, longer ones up to
+    ~990 values the warp-specialised one with 160- and 256-word tile rows,
+    longer still the cp.async kernel);
     the other levels go through the multi-level decoder. The output equals the
     oracle's decode -> reposition -> recompose in float bit for bit."""
     B = 32
