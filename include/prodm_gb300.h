@@ -1,6 +1,6 @@
 /*
  * prodm_gb300 -- C ABI of the GB300 (sm_103a) implementation of ProDM's MDR
- * refactor / retrieve path (lxAltria/ProDM, include/MDR/**).
+ * refactor / retrieve path (lxAltria/ProDM, the headers under include/MDR).
  *
  * Plain C types only: device buffers are raw pointers, CUDA streams are passed
  * as void* (cudaStream_t), sizes are 64-bit. Every function returns a status

@@ -118,23 +118,6 @@ template <> struct Acc<double> { using type = double; static constexpr int N = 6
 struct NbErr32 {
     float acc[32];
     float accx;
-    __device__ void zero() {
-#pragma unroll
-        for (int k = 0; k < 32; k++) acc[k] = 0.f;
-        accx = 0.f;
-    }
-    __device__ __forceinline__ void add(uint32_t nb, float shifted, float m, int B) {
-        float d = m;
-        acc[0] += m * m;
-#pragma unroll
-        for (int k = 1; k < 32; k++) {
-            if (k < B) {
-                if ((nb >> (k - 1)) & 1u) d += nbw(k - 1);
-                acc[k] += d * d;
-            }
-        }
-        accx += shifted * shifted;
-    }
     // table entry B-k <- acc[k]; entry B <- acc[0]; entry 0 <- accx
     __device__ void flush(int B, double* partial) {
         __shared__ double red[33];

@@ -1090,8 +1090,6 @@ int mdr_unpack_loaded(prodm_mdr* h, cudaStream_t st) {
             if (h->loaded[l] < hdr) continue;
             PRODM_CUDA(cudaMemcpyAsync(h->rbs + h->rb_off[l], h->lfile[l] + 4, nbk, cudaMemcpyDeviceToDevice, st));
             if ((rc = launch_chunk_words_from_rb(h->rbs + h->rb_off[l], nbk, B, h->chunk_words, st))) return rc;
-            uint32_t* scratch_sizes = (uint32_t*)h->rsz;   // sizes are known from the metadata
-            (void)scratch_sizes;
             if ((rc = launch_gr_scan_only(h->chunk_words, gr_nchunks(nbk), B, nbk, wb, h->chunk_off + h->co_off[l],
                                           (uint32_t*)h->partial, st)))
                 return rc;

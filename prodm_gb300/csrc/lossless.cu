@@ -336,7 +336,7 @@ int ll_compress_level(const uint8_t* d_raw, const uint32_t* h_sizes, int B, int 
         o += h_sizes[p];
     }
     ZJob j;
-    uint8_t* area;
+    uint8_t* area = nullptr;
     int rc = j.setup(ss, scr, &area, st);
     if (rc) return rc;
     for (int p = 0; p < B; p++) ss[p].dst = area + doff[p];
