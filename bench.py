@@ -231,7 +231,7 @@ def fused_from(level_dims, L):
 
 
 def stage_bytes(mdr, kind, level, step_bytes_info):
-    """algorithmic bytes of one launch of a stage."""
+    """algorithmic bytes of one launch of a stage: what the stage must read and write."""
     import numpy as np
     ld = mdr.level_dims
     box = lambda l: int(np.prod(ld[l].astype(np.int64)))

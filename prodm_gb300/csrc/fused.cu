@@ -733,7 +733,7 @@ bool decode_recompose_nb32_ok(const Box& F) {
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
-// against the driver library); NULL when the driver does not provide it
+// against the CUDA driver library); NULL when the CUDA driver does not provide it
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
