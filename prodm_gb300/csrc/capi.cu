@@ -591,6 +591,7 @@ struct prodm_mdr {
     int* pbstatus = nullptr;                       // per-bit: parse status of loaded streams
     int* kstatus = nullptr;                        // bounded device waits of retrievals (0 or a PRODM_E* code)
     uint8_t* hmap = nullptr;                       // mapped pinned host memory: plane counts [0, 64), status [64, 68)
+    bool after_reconstruct = false;                // the last call on the handle was a reconstruction
     uint8_t* dmap = nullptr;                       // its device address
     std::vector<void*> allocs;
     void* coef = nullptr;
@@ -1016,8 +1017,12 @@ int mdr_interpret(prodm_mdr* h, double tol, int interp, int est, double s, cudaS
         errs = h->sqerr;
     }
     Stage sg(h, 2, 0, st);
+    // right after a reconstruction (whose kernels write none of the tables
+    // and read the plane counts), the interpreter may tabulate before it waits
+    const bool early = h->after_reconstruct;
+    h->after_reconstruct = false;
     return launch_interpret<T>(1, interp, est, h->ndims_d, h->levels_d, s, B, h->sizes, 0, errs, 0, nullptr, tol,
-                               h->index, 0, h->rsz, st, true);
+                               h->index, 0, h->rsz, st, true, early);
 }
 
 // grouped levels loaded from files: header -> rb + chunk offsets, then the
@@ -1192,9 +1197,12 @@ int mdr_ll_expand(prodm_mdr* h, cudaStream_t st) {
 template <class T>
 int mdr_reconstruct(prodm_mdr* h, T* out, cudaStream_t st) {
     int rc;
+    h->after_reconstruct = false;
     if (h->from_files && h->ll_latter >= 0 && (rc = mdr_ll_expand(h, st))) return rc;
     if (h->from_files && !h->nb && (rc = mdr_unpack_loaded(h, st))) return rc;
-    return mdr_decode_recompose<T>(h, out, st);
+    if ((rc = mdr_decode_recompose<T>(h, out, st))) return rc;
+    h->after_reconstruct = true;
+    return PRODM_OK;
 }
 
 template <class T>
@@ -1661,6 +1669,7 @@ static int mdr_lossless_sizes(prodm_mdr* h, cudaStream_t st);
 
 int prodm_mdr_refactor(prodm_mdr* h, const void* field, void* stream) {
     if (!h || !field) return fail(PRODM_EINVAL, "prodm_mdr_refactor: NULL pointer");
+    h->after_reconstruct = false;
     cudaStream_t st = (cudaStream_t)stream;
     if (h->from_files) h->ll_latter = -1;   // a loaded stage does not carry over to a new refactor
     h->from_files = false;
@@ -1930,6 +1939,7 @@ int prodm_mdr_export_level_range(prodm_mdr* h, int level, uint64_t offset, uint6
 
 int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    h->after_reconstruct = false;
     if (h->from_files) return fail(PRODM_EINVAL, "set_lossless: a handle fed from files takes the stage from its metadata");
     h->hsz_valid = false;
     cudaStream_t st = (cudaStream_t)stream;
@@ -1969,6 +1979,7 @@ int prodm_mdr_reconstruct(prodm_mdr* h, void* out, void* stream) {
 
 int prodm_mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, void* stream) {
     if (!h || !buf) return fail(PRODM_EINVAL, "NULL pointer");
+    h->after_reconstruct = false;
     cudaStream_t st = (cudaStream_t)stream;
     if (h->cfg.dtype == PRODM_F64) return mdr_load_metadata<double>(h, buf, len, st);
     return mdr_load_metadata<float>(h, buf, len, st);
@@ -1976,6 +1987,7 @@ int prodm_mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, void* 
 
 int prodm_mdr_load_level(prodm_mdr* h, int level, const void* src, uint64_t off, uint64_t bytes, int host, void* stream) {
     if (!h || (!src && bytes)) return fail(PRODM_EINVAL, "NULL pointer");
+    h->after_reconstruct = false;
     if (level < 0 || level > h->g.L) return fail(PRODM_EINVAL, "level out of range");
     if (h->from_files && h->ll_latter >= 0) return mdr_ll_load(h, level, src, off, bytes, host, (cudaStream_t)stream);
     return mdr_load_level(h, level, src, off, bytes, host, (cudaStream_t)stream);
@@ -1984,6 +1996,7 @@ int prodm_mdr_load_level(prodm_mdr* h, int level, const void* src, uint64_t off,
 int prodm_mdr_load_level_file(prodm_mdr* h, int level, const char* path, uint64_t file_offset, uint64_t level_offset,
                               uint64_t bytes, void* stream) {
     if (!h || !path) return fail(PRODM_EINVAL, "NULL pointer");
+    h->after_reconstruct = false;
     if (level < 0 || level > h->g.L) return fail(PRODM_EINVAL, "level out of range");
     if (!h->from_files) return fail(PRODM_EINVAL, "load_level_file: load the metadata first");
     cudaStream_t st = (cudaStream_t)stream;
@@ -2082,6 +2095,7 @@ int prodm_debug_tile_wait(int extra_tx_bytes, long long wait_cycles) {
 
 int prodm_mdr_reset_retrieval(prodm_mdr* h, void* stream) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    h->after_reconstruct = false;
     PRODM_CUDA(cudaMemsetAsync(h->index, 0, h->g.L + 1, (cudaStream_t)stream));
     return PRODM_OK;
 }

@@ -306,9 +306,16 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
                                                    const double* __restrict__ errs, uint64_t err_stride,
                                                    const double* __restrict__ tols, double tol0,
                                                    uint8_t* __restrict__ index, uint64_t idx_stride,
-                                                   uint32_t* __restrict__ rsz) {
-    pdl_wait();   // writes the plane counts the previous retrieval's kernels read
-    pdl_release();
+                                                   uint32_t* __restrict__ rsz, bool early) {
+    // The kernel writes the plane counts that the previous retrieval's kernels
+    // read, so it waits for them before the walk. With `early` (the host knows
+    // that only this handle's reconstruction kernels, which write none of the
+    // tables, ran since they were last written) the tables are read and
+    // tabulated before that wait; otherwise everything waits.
+    if (!early) {
+        pdl_wait();
+        pdl_release();
+    }
     const int f = blockIdx.x;
     if (f >= nfields) return;
     const int L = levels[f];
@@ -348,6 +355,10 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
         s_en[l * 64 + j] = (int8_t)num;
     }
     __syncthreads();
+    if (early) {
+        pdl_wait();
+        pdl_release();
+    }
     __shared__ uint32_t s_rs[kMaxLevels];
     __shared__ int s_ok;
     uint32_t* gr = rsz + f * idx_stride;
@@ -378,20 +389,20 @@ template <class T>
 int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, const int* d_levels, double s, int B,
                      const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
-                     cudaStream_t st, bool pdl) {
+                     cudaStream_t st, bool pdl, bool early) {
     count_launch();
     const cudaError_t e = launch_chain(pdl, k_interpret<T>, dim3(nfields), dim3(256), 0, st, nfields, kind, est_kind,
                                        d_ndims, d_levels, s, B, d_sizes, sz_stride, d_errs, err_stride, d_tols, tol0,
-                                       d_index, idx_stride, d_rsz);
+                                       d_index, idx_stride, d_rsz, pdl && early);
     if (e != cudaSuccess) return cuda_status(e, "k_interpret");
     return PRODM_OK;
 }
 
 template int launch_interpret<float>(int, int, int, const int*, const int*, double, int, const uint32_t*, uint64_t,
                                      const double*, uint64_t, const double*, double, uint8_t*, uint64_t,
-                                     uint32_t*, cudaStream_t, bool);
+                                     uint32_t*, cudaStream_t, bool, bool);
 template int launch_interpret<double>(int, int, int, const int*, const int*, double, int, const uint32_t*, uint64_t,
                                       const double*, uint64_t, const double*, double, uint8_t*, uint64_t,
-                                      uint32_t*, cudaStream_t, bool);
+                                      uint32_t*, cudaStream_t, bool, bool);
 
 }  // namespace prodm

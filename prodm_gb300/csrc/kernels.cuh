@@ -69,7 +69,7 @@ template <class T>
 int launch_interpret(int nfields, int kind, int est_kind, const int* d_ndims, const int* d_levels, double s, int B,
                      const uint32_t* d_sizes, uint64_t sz_stride, const double* d_errs, uint64_t err_stride,
                      const double* d_tols, double tol0, uint8_t* d_index, uint64_t idx_stride, uint32_t* d_rsz,
-                     cudaStream_t st, bool pdl = false);
+                     cudaStream_t st, bool pdl = false, bool early = false);
 
 // one segment per (field, level) of the multi-level fp32 negabinary encode /
 // decode launches; chunk_begin is the segment's first global chunk
