@@ -174,9 +174,12 @@ int prodm_collect_squared(int dtype, const void* d_data, uint64_t n, int num_bit
  * cudaMalloc/cudaFree inside their callbacks) and have no workspace to pass.
  * Its scratch is a fixed 316,160-byte device array, enough for
  * num_bitplanes <= 64 (fp64) / 32 (fp32); larger values return PRODM_EINVAL.
- * The first call on a device looks up that array's address (make it before
- * any stream capture). All calls on a device share the array: calls that
- * overlap on the GPU race; calls on one stream are ordered. */
+ * Every call on a stream that is not capturing looks up that array's address
+ * on the current device (so it stays right after cudaDeviceReset); a call
+ * during a stream capture uses the address of the device's last uncaptured
+ * call, so make the first call before any capture. All calls on a device
+ * share the array: calls that overlap on the GPU race; calls on one stream
+ * are ordered. */
 int prodm_collect_squared_noalloc(int dtype, const void* d_data, uint64_t n, int num_bitplanes,
                                   double max_level_error, double* d_out, void* stream);
 

@@ -85,15 +85,14 @@ __global__ void __launch_bounds__(256) k_recompose_multi(const RowSeg* __restric
 __global__ void __launch_bounds__(256) k_nb_encode_multi(const ChunkSeg* __restrict__ segs, int nseg, uint64_t total,
                                                         int B) {
     __shared__ uint32_t tile[32 * NB_TILE_LD];
-    float acc[32], accx = 0.f;
     for (uint64_t c = blockIdx.x; c < total; c += gridDim.x) {
         const int s = find_seg(segs, nseg, c, &ChunkSeg::chunk_begin);
         const ChunkSeg& q = segs[s];
         const int exp = frexp_exp(__uint_as_float(*q.key)) + 2;     // NegaBinaryBPEncoder.hpp:21
         const int se = B - exp;
         const bool fast = pow2_normal(se);
-        nb_encode32_chunk<false>(q.x, q.n, q.nblocks, B, se, fast, fast ? pow2f(se) : 1.f, q.words, q.stride,
-                                 c - q.chunk_begin, tile, acc, accx);
+        nb_encode32_chunk(q.x, q.n, q.nblocks, B, se, fast, fast ? pow2f(se) : 1.f, q.words, q.stride,
+                          c - q.chunk_begin, tile);
     }
 }
 

@@ -12,9 +12,13 @@
 // transposes one bitplane of the block into one stream word; lane p then
 // owns the word of plane p (and p + 32 for fp64).
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
+#include "errtab.cuh"
 #include "kernels.cuh"
 #include "nbcodec.cuh"
 
@@ -34,39 +38,32 @@ __device__ __forceinline__ int32_t trunc_fps(float v) { return (int32_t)v; }
 __device__ __forceinline__ int64_t trunc_fps(double v) { return (int64_t)v; }
 
 // ---------------------------------------------------------------------------
-// per-thread error accumulators -> per-CTA partial tables (B+1 doubles each)
+// per-thread error accumulators -> per-CTA partial tables (B+1 doubles each):
+// a fixed butterfly per warp, then the warps' totals in warp order, so a
+// table does not depend on scheduling
 // ---------------------------------------------------------------------------
 template <int NACC, class A>
 __device__ void flush_errors(A (&acc)[NACC], int B, double* partial) {
-    __shared__ double red[NACC];
-    for (int k = threadIdx.x; k < NACC; k += blockDim.x) red[k] = 0;
-    __syncthreads();
+    __shared__ double red[8][NACC];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NACC; k++) {
-        A v = acc[k];
+        double v = (double)acc[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-        if ((threadIdx.x & 31) == 0 && k <= B) atomicAdd(&red[k], (double)v);
+        if (lane == 0) red[warp][k] = v;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k <= B; k += blockDim.x) partial[(size_t)blockIdx.x * (B + 1) + k] = red[k];
+    for (int k = threadIdx.x; k <= B && k < NACC; k += blockDim.x) {
+        double v = 0;
+        for (int w = 0; w < nw; w++) v += red[w][k];
+        partial[(size_t)blockIdx.x * (B + 1) + k] = v;
+    }
 }
 
 // NegaBinaryBPEncoder::collect_level_errors (NegaBinaryBPEncoder.hpp:231-239)
 // in shifted units: acc[B] += m^2, acc[B-k] += (nb2bin(nb & (2^k-1)) + m)^2,
 // acc[0] += shifted^2.
-template <int NACC>
-__device__ __forceinline__ void nb_errors(float (&acc)[NACC], uint32_t nb, float shifted, float m, int B) {
-    acc[B < NACC ? B : NACC - 1] += m * m;
-#pragma unroll
-    for (int k = 1; k < NACC - 1; k++) {
-        if (k < B) {
-            float d = (float)nb_to_bin(nb & ((1u << k) - 1u)) + m;
-            acc[B - k] += d * d;
-        }
-    }
-    acc[0] += shifted * shifted;
-}
 template <int NACC>
 __device__ __forceinline__ void nb_errors(double (&acc)[NACC], uint64_t nb, double shifted, double m, int B) {
     acc[B < NACC ? B : NACC - 1] += m * m;
@@ -80,20 +77,6 @@ __device__ __forceinline__ void nb_errors(double (&acc)[NACC], uint64_t nb, doub
     acc[0] += shifted * shifted;
 }
 // GroupedBPEncoder::collect_level_errors (GroupedBPEncoder.hpp:324-335), a = |shifted|
-template <int NACC>
-__device__ __forceinline__ void gr_errors(float (&acc)[NACC], float a, int B) {
-    uint32_t fp = (uint32_t)a;
-    float m = a - (float)fp;
-    acc[B < NACC ? B : NACC - 1] += m * m;
-#pragma unroll
-    for (int k = 1; k < NACC - 1; k++) {
-        if (k < B) {
-            float d = (float)(fp & ((1u << k) - 1u)) + m;
-            acc[B - k] += d * d;
-        }
-    }
-    acc[0] += a * a;
-}
 template <int NACC>
 __device__ __forceinline__ void gr_errors(double (&acc)[NACC], double a, int B) {
     uint64_t fp = (uint64_t)a;
@@ -109,85 +92,15 @@ __device__ __forceinline__ void gr_errors(double (&acc)[NACC], double a, int B) 
     acc[0] += a * a;
 }
 
-template <class T> struct Acc { using type = float; static constexpr int N = 33; };
+// per-lane accumulators of the fp64 tables and of the squared-error collector:
+// double whatever the data type (the reference sums in double)
+template <class T> struct Acc { using type = double; static constexpr int N = 33; };
 template <> struct Acc<double> { using type = double; static constexpr int N = 65; };
 
-// per-lane squared-error accumulators of the negabinary table, indexed by
-// the number k of dropped low digits: acc[0] = m^2 (all planes kept),
-// acc[k] = (value of digits 0..k-1 + m)^2, accx = shifted^2 (no plane kept)
-struct NbErr32 {
-    float acc[32];
-    float accx;
-    // table entry B-k <- acc[k]; entry B <- acc[0]; entry 0 <- accx
-    __device__ void flush(int B, double* partial) {
-        __shared__ double red[33];
-        for (int k = threadIdx.x; k < 33; k += blockDim.x) red[k] = 0;
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < 33; k++) {
-            float v = k < 32 ? acc[k] : accx;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-            if ((threadIdx.x & 31) == 0) {
-                int idx = k == 32 ? 0 : B - k;
-                if (k == 32 || k < B) atomicAdd(&red[idx], (double)v);
-            }
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k <= B; k += blockDim.x) partial[(size_t)blockIdx.x * (B + 1) + k] = red[k];
-    }
-};
-
-// grouped table (GroupedBPEncoder.hpp:324-335) on a = |shifted|: fp = (u32)a,
-// m = a - fp; acc[0] = m^2, acc[k] = ((fp & (2^k-1)) + m)^2, accx = a^2
-struct GrErr32 {
-    float acc[32];
-    float accx;
-    __device__ void zero() {
-#pragma unroll
-        for (int k = 0; k < 32; k++) acc[k] = 0.f;
-        accx = 0.f;
-    }
-    __device__ __forceinline__ void add(float a, int B) {
-        const uint32_t fp = (uint32_t)a;
-        const float m = a - (float)fp;
-        float d = m;
-        acc[0] += m * m;
-#pragma unroll
-        for (int k = 1; k < 32; k++) {
-            if (k < B) {
-                if ((fp >> (k - 1)) & 1u) d += (float)(1u << (k - 1));
-                acc[k] += d * d;
-            }
-        }
-        accx += a * a;
-    }
-    __device__ void flush(int B, double* partial) {
-        __shared__ double red[33];
-        for (int k = threadIdx.x; k < 33; k += blockDim.x) red[k] = 0;
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < 33; k++) {
-            float v = k < 32 ? acc[k] : accx;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-            if ((threadIdx.x & 31) == 0) {
-                int idx = k == 32 ? 0 : B - k;
-                if (k == 32 || k < B) atomicAdd(&red[idx], (double)v);
-            }
-        }
-        __syncthreads();
-        for (int k = threadIdx.x; k <= B; k += blockDim.x) partial[(size_t)blockIdx.x * (B + 1) + k] = red[k];
-    }
-};
-
-
-// fp32 negabinary encoder: grid-stride over NB_CHUNK-block chunks
-template <bool ERR>
+// fp32 negabinary encoder without tables: grid-stride over NB_CHUNK-block chunks
 __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x, uint64_t n,
                                                     const uint32_t* __restrict__ maxkey, int exp_arg, int B,
-                                                    uint32_t* __restrict__ out, uint64_t stride,
-                                                    double* __restrict__ partial) {
+                                                    uint32_t* __restrict__ out, uint64_t stride) {
     __shared__ uint32_t tile[32 * NB_TILE_LD];
     const int exp = (maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg) + 2;   // NegaBinaryBPEncoder.hpp:21
     const uint64_t nblocks = (n + 31) / 32;
@@ -195,46 +108,15 @@ __global__ void __launch_bounds__(256) k_nb_encode32(const float* __restrict__ x
     const int se = B - exp;
     const bool fast = pow2_normal(se);
     const float scale = fast ? pow2f(se) : 1.f;
-    float acc[32], accx = 0.f;
-#pragma unroll
-    for (int k = 0; k < 32; k++) acc[k] = 0.f;
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x)
-        nb_encode32_chunk<ERR>(x, n, nblocks, B, se, fast, scale, out, stride, c, tile, acc, accx);
-    if (ERR) {
-        NbErr32 er;
-#pragma unroll
-        for (int k = 0; k < 32; k++) er.acc[k] = acc[k];
-        er.accx = accx;
-        er.flush(B, partial);
-    }
+        nb_encode32_chunk(x, n, nblocks, B, se, fast, scale, out, stride, c, tile);
 }
 
-// Every level of one fp32 field in one launch: segments are the levels in
-// chunk order, a CTA walks its chunks in increasing order and flushes its
-// error accumulators whenever the level changes. The per-level partial tables
-// sit at partial + level * gridDim.x * (B + 1); a CTA writes zero rows for the
-// levels it never visits, so every row the reduction reads is written.
-template <bool ERR>
+// Every level of one fp32 field in one launch, without tables: segments are
+// the levels in chunk order.
 __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* __restrict__ segs, int nseg,
-                                                           uint64_t total, int B, double* __restrict__ partial) {
+                                                               uint64_t total, int B) {
     __shared__ uint32_t tile[32 * NB_TILE_LD];
-    float acc[32], accx = 0.f;
-#pragma unroll
-    for (int k = 0; k < 32; k++) acc[k] = 0.f;
-    const size_t rows_per_level = (size_t)gridDim.x * (B + 1);
-    auto zero_rows = [&](int s0, int s1) {   // levels [s0, s1)
-        for (int s = s0; s < s1; s++)
-            for (int k = threadIdx.x; k <= B; k += blockDim.x)
-                partial[s * rows_per_level + (size_t)blockIdx.x * (B + 1) + k] = 0.0;
-    };
-    auto flush = [&](int s) {
-        NbErr32 er;
-#pragma unroll
-        for (int k = 0; k < 32; k++) { er.acc[k] = acc[k]; acc[k] = 0.f; }
-        er.accx = accx;
-        accx = 0.f;
-        er.flush(B, partial + s * rows_per_level);
-    };
     int cur = -1, se = 0;
     bool fast = true;
     float scale = 1.f;
@@ -242,26 +124,211 @@ __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* _
         const int s = find_seg(segs, nseg, c, &ChunkSeg::chunk_begin);
         const ChunkSeg& q = segs[s];
         if (s != cur) {
-            if (ERR) {
-                if (cur >= 0) flush(cur);
-                zero_rows(cur + 1, s);
-            }
             cur = s;
             se = B - (frexp_exp(__uint_as_float(*q.key)) + 2);     // NegaBinaryBPEncoder.hpp:21
             fast = pow2_normal(se);
             scale = fast ? pow2f(se) : 1.f;
         }
         if (B == 32)
-            nb_encode32_chunk<ERR, true>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin,
-                                         tile, acc, accx);
+            nb_encode32_chunk<true>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin, tile);
         else
-            nb_encode32_chunk<ERR>(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin, tile,
-                                   acc, accx);
+            nb_encode32_chunk(q.x, q.n, q.nblocks, B, se, fast, scale, q.words, q.stride, c - q.chunk_begin, tile);
     }
-    if (ERR) {
-        if (cur >= 0) flush(cur);
-        zero_rows(cur + 1, nseg);
+}
+
+// ---------------------------------------------------------------------------
+// fp32 negabinary encoder with exact squared-error tables (errtab.cuh):
+// NegaBinaryBPEncoder.hpp:65-125. Each lane takes four values per step (one
+// from each of four consecutive blocks): their scaled values, negabinary
+// digits and t = nb ^ 0xAAAAAAAA; the byte products of t go to the lane's
+// exact sums, values below 2^23 to the warp's queue, and the four digit words
+// are transposed into the plane tile (whose popcounts give the bit counts).
+// ---------------------------------------------------------------------------
+constexpr int kErrTileBytes = 32 * NB_TILE_LD * 4;
+constexpr size_t kErrSmemNB = (size_t)((kErrTileBytes + 15) / 16 * 16) + 8 * sizeof(errtab::WarpQ) +
+                              errtab::kSlotsPad * sizeof(unsigned long long);
+// chunks a CTA encodes between two flushes of its 32-bit lane sums (each
+// chunk adds at most 8 * 260100 to a lane sum)
+constexpr int kErrFlushChunks = 2048;
+
+template <bool FULLB>
+__device__ __forceinline__ void nb_encode32_chunk_err(const float* __restrict__ x, uint64_t n, uint64_t nblocks, int B,
+                                                      int se, bool fast, float scale, uint32_t* __restrict__ out,
+                                                      uint64_t stride, uint64_t c, uint32_t* tile, errtab::Lane& acc,
+                                                      errtab::WarpQ& wq, uint32_t& head, int& qn) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
+    const uint64_t cb0 = c * NB_CHUNK;
+    const uint64_t wb0 = cb0 + (uint64_t)warp * 32;
+#pragma unroll 1
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+        float sh[4];
+        bool ok[4];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const uint64_t i = (wb0 + j0 + g) * 32 + lane;
+            ok[g] = i < n;
+            const float v = ok[g] ? __ldcs(x + i) : 0.f;
+            sh[g] = fast ? v * scale : ldexpf(v, se);            // NegaBinaryBPEncoder.hpp:42
+        }
+        uint32_t t[4], nb[4];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const uint32_t tq = (uint32_t)(int32_t)sh[g] + 0xaaaaaaaau;   // :43-44; nb = t ^ 0xAAAAAAAA
+            nb[g] = tq ^ 0xaaaaaaaau;
+            t[g] = ok[g] ? tq : 0u;                                        // padding adds nothing
+            const bool big = fabsf(sh[g]) >= 8388608.f;
+            if (ok[g] && big) acc.add_big_square(sh[g]);
+            const bool small = ok[g] && !big;
+            const uint32_t bal = __ballot_sync(FULL, small);
+            if (bal) errtab::enqueue(wq, head, qn, bal, small, sh[g], lane);
+        }
+        errtab::drain_full<true>(wq, head, qn, lane);
+        acc.add4(t[0], t[1], t[2], t[3]);
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const uint32_t w = transpose32(nb[g], lane);
+            acc.pc += __popc(w);
+            if (FULLB || lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
+        }
     }
+    __syncthreads();
+    const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
+    for (int p = warp; p < B; p += 8) {
+        uint32_t* dst = out + (uint64_t)p * stride + cb0;
+        const uint32_t* row = tile + p * NB_TILE_LD;
+        for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
+    }
+    __syncthreads();
+}
+
+// Every level (segment) of one fp32 field with tables in one launch. Records
+// (errtab::kSlotsPad u64 each) sit at recs + (level * gridDim.x + CTA); a CTA
+// zeroes the record of every level it enters or skips and adds its sums at
+// each level change, so every record the final reduction reads is written.
+__global__ void __launch_bounds__(256, 2) k_nb_encode32_err(const ChunkSeg* __restrict__ segs, ChunkSeg one,
+                                                            int nseg, uint64_t total, int B, int exp_arg,
+                                                            unsigned long long* __restrict__ recs) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* tile = (uint32_t*)smem;
+    errtab::WarpQ* wq = (errtab::WarpQ*)(smem + (kErrTileBytes + 15) / 16 * 16);
+    unsigned long long* red = (unsigned long long*)(wq + 8);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    errtab::Lane acc;
+    acc.zero();
+    errtab::zero_q(wq[warp], lane);
+    uint32_t head = 0;
+    int qn = 0;
+    auto rec_of = [&](int s) { return recs + ((size_t)s * gridDim.x + blockIdx.x) * errtab::kSlotsPad; };
+    auto zero_recs = [&](int s0, int s1) {   // levels [s0, s1)
+        for (int s = s0; s < s1; s++)
+            for (int k = threadIdx.x; k < errtab::kSlotsPad; k += blockDim.x) rec_of(s)[k] = 0;
+        __syncthreads();
+    };
+    auto flush = [&](int s) {
+        if (qn) {   // the queue's last partial batch
+            __syncwarp();
+            errtab::run_batch<true>(wq[warp], head, qn, lane);
+            head += qn;
+            qn = 0;
+        }
+        errtab::flush(acc, wq, red, rec_of(s));
+    };
+    int cur = -1, se = 0, since = 0;
+    bool fast = true;
+    float scale = 1.f;
+    const float* qx = one.x;
+    uint32_t* qw = one.words;
+    uint64_t qnv = one.n, qnb = one.nblocks, qst = one.stride, qc0 = 0;
+    // one flush site: at a level change, every kErrFlushChunks chunks, and at the end
+    for (uint64_t c = blockIdx.x;; c += gridDim.x) {
+        const bool done = c >= total;
+        const int s = done ? nseg : (segs ? find_seg(segs, nseg, c, &ChunkSeg::chunk_begin) : 0);
+        if (cur >= 0 && (s != cur || since == kErrFlushChunks)) {
+            flush(cur);
+            since = 0;
+        }
+        if (s != cur) {
+            zero_recs(cur + 1, s < nseg ? s + 1 : nseg);
+            if (done) break;
+            cur = s;
+            const uint32_t* key = one.key;
+            if (segs) {
+                qx = segs[s].x;
+                qw = segs[s].words;
+                qnv = segs[s].n;
+                qnb = segs[s].nblocks;
+                qst = segs[s].stride;
+                qc0 = segs[s].chunk_begin;
+                key = segs[s].key;
+            }
+            se = B - ((key ? frexp_exp(__uint_as_float(*key)) : exp_arg) + 2);   // NegaBinaryBPEncoder.hpp:21
+            fast = pow2_normal(se);
+            scale = fast ? pow2f(se) : 1.f;
+        }
+        since++;
+        if (B == 32)
+            nb_encode32_chunk_err<true>(qx, qnv, qnb, B, se, fast, scale, qw, qst, c - qc0, tile, acc, wq[warp], head,
+                                        qn);
+        else
+            nb_encode32_chunk_err<false>(qx, qnv, qnb, B, se, fast, scale, qw, qst, c - qc0, tile, acc, wq[warp], head,
+                                         qn);
+    }
+}
+
+// Tables of every level from the CTA records: one CTA per level; warp w sums
+// record slots w, w + 8, ... (lane-strided over records, then a fixed
+// butterfly, so the doubles are summed in a fixed order), then thread i
+// computes entry i. keys (or exp_arg when keys is null) give the level
+// exponent, exp_add the encoder's offset (2 for negabinary).
+template <bool NB>
+__global__ void __launch_bounds__(256) k_errtab_final(const unsigned long long* __restrict__ recs, int nrec, int B,
+                                                      const ChunkSeg* __restrict__ segs, ChunkSeg one, int exp_arg,
+                                                      int exp_add, double* __restrict__ out) {
+    __shared__ unsigned long long R[errtab::kSlotsPad];
+    const int l = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned long long* rl = recs + (size_t)l * nrec * errtab::kSlotsPad;
+    for (int i = warp; i < errtab::WORDS; i += nw) {
+        const bool pair = i >= errtab::S6A && i < errtab::S5;              // 128-bit sums
+        if (pair && ((i - errtab::S6A) & 1)) continue;                    // high words go with their low word
+        const bool dbl = i >= errtab::S5;
+        if (dbl) {
+            double v = 0;
+            for (int r = lane; r < nrec; r += 32) v += __longlong_as_double(rl[(size_t)r * errtab::kSlotsPad + i]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if (lane == 0) R[i] = __double_as_longlong(v);
+        } else if (pair) {
+            unsigned long long lo = 0, hi = 0;
+            for (int r = lane; r < nrec; r += 32) {
+                const unsigned long long* p = rl + (size_t)r * errtab::kSlotsPad + i;
+                const unsigned long long o = lo;
+                lo += p[0];
+                hi += p[1] + (lo < o ? 1 : 0);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long l2 = __shfl_xor_sync(FULL, lo, o), h2 = __shfl_xor_sync(FULL, hi, o);
+                const unsigned long long ol = lo;
+                lo += l2;
+                hi += h2 + (lo < ol ? 1 : 0);
+            }
+            if (lane == 0) { R[i] = lo; R[i + 1] = hi; }
+        } else {
+            unsigned long long v = 0;
+            for (int r = lane; r < nrec; r += 32) v += rl[(size_t)r * errtab::kSlotsPad + i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if (lane == 0) R[i] = v;
+        }
+    }
+    __syncthreads();
+    const uint32_t* key = segs ? segs[l].key : one.key;
+    const uint64_t n = segs ? segs[l].n : one.n;
+    const int e = (key ? frexp_exp(__uint_as_float(*key)) : exp_arg) + exp_add;
+    for (int i = threadIdx.x; i <= B; i += blockDim.x)
+        out[(size_t)l * (B + 1) + i] = errtab::table_entry<NB>(R, n, B, e, i);
 }
 
 // Every level of one fp32 field decoded in one launch (segments = levels in
@@ -345,27 +412,6 @@ __global__ void __launch_bounds__(256) k_nb_decode_levels(const ChunkSeg* __rest
         }
     }
     cp_async_wait_all();
-}
-
-// per-level tables from the partial rows of k_nb_encode32_levels, scaled to
-// value units (NegaBinaryBPEncoder.hpp:121-123); one warp per table entry
-__global__ void k_reduce_partials_levels(const double* __restrict__ partial, int nparts, int B, int nl,
-                                         const uint32_t* __restrict__ keys, double* __restrict__ out) {
-    const int lane = threadIdx.x & 31;
-    const int entries = nl * (B + 1);
-    for (int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); e < entries;
-         e += gridDim.x * (blockDim.x >> 5)) {
-        const int l = e / (B + 1), k = e - l * (B + 1);
-        const double* rows = partial + (size_t)l * nparts * (B + 1);
-        double s = 0;
-        for (int p = lane; p < nparts; p += 32) s += rows[(size_t)p * (B + 1) + k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-        if (lane == 0) {
-            const int exp = frexp_exp(__uint_as_float(keys[l])) + 2;
-            out[e] = ldexp(s, 2 * (-B + exp));
-        }
-    }
 }
 
 // fp32 negabinary decoder, planes [s, s+num) at base[i * stride]
@@ -676,12 +722,20 @@ __global__ void __launch_bounds__(256) k_gr_write(const T* __restrict__ x, uint6
     }
 }
 
-// fp32 grouped writer: one transpose per block instead of B ballots
+// fp32 grouped writer: one transpose per block instead of B ballots. With
+// ERR, the exact squared-error tables (errtab.cuh, GroupedBPEncoder.hpp:76-145
+// with collect_level_errors :324-335) of the CTA's chunk go to its record
+// recs + blockIdx.x: four blocks per step, t = trunc(|x|), bit counts from the
+// transposed magnitude words.
+constexpr size_t kErrSmemGR = 8 * sizeof(errtab::WarpQ) + errtab::kSlotsPad * sizeof(unsigned long long);
+
+template <bool ERR>
 __global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x, uint64_t n,
                                                    const uint32_t* __restrict__ maxkey, int exp_arg, int B,
                                                    const uint8_t* __restrict__ rbs,
                                                    const uint32_t* __restrict__ chunk_off, uint32_t* __restrict__ out,
-                                                   uint64_t cap) {
+                                                   uint64_t cap, unsigned long long* __restrict__ recs) {
+    extern __shared__ __align__(16) unsigned char smem[];
     const int exp = maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t nblocks = (n + 31) / 32;
@@ -692,24 +746,66 @@ __global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x,
     const bool fast = pow2_normal(B - exp);
     const float sc = fast ? pow2f(B - exp) : 1.f;
     const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
-    for (int j = 0; j < GR_BPW; j++) {
-        const uint64_t b = b0 + j;
-        if (b >= nblocks) break;
-        const uint64_t i = b * 32 + lane;
-        float v = i < n ? __ldcs(x + i) : 0.f;
-        const float sh = scale2(v, B - exp, fast, sc);
-        const int64_t fix = (int64_t)sh;
-        const bool neg = v < 0.f;
-        const uint32_t q = (uint32_t)(neg ? -fix : fix);
-        const uint32_t sign = __ballot_sync(FULL, neg);
-        const uint32_t w = transpose32(q, lane);
-        const int r = rbs[b];
-        if (lane < B && plane >= r) {
-            uint32_t* dst = out + (uint64_t)plane * cap + off;
-            if (plane == r) { dst[0] = sign; dst[1] = w; }
-            else dst[0] = w;
+    errtab::WarpQ* wq = (errtab::WarpQ*)smem;
+    unsigned long long* red = (unsigned long long*)(wq + 8);
+    errtab::Lane acc;
+    uint32_t head = 0;
+    int qn = 0;
+    if (ERR) {
+        acc.zero();
+        errtab::zero_q(wq[warp], lane);
+    }
+    for (int j0 = 0; j0 < GR_BPW; j0 += 4) {
+        float sh[4];
+        uint32_t q[4], sign[4];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const uint64_t i = (b0 + j0 + g) * 32 + lane;
+            const bool ok = i < n;
+            const float v = ok ? __ldcs(x + i) : 0.f;
+            sh[g] = scale2(v, B - exp, fast, sc);
+            const int64_t fix = (int64_t)sh[g];
+            const bool neg = v < 0.f;
+            q[g] = (uint32_t)(neg ? -fix : fix);
+            sign[g] = __ballot_sync(FULL, neg);
+            if (ERR) {
+                const float a = fabsf(sh[g]);
+                const bool big = a >= 8388608.f;
+                if (ok && big) acc.add_big_square(a);
+                const bool small = ok && !big;
+                const uint32_t bal = __ballot_sync(FULL, small);
+                if (bal) errtab::enqueue(wq[warp], head, qn, bal, small, a, lane);
+            }
         }
-        off += gr_words(r, plane);
+        if (ERR) {
+            errtab::drain_full<false>(wq[warp], head, qn, lane);
+            acc.add4(q[0], q[1], q[2], q[3]);
+        }
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const uint64_t b = b0 + j0 + g;
+            const uint32_t w = transpose32(q[g], lane);
+            if (ERR) acc.pc += __popc(w);
+            if (b < nblocks) {
+                const int r = rbs[b];
+                if (lane < B && plane >= r) {
+                    uint32_t* dst = out + (uint64_t)plane * cap + off;
+                    if (plane == r) { dst[0] = sign[g]; dst[1] = w; }
+                    else dst[0] = w;
+                }
+                off += gr_words(r, plane);
+            }
+        }
+    }
+    if (ERR) {
+        if (qn) {
+            __syncwarp();
+            errtab::run_batch<false>(wq[warp], head, qn, lane);
+        }
+        unsigned long long* rec = recs + (size_t)blockIdx.x * errtab::kSlotsPad;
+        for (int k = threadIdx.x; k < errtab::kSlotsPad; k += blockDim.x) rec[k] = 0;
+        __syncthreads();
+        errtab::flush(acc, wq, red, rec);
     }
 }
 
@@ -759,12 +855,10 @@ __global__ void __launch_bounds__(256) k_gr_decode32(const uint32_t* const* __re
     }
 }
 
-// fp32 grouped pass 1 with register error accumulators
-template <bool ERR>
+// fp32 grouped pass 1: each block's recording bitplane and the chunk's word counts
 __global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, uint64_t n,
                                                 const uint32_t* __restrict__ maxkey, int exp_arg, int B,
-                                                uint8_t* __restrict__ rbs, uint32_t* __restrict__ chunk_words,
-                                                double* __restrict__ partial) {
+                                                uint8_t* __restrict__ rbs, uint32_t* __restrict__ chunk_words) {
     const int exp = maxkey ? frexp_exp(__uint_as_float(*maxkey)) : exp_arg;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t nblocks = (n + 31) / 32;
@@ -772,8 +866,6 @@ __global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, ui
     uint32_t c0 = 0;
     const bool fast = pow2_normal(B - exp);
     const float sc = fast ? pow2f(B - exp) : 1.f;
-    GrErr32 er;
-    if (ERR) er.zero();
     const uint64_t b0 = (uint64_t)blockIdx.x * GR_CHUNK + (uint64_t)warp * GR_BPW;
     for (int j = 0; j < GR_BPW; j++) {
         const uint64_t b = b0 + j;
@@ -784,7 +876,6 @@ __global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, ui
             const float sh = scale2(__ldg(x + i), B - exp, fast, sc);
             const int64_t fix = (int64_t)sh;
             q = (uint32_t)(fix < 0 ? -fix : fix);
-            if (ERR) er.add(fabsf(sh), B);
         }
         const uint32_t o = __reduce_or_sync(FULL, q);
         const int r = o ? B - 1 - (31 - __clz(o)) : B;
@@ -798,7 +889,6 @@ __global__ void __launch_bounds__(256) k_gr_rb32(const float* __restrict__ x, ui
         for (int w = 0; w < GR_WARPS; w++) t += cnt[w][threadIdx.x];
         chunk_words[(uint64_t)blockIdx.x * B + threadIdx.x] = t;
     }
-    if (ERR) er.flush(B, partial);
 }
 
 // GroupedBPEncoder::progressive_decode -- :210-297 (planes [s, e)); plane p's
@@ -985,9 +1075,39 @@ __global__ void k_chunk_words_from_rb(const uint8_t* __restrict__ rbs, uint64_t 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-int encode_partial_slots(uint64_t n, int elem_bytes) {
-    (void)n; (void)elem_bytes;
-    return kSMs * 4;
+// opt-in to more than 48 KB of dynamic shared memory, once per device and kernel
+static int allow_smem(const void* k, size_t bytes) {
+    static std::mutex mu;
+    static std::vector<std::pair<int, const void*>> done;
+    int dev = 0;
+    PRODM_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto& d : done)
+        if (d.first == dev && d.second == k) return PRODM_OK;
+    PRODM_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    done.push_back({dev, k});
+    return PRODM_OK;
+}
+
+// the opt-in comes first: the occupancy query counts it
+static unsigned nb_err_grid(uint64_t need) {
+    (void)allow_smem((const void*)k_nb_encode32_err, kErrSmemNB);
+    return persistent_grid_for((const void*)k_nb_encode32_err, 256, kErrSmemNB, need, kPartialSlots);
+}
+
+// fp32 negabinary with tables: the encode launch (records in partial), then
+// the final reduction of nseg levels into errs_out
+static int nb_err_launch(const ChunkSeg* segs, const ChunkSeg& one, int nseg, uint64_t total, int B, int exp,
+                         double* partial, double* errs_out, cudaStream_t st) {
+    int rc;
+    if ((rc = allow_smem((const void*)k_nb_encode32_err, kErrSmemNB))) return rc;
+    const unsigned grid = nb_err_grid(segs ? (uint64_t)kPartialSlots : total);
+    unsigned long long* recs = (unsigned long long*)partial;
+    k_nb_encode32_err<<<grid, 256, kErrSmemNB, st>>>(segs, one, nseg, total, B, exp, recs);
+    PRODM_CHECK_LAUNCH("k_nb_encode32_err");
+    k_errtab_final<true><<<nseg, 256, 0, st>>>(recs, (int)grid, B, segs, one, exp, 2, errs_out);
+    PRODM_CHECK_LAUNCH("k_errtab_final");
+    return PRODM_OK;
 }
 
 template <class T>
@@ -999,19 +1119,19 @@ int launch_nb_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     const int th = 256;
     if (std::is_same<T, float>::value) {
         const uint64_t nch = (nblocks + NB_CHUNK - 1) / NB_CHUNK;
-        const unsigned grid = errs_out ? persistent_grid_for((const void*)k_nb_encode32<true>, th, 0, nch, kPartialSlots)
-                                       : persistent_grid_for((const void*)k_nb_encode32<false>, th, 0, nch, nch);
-        if (errs_out)
-            k_nb_encode32<true><<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
-                                                     (uint32_t*)out, stride, partial);
-        else
-            k_nb_encode32<false><<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
-                                                      (uint32_t*)out, stride, nullptr);
-        PRODM_CHECK_LAUNCH("k_nb_encode32");
         if (errs_out) {
-            k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)grid, B, (const K*)maxkey, exp, 2, 1, errs_out);
-            PRODM_CHECK_LAUNCH("k_reduce_partials");
+            ChunkSeg one = {};
+            one.x = (const float*)x;
+            one.words = (uint32_t*)out;
+            one.n = n;
+            one.nblocks = nblocks;
+            one.stride = stride;
+            one.key = (const uint32_t*)maxkey;
+            return nb_err_launch(nullptr, one, 1, nch, B, exp, partial, errs_out, st);
         }
+        const unsigned grid = persistent_grid_for((const void*)k_nb_encode32, th, 0, nch, nch);
+        k_nb_encode32<<<grid, th, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B, (uint32_t*)out, stride);
+        PRODM_CHECK_LAUNCH("k_nb_encode32");
         return PRODM_OK;
     }
     const unsigned grid = errs_out ? persistent_grid_for((const void*)k_nb_encode<T, true>, th, 0, nblocks, kPartialSlots)
@@ -1039,23 +1159,17 @@ int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunk
 }
 
 int nb_encode_levels_grid(int with_errors) {
-    const void* k = with_errors ? (const void*)k_nb_encode32_levels<true> : (const void*)k_nb_encode32_levels<false>;
-    return (int)persistent_grid_for(k, 256, 0, (uint64_t)kPartialSlots, kPartialSlots);
+    if (with_errors) return (int)nb_err_grid((uint64_t)kPartialSlots);
+    return (int)persistent_grid_for((const void*)k_nb_encode32_levels, 256, 0, (uint64_t)kPartialSlots, kPartialSlots);
 }
 
 int launch_nb_encode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, int B, double* partial,
                             const uint32_t* keys, double* errs_out, cudaStream_t st) {
-    const unsigned grid = (unsigned)nb_encode_levels_grid(errs_out != nullptr);
-    if (errs_out) {
-        k_nb_encode32_levels<true><<<grid, 256, 0, st>>>(segs, nseg, total_chunks, B, partial);
-        PRODM_CHECK_LAUNCH("k_nb_encode32_levels");
-        const int warps = nseg * (B + 1);
-        k_reduce_partials_levels<<<(warps + 7) / 8, 256, 0, st>>>(partial, (int)grid, B, nseg, keys, errs_out);
-        PRODM_CHECK_LAUNCH("k_reduce_partials_levels");
-    } else {
-        k_nb_encode32_levels<false><<<grid, 256, 0, st>>>(segs, nseg, total_chunks, B, nullptr);
-        PRODM_CHECK_LAUNCH("k_nb_encode32_levels");
-    }
+    (void)keys;   // each segment carries its level's key
+    if (errs_out) return nb_err_launch(segs, ChunkSeg{}, nseg, total_chunks, B, 0, partial, errs_out, st);
+    const unsigned grid = (unsigned)nb_encode_levels_grid(0);
+    k_nb_encode32_levels<<<grid, 256, 0, st>>>(segs, nseg, total_chunks, B);
+    PRODM_CHECK_LAUNCH("k_nb_encode32_levels");
     return PRODM_OK;
 }
 
@@ -1091,22 +1205,26 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
     const uint64_t nblocks = (n + BS - 1) / BS;
     const uint64_t nch = gr_nchunks(nblocks);
     if (std::is_same<T, float>::value) {
-        if (errs_out)
-            k_gr_rb32<true><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B,
-                                                                     rbs, chunk_words, partial);
-        else
-            k_gr_rb32<false><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp,
-                                                                      B, rbs, chunk_words, nullptr);
+        k_gr_rb32<<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B, rbs,
+                                                          chunk_words);
         PRODM_CHECK_LAUNCH("k_gr_rb32");
-        if (errs_out) {
-            k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
-            PRODM_CHECK_LAUNCH("k_reduce_partials");
-        }
         k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, 4, chunk_off, sizes);
         PRODM_CHECK_LAUNCH("k_gr_scan");
-        k_gr_write32<<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B, rbs,
-                                                             chunk_off, (uint32_t*)out, cap);
-        PRODM_CHECK_LAUNCH("k_gr_write32");
+        unsigned long long* recs = (unsigned long long*)partial;
+        if (errs_out) {
+            k_gr_write32<true><<<(unsigned)nch, GR_WARPS * 32, kErrSmemGR, st>>>(
+                (const float*)x, n, (const uint32_t*)maxkey, exp, B, rbs, chunk_off, (uint32_t*)out, cap, recs);
+            PRODM_CHECK_LAUNCH("k_gr_write32");
+            ChunkSeg one = {};
+            one.n = n;
+            one.key = (const uint32_t*)maxkey;
+            k_errtab_final<false><<<1, 256, 0, st>>>(recs, (int)nch, B, nullptr, one, exp, 0, errs_out);
+            PRODM_CHECK_LAUNCH("k_errtab_final");
+        } else {
+            k_gr_write32<false><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(
+                (const float*)x, n, (const uint32_t*)maxkey, exp, B, rbs, chunk_off, (uint32_t*)out, cap, nullptr);
+            PRODM_CHECK_LAUNCH("k_gr_write32");
+        }
         return PRODM_OK;
     }
     if (errs_out) {

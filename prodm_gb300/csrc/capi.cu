@@ -296,7 +296,7 @@ void encode_reserve(Workspace& ws, int enc, int dtype, uint64_t n, int B) {
     uint64_t nb = nblocks_of(dtype, n);
     uint64_t nch = gr_nchunks(nb);
     uint64_t parts = nch > (uint64_t)kPartialSlots ? nch : (uint64_t)kPartialSlots;
-    ws.reserve(parts * (B + 1) * sizeof(double));
+    ws.reserve(partial_bytes(parts, B));
     if (enc == PRODM_ENC_PERBIT) {
         ws.reserve((uint64_t)(B + 1) * pb_row_words(n) * 4);   // magnitude + sign rows
         ws.reserve(64 * 4);                                    // first-one counts
@@ -325,7 +325,7 @@ int encode_impl(int enc, const T* x, uint64_t n, int exp, int B, uint8_t* blob, 
     Workspace ws(wsp, wsb, st);
     encode_reserve(ws, enc, dtype, n, B);
     if ((rc = ws.commit())) return rc;
-    double* partial = (double*)ws.take(parts * (B + 1) * sizeof(double));
+    double* partial = (double*)ws.take(partial_bytes(parts, B));
     if (enc == PRODM_ENC_PERBIT) {
         if ((uintptr_t)blob % 8) return fail(PRODM_EINVAL, "encode: the per-bit blob must be 8-byte aligned");
         const uint64_t rw = pb_row_words(n);
@@ -794,7 +794,7 @@ int mdr_alloc_all(prodm_mdr* h) {
     if ((rc = h->alloc((void**)&h->sqerr, (L + 1) * (B + 1) * 8))) return rc;
     if ((rc = h->alloc((void**)&h->maxerr, (L + 1) * (B + 1) * 8))) return rc;
     uint64_t parts = maxch > (uint64_t)kPartialSlots ? maxch : (uint64_t)kPartialSlots;
-    if ((rc = h->alloc((void**)&h->partial, parts * (B + 1) * 8))) return rc;
+    if ((rc = h->alloc((void**)&h->partial, partial_bytes(parts, B)))) return rc;
     if ((rc = h->alloc((void**)&h->index, L + 1 + 15))) return rc;
     if ((rc = h->alloc((void**)&h->rsz, (L + 1) * 4))) return rc;
     if ((rc = h->alloc((void**)&h->kstatus, 16))) return rc;
@@ -869,7 +869,7 @@ int mdr_alloc_all(prodm_mdr* h) {
         h->eseg_chunks = chunks;
         if (h->sq) {
             const size_t rows = (size_t)(L + 1) * nb_encode_levels_grid(1);
-            if ((rc = h->alloc((void**)&h->lpartial, rows * (B + 1) * sizeof(double)))) return rc;
+            if ((rc = h->alloc((void**)&h->lpartial, rows * kErrRecWords * 8))) return rc;
         }
     }
     return PRODM_OK;

@@ -63,6 +63,12 @@ int launch_sq_collect(const T* x, uint64_t n, int B, T maxv, double* partial, do
 template <class T>
 int launch_max_collect(const T* bounds, int nl, int B, double* out, cudaStream_t st);
 constexpr int kPartialSlots = kSMs * 4;   // per-CTA partial error tables of the fused collectors
+// bytes of `parts` per-CTA partials: B + 1 doubles (fp64 tables, squared-error
+// collector) or one record of the exact fp32 tables (errtab.cuh)
+constexpr int kErrRecWords = 196;   // errtab::kSlotsPad
+inline uint64_t partial_bytes(uint64_t parts, int B) {
+    return parts * (uint64_t)(kErrRecWords > B + 1 ? kErrRecWords : B + 1) * 8;
+}
 
 // interpret.cu
 template <class T>
@@ -88,7 +94,7 @@ constexpr int kDecodeChunkBlocks = 128;
 int launch_nb_decode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, cudaStream_t st, bool pdl = false);
 // bitplane.cu: every level of one fp32 field in one encode launch; with
 // errs_out, per-level squared-error tables (partial: nseg * nb_encode_levels_grid(1)
-// * (B + 1) doubles)
+// records of kErrRecWords words)
 int nb_encode_levels_grid(int with_errors);
 int launch_nb_encode_levels(const ChunkSeg* segs, int nseg, uint64_t total_chunks, int B, double* partial,
                             const uint32_t* keys, double* errs_out, cudaStream_t st);

@@ -93,15 +93,13 @@ constexpr int NB_TILE_LD = NB_CHUNK + 1;   // padded tile row: conflict-free col
 
 // Encode chunk c (NB_CHUNK consecutive 32-value blocks) of a level: each warp
 // transposes 32 blocks into the shared [plane][block] tile, then the CTA
-// writes every plane's words of the chunk as one contiguous run.
-// Errors (ERR): negabinary truncation tables, NegaBinaryBPEncoder.hpp:231-239,
-// in per-lane accumulators indexed by dropped digits (acc[0] = m^2).
+// writes every plane's words of the chunk as one contiguous run
+// (NegaBinaryBPEncoder.hpp:18-62). The error-table variant is in bitplane.cu.
 // FULLB: B == 32, so every digit has a plane and no per-digit guard is needed
-template <bool ERR, bool FULLB = false>
+template <bool FULLB = false>
 __device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, uint64_t n, uint64_t nblocks, int B,
                                                   int se, bool fast, float scale, uint32_t* __restrict__ out,
-                                                  uint64_t stride, uint64_t c, uint32_t* tile, float (&acc)[32],
-                                                  float& accx) {
+                                                  uint64_t stride, uint64_t c, uint32_t* tile) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
     const uint64_t cb0 = c * NB_CHUNK;
@@ -114,43 +112,12 @@ __device__ __forceinline__ void nb_encode32_chunk(const float* __restrict__ x, u
             const uint64_t i = (wb0 + j0 + g) * 32 + lane;
             v[g] = i < n ? __ldcs(x + i) : 0.f;
         }
-        uint32_t nb[NB_G];
-        float sh[NB_G], d[NB_G];
-        // NegaBinaryBPEncoder.hpp:42; the scaling is chosen once per chunk
-        // (an exact multiplication whenever 2^se is a normal float)
-        if (fast) {
-#pragma unroll
-            for (int g = 0; g < NB_G; g++) sh[g] = v[g] * scale;
-        } else {
-#pragma unroll
-            for (int g = 0; g < NB_G; g++) sh[g] = ldexpf(v[g], se);
-        }
 #pragma unroll
         for (int g = 0; g < NB_G; g++) {
-            const int32_t q = (int32_t)sh[g];
-            nb[g] = nb_from_bin(q);
-            d[g] = sh[g] - (float)q;                             // exact fraction
-        }
-        if (ERR) {
-#pragma unroll
-            for (int g = 0; g < NB_G; g++) {
-                acc[0] += d[g] * d[g];
-                accx += sh[g] * sh[g];
-            }
-#pragma unroll
-            for (int k = 1; k < 32; k++) {
-                if (FULLB || k < B) {
-#pragma unroll
-                    for (int g = 0; g < NB_G; g++) {
-                        if ((nb[g] >> (k - 1)) & 1u) d[g] += nbw(k - 1);
-                        acc[k] += d[g] * d[g];
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int g = 0; g < NB_G; g++) {
-            const uint32_t w = transpose32(nb[g], lane);
+            // NegaBinaryBPEncoder.hpp:42; the scaling is chosen once per chunk
+            // (an exact multiplication whenever 2^se is a normal float)
+            const float sh = fast ? v[g] * scale : ldexpf(v[g], se);
+            const uint32_t w = transpose32(nb_from_bin((int32_t)sh), lane);
             if (FULLB || lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
         }
     }

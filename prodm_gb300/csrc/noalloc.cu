@@ -13,10 +13,13 @@
 // 316,160 bytes, enough for the largest table (64 bitplanes, fp64). Larger
 // num_bitplanes are rejected with PRODM_EINVAL.
 //
-// Set-up: the first call on a device (the device current on the calling
-// thread) looks up the array's device address with cudaGetSymbolAddress and
-// caches it for that device; that first call should come before any stream
-// capture on the device. Later calls do no set-up.
+// Set-up: a call on a stream that is not capturing looks up the array's
+// device address (cudaGetSymbolAddress, with the calling thread's current
+// device) and remembers it for that device; a call on a capturing stream uses
+// the remembered address, so the first call on a device should come before
+// any stream capture. Looking the address up again on every uncaptured call
+// keeps it right after cudaDeviceReset or a switch of the device's context,
+// where the module and its array are loaded anew.
 //
 // Sharing: every call on every stream of a device uses the same array, which
 // keeps the last call's contents. Each call writes every partial entry that it
@@ -45,19 +48,26 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 double* g_scratch_ptr[kMaxDevices] = {};
 
-// the scratch address on the current device, looked up once per device
-int scratch_on_current_device(double** out) {
+// the scratch address on the current device: looked up on every call whose
+// stream is not capturing, remembered for calls made during a capture
+int scratch_on_current_device(cudaStream_t st, double** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_status(e, "prodm_collect_squared_noalloc: cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices)
         return fail(PRODM_EUNSUPPORTED, "prodm_collect_squared_noalloc: device index above 63");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return cuda_status(e, "prodm_collect_squared_noalloc: cudaStreamIsCapturing");
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_sq_scratch);
         if (e != cudaSuccess) return cuda_status(e, "prodm_collect_squared_noalloc: cudaGetSymbolAddress");
         g_scratch_ptr[dev] = (double*)p;
+    } else if (!g_scratch_ptr[dev]) {
+        return fail(PRODM_EINVAL, "prodm_collect_squared_noalloc: first call on this device made during a stream "
+                                  "capture (call it once before capturing)");
     }
     *out = g_scratch_ptr[dev];
     return PRODM_OK;
@@ -78,9 +88,9 @@ extern "C" int prodm_collect_squared_noalloc(int dtype, const void* d, uint64_t 
         return fail(PRODM_EINVAL, "prodm_collect_squared_noalloc: num_bitplanes must be in [1, " +
                                       std::to_string(maxB) + "] (fixed scratch of " +
                                       std::to_string(kNoallocScratchDoubles * sizeof(double)) + " bytes)");
-    double* partial = nullptr;
-    if ((rc = scratch_on_current_device(&partial))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    double* partial = nullptr;
+    if ((rc = scratch_on_current_device(st, &partial))) return rc;
     if (dtype == PRODM_F64) return launch_sq_collect<double>((const double*)d, n, B, maxv, partial, out, st);
     return launch_sq_collect<float>((const float*)d, n, B, (float)maxv, partial, out, st);
 }

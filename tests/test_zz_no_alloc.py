@@ -10,7 +10,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-ERR_RTOL = 1e-4   # the tolerance of the other squared-error table tests
+ERR_RTOL = 1e-12   # the tolerance of the other squared-error table tests
 F32, F64 = 0, 1
 
 
@@ -85,3 +85,25 @@ def test_noalloc_small_inputs_and_limits():
     rc = lib.prodm_collect_squared_noalloc(F64, C.c_void_p(x64.data_ptr()), x64.numel(), 65, m,
                                            C.c_void_p(out.data_ptr()), _stream())
     assert rc == 1 and b"num_bitplanes" in lib.prodm_last_error_string()
+
+
+def test_noalloc_allocates_no_device_memory():
+    # warmed up (address looked up, torch's own tensors allocated), then two
+    # more calls leave the device's free memory exactly as it was
+    lib = _lib()
+    x, m = _case(5, (1 << 20) + 3, torch.float64)
+    out = torch.zeros(65, dtype=torch.float64, device="cuda")
+    st = _stream()
+
+    def call():
+        rc = lib.prodm_collect_squared_noalloc(F64, C.c_void_p(x.data_ptr()), x.numel(), 64, m,
+                                               C.c_void_p(out.data_ptr()), st)
+        assert rc == 0, lib.prodm_last_error_string()
+
+    call()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    call()
+    call()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
