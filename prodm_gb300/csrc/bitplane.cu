@@ -144,12 +144,69 @@ __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* _
 // exact sums, values below 2^23 to the warp's queue, and the four digit words
 // are transposed into the plane tile (whose popcounts give the bit counts).
 // ---------------------------------------------------------------------------
-constexpr int kErrTileBytes = 32 * NB_TILE_LD * 4;
-constexpr size_t kErrSmemNB = (size_t)((kErrTileBytes + 15) / 16 * 16) + 8 * sizeof(errtab::WarpQ) +
+// plane tile of the table encoder: rows of ERR_LD words (16-byte aligned), so
+// each lane stores its four transposed words of a step as one 16-byte store
+// (conflict-free: rows differ by 65 16-byte units) and the chunk's plane runs
+// leave with 16-byte copies
+constexpr int ERR_LD = 260;
+constexpr int kErrTileBytes = 32 * ERR_LD * 4;
+constexpr size_t kErrSmemNB = (size_t)kErrTileBytes + 8 * sizeof(errtab::WarpQ) +
                               errtab::kSlotsPad * sizeof(unsigned long long);
 // chunks a CTA encodes between two flushes of its 32-bit lane sums (each
 // chunk adds at most 8 * 260100 to a lane sum)
 constexpr int kErrFlushChunks = 2048;
+
+// the 8 four-value steps of one warp over its 32 blocks; FULLW: every value
+// of the blocks is inside the level (no bounds checks)
+template <bool FULLB, bool FULLW>
+__device__ __forceinline__ void nb_err_steps(const float* __restrict__ xw, int64_t rem, int B, int se, bool fast,
+                                             float scale, uint32_t* trow, errtab::Lane& acc, errtab::WarpQ& wq,
+                                             uint32_t& head, int& qn) {
+    const int lane = threadIdx.x & 31;
+    float vn[4];
+    auto load4 = [&](int j0) {
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const int o = (j0 + g) * 32;
+            vn[g] = (FULLW || o < rem) ? __ldcs(xw + o) : 0.f;
+        }
+    };
+    load4(0);
+#pragma unroll 1
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+        float sh[4];
+        if (fast) {                                                 // NegaBinaryBPEncoder.hpp:42
+#pragma unroll
+            for (int g = 0; g < 4; g++) sh[g] = vn[g] * scale;
+        } else {
+#pragma unroll
+            for (int g = 0; g < 4; g++) sh[g] = ldexpf(vn[g], se);
+        }
+        if (j0 + 4 < 32) load4(j0 + 4);                            // next step's values in flight
+        uint32_t t[4], nb[4];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            const bool ok = FULLW || (j0 + g) * 32 < rem;
+            const uint32_t tq = (uint32_t)(int32_t)sh[g] + 0xaaaaaaaau;   // :43-44; nb = t ^ 0xAAAAAAAA
+            nb[g] = tq ^ 0xaaaaaaaau;
+            t[g] = ok ? tq : 0u;                                          // padding adds nothing
+            const bool big = fabsf(sh[g]) >= 8388608.f;
+            acc.add_big_square(sh[g], big);                               // padding is 0: never big
+            const bool small = ok && !big;
+            const uint32_t bal = __ballot_sync(FULL, small);
+            if (bal) errtab::enqueue(wq, head, qn, bal, small, sh[g], lane);
+        }
+        errtab::drain_full<true>(wq, head, qn, lane);
+        acc.add4(t[0], t[1], t[2], t[3]);
+        uint32_t w[4];
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            w[g] = transpose32(nb[g], lane);
+            acc.pc += __popc(w[g]);
+        }
+        if (FULLB || lane < B) *reinterpret_cast<uint4*>(trow + j0) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
 
 template <bool FULLB>
 __device__ __forceinline__ void nb_encode32_chunk_err(const float* __restrict__ x, uint64_t n, uint64_t nblocks, int B,
@@ -159,45 +216,31 @@ __device__ __forceinline__ void nb_encode32_chunk_err(const float* __restrict__ 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int plane = B - 1 - lane;      // lane k owns bit k = plane B-1-k
     const uint64_t cb0 = c * NB_CHUNK;
-    const uint64_t wb0 = cb0 + (uint64_t)warp * 32;
-#pragma unroll 1
-    for (int j0 = 0; j0 < 32; j0 += 4) {
-        float sh[4];
-        bool ok[4];
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            const uint64_t i = (wb0 + j0 + g) * 32 + lane;
-            ok[g] = i < n;
-            const float v = ok[g] ? __ldcs(x + i) : 0.f;
-            sh[g] = fast ? v * scale : ldexpf(v, se);            // NegaBinaryBPEncoder.hpp:42
-        }
-        uint32_t t[4], nb[4];
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            const uint32_t tq = (uint32_t)(int32_t)sh[g] + 0xaaaaaaaau;   // :43-44; nb = t ^ 0xAAAAAAAA
-            nb[g] = tq ^ 0xaaaaaaaau;
-            t[g] = ok[g] ? tq : 0u;                                        // padding adds nothing
-            const bool big = fabsf(sh[g]) >= 8388608.f;
-            if (ok[g] && big) acc.add_big_square(sh[g]);
-            const bool small = ok[g] && !big;
-            const uint32_t bal = __ballot_sync(FULL, small);
-            if (bal) errtab::enqueue(wq, head, qn, bal, small, sh[g], lane);
-        }
-        errtab::drain_full<true>(wq, head, qn, lane);
-        acc.add4(t[0], t[1], t[2], t[3]);
-#pragma unroll
-        for (int g = 0; g < 4; g++) {
-            const uint32_t w = transpose32(nb[g], lane);
-            acc.pc += __popc(w);
-            if (FULLB || lane < B) tile[plane * NB_TILE_LD + warp * 32 + j0 + g] = w;
-        }
-    }
+    const uint64_t v0 = (cb0 + (uint64_t)warp * 32) * 32;     // first value of the warp's 32 blocks
+    const float* xw = x + v0 + lane;
+    const int64_t rem = (int64_t)n - (int64_t)v0 - lane;      // this lane's values left in the level
+    uint32_t* trow = tile + plane * ERR_LD + warp * 32;
+    if ((int64_t)n - (int64_t)v0 >= 1024)                     // warp-uniform: all 32 blocks inside
+        nb_err_steps<FULLB, true>(xw, rem, B, se, fast, scale, trow, acc, wq, head, qn);
+    else
+        nb_err_steps<FULLB, false>(xw, rem, B, se, fast, scale, trow, acc, wq, head, qn);
     __syncthreads();
     const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
-    for (int p = warp; p < B; p += 8) {
-        uint32_t* dst = out + (uint64_t)p * stride + cb0;
-        const uint32_t* row = tile + p * NB_TILE_LD;
-        for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
+    if ((stride & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+        // 16-byte runs; words past nvalid are zero (blocks past the level) and
+        // land in the plane row's padding to a multiple of four words
+        const int nq = (nvalid + 3) >> 2;
+        for (int p = warp; p < B; p += 8) {
+            uint4* dst = reinterpret_cast<uint4*>(out + (uint64_t)p * stride + cb0);
+            const uint4* row = reinterpret_cast<const uint4*>(tile + p * ERR_LD);
+            for (int j = lane; j < nq; j += 32) dst[j] = row[j];
+        }
+    } else {
+        for (int p = warp; p < B; p += 8) {
+            uint32_t* dst = out + (uint64_t)p * stride + cb0;
+            const uint32_t* row = tile + p * ERR_LD;
+            for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
+        }
     }
     __syncthreads();
 }
@@ -211,7 +254,7 @@ __global__ void __launch_bounds__(256, 2) k_nb_encode32_err(const ChunkSeg* __re
                                                             unsigned long long* __restrict__ recs) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t* tile = (uint32_t*)smem;
-    errtab::WarpQ* wq = (errtab::WarpQ*)(smem + (kErrTileBytes + 15) / 16 * 16);
+    errtab::WarpQ* wq = (errtab::WarpQ*)(smem + kErrTileBytes);
     unsigned long long* red = (unsigned long long*)(wq + 8);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     errtab::Lane acc;
@@ -771,7 +814,7 @@ __global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x,
             if (ERR) {
                 const float a = fabsf(sh[g]);
                 const bool big = a >= 8388608.f;
-                if (ok && big) acc.add_big_square(a);
+                acc.add_big_square(a, big);                                   // padding is 0: never big
                 const bool small = ok && !big;
                 const uint32_t bal = __ballot_sync(FULL, small);
                 if (bal) errtab::enqueue(wq[warp], head, qn, bal, small, a, lane);

@@ -24,10 +24,11 @@
 //   2^23 below 2^65 (accumulated exactly as fl(x^2) / 2^23).
 // * 1 <= |x| < 2^23: m = M * 2^-23 with an integer M, and
 //   (r_k + m)^2 = r_k^2 + 2^-22 r_k M + 2^-46 M^2: the cross sums
-//   sum u_k M (k = 1..31) and sum M^2 are exact integers. |x| < 1: r_k = 0,
+//   sum u_k M = sum_{b<k} 2^b sum_{bit b of t} M and sum M^2 are exact
+//   integers. |x| < 1: r_k = 0,
 //   m = x and x^2 is exact in double. These values (about 5 % of a 32-plane
 //   level) are queued per warp and handled 32 at a time: one lane per value
-//   for their own terms, then one lane per k for the cross sums.
+//   for their own terms, then one lane per bit b of t for the masked sums.
 // * Doubles (the |x| < 2^23 float-rounded squares and x^2 for |x| < 1) are
 //   summed per lane and reduced in a fixed order, so every table is
 //   bitwise reproducible.
@@ -42,7 +43,7 @@ constexpr int SQ = 0;       // 31: sum h_{J,s}^2, slot k-1 for k = 8J + s
 constexpr int CR = 31;      // 45: sum t_j h_{J,s} (j < J), slot cr_slot(j, J, s)
 constexpr int PC = 76;      // 32: count of bit b of t over the CTA's values
 constexpr int S6A = 108;    // u128: sum fl(x^2) / 2^23 over |x| >= 2^23
-constexpr int X = 110;      // 31 x i128: sum u_k M over 1 <= |x| < 2^23, slot X + 2(k-1)
+constexpr int X = 110;      // 31 x i128: Y_b = sum of M over 1 <= |x| < 2^23 with bit b of t, slot X + 2b
 constexpr int S4 = 172;     // u128: sum M^2
 constexpr int SM = 174;     // i128: sum M
 constexpr int S5 = 176;     // double: sum x^2 over |x| < 1
@@ -108,12 +109,15 @@ struct Lane {
         }
     }
 
-    // fl(x^2) / 2^23 for |x| >= 2^23 (x^2 >= 2^46 rounds to a multiple of 2^23, < 2^65)
-    __device__ __forceinline__ void add_big_square(float x) {
+    // fl(x^2) / 2^23 when big (|x| >= 2^23: x^2 >= 2^46 rounds to a multiple
+    // of 2^23, at most 2^64, so the scaled product is an integer below 2^42:
+    // its significand shifted by the exponent - 46); no branch
+    __device__ __forceinline__ void add_big_square(float x, bool big) {
         const uint32_t b = __float_as_uint(__fmul_rn(x, x));
         const uint32_t mant = (b & 0x7fffffu) | 0x800000u;
-        const int sh = (int)(b >> 23) - 173;     // biased exponent - 127 - 46, in [0, 18]
-        s6a += (unsigned long long)mant << sh;
+        const uint32_t sh = ((b >> 23) - 173u) & 31u;   // biased exponent - 127 - 46, in [0, 18] when big
+        const unsigned long long v = (unsigned long long)mant << sh;
+        s6a += big ? v : 0ull;
     }
 };
 
@@ -134,7 +138,10 @@ __device__ __forceinline__ void zero_q(WarpQ& q, int lane) {
 }
 
 // Process cnt (<= 32) queued values starting at ring slot head. NB: values are
-// the signed scaled values; grouped: their magnitudes.
+// the signed scaled values; grouped: their magnitudes. Lane e takes value e's
+// own terms; then lane b adds the M of the batch's values whose t has bit b
+// set (Y_b; the cross sums are sum_k u_k M = sum_{b<k} 2^b Y_b). Entries past
+// cnt are (0, 0) and add nothing.
 template <bool NB>
 __device__ __forceinline__ void run_batch(WarpQ& q, uint32_t head, int cnt, int lane) {
     int32_t M = 0;
@@ -156,19 +163,16 @@ __device__ __forceinline__ void run_batch(WarpQ& q, uint32_t head, int cnt, int 
     }
     q.batch[lane] = make_uint2(t, (uint32_t)M);
     __syncwarp();
-    // lane k-1 sums u_k M over the batch (k = 1..31; lane 31 idles)
-    const uint32_t mk = (2u << lane) - 1u;
-    long long xs = 0;
-    for (int e = 0; e < cnt; e++) {
-        const uint2 b = q.batch[e];
-        xs += (long long)(int32_t)(b.x & mk) * (long long)(int32_t)b.y;   // |.| < 2^54
+    int32_t y = 0;                                            // |y| < 32 * 2^23
+#pragma unroll
+    for (int e2 = 0; e2 < 32; e2++) {
+        const uint2 b = q.batch[e2];
+        if ((b.x >> lane) & 1u) y += (int32_t)b.y;
     }
-    add128(q.xlo[lane], q.xhi[lane], xs);
+    add128(q.xlo[lane], q.xhi[lane], y);
     __syncwarp();
 }
 
-// Queue the values of one group (bal: lanes with |x| < 2^23) and run full
-// batches. Returns the new queue length (warp-uniform).
 __device__ __forceinline__ void enqueue(WarpQ& q, uint32_t& head, int& qn, uint32_t bal, bool mine, float v,
                                         int lane) {
     if (mine) q.ring[(head + qn + __popc(bal & ((1u << lane) - 1u))) & (kRing - 1)] = v;
@@ -218,7 +222,7 @@ __device__ __forceinline__ void flush(Lane& a, WarpQ* wq, unsigned long long* re
         if (lane == 0) { red[WORDS + 2 * warp] = lo; red[WORDS + 2 * warp + 1] = hi; }
     }
     __syncthreads();
-    if (threadIdx.x < 31) {            // X_k, k = threadIdx.x + 1: 128-bit over warps
+    if (threadIdx.x < 31) {            // Y_b, b = threadIdx.x: 128-bit over warps
         unsigned long long lo = 0;
         long long hi = 0;
         for (int w = 0; w < nw; w++) {
@@ -319,7 +323,8 @@ __device__ double table_entry(const unsigned long long* R, uint64_t n, int B, in
         }
         const unsigned __int128 ak = (unsigned __int128)(k == 32 ? A : (A & ((1u << k) - 1u)));
         const __int128 sr2 = (__int128)su2 - (__int128)(2 * ak * su) + (__int128)(ak * ak * n);
-        const __int128 xk = ((__int128)rd_u128(R + X + 2 * (k - 1))) - (__int128)ak * (__int128)rd_u128(R + SM);
+        __int128 xk = -(__int128)ak * (__int128)rd_u128(R + SM);       // sum r_k M = sum u_k M - A_k sum M
+        for (int b = 0; b < k; b++) xk += (__int128)rd_u128(R + X + 2 * b) << b;
         v = i128_to_double(sr2) + i128_to_double(xk) * 0x1p-22 + u128_to_double(rd_u128(R + S4)) * 0x1p-46 +
             __longlong_as_double(R[S5]);
     }
