@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--no-perbit", action="store_true", help="skip the fp64 per-bit encoder measurement")
     ap.add_argument("--no-lossless", action="store_true", help="skip the lossless-stage measurement")
     ap.add_argument("--no-files", action="store_true", help="skip the level-file read / write measurement")
+    ap.add_argument("--no-ortho", action="store_true", help="skip the fp64 orthogonal-basis configuration")
     return ap.parse_args()
 
 
@@ -180,21 +181,31 @@ def cpu_sample_field(seed):
     return x
 
 
-def cpu_work(x):
-    """One bounded sample: refactor + progressive retrieval at the five tolerances."""
-    import numpy as np
+def cpu_libraries():
+    """(reference harness or None, oracle), loaded once before threads start."""
     import oracle
-    O = oracle.oracle()
+    return oracle.reference(), oracle.oracle()
+
+
+def cpu_work(x, libs):
+    """One bounded sample: refactor + progressive retrieval at the five
+    tolerances, on the reference's own classes when its harness is built
+    (oracle/_ref), else on the oracle's restatement. Returns (bytes, kind)."""
+    import numpy as np
     L, B = CPU_LEVELS, BITPLANES
+    norm2 = float(np.sum(x.astype(np.float64) ** 2))
+    tols = [(rel ** 2) * norm2 for rel in REL_TOLS]
+    R, O = libs
+    if R is not None:
+        return R.headline_step(x, L, B, tols), "reference"
     r = O.refactor(x, L, B, "negabinary", True, True)
     nbytes = x.size * 4 + r["blob"].size
-    norm2 = float(np.sum(x.astype(np.float64) ** 2))
     idx = np.zeros(L + 1, np.uint8)
-    for rel in REL_TOLS:
-        idx, _ = O.interpret("negabinary", "l2_hb", r["sizes"], r["errs"], (rel ** 2) * norm2, idx)
+    for tol in tols:
+        idx, _ = O.interpret("negabinary", "l2_hb", r["sizes"], r["errs"], tol, idx)
         O.retrieve(x.shape, L, B, r["blob"], r["sizes"], r["bounds"], idx, "negabinary", True)
         nbytes += int(sum(int(r["sizes"][l, :idx[l]].astype(np.int64).sum()) for l in range(L + 1))) + x.size * 4
-    return nbytes
+    return nbytes, "port"
 
 
 def cpu_baseline(steps, warmup, threads=None):
@@ -202,9 +213,15 @@ def cpu_baseline(steps, warmup, threads=None):
     base = cpu_sample_field(100)
     fields = [base] * threads            # read-only input; each refactor works on its own copy
     results = [0] * threads
+    kinds = ["port"] * threads
+    errors = []
+    libs = cpu_libraries()
 
     def run(t):
-        results[t] = cpu_work(fields[t])
+        try:
+            results[t], kinds[t] = cpu_work(fields[t], libs)
+        except Exception as e:   # reported after the join
+            errors.append(repr(e))
 
     total_bytes, total_time = 0, 0.0
     for s in range(warmup + steps):
@@ -215,10 +232,12 @@ def cpu_baseline(steps, warmup, threads=None):
         for th in ths:
             th.join()
         dt = time.perf_counter() - t0
+        if errors:
+            raise RuntimeError("CPU baseline failed: " + errors[0])
         if s >= warmup:
             total_bytes += sum(results)
             total_time += dt
-    return total_bytes / total_time / 1e9, threads, total_time / max(steps, 1), "port"
+    return total_bytes / total_time / 1e9, threads, total_time / max(steps, 1), kinds[0]
 
 
 def cpu_sample_text(cores, kind):
@@ -427,6 +446,7 @@ def run_ours(args):
     perbit = run_perbit() if (not args.no_perbit and world == 1) else None
     lossless = run_lossless() if (not args.no_lossless and world == 1) else None
     files = run_files() if (not args.no_files and world == 1) else None
+    ortho = run_ortho() if (not args.no_ortho and world == 1) else None
 
     # end-to-end through the reference-facing flow with host buffers
     e2e = run_e2e(args, mdr, x, tols, refactor_bytes, step_bytes, dev) if args.e2e_steps > 0 else None
@@ -451,6 +471,7 @@ def run_ours(args):
             "perbit": perbit,
             "lossless": lossless,
             "files": files,
+            "ortho": ortho,
             "clocks": clocks,
         }
     if world > 1:
@@ -802,6 +823,79 @@ def run_perbit(shape=(513, 513, 513), levels=7, planes=60, rels=(1e-3, 1e-5, 1e-
     }
 
 
+def run_ortho(shape=(1025, 1025, 513), levels=8, planes=60, rels=(1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 1e-8, 1e-9),
+              steps=2):
+    """The double-precision configuration: a 1025x1025x513 fp64 tanh shear
+    layer + 1e-6 relative noise, 9 levels, 60 planes, grouped encoder, max
+    collector, MGARD orthogonal basis (FP64 mass-matrix correction solves),
+    SignExclude interpreter with MaxErrorEstimatorOB, relative L-inf bounds
+    1e-3..1e-9 of the value range, progressive. Step bytes as the headline's
+    (field read + streams written; per tolerance the retrieved streams + the
+    field written); per-stage event times from a separate instrumented pass."""
+    import numpy as np
+    import torch
+    from prodm_gb300 import api, fields
+
+    x = fields.shear_layer(shape, delta=0.05, noise_rel=1e-6, seed=9, dtype=torch.float64, device="cuda")
+    N = x.numel()
+    vr = float(x.max() - x.min())
+    m = api.MDRField(shape, torch.float64, levels, planes, "grouped", "orthogonal", "max")
+    out = torch.empty_like(x)
+
+    def step(record=None):
+        m.refactor(x)
+        m.reset()
+        for r in rels:
+            m.retrieve(r * vr, out=out, interpreter="sign_exclude", estimator="max_ob")
+            if record is not None:
+                record.append(m.index().astype(np.int64))
+
+    idxs = []
+    step(idxs)
+    torch.cuda.synchronize()
+    errs_ok = bool(float((out - x).abs().max()) <= rels[-1] * vr)
+    sizes, _, _ = m.level_info()
+    sizes = sizes.astype(np.int64)
+    stream_bytes = int(sizes.sum())
+    retrieved = [int(sum(sizes[l, :ix[l]].sum() for l in range(levels + 1))) for ix in idxs]
+    step_bytes = (N * 8 + stream_bytes) + sum(r + N * 8 for r in retrieved)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    m.set_timing(True)
+    step()
+    torch.cuda.synchronize()
+    st = m.stage_times()
+    m.set_timing(False)
+    peak, peak_src = measured_peak()
+    ld, lel = api.level_dims(shape, levels)
+    box = [int(np.prod(ld[l].astype(np.int64))) for l in range(levels + 1)]
+    stages = {}
+    for (kind, level), (t, cnt) in sorted(st.items(), key=lambda kv: -kv[1][0])[:12]:
+        b = None
+        if kind == "decompose":     # level box read + written, the correction's boxes
+            b = 2 * 8 * box[level]
+        stages["%s_l%d" % (kind, level)] = {"ms": t / cnt, "launches": cnt,
+                                            "gbs": (b / (t / cnt) / 1e6) if b else None,
+                                            "frac": (b / (t / cnt) / 1e6 / peak) if b else None}
+    m.close()
+    del x, out
+    torch.cuda.empty_cache()
+    return {
+        "workload": "%s fp64 tanh shear layer + 1e-6 relative noise (seeded), %d levels, %d planes, grouped encoder, "
+                    "max collector, orthogonal basis, SignExclude greedy interpreter + MaxErrorEstimatorOB, relative "
+                    "L-inf %s" % ("x".join(map(str, shape)), levels + 1, planes, list(rels)),
+        "step": {"ms": ms, "bytes": step_bytes, "gbs": step_bytes / ms / 1e6, "frac": step_bytes / ms / 1e6 / peak,
+                 "tightest_bound_met": errs_ok, "planes_per_level": [ix.tolist() for ix in idxs]},
+        "stages": stages,
+        "peak": {"gbs": peak, "source": peak_src},
+    }
+
+
 def run_lossless(reps=3):
     """The lossless stage (AdaptiveLevelCompressor's rule, ZCB codec) on the
     headline workload's streams: stored / raw sizes and stopping indices per
@@ -859,6 +953,33 @@ def run_lossless(reps=3):
         O.zcb_compress(host[offs[p]:offs[p + 1]])
     t_cpu = time.time() - t0
     cpu_bytes = int(offs[4])
+    # the reference's own AdaptiveLevelCompressor (zstd level 3, latter index
+    # 26) on the same streams, and what its interpreter would retrieve with
+    # those stored sizes (the oracle interpreter, pinned to the reference's)
+    zstd = {"available": False}
+    import importlib
+    ob = importlib.import_module("oracle.build_oracle")
+    R = oracle.reference()
+    if R is not None and ob.zstd_library():
+        _, _, errs = m.level_info()
+        zs = np.zeros_like(raw)
+        zstop = []
+        t0 = time.time()
+        for l in range(LEVELS + 1):
+            stp, kept, _ = R.adaptive_compress(m.export_level(l), raw[l].astype(np.uint32), 26)
+            zs[l] = kept
+            zstop.append(int(stp))
+        t_z = time.time() - t0
+        idx = np.zeros(LEVELS + 1, np.uint8)
+        zret = []
+        for rel in REL_TOLS:
+            idx, _ = O.interpret("negabinary", "l2_hb", zs.astype(np.uint32), errs, rel * rel * norm2, idx)
+            zret.append(int(sum(int(zs[l, :idx[l]].astype(np.int64).sum()) for l in range(LEVELS + 1))))
+        zl = zs.astype(np.int64).sum(axis=1)
+        zstd = {"available": True, "stored_bytes_per_level": zl.tolist(), "stopping_indices": zstop,
+                "ratio": float(raw.astype(np.int64).sum() / zl.sum()), "retrieved_bytes": zret,
+                "cpu_seconds_all_levels": t_z, "cores": 1,
+                "codec": "reference AdaptiveLevelCompressor + ZSTD (level 3), system libzstd"}
     m.close()
     del x, out, blob, comp, back
     torch.cuda.empty_cache()
@@ -867,6 +988,7 @@ def run_lossless(reps=3):
             "raw_bytes_per_level": rs.tolist(), "stored_bytes_per_level": ss.tolist(),
             "ratio": float(rs.sum() / ss.sum()),
             "retrieved_bytes_raw": raw_ret, "retrieved_bytes_stored": stored_ret,
+            "reference_zstd": zstd,
             "finest_level": {"raw_bytes": nbytes, "stopping_index": stop, "stored_bytes": int(csz.astype(np.int64).sum()),
                              "compress_seconds": t_c, "compress_gbs": nbytes / t_c / 1e9,
                              "decompress_seconds": t_d, "decompress_gbs": nbytes / t_d / 1e9,
@@ -1006,8 +1128,11 @@ def main():
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
             value, cores, sec, kind = cpu_baseline(1, 0)
+            one, _, one_sec, _ = cpu_baseline(1, 0, threads=1)
             res["cpu_baseline"] = {"value": value, "unit": "GB/s", "cores": cores, "kind": kind,
-                                   "sample": cpu_sample_text(cores, kind)}
+                                   "sample": cpu_sample_text(cores, kind),
+                                   "one_core": {"value": one, "unit": "GB/s", "cores": 1,
+                                                "seconds_per_field": one_sec}}
         print(json.dumps(res))
     return 0
 

@@ -141,7 +141,7 @@ class GpuDirectInterleaver PRODM_BASE(MDR::concepts::InterleaverInterface<T>) {
     void interleave(T const* data, const std::vector<uint32_t>& dims, const std::vector<uint32_t>& dims_fine,
                     const std::vector<uint32_t>& dims_coarse, T* buffer,
                     std::vector<uint32_t> strides = std::vector<uint32_t>()) const {
-        const size_t n = product(dims), m = count(dims_fine, dims_coarse);
+        const size_t n = span(dims, strides), m = count(dims_fine, dims_coarse);
         DeviceBuffer d(n * sizeof(T)), b(m * sizeof(T));
         cuda_check(cudaMemcpy(d.get(), data, n * sizeof(T), cudaMemcpyHostToDevice), "H2D");
         check(prodm_interleave(dtype_of<T>(), d.get(), (int)dims.size(), dims.data(), dims_fine.data(), dims_coarse.data(),
@@ -152,7 +152,7 @@ class GpuDirectInterleaver PRODM_BASE(MDR::concepts::InterleaverInterface<T>) {
     void reposition(T const* buffer, const std::vector<uint32_t>& dims, const std::vector<uint32_t>& dims_fine,
                     const std::vector<uint32_t>& dims_coarse, T* data,
                     std::vector<uint32_t> strides = std::vector<uint32_t>()) const {
-        const size_t n = product(dims), m = count(dims_fine, dims_coarse);
+        const size_t n = span(dims, strides), m = count(dims_fine, dims_coarse);
         DeviceBuffer d(n * sizeof(T)), b(m * sizeof(T));
         cuda_check(cudaMemcpy(d.get(), data, n * sizeof(T), cudaMemcpyHostToDevice), "H2D");
         cuda_check(cudaMemcpy(b.get(), buffer, m * sizeof(T), cudaMemcpyHostToDevice), "H2D");
@@ -167,6 +167,15 @@ class GpuDirectInterleaver PRODM_BASE(MDR::concepts::InterleaverInterface<T>) {
     static size_t count(const std::vector<uint32_t>& f, const std::vector<uint32_t>& c) {
         size_t a = product(f), b = product(c);
         return a - b;
+    }
+    // elements the strided array spans: the reference passes the full array's
+    // strides with a smaller box when it reconstructs a coarser level
+    // (ComposedReconstructor.hpp:190, :208, :246)
+    static size_t span(const std::vector<uint32_t>& dims, const std::vector<uint32_t>& strides) {
+        if (strides.empty()) return product(dims);
+        size_t n = 1;
+        for (size_t i = 0; i < dims.size(); i++) n += (size_t)(dims[i] - 1) * strides[i];
+        return n;
     }
 };
 

@@ -392,6 +392,20 @@ class Reference(Oracle):
         stop = f(np.ascontiguousarray(blob, np.uint8), np.ascontiguousarray(sizes, np.uint32), B, int(latter), out, zs)
         return stop, out, zs
 
+    def headline_step(self, field, L, B, tols, out=None):
+        """One benchmark step on the reference's own classes (fp32, negabinary,
+        encoder squared-error tables, NegaBinary greedy interpreter with
+        L2ErrorEstimator_HB, hierarchical basis); tols are absolute squared
+        tolerances. Returns the step's algorithmic bytes."""
+        f = self._fn("ref_headline_step_f32", C.c_int64, _f32p, _u32p, C.c_int, C.c_int, C.c_int, _f64p, C.c_void_p)
+        tols = np.ascontiguousarray(tols, np.float64)
+        x = np.ascontiguousarray(field, np.float32)
+        optr = out.ctypes.data_as(C.c_void_p) if out is not None else None
+        r = f(x.ravel(), np.asarray(field.shape, np.uint32), int(L), int(B), len(tols), tols, optr)
+        if r < 0:
+            raise RuntimeError("reference step failed")
+        return int(r)
+
     def composed(self, field, L, B, encoder, hierarchical, tols, workdir):
         dims = np.asarray(field.shape, np.uint32)
         dt = field.dtype

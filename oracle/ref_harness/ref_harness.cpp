@@ -6,6 +6,7 @@
 // the oracle's restatement, so composed-refactor parity at that boundary stays
 // unpinned. Built into oracle/_ref/ by oracle/build_oracle.py.
 #include <iostream>
+#include <mutex>
 #include <sstream>
 #include <vector>
 #include <string>
@@ -27,11 +28,28 @@
 #include "qoi_utils.hpp"
 
 namespace {
-struct Quiet {  // the reference interpreters print to std::cout
-    std::streambuf* old;
-    std::ostringstream sink;
-    Quiet() { old = std::cout.rdbuf(sink.rdbuf()); }
-    ~Quiet() { std::cout.rdbuf(old); }
+// The reference's classes print to std::cout. While any harness call runs,
+// std::cout writes into one stateless discarding buffer; the first caller
+// swaps it in and the last one restores the original, so calls from several
+// threads at once (the benchmark's CPU arm) never leave std::cout pointing at
+// a buffer that is gone.
+struct DiscardBuf : std::streambuf {
+    int overflow(int c) override { return c == EOF ? 0 : c; }
+    std::streamsize xsputn(const char*, std::streamsize n) override { return n; }
+};
+struct Quiet {
+    static std::mutex& mu() { static std::mutex m; return m; }
+    static int& depth() { static int d = 0; return d; }
+    static std::streambuf*& saved() { static std::streambuf* s = nullptr; return s; }
+    static DiscardBuf& sink() { static DiscardBuf b; return b; }
+    Quiet() {
+        std::lock_guard<std::mutex> lock(mu());
+        if (depth()++ == 0) saved() = std::cout.rdbuf(&sink());
+    }
+    ~Quiet() {
+        std::lock_guard<std::mutex> lock(mu());
+        if (--depth() == 0) std::cout.rdbuf(saved());
+    }
 };
 std::vector<uint32_t> vec(const uint32_t* p, int n) { return std::vector<uint32_t>(p, p + n); }
 
@@ -232,6 +250,81 @@ REF_T(f64, double, uint64_t)
 
 REF_PB(f32, float)
 REF_PB(f64, double)
+
+// One step of the benchmark workload on the reference's own classes: the
+// refactor loop of ComposedRefactor::refactor (ComposedRefactor.hpp:78-141:
+// decompose, then per level interleave, level max, exponent, encode) and, per
+// tolerance, the progressive loop of ComposedReconstructor::reconstruct
+// (ComposedReconstructor.hpp:27-100, :187-258: interpret, decode the new
+// planes of each level, reposition, recompose, add the previous
+// reconstruction). The squared-error tables come from the encoder's
+// error-collecting overload (NegaBinaryBPEncoder.hpp:65-125), the call
+// ComposedRefactor leaves commented out (:117-118), because its reconstructor
+// needs them for an L2 tolerance; streams stay in memory (NullLevelCompressor,
+// no files). tols are absolute squared tolerances. Returns the step's
+// algorithmic bytes (field read + all streams written; per tolerance the
+// streams retrieved so far + the field written), or -1.
+extern "C" int64_t ref_headline_step_f32(const float* field, const uint32_t* dims3, int L, int B, int ntol,
+                                         const double* tols, float* out) {
+    using Enc = MDR::NegaBinaryBPEncoder<float, uint32_t>;
+    std::vector<uint32_t> dims(dims3, dims3 + 3);
+    const size_t N = (size_t)dims[0] * dims[1] * dims[2];
+    std::vector<float> data(field, field + N);
+    MDR::MGARDHierarchicalDecomposer<float> decomposer;
+    MDR::DirectInterleaver<float> interleaver;
+    Enc encoder;
+    Quiet q;
+    decomposer.decompose(data.data(), dims, (uint32_t)L);
+    auto level_dims = MDR::compute_level_dims(dims, (uint32_t)L);
+    auto level_elements = MDR::compute_level_elements(level_dims, (uint32_t)L);
+    std::vector<uint32_t> dims_dummy(3, 0);
+    std::vector<std::vector<uint8_t*>> comps(L + 1);
+    std::vector<std::vector<uint32_t>> sizes(L + 1);
+    std::vector<std::vector<double>> errs(L + 1);
+    std::vector<float> bounds(L + 1);
+    int64_t bytes = (int64_t)(N * sizeof(float));
+    for (int i = 0; i <= L; i++) {
+        const std::vector<uint32_t>& prev = i == 0 ? dims_dummy : level_dims[i - 1];
+        std::vector<float> buf(level_elements[i]);
+        interleaver.interleave(data.data(), dims, level_dims[i], prev, buf.data());
+        const float mx = MDR::compute_max_abs_value(buf.data(), level_elements[i]);
+        bounds[i] = mx * 4;
+        int exp = 0;
+        frexp(mx, &exp);
+        comps[i] = encoder.encode(buf.data(), (int32_t)level_elements[i], exp, (uint8_t)B, sizes[i], errs[i]);
+        for (uint32_t s : sizes[i]) bytes += s;
+    }
+    MDR::NegaBinaryGreedyBasedSizeInterpreter<MDR::L2ErrorEstimator_HB<float>> interp(
+        MDR::L2ErrorEstimator_HB<float>(3, L));
+    std::vector<uint8_t> nbp(L + 1, 0);
+    std::vector<float> rec(N, 0.f), cur(N);
+    std::vector<uint32_t> strides = {dims[1] * dims[2], dims[2], 1};
+    for (int t = 0; t < ntol; t++) {
+        std::vector<uint8_t> prev_nbp(nbp);
+        interp.interpret_retrieve_size(sizes, errs, tols[t], nbp);
+        std::fill(cur.begin(), cur.end(), 0.f);
+        for (int i = 0; i <= L; i++) {
+            if (nbp[i] > prev_nbp[i]) {
+                int exp = 0;
+                frexp(bounds[i] / 4, &exp);
+                std::vector<const uint8_t*> planes(comps[i].begin() + prev_nbp[i], comps[i].end());
+                float* dec = encoder.progressive_decode(planes, (int32_t)level_elements[i], exp, prev_nbp[i],
+                                                        (uint8_t)(nbp[i] - prev_nbp[i]), i);
+                const std::vector<uint32_t>& prev = i == 0 ? dims_dummy : level_dims[i - 1];
+                interleaver.reposition(dec, dims, level_dims[i], prev, cur.data(), strides);
+                free(dec);
+            }
+            for (int p = 0; p < nbp[i]; p++) bytes += sizes[i][p];
+        }
+        decomposer.recompose(cur.data(), dims, (uint32_t)L, strides);
+        for (size_t k = 0; k < N; k++) rec[k] += cur[k];
+        bytes += (int64_t)(N * sizeof(float));
+    }
+    if (out) std::memcpy(out, rec.data(), N * sizeof(float));
+    for (auto& c : comps)
+        for (auto* p : c) free(p);
+    return bytes;
+}
 
 // AdaptiveLevelCompressor (zstd, level 3) on B streams concatenated in blob:
 // returns the stopping index; out_sizes = the sizes it leaves (compressed or

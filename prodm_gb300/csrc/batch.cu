@@ -272,7 +272,7 @@ int batch_build_segments(prodm_batch* h) {
 
 unsigned persistent_grid(const prodm_batch* h, uint64_t work_items, unsigned items_per_cta) {
     uint64_t need = (work_items + items_per_cta - 1) / items_per_cta;
-    uint64_t cap = (uint64_t)kSMs * h->ctas_per_sm;
+    uint64_t cap = (uint64_t)device_sms() * h->ctas_per_sm;
     uint64_t g = need < cap ? need : cap;
     return (unsigned)(g ? g : 1);
 }

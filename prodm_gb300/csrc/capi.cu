@@ -36,6 +36,21 @@ int cuda_status(cudaError_t e, const char* where) {
     return e == cudaErrorMemoryAllocation ? PRODM_ENOMEM : PRODM_ECUDA;
 }
 
+int device_sms() {
+    static std::mutex mu;
+    static std::vector<std::pair<int, int>> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto& e : cache)
+        if (e.first == dev) return e.second;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = kSMs;
+    (void)cudaGetLastError();
+    cache.push_back({dev, sms});
+    return sms;
+}
+
 unsigned resident_ctas(const void* kernel, int threads, size_t smem) {
     struct Entry {
         int dev;
@@ -53,8 +68,8 @@ unsigned resident_ctas(const void* kernel, int threads, size_t smem) {
         for (const Entry& e : cache)
             if (e.dev == dev && e.k == kernel && e.threads == threads && e.smem == smem) return e.ctas;
     }
-    int sms = 0, per_sm = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = kSMs;
+    const int sms = device_sms();
+    int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
     (void)cudaGetLastError();
@@ -749,7 +764,6 @@ int mdr_alloc_all(prodm_mdr* h) {
     if (h->orth && L >= 1) {
         const Box& F = g.box[L];
         Box C{{coarse_len(F.n[0]), coarse_len(F.n[1]), coarse_len(F.n[2])}};
-        if ((rc = h->alloc(&h->os.fnat, F.size() * es))) return rc;
         if ((rc = h->alloc(&h->os.t1, (uint64_t)F.n[0] * F.n[1] * C.n[2] * es))) return rc;
         if ((rc = h->alloc(&h->os.t2, (uint64_t)F.n[0] * C.n[1] * C.n[2] * es))) return rc;
         if ((rc = h->alloc(&h->os.z, C.size() * es))) return rc;
@@ -900,12 +914,13 @@ int mdr_refactor(prodm_mdr* h, const T* field, cudaStream_t st) {
             T* cout = (l == 1) ? coef + g.offset[0] : (T*)h->cbuf[l & 1];
             Stage sg(h, 0, l, st);
             if ((rc = launch_decompose_level_packed<T>(in, (uint64_t)F.n[1] * F.n[2], F.n[2], F, C, coef + g.offset[l],
-                                                       cout, h->orth ? (T*)h->os.fnat : nullptr, keys + l,
+                                                       cout, nullptr, keys + l,
                                                        (l == 1 && !h->orth) ? (void*)keys : nullptr, st)))
                 return rc;
-            if (h->orth) {
+            if (h->orth) {   // the correction reads the level's packed coefficients
                 const T* tabs[3] = {level_tabs<T>(h, l, 0), level_tabs<T>(h, l, 1), level_tabs<T>(h, l, 2)};
-                if ((rc = launch_l2_correction<T>((T*)h->os.fnat, F, (T*)h->os.t1, (T*)h->os.t2, (T*)h->os.z, tabs, st)))
+                if ((rc = launch_l2_correction<T>(nullptr, F, (T*)h->os.t1, (T*)h->os.t2, (T*)h->os.z, tabs, st,
+                                                  coef + g.offset[l], &C)))
                     return rc;
                 if ((rc = launch_add_box<T>(cout, (uint64_t)C.n[1] * C.n[2], C.n[2], (T*)h->os.z, C, (T)1, st))) return rc;
             }
@@ -992,8 +1007,8 @@ int mdr_decode_recompose(prodm_mdr* h, T* out, cudaStream_t st) {
         }
         if (h->orth) {
             const T* tabs[3] = {level_tabs<T>(h, l, 0), level_tabs<T>(h, l, 1), level_tabs<T>(h, l, 2)};
-            if ((rc = launch_coef_to_natural<T>(rcoef + h->roff[l], F, C, (T*)h->os.fnat, st))) return rc;
-            if ((rc = launch_l2_correction<T>((T*)h->os.fnat, F, (T*)h->os.t1, (T*)h->os.t2, (T*)h->os.z, tabs, st)))
+            if ((rc = launch_l2_correction<T>(nullptr, F, (T*)h->os.t1, (T*)h->os.t2, (T*)h->os.z, tabs, st,
+                                              rcoef + h->roff[l], &C)))
                 return rc;
             if ((rc = launch_add_box<T>(cin, (uint64_t)C.n[1] * C.n[2], C.n[2], (T*)h->os.z, C, (T)-1, st))) return rc;
         }

@@ -29,7 +29,11 @@ void count_launch();
         if (_e != cudaSuccess) return ::prodm::cuda_status(_e, name);     \
     } while (0)
 
-constexpr int kSMs = 152;   // GB300: 2 dies x 76 SMs
+// GB300's SM count (2 dies x 76): the fallback when the device cannot be
+// queried and the basis of fixed buffer sizes (kPartialSlots); grids are
+// sized from the current device's own count (device_sms)
+constexpr int kSMs = 152;
+int device_sms();   // multiprocessors of the current device (cached per device)
 
 // ---------------------------------------------------------------------------
 // Programmatic dependent launch along a chain of dependent kernels (one
@@ -77,7 +81,7 @@ inline unsigned persistent_grid_for(const void* kernel, int threads, size_t smem
 
 inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
     size_t g = (work + threads - 1) / threads;
-    size_t cap = (size_t)kSMs * per_sm;
+    size_t cap = (size_t)device_sms() * per_sm;
     if (g > cap) g = cap;
     if (g == 0) g = 1;
     return (unsigned)g;

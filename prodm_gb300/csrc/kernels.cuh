@@ -28,8 +28,10 @@ template <class T>
 int launch_reordered_to_natural(const T* rin, const Box& F, const Box& C, T* fnat, cudaStream_t st);
 template <class W>
 void mass_factors(uint32_t n, W* tab);
+// coef != nullptr: read the level's packed coefficients (coarse box *C) instead of fnat
 template <class T>
-int launch_l2_correction(const T* fnat, const Box& F, T* t1, T* t2, T* z, const T* const tabs[3], cudaStream_t st);
+int launch_l2_correction(const T* fnat, const Box& F, T* t1, T* t2, T* z, const T* const tabs[3], cudaStream_t st,
+                         const T* coef = nullptr, const Box* C = nullptr);
 template <class T>
 int launch_add_box(T* dst, uint64_t b0, uint64_t b1, const T* z, const Box& B, T sign, cudaStream_t st);
 template <class T>

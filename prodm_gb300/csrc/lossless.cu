@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(32 * ZW) k_zcb_read(const ZStream* __restrict_
 
 unsigned zgrid(uint64_t chunks) {
     uint64_t g = (chunks + ZW - 1) / ZW;
-    const uint64_t cap = (uint64_t)kSMs * 8;
+    const uint64_t cap = (uint64_t)device_sms() * 8;
     return (unsigned)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 

@@ -307,6 +307,130 @@ __global__ void k_l2_line(const T* __restrict__ src, Box S, int d, T* __restrict
     }
 }
 
+// The dim-2 (contiguous) pass of the L2 projection with shared-memory staging:
+// one warp per 32 lines (fine rows (x0, x1) of F). Forward sweep: tiles of 64
+// fine columns plus two halo columns each side are staged row by row with
+// coalesced loads; lane r then sweeps row r's coarse nodes of the tile
+// (right-hand side from the 5-point neighbourhood, Thomas forward step) into
+// an output tile stored with coalesced writes. Backward sweep: the stored
+// tiles come back from the end, lane r substitutes back along its row, and
+// they are stored again. PACKED: the rows are read straight from the level's
+// packed coefficients (a natural row is an even/odd split of one contiguous
+// run of interleaved ranks; coarse nodes of rows inside the coarse box are
+// zero), so no natural-order copy is needed; else from a natural field.
+constexpr int L2_TILE = 64;                 // fine columns per tile
+constexpr int L2_IN_LD = L2_TILE + 5;       // staged row: 2 + 64 + 2 columns, odd stride (no bank conflicts)
+constexpr int L2_OUT_LD = 35;               // up to 33 coarse nodes per tile, odd stride
+
+template <class T, class W, bool PACKED>
+__global__ void __launch_bounds__(32) k_l2_rows(const T* __restrict__ src, Box F, Box C, T* __restrict__ dst,
+                                                const W* __restrict__ cp, const W* __restrict__ lo_w,
+                                                const W* __restrict__ inv_den) {
+    __shared__ W sin_[32 * L2_IN_LD];
+    __shared__ W sout[32 * L2_OUT_LD];
+    const int lane = threadIdx.x;
+    const uint32_t nf = F.n[2], nc = coarse_len(nf);
+    const uint64_t lines = (uint64_t)F.n[0] * F.n[1];
+    const uint32_t c2n = C.n[2];
+    const uint64_t l0 = (uint64_t)blockIdx.x * 32;
+    if (l0 >= lines) return;
+    const int nl = (int)min((uint64_t)32, lines - l0);
+    // row r's source: base offset, whether it lies inside the coarse box
+    auto row_src = [&](int r, uint64_t& base, bool& cc) {
+        const uint64_t li = l0 + r;
+        const uint32_t x0 = (uint32_t)(li / F.n[1]), x1 = (uint32_t)(li - (uint64_t)x0 * F.n[1]);
+        if (PACKED) {
+            const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
+            cc = r0 < C.n[0] && r1 < C.n[1];
+            base = level_rank(r0, r1, cc ? c2n : 0u, F, C);
+        } else {
+            cc = false;
+            base = li * nf;
+        }
+    };
+    auto fine_at = [&](uint64_t base, bool cc, int64_t x) -> W {   // natural column x of a row, 0 outside
+        if (x < 0 || x >= (int64_t)nf) return (W)0;
+        if (!PACKED) return (W)src[base + x];
+        const uint32_t xx = (uint32_t)x;
+        const uint32_t r2 = reord(xx, nf, c2n);
+        if (cc) return is_coarse(xx, nf) ? (W)0 : (W)src[base + (r2 - c2n)];
+        return (W)src[base + r2];
+    };
+    if (nc == nf) {   // no coarse subset along this dim: the projection is the identity
+        for (int r = 0; r < nl; r++) {
+            uint64_t base;
+            bool cc;
+            row_src(r, base, cc);
+            for (uint32_t j = lane; j < nf; j += 32) dst[(l0 + r) * nc + j] = (T)fine_at(base, cc, j);
+        }
+        return;
+    }
+    const uint32_t ntiles = (nf + L2_TILE - 1) / L2_TILE;
+    W prev = 0;
+    uint32_t m = 0;                                    // next coarse node of this lane's row
+    for (uint32_t t = 0; t < ntiles; t++) {
+        const int64_t x0 = (int64_t)t * L2_TILE - 2;   // first staged column
+        for (int r = 0; r < nl; r++) {
+            uint64_t base;
+            bool cc;
+            row_src(r, base, cc);
+            for (int j = lane; j < L2_TILE + 4; j += 32) sin_[r * L2_IN_LD + j] = fine_at(base, cc, x0 + j);
+        }
+        __syncwarp();
+        // coarse nodes whose fine position falls in [64t, 64t + 64)
+        const uint32_t xe = min((uint32_t)(t + 1) * L2_TILE, nf);
+        const uint32_t mt0 = m;
+        if (lane < nl) {
+            const W* s = sin_ + lane * L2_IN_LD;
+            auto sv = [&](int64_t x) -> W { return s[x - x0]; };
+            auto mf = [&](int64_t x) -> W {           // (M_f line)[x]
+                const W dg = (x == 0 || x == (int64_t)nf - 1) ? (W)1 / 3 : (W)2 / 3;
+                return dg * sv(x) + (sv(x - 1) + sv(x + 1)) / 6;
+            };
+            for (uint32_t mm = mt0; mm < nc; mm++) {
+                const uint32_t c = fine_of_coarse(mm, nf, nc);
+                if (c >= xe) break;
+                W b = mf(c);
+                if (c > 0 && !is_coarse(c - 1, nf)) b += (W)0.5 * mf((int64_t)c - 1);
+                if (c + 1 < nf && !is_coarse(c + 1, nf)) b += (W)0.5 * mf((int64_t)c + 1);
+                const W dp = (mm == 0) ? b * inv_den[0] : (b - lo_w[mm] * prev) * inv_den[mm];
+                sout[lane * L2_OUT_LD + (mm - mt0)] = dp;
+                prev = dp;
+            }
+        }
+        // the tile's coarse range is the same for every row
+        uint32_t mt1 = mt0;
+        while (mt1 < nc && fine_of_coarse(mt1, nf, nc) < xe) mt1++;
+        m = mt1;
+        __syncwarp();
+        for (int r = 0; r < nl; r++)
+            for (uint32_t j = lane; j < mt1 - mt0; j += 32)
+                dst[(l0 + r) * nc + mt0 + j] = (T)sout[r * L2_OUT_LD + j];
+        __syncwarp();
+    }
+    // backward substitution, tiles from the end
+    W z = 0;
+    uint32_t mhi = nc;
+    while (mhi > 0) {
+        const uint32_t mlo = mhi > 32 ? mhi - 32 : 0;
+        for (int r = 0; r < nl; r++)
+            for (uint32_t j = lane; j < mhi - mlo; j += 32) sout[r * L2_OUT_LD + j] = (W)dst[(l0 + r) * nc + mlo + j];
+        __syncwarp();
+        if (lane < nl) {
+            W* o = sout + lane * L2_OUT_LD;
+            for (uint32_t mm = mhi; mm-- > mlo;) {
+                z = (mm == nc - 1) ? o[mm - mlo] : o[mm - mlo] - cp[mm] * z;
+                o[mm - mlo] = z;
+            }
+        }
+        __syncwarp();
+        for (int r = 0; r < nl; r++)
+            for (uint32_t j = lane; j < mhi - mlo; j += 32) dst[(l0 + r) * nc + mlo + j] = (T)sout[r * L2_OUT_LD + j];
+        __syncwarp();
+        mhi = mlo;
+    }
+}
+
 // dst[i] += sign * z[i] over a compact box written into a strided box
 template <class T>
 __global__ void k_add_box(T* __restrict__ dst, uint64_t b0, uint64_t b1, const T* __restrict__ z, Box B, T sign) {
@@ -348,7 +472,7 @@ unsigned row_threads(uint32_t) { return 256; }
 unsigned row_grid(uint64_t rows, unsigned th) {
     const uint64_t wpb = th / 32;
     uint64_t need = (rows + wpb - 1) / wpb;
-    uint64_t cap = (uint64_t)kSMs * 8 * 4;
+    uint64_t cap = (uint64_t)device_sms() * 8 * 4;
     uint64_t g = need < cap ? need : cap;
     return (unsigned)(g ? g : 1);
 }
@@ -443,15 +567,29 @@ void mass_factors(uint32_t n, W* tab) {
 template void mass_factors<float>(uint32_t, float*);
 template void mass_factors<double>(uint32_t, double*);
 
-// z (compact C box) = L2 projection of the natural coefficient field fnat (F box).
-// tabs[d] = device Thomas factors for dim d; t1/t2 scratch boxes.
+// z (compact C box) = L2 projection of the natural coefficient field (F box):
+// from fnat, or (coef != nullptr) straight from the level's packed
+// coefficients (coarse box C). tabs[d] = device Thomas factors for dim d;
+// t1/t2 scratch boxes. The contiguous dim goes first through the staged row
+// kernel, the two strided dims through the line kernel (coalesced there).
 template <class T>
-int launch_l2_correction(const T* fnat, const Box& F, T* t1, T* t2, T* z, const T* const tabs[3], cudaStream_t st) {
+int launch_l2_correction(const T* fnat, const Box& F, T* t1, T* t2, T* z, const T* const tabs[3], cudaStream_t st,
+                         const T* coef, const Box* C) {
     const int th = 128;
     Box a = F;
-    const T* src = fnat;
     T* bufs[3] = {t1, t2, z};
-    for (int k = 0, d = 2; d >= 0; d--, k++) {
+    {
+        const uint32_t nc = coarse_len(F.n[2]);
+        const T* tab = tabs[2];
+        const uint64_t lines = (uint64_t)F.n[0] * F.n[1];
+        const unsigned grid = (unsigned)((lines + 31) / 32);
+        if (coef) k_l2_rows<T, T, true><<<grid, 32, 0, st>>>(coef, F, *C, t1, tab, tab + nc, tab + 2 * nc);
+        else k_l2_rows<T, T, false><<<grid, 32, 0, st>>>(fnat, F, F, t1, tab, tab + nc, tab + 2 * nc);
+        PRODM_CHECK_LAUNCH("k_l2_rows");
+        a.n[2] = nc;
+    }
+    const T* src = t1;
+    for (int k = 1, d = 1; d >= 0; d--, k++) {
         Box b = a;
         b.n[d] = coarse_len(a.n[d]);
         uint64_t lines = a.size() / a.n[d];
@@ -495,7 +633,8 @@ int launch_interleave(T* data, uint64_t s0, uint64_t s1, const Box& F, const Box
     template int launch_copy_box<T>(const T*, uint64_t, uint64_t, const Box&, T*, uint64_t, uint64_t, cudaStream_t); \
     template int launch_coef_to_natural<T>(const T*, const Box&, const Box&, T*, cudaStream_t);                     \
     template int launch_reordered_to_natural<T>(const T*, const Box&, const Box&, T*, cudaStream_t);                \
-    template int launch_l2_correction<T>(const T*, const Box&, T*, T*, T*, const T* const[3], cudaStream_t);        \
+    template int launch_l2_correction<T>(const T*, const Box&, T*, T*, T*, const T* const[3], cudaStream_t,      \
+                                         const T*, const Box*);                                                     \
     template int launch_add_box<T>(T*, uint64_t, uint64_t, const T*, const Box&, T, cudaStream_t);                  \
     template int launch_interleave<T>(T*, uint64_t, uint64_t, const Box&, const Box&, T*, bool, cudaStream_t);
 INST(float)

@@ -101,7 +101,7 @@ __global__ void k_fill_u32(uint32_t* dst, uint64_t n, uint32_t v) {
 
 int launch_gr_pack(const void* const* planes, const uint32_t* sizes, int B, uint64_t nblocks, const uint8_t* rbs,
                    int word_bytes, uint8_t* dst, cudaStream_t st) {
-    dim3 grid(kSMs, B);
+    dim3 grid(device_sms(), B);
     if (word_bytes == 4) k_gr_pack<uint32_t><<<grid, 256, 0, st>>>((const uint32_t* const*)planes, sizes, B, nblocks, rbs, dst);
     else k_gr_pack<uint64_t><<<grid, 256, 0, st>>>((const uint64_t* const*)planes, sizes, B, nblocks, rbs, dst);
     PRODM_CHECK_LAUNCH("k_gr_pack");

@@ -7,8 +7,12 @@ import subprocess
 
 import pytest
 
+import importlib
+
+build_oracle = importlib.import_module("oracle.build_oracle")
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INC = "/root/reference/include"
+REF_INC = os.path.join(build_oracle.reference_tree(), "include")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_INC), reason="reference headers not present")
