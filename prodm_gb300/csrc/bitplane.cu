@@ -148,6 +148,8 @@ __global__ void __launch_bounds__(256, 3) k_nb_encode32_levels(const ChunkSeg* _
 // each lane stores its four transposed words of a step as one 16-byte store
 // (conflict-free: rows differ by 65 16-byte units) and the chunk's plane runs
 // leave with 16-byte copies
+static_assert(errtab::kSlotsPad == kErrRecWords && errtab::WORDS + 16 <= errtab::kSlotsPad,
+              "record width of the table encoders");
 constexpr int ERR_LD = 260;
 constexpr int kErrTileBytes = 32 * ERR_LD * 4;
 constexpr size_t kErrSmemNB = (size_t)kErrTileBytes + 8 * sizeof(errtab::WarpQ) +
@@ -184,6 +186,7 @@ __device__ __forceinline__ void nb_err_steps(const float* __restrict__ xw, int64
         }
         if (j0 + 4 < 32) load4(j0 + 4);                            // next step's values in flight
         uint32_t t[4], nb[4];
+        bool small[4];
 #pragma unroll
         for (int g = 0; g < 4; g++) {
             const bool ok = FULLW || (j0 + g) * 32 < rem;
@@ -192,10 +195,9 @@ __device__ __forceinline__ void nb_err_steps(const float* __restrict__ xw, int64
             t[g] = ok ? tq : 0u;                                          // padding adds nothing
             const bool big = fabsf(sh[g]) >= 8388608.f;
             acc.add_big_square(sh[g], big);                               // padding is 0: never big
-            const bool small = ok && !big;
-            const uint32_t bal = __ballot_sync(FULL, small);
-            if (bal) errtab::enqueue(wq, head, qn, bal, small, sh[g], lane);
+            small[g] = ok && !big;
         }
+        errtab::enqueue4(wq, head, qn, small, sh, lane);
         errtab::drain_full<true>(wq, head, qn, lane);
         acc.add4(t[0], t[1], t[2], t[3]);
         uint32_t w[4];
@@ -224,25 +226,37 @@ __device__ __forceinline__ void nb_encode32_chunk_err(const float* __restrict__ 
         nb_err_steps<FULLB, true>(xw, rem, B, se, fast, scale, trow, acc, wq, head, qn);
     else
         nb_err_steps<FULLB, false>(xw, rem, B, se, fast, scale, trow, acc, wq, head, qn);
-    __syncthreads();
+    __syncwarp();
+    // the warp writes out its own 32 columns of the tile (blocks warp*32 ..
+    // warp*32 + 31 of the chunk), so warps never wait for one another
     const int nvalid = (int)((nblocks - cb0) < (uint64_t)NB_CHUNK ? (nblocks - cb0) : NB_CHUNK);
+    const int wb = warp * 32;
     if ((stride & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
-        // 16-byte runs; words past nvalid are zero (blocks past the level) and
-        // land in the plane row's padding to a multiple of four words
+        // 16-byte runs, four planes per instruction (8 lanes per plane); words
+        // past nvalid are zero (blocks past the level) and land in the plane
+        // row's padding to a multiple of four words
         const int nq = (nvalid + 3) >> 2;
-        for (int p = warp; p < B; p += 8) {
-            uint4* dst = reinterpret_cast<uint4*>(out + (uint64_t)p * stride + cb0);
-            const uint4* row = reinterpret_cast<const uint4*>(tile + p * ERR_LD);
-            for (int j = lane; j < nq; j += 32) dst[j] = row[j];
+        const int q = lane & 7;
+        const bool ok = wb / 4 + q < nq;
+#pragma unroll
+        for (int p0 = 0; p0 < 32; p0 += 4) {
+            const int p = p0 + (lane >> 3);
+            if (p0 < B) {
+                const uint4 v = reinterpret_cast<const uint4*>(tile + p * ERR_LD + wb)[q];
+                if (ok && p < B) reinterpret_cast<uint4*>(out + (uint64_t)p * stride + cb0 + wb)[q] = v;
+            }
         }
     } else {
-        for (int p = warp; p < B; p += 8) {
-            uint32_t* dst = out + (uint64_t)p * stride + cb0;
-            const uint32_t* row = tile + p * ERR_LD;
-            for (int j = lane; j < nvalid; j += 32) dst[j] = row[j];
+        const bool ok = wb + lane < nvalid;
+        for (int p = 0; p < B; p++) {
+            const uint32_t v = tile[p * ERR_LD + wb + lane];
+            if (ok) out[(uint64_t)p * stride + cb0 + wb + lane] = v;
         }
     }
-    __syncthreads();
+    // the warp's own barrier (id 1 + warp, 32 threads) before its columns
+    // are written again; as a barrier it also keeps the compiler from
+    // interleaving the next chunk's loads with this copy (which spills)
+    asm volatile("bar.sync %0, 32;" ::"r"(warp + 1) : "memory");
 }
 
 // Every level (segment) of one fp32 field with tables in one launch. Records
@@ -319,59 +333,77 @@ __global__ void __launch_bounds__(256, 2) k_nb_encode32_err(const ChunkSeg* __re
     }
 }
 
-// Tables of every level from the CTA records: one CTA per level; warp w sums
-// record slots w, w + 8, ... (lane-strided over records, then a fixed
-// butterfly, so the doubles are summed in a fixed order), then thread i
+// Tables of every level from the CTA records: one CTA of 1024 threads per
+// level. Thread (k, i), k < 5, sums record word i over records k, k + 5, ..
+// (loads of all words in flight at once; low words of 128-bit sums also
+// count their carries), then thread i combines the five partial sums in k
+// order (so the doubles are summed in a fixed order) and thread i <= B
 // computes entry i. keys (or exp_arg when keys is null) give the level
 // exponent, exp_add the encoder's offset (2 for negabinary).
+constexpr int kFinalParts = 5;
+static_assert(kFinalParts * errtab::kSlotsPad <= 1024, "one thread per (part, record word)");
+
 template <bool NB>
-__global__ void __launch_bounds__(256) k_errtab_final(const unsigned long long* __restrict__ recs, int nrec, int B,
-                                                      const ChunkSeg* __restrict__ segs, ChunkSeg one, int exp_arg,
-                                                      int exp_add, double* __restrict__ out) {
+__global__ void __launch_bounds__(1024) k_errtab_final(const unsigned long long* __restrict__ recs, int nrec, int B,
+                                                       const ChunkSeg* __restrict__ segs, ChunkSeg one, int exp_arg,
+                                                       int exp_add, double* __restrict__ out) {
+    __shared__ unsigned long long P[kFinalParts][errtab::kSlotsPad];    // partial sums (u64 words or double bits)
+    __shared__ unsigned long long Cy[kFinalParts][errtab::kSlotsPad];   // carries out of the low words
     __shared__ unsigned long long R[errtab::kSlotsPad];
     const int l = blockIdx.x;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const unsigned long long* rl = recs + (size_t)l * nrec * errtab::kSlotsPad;
-    for (int i = warp; i < errtab::WORDS; i += nw) {
-        const bool pair = i >= errtab::S6A && i < errtab::S5;              // 128-bit sums
-        if (pair && ((i - errtab::S6A) & 1)) continue;                    // high words go with their low word
-        const bool dbl = i >= errtab::S5;
-        if (dbl) {
-            double v = 0;
-            for (int r = lane; r < nrec; r += 32) v += __longlong_as_double(rl[(size_t)r * errtab::kSlotsPad + i]);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-            if (lane == 0) R[i] = __double_as_longlong(v);
-        } else if (pair) {
-            unsigned long long lo = 0, hi = 0;
-            for (int r = lane; r < nrec; r += 32) {
-                const unsigned long long* p = rl + (size_t)r * errtab::kSlotsPad + i;
-                const unsigned long long o = lo;
-                lo += p[0];
-                hi += p[1] + (lo < o ? 1 : 0);
+    const int t = threadIdx.x;
+    if (t < kFinalParts * errtab::kSlotsPad) {
+        const int k = t / errtab::kSlotsPad, i = t - k * errtab::kSlotsPad;
+        if (i < errtab::WORDS) {
+            const unsigned long long* p = rl + i;
+            if (errtab::slot_kind(i) == 3) {
+                double v = 0;
+#pragma unroll 8
+                for (int r = k; r < nrec; r += kFinalParts) v += __longlong_as_double(p[(size_t)r * errtab::kSlotsPad]);
+                P[k][i] = __double_as_longlong(v);
+            } else {
+                unsigned long long v = 0, c = 0;
+#pragma unroll 8
+                for (int r = k; r < nrec; r += kFinalParts) {
+                    const unsigned long long o = v;
+                    v += p[(size_t)r * errtab::kSlotsPad];
+                    c += v < o ? 1 : 0;
+                }
+                P[k][i] = v;
+                Cy[k][i] = c;
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long l2 = __shfl_xor_sync(FULL, lo, o), h2 = __shfl_xor_sync(FULL, hi, o);
-                const unsigned long long ol = lo;
-                lo += l2;
-                hi += h2 + (lo < ol ? 1 : 0);
-            }
-            if (lane == 0) { R[i] = lo; R[i + 1] = hi; }
-        } else {
-            unsigned long long v = 0;
-            for (int r = lane; r < nrec; r += 32) v += rl[(size_t)r * errtab::kSlotsPad + i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-            if (lane == 0) R[i] = v;
         }
+    }
+    __syncthreads();
+    if (t < errtab::WORDS) {
+        const int kind = errtab::slot_kind(t);
+        if (kind == 3) {
+            double v = 0;
+            for (int k = 0; k < kFinalParts; k++) v += __longlong_as_double(P[k][t]);
+            R[t] = __double_as_longlong(v);
+        } else if (kind != 2) {
+            unsigned long long v = 0, c = 0;
+            for (int k = 0; k < kFinalParts; k++) {
+                const unsigned long long o = v;
+                v += P[k][t];
+                c += Cy[k][t] + (v < o ? 1 : 0);
+            }
+            R[t] = v;
+            Cy[0][t] = c;   // carries into the high word (read by thread t + 1 after the barrier)
+        }
+    }
+    __syncthreads();
+    if (t < errtab::WORDS && errtab::slot_kind(t) == 2) {
+        unsigned long long v = Cy[0][t - 1];
+        for (int k = 0; k < kFinalParts; k++) v += P[k][t];
+        R[t] = v;
     }
     __syncthreads();
     const uint32_t* key = segs ? segs[l].key : one.key;
     const uint64_t n = segs ? segs[l].n : one.n;
     const int e = (key ? frexp_exp(__uint_as_float(*key)) : exp_arg) + exp_add;
-    for (int i = threadIdx.x; i <= B; i += blockDim.x)
-        out[(size_t)l * (B + 1) + i] = errtab::table_entry<NB>(R, n, B, e, i);
+    for (int i = t; i <= B; i += blockDim.x) out[(size_t)l * (B + 1) + i] = errtab::table_entry<NB>(R, n, B, e, i);
 }
 
 // Every level of one fp32 field decoded in one launch (segments = levels in
@@ -799,8 +831,9 @@ __global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x,
         errtab::zero_q(wq[warp], lane);
     }
     for (int j0 = 0; j0 < GR_BPW; j0 += 4) {
-        float sh[4];
+        float sh[4], mag[4];
         uint32_t q[4], sign[4];
+        bool small[4];
 #pragma unroll
         for (int g = 0; g < 4; g++) {
             const uint64_t i = (b0 + j0 + g) * 32 + lane;
@@ -812,15 +845,14 @@ __global__ void __launch_bounds__(256) k_gr_write32(const float* __restrict__ x,
             q[g] = (uint32_t)(neg ? -fix : fix);
             sign[g] = __ballot_sync(FULL, neg);
             if (ERR) {
-                const float a = fabsf(sh[g]);
-                const bool big = a >= 8388608.f;
-                acc.add_big_square(a, big);                                   // padding is 0: never big
-                const bool small = ok && !big;
-                const uint32_t bal = __ballot_sync(FULL, small);
-                if (bal) errtab::enqueue(wq[warp], head, qn, bal, small, a, lane);
+                mag[g] = fabsf(sh[g]);
+                const bool big = mag[g] >= 8388608.f;
+                acc.add_big_square(mag[g], big);                              // padding is 0: never big
+                small[g] = ok && !big;
             }
         }
         if (ERR) {
+            errtab::enqueue4(wq[warp], head, qn, small, mag, lane);
             errtab::drain_full<false>(wq[warp], head, qn, lane);
             acc.add4(q[0], q[1], q[2], q[3]);
         }
@@ -1148,7 +1180,7 @@ static int nb_err_launch(const ChunkSeg* segs, const ChunkSeg& one, int nseg, ui
     unsigned long long* recs = (unsigned long long*)partial;
     k_nb_encode32_err<<<grid, 256, kErrSmemNB, st>>>(segs, one, nseg, total, B, exp, recs);
     PRODM_CHECK_LAUNCH("k_nb_encode32_err");
-    k_errtab_final<true><<<nseg, 256, 0, st>>>(recs, (int)grid, B, segs, one, exp, 2, errs_out);
+    k_errtab_final<true><<<nseg, 1024, 0, st>>>(recs, (int)grid, B, segs, one, exp, 2, errs_out);
     PRODM_CHECK_LAUNCH("k_errtab_final");
     return PRODM_OK;
 }
@@ -1261,7 +1293,7 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
             ChunkSeg one = {};
             one.n = n;
             one.key = (const uint32_t*)maxkey;
-            k_errtab_final<false><<<1, 256, 0, st>>>(recs, (int)nch, B, nullptr, one, exp, 0, errs_out);
+            k_errtab_final<false><<<1, 1024, 0, st>>>(recs, (int)nch, B, nullptr, one, exp, 0, errs_out);
             PRODM_CHECK_LAUNCH("k_errtab_final");
         } else {
             k_gr_write32<false><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(

@@ -25,13 +25,14 @@
 // * 1 <= |x| < 2^23: m = M * 2^-23 with an integer M, and
 //   (r_k + m)^2 = r_k^2 + 2^-22 r_k M + 2^-46 M^2: the cross sums
 //   sum u_k M = sum_{b<k} 2^b sum_{bit b of t} M and sum M^2 are exact
-//   integers. |x| < 1: r_k = 0,
-//   m = x and x^2 is exact in double. These values (about 5 % of a 32-plane
-//   level) are queued per warp and handled 32 at a time: one lane per value
-//   for their own terms, then one lane per bit b of t for the masked sums.
-// * Doubles (the |x| < 2^23 float-rounded squares and x^2 for |x| < 1) are
-//   summed per lane and reduced in a fixed order, so every table is
-//   bitwise reproducible.
+//   integers; so are the float-rounded squares the reference adds for
+//   entries 0 and B: fl(x^2) * 2^23 (below 2^69) and fl(m^2) * 2^46 (below
+//   2^46). |x| < 1: r_k = 0, m = x, x^2 is exact in double and fl(x^2) is
+//   summed in double. These values (about 5 % of a 32-plane level) are
+//   queued per warp and handled 32 at a time: one lane per value for their
+//   own terms, then one lane per bit b of t for the masked sums.
+// * The only doubles (the |x| < 1 terms, rare) are summed per lane and
+//   reduced in a fixed order, so every table is bitwise reproducible.
 #pragma once
 #include "common.cuh"
 
@@ -47,10 +48,18 @@ constexpr int X = 110;      // 31 x i128: Y_b = sum of M over 1 <= |x| < 2^23 wi
 constexpr int S4 = 172;     // u128: sum M^2
 constexpr int SM = 174;     // i128: sum M
 constexpr int S5 = 176;     // double: sum x^2 over |x| < 1
-constexpr int S6BC = 177;   // double: sum fl(x^2) over |x| < 2^23
-constexpr int S7 = 178;     // double: sum fl(m^2) over |x| < 2^23 (negabinary entry B)
-constexpr int WORDS = 179;
-constexpr int kSlotsPad = 196;   // WORDS + 2 x 8 warps of flush scratch, padded
+constexpr int STINY = 177;  // double: sum fl(x^2) over |x| < 1 (= sum fl(m^2) there)
+constexpr int S6B = 178;    // u128: sum fl(x^2) * 2^23 over 1 <= |x| < 2^23
+constexpr int S7B = 180;    // u128: sum fl(m^2) * 2^46 over 1 <= |x| < 2^23 (negabinary entry B)
+constexpr int WORDS = 182;
+constexpr int kSlotsPad = 200;   // WORDS + 2 x 8 warps of flush scratch, padded
+
+// how the final reduction sums slot i: 0 = u64, 1 = low word of a 128-bit
+// sum (its high word follows), 2 = high word, 3 = double
+__host__ __device__ constexpr int slot_kind(int i) {
+    return (i >= S6A && i < S5) || (i >= S6B && i < WORDS) ? (((i - (i >= S6B ? S6B : S6A)) & 1) ? 2 : 1)
+           : (i == S5 || i == STINY) ? 3 : 0;
+}
 
 __host__ __device__ constexpr int cr_slot(int j, int J, int s) {
     return J == 1 ? (s - 1) : J == 2 ? 8 + 8 * j + (s - 1) : 24 + 7 * j + (s - 1);
@@ -66,7 +75,8 @@ struct WarpQ {
     long long sm[32];
     unsigned long long xlo[32];
     long long xhi[32];
-    double s5[32], s6bc[32], s7[32];
+    unsigned long long s6lo[32], s6hi[32], s7[32];
+    double s5[32], stiny[32];
 };
 
 // per-lane register sums
@@ -132,9 +142,31 @@ __device__ __forceinline__ void zero_q(WarpQ& q, int lane) {
     q.sm[lane] = 0;
     q.xlo[lane] = 0;
     q.xhi[lane] = 0;
-    q.s5[lane] = 0;
-    q.s6bc[lane] = 0;
+    q.s6lo[lane] = 0;
+    q.s6hi[lane] = 0;
     q.s7[lane] = 0;
+    q.s5[lane] = 0;
+    q.stiny[lane] = 0;
+}
+
+// fl(x^2) * 2^23 for 1 <= |x| < 2^23 as (lo, hi): the float square is in
+// [1, 2^46), its significand shifted left by its exponent (0..45)
+__device__ __forceinline__ void square_2p23(float x, unsigned long long& lo, unsigned long long& hi) {
+    const uint32_t b = __float_as_uint(__fmul_rn(x, x));
+    const unsigned long long mant = (b & 0x7fffffu) | 0x800000u;
+    const int sh = (int)(b >> 23) - 127;
+    lo = mant << sh;
+    hi = sh ? mant >> (64 - sh) : 0ull;
+}
+
+// fl(m^2) * 2^46 for a fraction m = M * 2^-23, |M| < 2^23: zero, or a float
+// in [2^-46, 1) whose value times 2^46 is an integer (the significand
+// shifted by its exponent - 104, in -23..22; a right shift drops zeros only)
+__device__ __forceinline__ unsigned long long frac_square_2p46(float m) {
+    const uint32_t b = __float_as_uint(__fmul_rn(m, m));
+    const unsigned long long mant = (b & 0x7fffffu) | 0x800000u;
+    const int sh = (int)(b >> 23) - 104;
+    return b == 0 ? 0ull : (sh >= 0 ? mant << sh : mant >> -sh);
 }
 
 // Process cnt (<= 32) queued values starting at ring slot head. NB: values are
@@ -151,14 +183,19 @@ __device__ __forceinline__ void run_batch(WarpQ& q, uint32_t head, int cnt, int 
         const int32_t iq = (int32_t)x;                       // |x| < 2^23
         const float m = __fsub_rn(x, (float)iq);             // exact fraction
         t = NB ? (uint32_t)iq + 0xaaaaaaaau : (uint32_t)iq;
-        q.s6bc[lane] += (double)__fmul_rn(x, x);
-        if (NB) q.s7[lane] += (double)__fmul_rn(m, m);
         if (fabsf(x) >= 1.f) {
             M = (int32_t)(m * 8388608.f);                     // exact: m is a multiple of 2^-23
             q.s4[lane] += (unsigned long long)((long long)M * M);
             q.sm[lane] += M;
-        } else {
+            unsigned long long lo, hi;
+            square_2p23(x, lo, hi);
+            const unsigned long long o = q.s6lo[lane];
+            q.s6lo[lane] = o + lo;
+            q.s6hi[lane] += hi + (o + lo < o ? 1ull : 0ull);
+            if (NB) q.s7[lane] += frac_square_2p46(m);
+        } else {                                              // m = x
             q.s5[lane] += (double)x * (double)x;              // exact in double
+            q.stiny[lane] += (double)__fmul_rn(x, x);
         }
     }
     q.batch[lane] = make_uint2(t, (uint32_t)M);
@@ -173,10 +210,20 @@ __device__ __forceinline__ void run_batch(WarpQ& q, uint32_t head, int cnt, int 
     __syncwarp();
 }
 
-__device__ __forceinline__ void enqueue(WarpQ& q, uint32_t& head, int& qn, uint32_t bal, bool mine, float v,
-                                        int lane) {
-    if (mine) q.ring[(head + qn + __popc(bal & ((1u << lane) - 1u))) & (kRing - 1)] = v;
-    qn += __popc(bal);
+// Queue the values of one four-value step whose flag is set (|x| < 2^23) in
+// one pass: the four ballots give each value its ring slot, the stores are
+// predicated, and no branch depends on the data. qn is warp-uniform.
+__device__ __forceinline__ void enqueue4(WarpQ& q, uint32_t head, int& qn, const bool (&small)[4],
+                                         const float (&v)[4], int lane) {
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t pos = head + (uint32_t)qn;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, small[g]);
+        if (small[g]) q.ring[(pos + __popc(bal & lt)) & (kRing - 1)] = v[g];
+        pos += __popc(bal);
+    }
+    qn = (int)(pos - head);
 }
 
 template <bool NB>
@@ -235,26 +282,35 @@ __device__ __forceinline__ void flush(Lane& a, WarpQ* wq, unsigned long long* re
         r[0] = o + lo;
         r[1] = (unsigned long long)((long long)r[1] + hi + ((o + lo) < o ? 1 : 0));
     } else if (threadIdx.x == 32) {    // fixed-order double sums, 128-bit integer sums
-        double s5 = 0, s6 = 0, s7 = 0;
-        unsigned long long s4lo = 0, s4hi = 0, smlo = 0;
+        double s5 = 0, st = 0;
+        unsigned long long s4lo = 0, s4hi = 0, smlo = 0, s6lo = 0, s6hi = 0, s7lo = 0, s7hi = 0;
         long long smhi = 0;
         for (int w = 0; w < nw; w++)
             for (int l = 0; l < 32; l++) {
                 s5 += wq[w].s5[l];
-                s6 += wq[w].s6bc[l];
-                s7 += wq[w].s7[l];
-                const unsigned long long o = s4lo;
+                st += wq[w].stiny[l];
+                unsigned long long o = s4lo;
                 s4lo += wq[w].s4[l];
                 s4hi += s4lo < o ? 1 : 0;
                 add128(smlo, smhi, wq[w].sm[l]);
+                o = s6lo;
+                s6lo += wq[w].s6lo[l];
+                s6hi += wq[w].s6hi[l] + (s6lo < o ? 1 : 0);
+                o = s7lo;
+                s7lo += wq[w].s7[l];
+                s7hi += s7lo < o ? 1 : 0;
             }
         rec[S5] = __double_as_longlong(__longlong_as_double(rec[S5]) + s5);
-        rec[S6BC] = __double_as_longlong(__longlong_as_double(rec[S6BC]) + s6);
-        rec[S7] = __double_as_longlong(__longlong_as_double(rec[S7]) + s7);
-        unsigned long long o = rec[S4];
-        rec[S4] = o + s4lo;
-        rec[S4 + 1] += s4hi + (rec[S4] < o ? 1 : 0);
-        o = rec[SM];
+        rec[STINY] = __double_as_longlong(__longlong_as_double(rec[STINY]) + st);
+        auto add_u128 = [&](int slot, unsigned long long lo, unsigned long long hi) {
+            const unsigned long long o = rec[slot];
+            rec[slot] = o + lo;
+            rec[slot + 1] += hi + (rec[slot] < o ? 1 : 0);
+        };
+        add_u128(S4, s4lo, s4hi);
+        add_u128(S6B, s6lo, s6hi);
+        add_u128(S7B, s7lo, s7hi);
+        const unsigned long long o = rec[SM];
         rec[SM] = o + smlo;
         rec[SM + 1] = (unsigned long long)((long long)rec[SM + 1] + smhi + (rec[SM] < o ? 1 : 0));
     }
@@ -295,10 +351,10 @@ template <bool NB>
 __device__ double table_entry(const unsigned long long* R, uint64_t n, int B, int e, int i) {
     const uint32_t A = NB ? 0xaaaaaaaau : 0u;
     double v;
-    if (i == 0) {
-        v = u128_to_double(rd_u128(R + S6A)) * 8388608.0 + __longlong_as_double(R[S6BC]);
+    if (i == 0) {   // (S6A * 2^46 + S6B) * 2^-23: one exact 128-bit sum
+        v = u128_to_double((rd_u128(R + S6A) << 46) + rd_u128(R + S6B)) * 0x1p-23 + __longlong_as_double(R[STINY]);
     } else if (i == B) {
-        v = NB ? __longlong_as_double(R[S7])
+        v = NB ? u128_to_double(rd_u128(R + S7B)) * 0x1p-46 + __longlong_as_double(R[STINY])
                : u128_to_double(rd_u128(R + S4)) * 0x1p-46 + __longlong_as_double(R[S5]);
     } else {
         const int k = B - i;

@@ -67,7 +67,7 @@ int launch_max_collect(const T* bounds, int nl, int B, double* out, cudaStream_t
 constexpr int kPartialSlots = kSMs * 4;   // per-CTA partial error tables of the fused collectors
 // bytes of `parts` per-CTA partials: B + 1 doubles (fp64 tables, squared-error
 // collector) or one record of the exact fp32 tables (errtab.cuh)
-constexpr int kErrRecWords = 196;   // errtab::kSlotsPad
+constexpr int kErrRecWords = 200;   // errtab::kSlotsPad
 inline uint64_t partial_bytes(uint64_t parts, int B) {
     return parts * (uint64_t)(kErrRecWords > B + 1 ? kErrRecWords : B + 1) * 8;
 }

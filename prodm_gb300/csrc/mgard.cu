@@ -260,9 +260,35 @@ __global__ void k_reordered_to_natural(const T* __restrict__ rin, Box F, Box C, 
     }
 }
 
+// Right-hand side of the coarse projection at coarse node m of a line of nf
+// fine values: b = (M_f s)[c] + 1/2 (M_f s)[c-1] + 1/2 (M_f s)[c+1] with c
+// its fine position, the neighbours only when they are not coarse nodes, and
+// (M_f s)[x] = dg(x) s[x] + (s[x-1] + s[x+1]) / 6 (P1 mass matrix, dg = 1/3 at
+// the ends, else 2/3; s = 0 outside the line). Window: the fine values at
+// c-2 .. c+2. For double data an interior node takes the same sum regrouped as
+// one 5-point stencil, 5/6 s[c] + 1/2 (s[c-1] + s[c+1]) + 1/12 (s[c-2] + s[c+2]),
+// a third of the FP64 operations; float keeps the term order above.
+template <class W>
+__device__ __forceinline__ W l2_rhs(W sm2, W sm1, W s0, W s1, W s2, uint32_t c, uint32_t nf) {
+    if (sizeof(W) == 8 && c >= 2 && c + 3 <= nf && (c & 1u) == 0)
+        return (W)(5.0 / 6.0) * s0 + (W)0.5 * (sm1 + s1) + (W)(1.0 / 12.0) * (sm2 + s2);
+    auto mf = [&](W l, W x, W r, uint32_t pos) {
+        const W dg = (pos == 0 || pos == nf - 1) ? (W)1 / 3 : (W)2 / 3;
+        return dg * x + (l + r) / 6;
+    };
+    W b = mf(sm1, s0, s1, c);
+    if (c > 0 && !is_coarse(c - 1, nf)) b += (W)0.5 * mf(sm2, sm1, s0, c - 1);
+    if (c + 1 < nf && !is_coarse(c + 1, nf)) b += (W)0.5 * mf(s0, s1, s2, c + 1);
+    return b;
+}
+
 // One dim of the L2 projection: dst = M_c^-1 P^T M_f src along dim d.
-// Thread per line; forward sweep stores d'_m in dst, backward sweep in place.
-// cp / inv_den: Thomas factors of the coarse mass matrix (length nc, in W).
+// Thread per line (consecutive threads on consecutive lines of the two
+// faster dims, so every access is coalesced across a warp); the fine values
+// stream through a 5-value window (two loads per coarse node, issued one
+// node ahead), the forward sweep stores d'_m in dst, the backward sweep
+// substitutes in place. cp / lo_w / inv_den: Thomas factors of the coarse
+// mass matrix (length nc, in W).
 template <class T, class W>
 __global__ void k_l2_line(const T* __restrict__ src, Box S, int d, T* __restrict__ dst, Box D, const W* __restrict__ cp,
                           const W* __restrict__ lo_w, const W* __restrict__ inv_den) {
@@ -282,22 +308,25 @@ __global__ void k_l2_line(const T* __restrict__ src, Box S, int d, T* __restrict
             for (uint32_t x = 0; x < nf; x++) dl[x * dt] = sl[x * st];
             continue;
         }
-        auto mf = [&](uint32_t x) -> W {   // (M_f line)[x], spacing 1
-            W c = (W)sl[x * st];
-            W l = x > 0 ? (W)sl[(x - 1) * st] : (W)0;
-            W r = x + 1 < nf ? (W)sl[(x + 1) * st] : (W)0;
-            W dg = (x == 0 || x == nf - 1) ? (W)1 / 3 : (W)2 / 3;
-            return dg * c + (l + r) / 6;
-        };
+        auto at = [&](int64_t x) -> W { return (x >= 0 && x < (int64_t)nf) ? (W)sl[x * st] : (W)0; };
+        // regular coarse nodes sit at c = 2m; with an even nf the last one is nf - 1
+        const uint32_t nreg = (nf & 1u) ? nc : nc - 1;
+        W sm2 = 0, sm1 = 0, s0 = at(0), s1 = at(1), s2 = at(2);
         W prev = 0;
-        for (uint32_t m = 0; m < nc; m++) {
-            uint32_t c = fine_of_coarse(m, nf, nc);
-            W b = mf(c);
-            if (c > 0 && !is_coarse(c - 1, nf)) b += (W)0.5 * mf(c - 1);
-            if (c + 1 < nf && !is_coarse(c + 1, nf)) b += (W)0.5 * mf(c + 1);
-            W dp = (m == 0) ? b * inv_den[0] : (b - lo_w[m] * prev) * inv_den[m];
+        for (uint32_t m = 0; m < nreg; m++) {
+            const uint32_t c = 2 * m;
+            const W n3 = at((int64_t)c + 3), n4 = at((int64_t)c + 4);   // the next node's new values
+            const W b = l2_rhs<W>(sm2, sm1, s0, s1, s2, c, nf);
+            const W dp = (m == 0) ? b * inv_den[0] : (b - lo_w[m] * prev) * inv_den[m];
             dl[m * dt] = (T)dp;
             prev = dp;
+            sm2 = s0; sm1 = s1; s0 = s2; s1 = n3; s2 = n4;
+        }
+        if (nreg < nc) {   // even nf: the last coarse node is the last fine node
+            const uint32_t c = nf - 1, m = nc - 1;
+            const W b = l2_rhs<W>(at((int64_t)c - 2), at((int64_t)c - 1), at(c), (W)0, (W)0, c, nf);
+            const W dp = (b - lo_w[m] * prev) * inv_den[m];
+            dl[m * dt] = (T)dp;
         }
         W z = (W)dl[(nc - 1) * dt];
         for (uint32_t m = nc - 1; m-- > 0;) {
@@ -308,19 +337,22 @@ __global__ void k_l2_line(const T* __restrict__ src, Box S, int d, T* __restrict
 }
 
 // The dim-2 (contiguous) pass of the L2 projection with shared-memory staging:
-// one warp per 32 lines (fine rows (x0, x1) of F). Forward sweep: tiles of 64
-// fine columns plus two halo columns each side are staged row by row with
-// coalesced loads; lane r then sweeps row r's coarse nodes of the tile
-// (right-hand side from the 5-point neighbourhood, Thomas forward step) into
-// an output tile stored with coalesced writes. Backward sweep: the stored
-// tiles come back from the end, lane r substitutes back along its row, and
-// they are stored again. PACKED: the rows are read straight from the level's
+// one warp per 32 lines (fine rows (x0, x1) of F). Forward sweep: tiles of 32
+// fine columns plus two halo columns each side are staged with coalesced
+// loads (the 32 x 36 values as one flat loop); lane r then sweeps row r's
+// coarse nodes of the tile (right-hand side from the 5-point neighbourhood,
+// Thomas forward step) into an output tile stored with coalesced writes.
+// Backward sweep: the stored values come back from the end in 32-node chunks
+// (in the input tile, free by then), lane r substitutes back along its row,
+// and they are stored again. About 14 KB of shared memory per warp, so about
+// 15 warps share an SM. PACKED: the rows are read straight from the level's
 // packed coefficients (a natural row is an even/odd split of one contiguous
 // run of interleaved ranks; coarse nodes of rows inside the coarse box are
 // zero), so no natural-order copy is needed; else from a natural field.
-constexpr int L2_TILE = 64;                 // fine columns per tile
-constexpr int L2_IN_LD = L2_TILE + 5;       // staged row: 2 + 64 + 2 columns, odd stride (no bank conflicts)
-constexpr int L2_OUT_LD = 35;               // up to 33 coarse nodes per tile, odd stride
+constexpr int L2_TILE = 32;                 // fine columns per tile
+constexpr int L2_STAGE = L2_TILE + 4;       // staged columns: 2 + 32 + 2
+constexpr int L2_IN_LD = L2_STAGE + 1;      // odd stride (no bank conflicts); also holds 32-node chunks
+constexpr int L2_OUT_LD = 17;               // up to 17 coarse nodes per tile, odd stride
 
 template <class T, class W, bool PACKED>
 __global__ void __launch_bounds__(32) k_l2_rows(const T* __restrict__ src, Box F, Box C, T* __restrict__ dst,
@@ -335,97 +367,98 @@ __global__ void __launch_bounds__(32) k_l2_rows(const T* __restrict__ src, Box F
     const uint64_t l0 = (uint64_t)blockIdx.x * 32;
     if (l0 >= lines) return;
     const int nl = (int)min((uint64_t)32, lines - l0);
-    // row r's source: base offset, whether it lies inside the coarse box
-    auto row_src = [&](int r, uint64_t& base, bool& cc) {
-        const uint64_t li = l0 + r;
+    // each row's source (base offset, inside the coarse box or not), computed
+    // once by its lane
+    __shared__ uint64_t s_base[32];
+    __shared__ int s_cc[32];
+    if (lane < nl) {
+        const uint64_t li = l0 + lane;
         const uint32_t x0 = (uint32_t)(li / F.n[1]), x1 = (uint32_t)(li - (uint64_t)x0 * F.n[1]);
         if (PACKED) {
             const uint32_t r0 = reord(x0, F.n[0], C.n[0]), r1 = reord(x1, F.n[1], C.n[1]);
-            cc = r0 < C.n[0] && r1 < C.n[1];
-            base = level_rank(r0, r1, cc ? c2n : 0u, F, C);
+            const bool cc = r0 < C.n[0] && r1 < C.n[1];
+            s_cc[lane] = cc;
+            s_base[lane] = level_rank(r0, r1, cc ? c2n : 0u, F, C);
         } else {
-            cc = false;
-            base = li * nf;
+            s_cc[lane] = 0;
+            s_base[lane] = li * nf;
         }
-    };
-    auto fine_at = [&](uint64_t base, bool cc, int64_t x) -> W {   // natural column x of a row, 0 outside
+    }
+    __syncwarp();
+    auto fine_at = [&](int r, int64_t x) -> W {   // natural column x of row r, 0 outside
         if (x < 0 || x >= (int64_t)nf) return (W)0;
+        const uint64_t base = s_base[r];
         if (!PACKED) return (W)src[base + x];
         const uint32_t xx = (uint32_t)x;
         const uint32_t r2 = reord(xx, nf, c2n);
-        if (cc) return is_coarse(xx, nf) ? (W)0 : (W)src[base + (r2 - c2n)];
+        if (s_cc[r]) return is_coarse(xx, nf) ? (W)0 : (W)src[base + (r2 - c2n)];
         return (W)src[base + r2];
     };
+    T* drow = dst + l0 * nc;                       // the warp's rows are consecutive in dst
     if (nc == nf) {   // no coarse subset along this dim: the projection is the identity
-        for (int r = 0; r < nl; r++) {
-            uint64_t base;
-            bool cc;
-            row_src(r, base, cc);
-            for (uint32_t j = lane; j < nf; j += 32) dst[(l0 + r) * nc + j] = (T)fine_at(base, cc, j);
-        }
+        for (int r = 0; r < nl; r++)
+            for (uint32_t j = lane; j < nf; j += 32) drow[(uint64_t)r * nc + j] = (T)fine_at(r, j);
         return;
     }
     const uint32_t ntiles = (nf + L2_TILE - 1) / L2_TILE;
     W prev = 0;
-    uint32_t m = 0;                                    // next coarse node of this lane's row
+    uint32_t m = 0;                                    // next coarse node of the tile
     for (uint32_t t = 0; t < ntiles; t++) {
         const int64_t x0 = (int64_t)t * L2_TILE - 2;   // first staged column
-        for (int r = 0; r < nl; r++) {
-            uint64_t base;
-            bool cc;
-            row_src(r, base, cc);
-            for (int j = lane; j < L2_TILE + 4; j += 32) sin_[r * L2_IN_LD + j] = fine_at(base, cc, x0 + j);
+        for (int i = lane; i < nl * L2_STAGE; i += 32) {
+            const int r = i / L2_STAGE, j = i - r * L2_STAGE;
+            sin_[r * L2_IN_LD + j] = fine_at(r, x0 + j);
         }
         __syncwarp();
-        // coarse nodes whose fine position falls in [64t, 64t + 64)
+        // coarse nodes whose fine position falls in [32t, 32t + 32): the same
+        // range for every row
         const uint32_t xe = min((uint32_t)(t + 1) * L2_TILE, nf);
         const uint32_t mt0 = m;
+        uint32_t mt1 = mt0;
+        while (mt1 < nc && fine_of_coarse(mt1, nf, nc) < xe) mt1++;
+        m = mt1;
         if (lane < nl) {
             const W* s = sin_ + lane * L2_IN_LD;
-            auto sv = [&](int64_t x) -> W { return s[x - x0]; };
-            auto mf = [&](int64_t x) -> W {           // (M_f line)[x]
-                const W dg = (x == 0 || x == (int64_t)nf - 1) ? (W)1 / 3 : (W)2 / 3;
-                return dg * sv(x) + (sv(x - 1) + sv(x + 1)) / 6;
-            };
-            for (uint32_t mm = mt0; mm < nc; mm++) {
+            for (uint32_t mm = mt0; mm < mt1; mm++) {
                 const uint32_t c = fine_of_coarse(mm, nf, nc);
-                if (c >= xe) break;
-                W b = mf(c);
-                if (c > 0 && !is_coarse(c - 1, nf)) b += (W)0.5 * mf((int64_t)c - 1);
-                if (c + 1 < nf && !is_coarse(c + 1, nf)) b += (W)0.5 * mf((int64_t)c + 1);
+                const W* w = s + ((int64_t)c - x0);   // staged columns c-2 .. c+2
+                const W b = l2_rhs<W>(w[-2], w[-1], w[0], w[1], w[2], c, nf);
                 const W dp = (mm == 0) ? b * inv_den[0] : (b - lo_w[mm] * prev) * inv_den[mm];
                 sout[lane * L2_OUT_LD + (mm - mt0)] = dp;
                 prev = dp;
             }
         }
-        // the tile's coarse range is the same for every row
-        uint32_t mt1 = mt0;
-        while (mt1 < nc && fine_of_coarse(mt1, nf, nc) < xe) mt1++;
-        m = mt1;
         __syncwarp();
-        for (int r = 0; r < nl; r++)
-            for (uint32_t j = lane; j < mt1 - mt0; j += 32)
-                dst[(l0 + r) * nc + mt0 + j] = (T)sout[r * L2_OUT_LD + j];
+        const int cnt = (int)(mt1 - mt0);
+        for (int i = lane; i < nl * cnt; i += 32) {
+            const int r = i / cnt, j = i - r * cnt;
+            drow[(uint64_t)r * nc + mt0 + j] = (T)sout[r * L2_OUT_LD + j];
+        }
         __syncwarp();
     }
-    // backward substitution, tiles from the end
+    // backward substitution, 32-node chunks from the end, in the input tile
     W z = 0;
     uint32_t mhi = nc;
     while (mhi > 0) {
         const uint32_t mlo = mhi > 32 ? mhi - 32 : 0;
-        for (int r = 0; r < nl; r++)
-            for (uint32_t j = lane; j < mhi - mlo; j += 32) sout[r * L2_OUT_LD + j] = (W)dst[(l0 + r) * nc + mlo + j];
+        const int cnt = (int)(mhi - mlo);
+        for (int i = lane; i < nl * cnt; i += 32) {
+            const int r = i / cnt, j = i - r * cnt;
+            sin_[r * L2_IN_LD + j] = (W)drow[(uint64_t)r * nc + mlo + j];
+        }
         __syncwarp();
         if (lane < nl) {
-            W* o = sout + lane * L2_OUT_LD;
+            W* o = sin_ + lane * L2_IN_LD;
             for (uint32_t mm = mhi; mm-- > mlo;) {
                 z = (mm == nc - 1) ? o[mm - mlo] : o[mm - mlo] - cp[mm] * z;
                 o[mm - mlo] = z;
             }
         }
         __syncwarp();
-        for (int r = 0; r < nl; r++)
-            for (uint32_t j = lane; j < mhi - mlo; j += 32) dst[(l0 + r) * nc + mlo + j] = (T)sout[r * L2_OUT_LD + j];
+        for (int i = lane; i < nl * cnt; i += 32) {
+            const int r = i / cnt, j = i - r * cnt;
+            drow[(uint64_t)r * nc + mlo + j] = (T)sin_[r * L2_IN_LD + j];
+        }
         __syncwarp();
         mhi = mlo;
     }

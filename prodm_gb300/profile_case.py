@@ -9,6 +9,10 @@ and prints per-stage CUDA-event times of the last step. With --encoder perbit
 the step is the GE applications' configuration instead: a seeded fp64 tanh
 shear layer (+1e-6 relative noise), 60 planes, max collector, SignExclude
 interpreter with MaxErrorEstimatorHB, relative L-inf tolerances 1e-3..1e-9.
+With --basis orthogonal: the orthogonal MGARD basis on the same fp64 shear
+layer with the grouped encoder, 60 planes, max collector, SignExclude
+interpreter with MaxErrorEstimatorOB and relative L-inf tolerances 1e-3,
+1e-6, 1e-9. --shape takes one edge (a cube) or AxBxC.
 """
 import argparse
 import math
@@ -20,7 +24,7 @@ from . import api, fields
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--shape", type=int, default=257)
+    ap.add_argument("--shape", default="257", help="edge of a cube, or AxBxC")
     ap.add_argument("--levels", type=int, default=None)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--encoder", default="negabinary")
@@ -30,7 +34,11 @@ def main():
     ap.add_argument("--import-streams", action="store_true",
                     help="per-bit only: export the level files and load them into a second handle (the parse)")
     a = ap.parse_args()
-    shape = (a.shape,) * 3
+    dims = tuple(int(v) for v in a.shape.split("x"))
+    shape = dims * 3 if len(dims) == 1 else dims
+    if a.basis == "orthogonal":
+        L = a.levels if a.levels is not None else api.max_level(shape)
+        return orthogonal(shape, L, a.reps)
     L = a.levels if a.levels is not None else min(7, api.max_level(shape))
     if a.encoder == "perbit":
         return perbit(shape, L, a.reps, a.import_streams)
@@ -87,6 +95,24 @@ def perbit(shape, L, reps, import_streams=False):
         ref = mdr.retrieve_planes([60] * (L + 1))
         torch.cuda.synchronize()
         print("imported streams reconstruct identically: %s" % bool(torch.equal(full, ref)))
+
+
+def orthogonal(shape, L, reps):
+    x = fields.shear_layer(shape, delta=0.05, noise_rel=1e-6, seed=9, dtype=torch.float64, device="cuda")
+    vr = float((x.max() - x.min()).item())
+    mdr = api.MDRField(shape, torch.float64, L, 60, "grouped", "orthogonal", "max")
+    out = torch.empty_like(x)
+    for r in range(reps):
+        if r == reps - 1:
+            mdr.set_timing(True)
+        mdr.refactor(x)
+        mdr.reset()
+        for rel in (1e-3, 1e-6, 1e-9):
+            mdr.retrieve(rel * vr, out=out, interpreter="sign_exclude", estimator="max_ob")
+    torch.cuda.synchronize()
+    for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
+        print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
+    print("final max error %.3g of range %.3g" % (float((out - x).abs().max().item()), vr))
 
 
 if __name__ == "__main__":

@@ -1,6 +1,10 @@
-"""Batched refactor / retrieve against the single-field device path: the same
-streams, the same plane counts and the same reconstructions (the batched
-launches run the same per-row / per-chunk code)."""
+"""Batched refactor / retrieve against the oracle and against the single-field
+device path: the plane counts the oracle interpreter picks from the batch's
+sizes and level bounds, reconstructions equal to the oracle's decode ->
+reposition -> recompose bit for bit, level bounds within float rounding of the
+oracle's decomposition; and the same streams, plane counts and
+reconstructions as the single-field path (the batched launches run the same
+per-row / per-chunk code)."""
 import math
 
 import numpy as np
@@ -38,6 +42,46 @@ def test_batch_matches_single_field_path():
         assert np.array_equal(one.index(), idxb)
         assert torch.equal(out1, outs[i]), i
         assert float((outs[i] - x).abs().max()) <= tols[i]
+
+
+def test_batch_matches_oracle():
+    """Each field of a batch checked against the oracle alone (not through the
+    single-field path): the oracle interpreter (negabinary look-ahead,
+    MaxErrorEstimatorHB on the max-collector tables of the batch's level
+    bounds) picks the batch's plane counts; the oracle's retrieval of the
+    batch's level streams with those counts equals the batch's output bit for
+    bit; the oracle's FP64 decomposition of the field gives the same stream
+    sizes and level bounds within 1e-6 of max|x|; every bound is met."""
+    import oracle
+    from prodm_gb300 import api, fields
+    O = oracle.oracle()
+    B = 32
+    shapes = [(65, 65, 65), (129, 65), (33, 65, 17), (1000,), (9, 9, 9), (40, 33, 21)]
+    xs = [fields.spectral_grf(s, slope=-2.0, seed=40 + i).contiguous() for i, s in enumerate(shapes)]
+    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+    batch = api.MDRBatch(xs, levels, B)
+    batch.refactor()
+    tols = [float(x.max() - x.min()) * 10.0 ** (-1 - i % 5) for i, x in enumerate(xs)]
+    batch.set_tolerances(tols)
+    batch.reset()
+    outs = [o.clone() for o in batch.retrieve("negabinary", "max_hb")]
+    torch.cuda.synchronize()
+    for i, (s, x) in enumerate(zip(shapes, xs)):
+        L = levels[i]
+        xh = x.cpu().numpy()
+        idx, sizes, bounds = batch.field_info(i)
+        blob = np.concatenate([batch.export_level(i, l) for l in range(L + 1)])
+        errs = np.stack([O.max_collect(np.float32(b), B, np.float32) for b in bounds])
+        idx_o, _ = O.interpret("negabinary", "max_hb", sizes, errs, tols[i], np.zeros(L + 1, np.uint8),
+                               ndims=len(s))
+        assert np.array_equal(idx, idx_o), (i, idx, idx_o)
+        rec_o = O.retrieve(s, L, B, blob, sizes, bounds.astype(np.float32), idx, "negabinary", True)
+        out = outs[i].cpu().numpy()
+        assert np.array_equal(out.view(np.uint32), rec_o.view(np.uint32)), i
+        ref = O.refactor(xh, L, B, "negabinary")
+        assert np.array_equal(ref["sizes"], sizes), i
+        np.testing.assert_allclose(bounds, ref["bounds"], rtol=0, atol=1e-6 * float(np.abs(xh).max()))
+        assert float(np.abs(out - xh).max()) <= tols[i]
 
 
 def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
