@@ -57,8 +57,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--graph", action="store_true", help="replay the step as a captured CUDA graph (captured "
-                    "without stage events; stage times come from the instrumented pass after the timed region)")
+    ap.add_argument("--no-graph", dest="graph", action="store_false",
+                    help="time host launches of the step instead of replaying it as a captured CUDA graph (the "
+                         "default: captured without stage events; stage times come from the instrumented pass after "
+                         "the timed region)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-field batched vs per-field-loop measurement")
     ap.add_argument("--no-qoi", action="store_true", help="skip the QoI-guided vs uniform-halving retrieval comparison")
     ap.add_argument("--no-perbit", action="store_true", help="skip the fp64 per-bit encoder measurement")
@@ -343,8 +345,9 @@ def run_ours(args):
                     for l in range(LEVELS + 1)]
 
     # one step captured as a CUDA graph (the interpreter's plane counts stay on
-    # the device, so the whole refactor + retrieve sequence is capturable);
-    # stage events are captured too and time every kernel group of each replay
+    # the device, so the whole refactor + retrieve sequence is capturable; the
+    # kernels' programmatic launch dependencies become graph edges). Measured
+    # at 513^3: 2.843 ms per replayed step against 2.874 ms with host launches.
     graph = None
     launches_per_step = None
     if args.graph:

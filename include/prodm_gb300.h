@@ -290,9 +290,28 @@ int prodm_mdr_export_level_range(prodm_mdr* h, int level, uint64_t offset, uint6
  * prodm_mdr_export_level writes the stored streams and the metadata the
  * stopping indices plus a "ZCB1" marker with the latter index. A handle fed by
  * prodm_mdr_load_metadata takes the stage from the metadata; levels whose
- * metadata has stopping indices but no marker (the reference's zstd stage)
- * return PRODM_EUNSUPPORTED. */
+ * metadata has stopping indices but no marker were written by the reference's
+ * zstd stage (see prodm_mdr_set_zstd_latter). */
 int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream);
+
+/* Reading level files that the reference's lossless stage wrote: metadata
+ * with stopping indices and no "ZCB1" marker came from
+ * AdaptiveLevelCompressor (AdaptiveLevelCompressor.hpp:13-60), whose planes
+ * at or below a level's stopping index and from its latter index on are zstd
+ * frames (ZSTD.hpp:11-28: an 8-byte raw length, then the frame). The latter
+ * index is the compressor's constructor argument and is not in the metadata:
+ * this call gives it (26, the reference's default, when never called) and
+ * must come before prodm_mdr_load_metadata. Such planes are expanded on the
+ * host with libzstd.so.1, opened at run time, as their bytes complete (the
+ * level bytes are kept on the host until then), and go to the device raw;
+ * the stored sizes stay the interpreter's cost model, as in the reference's
+ * reconstructor. Without libzstd, loading such metadata returns
+ * PRODM_EUNSUPPORTED; a frame that does not expand to its recorded length
+ * (for example with the wrong latter index) PRODM_ECORRUPT at the next
+ * reconstruction. Replaces the reference's AdaptiveLevelCompressor::
+ * decompress_level in ComposedReconstructor::progressive_reconstruct
+ * (ComposedReconstructor.hpp:199-206) for the device-resident handle. */
+int prodm_mdr_set_zstd_latter(prodm_mdr* h, int latter_index);
 /* Level files (ConcatLevelFileWriter / ConcatLevelFileRetriever,
  * FileWriter.hpp:13-39, FileRetriever.hpp:15-35). load_level_file reads bytes
  * [file_offset, file_offset + bytes) of a level file straight into device

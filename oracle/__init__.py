@@ -430,6 +430,24 @@ class Reference(Oracle):
             raise RuntimeError("reference composed round trip failed")
         return outs.reshape((len(tols),) + field.shape), ret
 
+    def composed_zstd(self, field, L, B, encoder, latter, tols, workdir):
+        """The round trip above with the reference's zstd stage,
+        AdaptiveLevelCompressor(latter) (fp32, hierarchical basis): writes
+        workdir/metadata.bin and workdir/level_<l>.bin as a stock refactor
+        does, and returns the reference reconstructor's outputs and retrieved
+        sizes for the tolerances (SignExclude greedy, MaxErrorEstimatorHB)."""
+        dims = np.asarray(field.shape, np.uint32)
+        tols = np.asarray(tols, np.float64)
+        outs = np.zeros((len(tols), field.size), np.float32)
+        ret = np.zeros(len(tols), np.uint64)
+        f = self._fn("ref_composed_zstd_f32", C.c_int, _tp(np.float32), C.c_int, _u32p, C.c_int, C.c_int, C.c_int,
+                     C.c_int, C.c_char_p, C.c_int, _f64p, _tp(np.float32), np.ctypeslib.ndpointer(np.uint64))
+        rc = f(np.ascontiguousarray(field, np.float32).ravel(), len(dims), dims, L, B, ENCODERS[encoder], int(latter),
+               workdir.encode(), len(tols), tols, outs, ret)
+        if rc != 0:
+            raise RuntimeError("reference composed round trip failed")
+        return outs.reshape((len(tols),) + field.shape), ret
+
 
 class _RefDecoder:
     def __init__(self, lib, kind, dtype):

@@ -105,10 +105,12 @@ void interp_any(int kind, int est_kind, int ndims, int L, double s, int nl, int 
 }
 
 // ComposedRefactor + ComposedReconstructor driven as test/test_mdr_refactor.cpp
-// and test/test_mdr_reconstructor.cpp do, on files under dir.
-template <class T, class S, class Dec, class Enc, class Est>
+// and test/test_mdr_reconstructor.cpp do, on files under dir (level
+// compressor Comp: NullLevelCompressor, or AdaptiveLevelCompressor(latter)).
+template <class T, class S, class Dec, class Enc, class Est, class Comp = MDR::NullLevelCompressor>
 int composed_roundtrip(const T* field, int ndims, const uint32_t* dims, int L, int B, bool negabinary,
-                       const char* dir, int ntol, const double* tols, T* outs, uint64_t* retrieved) {
+                       const char* dir, int ntol, const double* tols, T* outs, uint64_t* retrieved,
+                       const Comp& comp = Comp()) {
     std::string d(dir);
     std::string meta = d + "/metadata.bin";
     std::vector<std::string> files;
@@ -116,17 +118,17 @@ int composed_roundtrip(const T* field, int ndims, const uint32_t* dims, int L, i
     size_t N = 1; for (int i = 0; i < ndims; i++) N *= dims[i];
     Quiet q;
     {
-        auto refactor = MDR::ComposedRefactor<T, Dec, MDR::DirectInterleaver<T>, Enc, MDR::NullLevelCompressor,
+        auto refactor = MDR::ComposedRefactor<T, Dec, MDR::DirectInterleaver<T>, Enc, Comp,
                                               MDR::MaxErrorCollector<T>, MDR::ConcatLevelFileWriter>(
-            Dec(), MDR::DirectInterleaver<T>(), Enc(), MDR::NullLevelCompressor(), MDR::MaxErrorCollector<T>(),
+            Dec(), MDR::DirectInterleaver<T>(), Enc(), comp, MDR::MaxErrorCollector<T>(),
             MDR::ConcatLevelFileWriter(meta, files));
         refactor.negabinary = negabinary;
         refactor.refactor(field, vec(dims, ndims), (uint8_t)L, (uint8_t)B);
     }
-    auto rec = MDR::ComposedReconstructor<T, Dec, MDR::DirectInterleaver<T>, Enc, MDR::NullLevelCompressor,
+    auto rec = MDR::ComposedReconstructor<T, Dec, MDR::DirectInterleaver<T>, Enc, Comp,
                                           MDR::SignExcludeGreedyBasedSizeInterpreter<Est>, Est,
                                           MDR::ConcatLevelFileRetriever>(
-        Dec(), MDR::DirectInterleaver<T>(), Enc(), MDR::NullLevelCompressor(),
+        Dec(), MDR::DirectInterleaver<T>(), Enc(), comp,
         MDR::SignExcludeGreedyBasedSizeInterpreter<Est>(Est()), MDR::ConcatLevelFileRetriever(meta, files));
     rec.load_metadata();
     for (int t = 0; t < ntol; t++) {
@@ -221,6 +223,24 @@ extern "C" {
 
 REF_T(f32, float, uint32_t)
 REF_T(f64, double, uint64_t)
+
+// The same round trip with the reference's zstd stage,
+// AdaptiveLevelCompressor(latter) (hierarchical basis; enc 0 negabinary,
+// else grouped): the level files and metadata a stock refactor writes.
+extern "C" int ref_composed_zstd_f32(const float* field, int ndims, const uint32_t* dims, int L, int B, int enc,
+                                     int latter, const char* dir, int ntol, const double* tols, float* outs,
+                                     uint64_t* retrieved) {
+    const MDR::AdaptiveLevelCompressor comp(latter);
+    if (enc == 0)
+        return composed_roundtrip<float, uint32_t, MDR::MGARDHierarchicalDecomposer<float>,
+                                  MDR::NegaBinaryBPEncoder<float, uint32_t>, MDR::MaxErrorEstimatorHB<float>,
+                                  MDR::AdaptiveLevelCompressor>(field, ndims, dims, L, B, true, dir, ntol, tols, outs,
+                                                                retrieved, comp);
+    return composed_roundtrip<float, uint32_t, MDR::MGARDHierarchicalDecomposer<float>,
+                              MDR::GroupedBPEncoder<float, uint32_t>, MDR::MaxErrorEstimatorHB<float>,
+                              MDR::AdaptiveLevelCompressor>(field, ndims, dims, L, B, false, dir, ntol, tols, outs,
+                                                            retrieved, comp);
+}
 
 // PerBitBPEncoder with the stream word type the GE applications instantiate it
 // with (refactorGE.cpp:72: PerBitBPEncoder<Type, uint32_t>)

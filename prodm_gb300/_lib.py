@@ -73,6 +73,7 @@ _SIGS = {
     "prodm_mdr_metadata": (_i, [_P, _u8p, C.c_size_t, C.POINTER(C.c_size_t), _P]),
     "prodm_mdr_export_level": (_i, [_P, _i, _P, C.c_uint64, _i, _u64p, _P]),
     "prodm_mdr_set_lossless": (_i, [_P, _i, _P]),
+    "prodm_mdr_set_zstd_latter": (_i, [_P, _i]),
     "prodm_mdr_export_level_range": (_i, [_P, _i, C.c_uint64, C.c_uint64, _P, _i, _P]),
     "prodm_mdr_load_level_file": (_i, [_P, _i, C.c_char_p, C.c_uint64, C.c_uint64, C.c_uint64, _P]),
     "prodm_mdr_write_level_file": (_i, [_P, _i, C.c_char_p, _P]),

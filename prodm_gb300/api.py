@@ -345,6 +345,11 @@ class MDRField:
         """Lossless stage on (latter_index >= 0, the reference's default 26) or off (None / < 0)."""
         call("prodm_mdr_set_lossless", self.h, -1 if latter_index is None else int(latter_index), _stream(stream))
 
+    def set_zstd_latter(self, latter_index=26):
+        """Latter index of the reference's AdaptiveLevelCompressor that wrote
+        zstd level files (its constructor argument); call before load_metadata."""
+        call("prodm_mdr_set_zstd_latter", self.h, int(latter_index))
+
     def retrieve(self, tolerance, out=None, interpreter="sign_exclude", estimator="max_hb", s=0.0, stream=None):
         if out is None:
             out = torch.empty(self.shape, dtype=self.dtype, device="cuda")

@@ -27,6 +27,9 @@ bool pdl_enabled() {
     return on;
 }
 void set_error(const std::string& msg) { g_err = msg; }
+bool zstd_available();
+int zstd_expand_plane(const uint8_t* src, uint64_t stored, uint64_t max_raw, std::vector<uint8_t>& out);
+
 int fail(int status, const std::string& msg) {
     g_err = msg;
     return status;
@@ -599,6 +602,12 @@ struct prodm_mdr {
     std::vector<uint64_t> ll_cloaded, ll_rawoff;   // stored bytes loaded, raw bytes expanded, per level
     std::vector<int> ll_expanded;                  // planes expanded per level
     std::vector<uint32_t> ll_stored;               // loading: stored sizes from the metadata
+    // loading level files of the reference's zstd stage: their latter index
+    // (AdaptiveLevelCompressor's constructor argument) and the stored bytes,
+    // kept on the host until their planes are complete and expanded there
+    bool ll_zstd = false;
+    int zstd_latter = 26;
+    std::vector<std::vector<uint8_t>> ll_hbuf;
     FileStaging* fstage = nullptr;                 // level-file reads: staging buffers
     std::vector<uint32_t> hsz;                     // host copy of `sizes` (export), valid while hsz_valid
     bool hsz_valid = false;
@@ -1160,6 +1169,18 @@ int mdr_ll_load(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t byt
     for (int p = 0; p < B; p++) total += h->ll_stored[l * B + p];
     if (off + bytes > total) return fail(PRODM_EINVAL, "load_level: range beyond the level file");
     if (bytes == 0) return PRODM_OK;
+    if (h->ll_zstd) {   // zstd planes are expanded on the host
+        std::vector<uint8_t>& hb = h->ll_hbuf[l];
+        if (hb.size() < total) hb.resize(total);
+        if (host) {
+            memcpy(hb.data() + off, src, bytes);
+        } else {
+            PRODM_CUDA(cudaMemcpyAsync(hb.data() + off, src, bytes, cudaMemcpyDeviceToHost, st));
+            PRODM_CUDA(cudaStreamSynchronize(st));
+        }
+        if (off + bytes > h->ll_cloaded[l]) h->ll_cloaded[l] = off + bytes;
+        return PRODM_OK;
+    }
     if (!h->ll_cbuf[l]) {
         int rc = h->alloc((void**)&h->ll_cbuf[l], total);
         if (rc) return rc;
@@ -1172,8 +1193,52 @@ int mdr_ll_load(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t byt
 
 // stored planes completely loaded and not expanded yet -> raw plane bytes
 // (decompressed where the stage compressed them) -> the raw loading path
+int mdr_ll_expand_zstd(prodm_mdr* h, cudaStream_t st) {
+    const int L = h->g.L, B = h->B;
+    for (int l = 0; l <= L; l++) {
+        const std::vector<uint8_t>& hb = h->ll_hbuf[l];
+        if (hb.empty()) continue;
+        uint64_t off = 0, soff = 0;
+        int complete = 0;
+        for (int p = 0; p < B; p++) {
+            off += h->ll_stored[l * B + p];
+            if (off <= h->ll_cloaded[l]) complete = p + 1;
+            else break;
+        }
+        const int first = h->ll_expanded[l];
+        if (complete <= first) continue;
+        for (int p = 0; p < first; p++) soff += h->ll_stored[l * B + p];
+        const uint64_t cap = encode_bound(h->cfg.encoder, h->cfg.dtype, h->g.elems[l], B);
+        std::vector<uint8_t> raw;
+        for (int p = first; p < complete; p++) {
+            const uint32_t sz = h->ll_stored[l * B + p];
+            const size_t at = raw.size();
+            if (h->ll_flags[(size_t)l * B + p]) {
+                int rc = zstd_expand_plane(hb.data() + soff, sz, cap, raw);
+                if (rc) return rc;
+            } else {
+                raw.insert(raw.end(), hb.data() + soff, hb.data() + soff + sz);
+            }
+            h->hsizes[l * B + p] = (uint32_t)(raw.size() - at);
+            soff += sz;
+        }
+        if (!raw.empty()) {
+            int rc = mdr_load_level(h, l, raw.data(), h->ll_rawoff[l], raw.size(), 1, st);
+            if (!rc) {
+                cudaError_t e = cudaStreamSynchronize(st);   // raw is pageable host memory
+                if (e != cudaSuccess) rc = cuda_status(e, "zstd plane upload");
+            }
+            if (rc) return rc;
+        }
+        h->ll_rawoff[l] += raw.size();
+        h->ll_expanded[l] = complete;
+    }
+    return PRODM_OK;
+}
+
 int mdr_ll_expand(prodm_mdr* h, cudaStream_t st) {
     const int L = h->g.L, B = h->B;
+    if (h->ll_zstd) return mdr_ll_expand_zstd(h, st);
     for (int l = 0; l <= L; l++) {
         if (!h->ll_cbuf[l]) continue;
         uint64_t off = 0, soff = 0;
@@ -1274,13 +1339,21 @@ int mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, cudaStream_t
         p += nl * (B + 1) * 8;
     }
     int latter = -1;
+    bool zstd = false;
     if (need(8) && memcmp(p, "ZCB1", 4) == 0) {
         uint32_t lt;
         memcpy(&lt, p + 4, 4);
         if (lt > 255) return fail(PRODM_ECORRUPT, "metadata: bad lossless-stage extension");
         latter = (int)lt;
     } else if (any_stop) {
-        return fail(PRODM_EUNSUPPORTED, "metadata: levels compressed by the reference's zstd stage");
+        // stopping indices without this library's marker: the reference's
+        // AdaptiveLevelCompressor wrote the levels with zstd; its latter index
+        // is not in the metadata (the handle's, 26 unless set)
+        if (!zstd_available())
+            return fail(PRODM_EUNSUPPORTED, "metadata: levels compressed by the reference's zstd stage, and "
+                                            "libzstd.so.1 could not be opened");
+        latter = h->zstd_latter;
+        zstd = true;
     }
     // device state: sizes, bounds, level max keys (exponents) and error tables
     using K = typename KeyOf<T>::type;
@@ -1321,6 +1394,8 @@ int mdr_load_metadata(prodm_mdr* h, const uint8_t* buf, size_t len, cudaStream_t
         h->ll_expanded.assign(nl, 0);
         if (h->ll_cbuf.empty()) h->ll_cbuf.assign(nl, nullptr);
     }
+    h->ll_zstd = zstd;
+    h->ll_hbuf.assign(zstd ? nl : 0, std::vector<uint8_t>());
     if (h->lfile.empty()) h->lfile.assign(nl, nullptr);
     return PRODM_OK;
 }
@@ -1967,6 +2042,13 @@ int prodm_mdr_set_lossless(prodm_mdr* h, int latter_index, void* stream) {
     if (h->ll_latter >= 0) PRODM_CUDA(cudaMemcpyAsync(h->sizes, h->rsizes, nl * B * 4, cudaMemcpyDeviceToDevice, st));
     h->ll_latter = latter_index;
     return h->refactored ? mdr_lossless_sizes(h, st) : PRODM_OK;
+}
+
+int prodm_mdr_set_zstd_latter(prodm_mdr* h, int latter_index) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    if (latter_index < 0 || latter_index > 255) return fail(PRODM_EINVAL, "set_zstd_latter: latter index outside 0..255");
+    h->zstd_latter = latter_index;
+    return PRODM_OK;
 }
 
 int prodm_mdr_retrieve(prodm_mdr* h, double tol, int interp, int est, double s, void* out, void* stream) {

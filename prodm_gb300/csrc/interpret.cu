@@ -297,6 +297,208 @@ __device__ bool interpret_warp(int kind, int nl, int B, const uint32_t* __restri
     return true;
 }
 
+// The same walk with the pop order computed in parallel. A level's entries
+// (its chain: idx, idx + num, ..) fall into blocks: a block starts at an
+// entry whose efficiency is below every earlier one of the level (the first
+// entry starts one) and runs until the next such entry. When the largest
+// head is unique at every pop, a popped block start is larger than every
+// other head, and the rest of its block is at least as large, so a block
+// leaves the heap in one run, and blocks leave in decreasing order of their
+// start efficiency. So the pop order is the blocks sorted by start key, each
+// in chain order; a pop meets a tie exactly when it starts a block whose key
+// another level's block shares (tied blocks are ordered by level and flag
+// their first entry). Thread 0 then runs the estimate `acc` along that order
+// in the reference's arithmetic (two dependent double adds per pop, eight
+// pops per round before their comparisons), stopping at the first estimate
+// below the tolerance. Returns false -- nothing written -- when an
+// efficiency is NaN or the walk reaches a tie before it stops; the caller
+// then runs the walks above. All threads of the CTA call it.
+struct BlockWalkSmem {
+    uint8_t ch_j[kMaxLevels][64];      // chain entries of each level (plane index)
+    uint16_t order[kMaxLevels * 64];   // pop order: level << 8 | plane index
+    uint8_t tie[kMaxLevels * 64];      // 1: the pop at this position starts a tied block
+    // every level's blocks in one list (levels in any order): level | block
+    // index within the level << 8 | entry count << 16 | first entry << 24
+    uint32_t binfo[kMaxLevels * 64];
+    uint32_t rs[kMaxLevels];
+    int nidx[kMaxLevels];
+    uint8_t start[kMaxLevels], n_ent[kMaxLevels], in_heap[kMaxLevels];
+    int nblk, npos, fail, met0, stop;
+    double acc0;
+};
+
+__device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __restrict__ sizes,
+                                 const double* __restrict__ ev, const long long* __restrict__ ekey,
+                                 const int8_t* __restrict__ enan, const int8_t* __restrict__ en, double tol,
+                                 uint8_t* index, uint32_t* rsz, long long* blk_key /* [kMaxLevels][64] */,
+                                 BlockWalkSmem& w) {
+    const int tid = threadIdx.x, nth = blockDim.x;
+    // initial estimate, the sign-exclude first planes, heap membership
+    if (tid == 0) {
+        double acc = 0;
+        for (int i = 0; i < nl; i++) acc += ev[i * 65 + index[i]];
+        bool met = false;
+        w.fail = 0;
+        for (int i = 0; i < nl; i++) {
+            w.start[i] = index[i];
+            w.rs[i] = 0;
+            w.in_heap[i] = kind != 1 && index[i] != B;
+        }
+        if (kind == 1) {
+            if (acc < tol) {
+                met = true;   // nothing retrieved, nothing pushed
+            } else {
+                double minerr = acc;
+                for (int i = 0; i < nl; i++) {
+                    const int ii = index[i];
+                    minerr -= ev[i * 65 + ii];
+                    minerr += ev[i * 65 + B];
+                    int ni = ii;
+                    if (ii == 0) {
+                        acc -= ev[i * 65 + 0];
+                        acc += ev[i * 65 + 1];
+                        ni = 1;
+                        w.rs[i] = sizes[(size_t)i * B];
+                        w.start[i] = 1;
+                    }
+                    w.in_heap[i] = ni != B;
+                    if (minerr < tol) break;
+                }
+                met = acc < tol;
+            }
+        } else if (kind == 2) {
+            met = acc < tol;
+        }
+        w.met0 = met;
+        w.acc0 = acc;
+        w.nblk = 0;
+        w.npos = 0;
+    }
+    __syncthreads();
+    // each level's chain and blocks (one thread per level): block keys in
+    // blk_key's row of the level, the blocks themselves in the shared list
+    uint8_t* lfirst = reinterpret_cast<uint8_t*>(w.order);   // [kMaxLevels][64]: first entry of each block
+    if (tid < nl) {
+        const int l = tid;
+        int cnt = 0, nb = 0;
+        if (w.in_heap[l]) {
+            long long runmin = 0;
+            for (int j = w.start[l]; j < B; j += en[l * 64 + j]) {
+                const long long k = ekey[l * 64 + j];
+                if (enan[l * 64 + j]) w.fail = 1;
+                if (cnt == 0 || k < runmin) {
+                    lfirst[l * 64 + nb] = (uint8_t)cnt;
+                    blk_key[l * 64 + nb] = k;
+                    nb++;
+                    runmin = k;
+                }
+                w.ch_j[l][cnt++] = (uint8_t)j;
+            }
+        }
+        w.n_ent[l] = (uint8_t)cnt;
+        if (nb) {
+            atomicAdd(&w.npos, cnt);
+            const int at = atomicAdd(&w.nblk, nb);
+            for (int b = 0; b < nb; b++) {
+                const int f0 = lfirst[l * 64 + b], f1 = b + 1 < nb ? lfirst[l * 64 + b + 1] : cnt;
+                w.binfo[at + b] = (uint32_t)l | (uint32_t)b << 8 | (uint32_t)(f1 - f0) << 16 | (uint32_t)f0 << 24;
+            }
+        }
+    }
+    __syncthreads();
+    if (w.fail) return false;
+    // rank of each block: the entries of every block with a larger key, or an
+    // equal key at a lower level (a tie, flagged); same-level blocks have
+    // larger keys exactly when they come first, so they are counted too
+    const int nblk = w.nblk;
+    for (int t = tid; t < nblk; t += nth) {
+        const uint32_t bi = w.binfo[t];
+        const int l = bi & 255;
+        const long long k = blk_key[l * 64 + ((bi >> 8) & 255)];
+        int rank = 0;
+        bool tie = false;
+#pragma unroll 8
+        for (int u = 0; u < nblk; u++) {
+            const uint32_t b2 = w.binfo[u];
+            const int l2 = b2 & 255;
+            const long long k2 = blk_key[l2 * 64 + ((b2 >> 8) & 255)];
+            const bool eq = k2 == k && l2 != l;
+            tie |= eq;
+            if (k2 > k || (eq && l2 < l)) rank += (b2 >> 16) & 255;
+        }
+        const int f0 = bi >> 24, n = (bi >> 16) & 255;
+        for (int e = 0; e < n; e++) {
+            w.order[rank + e] = (uint16_t)(l << 8 | w.ch_j[l][f0 + e]);
+            w.tie[rank + e] = (uint8_t)(tie && e == 0);
+        }
+    }
+    __syncthreads();
+    // the estimate along the order (thread 0): each round loads eight pops'
+    // terms, runs the two dependent double adds per pop, then compares the
+    // eight estimates with the tolerance as order-preserving integers (a NaN
+    // estimate is never below it)
+    if (tid == 0) {
+        const int np = w.npos;
+        int stop = np;   // pops [0, stop)
+        bool bail = false;
+        if (w.met0) {
+            stop = 0;
+        } else {
+            double acc = w.acc0;
+            long long tkey;
+            int tnan;
+            eff_key(tol, tkey, tnan);
+            for (int p = 0; p < np && stop == np && !bail; p += 8) {
+                double sub[8], add[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    sub[u] = 0;
+                    add[u] = 0;
+                    if (p + u < np) {
+                        const int o = w.order[p + u], l = o >> 8, j = o & 255;
+                        sub[u] = ev[l * 65 + j];
+                        add[u] = ev[l * 65 + j + en[l * 64 + j]];
+                    }
+                }
+                long long akey[8];
+                int anan[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    acc -= sub[u];   // past np: - 0 + 0, never compared
+                    acc += add[u];
+                    eff_key(acc, akey[u], anan[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    if (p + u >= np || stop < np || bail) continue;
+                    if (w.tie[p + u]) bail = true;
+                    else if (!anan[u] && !tnan && akey[u] < tkey) stop = p + u + 1;
+                }
+            }
+        }
+        w.fail = bail;
+        w.stop = stop;
+    }
+    __syncthreads();
+    if (w.fail) return false;
+    // each level's new index: past its last popped entry
+    if (tid < nl) w.nidx[tid] = w.start[tid];
+    __syncthreads();
+    for (int p = tid; p < w.stop; p += nth) {
+        const int o = w.order[p], l = o >> 8, j = o & 255;
+        atomicMax(&w.nidx[l], j + en[l * 64 + j]);
+    }
+    __syncthreads();
+    if (tid < nl) {
+        uint32_t r = w.rs[tid];
+        for (int j = w.start[tid]; j < w.nidx[tid]; j++) r += sizes[(size_t)tid * B + j];
+        rsz[tid] = r;
+        index[tid] = (uint8_t)w.nidx[tid];
+    }
+    __syncthreads();
+    return true;
+}
+
 // one CTA per field: all threads tabulate the efficiencies, warp 0 walks the
 // levels (the exact heap walk on thread 0 when the warp walk declines)
 template <class T>
@@ -363,6 +565,17 @@ __global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int es
     __shared__ int s_ok;
     uint32_t* gr = rsz + f * idx_stride;
     const double tol = tols ? tols[f] : tol0;
+    {   // the block-ordered walk; s_errs is free after the tabulation and holds its block keys
+        __shared__ BlockWalkSmem s_bw;
+        if (interpret_blocks(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tol, s_idx, s_rs,
+                             reinterpret_cast<long long*>(s_errs), s_bw)) {
+            if (threadIdx.x < nl) {
+                gi[threadIdx.x] = s_idx[threadIdx.x];
+                gr[threadIdx.x] = s_rs[threadIdx.x];
+            }
+            return;
+        }
+    }
     if (threadIdx.x < 32) {
         const bool ok = nl <= 32 && interpret_warp(kind, nl, B, s_sizes, s_ev, s_key, s_nan, s_en, tol, s_idx, s_rs,
                                                    threadIdx.x);

@@ -174,17 +174,72 @@ def test_handle_with_lossless_stage(shape, L, dt, B, enc, col, interp, est, tmp_
     assert np.array_equal(s3, raw_sizes)
 
 
-def test_reference_zstd_levels_rejected():
-    """metadata with stopping indices but no ZCB1 marker: levels the
-    reference's zstd stage compressed"""
-    from prodm_gb300._lib import ProdmError
-    g = np.load(os.path.join(HERE, "golden", "composed.npz"))
-    meta = bytearray(g["grouped_metadata"].tobytes())
-    nd = meta[0]
-    nl = meta[1 + 4 * nd]
+def reference_or_skip():
+    """The reference harness with libzstd (it writes the zstd level files)."""
+    import importlib
+    if importlib.import_module("oracle.build_oracle").zstd_library() is None:
+        pytest.skip("no libzstd on this host")
+    R = oracle.reference()
+    if R is None:
+        pytest.skip("the reference harness is not built on this host")
+    return R
+
+
+# shapes the reference's composed classes take (some 2-D and thin shapes
+# make them exit or crash, which would end the test process)
+REF_ZSTD_CASES = [("negabinary", 26, (65, 65, 65), 3), ("grouped", 20, (33, 40, 21), 2),
+                  ("negabinary", 64, (65, 33, 33), 3)]
+
+
+@pytest.mark.parametrize("enc,latter,shape,L", REF_ZSTD_CASES)
+def test_reference_zstd_level_files(enc, latter, shape, L, tmp_path):
+    """Level files and metadata written by the reference's ComposedRefactor
+    with its zstd stage (AdaptiveLevelCompressor(latter)) load into the
+    device handle: the plane counts, retrieved (stored) bytes and
+    reconstructions equal the reference ComposedReconstructor's on the same
+    files, every bound met; the files go in in consecutive pieces per
+    tolerance, as the reference's retriever reads them."""
+    R = reference_or_skip()
     B = 32
-    stops_at = 2 + 4 * nd + nl * 4 + nl * (4 + 4 * B)
-    meta[stops_at] = 3
-    r = api().MDRField((33, 33, 33), torch.float32, 3, 32, "grouped", "hierarchical", "max")
+    rng = np.random.default_rng(latter + L)
+    field = (np.cumsum(rng.standard_normal(shape), axis=-1) + 0.05 * rng.standard_normal(shape)).astype(np.float32)
+    vr = float(field.max() - field.min())
+    tols = [r * vr for r in (1e-2, 1e-4, 1e-6)]
+    outs, ret = R.composed_zstd(field, L, B, enc, latter, tols, str(tmp_path))
+    meta = (tmp_path / "metadata.bin").read_bytes()
+    files = [(tmp_path / ("level_%d.bin" % l)).read_bytes() for l in range(L + 1)]
+    m = api().MDRField(shape, torch.float32, L, B, enc, "hierarchical", "max")
+    m.set_zstd_latter(latter)
+    m.load_metadata(meta)
+    stored, _, _ = m.level_info()
+    loaded = [0] * (L + 1)
+    for t, tol in enumerate(tols):
+        m.interpret(tol, interpreter="sign_exclude", estimator="max_hb")
+        idx = m.index()
+        for l in range(L + 1):
+            need = int(stored[l, :idx[l]].astype(np.int64).sum())
+            if need > loaded[l]:
+                m.load_level(l, np.frombuffer(files[l][loaded[l]:need], np.uint8), loaded[l])
+                loaded[l] = need
+        assert sum(loaded) == int(ret[t]), (t, sum(loaded), int(ret[t]))
+        out = m.reconstruct().cpu().numpy()
+        np.testing.assert_allclose(out, outs[t], rtol=0, atol=2e-6 * float(np.abs(field).max()))
+        assert float(np.abs(out - field).max()) <= tol
+
+
+def test_wrong_latter_index_is_reported(tmp_path):
+    """zstd files read with a latter index other than the writer's: a plane
+    that is not a zstd frame is reported as corrupt (and nothing hangs)."""
+    from prodm_gb300._lib import ProdmError
+    R = reference_or_skip()
+    shape, L, B = (65, 65, 65), 3, 32
+    rng = np.random.default_rng(3)
+    field = np.cumsum(rng.standard_normal(shape), axis=-1).astype(np.float32)
+    R.composed_zstd(field, L, B, "negabinary", 64, [1e-3], str(tmp_path))
+    m = api().MDRField(shape, torch.float32, L, B, "negabinary", "hierarchical", "max")
+    m.set_zstd_latter(20)   # planes 20.. taken as frames; the writer left them raw
+    m.load_metadata((tmp_path / "metadata.bin").read_bytes())
+    for l in range(L + 1):
+        m.load_level(l, np.frombuffer((tmp_path / ("level_%d.bin" % l)).read_bytes(), np.uint8), 0)
     with pytest.raises(ProdmError):
-        r.load_metadata(bytes(meta))
+        m.retrieve_planes([B] * (L + 1))
