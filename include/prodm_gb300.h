@@ -375,7 +375,18 @@ int prodm_mdr_destroy(prodm_mdr* h);
 typedef struct prodm_batch prodm_batch;
 int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs);
 int prodm_batch_bind(prodm_batch* h, const void* const* d_fields, void* const* d_outs);
+/* launch shape of the row stages (decompose, recompose: 64, 128 or 256
+ * threads per CTA, 1..32 CTAs per SM) and the encode grid (min(ctas, 8) CTAs
+ * of 256 threads per SM) */
 int prodm_batch_set_launch(prodm_batch* h, int threads_per_cta, int ctas_per_sm);
+/* one stage's launch shape, as the autotuner sets them one stage at a time:
+ * PRODM_BATCH_DECOMPOSE / PRODM_BATCH_RECOMPOSE (one warp per fine row;
+ * threads 64, 128 or 256, CTAs per SM 1..32) or PRODM_BATCH_ENCODE (256
+ * threads, 1..8 CTAs per SM) */
+#define PRODM_BATCH_DECOMPOSE 0
+#define PRODM_BATCH_ENCODE 1
+#define PRODM_BATCH_RECOMPOSE 2
+int prodm_batch_set_stage_launch(prodm_batch* h, int stage, int threads_per_cta, int ctas_per_sm);
 int prodm_batch_refactor(prodm_batch* h, void* stream);
 int prodm_batch_set_tolerances(prodm_batch* h, const double* h_tolerances, void* stream);
 int prodm_batch_retrieve(prodm_batch* h, int interpreter, int estimator, double s, void* stream);

@@ -93,6 +93,7 @@ _SIGS = {
     "prodm_batch_create": (_i, [C.POINTER(_P), _i, C.POINTER(prodm_config)]),
     "prodm_batch_bind": (_i, [_P, C.POINTER(_P), C.POINTER(_P)]),
     "prodm_batch_set_launch": (_i, [_P, _i, _i]),
+    "prodm_batch_set_stage_launch": (_i, [_P, _i, _i, _i]),
     "prodm_batch_refactor": (_i, [_P, _P]),
     "prodm_batch_set_tolerances": (_i, [_P, _dp, _P]),
     "prodm_batch_retrieve": (_i, [_P, _i, _i, C.c_double, _P]),

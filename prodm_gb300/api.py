@@ -502,6 +502,12 @@ class MDRBatch:
     def set_launch(self, threads_per_cta, ctas_per_sm):
         call("prodm_batch_set_launch", self.h, int(threads_per_cta), int(ctas_per_sm))
 
+    STAGES = {"decompose": 0, "encode": 1, "recompose": 2}
+
+    def set_stage_launch(self, stage, threads_per_cta, ctas_per_sm):
+        """stage: "decompose", "encode" or "recompose"."""
+        call("prodm_batch_set_stage_launch", self.h, self.STAGES[stage], int(threads_per_cta), int(ctas_per_sm))
+
     def refactor(self, stream=None):
         call("prodm_batch_refactor", self.h, _stream(stream))
 

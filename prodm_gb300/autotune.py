@@ -1,9 +1,14 @@
 """Launch-shape autotuner for the batched executor.
 
-Times a small set of (threads per CTA, CTAs per SM) choices for the
-persistent multi-field launches on the actual batch and keeps the fastest.
-Results persist in a JSON cache keyed by the GPU name and the batch's shapes
-and level counts ($PRODM_AUTOTUNE_CACHE, default ~/.cache/prodm_gb300/autotune.json).
+Times launch shapes for the persistent multi-field launches on the actual
+batch and keeps the fastest, one stage at a time (coordinate descent): the
+row stages (decomposition, recomposition: threads per CTA = warps = fine rows
+in flight per CTA, and CTAs per SM, i.e. how many row groups share an SM) and
+the encoder (CTAs per SM of its 256-thread chunk workers), each timed as the
+whole refactor + retrieve step with the other stages at their best shape so
+far. Results persist in a JSON cache keyed by the GPU name and the batch's
+shapes and level counts ($PRODM_AUTOTUNE_CACHE, default
+~/.cache/prodm_gb300/autotune.json).
 """
 import hashlib
 import json
@@ -11,6 +16,12 @@ import os
 
 import torch
 
+# (threads per CTA, CTAs per SM) per stage
+ROW_CANDIDATES = ((64, 16), (64, 32), (128, 8), (128, 16), (256, 4), (256, 8))
+ENCODE_CANDIDATES = ((256, 1), (256, 2), (256, 4), (256, 8))
+STAGE_CANDIDATES = {"decompose": ROW_CANDIDATES, "recompose": ROW_CANDIDATES, "encode": ENCODE_CANDIDATES}
+DEFAULT = {"decompose": (256, 8), "encode": (256, 8), "recompose": (256, 8)}
+# the uniform shapes of the earlier single-shape tuner (still accepted by set_launch)
 CANDIDATES = ((128, 8), (256, 4), (256, 8), (256, 16))
 
 
@@ -43,34 +54,50 @@ def _store(cache):
         pass
 
 
-def tune(batch, reps=3, use_cache=True):
-    """Pick and apply the fastest launch shape; returns (threads, ctas_per_sm, timings)."""
-    sig = signature(batch)
-    cache = _load() if use_cache else {}
-    if sig in cache:
-        t, c = cache[sig]["threads"], cache[sig]["ctas_per_sm"]
-        batch.set_launch(t, c)
-        return t, c, cache[sig].get("ms", {})
-    timings = {}
-    for t, c in CANDIDATES:
-        batch.set_launch(t, c)
+def _time(batch, reps):
+    batch.refactor()
+    batch.reset()
+    batch.retrieve()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
         batch.refactor()
         batch.reset()
         batch.retrieve()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            batch.refactor()
-            batch.reset()
-            batch.retrieve()
-        e1.record()
-        torch.cuda.synchronize()
-        timings["%dx%d" % (t, c)] = e0.elapsed_time(e1) / reps
-    best = min(timings, key=timings.get)
-    t, c = (int(x) for x in best.split("x"))
-    batch.set_launch(t, c)
-    cache[sig] = {"threads": t, "ctas_per_sm": c, "ms": timings}
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _apply(batch, shapes):
+    for stage, (t, c) in shapes.items():
+        batch.set_stage_launch(stage, t, c)
+
+
+def tune(batch, reps=3, use_cache=True):
+    """Pick and apply the fastest launch shape of every stage; returns
+    (shapes {stage: (threads, ctas_per_sm)}, timings {"stage:TxC": ms})."""
+    sig = signature(batch)
+    cache = _load() if use_cache else {}
+    if sig in cache and "stages" in cache[sig]:
+        shapes = {k: tuple(v) for k, v in cache[sig]["stages"].items()}
+        _apply(batch, shapes)
+        return shapes, cache[sig].get("ms", {})
+    shapes = dict(DEFAULT)
+    _apply(batch, shapes)
+    timings = {}
+    for stage in ("decompose", "recompose", "encode"):
+        best = None
+        for t, c in STAGE_CANDIDATES[stage]:
+            batch.set_stage_launch(stage, t, c)
+            ms = _time(batch, reps)
+            timings["%s:%dx%d" % (stage, t, c)] = ms
+            if best is None or ms < best[0]:
+                best = (ms, (t, c))
+        shapes[stage] = best[1]
+        batch.set_stage_launch(stage, *best[1])
+    cache[sig] = {"stages": {k: list(v) for k, v in shapes.items()}, "ms": timings}
     if use_cache:
         _store(cache)
-    return t, c, timings
+    return shapes, timings

@@ -154,7 +154,9 @@ struct prodm_batch {
     std::vector<const float*> fields;
     std::vector<float*> outs;
     bool bound = false;
-    int threads = 256, ctas_per_sm = 8;
+    // launch shape per stage (decompose, encode, recompose): threads per CTA,
+    // CTAs per SM of the persistent grid
+    int st_threads[3] = {256, 256, 256}, st_ctas[3] = {8, 8, 8};
     ~prodm_batch() {
         for (void* p : allocs) cudaFree(p);
     }
@@ -270,16 +272,16 @@ int batch_build_segments(prodm_batch* h) {
     return PRODM_OK;
 }
 
-unsigned persistent_grid(const prodm_batch* h, uint64_t work_items, unsigned items_per_cta) {
+unsigned persistent_grid(const prodm_batch* h, int stage, uint64_t work_items, unsigned items_per_cta) {
     uint64_t need = (work_items + items_per_cta - 1) / items_per_cta;
-    uint64_t cap = (uint64_t)device_sms() * h->ctas_per_sm;
+    uint64_t cap = (uint64_t)device_sms() * h->st_ctas[stage];
     uint64_t g = need < cap ? need : cap;
     return (unsigned)(g ? g : 1);
 }
 
 int batch_refactor(prodm_batch* h, cudaStream_t st) {
     PRODM_CUDA(cudaMemsetAsync(h->keys, 0, (size_t)h->nf * kMaxL * 4, st));
-    const unsigned th = (unsigned)h->threads;
+    const unsigned th = (unsigned)h->st_threads[0];
     for (int f = 0; f < h->nf; f++)
         if (h->g[f].L == 0) {
             PRODM_CUDA(cudaMemcpyAsync(h->coef + h->coef_off[f], h->fields[f], h->g[f].total * 4, cudaMemcpyDeviceToDevice, st));
@@ -288,10 +290,10 @@ int batch_refactor(prodm_batch* h, cudaStream_t st) {
         }
     for (int d = 0; d < h->maxL; d++) {
         if (!h->dn[d]) continue;
-        k_decompose_multi<<<persistent_grid(h, h->drows[d], th / 32), th, 0, st>>>(h->dseg[d], h->dn[d], h->drows[d]);
+        k_decompose_multi<<<persistent_grid(h, 0, h->drows[d], th / 32), th, 0, st>>>(h->dseg[d], h->dn[d], h->drows[d]);
         PRODM_CHECK_LAUNCH("k_decompose_multi");
     }
-    k_nb_encode_multi<<<persistent_grid(h, h->echunks, 1), 256, 0, st>>>(h->eseg, h->en, h->echunks, h->B);
+    k_nb_encode_multi<<<persistent_grid(h, 1, h->echunks, 1), 256, 0, st>>>(h->eseg, h->en, h->echunks, h->B);
     PRODM_CHECK_LAUNCH("k_nb_encode_multi");
     k_bounds_tables_multi<<<(h->nf * kMaxL + 127) / 128, 128, 0, st>>>(h->keys, h->levels_d, h->nf, h->B, h->bounds,
                                                                         h->maxerr);
@@ -301,7 +303,7 @@ int batch_refactor(prodm_batch* h, cudaStream_t st) {
 
 int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t st) {
     int rc;
-    const unsigned th = (unsigned)h->threads;
+    const unsigned th = (unsigned)h->st_threads[2];
     if ((rc = launch_interpret<float>(h->nf, interp, est, h->ndims_d, h->levels_d, s, h->B, h->sizes,
                                       (uint64_t)kMaxL * h->B, h->maxerr, (uint64_t)kMaxL * (h->B + 1), h->tols, 0.0,
                                       h->index, kMaxL, h->rsz, st)))
@@ -312,7 +314,7 @@ int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t s
             PRODM_CUDA(cudaMemcpyAsync(h->outs[f], h->rcoef + h->rcoef_off[f], h->g[f].total * 4, cudaMemcpyDeviceToDevice, st));
     for (int d = 0; d < h->maxL; d++) {
         if (!h->rn[d]) continue;
-        k_recompose_multi<<<persistent_grid(h, h->rrows[d], th / 32), th, 0, st>>>(h->rseg[d], h->rn[d], h->rrows[d]);
+        k_recompose_multi<<<persistent_grid(h, 2, h->rrows[d], th / 32), th, 0, st>>>(h->rseg[d], h->rn[d], h->rrows[d]);
         PRODM_CHECK_LAUNCH("k_recompose_multi");
     }
     return PRODM_OK;
@@ -407,13 +409,32 @@ int prodm_batch_bind(prodm_batch* h, const void* const* d_fields, void* const* d
     return batch_build_segments(h);
 }
 
+int prodm_batch_set_stage_launch(prodm_batch* h, int stage, int threads_per_cta, int ctas_per_sm) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    if (stage < PRODM_BATCH_DECOMPOSE || stage > PRODM_BATCH_RECOMPOSE) return fail(PRODM_EINVAL, "unknown batch stage");
+    if (stage == PRODM_BATCH_ENCODE) {
+        if (threads_per_cta != 256) return fail(PRODM_EINVAL, "the encode stage runs 256 threads per CTA");
+        if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail(PRODM_EINVAL, "encode CTAs per SM must be in [1, 8]");
+    } else {
+        if (threads_per_cta != 64 && threads_per_cta != 128 && threads_per_cta != 256)
+            return fail(PRODM_EINVAL, "threads per CTA must be 64, 128 or 256");
+        if (ctas_per_sm < 1 || ctas_per_sm > 32) return fail(PRODM_EINVAL, "CTAs per SM must be in [1, 32]");
+    }
+    h->st_threads[stage] = threads_per_cta;
+    h->st_ctas[stage] = ctas_per_sm;
+    return PRODM_OK;
+}
+
 int prodm_batch_set_launch(prodm_batch* h, int threads_per_cta, int ctas_per_sm) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
     if (threads_per_cta != 64 && threads_per_cta != 128 && threads_per_cta != 256)
         return fail(PRODM_EINVAL, "threads per CTA must be 64, 128 or 256");
     if (ctas_per_sm < 1 || ctas_per_sm > 32) return fail(PRODM_EINVAL, "CTAs per SM must be in [1, 32]");
-    h->threads = threads_per_cta;
-    h->ctas_per_sm = ctas_per_sm;
+    for (int st = PRODM_BATCH_DECOMPOSE; st <= PRODM_BATCH_RECOMPOSE; st += 2) {
+        h->st_threads[st] = threads_per_cta;
+        h->st_ctas[st] = ctas_per_sm;
+    }
+    h->st_ctas[PRODM_BATCH_ENCODE] = ctas_per_sm < 8 ? ctas_per_sm : 8;
     return PRODM_OK;
 }
 

@@ -317,8 +317,8 @@ struct BlockWalkSmem {
     uint8_t ch_j[kMaxLevels][64];      // chain entries of each level (plane index)
     uint16_t order[kMaxLevels * 64];   // pop order: level << 8 | plane index
     uint8_t tie[kMaxLevels * 64];      // 1: the pop at this position starts a tied block
-    // every level's blocks in one list (levels in any order): level | block
-    // index within the level << 8 | entry count << 16 | first entry << 24
+    // every level's blocks in one list (levels in any order): level | entry
+    // count << 16 | first entry << 24 (their keys in the caller's blk_key)
     uint32_t binfo[kMaxLevels * 64];
     uint32_t rs[kMaxLevels];
     int nidx[kMaxLevels];
@@ -375,8 +375,8 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
         w.npos = 0;
     }
     __syncthreads();
-    // each level's chain and blocks (one thread per level): block keys in
-    // blk_key's row of the level, the blocks themselves in the shared list
+    // each level's chain and blocks (one thread per level), the blocks into
+    // one shared list
     uint8_t* lfirst = reinterpret_cast<uint8_t*>(w.order);   // [kMaxLevels][64]: first entry of each block
     if (tid < nl) {
         const int l = tid;
@@ -387,21 +387,20 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
                 const long long k = ekey[l * 64 + j];
                 if (enan[l * 64 + j]) w.fail = 1;
                 if (cnt == 0 || k < runmin) {
-                    lfirst[l * 64 + nb] = (uint8_t)cnt;
-                    blk_key[l * 64 + nb] = k;
-                    nb++;
+                    lfirst[l * 64 + nb++] = (uint8_t)cnt;
                     runmin = k;
                 }
                 w.ch_j[l][cnt++] = (uint8_t)j;
             }
         }
         w.n_ent[l] = (uint8_t)cnt;
-        if (nb) {
+        if (nb) {   // the level's blocks into the shared list: key (its first entry's) and info
             atomicAdd(&w.npos, cnt);
             const int at = atomicAdd(&w.nblk, nb);
             for (int b = 0; b < nb; b++) {
                 const int f0 = lfirst[l * 64 + b], f1 = b + 1 < nb ? lfirst[l * 64 + b + 1] : cnt;
-                w.binfo[at + b] = (uint32_t)l | (uint32_t)b << 8 | (uint32_t)(f1 - f0) << 16 | (uint32_t)f0 << 24;
+                blk_key[at + b] = ekey[l * 64 + w.ch_j[l][f0]];
+                w.binfo[at + b] = (uint32_t)l | (uint32_t)(f1 - f0) << 16 | (uint32_t)f0 << 24;
             }
         }
     }
@@ -414,18 +413,28 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
     for (int t = tid; t < nblk; t += nth) {
         const uint32_t bi = w.binfo[t];
         const int l = bi & 255;
-        const long long k = blk_key[l * 64 + ((bi >> 8) & 255)];
+        const long long k = blk_key[t];
         int rank = 0;
         bool tie = false;
-#pragma unroll 8
-        for (int u = 0; u < nblk; u++) {
-            const uint32_t b2 = w.binfo[u];
+        auto count = [&](long long k2, uint32_t b2) {
             const int l2 = b2 & 255;
-            const long long k2 = blk_key[l2 * 64 + ((b2 >> 8) & 255)];
             const bool eq = k2 == k && l2 != l;
             tie |= eq;
             if (k2 > k || (eq && l2 < l)) rank += (b2 >> 16) & 255;
+        };
+        int u = 0;
+        for (; u + 8 <= nblk; u += 8) {   // eight blocks' loads in flight, then their counts
+            long long k2[8];
+            uint32_t b2[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                k2[q] = blk_key[u + q];
+                b2[q] = w.binfo[u + q];
+            }
+#pragma unroll
+            for (int q = 0; q < 8; q++) count(k2[q], b2[q]);
         }
+        for (; u < nblk; u++) count(blk_key[u], w.binfo[u]);
         const int f0 = bi >> 24, n = (bi >> 16) & 255;
         for (int e = 0; e < n; e++) {
             w.order[rank + e] = (uint16_t)(l << 8 | w.ch_j[l][f0 + e]);
@@ -433,10 +442,17 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
         }
     }
     __syncthreads();
+    // each pop's two estimate terms as indices into ev (the block list is
+    // free again): ev[lo] leaves the estimate, ev[hi] enters it
+    uint32_t* terms = w.binfo;
+    for (int p = tid; p < w.npos; p += nth) {
+        const int o = w.order[p], l = o >> 8, j = o & 255;
+        terms[p] = (uint32_t)(l * 65 + j) | (uint32_t)(l * 65 + j + en[l * 64 + j]) << 16;
+    }
+    __syncthreads();
     // the estimate along the order (thread 0): each round loads eight pops'
     // terms, runs the two dependent double adds per pop, then compares the
-    // eight estimates with the tolerance as order-preserving integers (a NaN
-    // estimate is never below it)
+    // eight estimates with the tolerance
     if (tid == 0) {
         const int np = w.npos;
         int stop = np;   // pops [0, stop)
@@ -445,34 +461,28 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
             stop = 0;
         } else {
             double acc = w.acc0;
-            long long tkey;
-            int tnan;
-            eff_key(tol, tkey, tnan);
             for (int p = 0; p < np && stop == np && !bail; p += 8) {
+                uint32_t tq[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) tq[u] = p + u < np ? terms[p + u] : 0u;
                 double sub[8], add[8];
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
-                    sub[u] = 0;
-                    add[u] = 0;
-                    if (p + u < np) {
-                        const int o = w.order[p + u], l = o >> 8, j = o & 255;
-                        sub[u] = ev[l * 65 + j];
-                        add[u] = ev[l * 65 + j + en[l * 64 + j]];
-                    }
+                    sub[u] = p + u < np ? ev[tq[u] & 0xffffu] : 0.0;
+                    add[u] = p + u < np ? ev[tq[u] >> 16] : 0.0;
                 }
-                long long akey[8];
-                int anan[8];
+                double a[8];
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
                     acc -= sub[u];   // past np: - 0 + 0, never compared
                     acc += add[u];
-                    eff_key(acc, akey[u], anan[u]);
+                    a[u] = acc;
                 }
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
                     if (p + u >= np || stop < np || bail) continue;
                     if (w.tie[p + u]) bail = true;
-                    else if (!anan[u] && !tnan && akey[u] < tkey) stop = p + u + 1;
+                    else if (a[u] < tol) stop = p + u + 1;
                 }
             }
         }
@@ -502,7 +512,7 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
 // one CTA per field: all threads tabulate the efficiencies, warp 0 walks the
 // levels (the exact heap walk on thread 0 when the warp walk declines)
 template <class T>
-__global__ void __launch_bounds__(256) k_interpret(int nfields, int kind, int est_kind, const int* __restrict__ ndims,
+__global__ void __launch_bounds__(256, 1) k_interpret(int nfields, int kind, int est_kind, const int* __restrict__ ndims,
                                                    const int* __restrict__ levels, double s, int B,
                                                    const uint32_t* __restrict__ sizes, uint64_t sz_stride,
                                                    const double* __restrict__ errs, uint64_t err_stride,

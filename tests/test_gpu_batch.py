@@ -90,9 +90,11 @@ def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
     shapes = [(65, 65, 65), (129, 129), (33, 65, 17)]
     xs = [fields.spectral_grf(s, seed=10 + i) for i, s in enumerate(shapes)]
     batch = api.MDRBatch(xs, None, 32)
-    t, c, timings = autotune.tune(batch, reps=1)
-    assert (t, c) in autotune.CANDIDATES and len(timings) == len(autotune.CANDIDATES)
-    assert autotune.tune(batch)[:2] == (t, c)          # served from the cache
+    tuned, timings = autotune.tune(batch, reps=1)
+    for stage, shape in tuned.items():
+        assert shape in autotune.STAGE_CANDIDATES[stage]
+    assert len(timings) == sum(len(c) for c in autotune.STAGE_CANDIDATES.values())
+    assert autotune.tune(batch)[0] == tuned            # served from the cache
     batch.set_tolerances([1e-3] * 3)
     ref = None
     for capture in (False, True):
