@@ -603,12 +603,34 @@ constexpr int GR_WARPS = 8;
 constexpr int GR_BPW = 32;                       // blocks per warp
 constexpr int GR_CHUNK = GR_WARPS * GR_BPW;      // blocks per CTA
 
-template <class T>
+// |trunc(ldexp(v, B - exp))| and the sign (GroupedBPEncoder.hpp:41-42). For
+// doubles whose scaled value is not needed (SH false: no error tables) the
+// magnitude comes from the bits with integer operations (fixed_mag).
+template <class T, bool SH = true>
 __device__ __forceinline__ typename Traits<T>::FP gr_mag(T v, int B, int exp, bool& neg, T& shifted) {
-    shifted = ldexp_t(v, B - exp);                  // :41
-    int64_t fix = (int64_t)shifted;                 // :42
-    neg = v < 0;
-    return (typename Traits<T>::FP)(neg ? -fix : fix);
+    if constexpr (std::is_same<T, double>::value && !SH) {
+        neg = below_zero(v);
+        return fixed_mag(v, B - exp);
+    } else {
+        shifted = ldexp_t(v, B - exp);                  // :41
+        int64_t fix = (int64_t)shifted;                 // :42
+        neg = v < 0;
+        return (typename Traits<T>::FP)(neg ? -fix : fix);
+    }
+}
+
+// ldexp((T)acc, s), negated when neg (GroupedBPEncoder.hpp:359-368); for
+// doubles with a normal result by integer operations (fixed_value)
+template <class T>
+__device__ __forceinline__ T gr_value(typename Traits<T>::FP acc, int s, bool neg) {
+    if constexpr (std::is_same<T, double>::value) {
+        if (fixed_value_normal(s)) {
+            const long long b = __double_as_longlong(fixed_value(acc, s));
+            return __longlong_as_double(neg ? b ^ (long long)0x8000000000000000ull : b);
+        }
+    }
+    const T v = ldexp_t((T)acc, s);
+    return neg ? -v : v;
 }
 
 // word counts contributed by a block with recording plane r to plane p
@@ -643,7 +665,7 @@ __global__ void __launch_bounds__(256) k_gr_rb(const T* __restrict__ x, uint64_t
             if (i < n) {
                 bool neg;
                 T sh;
-                FP q = gr_mag<T>(x[i], B, exp, neg, sh);
+                FP q = gr_mag<T, ERR>(x[i], B, exp, neg, sh);
                 orv |= q;
                 if (ERR) gr_errors(acc, (A)fabs(sh), B);
             }
@@ -674,11 +696,14 @@ __global__ void __launch_bounds__(256) k_gr_rb(const T* __restrict__ x, uint64_t
 }
 
 // exclusive scan of chunk_words over chunks, per plane; stream byte sizes.
+// One CTA per plane (the planes are independent).
 __global__ void k_gr_scan(const uint32_t* __restrict__ chunk_words, uint64_t nchunks, int B, uint64_t nblocks,
                           int word_bytes, uint32_t* __restrict__ chunk_off, uint32_t* __restrict__ sizes) {
     __shared__ uint32_t wsum[32];
     __shared__ uint32_t carry;
-    for (int p = 0; p < B; p++) {
+    {
+        const int p = blockIdx.x;
+        if (p >= B) return;
         if (threadIdx.x == 0) carry = 0;
         __syncthreads();
         for (uint64_t base = 0; base < nchunks; base += blockDim.x) {
@@ -742,7 +767,7 @@ __device__ __forceinline__ void gr_warp_offsets(const uint8_t* __restrict__ rbs,
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) k_gr_write(const T* __restrict__ x, uint64_t n,
+__global__ void __launch_bounds__(256, 4) k_gr_write(const T* __restrict__ x, uint64_t n,
                                                   const typename KeyOf<T>::type* __restrict__ maxkey, int exp_arg,
                                                   int B, const uint8_t* __restrict__ rbs,
                                                   const uint32_t* __restrict__ chunk_off,
@@ -768,18 +793,37 @@ __global__ void __launch_bounds__(256) k_gr_write(const T* __restrict__ x, uint6
             q[h] = 0;
             if (i < n) {
                 T sh;
-                q[h] = gr_mag<T>(x[i], B, exp, neg, sh);
+                q[h] = gr_mag<T, false>(x[i], B, exp, neg, sh);
             }
             sign |= (S)__ballot_sync(FULL, neg) << (h * 32);
         }
         const int r = rbs[b];
         S mine0 = 0, mine1 = 0;
-        for (int p = r; p < B; p++) {                          // encode_block :337-357
-            const int k = B - 1 - p;
-            S w = (S)__ballot_sync(FULL, (q[0] >> k) & 1u);
-            if (BS == 64) w |= (S)__ballot_sync(FULL, (q[BS / 32 - 1] >> k) & 1u) << (BS == 64 ? 32 : 0);
-            if ((p & 31) == lane) {
-                if (p < 32) mine0 = w; else mine1 = w;
+        if constexpr (BS == 64) {
+            // encode_block :337-357 by four warp bit transposes: lane k gets the
+            // words of magnitude bit k (low halves) and bit 32 + k (high halves)
+            // of values 0..31 and 32..63; lane p then fetches plane p (bit
+            // B-1-p) and plane p + 32 (bit B-33-p). Planes below r are not written.
+            const uint32_t lo0 = transpose32((uint32_t)q[0], lane), hi0 = transpose32((uint32_t)(q[0] >> 32), lane);
+            const uint32_t lo1 = transpose32((uint32_t)q[1], lane), hi1 = transpose32((uint32_t)(q[1] >> 32), lane);
+            S w[2];
+#pragma unroll
+            for (int t = 0; t < 2; t++) {   // plane lane + 32 t (a valid plane for the shuffles' sake)
+                const int p = lane + 32 * t < B ? lane + 32 * t : 0;
+                const int k = B - 1 - p, src = k & 31;
+                const uint32_t a0 = __shfl_sync(FULL, lo0, src), b0 = __shfl_sync(FULL, hi0, src);
+                const uint32_t a1 = __shfl_sync(FULL, lo1, src), b1 = __shfl_sync(FULL, hi1, src);
+                w[t] = k >= 32 ? ((S)b1 << 32 | b0) : ((S)a1 << 32 | a0);
+            }
+            mine0 = lane >= r ? w[0] : 0;
+            mine1 = lane + 32 >= r ? w[1] : 0;
+        } else {
+            for (int p = r; p < B; p++) {                      // encode_block :337-357
+                const int k = B - 1 - p;
+                S w = (S)__ballot_sync(FULL, (q[0] >> k) & 1u);
+                if ((p & 31) == lane) {
+                    if (p < 32) mine0 = w; else mine1 = w;
+                }
             }
         }
         if (lane < B && lane >= r) {
@@ -1011,20 +1055,35 @@ __global__ void __launch_bounds__(256) k_gr_decode(const typename Traits<T>::S* 
             FP acc[BS / 32];
 #pragma unroll
             for (int h = 0; h < BS / 32; h++) acc[h] = 0;
-            const int first = r > s ? r : s;
-            for (int p = first; p < e; p++) {                 // decode_block :359-368
-                S w = __shfl_sync(FULL, p < 32 ? w0 : w1, p & 31);
-                const int k = e - 1 - p;
+            if constexpr (BS == 64) {
+                // decode_block :359-368 by four warp bit transposes: lane p holds
+                // planes p and p + 32 (zero where not read); after the
+                // transposes lane v holds, per half h of the block, a word whose
+                // bit p is plane p's bit of value 32 h + v (planes 0..31) and one
+                // for planes 32..63. Plane p weighs 2^(e-1-p): the bit-reversed
+                // words, shifted into place.
+                const uint32_t pl0 = transpose32((uint32_t)w0, lane), ph0 = transpose32((uint32_t)(w0 >> 32), lane);
+                const uint32_t pl1 = transpose32((uint32_t)w1, lane), ph1 = transpose32((uint32_t)(w1 >> 32), lane);
+                const uint32_t lo[2] = {pl0, ph0}, hi[2] = {pl1, ph1};
 #pragma unroll
-                for (int h = 0; h < BS / 32; h++) acc[h] |= (FP)((w >> (h * 32 + lane)) & 1u) << k;
+                for (int h = 0; h < 2; h++) {
+                    // planes 0..31 -> bits e-1 .. e-32, planes 32..63 -> bits e-33 ..
+                    const uint64_t a = (uint64_t)__brev(lo[h]) << 32 | __brev(hi[h]);   // plane p at bit 63 - p
+                    acc[h] = (FP)(e > 0 ? a >> (64 - e) : 0ull);
+                }
+            } else {
+                const int first = r > s ? r : s;
+                for (int p = first; p < e; p++) {             // decode_block :359-368
+                    S w = __shfl_sync(FULL, p < 32 ? w0 : w1, p & 31);
+                    const int k = e - 1 - p;
+#pragma unroll
+                    for (int h = 0; h < BS / 32; h++) acc[h] |= (FP)((w >> (h * 32 + lane)) & 1u) << k;
+                }
             }
 #pragma unroll
             for (int h = 0; h < BS / 32; h++) {
                 uint64_t i = b * BS + h * 32 + lane;
-                if (i < n) {
-                    T v = ldexp_t((T)acc[h], -e + exp);
-                    out[i] = ((sign >> (h * 32 + lane)) & 1u) ? -v : v;
-                }
+                if (i < n) out[i] = gr_value<T>(acc[h], -e + exp, (sign >> (h * 32 + lane)) & 1u);
             }
         } else {
 #pragma unroll
@@ -1283,7 +1342,7 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
         k_gr_rb32<<<(unsigned)nch, GR_WARPS * 32, 0, st>>>((const float*)x, n, (const uint32_t*)maxkey, exp, B, rbs,
                                                           chunk_words);
         PRODM_CHECK_LAUNCH("k_gr_rb32");
-        k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, 4, chunk_off, sizes);
+        k_gr_scan<<<B, 1024, 0, st>>>(chunk_words, nch, B, nblocks, 4, chunk_off, sizes);
         PRODM_CHECK_LAUNCH("k_gr_scan");
         unsigned long long* recs = (unsigned long long*)partial;
         if (errs_out) {
@@ -1314,7 +1373,7 @@ int launch_gr_encode(const T* x, uint64_t n, const void* maxkey, int exp, int B,
         k_reduce_partials<T><<<(B + 8) / 8, 256, 0, st>>>(partial, (int)nch, B, (const K*)maxkey, exp, 0, 1, errs_out);
         PRODM_CHECK_LAUNCH("k_reduce_partials");
     }
-    k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nch, B, nblocks, (int)sizeof(typename Traits<T>::S), chunk_off, sizes);
+    k_gr_scan<<<B, 1024, 0, st>>>(chunk_words, nch, B, nblocks, (int)sizeof(typename Traits<T>::S), chunk_off, sizes);
     PRODM_CHECK_LAUNCH("k_gr_scan");
     k_gr_write<T><<<(unsigned)nch, GR_WARPS * 32, 0, st>>>(x, n, (const K*)maxkey, exp, B, rbs, chunk_off,
                                                            (typename Traits<T>::S*)out, cap);
@@ -1331,7 +1390,7 @@ int launch_chunk_words_from_rb(const uint8_t* rbs, uint64_t nblocks, int B, uint
 
 int launch_gr_scan_only(const uint32_t* chunk_words, uint64_t nchunks, int B, uint64_t nblocks, int word_bytes,
                         uint32_t* chunk_off, uint32_t* sizes, cudaStream_t st) {
-    k_gr_scan<<<1, 1024, 0, st>>>(chunk_words, nchunks, B, nblocks, word_bytes, chunk_off, sizes);
+    k_gr_scan<<<B, 1024, 0, st>>>(chunk_words, nchunks, B, nblocks, word_bytes, chunk_off, sizes);
     PRODM_CHECK_LAUNCH("k_gr_scan");
     return PRODM_OK;
 }

@@ -167,6 +167,54 @@ __device__ __forceinline__ int frexp_exp(double v) { int e; frexp(v, &e); return
 __device__ __forceinline__ float ldexp_t(float v, int e) { return ldexpf(v, e); }
 __device__ __forceinline__ double ldexp_t(double v, int e) { return ldexp(v, e); }
 
+// floor(|v| * 2^k) of a double whose scaled magnitude stays below 2^63 (the
+// encoders' |trunc(ldexp(v, k))|), from its exponent and mantissa bits with
+// integer operations: GB300's FP64 pipe takes about two lane operations per
+// SM cycle, too slow for a conversion per value
+__device__ __forceinline__ uint64_t fixed_mag(double v, int k) {
+    const uint64_t bits = (uint64_t)__double_as_longlong(v);
+    const int ev = (int)((bits >> 52) & 0x7ff);
+    uint64_t m = bits & 0xfffffffffffffull;
+    int e = -1074;
+    if (ev) {
+        m |= 1ull << 52;
+        e = ev - 1075;
+    }
+    const int sh = e + k;   // |v| * 2^k = m * 2^sh
+    if (sh >= 0) return m << sh;
+    return sh <= -64 ? 0ull : m >> (-sh);
+}
+// v < 0 for a double that is not NaN, without an FP64 comparison
+__device__ __forceinline__ bool below_zero(double v) {
+    const uint64_t bits = (uint64_t)__double_as_longlong(v);
+    return (bits >> 63) && (bits << 1) != 0;
+}
+// ldexp((double)acc, s) for results that are normal (-1022 <= s <= 960): acc
+// rounded once to 53 bits (nearest, ties to even, as the conversion does) and
+// the exponent field written directly
+__device__ __forceinline__ double fixed_value(uint64_t acc, int s) {
+    if (acc == 0) return 0.0;
+    const int msb = 63 - __clzll((long long)acc);
+    int e2 = msb;
+    uint64_t mant;
+    if (msb <= 52) {
+        mant = acc << (52 - msb);
+    } else {
+        const int sh = msb - 52;
+        mant = acc >> sh;
+        const uint64_t rem = acc & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1))) {
+            mant++;
+            if (mant >> 53) {
+                mant >>= 1;
+                e2++;
+            }
+        }
+    }
+    return __longlong_as_double((long long)(((uint64_t)(e2 + s + 1023) << 52) | (mant & 0xfffffffffffffull)));
+}
+__device__ __forceinline__ bool fixed_value_normal(int s) { return s >= -1022 && s <= 960; }
+
 // uncontracted arithmetic (no FMA fusion), so that results match a host
 // evaluation of the same expression tree operation by operation
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }

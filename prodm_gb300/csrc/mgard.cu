@@ -337,22 +337,23 @@ __global__ void k_l2_line(const T* __restrict__ src, Box S, int d, T* __restrict
 }
 
 // The dim-2 (contiguous) pass of the L2 projection with shared-memory staging:
-// one warp per 32 lines (fine rows (x0, x1) of F). Forward sweep: tiles of 32
+// one warp per 32 lines (fine rows (x0, x1) of F). Forward sweep: tiles of 16
 // fine columns plus two halo columns each side are staged with coalesced
-// loads (the 32 x 36 values as one flat loop); lane r then sweeps row r's
+// loads (the 32 x 20 values as one flat loop); lane r then sweeps row r's
 // coarse nodes of the tile (right-hand side from the 5-point neighbourhood,
 // Thomas forward step) into an output tile stored with coalesced writes.
-// Backward sweep: the stored values come back from the end in 32-node chunks
+// Backward sweep: the stored values come back from the end in 16-node chunks
 // (in the input tile, free by then), lane r substitutes back along its row,
-// and they are stored again. About 14 KB of shared memory per warp, so about
-// 15 warps share an SM. PACKED: the rows are read straight from the level's
+// and they are stored again. About 8 KB of shared memory per warp, so about
+// 28 warps share an SM (with 32-column tiles, 14 KB and 15 warps, the
+// passes took 9 % longer at 513 x 513 x 257 fp64). PACKED: the rows are read straight from the level's
 // packed coefficients (a natural row is an even/odd split of one contiguous
 // run of interleaved ranks; coarse nodes of rows inside the coarse box are
 // zero), so no natural-order copy is needed; else from a natural field.
-constexpr int L2_TILE = 32;                 // fine columns per tile
-constexpr int L2_STAGE = L2_TILE + 4;       // staged columns: 2 + 32 + 2
-constexpr int L2_IN_LD = L2_STAGE + 1;      // odd stride (no bank conflicts); also holds 32-node chunks
-constexpr int L2_OUT_LD = 17;               // up to 17 coarse nodes per tile, odd stride
+constexpr int L2_TILE = 16;                 // fine columns per tile
+constexpr int L2_STAGE = L2_TILE + 4;       // staged columns: 2 + 16 + 2
+constexpr int L2_IN_LD = L2_STAGE + 1;      // odd stride (no bank conflicts); also holds 16-node chunks
+constexpr int L2_OUT_LD = 9;                // up to 9 coarse nodes per tile, odd stride
 
 template <class T, class W, bool PACKED>
 __global__ void __launch_bounds__(32) k_l2_rows(const T* __restrict__ src, Box F, Box C, T* __restrict__ dst,
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(32) k_l2_rows(const T* __restrict__ src, Box F
     W z = 0;
     uint32_t mhi = nc;
     while (mhi > 0) {
-        const uint32_t mlo = mhi > 32 ? mhi - 32 : 0;
+        const uint32_t mlo = mhi > L2_TILE ? mhi - L2_TILE : 0;
         const int cnt = (int)(mhi - mlo);
         for (int i = lane; i < nl * cnt; i += 32) {
             const int r = i / cnt, j = i - r * cnt;

@@ -41,19 +41,7 @@ __device__ __forceinline__ int pb_exp(const typename KeyOf<T>::type* maxkey, int
 // is taken from the exponent and mantissa bits with integer operations
 // (GB300's FP64 pipe is slow); for floats by one multiplication with an exact
 // power of two where that is a normal float, else ldexpf.
-__device__ __forceinline__ uint64_t pb_mag(double v, int k, bool, float) {
-    const uint64_t bits = (uint64_t)__double_as_longlong(v);
-    const int ev = (int)((bits >> 52) & 0x7ff);
-    uint64_t m = bits & 0xfffffffffffffull;
-    int e = -1074;
-    if (ev) {
-        m |= 1ull << 52;
-        e = ev - 1075;
-    }
-    const int sh = e + k;   // |v| * 2^k = m * 2^sh
-    if (sh >= 0) return m << sh;
-    return sh <= -64 ? 0ull : m >> (-sh);
-}
+__device__ __forceinline__ uint64_t pb_mag(double v, int k, bool, float) { return fixed_mag(v, k); }
 __device__ __forceinline__ uint32_t pb_mag(float v, int k, bool fast, float sc) {
     return (uint32_t)fabsf(fast ? v * sc : ldexpf(v, k));
 }
@@ -65,26 +53,7 @@ __device__ __forceinline__ bool pb_neg(float v) { return v < 0.f; }
 // ties to even, as the conversion does) and the exponent field written
 // directly; otherwise, and for floats, the conversion and an exact scaling.
 __device__ __forceinline__ double pb_value(uint64_t acc, int s, bool fast, float) {
-    if (!fast) return ldexp((double)acc, s);
-    if (acc == 0) return 0.0;
-    const int msb = 63 - __clzll((long long)acc);
-    int e2 = msb;
-    uint64_t mant;
-    if (msb <= 52) {
-        mant = acc << (52 - msb);
-    } else {
-        const int sh = msb - 52;
-        mant = acc >> sh;
-        const uint64_t rem = acc & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-        if (rem > half || (rem == half && (mant & 1))) {
-            mant++;
-            if (mant >> 53) {
-                mant >>= 1;
-                e2++;
-            }
-        }
-    }
-    return __longlong_as_double((long long)(((uint64_t)(e2 + s + 1023) << 52) | (mant & 0xfffffffffffffull)));
+    return fast ? fixed_value(acc, s) : ldexp((double)acc, s);
 }
 __device__ __forceinline__ float pb_value(uint32_t acc, int s, bool fast, float sc) {
     return fast ? (float)acc * sc : ldexpf((float)acc, s);
@@ -93,7 +62,7 @@ __device__ __forceinline__ double pb_negate(double v) {
     return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
 }
 __device__ __forceinline__ float pb_negate(float v) { return -v; }
-__device__ __forceinline__ bool pb_value_fast(double*, int s) { return s >= -1022 && s <= 960; }
+__device__ __forceinline__ bool pb_value_fast(double*, int s) { return fixed_value_normal(s); }
 __device__ __forceinline__ bool pb_value_fast(float*, int s) { return pow2_normal(s); }
 
 __device__ __forceinline__ uint32_t valid_mask(int nvalid) { return nvalid >= 32 ? FULL : ((1u << nvalid) - 1u); }
