@@ -184,7 +184,8 @@ int prodm_collect_squared_noalloc(int dtype, const void* d_data, uint64_t n, int
                                   double max_level_error, double* d_out, void* stream);
 
 /* ---------------------------------------------------------------------------
- * Packed level coefficients <-> natural field, hierarchical basis.
+ * Packed level coefficients <-> natural field (hierarchical basis; the
+ * _basis forms below take either basis).
  * prodm_recompose_packed: d_coef holds every level's coefficients packed as
  * the retrieval decodes them (level 0 box, then box(l) minus box(l-1) per
  * level in interleaved order, the layout of prodm_mdr_coefficients); output
@@ -204,6 +205,21 @@ int prodm_recompose_packed(int dtype, const void* d_coef, int ndims, const uint3
                            void* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
 int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint32_t* dims, uint32_t target_level,
                             void* d_grad_coef, void* d_workspace, size_t workspace_bytes, void* stream);
+/* The same three for either basis (PRODM_BASIS_HIERARCHICAL as above, or
+ * PRODM_BASIS_ORTHOGONAL: MGARDOrthoganalDecomposer's recomposition,
+ * MGARD.hpp:11-39, which removes each level's L2 correction from its coarse
+ * box before interpolating; its adjoint runs the correction's transpose --
+ * per dim a coarse mass-matrix solve, the interpolation and the fine mass
+ * matrix). The orthogonal workspace adds the correction's scratch boxes and
+ * the adjoint's, the largest the level-L box. */
+int prodm_recompose_packed_basis_workspace(int dtype, int basis, int ndims, const uint32_t* dims,
+                                           uint32_t target_level, size_t* bytes);
+int prodm_recompose_packed_basis(int dtype, int basis, const void* d_coef, int ndims, const uint32_t* dims,
+                                 uint32_t target_level, void* d_out, void* d_workspace, size_t workspace_bytes,
+                                 void* stream);
+int prodm_recompose_adjoint_basis(int dtype, int basis, const void* d_grad, int ndims, const uint32_t* dims,
+                                  uint32_t target_level, void* d_grad_coef, void* d_workspace, size_t workspace_bytes,
+                                  void* stream);
 
 /* ---------------------------------------------------------------------------
  * GE quantities of interest (fp64 fields), for QoI-bounded retrieval.

@@ -60,6 +60,9 @@ _SIGS = {
     "prodm_recompose_packed_workspace": (_i, [_i, _i, _u32p, C.c_uint32, C.POINTER(C.c_size_t)]),
     "prodm_recompose_packed": (_i, [_i, _P, _i, _u32p, C.c_uint32, _P, _P, C.c_size_t, _P]),
     "prodm_recompose_adjoint": (_i, [_i, _P, _i, _u32p, C.c_uint32, _P, _P, C.c_size_t, _P]),
+    "prodm_recompose_packed_basis_workspace": (_i, [_i, _i, _i, _u32p, C.c_uint32, C.POINTER(C.c_size_t)]),
+    "prodm_recompose_packed_basis": (_i, [_i, _i, _P, _i, _u32p, C.c_uint32, _P, _P, C.c_size_t, _P]),
+    "prodm_recompose_adjoint_basis": (_i, [_i, _i, _P, _i, _u32p, C.c_uint32, _P, _P, C.c_size_t, _P]),
     "prodm_qoi_ge_values": (_i, [_i, _P, _P, _P, _P, _P, C.c_uint64, _P, _P, _P, _P, _P, _P, _P]),
     "prodm_qoi_ge_bounds": (_i, [_i, _P, _P, _P, _P, _P, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, _P, _P, _P, _P]),

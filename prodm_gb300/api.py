@@ -169,27 +169,27 @@ def collect_squared(data, num_bitplanes, max_level_error, stream=None):
     return out.cpu().numpy()
 
 
-def recompose_packed(coef, shape, target_level, out=None, stream=None):
+def recompose_packed(coef, shape, target_level, out=None, stream=None, basis="hierarchical"):
     """Packed level coefficients (the layout of MDRField.coefficients()) ->
-    natural-order field of `shape` (hierarchical basis)."""
+    natural-order field of `shape` (hierarchical or orthogonal basis)."""
     shape = tuple(int(n) for n in shape)
     if out is None:
         out = torch.empty(shape, dtype=coef.dtype, device=coef.device)
     dims = _u32(shape)
-    call("prodm_recompose_packed", _dtype(coef), _ptr(coef), len(shape), dims, int(target_level), _ptr(out), None, 0,
-         _stream(stream))
+    call("prodm_recompose_packed_basis", _dtype(coef), BASIS[basis], _ptr(coef), len(shape), dims, int(target_level),
+         _ptr(out), None, 0, _stream(stream))
     return out
 
 
-def recompose_adjoint(grad, target_level, out=None, stream=None):
+def recompose_adjoint(grad, target_level, out=None, stream=None, basis="hierarchical"):
     """Transpose of recompose_packed: gradient with respect to the natural-order
     field -> gradient with respect to the packed level coefficients."""
     shape = tuple(grad.shape)
     if out is None:
         out = torch.empty(grad.numel(), dtype=grad.dtype, device=grad.device)
     dims = _u32(shape)
-    call("prodm_recompose_adjoint", _dtype(grad), _ptr(grad.contiguous()), len(shape), dims, int(target_level),
-         _ptr(out), None, 0, _stream(stream))
+    call("prodm_recompose_adjoint_basis", _dtype(grad), BASIS[basis], _ptr(grad.contiguous()), len(shape), dims,
+         int(target_level), _ptr(out), None, 0, _stream(stream))
     return out
 
 

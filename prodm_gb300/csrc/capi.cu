@@ -1437,35 +1437,84 @@ int mdr_load_level(prodm_mdr* h, int l, const void* src, uint64_t off, uint64_t 
 }  // namespace prodm
 
 // ===========================================================================
-// packed level coefficients <-> natural field (hierarchical basis), the pair
-// behind the QoI gradient: forward = reposition every level + recompose
-// (ComposedReconstructor.hpp:124-131 with MGARD.hpp:25-35), adjoint = its
-// transpose. Workspace: two boxes of level L-1.
+// packed level coefficients <-> natural field, the pair behind the QoI
+// gradient: forward = reposition every level + recompose
+// (ComposedReconstructor.hpp:124-131 with MGARD.hpp:25-35; the orthogonal
+// basis removes each level's L2 correction from its coarse box first),
+// adjoint = its transpose. Workspace: two boxes of level L-1; orthogonal
+// adds the Thomas tables, the correction's scratch boxes of level L and the
+// adjoint's (boxes (n0, c1, c2), (n0, n1, c2), the level-L box, one coarse box).
 namespace prodm {
+void packed_pair_reserve(Workspace& ws, const LevelGeom& g, int basis, size_t es) {
+    const int L = g.L;
+    if (L == 0) return;
+    const size_t cb = g.box[L - 1].size() * es;
+    ws.reserve(cb);
+    ws.reserve(cb);
+    if (basis != PRODM_BASIS_ORTHOGONAL) return;
+    const Box& F = g.box[L];
+    const Box& C = g.box[L - 1];
+    ws.reserve((tab_elems(g) + 1) * es);
+    ws.reserve((uint64_t)F.n[0] * C.n[1] * C.n[2] * es);   // t2 / s_a
+    ws.reserve((uint64_t)F.n[0] * F.n[1] * C.n[2] * es);   // t1 / s_b
+    ws.reserve(F.size() * es);                               // s_w
+    ws.reserve(C.size() * es);                               // z / s_u
+}
+
 template <class T>
-int packed_pair_impl(const T* in, int ndims, const uint32_t* dims, int L, T* out, bool adjoint, void* wsp, size_t wsb,
-                     cudaStream_t st) {
+int packed_pair_impl(const T* in, int ndims, const uint32_t* dims, int L, T* out, bool adjoint, int basis, void* wsp,
+                     size_t wsb, cudaStream_t st) {
     LevelGeom g;
     int rc;
     if ((rc = make_geom(ndims, dims, L, g))) return rc;
     if (L > max_level(ndims, dims)) return fail(PRODM_EINVAL, "target level above the maximum for these dims");
+    if (basis != PRODM_BASIS_HIERARCHICAL && basis != PRODM_BASIS_ORTHOGONAL) return fail(PRODM_EINVAL, "unknown basis");
     if (L == 0) {
         PRODM_CUDA(cudaMemcpyAsync(out, in, g.total * sizeof(T), cudaMemcpyDeviceToDevice, st));
         return PRODM_OK;
     }
+    const bool orth = basis == PRODM_BASIS_ORTHOGONAL;
     const size_t cb = g.box[L - 1].size() * sizeof(T);
     Workspace ws(wsp, wsb, st);
-    ws.reserve(cb);
-    ws.reserve(cb);
+    packed_pair_reserve(ws, g, basis, sizeof(T));
     if ((rc = ws.commit())) return rc;
     T* buf[2] = {(T*)ws.take(cb), (T*)ws.take(cb)};
+    T *dtab = nullptr, *s_a = nullptr, *s_b = nullptr, *s_w = nullptr, *s_u = nullptr;
+    std::vector<size_t> toff;
+    if (orth) {
+        const Box& F = g.box[L];
+        const Box& C = g.box[L - 1];
+        std::vector<T> tab = build_tabs<T>(g, toff);
+        dtab = (T*)ws.take((tab_elems(g) + 1) * sizeof(T));
+        s_a = (T*)ws.take((uint64_t)F.n[0] * C.n[1] * C.n[2] * sizeof(T));
+        s_b = (T*)ws.take((uint64_t)F.n[0] * F.n[1] * C.n[2] * sizeof(T));
+        s_w = (T*)ws.take(F.size() * sizeof(T));
+        s_u = (T*)ws.take(C.size() * sizeof(T));
+        PRODM_CUDA(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        PRODM_CUDA(cudaStreamSynchronize(st));   // host table lifetime
+    }
+    auto tabs_of = [&](int l, const T* (&t)[3]) {
+        for (int d = 0; d < 3; d++) t[d] = dtab + toff[l * 3 + d];
+    };
     if (!adjoint) {
         for (int l = 1; l <= L; l++) {
             const Box& F = g.box[l];
+            const Box& C = g.box[l - 1];
             const T* cin = (l == 1) ? in + g.offset[0] : buf[(l - 1) & 1];
             T* o = (l == L) ? out : buf[l & 1];
-            if ((rc = launch_recompose_level_packed<T>(cin, in + g.offset[l], F, g.box[l - 1], o,
-                                                       (uint64_t)F.n[1] * F.n[2], F.n[2], st)))
+            if (orth) {   // coarse box minus the level's correction (a copy of level 0 first)
+                if (l == 1) {
+                    PRODM_CUDA(cudaMemcpyAsync(buf[0], cin, C.size() * sizeof(T), cudaMemcpyDeviceToDevice, st));
+                    cin = buf[0];
+                }
+                const T* tabs[3];
+                tabs_of(l, tabs);
+                if ((rc = launch_l2_correction<T>(nullptr, F, s_b, s_a, s_u, tabs, st, in + g.offset[l], &C))) return rc;
+                if ((rc = launch_add_box<T>(const_cast<T*>(cin), (uint64_t)C.n[1] * C.n[2], C.n[2], s_u, C, (T)-1, st)))
+                    return rc;
+            }
+            if ((rc = launch_recompose_level_packed<T>(cin, in + g.offset[l], F, C, o, (uint64_t)F.n[1] * F.n[2], F.n[2],
+                                                       st)))
                 return rc;
         }
         return PRODM_OK;
@@ -1473,8 +1522,15 @@ int packed_pair_impl(const T* in, int ndims, const uint32_t* dims, int L, T* out
     const T* gin = in;
     for (int l = L; l >= 1; l--) {
         T* gout = (l == 1) ? out + g.offset[0] : buf[l & 1];
-        if ((rc = launch_recompose_adjoint_level<T>(gin, g.box[l], g.box[l - 1], out + g.offset[l], gout, st)))
-            return rc;
+        if (orth) {
+            const T* tabs[3];
+            tabs_of(l, tabs);
+            rc = launch_recompose_adjoint_level_orth<T>(gin, g.box[l], g.box[l - 1], out + g.offset[l], gout, tabs, s_a,
+                                                        s_b, s_w, s_u, st);
+        } else {
+            rc = launch_recompose_adjoint_level<T>(gin, g.box[l], g.box[l - 1], out + g.offset[l], gout, st);
+        }
+        if (rc) return rc;
         gin = gout;
     }
     return PRODM_OK;
@@ -1642,38 +1698,58 @@ int prodm_collect_max(int dtype, double bound, int B, double* out) {
     return PRODM_OK;
 }
 
-int prodm_recompose_packed_workspace(int dtype, int ndims, const uint32_t* dims, uint32_t L, size_t* bytes) {
+int prodm_recompose_packed_basis_workspace(int dtype, int basis, int ndims, const uint32_t* dims, uint32_t L,
+                                           size_t* bytes) {
     int rc = check_dtype(dtype);
     if (rc) return rc;
     if (!dims || !bytes) return fail(PRODM_EINVAL, "NULL pointer");
+    if (basis != PRODM_BASIS_HIERARCHICAL && basis != PRODM_BASIS_ORTHOGONAL) return fail(PRODM_EINVAL, "unknown basis");
     LevelGeom g;
     if ((rc = make_geom(ndims, dims, (int)L, g))) return rc;
-    *bytes = L == 0 ? 0 : 2 * Workspace::align(g.box[L - 1].size() * esize(dtype));
+    Workspace ws(nullptr, 0, 0);
+    packed_pair_reserve(ws, g, basis, esize(dtype));
+    *bytes = ws.needed();
     return PRODM_OK;
 }
 
-int prodm_recompose_packed(int dtype, const void* d_coef, int ndims, const uint32_t* dims, uint32_t L, void* d_out,
-                           void* ws, size_t wsb, void* stream) {
+int prodm_recompose_packed_workspace(int dtype, int ndims, const uint32_t* dims, uint32_t L, size_t* bytes) {
+    return prodm_recompose_packed_basis_workspace(dtype, PRODM_BASIS_HIERARCHICAL, ndims, dims, L, bytes);
+}
+
+int prodm_recompose_packed_basis(int dtype, int basis, const void* d_coef, int ndims, const uint32_t* dims, uint32_t L,
+                                 void* d_out, void* ws, size_t wsb, void* stream) {
     int rc = check_dtype(dtype);
     if (rc) return rc;
     if (!d_coef || !d_out || !dims) return fail(PRODM_EINVAL, "prodm_recompose_packed: NULL pointer");
     if (dtype == PRODM_F64)
-        return packed_pair_impl<double>((const double*)d_coef, ndims, dims, (int)L, (double*)d_out, false, ws, wsb,
-                                        (cudaStream_t)stream);
-    return packed_pair_impl<float>((const float*)d_coef, ndims, dims, (int)L, (float*)d_out, false, ws, wsb,
+        return packed_pair_impl<double>((const double*)d_coef, ndims, dims, (int)L, (double*)d_out, false, basis, ws,
+                                        wsb, (cudaStream_t)stream);
+    return packed_pair_impl<float>((const float*)d_coef, ndims, dims, (int)L, (float*)d_out, false, basis, ws, wsb,
                                    (cudaStream_t)stream);
 }
 
-int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint32_t* dims, uint32_t L,
-                            void* d_grad_coef, void* ws, size_t wsb, void* stream) {
+int prodm_recompose_packed(int dtype, const void* d_coef, int ndims, const uint32_t* dims, uint32_t L, void* d_out,
+                           void* ws, size_t wsb, void* stream) {
+    return prodm_recompose_packed_basis(dtype, PRODM_BASIS_HIERARCHICAL, d_coef, ndims, dims, L, d_out, ws, wsb,
+                                        stream);
+}
+
+int prodm_recompose_adjoint_basis(int dtype, int basis, const void* d_grad, int ndims, const uint32_t* dims,
+                                  uint32_t L, void* d_grad_coef, void* ws, size_t wsb, void* stream) {
     int rc = check_dtype(dtype);
     if (rc) return rc;
     if (!d_grad || !d_grad_coef || !dims) return fail(PRODM_EINVAL, "prodm_recompose_adjoint: NULL pointer");
     if (dtype == PRODM_F64)
-        return packed_pair_impl<double>((const double*)d_grad, ndims, dims, (int)L, (double*)d_grad_coef, true, ws,
-                                        wsb, (cudaStream_t)stream);
-    return packed_pair_impl<float>((const float*)d_grad, ndims, dims, (int)L, (float*)d_grad_coef, true, ws, wsb,
-                                   (cudaStream_t)stream);
+        return packed_pair_impl<double>((const double*)d_grad, ndims, dims, (int)L, (double*)d_grad_coef, true, basis,
+                                        ws, wsb, (cudaStream_t)stream);
+    return packed_pair_impl<float>((const float*)d_grad, ndims, dims, (int)L, (float*)d_grad_coef, true, basis, ws,
+                                   wsb, (cudaStream_t)stream);
+}
+
+int prodm_recompose_adjoint(int dtype, const void* d_grad, int ndims, const uint32_t* dims, uint32_t L,
+                            void* d_grad_coef, void* ws, size_t wsb, void* stream) {
+    return prodm_recompose_adjoint_basis(dtype, PRODM_BASIS_HIERARCHICAL, d_grad, ndims, dims, L, d_grad_coef, ws, wsb,
+                                         stream);
 }
 
 int prodm_collect_squared_workspace(int dtype, int B, size_t* bytes) {

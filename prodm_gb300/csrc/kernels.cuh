@@ -43,6 +43,11 @@ int launch_interleave(T* data, uint64_t s0, uint64_t s1, const Box& F, const Box
 // coarse box C, natural order)
 template <class T>
 int launch_recompose_adjoint_level(const T* g, const Box& F, const Box& C, T* gcoef, T* gcoarse, cudaStream_t st);
+// the same for the orthogonal basis (tabs: Thomas factors per dim; scratch
+// boxes (n0, c1, c2), (n0, n1, c2), F, and one C box)
+template <class T>
+int launch_recompose_adjoint_level_orth(const T* g, const Box& F, const Box& C, T* gcoef, T* gcoarse,
+                                        const T* const tabs[3], T* s_a, T* s_b, T* s_w, T* s_u, cudaStream_t st);
 
 // bitplane.cu
 template <class T>

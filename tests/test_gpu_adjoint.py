@@ -1,5 +1,7 @@
 """Adjoint recomposition (prodm_recompose_adjoint) and its forward pair
-(prodm_recompose_packed), hierarchical basis.
+(prodm_recompose_packed), hierarchical basis; the orthogonal basis through
+the _basis entry points (forward against the FP64 oracle, adjoint by the
+dot-product test).
 
 * forward: equal to the oracle's reposition + recompose (bit for bit in both
   precisions: the same uncontracted operations);
@@ -52,6 +54,42 @@ def test_adjoint_matches_oracle_and_dot_product(shape, L, dt):
         f = api().recompose_packed(torch.from_numpy(c).cuda(), shape, L).cpu().numpy()
         lhs, rhs = float(np.sum(f * g)), float(np.sum(c * got))
         assert abs(lhs - rhs) <= 1e-12 * (abs(lhs) + float(np.sum(np.abs(f * g))))
+
+
+ORTH_SHAPES = [((65, 65, 65), 3), ((17, 9, 33), 2), ((40, 33, 21), 2), ((100,), 5), ((33, 64), 4), ((12, 10, 7), 1),
+               ((9, 9, 9), 0), ((6, 20, 9), 1), ((33, 17, 5), 1)]
+
+
+@pytest.mark.parametrize("shape,L", ORTH_SHAPES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_orthogonal_forward_matches_oracle(shape, L, dt):
+    """Orthogonal basis: the packed recomposition (each level's L2 correction
+    removed from its coarse box, then the interpolation) against the FP64
+    oracle's recomposition of the same packed coefficients."""
+    rng = np.random.default_rng(len(shape) * 5 + L)
+    c = rng.standard_normal(int(np.prod(shape))).astype(dt)
+    got = api().recompose_packed(torch.from_numpy(c).cuda(), shape, L, basis="orthogonal").cpu().numpy()
+    ref = O.recompose_packed(c.astype(np.float64), shape, L, False)
+    tol = (2e-5 if dt == np.float32 else 1e-12) * float(np.abs(ref).max())
+    assert np.max(np.abs(got.astype(np.float64) - ref)) <= tol
+
+
+@pytest.mark.parametrize("shape,L", ORTH_SHAPES)
+def test_orthogonal_adjoint_dot_product(shape, L):
+    """<R c, g> = <c, R^T g> for the orthogonal recomposition (FP64), and the
+    fp32 adjoint within float rounding of the FP64 one."""
+    rng = np.random.default_rng(len(shape) * 13 + L)
+    g = rng.standard_normal(shape)
+    c = rng.standard_normal(int(np.prod(shape)))
+    f = api().recompose_packed(torch.from_numpy(c).cuda(), shape, L, basis="orthogonal").cpu().numpy()
+    gc = api().recompose_adjoint(torch.from_numpy(g).cuda(), L, basis="orthogonal").cpu().numpy()
+    lhs, rhs = float(np.sum(f * g)), float(np.sum(c * gc))
+    assert abs(lhs - rhs) <= 1e-11 * (float(np.sum(np.abs(f * g))) + float(np.sum(np.abs(c * gc))))
+    g32 = api().recompose_adjoint(torch.from_numpy(g.astype(np.float32)).cuda(), L, basis="orthogonal").cpu().numpy()
+    assert np.max(np.abs(g32.astype(np.float64) - gc)) <= 2e-5 * float(np.abs(gc).max())
+    if L > 0:   # the correction's share is not zero: the hierarchical transpose differs
+        gh = api().recompose_adjoint(torch.from_numpy(g).cuda(), L).cpu().numpy()
+        assert np.max(np.abs(gh - gc)) > 1e-6 * float(np.abs(gc).max())
 
 
 class Recompose(torch.autograd.Function):
