@@ -313,6 +313,31 @@ __device__ bool interpret_warp(int kind, int nl, int B, const uint32_t* __restri
 // below the tolerance. Returns false -- nothing written -- when an
 // efficiency is NaN or the walk reaches a tie before it stops; the caller
 // then runs the walks above. All threads of the CTA call it.
+// x (a finite double) as a signed integer count of 2^elsb, truncated toward
+// zero (off by less than one unit); |x| < 2^(elsb + 114) keeps the shift
+// below 61 bits and the result below 2^114
+__device__ __forceinline__ __int128 fixed_units(double x, int elsb) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int ev = (int)((b >> 52) & 0x7ff);
+    uint64_t m = b & 0xfffffffffffffull;
+    int e = -1074;   // |x| = m * 2^e
+    if (ev) {
+        m |= 1ull << 52;
+        e = ev - 1075;
+    }
+    const int sh = e - elsb;
+    const __int128 v = sh >= 0 ? (__int128)m << sh : (sh <= -64 ? (__int128)0 : (__int128)(m >> -sh));
+    return (b >> 63) ? -v : v;
+}
+__device__ __forceinline__ int exp_field(double x) { return (int)(((uint64_t)__double_as_longlong(x) >> 52) & 0x7ff); }
+// an upper bound of |v| / 2^80 (at least 1; below 2^46 for |v| < 2^125)
+__device__ __forceinline__ uint64_t mag_units80(__int128 v) {
+    const unsigned __int128 a = (unsigned __int128)(v < 0 ? -v : v);
+    return (uint64_t)(a >> 80) + 1;
+}
+
+constexpr int kFixK = 5;   // positions per thread in the fixed-point pass (256 threads cover 17 x 64)
+
 struct BlockWalkSmem {
     uint8_t ch_j[kMaxLevels][64];      // chain entries of each level (plane index)
     uint16_t order[kMaxLevels * 64];   // pop order: level << 8 | plane index
@@ -325,6 +350,10 @@ struct BlockWalkSmem {
     uint8_t start[kMaxLevels], n_ent[kMaxLevels], in_heap[kMaxLevels];
     int nblk, npos, fail, met0, stop;
     double acc0;
+    // the fixed-point pass: largest exponent field, per-thread totals for the
+    // scans, first positions (certainly met, undecided, tie)
+    int maxev, first_met, first_amb, first_tie, fixed_ok;
+    __int128 tot[256];
 };
 
 __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __restrict__ sizes,
@@ -450,15 +479,114 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
         terms[p] = (uint32_t)(l * 65 + j) | (uint32_t)(l * 65 + j + en[l * 64 + j]) << 16;
     }
     __syncthreads();
-    // the estimate along the order (thread 0): each round loads eight pops'
-    // terms, runs the two dependent double adds per pop, then compares the
-    // eight estimates with the tolerance
+    // The stop from exact prefix sums (all threads). With R_p the exact sum
+    // acc0 + sum_{i<=p} (add_i - sub_i) and R'_p = R_{p-1} - sub_p, the
+    // reference's rounded estimate differs from R_p by at most
+    // E_p = 2^-52 sum_{i<=p} (|R'_i| + |R_i|) (each double add rounds by at most
+    // 2^-53 of its result; the factor 2 covers the compounding). The sums run
+    // in 128-bit fixed point (unit 2^-113 of the largest value, truncations
+    // counted in the bound); a position is certainly met when R_p + E_p is
+    // below the tolerance, certainly not when R_p - E_p is above it. The stop
+    // is the first certain one when nothing undecided comes before it; a tie
+    // reached first bails out; an undecided position (the estimate within
+    // rounding of the tolerance) leaves the decision to the sequential walk
+    // below, as does a non-finite value or a tolerance that is not positive.
+    const int np = w.npos;
     if (tid == 0) {
-        const int np = w.npos;
+        w.maxev = max(exp_field(w.acc0), exp_field(tol));
+        w.first_met = w.first_amb = w.first_tie = np;
+        w.fixed_ok = !w.met0 && tol > 0.0 && np > 0;
+    }
+    __syncthreads();
+    for (int p = tid; p < np; p += nth) {
+        const uint32_t tq = terms[p];
+        atomicMax(&w.maxev, max(exp_field(ev[tq & 0xffffu]), exp_field(ev[tq >> 16])));
+    }
+    __syncthreads();
+    if (w.fixed_ok && w.maxev < 0x7ff) {
+        const int elsb = (w.maxev - 1022 + 1) + 12 - 125;   // all |values| < 2^(maxev - 1022 + 1); 2^11 pops of headroom
+        const int p0 = tid * kFixK;
+        __int128 rr[kFixK], rp[kFixK];
+        __int128 dsum = 0;
+#pragma unroll
+        for (int u = 0; u < kFixK; u++) {
+            rr[u] = rp[u] = 0;
+            if (p0 + u < np) {
+                const uint32_t tq = terms[p0 + u];
+                const __int128 a = fixed_units(ev[tq & 0xffffu], elsb), b = fixed_units(ev[tq >> 16], elsb);
+                rp[u] = -a;   // R'_p - R_{p-1} for now
+                rr[u] = b - a;
+                dsum += b - a;
+            }
+        }
+        // exclusive scan of the threads' sums (Hillis-Steele in shared memory)
+        w.tot[tid] = dsum;
+        __syncthreads();
+        for (int o = 1; o < 256; o <<= 1) {
+            const __int128 v = tid >= o ? w.tot[tid - o] : (__int128)0;
+            __syncthreads();
+            w.tot[tid] += v;
+            __syncthreads();
+        }
+        __int128 run = fixed_units(w.acc0, elsb) + w.tot[tid] - dsum;   // R_{p0 - 1}
+        __syncthreads();
+        uint64_t usum = 0, uu[kFixK];
+#pragma unroll
+        for (int u = 0; u < kFixK; u++) {
+            uu[u] = 0;
+            if (p0 + u < np) {
+                rp[u] += run;    // R'_p
+                run += rr[u];    // R_p
+                rr[u] = run;
+                uu[u] = mag_units80(rp[u]) + mag_units80(rr[u]);
+                usum += uu[u];
+            }
+        }
+        w.tot[tid] = (__int128)usum;
+        __syncthreads();
+        for (int o = 1; o < 256; o <<= 1) {
+            const __int128 v = tid >= o ? w.tot[tid - o] : (__int128)0;
+            __syncthreads();
+            w.tot[tid] += v;
+            __syncthreads();
+        }
+        uint64_t srun = (uint64_t)w.tot[tid] - usum;
+        const __int128 tfix = fixed_units(tol, elsb);
+        int fm = np, fa = np, ft = np;
+#pragma unroll
+        for (int u = 0; u < kFixK; u++) {
+            const int p = p0 + u;
+            if (p >= np) break;
+            srun += uu[u];
+            const __int128 e = ((__int128)srun << 28) + 2 * p + 4;   // in units; 2^-52 * 2^80 = 2^28
+            if (w.tie[p] && ft == np) ft = p;
+            if (rr[u] + e < tfix) {
+                if (fm == np) fm = p;
+            } else if (!(rr[u] - e >= tfix + 1)) {
+                if (fa == np) fa = p;
+            }
+        }
+        if (fm < np) atomicMin(&w.first_met, fm);
+        if (fa < np) atomicMin(&w.first_amb, fa);
+        if (ft < np) atomicMin(&w.first_tie, ft);
+    } else if (tid == 0) {
+        w.fixed_ok = 0;
+    }
+    __syncthreads();
+    // the sequential estimate (thread 0) where the fixed-point pass left the
+    // decision open: each round loads eight pops' terms, runs the two
+    // dependent double adds per pop, then compares the eight estimates with
+    // the tolerance
+    if (tid == 0) {
         int stop = np;   // pops [0, stop)
         bool bail = false;
+        const int fm = w.first_met, fa = w.first_amb, ft = w.first_tie;
+        const bool decided = w.fixed_ok && (ft <= fm && ft <= fa || fm < fa);
         if (w.met0) {
             stop = 0;
+        } else if (decided) {
+            if (ft <= fm && ft <= fa && ft < np) bail = true;   // the walk meets the tie before any stop
+            else stop = fm < np ? fm + 1 : np;
         } else {
             double acc = w.acc0;
             for (int p = 0; p < np && stop == np && !bail; p += 8) {
