@@ -338,6 +338,38 @@ __device__ __forceinline__ uint64_t mag_units80(__int128 v) {
 
 constexpr int kFixK = 5;   // positions per thread in the fixed-point pass (256 threads cover 17 x 64)
 
+__device__ __forceinline__ __int128 shfl_up128(__int128 x, int o) {
+    const unsigned long long lo = __shfl_up_sync(0xffffffffu, (unsigned long long)x, o);
+    const unsigned long long hi = __shfl_up_sync(0xffffffffu, (unsigned long long)((unsigned __int128)x >> 64), o);
+    return (__int128)(((unsigned __int128)hi << 64) | lo);
+}
+// exclusive prefix over the CTA's threads (in thread order) of one value per
+// thread: warp scans by shuffles, then the warp totals; tot: one slot per warp
+__device__ __int128 cta_exclusive_scan(__int128 v, __int128* tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __int128 x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const __int128 y = shfl_up128(x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        __int128 t = lane < nw ? tot[lane] : (__int128)0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const __int128 y = shfl_up128(t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < nw) tot[lane] = t;
+    }
+    __syncthreads();
+    const __int128 off = wid > 0 ? tot[wid - 1] : (__int128)0;
+    __syncthreads();   // the slots may be reused right after
+    return off + x - v;
+}
+
 struct BlockWalkSmem {
     uint8_t ch_j[kMaxLevels][64];      // chain entries of each level (plane index)
     uint16_t order[kMaxLevels * 64];   // pop order: level << 8 | plane index
@@ -345,6 +377,7 @@ struct BlockWalkSmem {
     // every level's blocks in one list (levels in any order): level | entry
     // count << 16 | first entry << 24 (their keys in the caller's blk_key)
     uint32_t binfo[kMaxLevels * 64];
+    int lat[kMaxLevels], lnb[kMaxLevels];   // each level's blocks: [lat, lat + lnb) of the list, keys falling
     uint32_t rs[kMaxLevels];
     int nidx[kMaxLevels];
     uint8_t start[kMaxLevels], n_ent[kMaxLevels], in_heap[kMaxLevels];
@@ -353,7 +386,7 @@ struct BlockWalkSmem {
     // the fixed-point pass: largest exponent field, per-thread totals for the
     // scans, first positions (certainly met, undecided, tie)
     int maxev, first_met, first_amb, first_tie, fixed_ok;
-    __int128 tot[256];
+    __int128 tot[32];   // one per warp (scans)
 };
 
 __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __restrict__ sizes,
@@ -423,9 +456,12 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
             }
         }
         w.n_ent[l] = (uint8_t)cnt;
+        w.lnb[l] = nb;
+        w.lat[l] = 0;
         if (nb) {   // the level's blocks into the shared list: key (its first entry's) and info
             atomicAdd(&w.npos, cnt);
             const int at = atomicAdd(&w.nblk, nb);
+            w.lat[l] = at;
             for (int b = 0; b < nb; b++) {
                 const int f0 = lfirst[l * 64 + b], f1 = b + 1 < nb ? lfirst[l * 64 + b + 1] : cnt;
                 blk_key[at + b] = ekey[l * 64 + w.ch_j[l][f0]];
@@ -436,34 +472,34 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
     __syncthreads();
     if (w.fail) return false;
     // rank of each block: the entries of every block with a larger key, or an
-    // equal key at a lower level (a tie, flagged); same-level blocks have
-    // larger keys exactly when they come first, so they are counted too
+    // equal key at a lower level (a tie, flagged). Its own level's earlier
+    // blocks are the entries before it there; in every other level the
+    // blocks' keys fall strictly, so a binary search finds the first block
+    // whose key is not larger, and that block's first entry is the count.
     const int nblk = w.nblk;
     for (int t = tid; t < nblk; t += nth) {
         const uint32_t bi = w.binfo[t];
         const int l = bi & 255;
         const long long k = blk_key[t];
-        int rank = 0;
+        int rank = (int)(bi >> 24);
         bool tie = false;
-        auto count = [&](long long k2, uint32_t b2) {
-            const int l2 = b2 & 255;
-            const bool eq = k2 == k && l2 != l;
-            tie |= eq;
-            if (k2 > k || (eq && l2 < l)) rank += (b2 >> 16) & 255;
-        };
-        int u = 0;
-        for (; u + 8 <= nblk; u += 8) {   // eight blocks' loads in flight, then their counts
-            long long k2[8];
-            uint32_t b2[8];
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                k2[q] = blk_key[u + q];
-                b2[q] = w.binfo[u + q];
+        for (int l2 = 0; l2 < nl; l2++) {
+            const int nb2 = w.lnb[l2];
+            if (l2 == l || nb2 == 0) continue;
+            const int base = w.lat[l2];
+            int lo = 0, hi = nb2;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (blk_key[base + mid] > k) lo = mid + 1;
+                else hi = mid;
             }
-#pragma unroll
-            for (int q = 0; q < 8; q++) count(k2[q], b2[q]);
+            int first = lo;
+            if (lo < nb2 && blk_key[base + lo] == k) {
+                tie = true;
+                if (l2 < l) first = lo + 1;   // the lower level's tied block goes first
+            }
+            rank += first < nb2 ? (int)(w.binfo[base + first] >> 24) : (int)w.n_ent[l2];
         }
-        for (; u < nblk; u++) count(blk_key[u], w.binfo[u]);
         const int f0 = bi >> 24, n = (bi >> 16) & 255;
         for (int e = 0; e < n; e++) {
             w.order[rank + e] = (uint16_t)(l << 8 | w.ch_j[l][f0 + e]);
@@ -519,17 +555,7 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
                 dsum += b - a;
             }
         }
-        // exclusive scan of the threads' sums (Hillis-Steele in shared memory)
-        w.tot[tid] = dsum;
-        __syncthreads();
-        for (int o = 1; o < 256; o <<= 1) {
-            const __int128 v = tid >= o ? w.tot[tid - o] : (__int128)0;
-            __syncthreads();
-            w.tot[tid] += v;
-            __syncthreads();
-        }
-        __int128 run = fixed_units(w.acc0, elsb) + w.tot[tid] - dsum;   // R_{p0 - 1}
-        __syncthreads();
+        __int128 run = fixed_units(w.acc0, elsb) + cta_exclusive_scan(dsum, w.tot);   // R_{p0 - 1}
         uint64_t usum = 0, uu[kFixK];
 #pragma unroll
         for (int u = 0; u < kFixK; u++) {
@@ -542,15 +568,7 @@ __device__ bool interpret_blocks(int kind, int nl, int B, const uint32_t* __rest
                 usum += uu[u];
             }
         }
-        w.tot[tid] = (__int128)usum;
-        __syncthreads();
-        for (int o = 1; o < 256; o <<= 1) {
-            const __int128 v = tid >= o ? w.tot[tid - o] : (__int128)0;
-            __syncthreads();
-            w.tot[tid] += v;
-            __syncthreads();
-        }
-        uint64_t srun = (uint64_t)w.tot[tid] - usum;
+        uint64_t srun = (uint64_t)cta_exclusive_scan((__int128)usum, w.tot);
         const __int128 tfix = fixed_units(tol, elsb);
         int fm = np, fa = np, ft = np;
 #pragma unroll
