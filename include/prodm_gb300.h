@@ -397,11 +397,14 @@ int prodm_batch_bind(prodm_batch* h, const void* const* d_fields, void* const* d
 int prodm_batch_set_launch(prodm_batch* h, int threads_per_cta, int ctas_per_sm);
 /* one stage's launch shape, as the autotuner sets them one stage at a time:
  * PRODM_BATCH_DECOMPOSE / PRODM_BATCH_RECOMPOSE (one warp per fine row;
- * threads 64, 128 or 256, CTAs per SM 1..32) or PRODM_BATCH_ENCODE (256
- * threads, 1..8 CTAs per SM) */
+ * threads 64, 128 or 256, CTAs per SM 1..32), PRODM_BATCH_ENCODE (256
+ * threads, 1..8 CTAs per SM) or PRODM_BATCH_FUSED (the finest levels, decoded
+ * inside their recomposition: 256 threads, 1..8 CTAs per SM, capped by what
+ * fits on an SM) */
 #define PRODM_BATCH_DECOMPOSE 0
 #define PRODM_BATCH_ENCODE 1
 #define PRODM_BATCH_RECOMPOSE 2
+#define PRODM_BATCH_FUSED 3
 int prodm_batch_set_stage_launch(prodm_batch* h, int stage, int threads_per_cta, int ctas_per_sm);
 int prodm_batch_refactor(prodm_batch* h, void* stream);
 int prodm_batch_set_tolerances(prodm_batch* h, const double* h_tolerances, void* stream);
@@ -411,6 +414,9 @@ int prodm_batch_field_info(prodm_batch* h, int field, uint8_t* h_index, uint32_t
                            void* stream);
 int prodm_batch_export_level(prodm_batch* h, int field, int level, void* dst, uint64_t capacity, int dst_is_host,
                              uint64_t* len, void* stream);
+/* status of the batched fused kernels since the last call (PRODM_ETIMEOUT when
+ * a wait for plane tiles gave up), reported once */
+int prodm_batch_status(prodm_batch* h, void* stream);
 int prodm_batch_destroy(prodm_batch* h);
 
 /* ---------------------------------------------------------------------------

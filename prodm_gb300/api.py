@@ -502,10 +502,11 @@ class MDRBatch:
     def set_launch(self, threads_per_cta, ctas_per_sm):
         call("prodm_batch_set_launch", self.h, int(threads_per_cta), int(ctas_per_sm))
 
-    STAGES = {"decompose": 0, "encode": 1, "recompose": 2}
+    STAGES = {"decompose": 0, "encode": 1, "recompose": 2, "fused": 3}
 
     def set_stage_launch(self, stage, threads_per_cta, ctas_per_sm):
-        """stage: "decompose", "encode" or "recompose"."""
+        """stage: "decompose", "encode", "recompose" or "fused" (the finest
+        levels, decoded inside their recomposition)."""
         call("prodm_batch_set_stage_launch", self.h, self.STAGES[stage], int(threads_per_cta), int(ctas_per_sm))
 
     def refactor(self, stream=None):
@@ -521,6 +522,11 @@ class MDRBatch:
 
     def reset(self, stream=None):
         call("prodm_batch_reset", self.h, _stream(stream))
+
+    def status(self, stream=None):
+        """Raises ProdmError when a fused kernel reported an error since the
+        last call (PRODM_ETIMEOUT: a wait for plane tiles gave up)."""
+        call("prodm_batch_status", self.h, _stream(stream))
 
     def field_info(self, i, stream=None):
         nl = self.levels[i] + 1

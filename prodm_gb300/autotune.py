@@ -4,7 +4,8 @@ Times launch shapes for the persistent multi-field launches on the actual
 batch and keeps the fastest, one stage at a time (coordinate descent): the
 row stages (decomposition, recomposition: threads per CTA = warps = fine rows
 in flight per CTA, and CTAs per SM, i.e. how many row groups share an SM) and
-the encoder (CTAs per SM of its 256-thread chunk workers), each timed as the
+the encoder (CTAs per SM of its 256-thread chunk workers) and the fused
+finest-level decode + recomposition (CTAs per SM of its 8-row units), each timed as the
 whole refactor + retrieve step with the other stages at their best shape so
 far. Results persist in a JSON cache keyed by the GPU name and the batch's
 shapes and level counts ($PRODM_AUTOTUNE_CACHE, default
@@ -19,8 +20,12 @@ import torch
 # (threads per CTA, CTAs per SM) per stage
 ROW_CANDIDATES = ((64, 16), (64, 32), (128, 8), (128, 16), (256, 4), (256, 8))
 ENCODE_CANDIDATES = ((256, 1), (256, 2), (256, 4), (256, 8))
-STAGE_CANDIDATES = {"decompose": ROW_CANDIDATES, "recompose": ROW_CANDIDATES, "encode": ENCODE_CANDIDATES}
-DEFAULT = {"decompose": (256, 8), "encode": (256, 8), "recompose": (256, 8)}
+# the fused finest levels: 256-thread CTAs of 8-row (or longer) units, 2..5 per
+# SM (fewer where a unit's tiles do not fit)
+FUSED_CANDIDATES = ((256, 2), (256, 3), (256, 4), (256, 5))
+STAGE_CANDIDATES = {"decompose": ROW_CANDIDATES, "recompose": ROW_CANDIDATES, "encode": ENCODE_CANDIDATES,
+                    "fused": FUSED_CANDIDATES}
+DEFAULT = {"decompose": (256, 8), "encode": (256, 8), "recompose": (256, 8), "fused": (256, 5)}
 # the uniform shapes of the earlier single-shape tuner (still accepted by set_launch)
 CANDIDATES = ((128, 8), (256, 4), (256, 8), (256, 16))
 
@@ -87,7 +92,7 @@ def tune(batch, reps=3, use_cache=True):
     shapes = dict(DEFAULT)
     _apply(batch, shapes)
     timings = {}
-    for stage in ("decompose", "recompose", "encode"):
+    for stage in ("decompose", "recompose", "encode", "fused"):
         best = None
         for t, c in STAGE_CANDIDATES[stage]:
             batch.set_stage_launch(stage, t, c)

@@ -35,16 +35,25 @@ struct RowSeg {
     uint32_t* key_c;        // decompose at level 1: level-0 |max| key
 };
 
-__device__ __forceinline__ int find_row_seg(const RowSeg* segs, int nseg, uint32_t g) {
+// segment of global row g: binary search over the segments' first rows,
+// staged in shared memory (one dependent shared load per step instead of a
+// global one)
+__device__ __forceinline__ int find_row_seg(const uint32_t* begins, int nseg, uint32_t g) {
     int lo = 0, hi = nseg - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
-        if (segs[mid].row_begin <= g) lo = mid; else hi = mid - 1;
+        if (begins[mid] <= g) lo = mid; else hi = mid - 1;
     }
     return lo;
 }
+__device__ __forceinline__ void stage_row_begins(const RowSeg* segs, int nseg, uint32_t* begins) {
+    for (int i = threadIdx.x; i < nseg; i += blockDim.x) begins[i] = segs[i].row_begin;
+    __syncthreads();
+}
 
-__global__ void __launch_bounds__(256) k_decompose_multi(const RowSeg* __restrict__ segs, int nseg, uint32_t total) {
+__global__ void __launch_bounds__(256, 4) k_decompose_multi(const RowSeg* __restrict__ segs, int nseg, uint32_t total) {
+    extern __shared__ uint32_t s_begin[];
+    stage_row_begins(segs, nseg, s_begin);
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     uint32_t mk = 0, mc = 0;
     int cur = -1;
@@ -58,7 +67,7 @@ __global__ void __launch_bounds__(256) k_decompose_multi(const RowSeg* __restric
         mk = mc = 0;
     };
     for (uint32_t g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
-        const int s = find_row_seg(segs, nseg, g);
+        const int s = find_row_seg(s_begin, nseg, g);
         if (s != cur) { flush(); cur = s; }
         const RowSeg& q = segs[s];
         if (q.F.n[2] & 1u)
@@ -71,9 +80,11 @@ __global__ void __launch_bounds__(256) k_decompose_multi(const RowSeg* __restric
 }
 
 __global__ void __launch_bounds__(256) k_recompose_multi(const RowSeg* __restrict__ segs, int nseg, uint32_t total) {
+    extern __shared__ uint32_t s_begin[];
+    stage_row_begins(segs, nseg, s_begin);
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     for (uint32_t g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
-        const int s = find_row_seg(segs, nseg, g);
+        const int s = find_row_seg(s_begin, nseg, g);
         const RowSeg& q = segs[s];
         if (q.F.n[2] & 1u)
             recompose_row_odd_any<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
@@ -149,14 +160,26 @@ struct prodm_batch {
     std::vector<uint32_t> drows, rrows;
     ChunkSeg* eseg = nullptr;
     ChunkSeg* decseg = nullptr;                    // decode: kDecodeChunkBlocks blocks per chunk
-    int en = 0;
+    int en = 0, decn = 0;
     uint64_t echunks = 0, dchunks = 0;
+    // finest levels decoded inside their recomposition: fields whose plane
+    // runs fit a TMA box of at most 96 words (fseg[0]) or 160 words (fseg[1])
+    // (tensor maps in fmaps, one per field), and fields with longer rows
+    // (fseg[2]: cp.async staging)
+    FusedSeg* fseg[3] = {nullptr, nullptr, nullptr};
+    int fn[3] = {0, 0, 0};
+    uint64_t funits[3] = {0, 0, 0};
+    uint32_t ftld[3] = {0, 0, 0};
+    uint32_t fbw[3] = {0, 0, 0};                   // widest TMA box of each class
+    uint8_t* fmaps = nullptr;                      // [nf][128] tensor maps
+    int* kstatus = nullptr;                        // status word of the fused kernels
+    std::vector<char> fused;                       // per field
     std::vector<const float*> fields;
     std::vector<float*> outs;
     bool bound = false;
     // launch shape per stage (decompose, encode, recompose): threads per CTA,
     // CTAs per SM of the persistent grid
-    int st_threads[3] = {256, 256, 256}, st_ctas[3] = {8, 8, 8};
+    int st_threads[4] = {256, 256, 256, 256}, st_ctas[4] = {8, 8, 8, 0};
     ~prodm_batch() {
         for (void* p : allocs) cudaFree(p);
     }
@@ -171,9 +194,19 @@ struct prodm_batch {
 namespace prodm {
 namespace {
 
+// a field's finest level is fused when its rows have odd length and an
+// 8-row unit's tiles fit the fused kernel's shared memory
+bool batch_field_fused(const LevelGeom& g) {
+    if (g.L < 1) return false;
+    const Box& F = g.box[g.L];
+    return (F.n[2] & 1u) && fused_multi_smem(fused_unit_blocks(F)) <= 200 * 1024;
+}
+
 int batch_build_segments(prodm_batch* h) {
     const int nf = h->nf, B = h->B;
     int rc;
+    h->fused.assign(nf, 0);
+    for (int f = 0; f < nf; f++) h->fused[f] = batch_field_fused(h->g[f]) ? 1 : 0;
     // decompose depths: depth d processes level L_f - d of every field with L_f - d >= 1
     h->dseg.assign(h->maxL, nullptr);
     h->rseg.assign(h->maxL, nullptr);
@@ -210,7 +243,7 @@ int batch_build_segments(prodm_batch* h) {
                 ds.push_back(s);
             }
             const int lr = d + 1;                 // recompose level at this depth
-            if (lr <= L) {
+            if (lr <= L && !(lr == L && h->fused[f])) {
                 RowSeg s{};
                 s.F = g.box[lr];
                 s.C = g.box[lr - 1];
@@ -237,7 +270,61 @@ int batch_build_segments(prodm_batch* h) {
             PRODM_CUDA(cudaMemcpy(h->rseg[d], rs.data(), rs.size() * sizeof(RowSeg), cudaMemcpyHostToDevice));
         }
     }
-    // encode / decode: every (field, level)
+    // fused finest levels
+    {
+        std::vector<FusedSeg> fs[3];
+        uint64_t units[3] = {0, 0, 0};
+        uint32_t tld[3] = {0, 0, 0};
+        std::vector<uint8_t> maps((size_t)nf * 128, 0);
+        if (!h->fmaps && (rc = h->alloc((void**)&h->fmaps, (size_t)nf * 128))) return rc;
+        for (int f = 0; f < nf; f++) {
+            if (!h->fused[f]) continue;
+            const LevelGeom& g = h->g[f];
+            const int L = g.L;
+            FusedSeg s{};
+            s.F = g.box[L];
+            s.C = g.box[L - 1];
+            const uint64_t nbk = (g.elems[L] + 31) / 32;
+            s.base = (const uint32_t*)(h->streams + h->lvl_stream_off[f][L]);
+            s.stride = (nbk + 3) / 4 * 4;
+            s.key = h->keys + f * kMaxL + L;
+            s.dnum = h->index + f * kMaxL + L;
+            float* rb0 = h->rbuf + h->cb_off[f];
+            float* rb1 = rb0 + h->cb_len[f];
+            s.coarse = (L == 1) ? h->rcoef + h->rcoef_off[f] + h->roff[f][0] : ((L - 1) & 1 ? rb1 : rb0);
+            s.out = h->outs[f];
+            s.s0 = (uint64_t)s.F.n[1] * s.F.n[2];
+            s.s1 = s.F.n[2];
+            uint32_t t = fused_unit_blocks(s.F);
+            s.rpu = fused_unit_rows(s.F);
+            s.bw = fused_tma_box(s.F, s.rpu);
+            int k = 2;
+            if (s.bw && encode_plane_map(maps.data() + (size_t)f * 128, s.base, nbk, B, s.stride, s.bw) == PRODM_OK) {
+                k = s.bw <= 96 ? 0 : 1;
+                s.map = h->fmaps + (size_t)f * 128;
+                t = fused_unit_blocks_rows(s.F, s.rpu);
+            } else {
+                s.bw = 0;
+                s.map = nullptr;
+                s.rpu = 8;
+            }
+            s.unit_begin = units[k];
+            units[k] += ((uint64_t)s.F.n[0] * s.F.n[1] + s.rpu - 1) / s.rpu;
+            tld[k] = std::max(tld[k], t);
+            fs[k].push_back(s);
+            h->fbw[k] = std::max(h->fbw[k], s.bw);
+        }
+        PRODM_CUDA(cudaMemcpy(h->fmaps, maps.data(), maps.size(), cudaMemcpyHostToDevice));
+        for (int k = 0; k < 3; k++) {
+            h->fn[k] = (int)fs[k].size();
+            h->funits[k] = units[k];
+            h->ftld[k] = tld[k];
+            if (fs[k].empty()) continue;
+            if (!h->fseg[k] && (rc = h->alloc((void**)&h->fseg[k], nf * sizeof(FusedSeg)))) return rc;
+            PRODM_CUDA(cudaMemcpy(h->fseg[k], fs[k].data(), fs[k].size() * sizeof(FusedSeg), cudaMemcpyHostToDevice));
+        }
+    }
+    // encode / decode: every (field, level); the decode skips fused finest levels
     std::vector<ChunkSeg> es, dc;
     uint64_t ch = 0, dch = 0;
     for (int f = 0; f < nf; f++) {
@@ -256,18 +343,21 @@ int batch_build_segments(prodm_batch* h) {
             s.chunk_begin = ch;
             ch += (s.nblocks + NB_CHUNK - 1) / NB_CHUNK;
             es.push_back(s);
+            if (l == g.L && h->fused[f]) continue;
             d.chunk_begin = dch;
             dch += (d.nblocks + kDecodeChunkBlocks - 1) / kDecodeChunkBlocks;
             dc.push_back(d);
         }
     }
     h->en = (int)es.size();
+    h->decn = (int)dc.size();
     h->echunks = ch;
     h->dchunks = dch;
     if (!h->eseg && (rc = h->alloc((void**)&h->eseg, es.size() * sizeof(ChunkSeg)))) return rc;
     PRODM_CUDA(cudaMemcpy(h->eseg, es.data(), es.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
-    if (!h->decseg && (rc = h->alloc((void**)&h->decseg, dc.size() * sizeof(ChunkSeg)))) return rc;
-    PRODM_CUDA(cudaMemcpy(h->decseg, dc.data(), dc.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
+    if (!h->decseg && (rc = h->alloc((void**)&h->decseg, es.size() * sizeof(ChunkSeg)))) return rc;
+    if (!dc.empty())
+        PRODM_CUDA(cudaMemcpy(h->decseg, dc.data(), dc.size() * sizeof(ChunkSeg), cudaMemcpyHostToDevice));
     (void)B;
     return PRODM_OK;
 }
@@ -290,7 +380,8 @@ int batch_refactor(prodm_batch* h, cudaStream_t st) {
         }
     for (int d = 0; d < h->maxL; d++) {
         if (!h->dn[d]) continue;
-        k_decompose_multi<<<persistent_grid(h, 0, h->drows[d], th / 32), th, 0, st>>>(h->dseg[d], h->dn[d], h->drows[d]);
+        k_decompose_multi<<<persistent_grid(h, 0, h->drows[d], th / 32), th, h->dn[d] * 4, st>>>(h->dseg[d], h->dn[d],
+                                                                                                 h->drows[d]);
         PRODM_CHECK_LAUNCH("k_decompose_multi");
     }
     k_nb_encode_multi<<<persistent_grid(h, 1, h->echunks, 1), 256, 0, st>>>(h->eseg, h->en, h->echunks, h->B);
@@ -308,15 +399,24 @@ int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t s
                                       (uint64_t)kMaxL * h->B, h->maxerr, (uint64_t)kMaxL * (h->B + 1), h->tols, 0.0,
                                       h->index, kMaxL, h->rsz, st)))
         return rc;
-    if ((rc = launch_nb_decode_levels(h->decseg, h->en, h->dchunks, st))) return rc;
+    if (h->dchunks && (rc = launch_nb_decode_levels(h->decseg, h->decn, h->dchunks, st))) return rc;
     for (int f = 0; f < h->nf; f++)
         if (h->g[f].L == 0)
             PRODM_CUDA(cudaMemcpyAsync(h->outs[f], h->rcoef + h->rcoef_off[f], h->g[f].total * 4, cudaMemcpyDeviceToDevice, st));
     for (int d = 0; d < h->maxL; d++) {
         if (!h->rn[d]) continue;
-        k_recompose_multi<<<persistent_grid(h, 2, h->rrows[d], th / 32), th, 0, st>>>(h->rseg[d], h->rn[d], h->rrows[d]);
+        k_recompose_multi<<<persistent_grid(h, 2, h->rrows[d], th / 32), th, h->rn[d] * 4, st>>>(h->rseg[d], h->rn[d],
+                                                                                                 h->rrows[d]);
         PRODM_CHECK_LAUNCH("k_recompose_multi");
     }
+    // the finest levels whose coarse boxes the depths above completed
+    const unsigned fc = (unsigned)h->st_ctas[PRODM_BATCH_FUSED];
+    for (int k = 0; k < 2; k++)
+        if (h->fn[k] && (rc = launch_decode_recompose_nb32_tma_multi(h->fseg[k], h->fn[k], h->funits[k], h->ftld[k],
+                                                                    h->fbw[k], fc, h->kstatus, st)))
+            return rc;
+    if (h->fn[2] && (rc = launch_decode_recompose_nb32_multi(h->fseg[2], h->fn[2], h->funits[2], h->ftld[2], fc, st)))
+        return rc;
     return PRODM_OK;
 }
 
@@ -329,6 +429,7 @@ extern "C" {
 
 int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs) {
     if (!out || !cfgs || nfields < 1) return fail(PRODM_EINVAL, "prodm_batch_create: bad arguments");
+    if (nfields > 4096) return fail(PRODM_EINVAL, "prodm_batch_create: at most 4096 fields per batch");
     const int B = cfgs[0].num_bitplanes;
     for (int f = 0; f < nfields; f++) {
         const prodm_config& c = cfgs[f];
@@ -383,7 +484,8 @@ int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs)
         (rc = h->alloc((void**)&h->bounds, slots * 4)) || (rc = h->alloc((void**)&h->sizes, slots * B * 4)) ||
         (rc = h->alloc((void**)&h->maxerr, slots * (B + 1) * 8)) || (rc = h->alloc((void**)&h->index, slots)) ||
         (rc = h->alloc((void**)&h->rsz, slots * 4)) || (rc = h->alloc((void**)&h->ndims_d, nfields * 4)) ||
-        (rc = h->alloc((void**)&h->levels_d, nfields * 4)) || (rc = h->alloc((void**)&h->tols, nfields * 8))) {
+        (rc = h->alloc((void**)&h->levels_d, nfields * 4)) || (rc = h->alloc((void**)&h->tols, nfields * 8)) ||
+        (rc = h->alloc((void**)&h->kstatus, 16))) {
         delete h;
         return rc;
     }
@@ -396,6 +498,7 @@ int prodm_batch_create(prodm_batch** out, int nfields, const prodm_config* cfgs)
     if (e == cudaSuccess) e = cudaMemcpy(h->ndims_d, ndims.data(), nfields * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(h->index, 0, slots);
     if (e == cudaSuccess) e = cudaMemset(h->maxerr, 0, slots * (B + 1) * 8);
+    if (e == cudaSuccess) e = cudaMemset(h->kstatus, 0, 16);
     if (e != cudaSuccess) { delete h; return cuda_status(e, "prodm_batch_create"); }
     *out = h;
     return PRODM_OK;
@@ -411,10 +514,10 @@ int prodm_batch_bind(prodm_batch* h, const void* const* d_fields, void* const* d
 
 int prodm_batch_set_stage_launch(prodm_batch* h, int stage, int threads_per_cta, int ctas_per_sm) {
     if (!h) return fail(PRODM_EINVAL, "NULL handle");
-    if (stage < PRODM_BATCH_DECOMPOSE || stage > PRODM_BATCH_RECOMPOSE) return fail(PRODM_EINVAL, "unknown batch stage");
-    if (stage == PRODM_BATCH_ENCODE) {
-        if (threads_per_cta != 256) return fail(PRODM_EINVAL, "the encode stage runs 256 threads per CTA");
-        if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail(PRODM_EINVAL, "encode CTAs per SM must be in [1, 8]");
+    if (stage < PRODM_BATCH_DECOMPOSE || stage > PRODM_BATCH_FUSED) return fail(PRODM_EINVAL, "unknown batch stage");
+    if (stage == PRODM_BATCH_ENCODE || stage == PRODM_BATCH_FUSED) {
+        if (threads_per_cta != 256) return fail(PRODM_EINVAL, "the encode and fused stages run 256 threads per CTA");
+        if (ctas_per_sm < 1 || ctas_per_sm > 8) return fail(PRODM_EINVAL, "encode / fused CTAs per SM must be in [1, 8]");
     } else {
         if (threads_per_cta != 64 && threads_per_cta != 128 && threads_per_cta != 256)
             return fail(PRODM_EINVAL, "threads per CTA must be 64, 128 or 256");
@@ -490,6 +593,18 @@ int prodm_batch_export_level(prodm_batch* h, int field, int level, void* dst, ui
     PRODM_CUDA(cudaMemcpy2DAsync(dst, nbk * 4, h->streams + h->lvl_stream_off[field][level], (nbk + 3) / 4 * 16, nbk * 4,
                                  h->B, dst_is_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
     PRODM_CUDA(cudaStreamSynchronize(st));
+    return PRODM_OK;
+}
+
+int prodm_batch_status(prodm_batch* h, void* stream) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    cudaStream_t st = (cudaStream_t)stream;
+    int code = 0;
+    PRODM_CUDA(cudaMemcpyAsync(&code, h->kstatus, 4, cudaMemcpyDeviceToHost, st));
+    PRODM_CUDA(cudaMemsetAsync(h->kstatus, 0, 4, st));
+    PRODM_CUDA(cudaStreamSynchronize(st));
+    if (code == PRODM_ETIMEOUT) return fail(code, "a batched fused kernel's wait for its plane tiles ran out");
+    if (code) return fail(code, "a batched fused kernel reported an error");
     return PRODM_OK;
 }
 

@@ -13,6 +13,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <mutex>
 
@@ -310,10 +311,10 @@ __device__ __forceinline__ void fused_row_rank(uint32_t rho, const Box& F, const
     len = cc ? F.n[2] - C.n[2] : F.n[2];
 }
 
-// block range [fb, fb + nbk) of the coefficients of rows [rho0, rho0 + 8)
+// block range [fb, fb + nbk) of the coefficients of rows [rho0, rho0 + nr)
 __device__ __forceinline__ void fused_block_range(uint32_t rho0, uint32_t rows, const Box& F, const Box& C,
-                                                  uint64_t& fb, uint32_t& nbk) {
-    const uint32_t rho_last = min(rho0 + 7, rows - 1);
+                                                  uint64_t& fb, uint32_t& nbk, uint32_t nr = 8) {
+    const uint32_t rho_last = min(rho0 + nr - 1, rows - 1);
     uint32_t a0, a1, z0, z1, alen, zlen;
     bool acc_, zcc;
     uint64_t abase, zbase;
@@ -472,6 +473,79 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_odd(const uint
     cp_async_wait_all();
 }
 
+// The finest levels of many fields in one persistent launch (the batched
+// retrieval): the global 8-row units of all segments are walked as in
+// k_decode_recompose_nb32_odd, with each unit's field looked up in the segment
+// table (one segment per field, odd row lengths). The plane count, exponent
+// and decode scale are the unit's field's; a fetch zeroes the tile words of
+// the planes its field did not retrieve. Staging, decode and recomposition
+// are those of the single-field kernel, so the results are bit-identical.
+__global__ void __launch_bounds__(256, 4) k_decode_recompose_nb32_multi(const FusedSeg* __restrict__ segs, int nseg,
+                                                                       uint64_t total, uint32_t tld) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* tiles = smem;                                  // [block][TB_LD]
+    float* cb = (float*)(smem + TB_LD * tld);                // [block][CB_LD]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ int s_seg[3];
+    __shared__ uint64_t s_fb[3];
+    __shared__ uint32_t s_nbk[3];
+    const uint64_t step = gridDim.x;
+    uint64_t u = blockIdx.x;
+    if (u >= total) return;
+    // thread 0: the field and block range of unit g into slot k
+    auto plan = [&](uint64_t g, int k) {
+        const int s = find_seg(segs, nseg, g, &FusedSeg::unit_begin);
+        const FusedSeg& q = segs[s];
+        s_seg[k] = s;
+        fused_block_range((uint32_t)(g - q.unit_begin) * 8, q.F.n[0] * q.F.n[1], q.F, q.C, s_fb[k], s_nbk[k]);
+    };
+    auto fetch = [&](int k) {
+        const FusedSeg& q = segs[s_seg[k]];
+        const int num = *q.dnum;
+        const int poff = 32 - num;
+        const uint64_t fb = s_fb[k];
+        const uint32_t nbk = s_nbk[k];
+        for (uint32_t i = threadIdx.x; i < nbk * (uint32_t)poff; i += blockDim.x) {
+            const uint32_t row = i / poff, p = i - row * poff;
+            tiles[row * TB_LD + p] = 0u;
+        }
+        for (int p = warp; p < num; p += 8) {
+            const uint32_t* src = q.base + (uint64_t)p * q.stride + fb;
+            for (uint32_t j = lane; j < nbk; j += 32) cp_async4(tiles + j * TB_LD + poff + p, src + j);
+        }
+        cp_async_commit();
+    };
+    if (threadIdx.x == 0) {
+        plan(u, 0);
+        if (u + step < total) plan(u + step, 1);
+    }
+    __syncthreads();
+    fetch(0);
+    for (int it = 0; u < total; it++, u += step) {
+        cp_async_wait_all();
+        __syncthreads();
+        const int k = it % 3;
+        const FusedSeg& q = segs[s_seg[k]];
+        const uint64_t fb = s_fb[k];
+        const uint32_t nbk = s_nbk[k];
+        if (threadIdx.x == 0 && u + 2 * step < total) plan(u + 2 * step, (it + 2) % 3);
+        const int num = *q.dnum;
+        const int exp = frexp_exp(__uint_as_float(*q.key)) + 2;
+        const bool neg = num != 0 && (num & 1);              // NegaBinaryBPEncoder.hpp:153, :177
+        const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
+        const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
+        if (dfast) decode_tile<true>(tiles, cb, nbk, num, exp, neg, dscale);
+        else decode_tile<false>(tiles, cb, nbk, num, exp, neg, dscale);
+        __syncthreads();
+        // the tile is free again: fetch the next unit's planes during the recomposition
+        if (u + step < total) fetch((it + 1) % 3);
+        const uint32_t rows = q.F.n[0] * q.F.n[1];
+        const uint32_t rho = (uint32_t)(u - q.unit_begin) * 8 + warp;
+        if (rho < rows) recompose_fine_row(fused_row(rho, q.F, q.C, q.s0, q.s1, fb), q.C, q.coarse, q.out, cb, lane);
+    }
+    cp_async_wait_all();
+}
+
 // decode of a plane-major tile (row 32 - num + p = plane p, rows below zero;
 // block t of the range at column t): the same half transposes, each thread
 // reading its block's 32 rows and combining rows 31-k and 15-k at once
@@ -587,6 +661,115 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
             rows_of(rho0 + step, s_fb[(it + 1) % 3], s_row[(it + 1) & 1]);
         }
         if (rho0 + warp < rows) recompose_fine_row(s_row[it & 1][warp], C, coarse, out, cb, lane);
+    }
+}
+
+// The TMA kernel over the finest levels of many fields (the batched
+// retrieval): each field's planes have their own tensor map in device memory
+// (FusedSeg::map, written before the launch; box FusedSeg::bw words <= RS),
+// each unit's field is looked up in the segment table. A unit is
+// FusedSeg::rpu consecutive rows (8 per warp-round; short rows take several
+// rounds, so that a unit moves about as many values as 8 rows of 257). Tile rows below a
+// unit's planes must be zero; the copies write rows 32 - num .. 31, so rows
+// below the lowest row copied so far are zero, and only a unit with fewer
+// planes than that zeroes the rows in between before its copies are issued.
+// Decode, recomposition and the bounded waits are those of
+// k_decode_recompose_nb32_tma, so results are bit-identical.
+template <int RS>
+__global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma_multi(const FusedSeg* __restrict__ segs, int nseg,
+                                                                           uint64_t total, int* __restrict__ status,
+                                                                           long long wait_limit, uint32_t tx_extra) {
+    extern __shared__ __align__(128) uint32_t tma_smem[];
+    uint32_t* tile = tma_smem;                               // [32][RS] plane-major
+    float* cb = (float*)(tma_smem + 32 * RS);                // [block][CB_LD]
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_seg[3];
+    __shared__ uint64_t s_fb[3];
+    __shared__ uint32_t s_nbk[3];
+    __shared__ FusedRow s_row[2][kMaxUnitRows];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t step = gridDim.x;
+    uint64_t u = blockIdx.x;
+    if (u >= total) return;
+    if ((smem_addr(tile) & 127u) != 0) {   // TMA destinations need 128-byte alignment
+        if (threadIdx.x == 0) atomicExch(status, PRODM_ECUDA);
+        return;
+    }
+    // thread 0: the field and block range of unit g into slot k
+    auto plan = [&](uint64_t g, int k) {
+        const int s = find_seg(segs, nseg, g, &FusedSeg::unit_begin);
+        const FusedSeg& q = segs[s];
+        s_seg[k] = s;
+        fused_block_range((uint32_t)(g - q.unit_begin) * q.rpu, q.F.n[0] * q.F.n[1], q.F, q.C, s_fb[k], s_nbk[k],
+                          q.rpu);
+    };
+    // every thread: rows [zlo, 32 - num) zeroed for the unit in slot k (rows
+    // below zlo are zero already); afterwards rows below 32 - num are zero
+    uint32_t zlo = 0;
+    auto zero_rows = [&](int k) {
+        const uint32_t lo = 32u - *segs[s_seg[k]].dnum;
+        for (uint32_t i = zlo * RS + threadIdx.x; i < lo * RS; i += blockDim.x) tile[i] = 0u;
+        zlo = lo;
+    };
+    // warp 0: the copies of the unit in slot k, and the row geometry of unit g
+    auto issue = [&](int k, uint64_t g, FusedRow* rows) {
+        const FusedSeg& q = segs[s_seg[k]];
+        const int num = *q.dnum;
+        if (lane == 0) mbar_arrive_expect_tx(&bar, (uint32_t)num * q.bw * 4u + tx_extra);
+        __syncwarp();
+        const int x = (int)(s_fb[k] & ~3ull);
+        for (int p = lane; p < num; p += 32)
+            tma_load_2d(tile + (32 - num + p) * RS, (const CUtensorMap*)q.map, x, p, &bar);
+        const uint32_t r0 = (uint32_t)(g - q.unit_begin) * q.rpu, nr = q.F.n[0] * q.F.n[1];
+        for (uint32_t r = lane; r < q.rpu; r += 32)
+            if (r0 + r < nr) rows[r] = fused_row(r0 + r, q.F, q.C, q.s0, q.s1, s_fb[k]);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        plan(u, 0);
+        if (u + step < total) plan(u + step, 1);
+    }
+    __syncthreads();
+    zero_rows(0);
+    __syncthreads();
+    if (warp == 0) issue(0, u, s_row[0]);
+    uint32_t parity = 0;
+    for (int it = 0; u < total; it++, u += step) {
+        const bool ok = mbar_wait_bounded(&bar, parity, wait_limit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) atomicExch(status, PRODM_ETIMEOUT);
+            mbar_wait_bounded(&bar, parity, wait_limit);
+            return;
+        }
+        parity ^= 1u;
+        const int k = it % 3;
+        const FusedSeg& q = segs[s_seg[k]];
+        const uint64_t fb = s_fb[k];
+        const uint32_t nbk = s_nbk[k];
+        if (threadIdx.x == 0 && u + 2 * step < total) plan(u + 2 * step, (it + 2) % 3);
+        const int num = *q.dnum;
+        const int exp = frexp_exp(__uint_as_float(*q.key)) + 2;
+        const bool neg = num != 0 && (num & 1);              // NegaBinaryBPEncoder.hpp:153, :177
+        const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
+        const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
+        const uint32_t* t0 = tile + (fb & 3u);
+        if (dfast) decode_tile_pm<true, RS>(t0, cb, nbk, num, exp, neg, dscale);
+        else decode_tile_pm<false, RS>(t0, cb, nbk, num, exp, neg, dscale);
+        __syncthreads();
+        // the tile is free again: the next unit's rows below its planes are
+        // zeroed (rows the copies do not write) and its planes arrive during
+        // the recomposition
+        if (u + step < total) {
+            zero_rows((it + 1) % 3);
+            if (warp == 0) {
+                fence_proxy_async_smem();
+                issue((it + 1) % 3, u + step, s_row[(it + 1) & 1]);
+            }
+        }
+        const uint32_t rows = q.F.n[0] * q.F.n[1];
+        const uint32_t rho0 = (uint32_t)(u - q.unit_begin) * q.rpu;
+        for (uint32_t r = warp; r < q.rpu && rho0 + r < rows; r += 8)
+            recompose_fine_row(s_row[it & 1][r], q.C, q.coarse, q.out, cb, lane);
     }
 }
 
@@ -857,6 +1040,76 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
     k_decode_recompose_nb32<<<grid, 256, smem, st>>>((const uint32_t*)base, stride, (const uint32_t*)maxkey, dnum,
                                                      coarse, F, C, out, s0, s1, fused_max_blocks(F));
     PRODM_CHECK_LAUNCH("k_decode_recompose_nb32");
+    return PRODM_OK;
+}
+
+uint32_t fused_unit_blocks(const Box& F) { return fused_max_blocks(F); }
+
+uint32_t fused_unit_rows(const Box& F) {
+    const uint32_t m = 264 / (F.n[2] ? F.n[2] : 1);
+    return 8 * (m < 1 ? 1 : (m > kMaxUnitRows / 8 ? kMaxUnitRows / 8 : m));
+}
+uint32_t fused_unit_blocks_rows(const Box& F, uint32_t nr) { return (uint32_t)(((uint64_t)nr * F.n[2] + 31) / 32 + 2); }
+
+uint32_t fused_tma_box(const Box& F, uint32_t nr) {
+    if (!(F.n[2] & 1u)) return 0;
+    const uint32_t bw = (fused_unit_blocks_rows(F, nr) + 3 + 3) & ~3u;   // block range + up to 3 words of alignment
+    return bw <= 160 ? bw : 0;
+}
+
+int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || !bw || (uintptr_t)base % 16 != 0 || stride % 4 != 0) return PRODM_EUNSUPPORTED;
+    const cuuint64_t dims[2] = {nblocks, (cuuint64_t)planes};
+    const cuuint64_t strides[1] = {stride * 4};
+    const cuuint32_t box[2] = {bw, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    if (enc((CUtensorMap*)map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return PRODM_EUNSUPPORTED;
+    return PRODM_OK;
+}
+
+template <int RS>
+static int launch_tma_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld, unsigned ctas_per_sm,
+                            int* status, cudaStream_t st) {
+    const size_t smem = (size_t)32 * RS * 4 + (size_t)tld * CB_LD * 4;
+    const void* kern = (const void*)k_decode_recompose_nb32_tma_multi<RS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+    uint64_t cap = persistent_grid_for(kern, 256, smem, total_units, total_units);
+    if (ctas_per_sm) cap = std::min<uint64_t>(cap, (uint64_t)device_sms() * ctas_per_sm);
+    const unsigned grid = (unsigned)std::max<uint64_t>(cap, 1);
+    k_decode_recompose_nb32_tma_multi<RS><<<grid, 256, smem, st>>>(segs, nseg, total_units, status, g_tma_wait_cycles,
+                                                                  (uint32_t)g_tma_tx_extra);
+    PRODM_CHECK_LAUNCH("k_decode_recompose_nb32_tma_multi");
+    return PRODM_OK;
+}
+
+int launch_decode_recompose_nb32_tma_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
+                                           uint32_t max_bw, unsigned ctas_per_sm, int* status, cudaStream_t st) {
+    if (!total_units) return PRODM_OK;
+    if (max_bw <= 96) return launch_tma_multi<96>(segs, nseg, total_units, tld, ctas_per_sm, status, st);
+    if (max_bw <= 160) return launch_tma_multi<160>(segs, nseg, total_units, tld, ctas_per_sm, status, st);
+    return fail(PRODM_EUNSUPPORTED, "batched fused level: TMA box above 160 words");
+}
+size_t fused_multi_smem(uint32_t tld) { return (size_t)tld * TB_LD * 4 + (size_t)tld * CB_LD * 4; }
+
+// ctas_per_sm == 0: as many as fit
+int launch_decode_recompose_nb32_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
+                                       unsigned ctas_per_sm, cudaStream_t st) {
+    if (!total_units) return PRODM_OK;
+    const size_t smem = fused_multi_smem(tld);
+    if (smem > 200 * 1024) return fail(PRODM_EUNSUPPORTED, "batched fused level: rows too long");
+    const void* kern = (const void*)k_decode_recompose_nb32_multi;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+    uint64_t cap = persistent_grid_for(kern, 256, smem, total_units, total_units);
+    if (ctas_per_sm) cap = std::min<uint64_t>(cap, (uint64_t)device_sms() * ctas_per_sm);
+    const unsigned grid = (unsigned)std::max<uint64_t>(cap, 1);
+    k_decode_recompose_nb32_multi<<<grid, 256, smem, st>>>(segs, nseg, total_units, tld);
+    PRODM_CHECK_LAUNCH("k_decode_recompose_nb32_multi");
     return PRODM_OK;
 }
 

@@ -112,6 +112,40 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
                                  const uint8_t* dnum, const float* coarse, const Box& F, const Box& C, float* out,
                                  uint64_t s0, uint64_t s1, int* status, cudaStream_t st, bool pdl = false);
 void fused_tma_test_hook(int tx_extra, long long wait_cycles);
+// one segment per field of the batched fused launch: the finest level of an
+// fp32 negabinary field (odd row length) decoded and recomposed from its
+// coarse box; unit_begin is the field's first global 8-row unit
+struct FusedSeg {
+    const uint32_t* base;   // plane 0 of the level's streams
+    uint64_t stride;        // words per plane row
+    const uint32_t* key;    // level |max| key
+    const uint8_t* dnum;    // retrieved plane count
+    const float* coarse;
+    float* out;
+    Box F, C;
+    uint64_t s0, s1;
+    uint64_t unit_begin;
+    const void* map;        // TMA form: the planes' tensor map (a CUtensorMap in device memory)
+    uint32_t bw;            // TMA form: its box width in words
+    uint32_t rpu;           // TMA form: rows per unit (a multiple of 8, at most kMaxUnitRows)
+};
+constexpr uint32_t kMaxUnitRows = 64;
+// blocks of the plane tile of an 8-row unit of box F, and the launch's dynamic
+// shared memory for units of at most that many blocks
+uint32_t fused_unit_blocks(const Box& F);
+size_t fused_multi_smem(uint32_t tld);
+int launch_decode_recompose_nb32_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
+                                       unsigned ctas_per_sm, cudaStream_t st);
+// TMA form: box width of a level's tensor map for units of nr rows (0: rows
+// too long or even), the
+// map of one level's planes (CUtensorMap, 128 bytes, into `map`), the launch
+// over segments whose maps live in device memory (64-byte aligned)
+uint32_t fused_unit_rows(const Box& F);                          // rows per unit of the TMA form
+uint32_t fused_unit_blocks_rows(const Box& F, uint32_t nr);      // tile blocks of nr rows
+uint32_t fused_tma_box(const Box& F, uint32_t nr);
+int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw);
+int launch_decode_recompose_nb32_tma_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
+                                           uint32_t max_bw, unsigned ctas_per_sm, int* status, cudaStream_t st);
 
 // perbit.cu: per-bit format; rows of 32-element group words (magnitude
 // planes 0..B-1, sign row B, unseen row B+1), each row `stride` words

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 def test_batch_matches_single_field_path():
     from prodm_gb300 import api, fields
-    shapes = [(33, 33, 33), (65, 65, 65), (129, 65), (33, 65, 17), (1000,), (9, 9, 9), (257, 129)]
+    shapes = [(33, 33, 33), (65, 65, 65), (129, 65), (33, 65, 17), (1000,), (9, 9, 9), (257, 129), (33, 1025)]
     xs = [fields.spectral_grf(s, slope=-2.0, seed=i).contiguous() for i, s in enumerate(shapes)]
     levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
     batch = api.MDRBatch(xs, levels, 32)
@@ -56,7 +56,7 @@ def test_batch_matches_oracle():
     from prodm_gb300 import api, fields
     O = oracle.oracle()
     B = 32
-    shapes = [(65, 65, 65), (129, 65), (33, 65, 17), (1000,), (9, 9, 9), (40, 33, 21)]
+    shapes = [(65, 65, 65), (129, 65), (33, 65, 17), (1000,), (9, 9, 9), (40, 33, 21), (17, 1025), (20, 31, 64)]
     xs = [fields.spectral_grf(s, slope=-2.0, seed=40 + i).contiguous() for i, s in enumerate(shapes)]
     levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
     batch = api.MDRBatch(xs, levels, B)
@@ -115,3 +115,33 @@ def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
             batch.refactor(); batch.reset(); batch.retrieve()
             torch.cuda.synchronize()
             ref = [o.clone() for o in batch.outs]
+
+
+def test_batch_fused_tile_wait_timeout_is_reported_and_recoverable():
+    """The batched TMA fused kernel bounds its waits for plane tiles: with the
+    expected byte count raised (the test hook) every wait runs out, the kernel
+    reports PRODM_ETIMEOUT through prodm_batch_status (once) and the next
+    retrieval equals the one before."""
+    from prodm_gb300 import api, fields
+    from prodm_gb300._lib import ProdmError
+    shapes = [(65, 65, 65), (129, 129), (33, 65, 17)]
+    xs = [fields.spectral_grf(s, seed=20 + i) for i, s in enumerate(shapes)]
+    batch = api.MDRBatch(xs, None, 32)
+    batch.set_tolerances([float(x.max() - x.min()) * 1e-3 for x in xs])
+    batch.refactor()
+    batch.reset()
+    good = [o.clone() for o in batch.retrieve()]
+    batch.status()
+    api.debug_tile_wait(64, 20000)
+    try:
+        batch.reset()
+        batch.retrieve()
+        with pytest.raises(ProdmError) as e:
+            batch.status()
+        assert e.value.status == 4          # PRODM_ETIMEOUT
+    finally:
+        api.debug_tile_wait(0, 0)
+    batch.status()                          # reported once
+    batch.reset()
+    for a, b in zip(batch.retrieve(), good):
+        assert torch.equal(a, b)

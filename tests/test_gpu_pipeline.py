@@ -250,9 +250,12 @@ def test_reconstructor_fed_from_reference_files(enc):
             np.testing.assert_allclose(out, g[enc + "_recon"][t], rtol=0, atol=1e-5 * float(np.abs(field).max()))
 
 
-@pytest.mark.parametrize("shape,L", [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129, 129, 129), 4),
-                                     ((200, 131), 4), ((33, 33, 1025), 2), ((40, 33, 301), 3), ((33, 33, 513), 3),
-                                     ((40, 36, 411), 2), ((33, 32, 801), 2)])
+FUSED_SHAPES = [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129, 129, 129), 4), ((200, 131), 4),
+                ((33, 33, 1025), 2), ((40, 33, 301), 3), ((33, 33, 513), 3), ((40, 36, 411), 2), ((33, 32, 801), 2),
+                ((129, 513), 3), ((65, 9, 513), 2), ((65, 17, 513), 2)]
+
+
+@pytest.mark.parametrize("shape,L", FUSED_SHAPES)
 def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
     """fp32 negabinary hierarchical: the finest level is decoded inside the
     recomposition kernel (odd and even row lengths take different kernels;
