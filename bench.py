@@ -655,7 +655,9 @@ def run_batched(steps=5):
     return {"fields": len(xs), "bytes_per_step": nbytes, "ms_batched": ms_b, "ms_plain_loop": ms_p,
             "batched_gbs": nbytes / (ms_b / 1e3) / 1e9, "plain_loop_gbs": nbytes / (ms_p / 1e3) / 1e9,
             "speedup": ms_p / ms_b, "identical_results": bool(same),
-            "autotuned_launch": {k: {"threads_per_cta": v[0], "ctas_per_sm": v[1]} for k, v in tuned[0].items()},
+            "autotuned_launch": {k: {"threads_per_cta": v[0], "ctas_per_sm": v[1]} for k, v in tuned[0].items()
+                                 if k != "fused_unit"},
+            "autotuned_fused_unit_values": tuned[0].get("fused_unit", (None,))[0],
             "workload": "24 cubes {33,65,129,257}^3, 24 2-D {513,1025,2049}^2, 16 x 129x257x65; spectral slopes "
                         "U[-3,-1]; levels = largest keeping level 0 >= 32 values; 32 planes; negabinary; "
                         "relative L-inf tolerances log-U[1e-5,1e-2]; refactor + retrieve per step"}

@@ -406,6 +406,11 @@ int prodm_batch_set_launch(prodm_batch* h, int threads_per_cta, int ctas_per_sm)
 #define PRODM_BATCH_RECOMPOSE 2
 #define PRODM_BATCH_FUSED 3
 int prodm_batch_set_stage_launch(prodm_batch* h, int stage, int threads_per_cta, int ctas_per_sm);
+/* tile shape of the fused finest levels: about this many values per unit of
+ * consecutive fine rows (256..8192; default 2112 = 8 rows of 264); rows per
+ * unit are a multiple of 8, at most 64, and a unit whose planes no longer fit
+ * a TMA box takes the cp.async kernel */
+int prodm_batch_set_fused_unit(prodm_batch* h, int values_per_unit);
 int prodm_batch_refactor(prodm_batch* h, void* stream);
 int prodm_batch_set_tolerances(prodm_batch* h, const double* h_tolerances, void* stream);
 int prodm_batch_retrieve(prodm_batch* h, int interpreter, int estimator, double s, void* stream);

@@ -102,6 +102,7 @@ _SIGS = {
     "prodm_batch_retrieve": (_i, [_P, _i, _i, C.c_double, _P]),
     "prodm_batch_reset": (_i, [_P, _P]),
     "prodm_batch_status": (_i, [_P, _P]),
+    "prodm_batch_set_fused_unit": (_i, [_P, _i]),
     "prodm_batch_field_info": (_i, [_P, _i, _u8p, _u32p, _dp, _P]),
     "prodm_batch_export_level": (_i, [_P, _i, _i, _P, C.c_uint64, _i, _u64p, _P]),
     "prodm_batch_destroy": (_i, [_P]),

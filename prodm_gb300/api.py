@@ -509,6 +509,11 @@ class MDRBatch:
         levels, decoded inside their recomposition)."""
         call("prodm_batch_set_stage_launch", self.h, self.STAGES[stage], int(threads_per_cta), int(ctas_per_sm))
 
+    def set_fused_unit(self, values_per_unit):
+        """Tile shape of the fused finest levels: about this many values per
+        unit of consecutive fine rows (rebuilds the segment tables)."""
+        call("prodm_batch_set_fused_unit", self.h, int(values_per_unit))
+
     def refactor(self, stream=None):
         call("prodm_batch_refactor", self.h, _stream(stream))
 

@@ -1,4 +1,4 @@
-"""Launch-shape autotuner for the batched executor.
+"""Launch-shape and tile-shape autotuner for the batched executor.
 
 Times launch shapes for the persistent multi-field launches on the actual
 batch and keeps the fastest, one stage at a time (coordinate descent): the
@@ -7,7 +7,9 @@ in flight per CTA, and CTAs per SM, i.e. how many row groups share an SM) and
 the encoder (CTAs per SM of its 256-thread chunk workers) and the fused
 finest-level decode + recomposition (CTAs per SM of its 8-row units), each timed as the
 whole refactor + retrieve step with the other stages at their best shape so
-far. Results persist in a JSON cache keyed by the GPU name and the batch's
+far; then the tile shape of the fused finest levels (values per unit of
+consecutive fine rows: 8-row units of long rows, up to 64 rows of short
+ones). Results persist in a JSON cache keyed by the GPU name and the batch's
 shapes and level counts ($PRODM_AUTOTUNE_CACHE, default
 ~/.cache/prodm_gb300/autotune.json).
 """
@@ -26,6 +28,9 @@ FUSED_CANDIDATES = ((256, 2), (256, 3), (256, 4), (256, 5))
 STAGE_CANDIDATES = {"decompose": ROW_CANDIDATES, "recompose": ROW_CANDIDATES, "encode": ENCODE_CANDIDATES,
                     "fused": FUSED_CANDIDATES}
 DEFAULT = {"decompose": (256, 8), "encode": (256, 8), "recompose": (256, 8), "fused": (256, 5)}
+# values per unit of the fused finest levels
+UNIT_CANDIDATES = (1056, 2112, 4224)
+DEFAULT_UNIT = 2112
 # the uniform shapes of the earlier single-shape tuner (still accepted by set_launch)
 CANDIDATES = ((128, 8), (256, 4), (256, 8), (256, 16))
 
@@ -76,13 +81,17 @@ def _time(batch, reps):
 
 
 def _apply(batch, shapes):
-    for stage, (t, c) in shapes.items():
-        batch.set_stage_launch(stage, t, c)
+    for stage, v in shapes.items():
+        if stage == "fused_unit":
+            batch.set_fused_unit(v[0])
+        else:
+            batch.set_stage_launch(stage, v[0], v[1])
 
 
 def tune(batch, reps=3, use_cache=True):
-    """Pick and apply the fastest launch shape of every stage; returns
-    (shapes {stage: (threads, ctas_per_sm)}, timings {"stage:TxC": ms})."""
+    """Pick and apply the fastest launch shape of every stage and the fused
+    levels' tile shape; returns (shapes {stage: (threads, ctas_per_sm)} plus
+    {"fused_unit": (values,)}, timings {"stage:TxC": ms, "fused_unit:V": ms})."""
     sig = signature(batch)
     cache = _load() if use_cache else {}
     if sig in cache and "stages" in cache[sig]:
@@ -102,6 +111,15 @@ def tune(batch, reps=3, use_cache=True):
                 best = (ms, (t, c))
         shapes[stage] = best[1]
         batch.set_stage_launch(stage, *best[1])
+    best = None
+    for v in UNIT_CANDIDATES:
+        batch.set_fused_unit(v)
+        ms = _time(batch, reps)
+        timings["fused_unit:%d" % v] = ms
+        if best is None or ms < best[0]:
+            best = (ms, v)
+    shapes["fused_unit"] = (best[1],)
+    batch.set_fused_unit(best[1])
     cache[sig] = {"stages": {k: list(v) for k, v in shapes.items()}, "ms": timings}
     if use_cache:
         _store(cache)

@@ -180,6 +180,9 @@ struct prodm_batch {
     // launch shape per stage (decompose, encode, recompose): threads per CTA,
     // CTAs per SM of the persistent grid
     int st_threads[4] = {256, 256, 256, 256}, st_ctas[4] = {8, 8, 8, 0};
+    // values per unit of the fused finest levels (TMA form): the tile shape
+    // the autotuner searches with prodm_batch_set_fused_unit
+    uint32_t unit_values = 2112;
     ~prodm_batch() {
         for (void* p : allocs) cudaFree(p);
     }
@@ -296,7 +299,7 @@ int batch_build_segments(prodm_batch* h) {
             s.s0 = (uint64_t)s.F.n[1] * s.F.n[2];
             s.s1 = s.F.n[2];
             uint32_t t = fused_unit_blocks(s.F);
-            s.rpu = fused_unit_rows(s.F);
+            s.rpu = fused_unit_rows(s.F, h->unit_values);
             s.bw = fused_tma_box(s.F, s.rpu);
             int k = 2;
             if (s.bw && encode_plane_map(maps.data() + (size_t)f * 128, s.base, nbk, B, s.stride, s.bw) == PRODM_OK) {
@@ -526,6 +529,14 @@ int prodm_batch_set_stage_launch(prodm_batch* h, int stage, int threads_per_cta,
     h->st_threads[stage] = threads_per_cta;
     h->st_ctas[stage] = ctas_per_sm;
     return PRODM_OK;
+}
+
+int prodm_batch_set_fused_unit(prodm_batch* h, int values_per_unit) {
+    if (!h) return fail(PRODM_EINVAL, "NULL handle");
+    if (values_per_unit < 256 || values_per_unit > 8192)
+        return fail(PRODM_EINVAL, "values per fused unit must be in [256, 8192]");
+    h->unit_values = (uint32_t)values_per_unit;
+    return h->bound ? batch_build_segments(h) : PRODM_OK;
 }
 
 int prodm_batch_set_launch(prodm_batch* h, int threads_per_cta, int ctas_per_sm) {

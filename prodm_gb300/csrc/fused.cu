@@ -1045,8 +1045,8 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
 
 uint32_t fused_unit_blocks(const Box& F) { return fused_max_blocks(F); }
 
-uint32_t fused_unit_rows(const Box& F) {
-    const uint32_t m = 264 / (F.n[2] ? F.n[2] : 1);
+uint32_t fused_unit_rows(const Box& F, uint32_t values) {
+    const uint32_t m = values / 8 / (F.n[2] ? F.n[2] : 1);
     return 8 * (m < 1 ? 1 : (m > kMaxUnitRows / 8 ? kMaxUnitRows / 8 : m));
 }
 uint32_t fused_unit_blocks_rows(const Box& F, uint32_t nr) { return (uint32_t)(((uint64_t)nr * F.n[2] + 31) / 32 + 2); }

@@ -140,7 +140,8 @@ int launch_decode_recompose_nb32_multi(const FusedSeg* segs, int nseg, uint64_t 
 // too long or even), the
 // map of one level's planes (CUtensorMap, 128 bytes, into `map`), the launch
 // over segments whose maps live in device memory (64-byte aligned)
-uint32_t fused_unit_rows(const Box& F);                          // rows per unit of the TMA form
+// rows per unit of the TMA form: a multiple of 8, about `values` values
+uint32_t fused_unit_rows(const Box& F, uint32_t values);
 uint32_t fused_unit_blocks_rows(const Box& F, uint32_t nr);      // tile blocks of nr rows
 uint32_t fused_tma_box(const Box& F, uint32_t nr);
 int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw);

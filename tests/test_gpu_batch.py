@@ -44,6 +44,32 @@ def test_batch_matches_single_field_path():
         assert float((outs[i] - x).abs().max()) <= tols[i]
 
 
+@pytest.mark.parametrize("values", [256, 1056, 4224, 8192])
+def test_batch_fused_unit_shapes_match_single_field_path(values):
+    """Every tile shape the autotuner may pick (values per unit of the fused
+    finest levels; at 8192 the units of 257-wide rows no longer fit a TMA box
+    and take the cp.async kernel) gives the single-field path's
+    reconstructions bit for bit."""
+    from prodm_gb300 import api, fields
+    shapes = [(65, 65, 65), (129, 33), (33, 65, 17), (17, 513), (9, 9, 9), (33, 257)]
+    xs = [fields.spectral_grf(s, slope=-2.0, seed=60 + i).contiguous() for i, s in enumerate(shapes)]
+    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+    batch = api.MDRBatch(xs, levels, 32)
+    batch.set_fused_unit(values)
+    tols = [float(x.max() - x.min()) * 10.0 ** (-2 - i % 3) for i, x in enumerate(xs)]
+    batch.set_tolerances(tols)
+    batch.refactor()
+    batch.reset()
+    outs = batch.retrieve("negabinary", "max_hb")
+    torch.cuda.synchronize()
+    batch.status()
+    for i, (s, x) in enumerate(zip(shapes, xs)):
+        one = api.MDRField(s, torch.float32, levels[i], 32, "negabinary", "hierarchical", "max")
+        one.refactor(x)
+        out1 = one.retrieve(tols[i], interpreter="negabinary", estimator="max_hb")
+        assert torch.equal(out1, outs[i]), (values, i)
+
+
 def test_batch_matches_oracle():
     """Each field of a batch checked against the oracle alone (not through the
     single-field path): the oracle interpreter (negabinary look-ahead,
@@ -92,8 +118,11 @@ def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
     batch = api.MDRBatch(xs, None, 32)
     tuned, timings = autotune.tune(batch, reps=1)
     for stage, shape in tuned.items():
-        assert shape in autotune.STAGE_CANDIDATES[stage]
-    assert len(timings) == sum(len(c) for c in autotune.STAGE_CANDIDATES.values())
+        if stage == "fused_unit":
+            assert shape[0] in autotune.UNIT_CANDIDATES
+        else:
+            assert shape in autotune.STAGE_CANDIDATES[stage]
+    assert len(timings) == sum(len(c) for c in autotune.STAGE_CANDIDATES.values()) + len(autotune.UNIT_CANDIDATES)
     assert autotune.tune(batch)[0] == tuned            # served from the cache
     batch.set_tolerances([1e-3] * 3)
     ref = None
