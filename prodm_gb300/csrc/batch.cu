@@ -33,6 +33,7 @@ struct RowSeg {
     uint32_t row_begin;
     uint32_t* key_l;        // decompose: level |max| key
     uint32_t* key_c;        // decompose at level 1: level-0 |max| key
+    uint32_t patch;         // decompose: work items are patch items (decompose_patch_item), not rows
 };
 
 // segment of global row g: binary search over the segments' first rows,
@@ -51,7 +52,7 @@ __device__ __forceinline__ void stage_row_begins(const RowSeg* segs, int nseg, u
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(256, 4) k_decompose_multi(const RowSeg* __restrict__ segs, int nseg, uint32_t total) {
+__global__ void __launch_bounds__(256, 3) k_decompose_multi(const RowSeg* __restrict__ segs, int nseg, uint32_t total) {
     extern __shared__ uint32_t s_begin[];
     stage_row_begins(segs, nseg, s_begin);
     const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
@@ -70,7 +71,9 @@ __global__ void __launch_bounds__(256, 4) k_decompose_multi(const RowSeg* __rest
         const int s = find_row_seg(s_begin, nseg, g);
         if (s != cur) { flush(); cur = s; }
         const RowSeg& q = segs[s];
-        if (q.F.n[2] & 1u)
+        if (q.patch)
+            decompose_patch_item<float>(q.in, q.s0, q.s1, q.F, q.C, q.coef, q.out, g - q.row_begin, lane, mk, mc);
+        else if (q.F.n[2] & 1u)
             decompose_row_odd_any<float>(q.in, q.s0, q.s1, q.F, q.C, q.coef, q.out, nullptr, g - q.row_begin, lane,
                                          mk, mc);
         else
@@ -242,7 +245,8 @@ int batch_build_segments(prodm_batch* h) {
                 s.row_begin = drow;
                 s.key_l = h->keys + f * kMaxL + l;
                 s.key_c = l == 1 ? h->keys + f * kMaxL : nullptr;
-                drow += s.F.n[0] * s.F.n[1];
+                s.patch = patch_grid(s.F, s.C) ? 1u : 0u;
+                drow += s.patch ? (uint32_t)patch_items(s.C) : s.F.n[0] * s.F.n[1];
                 ds.push_back(s);
             }
             const int lr = d + 1;                 // recompose level at this depth

@@ -18,6 +18,8 @@
 //  * in place -- the reference layout: the level box of a strided array,
 //                reordered per dim so that coarse nodes come first
 //                (DecomposerInterface.hpp:14-16).
+#include <cstdlib>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "rows.cuh"
@@ -187,6 +189,30 @@ __global__ void __launch_bounds__(256) k_decompose_rows(const T* __restrict__ in
     if (maxkey_coarse) {
         mc = warp_max_key(mc);
         if ((threadIdx.x & 31) == 0 && mc) atomicMax(maxkey_coarse, mc);
+    }
+}
+
+// patch form (grids whose every dim is 2 C - 1, no natural-order copy): one
+// warp item = coarse columns 32g .. 32g + 31 of a 2 x 2 kPatchSteps strip of
+// fine rows (decompose_patch_item)
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_decompose_patch(const T* __restrict__ in, uint64_t s0, uint64_t s1, Box F,
+                                                         Box C, T* __restrict__ coef, T* __restrict__ coarse,
+                                                         typename KeyOf<T>::type* maxkey_level,
+                                                         typename KeyOf<T>::type* maxkey_coarse) {
+    using K = typename KeyOf<T>::type;
+    K mk = 0, mc = 0;
+    const uint64_t items = patch_items(C);
+    const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (uint64_t w = (uint64_t)blockIdx.x * wpb + (threadIdx.x >> 5); w < items; w += (uint64_t)gridDim.x * wpb)
+        decompose_patch_item<T>(in, s0, s1, F, C, coef, coarse, w, lane, mk, mc);
+    if (maxkey_level) {
+        mk = warp_max_key(mk);
+        if (lane == 0 && mk) atomicMax(maxkey_level, mk);
+    }
+    if (maxkey_coarse) {
+        mc = warp_max_key(mc);
+        if (lane == 0 && mc) atomicMax(maxkey_coarse, mc);
     }
 }
 
@@ -503,6 +529,11 @@ __global__ void k_interleave(T* __restrict__ data, uint64_t s0, uint64_t s1, Box
 // ---------------------------------------------------------------------------
 // one warp per row, 8 warps per CTA; enough CTAs for full occupancy
 unsigned row_threads(uint32_t) { return 256; }
+// PRODM_DECOMPOSE_PATCH=0 keeps every level on the row kernel (read per launch)
+bool decompose_patch_enabled() {
+    const char* v = getenv("PRODM_DECOMPOSE_PATCH");
+    return !(v && v[0] == '0');
+}
 unsigned row_grid(uint64_t rows, unsigned th) {
     const uint64_t wpb = th / 32;
     uint64_t need = (rows + wpb - 1) / wpb;
@@ -516,6 +547,12 @@ int launch_decompose_level_packed(const T* in, uint64_t s0, uint64_t s1, const B
                                   T* fnat, void* maxkey_level, void* maxkey_coarse, cudaStream_t st) {
     using K = typename KeyOf<T>::type;
     const unsigned th = row_threads(F.n[2]);
+    if (!fnat && patch_grid(F, C) && decompose_patch_enabled()) {
+        k_decompose_patch<T><<<row_grid(patch_items(C), th), th, 0, st>>>(in, s0, s1, F, C, coef, coarse,
+                                                                          (K*)maxkey_level, (K*)maxkey_coarse);
+        PRODM_CHECK_LAUNCH("k_decompose_patch");
+        return PRODM_OK;
+    }
     k_decompose_rows<T><<<row_grid((uint64_t)F.n[0] * F.n[1], th), th, 0, st>>>(in, s0, s1, F, C, coef, coarse, fnat,
                                                                                  (K*)maxkey_level, (K*)maxkey_coarse);
     PRODM_CHECK_LAUNCH("k_decompose_rows");

@@ -171,6 +171,183 @@ __device__ __forceinline__ void decompose_row_odd(const T* __restrict__ p, uint6
     }
 }
 
+// ---------------------------------------------------------------------------
+// Patch form of the decomposition for grids whose every dim is 2 C - 1 (the
+// 2^k + 1 grids): a warp takes coarse columns c = 32 g + lane of the fine
+// rows x0 in {2i, 2i+1} x x1 in {2b, 2b+1} for kPatchSteps consecutive b.
+// With q the fine values at even x2 (the corner nodes) of the rows 2i, 2i+2
+// (x0) and 2b, 2b+2 (x1), h = avg(q at 2c, q at 2c+2), the four rows' nodes
+// 2c, 2c+1 subtract
+//   (2i,   2b  ): -        | h00                 (even node: coarse node)
+//   (2i,   2b+1): V0       | HV0                 V0 = avg(q00, q02), HV0 = avg(h00, h02)
+//   (2i+1, 2b  ): avg(q00, q20)  | avg(h00, h20)
+//   (2i+1, 2b+1): avg(V0, V2)    | avg(HV0, HV2)  V2 = avg(q20, q22), HV2 = avg(h20, h22)
+// -- the row kernels' corner trees (dim 2 innermost, dim 0 outermost), so the
+// coefficients are bit-identical to decompose_row_odd's. Each interpolation
+// is formed once per 2 x 2 rows and the corner rows 2b + 2 carry over to the
+// next b. The last node of each row (x2 = F2 - 1, even only) is taken by the
+// lane holding coarse column P = C2 - 1 (or, when P is a multiple of 32, by
+// lane 31 of the last group, from the neighbour values it loads itself).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPatchSteps = 8;
+
+__host__ __device__ inline bool patch_grid(const Box& F, const Box& C) {
+    return F.n[0] == 2 * C.n[0] - 1 && F.n[1] == 2 * C.n[1] - 1 && F.n[2] == 2 * C.n[2] - 1 && C.n[2] >= 2;
+}
+// warp items of one level: slabs x strips x column groups
+__host__ __device__ inline uint64_t patch_items(const Box& C) {
+    const uint32_t npg = (C.n[2] - 1 + 31) >> 5;
+    return (uint64_t)C.n[0] * ((C.n[1] + kPatchSteps - 1) / kPatchSteps) * npg;
+}
+
+template <class T>
+__device__ __forceinline__ void decompose_patch_item(const T* __restrict__ in, uint64_t s0, uint64_t s1,
+                                                     const Box& F, const Box& C, T* __restrict__ coef,
+                                                     T* __restrict__ coarse, uint64_t item, uint32_t lane,
+                                                     typename KeyOf<T>::type& mk, typename KeyOf<T>::type& mc) {
+    using K = typename KeyOf<T>::type;
+    const uint32_t C0 = C.n[0], C1 = C.n[1], C2 = C.n[2];
+    const uint32_t P = C2 - 1, npg = (P + 31) >> 5, nstrip = (C1 + kPatchSteps - 1) / kPatchSteps;
+    const uint32_t g = (uint32_t)(item % npg);
+    const uint64_t r = item / npg;
+    const uint32_t u = (uint32_t)(r % nstrip), i = (uint32_t)(r / nstrip);
+    const uint32_t c = 32 * g + lane;
+    const bool act = c < P;                        // a column pair (2c, 2c+1)
+    const bool ld = c <= P;                        // holds coarse column c
+    const bool two = i + 1 < C0;                   // fine row 2i + 1 exists
+    // the last node: its own column (P not a multiple of 32) or lane 31's neighbour
+    const bool last = (g == npg - 1) && ((P & 31) ? (lane == (P & 31)) : (lane == 31));
+    const bool own = c == P;
+    const uint32_t b0 = u * kPatchSteps, b1 = min(b0 + kPatchSteps, C1);
+    const T* base = in + (uint64_t)(2 * i) * s0;
+    auto kmax = [](K& m, T v) { const K k = abs_key(v); m = k > m ? k : m; };
+    // the loads of one step, issued a step ahead of their use: the four
+    // rows' node pairs, the corner values of rows 2b + 2 at column c and (lane
+    // 31) at column c + 1, and the last node's even values
+    struct Step {
+        T a00, e01, o01, e10, o10, e11, o11, q02, q22, n02, n22, l01, l10, l11;
+    };
+    auto load_step = [&](uint32_t b, Step& S) {
+        const bool odd = b + 1 < C1;
+        const T* r00 = base + (uint64_t)(2 * b) * s1;
+        const T* r01 = r00 + s1;
+        const T* r10 = r00 + s0;
+        const T* r11 = r10 + s1;
+        const uint64_t x = 2 * (uint64_t)c, xl = 2 * (uint64_t)P;
+        S.a00 = act ? r00[x + 1] : (T)0;
+        S.e01 = act && odd ? r01[x] : (T)0;
+        S.o01 = act && odd ? r01[x + 1] : (T)0;
+        S.e10 = act && two ? r10[x] : (T)0;
+        S.o10 = act && two ? r10[x + 1] : (T)0;
+        S.e11 = act && two && odd ? r11[x] : (T)0;
+        S.o11 = act && two && odd ? r11[x + 1] : (T)0;
+        S.q02 = ld && odd ? r00[2 * s1 + x] : (T)0;
+        S.q22 = ld && odd && two ? r00[2 * s0 + 2 * s1 + x] : (T)0;
+        S.n02 = lane == 31 && act && odd ? r00[2 * s1 + x + 2] : (T)0;
+        S.n22 = lane == 31 && act && odd && two ? r00[2 * s0 + 2 * s1 + x + 2] : (T)0;
+        S.l01 = last && odd ? r01[xl] : (T)0;
+        S.l10 = last && two ? r10[xl] : (T)0;
+        S.l11 = last && two && odd ? r11[xl] : (T)0;
+    };
+    // corner values at column c + 1: the next lane's, lane 31's own load
+    auto next_col = [&](T q, T own_next) {
+        const T n = __shfl_down_sync(0xffffffffu, q, 1);
+        return lane == 31 ? own_next : n;
+    };
+    T q00, q20 = 0;
+    {
+        const T* r = base + (uint64_t)(2 * b0) * s1;
+        const uint64_t x = 2 * (uint64_t)c;
+        q00 = ld ? r[x] : (T)0;
+        T n00 = lane == 31 && act ? r[x + 2] : (T)0, n20 = 0;
+        if (two) {
+            q20 = ld ? r[2 * s0 + x] : (T)0;
+            n20 = lane == 31 && act ? r[2 * s0 + x + 2] : (T)0;
+        }
+        n00 = next_col(q00, n00);
+        n20 = next_col(q20, n20);
+        Step S;
+        load_step(b0, S);
+        T qn00 = n00, qn20 = n20;
+        T h00 = avg_rn(q00, qn00), h20 = avg_rn(q20, qn20);
+        for (uint32_t b = b0; b < b1; b++) {
+            Step Sn = S;
+            if (b + 1 < b1) load_step(b + 1, Sn);
+            const bool odd = b + 1 < C1;
+            const T qn02 = next_col(S.q02, S.n02), qn22 = next_col(S.q22, S.n22);
+            const T q02 = S.q02, q22 = S.q22;
+            const T h02 = avg_rn(q02, qn02), h22 = avg_rn(q22, qn22);
+            const uint64_t rb00 = level_rank(i, b, C2, F, C);              // even-even row: odd nodes only
+            const uint64_t rb01 = level_rank(i, C1 + b, 0, F, C);
+            const uint64_t rb10 = level_rank(C0 + i, b, 0, F, C);
+            const uint64_t rb11 = level_rank(C0 + i, C1 + b, 0, F, C);
+            T* crow = coarse + ((uint64_t)i * C1 + b) * C2;
+            const T v0 = avg_rn(q00, q02), hv0 = avg_rn(h00, h02);
+            const T v2 = avg_rn(q20, q22), hv2 = avg_rn(h20, h22);
+            if (act) {
+                crow[c] = q00;
+                kmax(mc, q00);
+                T d = sub_rn(S.a00, h00);
+                coef[rb00 + c] = d;
+                kmax(mk, d);
+                if (odd) {
+                    d = sub_rn(S.e01, v0);
+                    coef[rb01 + c] = d;
+                    kmax(mk, d);
+                    d = sub_rn(S.o01, hv0);
+                    coef[rb01 + C2 + c] = d;
+                    kmax(mk, d);
+                }
+                if (two) {
+                    d = sub_rn(S.e10, avg_rn(q00, q20));
+                    coef[rb10 + c] = d;
+                    kmax(mk, d);
+                    d = sub_rn(S.o10, avg_rn(h00, h20));
+                    coef[rb10 + C2 + c] = d;
+                    kmax(mk, d);
+                    if (odd) {
+                        d = sub_rn(S.e11, avg_rn(v0, v2));
+                        coef[rb11 + c] = d;
+                        kmax(mk, d);
+                        d = sub_rn(S.o11, avg_rn(hv0, hv2));
+                        coef[rb11 + C2 + c] = d;
+                        kmax(mk, d);
+                    }
+                }
+            }
+            if (last) {   // coarse column P: the rows' last (even) nodes
+                const T p00 = own ? q00 : qn00, p02 = own ? q02 : qn02;
+                const T p20 = own ? q20 : qn20, p22 = own ? q22 : qn22;
+                crow[P] = p00;
+                kmax(mc, p00);
+                const T w0 = avg_rn(p00, p02);
+                if (odd) {
+                    const T d = sub_rn(S.l01, w0);
+                    coef[rb01 + P] = d;
+                    kmax(mk, d);
+                }
+                if (two) {
+                    T d = sub_rn(S.l10, avg_rn(p00, p20));
+                    coef[rb10 + P] = d;
+                    kmax(mk, d);
+                    if (odd) {
+                        d = sub_rn(S.l11, avg_rn(w0, avg_rn(p20, p22)));
+                        coef[rb11 + P] = d;
+                        kmax(mk, d);
+                    }
+                }
+            }
+            q00 = q02;
+            qn00 = qn02;
+            h00 = h02;
+            q20 = q22;
+            qn20 = qn22;
+            h20 = h22;
+            S = Sn;
+        }
+    }
+}
+
 template <class T>
 __device__ __forceinline__ void decompose_row_odd_any(const T* __restrict__ in, uint64_t s0, uint64_t s1,
                                                       const Box& F, const Box& C, T* __restrict__ coef,
