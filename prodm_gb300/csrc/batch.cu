@@ -33,7 +33,9 @@ struct RowSeg {
     uint32_t row_begin;
     uint32_t* key_l;        // decompose: level |max| key
     uint32_t* key_c;        // decompose at level 1: level-0 |max| key
-    uint32_t patch;         // decompose: work items are patch items (decompose_patch_item), not rows
+    uint32_t patch;         // work items are patch items (decompose_ / recompose_patch_item), not rows:
+                            // every 2^k + 1 level of a batch (all fields' levels share one launch,
+                            // so the single-field path's minimum item count does not apply)
 };
 
 // segment of global row g: binary search over the segments' first rows,
@@ -89,7 +91,9 @@ __global__ void __launch_bounds__(256) k_recompose_multi(const RowSeg* __restric
     for (uint32_t g = blockIdx.x * wpb + (threadIdx.x >> 5); g < total; g += gridDim.x * wpb) {
         const int s = find_row_seg(s_begin, nseg, g);
         const RowSeg& q = segs[s];
-        if (q.F.n[2] & 1u)
+        if (q.patch)
+            recompose_patch_item<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
+        else if (q.F.n[2] & 1u)
             recompose_row_odd_any<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
         else
             recompose_row<float>(q.in, q.coef, q.F, q.C, q.out, q.s0, q.s1, g - q.row_begin, lane);
@@ -260,7 +264,8 @@ int batch_build_segments(prodm_batch* h) {
                 s.s0 = (uint64_t)s.F.n[1] * s.F.n[2];
                 s.s1 = s.F.n[2];
                 s.row_begin = rrow;
-                rrow += s.F.n[0] * s.F.n[1];
+                s.patch = patch_grid(s.F, s.C) ? 1u : 0u;
+                rrow += s.patch ? (uint32_t)patch_items(s.C) : s.F.n[0] * s.F.n[1];
                 rs.push_back(s);
             }
         }

@@ -216,6 +216,20 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_decompose_patch
     }
 }
 
+// patch form of the recomposition (recompose_patch_item), same items as k_decompose_patch
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_recompose_patch(const T* __restrict__ coarse,
+                                                                                  const T* __restrict__ coef, Box F,
+                                                                                  Box C, T* __restrict__ out,
+                                                                                  uint64_t s0, uint64_t s1) {
+    pdl_wait();   // the coarse box and the coefficients come from the previous launches
+    pdl_release();
+    const uint64_t items = patch_items(C);
+    const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    for (uint64_t w = (uint64_t)blockIdx.x * wpb + (threadIdx.x >> 5); w < items; w += (uint64_t)gridDim.x * wpb)
+        recompose_patch_item<T>(coarse, coef, F, C, out, s0, s1, w, lane);
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_recompose_rows(const T* __restrict__ coarse, const T* __restrict__ coef, Box F,
                                                         Box C, T* __restrict__ out, uint64_t s0, uint64_t s1) {
@@ -529,7 +543,8 @@ __global__ void k_interleave(T* __restrict__ data, uint64_t s0, uint64_t s1, Box
 // ---------------------------------------------------------------------------
 // one warp per row, 8 warps per CTA; enough CTAs for full occupancy
 unsigned row_threads(uint32_t) { return 256; }
-// PRODM_DECOMPOSE_PATCH=0 keeps every level on the row kernel (read per launch)
+// PRODM_DECOMPOSE_PATCH=0 keeps every level on the row kernels (decomposition and
+// recomposition; read per launch)
 bool decompose_patch_enabled() {
     const char* v = getenv("PRODM_DECOMPOSE_PATCH");
     return !(v && v[0] == '0');
@@ -547,7 +562,7 @@ int launch_decompose_level_packed(const T* in, uint64_t s0, uint64_t s1, const B
                                   T* fnat, void* maxkey_level, void* maxkey_coarse, cudaStream_t st) {
     using K = typename KeyOf<T>::type;
     const unsigned th = row_threads(F.n[2]);
-    if (!fnat && patch_grid(F, C) && decompose_patch_enabled()) {
+    if (!fnat && patch_level(F, C) && decompose_patch_enabled()) {
         k_decompose_patch<T><<<row_grid(patch_items(C), th), th, 0, st>>>(in, s0, s1, F, C, coef, coarse,
                                                                           (K*)maxkey_level, (K*)maxkey_coarse);
         PRODM_CHECK_LAUNCH("k_decompose_patch");
@@ -574,6 +589,12 @@ int launch_recompose_level_packed(const T* coarse, const T* coef, const Box& F, 
                                   uint64_t s1, cudaStream_t st, bool pdl) {
     const unsigned th = row_threads(F.n[2]);
     count_launch();
+    if (patch_level(F, C) && decompose_patch_enabled()) {
+        const cudaError_t e = launch_chain(pdl, k_recompose_patch<T>, dim3(row_grid(patch_items(C), th)), dim3(th), 0,
+                                           st, coarse, coef, F, C, out, s0, s1);
+        if (e != cudaSuccess) return cuda_status(e, "k_recompose_patch");
+        return PRODM_OK;
+    }
     const cudaError_t e = launch_chain(pdl, k_recompose_rows<T>, dim3(row_grid((uint64_t)F.n[0] * F.n[1], th)), dim3(th),
                                        0, st, coarse, coef, F, C, out, s0, s1);
     if (e != cudaSuccess) return cuda_status(e, "k_recompose_rows");

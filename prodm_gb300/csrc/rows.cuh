@@ -1,6 +1,7 @@
 // Per-row bodies of the row-parallel MGARD kernels (one warp per fine row),
 // shared by the single-field kernels and the multi-field batched kernels.
 #pragma once
+#include <cstdlib>
 #include "common.cuh"
 
 namespace prodm {
@@ -199,6 +200,19 @@ __host__ __device__ inline uint64_t patch_items(const Box& C) {
     const uint32_t npg = (C.n[2] - 1 + 31) >> 5;
     return (uint64_t)C.n[0] * ((C.n[1] + kPatchSteps - 1) / kPatchSteps) * npg;
 }
+// a level takes the patch kernels when it is a patch grid with enough items:
+// each item walks kPatchSteps steps one after another, so a small level (a
+// few hundred items) runs faster as one warp per row (at 513^3 levels 7 and 6
+// have 67,848 and 8,772 items; level 5 has 1,170). The threshold is 2048
+// items, or PRODM_PATCH_MIN_ITEMS (read at each use; the tests set 1 to run
+// the patch kernels on small grids).
+inline uint64_t patch_min_items() {
+    const char* v = getenv("PRODM_PATCH_MIN_ITEMS");
+    return v ? strtoull(v, nullptr, 10) : 2048ull;
+}
+inline bool patch_level(const Box& F, const Box& C) {
+    return patch_grid(F, C) && patch_items(C) >= patch_min_items();
+}
 
 template <class T>
 __device__ __forceinline__ void decompose_patch_item(const T* __restrict__ in, uint64_t s0, uint64_t s1,
@@ -345,6 +359,122 @@ __device__ __forceinline__ void decompose_patch_item(const T* __restrict__ in, u
             h20 = h22;
             S = Sn;
         }
+    }
+}
+
+// Patch form of the recomposition (the inverse of decompose_patch_item): the
+// same warp items; the corner values come from the compact coarse box (rows
+// (i, b), (i, b+1), (i+1, b), (i+1, b+1) of its coarse columns), the
+// coefficients from the packed level, and the four fine rows' nodes 2c, 2c+1
+// are the coefficient plus the interpolation of decompose_patch_item (the
+// row kernels' corner trees, so the output is bit-identical to theirs). Each
+// step's loads are issued a step ahead of their use.
+template <class T>
+__device__ __forceinline__ void recompose_patch_item(const T* __restrict__ coarse, const T* __restrict__ coef,
+                                                     const Box& F, const Box& C, T* __restrict__ out, uint64_t s0,
+                                                     uint64_t s1, uint64_t item, uint32_t lane) {
+    const uint32_t C0 = C.n[0], C1 = C.n[1], C2 = C.n[2];
+    const uint32_t P = C2 - 1, npg = (P + 31) >> 5, nstrip = (C1 + kPatchSteps - 1) / kPatchSteps;
+    const uint32_t g = (uint32_t)(item % npg);
+    const uint64_t r = item / npg;
+    const uint32_t u = (uint32_t)(r % nstrip), i = (uint32_t)(r / nstrip);
+    const uint32_t c = 32 * g + lane;
+    const bool act = c < P;
+    const bool ld = c <= P;
+    const bool two = i + 1 < C0;
+    const bool last = (g == npg - 1) && ((P & 31) ? (lane == (P & 31)) : (lane == 31));
+    const bool own = c == P;
+    const uint32_t b0 = u * kPatchSteps, b1 = min(b0 + kPatchSteps, C1);
+    const uint64_t cs0 = (uint64_t)C1 * C2;
+    const T* slab0 = coarse + (uint64_t)i * cs0;         // coarse rows (i, b)
+    const T* slab1 = slab0 + cs0;                         // (i + 1, b)
+    struct Step {
+        T q02, q22, n02, n22, ca, cbe, cbo, cce, cco, cde, cdo, lb, lc, ld_;
+    };
+    auto load_step = [&](uint32_t b, Step& S) {
+        const bool odd = b + 1 < C1;
+        const uint64_t rb00 = level_rank(i, b, C2, F, C);
+        const uint64_t rb01 = level_rank(i, C1 + b, 0, F, C);
+        const uint64_t rb10 = level_rank(C0 + i, b, 0, F, C);
+        const uint64_t rb11 = level_rank(C0 + i, C1 + b, 0, F, C);
+        const T* q0 = slab0 + (uint64_t)(b + 1) * C2;
+        const T* q1 = slab1 + (uint64_t)(b + 1) * C2;
+        S.q02 = ld && odd ? __ldg(q0 + c) : (T)0;
+        S.q22 = ld && odd && two ? __ldg(q1 + c) : (T)0;
+        S.n02 = lane == 31 && act && odd ? __ldg(q0 + c + 1) : (T)0;
+        S.n22 = lane == 31 && act && odd && two ? __ldg(q1 + c + 1) : (T)0;
+        S.ca = act ? __ldg(coef + rb00 + c) : (T)0;
+        S.cbe = act && odd ? __ldg(coef + rb01 + c) : (T)0;
+        S.cbo = act && odd ? __ldg(coef + rb01 + C2 + c) : (T)0;
+        S.cce = act && two ? __ldg(coef + rb10 + c) : (T)0;
+        S.cco = act && two ? __ldg(coef + rb10 + C2 + c) : (T)0;
+        S.cde = act && two && odd ? __ldg(coef + rb11 + c) : (T)0;
+        S.cdo = act && two && odd ? __ldg(coef + rb11 + C2 + c) : (T)0;
+        S.lb = last && odd ? __ldg(coef + rb01 + P) : (T)0;
+        S.lc = last && two ? __ldg(coef + rb10 + P) : (T)0;
+        S.ld_ = last && two && odd ? __ldg(coef + rb11 + P) : (T)0;
+    };
+    auto next_col = [&](T q, T own_next) {
+        const T n = __shfl_down_sync(0xffffffffu, q, 1);
+        return lane == 31 ? own_next : n;
+    };
+    const T* q0 = slab0 + (uint64_t)b0 * C2;
+    const T* q1 = slab1 + (uint64_t)b0 * C2;
+    T q00 = ld ? __ldg(q0 + c) : (T)0, q20 = ld && two ? __ldg(q1 + c) : (T)0;
+    T qn00 = next_col(q00, lane == 31 && act ? __ldg(q0 + c + 1) : (T)0);
+    T qn20 = next_col(q20, lane == 31 && act && two ? __ldg(q1 + c + 1) : (T)0);
+    T h00 = avg_rn(q00, qn00), h20 = avg_rn(q20, qn20);
+    Step S;
+    load_step(b0, S);
+    for (uint32_t b = b0; b < b1; b++) {
+        Step Sn = S;
+        if (b + 1 < b1) load_step(b + 1, Sn);
+        const bool odd = b + 1 < C1;
+        const T q02 = S.q02, q22 = S.q22;
+        const T qn02 = next_col(q02, S.n02), qn22 = next_col(q22, S.n22);
+        const T h02 = avg_rn(q02, qn02), h22 = avg_rn(q22, qn22);
+        const T v0 = avg_rn(q00, q02), hv0 = avg_rn(h00, h02);
+        const T v2 = avg_rn(q20, q22), hv2 = avg_rn(h20, h22);
+        T* o00 = out + (uint64_t)(2 * i) * s0 + (uint64_t)(2 * b) * s1;
+        T* o01 = o00 + s1;
+        T* o10 = o00 + s0;
+        T* o11 = o10 + s1;
+        if (act) {
+            const uint64_t x = 2 * (uint64_t)c;
+            o00[x] = q00;
+            o00[x + 1] = add_rn(S.ca, h00);
+            if (odd) {
+                o01[x] = add_rn(S.cbe, v0);
+                o01[x + 1] = add_rn(S.cbo, hv0);
+            }
+            if (two) {
+                o10[x] = add_rn(S.cce, avg_rn(q00, q20));
+                o10[x + 1] = add_rn(S.cco, avg_rn(h00, h20));
+                if (odd) {
+                    o11[x] = add_rn(S.cde, avg_rn(v0, v2));
+                    o11[x + 1] = add_rn(S.cdo, avg_rn(hv0, hv2));
+                }
+            }
+        }
+        if (last) {   // coarse column P: the rows' last (even) nodes
+            const uint64_t x = 2 * (uint64_t)P;
+            const T p00 = own ? q00 : qn00, p02 = own ? q02 : qn02;
+            const T p20 = own ? q20 : qn20, p22 = own ? q22 : qn22;
+            o00[x] = p00;
+            const T w0 = avg_rn(p00, p02);
+            if (odd) o01[x] = add_rn(S.lb, w0);
+            if (two) {
+                o10[x] = add_rn(S.lc, avg_rn(p00, p20));
+                if (odd) o11[x] = add_rn(S.ld_, avg_rn(w0, avg_rn(p20, p22)));
+            }
+        }
+        q00 = q02;
+        qn00 = qn02;
+        h00 = h02;
+        q20 = q22;
+        qn20 = qn22;
+        h20 = h22;
+        S = Sn;
     }
 }
 

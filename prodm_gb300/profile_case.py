@@ -12,7 +12,11 @@ interpreter with MaxErrorEstimatorHB, relative L-inf tolerances 1e-3..1e-9.
 With --basis orthogonal: the orthogonal MGARD basis on the same fp64 shear
 layer with the grouped encoder, 60 planes, max collector, SignExclude
 interpreter with MaxErrorEstimatorOB and relative L-inf tolerances 1e-3,
-1e-6, 1e-9. --shape takes one edge (a cube) or AxBxC.
+1e-6, 1e-9. --shape takes one edge (a cube) or AxBxC. With --batch N: a
+batch of N 257^3 and four 129x257x65 spectral fields (slope -2, largest
+level counts, 32 planes, negabinary, relative L-inf 1e-3) refactored and
+retrieved `reps` times through MDRBatch, with fixed launch shapes (no
+autotuning).
 """
 import argparse
 import math
@@ -33,7 +37,11 @@ def main():
                     help="after the steps, the lossless stage on the finest level's streams: compress + decompress")
     ap.add_argument("--import-streams", action="store_true",
                     help="per-bit only: export the level files and load them into a second handle (the parse)")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="N > 0: a batch of N 257^3 and four 129x257x65 fields instead of one field")
     a = ap.parse_args()
+    if a.batch:
+        return batch(a.batch, a.reps)
     dims = tuple(int(v) for v in a.shape.split("x"))
     shape = dims * 3 if len(dims) == 1 else dims
     if a.basis == "orthogonal":
@@ -113,6 +121,26 @@ def orthogonal(shape, L, reps):
     for (kind, level), (ms, n) in sorted(mdr.stage_times().items(), key=lambda kv: -kv[1][0]):
         print("%-10s l%-2d %8.4f ms over %d launches" % (kind, level, ms, n))
     print("final max error %.3g of range %.3g" % (float((out - x).abs().max().item()), vr))
+
+
+def batch(n, reps):
+    shapes = [(257, 257, 257)] * n + [(129, 257, 65)] * 4
+    xs = [fields.spectral_grf(s, slope=-2.0, seed=900 + i) for i, s in enumerate(shapes)]
+    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+    b = api.MDRBatch(xs, levels, 32)
+    for stage, shape in (("decompose", (256, 8)), ("encode", (256, 8)), ("recompose", (256, 4)), ("fused", (256, 5))):
+        b.set_stage_launch(stage, *shape)
+    b.set_tolerances([1e-3 * float(x.max() - x.min()) for x in xs])
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for r in range(reps):
+        e0.record()
+        b.refactor()
+        b.reset()
+        b.retrieve("negabinary", "max_hb")
+        e1.record()
+    torch.cuda.synchronize()
+    b.status()
+    print("batch of %d fields: last refactor + retrieve %.4f ms" % (len(xs), e0.elapsed_time(e1)))
 
 
 if __name__ == "__main__":

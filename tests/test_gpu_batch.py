@@ -70,6 +70,32 @@ def test_batch_fused_unit_shapes_match_single_field_path(values):
         assert torch.equal(out1, outs[i]), (values, i)
 
 
+def test_batch_patch_items_match_single_field_path(monkeypatch):
+    """The batched decomposition and recomposition with patch work items on
+    every 2^k + 1 level (PRODM_PATCH_MIN_ITEMS=1) give the single-field row
+    kernels' streams and reconstructions bit for bit."""
+    from prodm_gb300 import api, fields
+    monkeypatch.setenv("PRODM_PATCH_MIN_ITEMS", "1")
+    shapes = [(65, 65, 65), (129, 33), (33, 65, 17), (20, 31, 64)]
+    xs = [fields.spectral_grf(s, slope=-2.0, seed=80 + i).contiguous() for i, s in enumerate(shapes)]
+    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+    batch = api.MDRBatch(xs, levels, 32)
+    tols = [float(x.max() - x.min()) * 10.0 ** (-2 - i % 3) for i, x in enumerate(xs)]
+    batch.set_tolerances(tols)
+    batch.refactor()
+    batch.reset()
+    outs = [o.clone() for o in batch.retrieve("negabinary", "max_hb")]
+    torch.cuda.synchronize()
+    monkeypatch.setenv("PRODM_DECOMPOSE_PATCH", "0")
+    for i, (s, x) in enumerate(zip(shapes, xs)):
+        one = api.MDRField(s, torch.float32, levels[i], 32, "negabinary", "hierarchical", "max")
+        one.refactor(x)
+        for l in range(levels[i] + 1):
+            assert np.array_equal(batch.export_level(i, l), one.export_level(l)), (i, l)
+        out1 = one.retrieve(tols[i], interpreter="negabinary", estimator="max_hb")
+        assert torch.equal(out1, outs[i]), i
+
+
 def test_batch_matches_oracle():
     """Each field of a batch checked against the oracle alone (not through the
     single-field path): the oracle interpreter (negabinary look-ahead,

@@ -309,3 +309,36 @@ def test_fused_tile_wait_timeout_is_reported_and_recoverable(shape):
     m.status()                              # reported once
     m.reset()
     assert torch.equal(m.retrieve_planes(idx), good)
+
+
+@pytest.mark.parametrize("shape,L,dt", [((65, 65, 65), 3, np.float32), ((33, 17, 9), 2, np.float32),
+                                        ((129, 65), 4, np.float32), ((17, 9, 129), 2, np.float32),
+                                        ((33, 33, 33), 3, np.float64), ((17, 9, 33), 2, np.float64)])
+def test_patch_kernels_bit_identical_to_row_kernels(shape, L, dt, monkeypatch):
+    """The patch decomposition and recomposition (2^k + 1 grids; forced onto
+    small grids with PRODM_PATCH_MIN_ITEMS=1) give the row kernels'
+    coefficients, streams and reconstructions bit for bit (PRODM_DECOMPOSE_PATCH=0
+    keeps every level on the row kernels); the fp32 reconstructions also equal
+    the oracle's decode -> reposition -> recompose."""
+    B = 32 if dt == np.float32 else 60
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    x = fields().spectral_grf(shape, seed=sum(shape), dtype=tdt)
+    idx = [min(B, 9 + 3 * l) for l in range(L + 1)]
+    res = {}
+    for mode in ("patch", "rows"):
+        monkeypatch.setenv("PRODM_PATCH_MIN_ITEMS", "1")
+        monkeypatch.setenv("PRODM_DECOMPOSE_PATCH", "1" if mode == "patch" else "0")
+        m = api().MDRField(shape, tdt, L, B, "negabinary", "hierarchical", "max")
+        m.refactor(x)
+        coef = m.coefficients().cpu().numpy()
+        blob = np.concatenate([m.export_level(l) for l in range(L + 1)])
+        out = m.retrieve_planes(idx).cpu().numpy()
+        res[mode] = (coef, blob, out, m.level_info())
+        m.close()
+    for a, b in zip(res["patch"][:3], res["rows"][:3]):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    if dt == np.float32:
+        sizes, bounds, _ = res["patch"][3]
+        ref = O.retrieve(shape, L, B, res["patch"][1], sizes, bounds.astype(np.float32), np.array(idx, np.uint8),
+                         "negabinary", True)
+        assert np.array_equal(res["patch"][2].view(np.uint32), ref.view(np.uint32))
