@@ -16,7 +16,9 @@ interpreter with MaxErrorEstimatorOB and relative L-inf tolerances 1e-3,
 batch of N 257^3 and four 129x257x65 spectral fields (slope -2, largest
 level counts, 32 planes, negabinary, relative L-inf 1e-3) refactored and
 retrieved `reps` times through MDRBatch, with fixed launch shapes (no
-autotuning).
+autotuning). With --batch-config4: the benchmark's 64-field batch (24 cubes,
+24 2-D fields, 16 anisotropic fields; relative L-inf tolerances 1e-5..1e-2)
+with the same fixed launch shapes.
 """
 import argparse
 import math
@@ -39,9 +41,10 @@ def main():
                     help="per-bit only: export the level files and load them into a second handle (the parse)")
     ap.add_argument("--batch", type=int, default=0,
                     help="N > 0: a batch of N 257^3 and four 129x257x65 fields instead of one field")
+    ap.add_argument("--batch-config4", action="store_true", help="the benchmark's 64-field batch")
     a = ap.parse_args()
-    if a.batch:
-        return batch(a.batch, a.reps)
+    if a.batch or a.batch_config4:
+        return batch(a.batch, a.reps, a.batch_config4)
     dims = tuple(int(v) for v in a.shape.split("x"))
     shape = dims * 3 if len(dims) == 1 else dims
     if a.basis == "orthogonal":
@@ -123,14 +126,23 @@ def orthogonal(shape, L, reps):
     print("final max error %.3g of range %.3g" % (float((out - x).abs().max().item()), vr))
 
 
-def batch(n, reps):
-    shapes = [(257, 257, 257)] * n + [(129, 257, 65)] * 4
-    xs = [fields.spectral_grf(s, slope=-2.0, seed=900 + i) for i, s in enumerate(shapes)]
-    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+def batch(n, reps, config4=False):
+    if config4:
+        xs, tols, levels = [], [], []
+        for i, (shape, slope, rel) in enumerate(fields.batch_specs(seed=7)):
+            x = fields.spectral_grf(shape, slope=slope, seed=500 + i)
+            xs.append(x)
+            tols.append(rel * float(x.max() - x.min()))
+            levels.append(fields.batch_level(shape, api.max_level(shape)))
+    else:
+        shapes = [(257, 257, 257)] * n + [(129, 257, 65)] * 4
+        xs = [fields.spectral_grf(s, slope=-2.0, seed=900 + i) for i, s in enumerate(shapes)]
+        tols = [1e-3 * float(x.max() - x.min()) for x in xs]
+        levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
     b = api.MDRBatch(xs, levels, 32)
     for stage, shape in (("decompose", (256, 8)), ("encode", (256, 8)), ("recompose", (256, 4)), ("fused", (256, 5))):
         b.set_stage_launch(stage, *shape)
-    b.set_tolerances([1e-3 * float(x.max() - x.min()) for x in xs])
+    b.set_tolerances(tols)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for r in range(reps):
         e0.record()
