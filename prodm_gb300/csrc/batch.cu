@@ -311,7 +311,10 @@ int batch_build_segments(prodm_batch* h) {
             s.rpu = fused_unit_rows(s.F, h->unit_values);
             s.bw = fused_tma_box(s.F, s.rpu);
             int k = 2;
-            if (s.bw && encode_plane_map(maps.data() + (size_t)f * 128, s.base, nbk, B, s.stride, s.bw) == PRODM_OK) {
+            void* m = maps.data() + (size_t)f * 128;
+            s.tall = s.bw && fused_tma_tall() && B <= 32 &&
+                     encode_plane_map(m, s.base, nbk, B, s.stride, fused_tma_stride(s.bw), 32) == PRODM_OK;
+            if (s.tall || (s.bw && encode_plane_map(m, s.base, nbk, B, s.stride, s.bw) == PRODM_OK)) {
                 k = s.bw <= 96 ? 0 : 1;
                 s.map = h->fmaps + (size_t)f * 128;
                 t = fused_unit_blocks_rows(s.F, s.rpu);

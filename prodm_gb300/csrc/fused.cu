@@ -590,7 +590,7 @@ template <int RS>
 __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
     const __grid_constant__ CUtensorMap tmap, uint32_t bw, const uint32_t* __restrict__ maxkey,
     const uint8_t* __restrict__ dnum, const float* __restrict__ coarse, Box F, Box C, float* __restrict__ out,
-    uint64_t s0, uint64_t s1, int* __restrict__ status, long long wait_limit, uint32_t tx_extra) {
+    uint64_t s0, uint64_t s1, int* __restrict__ status, long long wait_limit, uint32_t tx_extra, int tall) {
     extern __shared__ __align__(128) uint32_t tma_smem[];
     uint32_t* tile = tma_smem;                               // [32][RS] plane-major
     float* cb = (float*)(tma_smem + 32 * RS);                // [block][CB_LD]
@@ -622,15 +622,20 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma(
         fused_block_range(rho0, rows, F, C, s_fb[0], s_nbk[0]);
         if (rho0 + step < rows) fused_block_range(rho0 + step, rows, F, C, s_fb[1], s_nbk[1]);
     }
-    for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) tile[i] = 0u;   // planes not retrieved
+    if (!tall)
+        for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) tile[i] = 0u;   // planes not retrieved
     __syncthreads();
     if (warp == 0) rows_of(rho0, s_fb[0], s_row[0]);
-    const uint32_t bytes = (uint32_t)num * bw * 4u + tx_extra;
+    const uint32_t bytes = (tall ? 32u * RS : (uint32_t)num * bw) * 4u + tx_extra;
     auto issue = [&](uint64_t fb) {   // warp 0
         if (lane == 0) mbar_arrive_expect_tx(&bar, bytes);
         __syncwarp();
         const int x = (int)(fb & ~3ull);
-        for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar);
+        if (tall) {   // one box of all 32 tile rows; rows of planes below 0 arrive as zeros
+            if (lane == 0) tma_load_2d(tile, &tmap, x, num - 32, &bar);
+        } else {
+            for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar);
+        }
     };
     if (warp == 0) issue(s_fb[0]);
     // the first tile is on its way; the coarse box and the output belong to
@@ -704,22 +709,29 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma_multi(cons
                           q.rpu);
     };
     // every thread: rows [zlo, 32 - num) zeroed for the unit in slot k (rows
-    // below zlo are zero already); afterwards rows below 32 - num are zero
+    // below zlo are zero already; a tall copy writes zeros there itself);
+    // afterwards rows below 32 - num are zero
     uint32_t zlo = 0;
     auto zero_rows = [&](int k) {
-        const uint32_t lo = 32u - *segs[s_seg[k]].dnum;
-        for (uint32_t i = zlo * RS + threadIdx.x; i < lo * RS; i += blockDim.x) tile[i] = 0u;
+        const FusedSeg& q = segs[s_seg[k]];
+        const uint32_t lo = 32u - *q.dnum;
+        if (!q.tall)
+            for (uint32_t i = zlo * RS + threadIdx.x; i < lo * RS; i += blockDim.x) tile[i] = 0u;
         zlo = lo;
     };
     // warp 0: the copies of the unit in slot k, and the row geometry of unit g
     auto issue = [&](int k, uint64_t g, FusedRow* rows) {
         const FusedSeg& q = segs[s_seg[k]];
         const int num = *q.dnum;
-        if (lane == 0) mbar_arrive_expect_tx(&bar, (uint32_t)num * q.bw * 4u + tx_extra);
+        if (lane == 0) mbar_arrive_expect_tx(&bar, (q.tall ? 32u * RS : (uint32_t)num * q.bw) * 4u + tx_extra);
         __syncwarp();
         const int x = (int)(s_fb[k] & ~3ull);
-        for (int p = lane; p < num; p += 32)
-            tma_load_2d(tile + (32 - num + p) * RS, (const CUtensorMap*)q.map, x, p, &bar);
+        if (q.tall) {   // one box of all 32 tile rows; rows of planes below 0 arrive as zeros
+            if (lane == 0) tma_load_2d(tile, (const CUtensorMap*)q.map, x, num - 32, &bar);
+        } else {
+            for (int p = lane; p < num; p += 32)
+                tma_load_2d(tile + (32 - num + p) * RS, (const CUtensorMap*)q.map, x, p, &bar);
+        }
         const uint32_t r0 = (uint32_t)(g - q.unit_begin) * q.rpu, nr = q.F.n[0] * q.F.n[1];
         for (uint32_t r = lane; r < q.rpu; r += 32)
             if (r0 + r < nr) rows[r] = fused_row(r0 + r, q.F, q.C, q.s0, q.s1, s_fb[k]);
@@ -792,7 +804,8 @@ template <int RS>
 __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     const __grid_constant__ CUtensorMap tmap, uint32_t bw, const uint32_t* __restrict__ maxkey,
     const uint8_t* __restrict__ dnum, const float* __restrict__ coarse, Box F, Box C, float* __restrict__ out,
-    uint64_t s0, uint64_t s1, uint32_t tld, int* __restrict__ status, long long wait_limit, uint32_t tx_extra) {
+    uint64_t s0, uint64_t s1, uint32_t tld, int* __restrict__ status, long long wait_limit, uint32_t tx_extra,
+    int tall) {
     extern __shared__ __align__(128) uint32_t ws_smem[];
     uint32_t* tiles = ws_smem;                               // [2][32][RS] plane-major
     float* cbs = (float*)(ws_smem + 2 * 32 * RS);            // [2][tld][CB_LD]
@@ -828,12 +841,13 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
         mbar_init(&bar_empty[0], GROUP);
         mbar_init(&bar_empty[1], GROUP);
     }
-    for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) {   // planes not retrieved
-        tiles[i] = 0u;
-        tiles[32 * RS + i] = 0u;
-    }
+    if (!tall)
+        for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) {   // planes not retrieved
+            tiles[i] = 0u;
+            tiles[32 * RS + i] = 0u;
+        }
     __syncthreads();
-    const uint32_t bytes = (uint32_t)num * bw * 4u + tx_extra;
+    const uint32_t bytes = (tall ? 32u * RS : (uint32_t)num * bw) * 4u + tx_extra;
     // warp 0: block range of unit k of this CTA into slot b, then its planes into tile b
     auto issue = [&](int k, int b) {
         if (lane == 0) {
@@ -844,7 +858,11 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
         __syncwarp();
         const int x = (int)(s_fb[b] & ~3ull);
         uint32_t* tile = tiles + b * 32 * RS;
-        for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar_tile[b]);
+        if (tall) {   // one box of all 32 tile rows; rows of planes below 0 arrive as zeros
+            if (lane == 0) tma_load_2d(tile, &tmap, x, num - 32, &bar_tile[b]);
+        } else {
+            for (int p = lane; p < num; p += 32) tma_load_2d(tile + (poff + p) * RS, &tmap, x, p, &bar_tile[b]);
+        }
     };
     if (warp == 0) {
         issue(0, 0);
@@ -957,7 +975,7 @@ static int fused_ws() {
 template <int RS>
 static int launch_fused_ws(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
                            const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
-                           int* status, cudaStream_t st, bool pdl) {
+                           int* status, cudaStream_t st, bool pdl, int tall) {
     const uint32_t tld = fused_max_blocks(F);
     const size_t smem = (size_t)2 * 32 * RS * 4 + (size_t)2 * tld * CB_LD * 4;
     const void* kern = (const void*)k_decode_recompose_nb32_ws<RS>;
@@ -968,7 +986,7 @@ static int launch_fused_ws(const CUtensorMap& map, uint32_t bw, const void* maxk
     count_launch();
     e = launch_chain(pdl, k_decode_recompose_nb32_ws<RS>, dim3(grid), dim3(512), smem, st, map, bw,
                      (const uint32_t*)maxkey, dnum, coarse, F, C, out, s0, s1, tld, status, g_tma_wait_cycles,
-                     (uint32_t)g_tma_tx_extra);
+                     (uint32_t)g_tma_tx_extra, tall);
     if (e != cudaSuccess) return cuda_status(e, "k_decode_recompose_nb32_ws");
     return PRODM_OK;
 }
@@ -976,9 +994,9 @@ static int launch_fused_ws(const CUtensorMap& map, uint32_t bw, const void* maxk
 template <int RS>
 static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
                             const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
-                            int* status, cudaStream_t st, bool pdl) {
+                            int* status, cudaStream_t st, bool pdl, int tall) {
     if (fused_ws() == 1 || (fused_ws() == 2 && RS >= 160))
-        return launch_fused_ws<RS>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
+        return launch_fused_ws<RS>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
     const size_t smem = (size_t)32 * RS * 4 + (size_t)fused_max_blocks(F) * CB_LD * 4;
     const void* kern = (const void*)k_decode_recompose_nb32_tma<RS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -989,10 +1007,18 @@ static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* max
     count_launch();
     e = launch_chain(pdl, k_decode_recompose_nb32_tma<RS>, dim3(grid), dim3(256), smem, st, map, bw,
                      (const uint32_t*)maxkey, dnum, coarse, F, C, out, s0, s1, status, g_tma_wait_cycles,
-                     (uint32_t)g_tma_tx_extra);
+                     (uint32_t)g_tma_tx_extra, tall);
     if (e != cudaSuccess) return cuda_status(e, "k_decode_recompose_nb32_tma");
     return PRODM_OK;
 }
+
+// PRODM_TMA_TALL: 1 (default) stages a unit's planes by one tall box, 0 by one box per plane
+static int tma_tall() {
+    const char* v = getenv("PRODM_TMA_TALL");
+    return v ? atoi(v) : 1;
+}
+bool fused_tma_tall() { return tma_tall() != 0; }
+uint32_t fused_tma_stride(uint32_t bw) { return bw <= 96 ? 96u : (bw <= 160 ? 160u : 256u); }
 
 // Returns PRODM_EUNSUPPORTED when the shape does not suit the row mapping
 // (the caller then runs the unfused kernels). Odd rows take the TMA kernel
@@ -1006,19 +1032,20 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
     const bool odd = (F.n[2] & 1u) != 0;
     if (odd && status && (uintptr_t)base % 16 == 0 && stride % 4 == 0) {
         const uint32_t bw = (fused_max_blocks(F) + 3 + 3) & ~3u;   // block range + up to 3 words of alignment
-        PFN_cuTensorMapEncodeTiled_v12000 enc = bw <= 256 ? tensor_map_encoder() : nullptr;
-        if (enc) {
-            CUtensorMap map;
-            const cuuint64_t dims[2] = {nblocks, (cuuint64_t)planes};
-            const cuuint64_t strides[1] = {stride * 4};
-            const cuuint32_t box[2] = {bw, 1};
-            const cuuint32_t estr[2] = {1, 1};
-            if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
-                if (bw <= 96) return launch_fused_tma<96>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
-                if (bw <= 160) return launch_fused_tma<160>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
-                return launch_fused_tma<256>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl);
+        if (bw <= 256) {
+            const uint32_t rs = fused_tma_stride(bw);
+            // tall: one box of rs words x 32 plane rows per unit (planes above
+            // the retrieved ones at negative coordinates, zero filled); else one
+            // box of bw words per retrieved plane
+            alignas(64) CUtensorMap map;
+            const int tall =
+                tma_tall() && planes <= 32 && encode_plane_map(&map, base, nblocks, planes, stride, rs, 32) == PRODM_OK;
+            if (tall || encode_plane_map(&map, base, nblocks, planes, stride, bw, 1) == PRODM_OK) {
+                if (rs == 96)
+                    return launch_fused_tma<96>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
+                if (rs == 160)
+                    return launch_fused_tma<160>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
+                return launch_fused_tma<256>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
             }
         }
     }
@@ -1057,12 +1084,13 @@ uint32_t fused_tma_box(const Box& F, uint32_t nr) {
     return bw <= 160 ? bw : 0;
 }
 
-int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw) {
+int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw,
+                     uint32_t box_planes) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc || !bw || (uintptr_t)base % 16 != 0 || stride % 4 != 0) return PRODM_EUNSUPPORTED;
     const cuuint64_t dims[2] = {nblocks, (cuuint64_t)planes};
     const cuuint64_t strides[1] = {stride * 4};
-    const cuuint32_t box[2] = {bw, 1};
+    const cuuint32_t box[2] = {bw, box_planes};
     const cuuint32_t estr[2] = {1, 1};
     if (enc((CUtensorMap*)map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void*>(base), dims, strides, box, estr,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,

@@ -126,8 +126,10 @@ struct FusedSeg {
     uint64_t s0, s1;
     uint64_t unit_begin;
     const void* map;        // TMA form: the planes' tensor map (a CUtensorMap in device memory)
-    uint32_t bw;            // TMA form: its box width in words
+    uint32_t bw;            // TMA form: the unit's block range plus alignment, in words
     uint32_t rpu;           // TMA form: rows per unit (a multiple of 8, at most kMaxUnitRows)
+    uint32_t tall;          // TMA form: 1 = the map's box is the tile's row stride x 32 plane rows
+                            // (one copy per unit), 0 = bw words x 1 plane (one copy per plane)
 };
 constexpr uint32_t kMaxUnitRows = 64;
 // blocks of the plane tile of an 8-row unit of box F, and the launch's dynamic
@@ -144,7 +146,10 @@ int launch_decode_recompose_nb32_multi(const FusedSeg* segs, int nseg, uint64_t 
 uint32_t fused_unit_rows(const Box& F, uint32_t values);
 uint32_t fused_unit_blocks_rows(const Box& F, uint32_t nr);      // tile blocks of nr rows
 uint32_t fused_tma_box(const Box& F, uint32_t nr);
-int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw);
+int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw,
+                     uint32_t box_planes = 1);
+bool fused_tma_tall();                                            // PRODM_TMA_TALL (default 1)
+uint32_t fused_tma_stride(uint32_t bw);                           // tile row stride of the TMA kernels for box bw
 int launch_decode_recompose_nb32_tma_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
                                            uint32_t max_bw, unsigned ctas_per_sm, int* status, cudaStream_t st);
 

@@ -44,13 +44,15 @@ def test_batch_matches_single_field_path():
         assert float((outs[i] - x).abs().max()) <= tols[i]
 
 
-@pytest.mark.parametrize("values", [256, 1056, 4224, 8192])
-def test_batch_fused_unit_shapes_match_single_field_path(values):
+@pytest.mark.parametrize("values,tall", [(256, "1"), (1056, "1"), (4224, "1"), (8192, "1"), (1056, "0"), (4224, "0")])
+def test_batch_fused_unit_shapes_match_single_field_path(values, tall, monkeypatch):
     """Every tile shape the autotuner may pick (values per unit of the fused
     finest levels; at 8192 the units of 257-wide rows no longer fit a TMA box
     and take the cp.async kernel) gives the single-field path's
-    reconstructions bit for bit."""
+    reconstructions bit for bit, with the planes staged by one tall box per
+    unit or (PRODM_TMA_TALL=0) by one box per plane."""
     from prodm_gb300 import api, fields
+    monkeypatch.setenv("PRODM_TMA_TALL", tall)
     shapes = [(65, 65, 65), (129, 33), (33, 65, 17), (17, 513), (9, 9, 9), (33, 257)]
     xs = [fields.spectral_grf(s, slope=-2.0, seed=60 + i).contiguous() for i, s in enumerate(shapes)]
     levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
@@ -172,13 +174,15 @@ def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
             ref = [o.clone() for o in batch.outs]
 
 
-def test_batch_fused_tile_wait_timeout_is_reported_and_recoverable():
+@pytest.mark.parametrize("tall", ["1", "0"])
+def test_batch_fused_tile_wait_timeout_is_reported_and_recoverable(tall, monkeypatch):
     """The batched TMA fused kernel bounds its waits for plane tiles: with the
     expected byte count raised (the test hook) every wait runs out, the kernel
     reports PRODM_ETIMEOUT through prodm_batch_status (once) and the next
     retrieval equals the one before."""
     from prodm_gb300 import api, fields
     from prodm_gb300._lib import ProdmError
+    monkeypatch.setenv("PRODM_TMA_TALL", tall)
     shapes = [(65, 65, 65), (129, 129), (33, 65, 17)]
     xs = [fields.spectral_grf(s, seed=20 + i) for i, s in enumerate(shapes)]
     batch = api.MDRBatch(xs, None, 32)

@@ -255,16 +255,20 @@ FUSED_SHAPES = [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129,
                 ((129, 513), 3), ((65, 9, 513), 2), ((65, 17, 513), 2)]
 
 
-@pytest.mark.parametrize("shape,L", FUSED_SHAPES)
-def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
+@pytest.mark.parametrize("shape,L,B,tall", [(s, L, 32, "1") for s, L in FUSED_SHAPES] +
+                         [((65, 65, 65), 3, 32, "0"), ((33, 33, 513), 3, 32, "0"), ((129, 513), 3, 32, "0"),
+                          ((65, 65, 65), 3, 20, "1"), ((33, 33, 513), 3, 24, "1")])
+def test_fused_finest_level_retrieval_is_bit_exact(shape, L, B, tall, monkeypatch):
     """fp32 negabinary hierarchical: the finest level is decoded inside the
     recomposition kernel (odd and even row lengths take different kernels;
     odd rows of up to ~360 values the 8-warp TMA kernel, longer ones up to
     ~990 values the warp-specialised one with 160- and 256-word tile rows,
     longer still the cp.async kernel);
-    the other levels go through the multi-level decoder. The output equals the
-    oracle's decode -> reposition -> recompose in float bit for bit."""
-    B = 32
+    the other levels go through the multi-level decoder. The TMA kernels stage
+    a unit's planes by one box of all 32 plane rows (with PRODM_TMA_TALL=0 by
+    one box per plane). The output equals the oracle's decode -> reposition ->
+    recompose in float bit for bit, also for streams of fewer than 32 planes."""
+    monkeypatch.setenv("PRODM_TMA_TALL", tall)
     x = fields().spectral_grf(shape, seed=sum(shape)).cpu().numpy()
     mdr = api().MDRField(shape, torch.float32, L, B, "negabinary", "hierarchical", "max")
     mdr.refactor(torch.from_numpy(x).cuda())
@@ -273,7 +277,7 @@ def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
     rng = np.random.default_rng(len(shape) + L)
     cases = [np.zeros(L + 1, np.uint8), np.full(L + 1, B, np.uint8)]
     cases += [rng.integers(0, B + 1, L + 1).astype(np.uint8) for _ in range(4)]
-    cases += [np.full(L + 1, k, np.uint8) for k in (1, 2, 7, 16, 17, 31)]
+    cases += [np.full(L + 1, k, np.uint8) for k in (1, 2, 7, 16, 17, 31) if k <= B]
     for idx in cases:
         mdr.reset()
         out = mdr.retrieve_planes([int(v) for v in idx]).cpu().numpy()
@@ -281,8 +285,9 @@ def test_fused_finest_level_retrieval_is_bit_exact(shape, L):
         assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), idx
 
 
+@pytest.mark.parametrize("tall", ["1", "0"])
 @pytest.mark.parametrize("shape", [(65, 65, 65), (33, 33, 513)])
-def test_fused_tile_wait_timeout_is_reported_and_recoverable(shape):
+def test_fused_tile_wait_timeout_is_reported_and_recoverable(shape, tall, monkeypatch):
     """The fused finest-level kernels (the 8-warp form at 65^3, the
     warp-specialised form at 33 x 33 x 513) wait for their TMA plane tiles on
     mbarriers, each wait bounded. With the expected byte count raised (the test
@@ -290,6 +295,7 @@ def test_fused_tile_wait_timeout_is_reported_and_recoverable(shape):
     reports PRODM_ETIMEOUT and returns; the status is cleared once read and
     the next retrieval is exact again."""
     from prodm_gb300._lib import ProdmError
+    monkeypatch.setenv("PRODM_TMA_TALL", tall)
     L = 3
     x = fields().spectral_grf(shape, seed=11, device="cuda")
     m = api().MDRField(shape, torch.float32, L, 32, "negabinary", "hierarchical", "max")
