@@ -785,8 +785,9 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma_multi(cons
     }
 }
 
-// Warp-specialised form of the TMA kernel: 16 warps, warps 0..7 decode and
-// warps 8..15 recompose, with both the plane tile and the coefficient tile
+// Warp-specialised form of the TMA kernel: 16 warps, warps 0..ND-1 decode and
+// the other 16 - ND recompose (a unit is 16 - ND consecutive rows, one per
+// recomposition warp), with both the plane tile and the coefficient tile
 // double buffered, so the decode of unit it + 1 runs while unit it is
 // recomposed. The groups meet only on mbarriers: tile_full (the TMA bytes of
 // a unit's planes), coef_full (all decode threads arrived after writing a
@@ -800,7 +801,7 @@ __global__ void __launch_bounds__(256, 5) k_decode_recompose_nb32_tma_multi(cons
 // in flight land, bounded again, and returns); a recomposition warp that
 // gives up writes the status and returns, and the other group's waits then
 // run out too.
-template <int RS>
+template <int RS, int ND>
 __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     const __grid_constant__ CUtensorMap tmap, uint32_t bw, const uint32_t* __restrict__ maxkey,
     const uint8_t* __restrict__ dnum, const float* __restrict__ coarse, Box F, Box C, float* __restrict__ out,
@@ -812,9 +813,10 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     __shared__ __align__(8) uint64_t bar_tile[2], bar_full[2], bar_empty[2];
     __shared__ uint64_t s_fb[2];
     __shared__ uint32_t s_nbk[2];
-    __shared__ FusedRow s_row[2][8];
+    constexpr int NR = 16 - ND;                              // recomposition warps = rows per unit
+    __shared__ FusedRow s_row[2][NR];
     __shared__ volatile int s_abort;
-    constexpr int GROUP = 256;                               // threads per group
+    constexpr int GROUP = 32 * ND, RGROUP = 32 * NR;         // threads of the decode / recomposition group
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool dec = threadIdx.x < GROUP;
     const int num = dnum[0];
@@ -823,7 +825,7 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
     const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
     const uint32_t rows = F.n[0] * F.n[1];
-    const uint32_t nunits = (rows + 7) / 8;
+    const uint32_t nunits = (rows + NR - 1) / NR;
     const int poff = 32 - num;
     const uint32_t u0 = blockIdx.x, step = gridDim.x;
     if (u0 >= nunits) return;
@@ -838,8 +840,8 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
         mbar_init(&bar_tile[1], 1);
         mbar_init(&bar_full[0], GROUP);
         mbar_init(&bar_full[1], GROUP);
-        mbar_init(&bar_empty[0], GROUP);
-        mbar_init(&bar_empty[1], GROUP);
+        mbar_init(&bar_empty[0], RGROUP);
+        mbar_init(&bar_empty[1], RGROUP);
     }
     if (!tall)
         for (uint32_t i = threadIdx.x; i < (uint32_t)poff * RS; i += blockDim.x) {   // planes not retrieved
@@ -851,8 +853,8 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     // warp 0: block range of unit k of this CTA into slot b, then its planes into tile b
     auto issue = [&](int k, int b) {
         if (lane == 0) {
-            const uint32_t r0 = (u0 + (uint32_t)k * step) * 8;
-            fused_block_range(r0, rows, F, C, s_fb[b], s_nbk[b]);
+            const uint32_t r0 = (u0 + (uint32_t)k * step) * NR;
+            fused_block_range(r0, rows, F, C, s_fb[b], s_nbk[b], NR);
             mbar_arrive_expect_tx(&bar_tile[b], bytes);
         }
         __syncwarp();
@@ -881,8 +883,8 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
             if (!ok) s_abort = 1;   // read by the whole group after its next barrier
             const uint64_t fb = s_fb[b];
             const uint32_t nbk = s_nbk[b];
-            if (warp == 0 && lane < 8) {
-                const uint32_t r = (u0 + (uint32_t)it * step) * 8 + lane;
+            if (warp == 0 && lane < NR) {
+                const uint32_t r = (u0 + (uint32_t)it * step) * NR + lane;
                 if (r < rows) s_row[b][lane] = fused_row(r, F, C, s0, s1, fb);
                 else s_row[b][lane].m01 = -1;
             }
@@ -972,19 +974,33 @@ static int fused_ws() {
     return mode;
 }
 
-template <int RS>
+// rows per unit of the warp-specialised kernel with nd decode warps (one per recomposition warp)
+static uint32_t ws_unit_rows(int nd) { return 16u - (uint32_t)nd; }
+static uint32_t ws_tile_blocks(const Box& F, int nd) { return (ws_unit_rows(nd) * F.n[2] + 31) / 32 + 2; }
+// Decode warps of the warp-specialised kernel (the other 16 - nd warps
+// recompose, one unit row each). Measured at 513^3 (level 7, CUDA events):
+// 8 decode warps (8-row units) 263 us, 7: 245 us, 6: 237 us, 5: 237 us
+// (step 2.692 / 2.590 / 2.543 / 2.534 ms): the recomposition group was the
+// slower one. PRODM_WS_ND overrides: 5 (default), 6 or 8.
+static int ws_decode_warps() {
+    const char* v = getenv("PRODM_WS_ND");
+    const int n = v ? atoi(v) : 5;
+    return n == 6 ? 6 : (n == 8 ? 8 : 5);
+}
+
+template <int RS, int ND>
 static int launch_fused_ws(const CUtensorMap& map, uint32_t bw, const void* maxkey, const uint8_t* dnum,
                            const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
                            int* status, cudaStream_t st, bool pdl, int tall) {
-    const uint32_t tld = fused_max_blocks(F);
+    const uint32_t tld = ws_tile_blocks(F, ND), nr = ws_unit_rows(ND);
     const size_t smem = (size_t)2 * 32 * RS * 4 + (size_t)2 * tld * CB_LD * 4;
-    const void* kern = (const void*)k_decode_recompose_nb32_ws<RS>;
+    const void* kern = (const void*)k_decode_recompose_nb32_ws<RS, ND>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
-    const uint64_t need = ((uint64_t)F.n[0] * F.n[1] + 7) / 8;
+    const uint64_t need = ((uint64_t)F.n[0] * F.n[1] + nr - 1) / nr;
     const unsigned grid = persistent_grid_for(kern, 512, smem, need, need);
     count_launch();
-    e = launch_chain(pdl, k_decode_recompose_nb32_ws<RS>, dim3(grid), dim3(512), smem, st, map, bw,
+    e = launch_chain(pdl, k_decode_recompose_nb32_ws<RS, ND>, dim3(grid), dim3(512), smem, st, map, bw,
                      (const uint32_t*)maxkey, dnum, coarse, F, C, out, s0, s1, tld, status, g_tma_wait_cycles,
                      (uint32_t)g_tma_tx_extra, tall);
     if (e != cudaSuccess) return cuda_status(e, "k_decode_recompose_nb32_ws");
@@ -996,7 +1012,7 @@ static int launch_fused_tma(const CUtensorMap& map, uint32_t bw, const void* max
                             const float* coarse, const Box& F, const Box& C, float* out, uint64_t s0, uint64_t s1,
                             int* status, cudaStream_t st, bool pdl, int tall) {
     if (fused_ws() == 1 || (fused_ws() == 2 && RS >= 160))
-        return launch_fused_ws<RS>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
+        return launch_fused_ws<RS, 8>(map, bw, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
     const size_t smem = (size_t)32 * RS * 4 + (size_t)fused_max_blocks(F) * CB_LD * 4;
     const void* kern = (const void*)k_decode_recompose_nb32_tma<RS>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1032,6 +1048,23 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
     const bool odd = (F.n[2] & 1u) != 0;
     if (odd && status && (uintptr_t)base % 16 == 0 && stride % 4 == 0) {
         const uint32_t bw = (fused_max_blocks(F) + 3 + 3) & ~3u;   // block range + up to 3 words of alignment
+        const int nd = ws_decode_warps();
+        const uint32_t bwn = (ws_tile_blocks(F, nd) + 3 + 3) & ~3u;
+        // rows long enough for the warp-specialised form, tile rows of at most
+        // 192 words (two CTAs per SM); longer rows keep 8-row units
+        if (nd != 8 && fused_ws() == 2 && bw > 96 && bwn <= 192) {
+            const uint32_t rs = bwn <= 160 ? 160 : 192;
+            alignas(64) CUtensorMap map;
+            const int tall =
+                tma_tall() && planes <= 32 && encode_plane_map(&map, base, nblocks, planes, stride, rs, 32) == PRODM_OK;
+            if (tall || encode_plane_map(&map, base, nblocks, planes, stride, bwn, 1) == PRODM_OK) {
+#define PRODM_WS_CASE(R, N)                                                                                   \
+    if (rs == R && nd == N)                                                                                   \
+        return launch_fused_ws<R, N>(map, bwn, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
+                PRODM_WS_CASE(160, 5) PRODM_WS_CASE(192, 5) PRODM_WS_CASE(160, 6) PRODM_WS_CASE(192, 6)
+#undef PRODM_WS_CASE
+            }
+        }
         if (bw <= 256) {
             const uint32_t rs = fused_tma_stride(bw);
             // tall: one box of rs words x 32 plane rows per unit (planes above

@@ -255,20 +255,27 @@ FUSED_SHAPES = [((65, 65, 65), 3), ((48, 40, 64), 2), ((33, 40, 129), 3), ((129,
                 ((129, 513), 3), ((65, 9, 513), 2), ((65, 17, 513), 2)]
 
 
-@pytest.mark.parametrize("shape,L,B,tall", [(s, L, 32, "1") for s, L in FUSED_SHAPES] +
-                         [((65, 65, 65), 3, 32, "0"), ((33, 33, 513), 3, 32, "0"), ((129, 513), 3, 32, "0"),
-                          ((65, 65, 65), 3, 20, "1"), ((33, 33, 513), 3, 24, "1")])
-def test_fused_finest_level_retrieval_is_bit_exact(shape, L, B, tall, monkeypatch):
+@pytest.mark.parametrize("shape,L,B,tall,nd", [(s, L, 32, "1", "5") for s, L in FUSED_SHAPES] +
+                         [((65, 65, 65), 3, 32, "0", "5"), ((33, 33, 513), 3, 32, "0", "5"),
+                          ((129, 513), 3, 32, "0", "5"), ((65, 65, 65), 3, 20, "1", "5"),
+                          ((33, 33, 513), 3, 24, "1", "5"), ((33, 33, 513), 3, 32, "1", "8"),
+                          ((40, 33, 301), 3, 32, "1", "8"), ((40, 36, 411), 2, 32, "1", "6"),
+                          ((65, 17, 513), 2, 32, "0", "6")])
+def test_fused_finest_level_retrieval_is_bit_exact(shape, L, B, tall, nd, monkeypatch):
     """fp32 negabinary hierarchical: the finest level is decoded inside the
     recomposition kernel (odd and even row lengths take different kernels;
     odd rows of up to ~360 values the 8-warp TMA kernel, longer ones up to
-    ~990 values the warp-specialised one with 160- and 256-word tile rows,
+    ~990 values the warp-specialised one: units of 11 rows where their tile
+    rows fit 192 words, else of 8 rows with 160- and 256-word tile rows;
     longer still the cp.async kernel);
     the other levels go through the multi-level decoder. The TMA kernels stage
     a unit's planes by one box of all 32 plane rows (with PRODM_TMA_TALL=0 by
     one box per plane). The output equals the oracle's decode -> reposition ->
-    recompose in float bit for bit, also for streams of fewer than 32 planes."""
+    recompose in float bit for bit, also for streams of fewer than 32 planes
+    and for 5, 6 or 8 decode warps in the warp-specialised kernel
+    (PRODM_WS_ND)."""
     monkeypatch.setenv("PRODM_TMA_TALL", tall)
+    monkeypatch.setenv("PRODM_WS_ND", nd)
     x = fields().spectral_grf(shape, seed=sum(shape)).cpu().numpy()
     mdr = api().MDRField(shape, torch.float32, L, B, "negabinary", "hierarchical", "max")
     mdr.refactor(torch.from_numpy(x).cuda())
