@@ -961,10 +961,12 @@ void fused_tma_test_hook(int tx_extra, long long wait_cycles) {
 // The TMA kernel for odd rows whose 8-row block range fits one box (at most
 // 256 words): box width and tile row stride (a multiple of 32 words, so that
 // every tile row starts on a 128-byte boundary).
-// Which TMA kernel a fused level takes: the warp-specialised form where the
-// tile rows are 160 words or more (rows of about 360 values and up), the
-// 8-warp form below that (measured at 513^3, step 3.047 ms with the 8-warp
-// form everywhere, 3.008 ms warp-specialised everywhere, 2.966 ms mixed).
+// Which TMA kernel a fused level takes: the warp-specialised form, with
+// 16 - nd rows per unit for rows of 257 values and up while its tile rows fit
+// 192 words, and with 8-row units where the 8-row tile rows are 160 words or
+// more; the 8-warp form below that. With 8 decode warps (before the units
+// grew) the split measured at 513^3: step 3.047 ms with the 8-warp form
+// everywhere, 3.008 ms warp-specialised everywhere, 2.966 ms mixed.
 // PRODM_FUSED_WS overrides: 0 never, 1 always, 2 the default rule.
 static int fused_ws() {
     static const int mode = [] {
@@ -1050,10 +1052,12 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
         const uint32_t bw = (fused_max_blocks(F) + 3 + 3) & ~3u;   // block range + up to 3 words of alignment
         const int nd = ws_decode_warps();
         const uint32_t bwn = (ws_tile_blocks(F, nd) + 3 + 3) & ~3u;
-        // rows long enough for the warp-specialised form, tile rows of at most
-        // 192 words (two CTAs per SM); longer rows keep 8-row units
-        if (nd != 8 && fused_ws() == 2 && bw > 96 && bwn <= 192) {
-            const uint32_t rs = bwn <= 160 ? 160 : 192;
+        // rows of 257 values and up take the warp-specialised form with
+        // 16 - nd rows per unit where its tile rows fit 192 words (two CTAs
+        // per SM; level 6 at 513^3: 46.4 us against 48.9 us for the 8-warp
+        // kernel); longer rows keep 8-row units
+        if (nd != 8 && ((fused_ws() == 2 && F.n[2] >= 257) || fused_ws() == 1) && bwn <= 192) {
+            const uint32_t rs = bwn <= 96 ? 96 : (bwn <= 160 ? 160 : 192);
             alignas(64) CUtensorMap map;
             const int tall =
                 tma_tall() && planes <= 32 && encode_plane_map(&map, base, nblocks, planes, stride, rs, 32) == PRODM_OK;
@@ -1061,7 +1065,8 @@ int launch_decode_recompose_nb32(const void* base, uint64_t stride, int planes, 
 #define PRODM_WS_CASE(R, N)                                                                                   \
     if (rs == R && nd == N)                                                                                   \
         return launch_fused_ws<R, N>(map, bwn, maxkey, dnum, coarse, F, C, out, s0, s1, status, st, pdl, tall);
-                PRODM_WS_CASE(160, 5) PRODM_WS_CASE(192, 5) PRODM_WS_CASE(160, 6) PRODM_WS_CASE(192, 6)
+                PRODM_WS_CASE(96, 5) PRODM_WS_CASE(160, 5) PRODM_WS_CASE(192, 5)
+                PRODM_WS_CASE(96, 6) PRODM_WS_CASE(160, 6) PRODM_WS_CASE(192, 6)
 #undef PRODM_WS_CASE
             }
         }
