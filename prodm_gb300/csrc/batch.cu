@@ -20,6 +20,16 @@
 #include "rows.cuh"
 
 namespace prodm {
+// Fused finest levels with rows of 257 values and up whose 11-row units fit
+// a 96-word box take the warp-specialised batched kernel (64-field batch,
+// same launch shapes: 2.60 ms per step against 2.73 ms with the 8-warp
+// kernel). PRODM_BATCH_WS=0 keeps them on the 8-warp kernel; read when a
+// batch is planned.
+static bool batch_ws() {
+    const char* v = getenv("PRODM_BATCH_WS");
+    return !v || atoi(v) != 0;
+}
+
 namespace {
 
 constexpr int kMaxL = 17;
@@ -171,13 +181,15 @@ struct prodm_batch {
     uint64_t echunks = 0, dchunks = 0;
     // finest levels decoded inside their recomposition: fields whose plane
     // runs fit a TMA box of at most 96 words (fseg[0]) or 160 words (fseg[1])
-    // (tensor maps in fmaps, one per field), and fields with longer rows
-    // (fseg[2]: cp.async staging)
-    FusedSeg* fseg[3] = {nullptr, nullptr, nullptr};
-    int fn[3] = {0, 0, 0};
-    uint64_t funits[3] = {0, 0, 0};
-    uint32_t ftld[3] = {0, 0, 0};
-    uint32_t fbw[3] = {0, 0, 0};                   // widest TMA box of each class
+    // (tensor maps in fmaps, one per field), fields with longer rows
+    // (fseg[2]: cp.async staging), and fields with rows of 257 values and up
+    // whose 11-row units fit a 96-word tall box (fseg[3]: the
+    // warp-specialised batched kernel; before the other classes)
+    FusedSeg* fseg[4] = {nullptr, nullptr, nullptr, nullptr};
+    int fn[4] = {0, 0, 0, 0};
+    uint64_t funits[4] = {0, 0, 0, 0};
+    uint32_t ftld[4] = {0, 0, 0, 0};
+    uint32_t fbw[4] = {0, 0, 0, 0};                // widest TMA box of each class
     uint8_t* fmaps = nullptr;                      // [nf][128] tensor maps
     int* kstatus = nullptr;                        // status word of the fused kernels
     std::vector<char> fused;                       // per field
@@ -284,9 +296,9 @@ int batch_build_segments(prodm_batch* h) {
     }
     // fused finest levels
     {
-        std::vector<FusedSeg> fs[3];
-        uint64_t units[3] = {0, 0, 0};
-        uint32_t tld[3] = {0, 0, 0};
+        std::vector<FusedSeg> fs[4];
+        uint64_t units[4] = {0, 0, 0, 0};
+        uint32_t tld[4] = {0, 0, 0, 0};
         std::vector<uint8_t> maps((size_t)nf * 128, 0);
         if (!h->fmaps && (rc = h->alloc((void**)&h->fmaps, (size_t)nf * 128))) return rc;
         for (int f = 0; f < nf; f++) {
@@ -312,9 +324,20 @@ int batch_build_segments(prodm_batch* h) {
             s.bw = fused_tma_box(s.F, s.rpu);
             int k = 2;
             void* m = maps.data() + (size_t)f * 128;
-            s.tall = s.bw && fused_tma_tall() && B <= 32 &&
-                     encode_plane_map(m, s.base, nbk, B, s.stride, fused_tma_stride(s.bw), 32) == PRODM_OK;
-            if (s.tall || (s.bw && encode_plane_map(m, s.base, nbk, B, s.stride, s.bw) == PRODM_OK)) {
+            const uint32_t wr = fused_ws_unit_rows();
+            const uint32_t wbw = (fused_unit_blocks_rows(s.F, wr) + 3 + 3) & ~3u;
+            if (batch_ws() && s.F.n[2] >= 257 && B <= 32 && wbw <= kWsMultiStride &&
+                encode_plane_map(m, s.base, nbk, B, s.stride, kWsMultiStride, 32) == PRODM_OK) {
+                k = 3;
+                s.tall = 1;
+                s.bw = wbw;
+                s.rpu = wr;
+                s.map = h->fmaps + (size_t)f * 128;
+                t = fused_unit_blocks_rows(s.F, wr);
+            } else if ((s.tall = s.bw && fused_tma_tall() && B <= 32 &&
+                                 encode_plane_map(m, s.base, nbk, B, s.stride, fused_tma_stride(s.bw), 32) ==
+                                     PRODM_OK) ||
+                       (s.bw && encode_plane_map(m, s.base, nbk, B, s.stride, s.bw) == PRODM_OK)) {
                 k = s.bw <= 96 ? 0 : 1;
                 s.map = h->fmaps + (size_t)f * 128;
                 t = fused_unit_blocks_rows(s.F, s.rpu);
@@ -330,7 +353,7 @@ int batch_build_segments(prodm_batch* h) {
             h->fbw[k] = std::max(h->fbw[k], s.bw);
         }
         PRODM_CUDA(cudaMemcpy(h->fmaps, maps.data(), maps.size(), cudaMemcpyHostToDevice));
-        for (int k = 0; k < 3; k++) {
+        for (int k = 0; k < 4; k++) {
             h->fn[k] = (int)fs[k].size();
             h->funits[k] = units[k];
             h->ftld[k] = tld[k];
@@ -431,6 +454,9 @@ int batch_retrieve(prodm_batch* h, int interp, int est, double s, cudaStream_t s
                                                                     h->fbw[k], fc, h->kstatus, st)))
             return rc;
     if (h->fn[2] && (rc = launch_decode_recompose_nb32_multi(h->fseg[2], h->fn[2], h->funits[2], h->ftld[2], fc, st)))
+        return rc;
+    if (h->fn[3] && (rc = launch_decode_recompose_nb32_ws_multi(h->fseg[3], h->fn[3], h->funits[3], h->ftld[3],
+                                                                 h->kstatus, st)))
         return rc;
     return PRODM_OK;
 }

@@ -921,6 +921,129 @@ __global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws(
     }
 }
 
+// The warp-specialised kernel over the finest levels of many fields (the
+// batched retrieval): units of 16 - ND rows of one field, found in the
+// segment table as in k_decode_recompose_nb32_tma_multi; every field's
+// tensor map is a tall one (box of RS words x 32 plane rows), so the tiles
+// are never zeroed and the plane count may change from unit to unit. The
+// field of the unit in tile b is kept for the recomposition group in
+// s_rseg[b] (written with the unit's row geometry, before coef_full).
+// Decode, recomposition and the bounded waits are those of
+// k_decode_recompose_nb32_ws, so results are bit-identical.
+template <int RS, int ND>
+__global__ void __launch_bounds__(512, 2) k_decode_recompose_nb32_ws_multi(const FusedSeg* __restrict__ segs, int nseg,
+                                                                          uint64_t total, uint32_t tld,
+                                                                          int* __restrict__ status,
+                                                                          long long wait_limit, uint32_t tx_extra) {
+    extern __shared__ __align__(128) uint32_t ws_smem[];
+    uint32_t* tiles = ws_smem;                               // [2][32][RS] plane-major
+    float* cbs = (float*)(ws_smem + 2 * 32 * RS);            // [2][tld][CB_LD]
+    constexpr int NR = 16 - ND;
+    constexpr int GROUP = 32 * ND, RGROUP = 32 * NR;
+    __shared__ __align__(8) uint64_t bar_tile[2], bar_full[2], bar_empty[2];
+    __shared__ uint64_t s_fb[2];
+    __shared__ uint32_t s_nbk[2];
+    __shared__ int s_seg[2], s_rseg[2];
+    __shared__ FusedRow s_row[2][NR];
+    __shared__ volatile int s_abort;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool dec = threadIdx.x < GROUP;
+    const uint64_t u0 = blockIdx.x, step = gridDim.x;
+    if (u0 >= total) return;
+    const int myunits = (int)((total - u0 + step - 1) / step);
+    if ((smem_addr(tiles) & 127u) != 0) {   // TMA destinations need 128-byte alignment
+        if (threadIdx.x == 0) atomicExch(status, PRODM_ECUDA);
+        return;
+    }
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        mbar_init(&bar_tile[0], 1);
+        mbar_init(&bar_tile[1], 1);
+        mbar_init(&bar_full[0], GROUP);
+        mbar_init(&bar_full[1], GROUP);
+        mbar_init(&bar_empty[0], RGROUP);
+        mbar_init(&bar_empty[1], RGROUP);
+    }
+    __syncthreads();
+    // lane 0 of warp 0: field and block range of unit k of this CTA into slot b, its planes into tile b
+    auto issue = [&](int k, int b) {
+        if (lane == 0) {
+            const uint64_t g = u0 + (uint64_t)k * step;
+            const int sg = find_seg(segs, nseg, g, &FusedSeg::unit_begin);
+            const FusedSeg& q = segs[sg];
+            s_seg[b] = sg;
+            fused_block_range((uint32_t)(g - q.unit_begin) * NR, q.F.n[0] * q.F.n[1], q.F, q.C, s_fb[b], s_nbk[b], NR);
+            mbar_arrive_expect_tx(&bar_tile[b], 32u * RS * 4u + tx_extra);
+            // one box of all 32 tile rows; rows of planes below 0 arrive as zeros
+            tma_load_2d(tiles + b * 32 * RS, (const CUtensorMap*)q.map, (int)(s_fb[b] & ~3ull), (int)*q.dnum - 32,
+                        &bar_tile[b]);
+        }
+    };
+    if (warp == 0) {
+        issue(0, 0);
+        if (myunits > 1) issue(1, 1);
+    }
+    // the first tiles are on their way; the coarse boxes and the outputs belong
+    // to the previous launches (the plane counts and the planes are older)
+    pdl_wait();
+    pdl_release();
+    if (dec) {
+        for (int it = 0; it < myunits; it++) {
+            const int b = it & 1;
+            const uint32_t ph = (uint32_t)(it >> 1) & 1u;
+            bool ok = mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
+            ok = ok && mbar_wait_bounded(&bar_empty[b], ph ^ 1u, wait_limit);   // first use: the phase before is done
+            if (!ok) s_abort = 1;   // read by the whole group after its next barrier
+            const int sg = s_seg[b];
+            const FusedSeg& q = segs[sg];
+            const uint64_t fb = s_fb[b];
+            const uint32_t nbk = s_nbk[b];
+            if (warp == 0 && lane < NR) {
+                const uint64_t g = u0 + (uint64_t)it * step;
+                const uint32_t r = (uint32_t)(g - q.unit_begin) * NR + lane;
+                if (r < q.F.n[0] * q.F.n[1]) s_row[b][lane] = fused_row(r, q.F, q.C, q.s0, q.s1, fb);
+                else s_row[b][lane].m01 = -1;
+                if (lane == 0) s_rseg[b] = sg;
+            }
+            const int num = *q.dnum;
+            const int exp = frexp_exp(__uint_as_float(*q.key)) + 2;
+            const bool neg = num != 0 && (num & 1);          // NegaBinaryBPEncoder.hpp:153, :177
+            const bool dfast = (exp - num) >= -126 && (exp - num) <= 127;
+            const float dscale = dfast ? (neg ? -pow2f_(exp - num) : pow2f_(exp - num)) : 1.f;
+            const uint32_t* t0 = tiles + b * 32 * RS + (fb & 3u);
+            float* cb = cbs + (size_t)b * tld * CB_LD;
+            if (dfast) decode_tile_pm<true, RS>(t0, cb, nbk, num, exp, neg, dscale, threadIdx.x, GROUP);
+            else decode_tile_pm<false, RS>(t0, cb, nbk, num, exp, neg, dscale, threadIdx.x, GROUP);
+            mbar_arrive(&bar_full[b]);
+            group_sync(GROUP);   // tile b is decoded: it may take unit it + 2
+            if (s_abort) {   // a wait gave up: report, let the copies in flight land, leave
+                if (threadIdx.x == 0) atomicExch(status, PRODM_ETIMEOUT);
+                mbar_wait_bounded(&bar_tile[b], ph, wait_limit);
+                if (it + 1 < myunits) mbar_wait_bounded(&bar_tile[b ^ 1], ((uint32_t)(it + 1) >> 1) & 1u, wait_limit);
+                return;
+            }
+            if (warp == 0 && it + 2 < myunits) {
+                fence_proxy_async_smem();
+                issue(it + 2, b);
+            }
+        }
+    } else {
+        const int rw = warp - ND;
+        for (int it = 0; it < myunits; it++) {
+            const int b = it & 1;
+            const uint32_t ph = (uint32_t)(it >> 1) & 1u;
+            if (!mbar_wait_bounded(&bar_full[b], ph, wait_limit)) {
+                if (lane == 0) atomicExch(status, PRODM_ETIMEOUT);
+                return;
+            }
+            const FusedRow r = s_row[b][rw];
+            const FusedSeg& q = segs[s_rseg[b]];
+            if (r.m01 >= 0) recompose_fine_row<true>(r, q.C, q.coarse, q.out, cbs + (size_t)b * tld * CB_LD, lane);
+            mbar_arrive(&bar_empty[b]);
+        }
+    }
+}
+
 }  // namespace
 
 static uint32_t fused_max_blocks(const Box& F) { return (8 * F.n[2] + 31) / 32 + 2; }
@@ -1159,6 +1282,22 @@ int launch_decode_recompose_nb32_tma_multi(const FusedSeg* segs, int nseg, uint6
     if (max_bw <= 96) return launch_tma_multi<96>(segs, nseg, total_units, tld, ctas_per_sm, status, st);
     if (max_bw <= 160) return launch_tma_multi<160>(segs, nseg, total_units, tld, ctas_per_sm, status, st);
     return fail(PRODM_EUNSUPPORTED, "batched fused level: TMA box above 160 words");
+}
+uint32_t fused_ws_unit_rows() { return ws_unit_rows(5); }
+
+int launch_decode_recompose_nb32_ws_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
+                                          int* status, cudaStream_t st) {
+    if (!total_units) return PRODM_OK;
+    constexpr int RS = kWsMultiStride;
+    const size_t smem = (size_t)2 * 32 * RS * 4 + (size_t)2 * tld * CB_LD * 4;
+    const void* kern = (const void*)k_decode_recompose_nb32_ws_multi<RS, 5>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute");
+    const unsigned grid = persistent_grid_for(kern, 512, smem, total_units, total_units);
+    k_decode_recompose_nb32_ws_multi<RS, 5><<<grid, 512, smem, st>>>(segs, nseg, total_units, tld, status,
+                                                                    g_tma_wait_cycles, (uint32_t)g_tma_tx_extra);
+    PRODM_CHECK_LAUNCH("k_decode_recompose_nb32_ws_multi");
+    return PRODM_OK;
 }
 size_t fused_multi_smem(uint32_t tld) { return (size_t)tld * TB_LD * 4 + (size_t)tld * CB_LD * 4; }
 

@@ -149,6 +149,12 @@ uint32_t fused_tma_box(const Box& F, uint32_t nr);
 int encode_plane_map(void* map, const void* base, uint64_t nblocks, int planes, uint64_t stride, uint32_t bw,
                      uint32_t box_planes = 1);
 bool fused_tma_tall();                                            // PRODM_TMA_TALL (default 1)
+// the warp-specialised batched kernel: units of fused_ws_unit_rows() rows,
+// tall maps with boxes of kWsMultiStride words x 32 plane rows
+constexpr uint32_t kWsMultiStride = 96;
+uint32_t fused_ws_unit_rows();
+int launch_decode_recompose_nb32_ws_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
+                                          int* status, cudaStream_t st);
 uint32_t fused_tma_stride(uint32_t bw);                           // tile row stride of the TMA kernels for box bw
 int launch_decode_recompose_nb32_tma_multi(const FusedSeg* segs, int nseg, uint64_t total_units, uint32_t tld,
                                            uint32_t max_bw, unsigned ctas_per_sm, int* status, cudaStream_t st);

@@ -72,6 +72,32 @@ def test_batch_fused_unit_shapes_match_single_field_path(values, tall, monkeypat
         assert torch.equal(out1, outs[i]), (values, i)
 
 
+@pytest.mark.parametrize("ws", ["1", "0"])
+def test_batch_warp_specialised_fused_levels_match_single_field_path(ws, monkeypatch):
+    """Fused finest levels with rows of 257 values (the warp-specialised
+    batched kernel by default, 11-row units, plane counts changing from field
+    to field; PRODM_BATCH_WS=0 the 8-warp one) give the single-field path's
+    reconstructions bit for bit, next to fields of the other fused classes."""
+    from prodm_gb300 import api, fields
+    monkeypatch.setenv("PRODM_BATCH_WS", ws)
+    shapes = [(33, 33, 257), (17, 65, 257), (65, 65, 65), (9, 9, 9), (40, 33, 257)]
+    xs = [fields.spectral_grf(s, slope=-2.0, seed=80 + i).contiguous() for i, s in enumerate(shapes)]
+    levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
+    batch = api.MDRBatch(xs, levels, 32)
+    tols = [float(x.max() - x.min()) * 10.0 ** (-1 - i % 5) for i, x in enumerate(xs)]
+    batch.set_tolerances(tols)
+    batch.refactor()
+    batch.reset()
+    outs = batch.retrieve("negabinary", "max_hb")
+    torch.cuda.synchronize()
+    batch.status()
+    for i, (s, x) in enumerate(zip(shapes, xs)):
+        one = api.MDRField(s, torch.float32, levels[i], 32, "negabinary", "hierarchical", "max")
+        one.refactor(x)
+        out1 = one.retrieve(tols[i], interpreter="negabinary", estimator="max_hb")
+        assert torch.equal(out1, outs[i]), (ws, i)
+
+
 def test_batch_patch_items_match_single_field_path(monkeypatch):
     """The batched decomposition and recomposition with patch work items on
     every 2^k + 1 level (PRODM_PATCH_MIN_ITEMS=1) give the single-field row
@@ -174,8 +200,8 @@ def test_batch_graph_capture_and_autotune(tmp_path, monkeypatch):
             ref = [o.clone() for o in batch.outs]
 
 
-@pytest.mark.parametrize("tall", ["1", "0"])
-def test_batch_fused_tile_wait_timeout_is_reported_and_recoverable(tall, monkeypatch):
+@pytest.mark.parametrize("tall,ws", [("1", "0"), ("0", "0"), ("1", "1")])
+def test_batch_fused_tile_wait_timeout_is_reported_and_recoverable(tall, ws, monkeypatch):
     """The batched TMA fused kernel bounds its waits for plane tiles: with the
     expected byte count raised (the test hook) every wait runs out, the kernel
     reports PRODM_ETIMEOUT through prodm_batch_status (once) and the next
@@ -183,7 +209,8 @@ def test_batch_fused_tile_wait_timeout_is_reported_and_recoverable(tall, monkeyp
     from prodm_gb300 import api, fields
     from prodm_gb300._lib import ProdmError
     monkeypatch.setenv("PRODM_TMA_TALL", tall)
-    shapes = [(65, 65, 65), (129, 129), (33, 65, 17)]
+    monkeypatch.setenv("PRODM_BATCH_WS", ws)
+    shapes = [(65, 65, 65), (129, 129), (33, 65, 17), (33, 33, 257)]
     xs = [fields.spectral_grf(s, seed=20 + i) for i, s in enumerate(shapes)]
     batch = api.MDRBatch(xs, None, 32)
     batch.set_tolerances([float(x.max() - x.min()) * 1e-3 for x in xs])
