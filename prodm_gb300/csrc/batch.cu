@@ -29,6 +29,13 @@ static bool batch_ws() {
     const char* v = getenv("PRODM_BATCH_WS");
     return !v || atoi(v) != 0;
 }
+// shortest row (values) that takes the warp-specialised batched kernel;
+// PRODM_BATCH_WS_MIN_ROW overrides 257 (64-field batch: 2.610 ms at 257,
+// 2.620 ms at 129, 2.782 ms at 65, where units of 11 short rows are small)
+static uint32_t batch_ws_min_row() {
+    const char* v = getenv("PRODM_BATCH_WS_MIN_ROW");
+    return v ? (uint32_t)atoi(v) : 257u;
+}
 
 namespace {
 
@@ -326,7 +333,7 @@ int batch_build_segments(prodm_batch* h) {
             void* m = maps.data() + (size_t)f * 128;
             const uint32_t wr = fused_ws_unit_rows();
             const uint32_t wbw = (fused_unit_blocks_rows(s.F, wr) + 3 + 3) & ~3u;
-            if (batch_ws() && s.F.n[2] >= 257 && B <= 32 && wbw <= kWsMultiStride &&
+            if (batch_ws() && s.F.n[2] >= batch_ws_min_row() && B <= 32 && wbw <= kWsMultiStride &&
                 encode_plane_map(m, s.base, nbk, B, s.stride, kWsMultiStride, 32) == PRODM_OK) {
                 k = 3;
                 s.tall = 1;

@@ -72,14 +72,15 @@ def test_batch_fused_unit_shapes_match_single_field_path(values, tall, monkeypat
         assert torch.equal(out1, outs[i]), (values, i)
 
 
-@pytest.mark.parametrize("ws", ["1", "0"])
-def test_batch_warp_specialised_fused_levels_match_single_field_path(ws, monkeypatch):
+@pytest.mark.parametrize("ws,min_row", [("1", "257"), ("0", "257"), ("1", "65")])
+def test_batch_warp_specialised_fused_levels_match_single_field_path(ws, min_row, monkeypatch):
     """Fused finest levels with rows of 257 values (the warp-specialised
     batched kernel by default, 11-row units, plane counts changing from field
     to field; PRODM_BATCH_WS=0 the 8-warp one) give the single-field path's
     reconstructions bit for bit, next to fields of the other fused classes."""
     from prodm_gb300 import api, fields
     monkeypatch.setenv("PRODM_BATCH_WS", ws)
+    monkeypatch.setenv("PRODM_BATCH_WS_MIN_ROW", min_row)   # 65: the 65^3 field too
     shapes = [(33, 33, 257), (17, 65, 257), (65, 65, 65), (9, 9, 9), (40, 33, 257)]
     xs = [fields.spectral_grf(s, slope=-2.0, seed=80 + i).contiguous() for i, s in enumerate(shapes)]
     levels = [fields.batch_level(s, api.max_level(s)) for s in shapes]
